@@ -1,0 +1,228 @@
+"""Python host mirror of the BSAM 1.2 multigrid interface over libbsamg.so.
+
+The methods follow the reference routines they stand for (see the citations
+in include/bsamg.h): a Hierarchy is the set of nodes the Fortran host visits
+with ApplyOnLevel, and multigrid_iterations / time_step are
+MultigridIterations and one TakeTimeSteps step.  All work runs in the CUDA
+library; there is no CPU path here, and a missing library is an error.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbsamg.so")
+
+FIELD = {"q": 0, "qold": 1, "qc": 2, "f": 3, "rf": 4, "ftmp": 5}
+PROBLEM = {"ch": 1, "biogrowth": 2}
+MODE = {"fp64": 0, "mixed": 1}
+
+_lib = None
+
+
+class BsamgError(RuntimeError):
+    def __init__(self, status, what):
+        L = lib()
+        msg = L.bsamg_strerror(status).decode()
+        detail = L.bsamg_last_error_detail().decode()
+        super().__init__(f"{what}: {msg} ({status}){': ' + detail if detail else ''}")
+        self.status = status
+
+
+def lib():
+    """Load libbsamg.so (built by __graft_entry__.build()); fail loudly if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libbsamg.so is not built ({LIB_PATH}); run __graft_entry__.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    I, D, P, SZ = ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_size_t
+    IP, DP = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+    sig = {
+        "bsamg_init": ([I, SZ, ctypes.POINTER(P)], I),
+        "bsamg_finalize": ([P], I),
+        "bsamg_ctx_usage": ([P, ctypes.POINTER(SZ), ctypes.POINTER(SZ)], I),
+        "bsamg_hier_create": ([P, I, I, I, I, DP, I, DP, ctypes.POINTER(P)], I),
+        "bsamg_hier_destroy": ([P], I),
+        "bsamg_patch_add": ([P, I, I, I, IP, IP, IP, IP, DP, DP], I),
+        "bsamg_build_uniform": ([P, IP, I, IP, DP, DP], I),
+        "bsamg_commit": ([P], I),
+        "bsamg_num_patches": ([P, IP], I),
+        "bsamg_field_size": ([P, I, I], SZ),
+        "bsamg_put_field": ([P, I, I, DP, SZ], I),
+        "bsamg_get_field": ([P, I, I, DP, SZ], I),
+        "bsamg_relax_level_color": ([P, I, I], I),
+        "bsamg_set_ghost": ([P, I, I], I),
+        "bsamg_level_relax": ([P, I, I], I),
+        "bsamg_fill_down": ([P, I, I, I], I),
+        "bsamg_copy_q_to_qold": ([P, I, I], I),
+        "bsamg_vcycle": ([P, I, I, I], I),
+        "bsamg_residual_norm": ([P, I, I, DP], I),
+        "bsamg_multigrid_iterations": ([P, I, I, I, I, D, I, I, I, I, IP, DP], I),
+        "bsamg_time_step": ([P, I, I, I, I, I, D, I, I, I, I, IP, DP], I),
+        "bsamg_sync": ([P], I),
+        "bsamg_stream": ([P, ctypes.POINTER(P)], I),
+        "bsamg_launch_count": ([P, ctypes.POINTER(ctypes.c_longlong)], I),
+        "bsamg_strerror": ([I], ctypes.c_char_p),
+        "bsamg_last_error_detail": ([], ctypes.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def exported_symbols():
+    """Names of the C-ABI entry points the Python mirror binds."""
+    lib()
+    return [n for n in dir(_lib) if n.startswith("bsamg_")]
+
+
+def _ck(rc, what):
+    if rc != 0:
+        raise BsamgError(rc, what)
+
+
+def _ia(x, n):
+    return (ctypes.c_int * n)(*[int(v) for v in x])
+
+
+def _da(x, n):
+    return (ctypes.c_double * n)(*[float(v) for v in x])
+
+
+class Context:
+    """One GPU and an HBM budget (bytes, 0 = unlimited)."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        h = ctypes.c_void_p()
+        _ck(lib().bsamg_init(device, hbm_budget, ctypes.byref(h)), "bsamg_init")
+        self.h = h
+
+    def usage(self):
+        u, b = ctypes.c_size_t(), ctypes.c_size_t()
+        _ck(lib().bsamg_ctx_usage(self.h, ctypes.byref(u), ctypes.byref(b)), "bsamg_ctx_usage")
+        return u.value, b.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().bsamg_finalize(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Hierarchy:
+    """A device-resident patch hierarchy (nodes of one mesh)."""
+
+    def __init__(self, ctx, ndims, nrvars, problem, params, qpo=None, mbc=1):
+        self.ctx = ctx
+        self.ndims, self.nrvars = ndims, nrvars
+        h = ctypes.c_void_p()
+        p = _da(params, len(params))
+        q = _da(qpo if qpo is not None else [0.0] * nrvars, nrvars)
+        _ck(lib().bsamg_hier_create(ctx.h, ndims, nrvars, mbc, PROBLEM[problem], p, len(params), q,
+                                    ctypes.byref(h)), "bsamg_hier_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().bsamg_hier_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def add_patch(self, level, id, parent_id, mx, mglobal, mbounds, mthbc, dx, xlower):
+        _ck(lib().bsamg_patch_add(self.h, level, id, parent_id, _ia(mx, 3), _ia(mglobal, 6),
+                                  _ia(mbounds, 6), _ia(mthbc, 6), _da(dx, 3), _da(xlower, 3)),
+            "bsamg_patch_add")
+
+    def build_uniform(self, mx, minlevel, mthbc, xlower, xupper):
+        _ck(lib().bsamg_build_uniform(self.h, _ia(mx, 3), minlevel, _ia(mthbc, 6), _da(xlower, 3),
+                                      _da(xupper, 3)), "bsamg_build_uniform")
+
+    def commit(self):
+        _ck(lib().bsamg_commit(self.h), "bsamg_commit")
+
+    def field_size(self, pid, field):
+        return lib().bsamg_field_size(self.h, pid, FIELD[field])
+
+    def put(self, pid, field, arr):
+        a = np.ascontiguousarray(np.asarray(arr, dtype=np.float64).ravel(order="F"))
+        _ck(lib().bsamg_put_field(self.h, pid, FIELD[field],
+                                  a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), a.size),
+            "bsamg_put_field")
+
+    def put_flat(self, pid, field, flat):
+        """put from an already Fortran-ordered contiguous float64 buffer (no copy)"""
+        _ck(lib().bsamg_put_field(self.h, pid, FIELD[field],
+                                  flat.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), flat.size),
+            "bsamg_put_field")
+
+    def get(self, pid, field, out=None):
+        n = self.field_size(pid, field)
+        a = out if out is not None else np.empty(n, dtype=np.float64)
+        _ck(lib().bsamg_get_field(self.h, pid, FIELD[field],
+                                  a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n),
+            "bsamg_get_field")
+        return a
+
+    def relax_level_color(self, level, ipass):
+        _ck(lib().bsamg_relax_level_color(self.h, level, ipass), "bsamg_relax_level_color")
+
+    def set_ghost(self, level, ipass):
+        _ck(lib().bsamg_set_ghost(self.h, level, ipass), "bsamg_set_ghost")
+
+    def level_relax(self, level, nsmooth):
+        _ck(lib().bsamg_level_relax(self.h, level, nsmooth), "bsamg_level_relax")
+
+    def fill_down(self, field, finest, minlevel):
+        _ck(lib().bsamg_fill_down(self.h, {"f": 1, "q": 2}[field], finest, minlevel), "bsamg_fill_down")
+
+    def copy_q_to_qold(self, minlevel, finest):
+        _ck(lib().bsamg_copy_q_to_qold(self.h, minlevel, finest), "bsamg_copy_q_to_qold")
+
+    def vcycle(self, level, minlevel, nsmooth):
+        _ck(lib().bsamg_vcycle(self.h, level, minlevel, nsmooth), "bsamg_vcycle")
+
+    def residual_norm(self, level, errortype=1):
+        r = ctypes.c_double()
+        _ck(lib().bsamg_residual_norm(self.h, level, errortype, ctypes.byref(r)), "bsamg_residual_norm")
+        return r.value
+
+    def multigrid_iterations(self, finest, minlevel, nsmooth=2, maxvcycles=20, tol=1e-9,
+                             updateauxfreq=1, errortype=1, mode="fp64", strict=False):
+        n = ctypes.c_int()
+        res = (ctypes.c_double * maxvcycles)()
+        _ck(lib().bsamg_multigrid_iterations(self.h, finest, minlevel, nsmooth, maxvcycles, tol,
+                                             updateauxfreq, errortype, MODE[mode], int(strict),
+                                             ctypes.byref(n), res), "bsamg_multigrid_iterations")
+        return n.value, list(res)[: n.value]
+
+    def time_step(self, first, finest, minlevel, nsmooth=2, maxvcycles=20, tol=1e-9,
+                  updateauxfreq=1, errortype=1, mode="fp64", strict=False):
+        n = ctypes.c_int()
+        res = (ctypes.c_double * maxvcycles)()
+        _ck(lib().bsamg_time_step(self.h, int(bool(first)), finest, minlevel, nsmooth, maxvcycles,
+                                  tol, updateauxfreq, errortype, MODE[mode], int(strict),
+                                  ctypes.byref(n), res), "bsamg_time_step")
+        return n.value, list(res)[: n.value]
+
+    def sync(self):
+        _ck(lib().bsamg_sync(self.h), "bsamg_sync")
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        _ck(lib().bsamg_stream(self.h, ctypes.byref(s)), "bsamg_stream")
+        return s.value
+
+    def launch_count(self):
+        n = ctypes.c_longlong()
+        _ck(lib().bsamg_launch_count(self.h, ctypes.byref(n)), "bsamg_launch_count")
+        return n.value

@@ -1,0 +1,632 @@
+// Plain FP64 kernels: the drop-in path.
+//
+// This translation unit is compiled with --fmad=false: every product and sum
+// is rounded separately, in the evaluation order of the reference Fortran, so
+// results agree bit for bit with a reference build that does not contract
+// multiply-adds (the CPU oracle is built that way).  Division is the IEEE
+// round-to-nearest `/`.
+//
+// On GB300 these kernels are bounded by the FP64 pipe, not by HBM: the CH
+// smoother needs ~22 FP64 operations and 2 divisions per cell update against
+// 32 bytes of algorithmic traffic, and the part issues FP64 at ~1.2 TFLOP/s.
+#include <cuda_runtime.h>
+
+#include "internal.h"
+#include "launch.h"
+
+namespace bsamg {
+
+// C/F interpolation weights, LIBRARY/boundary.f90:54-63
+__constant__ double kA1 = -01.0 / 05.0;
+__constant__ double kA2 = 02.0 / 03.0;
+__constant__ double kA3 = 08.0 / 15.0;
+__constant__ double kB1 = 05.0 / 32.0;
+__constant__ double kB2 = 15.0 / 16.0;
+__constant__ double kB3 = -03.0 / 32.0;
+__constant__ double kC1 = 09.0 / 16.0;
+__constant__ double kC2 = 03.0 / 16.0;
+__constant__ double kC3 = 03.0 / 16.0;
+__constant__ double kC4 = 01.0 / 16.0;
+
+__device__ __forceinline__ double cube(double c) { return c * c * c; }  // CH/problem.f90:918
+__device__ __forceinline__ double sqr(double c) { return c * c; }       // CH/problem.f90:931
+
+// offset of Fortran cell (i,j,k) (lower bound 0) in a ghosted plane
+template <int DIM>
+__device__ __forceinline__ long long gofs(const int* n, int i, int j, int k) {
+  if (DIM == 2) return (long long)j * n[0] + i;
+  return ((long long)k * n[1] + j) * n[0] + i;
+}
+// offset of Fortran cell (i,j,k) (lower bound 1) in an interior plane
+template <int DIM>
+__device__ __forceinline__ long long iofs(const int* mx, int i, int j, int k) {
+  if (DIM == 2) return (long long)(j - 1) * mx[0] + (i - 1);
+  return ((long long)(k - 1) * mx[1] + (j - 1)) * mx[0] + (i - 1);
+}
+
+// ULap2D / ULap3D, LIBRARY/gridutilities.f90:50-72, :372-399
+template <int DIM>
+__device__ __forceinline__ double ulap(const double* a, long long c, long long sy, long long sz) {
+  if (DIM == 2) return a[c + 1] + a[c - 1] + a[c + sy] + a[c - sy] - 4.0 * a[c];
+  return a[c + 1] + a[c - 1] + a[c + sy] + a[c - sy] + a[c + sz] + a[c - sz] - 6.0 * a[c];
+}
+
+// Operator2D/3D of the plugin at ghosted offset c of array a (planes of ps
+// elements), with qold value o0 (variable 1 at the same cell) and patch
+// coefficients cf.  CH: CH/problem.f90:393-422, :638-669; BioGrowth:
+// BioGrowth/problem.f90:320-353 (3D: zero stub, :497-522).
+template <int PROB, int DIM>
+__device__ __forceinline__ void op_eval(const double* a, long long c, long long sy, long long sz,
+                                        long long ps, double o0, const double* cf,
+                                        const ProbParams& pp, double& r0, double& r1) {
+  const double* a0 = a;
+  const double* a1 = a + ps;
+  if (PROB == kCH) {
+    r0 = a0[c] - cf[0] * ulap<DIM>(a1, c, sy, sz);
+    r1 = a1[c] - cube(a0[c]) + cf[1] * ulap<DIM>(a0, c, sy, sz);
+  } else {
+    if (DIM == 2) {
+      double dt = pp.dt;
+      r0 = a0[c] - cf[0] * ulap<DIM>(a0, c, sy, sz) + dt * cube(a0[c]) -
+           dt * (pp.gamma * 0.5 * (o0 + 1.0)) * (a1[c] - pp.czero);
+      r1 = -cf[1] * ulap<DIM>(a1, c, sy, sz) + (pp.lambda * 0.5 * (o0 + 1.0)) * a1[c];
+    } else {
+      r0 = 0.0;
+      r1 = 0.0;
+    }
+  }
+}
+
+// Source2D/3D + SourceUpdate2D/3D values (CH/problem.f90:425-476, :672-721;
+// BioGrowth/problem.f90:356-405, :525-575)
+template <int PROB, int DIM>
+__device__ __forceinline__ void source_eval(double o0, const ProbParams& pp, double& s0, double& s1) {
+  if (PROB == kCH) {
+    s0 = o0;
+    s1 = -o0;
+  } else if (DIM == 2) {
+    s0 = (1.0 + pp.dt) * o0;
+    s1 = 0.0;
+  } else {
+    s0 = 0.0;
+    s1 = 0.0;
+  }
+}
+
+// map a unit of a colour work list to an interior cell; false if the slot is
+// past the end of its row (odd mx) or past the patch.  The colour test is the
+// reference loop start i = 1 + MODULO(j(+k)+ipass, 2) (CH/problem.f90:350,
+// :591).
+template <int DIM>
+__device__ __forceinline__ bool color_cell(const PatchDev& p, int t, int ipass, int& i, int& j, int& k) {
+  int hx = (p.mx[0] + 1) >> 1;
+  int row = t / hx;
+  int s = t - row * hx;
+  if (DIM == 2) {
+    j = row + 1;
+    k = 1;
+    if (j > p.mx[1]) return false;
+    i = 1 + ((j + ipass) & 1) + 2 * s;
+  } else {
+    j = row % p.mx[1] + 1;
+    k = row / p.mx[1] + 1;
+    if (k > p.mx[2]) return false;
+    i = 1 + ((k + j + ipass) & 1) + 2 * s;
+  }
+  return i <= p.mx[0];
+}
+
+template <int DIM>
+__device__ __forceinline__ bool interior_cell(const int* mx, int t, int& i, int& j, int& k) {
+  i = t % mx[0] + 1;
+  int r = t / mx[0];
+  if (DIM == 2) {
+    j = r + 1;
+    k = 1;
+    return j <= mx[1];
+  }
+  j = r % mx[1] + 1;
+  k = r / mx[1] + 1;
+  return k <= mx[2];
+}
+
+template <int DIM>
+__device__ __forceinline__ bool ghosted_cell(const int* n, int t, int& i, int& j, int& k) {
+  i = t % n[0];
+  int r = t / n[0];
+  if (DIM == 2) {
+    j = r;
+    k = 0;
+    return j < n[1];
+  }
+  j = r % n[1];
+  k = r / n[1];
+  return k < n[2];
+}
+
+// ---------------------------------------------------------------------------
+// Red-black pointwise relaxation of one colour over all patches of a level.
+
+template <int PROB, int DIM>
+__global__ void __launch_bounds__(kBlock) k_relax(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                  const Blk* __restrict__ blk, int ipass, ProbParams pp) {
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  if (!color_cell<DIM>(p, b.start + threadIdx.x, ipass, i, j, k)) return;
+  double* q0 = pool + p.oq;
+  double* q1 = q0 + p.sq;
+  const double* f0 = pool + p.of;
+  const double* f1 = f0 + p.sf;
+  long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
+  long long c = gofs<DIM>(p.qn, i, j, k);
+  long long fc = iofs<DIM>(p.mx, i, j, k);
+  if (PROB == kCH) {
+    // RelaxGrid2D CH/problem.f90:349-367, RelaxGrid3D :589-612
+    double phi = q0[c];
+    double a21 = -3.0 * sqr(phi) - p.c[2];
+    double b1, b2;
+    if (DIM == 2) {
+      b1 = f0[fc] + p.c[0] * (q1[c - 1] + q1[c + 1] + q1[c - sy] + q1[c + sy]);
+      b2 = f1[fc] - p.c[1] * (q0[c + 1] + q0[c - 1] + q0[c + sy] + q0[c - sy]) - 2.0 * cube(phi);
+    } else {
+      b1 = f0[fc] + p.c[0] * (q1[c - 1] + q1[c + 1] + q1[c - sy] + q1[c + sy] + q1[c - sz] + q1[c + sz]);
+      b2 = f1[fc] - p.c[1] * (q0[c + 1] + q0[c - 1] + q0[c + sy] + q0[c - sy] + q0[c + sz] + q0[c - sz]) -
+           2.0 * cube(phi);
+    }
+    double det = 1.0 - p.c[3] * a21;
+    q0[c] = (b1 - p.c[3] * b2) / det;
+    q1[c] = (b2 - a21 * b1) / det;
+  } else {
+    if (DIM == 2) {
+      // RelaxGrid2D BioGrowth/problem.f90:280-294
+      const double* o0 = pool + p.oqold;
+      double dt = pp.dt;
+      double phi = q0[c];
+      double ol = o0[c];
+      double tmp2 = p.c[2] + dt * sqr(phi);
+      q0[c] = (f0[fc] + dt * (pp.gamma * 0.5 * (ol + 1.0)) * (q1[c] - pp.czero) +
+               p.c[0] * (q0[c - 1] + q0[c + 1] + q0[c - sy] + q0[c + sy])) / tmp2;
+      double tmp4 = p.c[3] + (pp.lambda * 0.5 * (ol + 1.0));
+      q1[c] = (f1[fc] + p.c[1] * (q1[c + 1] + q1[c - 1] + q1[c + sy] + q1[c - sy])) / tmp4;
+    } else {
+      // RelaxGrid3D BioGrowth/problem.f90:467-476 (zero stub)
+      q0[c] = 0.0;
+      q1[c] = 0.0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Restriction2D/3D (gridutilities.f90:103-126, :437-466) of plane `a`
+// (accessed through `at`) at coarse cell (ci,cj,ck).
+
+template <int DIM, typename F>
+__device__ __forceinline__ double restrict_at(F at, int ci, int cj, int ck) {
+  int i = 2 * ci, j = 2 * cj;
+  if (DIM == 2) return 0.25 * (at(i, j, 1) + at(i - 1, j, 1) + at(i, j - 1, 1) + at(i - 1, j - 1, 1));
+  int k = 2 * ck;
+  return 0.125 * (at(i, j, k) + at(i - 1, j, k) + at(i, j - 1, k) + at(i - 1, j - 1, k) + at(i, j, k - 1) +
+                  at(i - 1, j, k - 1) + at(i, j - 1, k - 1) + at(i - 1, j - 1, k - 1));
+}
+
+// RestrictSolution, afasroutines.f90:610-652: qc(1:cmx) = R(q);
+// parent q(mb) = qc.
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_restrict_q(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                       const Blk* __restrict__ blk, int nrvars) {
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int ci, cj, ck;
+  if (!interior_cell<DIM>(p.cmx, b.start + threadIdx.x, ci, cj, ck)) return;
+  const PatchDev& par = P[p.parent];
+  for (int v = 0; v < nrvars; v++) {
+    const double* q = pool + p.oq + v * p.sq;
+    auto at = [&](int i, int j, int k) { return q[gofs<DIM>(p.qn, i, j, k)]; };
+    double val = restrict_at<DIM>(at, ci, cj, ck);
+    pool[p.oqc + v * p.sc + gofs<DIM>(p.cn, ci, cj, ck)] = val;
+    pool[par.oq + v * par.sq + gofs<DIM>(par.qn, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 0)] = val;
+  }
+}
+
+// GetCoarseGhostPoints, boundary.f90:957-1015.  Every ring cell of qc is
+// covered by exactly one of its face statements, each of which copies
+// parent%q(mb-1+i, mb-1+j, mb-1+k).
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_coarse_ghost(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                         const Blk* __restrict__ blk, int nrvars) {
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  if (!ghosted_cell<DIM>(p.cn, b.start + threadIdx.x, i, j, k)) return;
+  bool ring = i == 0 || i == p.cmx[0] + 1 || j == 0 || j == p.cmx[1] + 1 ||
+              (DIM == 3 && (k == 0 || k == p.cmx[2] + 1));
+  if (!ring) return;
+  const PatchDev& par = P[p.parent];
+  long long src = gofs<DIM>(par.qn, p.mb[0] - 1 + i, p.mb[1] - 1 + j, DIM == 3 ? p.mb[2] - 1 + k : 0);
+  long long dst = gofs<DIM>(p.cn, i, j, k);
+  for (int v = 0; v < nrvars; v++) pool[p.oqc + v * p.sc + dst] = pool[par.oq + v * par.sq + src];
+}
+
+// CoarseLoadingFunction, afasroutines.f90:673-736, with Residual (:817-857):
+// rf = f - Op_h(q) on the children of a coarse cell;
+// parent f(mb) = R(rf) + Op_2h(qc, parent qold, h_parent).
+template <int PROB, int DIM>
+__global__ void __launch_bounds__(kBlock) k_coarse_load(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                        const Blk* __restrict__ blk, ProbParams pp) {
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int ci, cj, ck;
+  if (!interior_cell<DIM>(p.cmx, b.start + threadIdx.x, ci, cj, ck)) return;
+  const PatchDev& par = P[p.parent];
+  const double* q = pool + p.oq;
+  const double* qo = pool + p.oqold;
+  long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
+  double* rf0 = pool + p.orf;
+  double* rf1 = rf0 + p.sf;
+  const double* f0 = pool + p.of;
+  const double* f1 = f0 + p.sf;
+  const int nk = DIM == 3 ? 2 : 1;
+  for (int dk = 0; dk < nk; dk++)
+    for (int dj = 0; dj < 2; dj++)
+      for (int di = 0; di < 2; di++) {
+        int i = 2 * ci - di, j = 2 * cj - dj, k = DIM == 3 ? 2 * ck - dk : 1;
+        long long c = gofs<DIM>(p.qn, i, j, k);
+        long long fc = iofs<DIM>(p.mx, i, j, k);
+        double r0, r1;
+        op_eval<PROB, DIM>(q, c, sy, sz, p.sq, qo[c], p.c, pp, r0, r1);
+        rf0[fc] = f0[fc] - r0;
+        rf1[fc] = f1[fc] - r1;
+      }
+  // the restriction reads rf written above by this same thread
+  auto at0 = [&](int i, int j, int k) { return rf0[iofs<DIM>(p.mx, i, j, k)]; };
+  auto at1 = [&](int i, int j, int k) { return rf1[iofs<DIM>(p.mx, i, j, k)]; };
+  double R0 = restrict_at<DIM>(at0, ci, cj, ck);
+  double R1 = restrict_at<DIM>(at1, ci, cj, ck);
+  // coarse operator on qc with the parent's spacing; parent qold at the
+  // section parent%qold(mb-1:mb+1)
+  const double* qc = pool + p.oqc;
+  long long csy = p.cn[0], csz = (long long)p.cn[0] * p.cn[1];
+  long long cc = gofs<DIM>(p.cn, ci, cj, ck);
+  long long pc = gofs<DIM>(par.qn, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 0);
+  double o0 = pool[par.oqold + pc];
+  double c0, c1;
+  op_eval<PROB, DIM>(qc, cc, csy, csz, p.sc, o0, par.c, pp, c0, c1);
+  long long pf = iofs<DIM>(par.mx, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 1);
+  pool[par.of + pf] = R0 + c0;
+  pool[par.of + par.sf + pf] = R1 + c1;
+}
+
+// CorrectFine step 1, afasroutines.f90:892-895 / :934-938:
+// qc(0:cmx+1) = parent%q(mb-1:mb+1) - qc
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_correct_a(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                      const Blk* __restrict__ blk, int nrvars) {
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  if (!ghosted_cell<DIM>(p.cn, b.start + threadIdx.x, i, j, k)) return;
+  const PatchDev& par = P[p.parent];
+  long long src = gofs<DIM>(par.qn, p.mb[0] - 1 + i, p.mb[1] - 1 + j, DIM == 3 ? p.mb[2] - 1 + k : 0);
+  long long dst = gofs<DIM>(p.cn, i, j, k);
+  for (int v = 0; v < nrvars; v++) {
+    double* qc = pool + p.oqc + v * p.sc;
+    qc[dst] = pool[par.oq + v * par.sq + src] - qc[dst];
+  }
+}
+
+// CorrectFine step 2: q(0:mx+1) += BiLinProlongationP1(qc)
+// (gridutilities.f90:156-195) / TriLinProlongationP1 (:510-566).  Each
+// thread recomputes the intermediate b (and c) entries it needs with the
+// reference's expressions, so the sums match the array form exactly.
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_correct_b(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                      const Blk* __restrict__ blk, int nrvars) {
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  if (!ghosted_cell<DIM>(p.qn, b.start + threadIdx.x, i, j, k)) return;
+  int ci = i >> 1, cj = j >> 1, ck = k >> 1;
+  bool ei = (i & 1) == 0, ej = (j & 1) == 0, ek = (k & 1) == 0;
+  long long dst = gofs<DIM>(p.qn, i, j, k);
+  for (int v = 0; v < nrvars; v++) {
+    const double* a = pool + p.oqc + v * p.sc;
+    // x-direction: b(i, cy, cz) from a(ci, cy, cz), a(ci+1, cy, cz)
+    auto bx = [&](int cy, int cz) {
+      double lo = a[gofs<DIM>(p.cn, ci, cy, cz)], hi = a[gofs<DIM>(p.cn, ci + 1, cy, cz)];
+      return ei ? 3.0 * lo + hi : lo + 3.0 * hi;
+    };
+    double add;
+    if (DIM == 2) {
+      double blo = bx(cj, 0), bhi = bx(cj + 1, 0);
+      add = ej ? (3.0 * blo + bhi) / 16.0 : (blo + 3.0 * bhi) / 16.0;
+    } else {
+      auto cy = [&](int cz) {
+        double blo = bx(cj, cz), bhi = bx(cj + 1, cz);
+        return ej ? 3.0 * blo + bhi : blo + 3.0 * bhi;
+      };
+      double clo = cy(ck), chi = cy(ck + 1);
+      add = ek ? (3.0 * clo + chi) / 64.0 : (clo + 3.0 * chi) / 64.0;
+    }
+    double* q = pool + p.oq + v * p.sq;
+    q[dst] = q[dst] + add;
+  }
+}
+
+// FillDownLevel, afasroutines.f90:257-327: parent f or q (mb) = R(child).
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_fill_down(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                      const Blk* __restrict__ blk, int nrvars, int field) {
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int ci, cj, ck;
+  if (!interior_cell<DIM>(p.cmx, b.start + threadIdx.x, ci, cj, ck)) return;
+  const PatchDev& par = P[p.parent];
+  for (int v = 0; v < nrvars; v++) {
+    if (field == 1) {
+      const double* f = pool + p.of + v * p.sf;
+      auto at = [&](int i, int j, int k) { return f[iofs<DIM>(p.mx, i, j, k)]; };
+      pool[par.of + v * par.sf + iofs<DIM>(par.mx, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 1)] =
+          restrict_at<DIM>(at, ci, cj, ck);
+    } else {
+      const double* q = pool + p.oq + v * p.sq;
+      auto at = [&](int i, int j, int k) { return q[gofs<DIM>(p.qn, i, j, k)]; };
+      pool[par.oq + v * par.sq + gofs<DIM>(par.qn, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 0)] =
+          restrict_at<DIM>(at, ci, cj, ck);
+    }
+  }
+}
+
+// GetSourceFunction, afasroutines.f90:330-381: ftmp = Source(q, qold)
+template <int PROB, int DIM>
+__global__ void __launch_bounds__(kBlock) k_get_source(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                       const Blk* __restrict__ blk, ProbParams pp) {
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  if (!interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) return;
+  double o0 = pool[p.oqold + gofs<DIM>(p.qn, i, j, k)];
+  double s0, s1;
+  source_eval<PROB, DIM>(o0, pp, s0, s1);
+  long long fc = iofs<DIM>(p.mx, i, j, k);
+  pool[p.oftmp + fc] = s0;
+  pool[p.oftmp + p.sf + fc] = s1;
+}
+
+// UpdateSourceFunction, afasroutines.f90:438-492: f = ftmp + SourceUpdate
+// (SourceUpdate is zero in both plugins).
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_update_source(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                          const Blk* __restrict__ blk, int nrvars) {
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  if (!interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) return;
+  long long fc = iofs<DIM>(p.mx, i, j, k);
+  for (int v = 0; v < nrvars; v++) pool[p.of + v * p.sf + fc] = pool[p.oftmp + v * p.sf + fc] + 0.0;
+}
+
+// ErrorAFAS partial sums (afasroutines.f90:113-233): rf = f - Op(q) on the
+// level's patches, per-block sums of rf^2 per variable.
+template <int PROB, int DIM>
+__global__ void __launch_bounds__(kBlock) k_norm_partial(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                         const Blk* __restrict__ blk, ProbParams pp,
+                                                         double* __restrict__ partial, int store_rf) {
+  __shared__ double red[2][kBlock / 32];
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  double s0 = 0.0, s1 = 0.0;
+  if (interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) {
+    const double* q = pool + p.oq;
+    long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
+    long long c = gofs<DIM>(p.qn, i, j, k);
+    long long fc = iofs<DIM>(p.mx, i, j, k);
+    double r0, r1;
+    op_eval<PROB, DIM>(q, c, sy, sz, p.sq, pool[p.oqold + c], p.c, pp, r0, r1);
+    double e0 = pool[p.of + fc] - r0;
+    double e1 = pool[p.of + p.sf + fc] - r1;
+    if (store_rf) {
+      pool[p.orf + fc] = e0;
+      pool[p.orf + p.sf + fc] = e1;
+    }
+    s0 = e0 * e0;
+    s1 = e1 * e1;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 = s0 + __shfl_down_sync(0xffffffffu, s0, o);
+    s1 = s1 + __shfl_down_sync(0xffffffffu, s1, o);
+  }
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    red[0][w] = s0;
+    red[1][w] = s1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0.0, t1 = 0.0;
+    for (int n = 0; n < kBlock / 32; n++) {
+      t0 = t0 + red[0][n];
+      t1 = t1 + red[1][n];
+    }
+    partial[2 * blockIdx.x] = t0;
+    partial[2 * blockIdx.x + 1] = t1;
+  }
+}
+
+// Final deterministic reduction of the block partials in block order.
+__global__ void k_norm_finish(const double* __restrict__ partial, int nblk, int nrvars, double count,
+                              int errortype, double* out, int* nonfinite) {
+  __shared__ double red[2][kBlock];
+  double t0 = 0.0, t1 = 0.0;
+  for (int n = threadIdx.x; n < nblk; n += blockDim.x) {
+    t0 = t0 + partial[2 * n];
+    t1 = t1 + partial[2 * n + 1];
+  }
+  red[0][threadIdx.x] = t0;
+  red[1][threadIdx.x] = t1;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      red[0][threadIdx.x] = red[0][threadIdx.x] + red[0][threadIdx.x + s];
+      red[1][threadIdx.x] = red[1][threadIdx.x] + red[1][threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double a = red[0][0], c = red[1][0];
+    double r;
+    if (errortype == 1) {
+      r = sqrt((a + c) / count);  // integralresult(1)/integralresult(2), :135
+    } else {
+      double cells = count / nrvars;
+      double e0 = sqrt(a / cells), e1 = sqrt(c / cells);
+      r = e1 > e0 ? e1 : e0;  // MAXVAL of component errors, :146-153
+    }
+    out[0] = r;
+    out[1] = a + c;
+    nonfinite[0] = isfinite(r) ? 0 : 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Ghost programs (SetGhost, boundary.f90:67-97): one thread per operation,
+// all variables of the cell.
+
+__device__ __forceinline__ void ghost_apply(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                            const GhostOp& g, const ProbParams& pp) {
+  const PatchDev& d = P[g.dp];
+  const PatchDev& s = P[g.sp];
+  for (int v = 0; v < pp.nrvars; v++) {
+    double* dq = pool + d.oq + v * d.sq;
+    const double* sq = pool + s.oq + v * s.sq;
+    double val;
+    switch (g.type) {
+      case kGCopy: val = sq[g.s0]; break;
+      case kGCopyAdd: val = sq[g.s0] + pp.qpo[v]; break;
+      case kGCopySub: val = sq[g.s0] - pp.qpo[v]; break;
+      case kGBC: val = ((g.mask >> v) & 1) ? 2.0 - sq[g.s0] : sq[g.s0]; break;
+      case kGCfA: val = kA1 * dq[g.s0] + kA2 * dq[g.s1] + kA3 * sq[g.c0]; break;
+      case kGCfAB:
+        val = kA1 * dq[g.s0] + kA2 * dq[g.s1] + kA3 * (kB1 * sq[g.c0] + kB2 * sq[g.c1] + kB3 * sq[g.c2]);
+        break;
+      default:
+        val = kA1 * dq[g.s0] + kA2 * dq[g.s1] +
+              kA3 * (kC1 * sq[g.c0] + kC2 * sq[g.c1] + kC3 * sq[g.c2] + kC4 * sq[g.c3]);
+        break;
+    }
+    dq[g.dcell] = val;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_ghost_stage(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                        const GhostOp* __restrict__ ops, int n, ProbParams pp) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  GhostOp g = ops[t];
+  ghost_apply(P, pool, g, pp);
+}
+
+// whole program in one block: stages separated by __syncthreads
+__global__ void __launch_bounds__(kBlock) k_ghost_program(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                          const GhostOp* __restrict__ ops,
+                                                          const int* __restrict__ stage_off, int nstages,
+                                                          ProbParams pp) {
+  for (int s = 0; s < nstages; s++) {
+    int lo = stage_off[s], hi = stage_off[s + 1];
+    for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+      GhostOp g = ops[t];
+      ghost_apply(P, pool, g, pp);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+
+#define DISPATCH_DIM(c, KER, ...)                            \
+  do {                                                       \
+    if ((c).ndims == 2) KER<2><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__); \
+    else KER<3><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__);    \
+  } while (0)
+
+#define DISPATCH_PD(c, KER, ...)                                                      \
+  do {                                                                                \
+    if ((c).pp.problem == kCH) {                                                      \
+      if ((c).ndims == 2) KER<kCH, 2><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__);       \
+      else KER<kCH, 3><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__);                      \
+    } else {                                                                          \
+      if ((c).ndims == 2) KER<kBio, 2><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__);      \
+      else KER<kBio, 3><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__);                     \
+    }                                                                                 \
+  } while (0)
+
+int launch_relax(const LaunchCtx& c, const Blk* blk, int nblk, int ipass) {
+  if (nblk <= 0) return 0;
+  DISPATCH_PD(c, k_relax, c.P, c.pool, blk, ipass, c.pp);
+  return 1;
+}
+int launch_restrict_q(const LaunchCtx& c, const Blk* blk, int nblk) {
+  if (nblk <= 0) return 0;
+  DISPATCH_DIM(c, k_restrict_q, c.P, c.pool, blk, c.pp.nrvars);
+  return 1;
+}
+int launch_coarse_ghost(const LaunchCtx& c, const Blk* blk, int nblk) {
+  if (nblk <= 0) return 0;
+  DISPATCH_DIM(c, k_coarse_ghost, c.P, c.pool, blk, c.pp.nrvars);
+  return 1;
+}
+int launch_coarse_load(const LaunchCtx& c, const Blk* blk, int nblk) {
+  if (nblk <= 0) return 0;
+  DISPATCH_PD(c, k_coarse_load, c.P, c.pool, blk, c.pp);
+  return 1;
+}
+int launch_correct_a(const LaunchCtx& c, const Blk* blk, int nblk) {
+  if (nblk <= 0) return 0;
+  DISPATCH_DIM(c, k_correct_a, c.P, c.pool, blk, c.pp.nrvars);
+  return 1;
+}
+int launch_correct_b(const LaunchCtx& c, const Blk* blk, int nblk) {
+  if (nblk <= 0) return 0;
+  DISPATCH_DIM(c, k_correct_b, c.P, c.pool, blk, c.pp.nrvars);
+  return 1;
+}
+int launch_fill_down(const LaunchCtx& c, const Blk* blk, int nblk, int field) {
+  if (nblk <= 0) return 0;
+  DISPATCH_DIM(c, k_fill_down, c.P, c.pool, blk, c.pp.nrvars, field);
+  return 1;
+}
+int launch_get_source(const LaunchCtx& c, const Blk* blk, int nblk) {
+  if (nblk <= 0) return 0;
+  DISPATCH_PD(c, k_get_source, c.P, c.pool, blk, c.pp);
+  return 1;
+}
+int launch_update_source(const LaunchCtx& c, const Blk* blk, int nblk) {
+  if (nblk <= 0) return 0;
+  DISPATCH_DIM(c, k_update_source, c.P, c.pool, blk, c.pp.nrvars);
+  return 1;
+}
+int launch_norm_partial(const LaunchCtx& c, const Blk* blk, int nblk, double* partial, int store_rf) {
+  if (nblk <= 0) return 0;
+  DISPATCH_PD(c, k_norm_partial, c.P, c.pool, blk, c.pp, partial, store_rf);
+  return 1;
+}
+int launch_norm_finish(cudaStream_t s, const double* partial, int nblk, int nrvars, double count, int errortype,
+                       double* out, int* nonfinite) {
+  k_norm_finish<<<1, kBlock, 0, s>>>(partial, nblk, nrvars, count, errortype, out, nonfinite);
+  return 1;
+}
+int launch_ghost_stage(const LaunchCtx& c, const GhostOp* ops, int n) {
+  if (n <= 0) return 0;
+  int nb = (n + kBlock - 1) / kBlock;
+  k_ghost_stage<<<nb, kBlock, 0, c.s>>>(c.P, c.pool, ops, n, c.pp);
+  return 1;
+}
+int launch_ghost_program_1cta(const LaunchCtx& c, const GhostOp* ops, const int* stage_off, int nstages) {
+  if (nstages <= 0) return 0;
+  k_ghost_program<<<1, kBlock, 0, c.s>>>(c.P, c.pool, ops, stage_off, nstages, c.pp);
+  return 1;
+}
+
+}  // namespace bsamg

@@ -1,0 +1,398 @@
+// Ghost-program compiler.
+//
+// SetGhost (LIBRARY/boundary.f90:67-97) fills the ghost ring of every patch
+// of a level by a fixed sequence of writers: coarse-fine interpolation
+// (colour-selective), sibling copies (ApplyOnLevelPairs(TransferBC)),
+// self-periodic copies, periodic-image copies, then the plugin's physical
+// boundary condition.  Later writers overwrite earlier ones, and some writers
+// read ghost cells written earlier in the same sequence (for example the
+// bottom-face boundary condition reads the left-face ghost column).
+//
+// Instead of walking patch pairs on every call (the reference's O(P^2) pair
+// loops), the host emits the whole write sequence once per (level, ipass)
+// after a regrid, removes writes that are overwritten before anything reads
+// them, and groups the rest into stages such that no two operations of a
+// stage touch the same cell in a conflicting way.  Executing the stages in
+// order on the device gives exactly the state the sequential sequence gives.
+#include <algorithm>
+#include <cstdint>
+#include <unordered_map>
+
+#include "hier.h"
+
+namespace bsamg {
+
+namespace {
+
+struct Em {
+  GhostOp op;
+  int64_t dst;
+  int64_t src[2];
+  int nsrc;
+};
+
+struct Emitter {
+  const Hier& H;
+  std::vector<Em> out;
+  explicit Emitter(const Hier& h) : H(h) {}
+
+  int cell(int p, int i, int j, int k) const {
+    const HostPatch& P = H.patches[p];
+    if (H.ndims == 2) return j * P.qn[0] + i;
+    return (k * P.qn[1] + j) * P.qn[0] + i;
+  }
+  static int64_t key(int p, int c) { return ((int64_t)p << 32) | (uint32_t)c; }
+
+  void copy(int type, int dp, int dc, int sp, int sc) {
+    Em e{};
+    e.op.type = type;
+    e.op.dp = dp;
+    e.op.dcell = dc;
+    e.op.sp = sp;
+    e.op.s0 = sc;
+    e.dst = key(dp, dc);
+    e.src[0] = key(sp, sc);
+    e.nsrc = 1;
+    out.push_back(e);
+  }
+  void bc(int dp, int dc, int sc, int mask) {
+    Em e{};
+    e.op.type = kGBC;
+    e.op.dp = dp;
+    e.op.dcell = dc;
+    e.op.sp = dp;
+    e.op.s0 = sc;
+    e.op.mask = mask;
+    e.dst = key(dp, dc);
+    e.src[0] = key(dp, sc);
+    e.nsrc = 1;
+    out.push_back(e);
+  }
+  // a1*f(s0) + a2*f(s1) + a3*(coarse combination)
+  void cf(int type, int dp, int dc, int s0, int s1, int cp, int c0, int c1 = 0, int c2 = 0, int c3 = 0) {
+    Em e{};
+    e.op.type = type;
+    e.op.dp = dp;
+    e.op.dcell = dc;
+    e.op.sp = cp;
+    e.op.s0 = s0;
+    e.op.s1 = s1;
+    e.op.c0 = c0;
+    e.op.c1 = c1;
+    e.op.c2 = c2;
+    e.op.c3 = c3;
+    e.dst = key(dp, dc);
+    e.src[0] = key(dp, s0);
+    e.src[1] = key(dp, s1);
+    e.nsrc = 2;  // parent cells live on another level: never written here
+    out.push_back(e);
+  }
+
+  // Interpolate2D, boundary.f90:143-333 (same statement order)
+  void interpolate2d(int f, int ipass) {
+    const HostPatch& F = H.patches[f];
+    int c = F.parent;
+    int mx1 = F.mx[0], mx2 = F.mx[1];
+    int mb11 = F.mbounds[0][0], mb12 = F.mbounds[0][1];
+    int mb21 = F.mbounds[1][0], mb22 = F.mbounds[1][1];
+    const int* m = F.mthbc;
+    auto fq = [&](int i, int j) { return cell(f, i, j, 0); };
+    auto cq = [&](int i, int j) { return cell(c, i, j, 0); };
+    if (ipass == 1 || ipass == 0) {
+      cf(kGCfA, f, fq(mx1 + 1, mx2 + 1), fq(mx1 - 1, mx2 - 1), fq(mx1, mx2), c, cq(mb12 + 1, mb22 + 1));
+      cf(kGCfA, f, fq(0, 0), fq(2, 2), fq(1, 1), c, cq(mb11 - 1, mb21 - 1));
+    }
+    if (ipass == 2 || ipass == 0) {
+      cf(kGCfA, f, fq(mx1 + 1, 0), fq(mx1 - 1, 2), fq(mx1, 1), c, cq(mb12 + 1, mb21 - 1));
+      cf(kGCfA, f, fq(0, mx2 + 1), fq(2, mx2 - 1), fq(1, mx2), c, cq(mb11 - 1, mb22 + 1));
+    }
+    if (m[0] == 2 || m[0] == kInternalBC) {
+      if (ipass == 1 || ipass == 0) {
+        for (int j = 2, n = 0; j <= mx2 - 2; j += 2, n++)
+          cf(kGCfA, f, fq(0, j), fq(2, j + 2), fq(1, j + 1), c, cq(mb11 - 1, mb21 + n));
+        cf(kGCfAB, f, fq(0, mx2), fq(2, mx2), fq(1, mx2), c, cq(mb11 - 1, mb22 + 1), cq(mb11 - 1, mb22),
+           cq(mb11 - 1, mb22 - 1));
+      }
+      if (ipass == 2 || ipass == 0) {
+        for (int j = 3, n = 0; j <= mx2 - 1; j += 2, n++)
+          cf(kGCfA, f, fq(0, j), fq(2, j - 2), fq(1, j - 1), c, cq(mb11 - 1, mb21 + 1 + n));
+        cf(kGCfAB, f, fq(0, 1), fq(2, 1), fq(1, 1), c, cq(mb11 - 1, mb21 - 1), cq(mb11 - 1, mb21),
+           cq(mb11 - 1, mb21 + 1));
+      }
+    }
+    if (m[1] == 2 || m[1] == kInternalBC) {
+      if (ipass == 1 || ipass == 0) {
+        for (int j = 3, n = 0; j <= mx2 - 1; j += 2, n++)
+          cf(kGCfA, f, fq(mx1 + 1, j), fq(mx1 - 1, j - 2), fq(mx1, j - 1), c, cq(mb12 + 1, mb21 + 1 + n));
+        cf(kGCfAB, f, fq(mx1 + 1, 1), fq(mx1 - 1, 1), fq(mx1, 1), c, cq(mb12 + 1, mb21 - 1), cq(mb12 + 1, mb21),
+           cq(mb12 + 1, mb21 + 1));
+      }
+      if (ipass == 2 || ipass == 0) {
+        for (int j = 2, n = 0; j <= mx2 - 2; j += 2, n++)
+          cf(kGCfA, f, fq(mx1 + 1, j), fq(mx1 - 1, j + 2), fq(mx1, j + 1), c, cq(mb12 + 1, mb21 + n));
+        cf(kGCfAB, f, fq(mx1 + 1, mx2), fq(mx1 - 1, mx2), fq(mx1, mx2), c, cq(mb12 + 1, mb22 + 1),
+           cq(mb12 + 1, mb22), cq(mb12 + 1, mb22 - 1));
+      }
+    }
+    if (m[2] == 2 || m[2] == kInternalBC) {
+      if (ipass == 1 || ipass == 0) {
+        for (int i = 2, n = 0; i <= mx1 - 2; i += 2, n++)
+          cf(kGCfA, f, fq(i, 0), fq(i + 2, 2), fq(i + 1, 1), c, cq(mb11 + n, mb21 - 1));
+        cf(kGCfAB, f, fq(mx1, 0), fq(mx1, 2), fq(mx1, 1), c, cq(mb12 + 1, mb21 - 1), cq(mb12, mb21 - 1),
+           cq(mb12 - 1, mb21 - 1));
+      }
+      if (ipass == 2 || ipass == 0) {
+        for (int i = 3, n = 0; i <= mx1 - 1; i += 2, n++)
+          cf(kGCfA, f, fq(i, 0), fq(i - 2, 2), fq(i - 1, 1), c, cq(mb11 + 1 + n, mb21 - 1));
+        cf(kGCfAB, f, fq(1, 0), fq(1, 2), fq(1, 1), c, cq(mb11 - 1, mb21 - 1), cq(mb11, mb21 - 1),
+           cq(mb11 + 1, mb21 - 1));
+      }
+    }
+    if (m[3] == 2 || m[3] == kInternalBC) {
+      if (ipass == 1 || ipass == 0) {
+        for (int i = 3, n = 0; i <= mx1 - 1; i += 2, n++)
+          cf(kGCfA, f, fq(i, mx2 + 1), fq(i - 2, mx2 - 1), fq(i - 1, mx2), c, cq(mb11 + 1 + n, mb22 + 1));
+        cf(kGCfAB, f, fq(1, mx2 + 1), fq(1, mx2 - 1), fq(1, mx2), c, cq(mb11 - 1, mb22 + 1), cq(mb11, mb22 + 1),
+           cq(mb11 + 1, mb22 + 1));
+      }
+      if (ipass == 2 || ipass == 0) {
+        for (int i = 2, n = 0; i <= mx1 - 2; i += 2, n++)
+          cf(kGCfA, f, fq(i, mx2 + 1), fq(i + 2, mx2 - 1), fq(i + 1, mx2), c, cq(mb11 + n, mb22 + 1));
+        cf(kGCfAB, f, fq(mx1, mx2 + 1), fq(mx1, mx2 - 1), fq(mx1, mx2), c, cq(mb12 + 1, mb22 + 1),
+           cq(mb12, mb22 + 1), cq(mb12 - 1, mb22 + 1));
+      }
+    }
+  }
+
+  // GhostOverlap, boundary.f90:359-431 (the landscape part is mesh-build
+  // only).  Ghost cells of g1 that lie in the interior of g2 (shifted by
+  // off) take g2's values, then the converse.
+  void ghost_overlap(int g1, int g2, const int* off) {
+    const HostPatch& A = H.patches[g1];
+    const HostPatch& B = H.patches[g2];
+    int nd = H.ndims, mbc = H.mbc;
+    int mg1[3][2], mg2[3][2], ovg[3][2], ovg1[3][2], ovg2[3][2];
+    for (int n = 0; n < 3; n++)
+      for (int s = 0; s < 2; s++) mg1[n][s] = mg2[n][s] = ovg[n][s] = ovg1[n][s] = ovg2[n][s] = 1;
+    for (int n = 0; n < nd; n++) {
+      mg1[n][0] = A.mglobal[n][0];
+      mg1[n][1] = A.mglobal[n][1];
+      mg2[n][0] = B.mglobal[n][0] + (off ? off[n] : 0);
+      mg2[n][1] = B.mglobal[n][1] + (off ? off[n] : 0);
+    }
+    for (int n = 0; n < nd; n++) {
+      ovg[n][0] = std::max(mg1[n][0] - mbc, mg2[n][0] - mbc);
+      ovg[n][1] = std::min(mg1[n][1] + mbc, mg2[n][1] + mbc);
+    }
+    for (int n = 0; n < nd; n++)
+      if (ovg[n][1] - ovg[n][0] < 0) return;
+    for (int n = 0; n < nd; n++) {
+      ovg1[n][0] = std::max(ovg[n][0], mg2[n][0]);
+      ovg1[n][1] = std::min(ovg[n][1], mg2[n][1]);
+      ovg2[n][0] = std::max(ovg[n][0], mg1[n][0]);
+      ovg2[n][1] = std::min(ovg[n][1], mg1[n][1]);
+    }
+    auto xfer = [&](int dst, int src, int ov[3][2], int mgd[3][2], int mgs[3][2]) {
+      int lo[3], ls[3], ext[3];
+      for (int n = 0; n < 3; n++) {
+        if (n < nd) {
+          lo[n] = ov[n][0] - mgd[n][0] + 1;
+          ls[n] = ov[n][0] - mgs[n][0] + 1;
+          ext[n] = ov[n][1] - ov[n][0];
+        } else {
+          lo[n] = ls[n] = 1;
+          ext[n] = 0;
+        }
+      }
+      for (int k = 0; k <= ext[2]; k++)
+        for (int j = 0; j <= ext[1]; j++)
+          for (int i = 0; i <= ext[0]; i++)
+            copy(kGCopy, dst, cell(dst, lo[0] + i, lo[1] + j, nd == 3 ? lo[2] + k : 0), src,
+                 cell(src, ls[0] + i, ls[1] + j, nd == 3 ? ls[2] + k : 0));
+    };
+    xfer(g1, g2, ovg1, mg1, mg2);
+    xfer(g2, g1, ovg2, mg2, mg1);
+  }
+
+  // SelfPeriodicBC, boundary.f90:480-577
+  void self_periodic(int p) {
+    const HostPatch& P = H.patches[p];
+    int nd = H.ndims, mbc = H.mbc;
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+      lo[d] = d < nd ? 1 - mbc : 1;
+      hi[d] = d < nd ? P.mx[d] + mbc : 1;
+    }
+    auto cl = [&](int i, int j, int k) { return cell(p, i, j, nd == 3 ? k : 0); };
+    if (P.mthbc[0] == 2 && P.mthbc[1] == 2)
+      for (int ibc = 1; ibc <= mbc; ibc++) {
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++) copy(kGCopyAdd, p, cl(P.mx[0] + ibc, j, k), p, cl(ibc, j, k));
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++)
+            copy(kGCopySub, p, cl(1 - ibc, j, k), p, cl(P.mx[0] + 1 - ibc, j, k));
+      }
+    if (P.mthbc[2] == 2 && P.mthbc[3] == 2)
+      for (int ibc = 1; ibc <= mbc; ibc++) {
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int i = lo[0]; i <= hi[0]; i++) copy(kGCopy, p, cl(i, P.mx[1] + ibc, k), p, cl(i, ibc, k));
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int i = lo[0]; i <= hi[0]; i++) copy(kGCopy, p, cl(i, 1 - ibc, k), p, cl(i, P.mx[1] + 1 - ibc, k));
+      }
+    if (nd == 3 && P.mthbc[4] == 2 && P.mthbc[5] == 2)
+      for (int ibc = 1; ibc <= mbc; ibc++) {
+        for (int j = lo[1]; j <= hi[1]; j++)
+          for (int i = lo[0]; i <= hi[0]; i++) copy(kGCopy, p, cl(i, j, P.mx[2] + ibc), p, cl(i, j, ibc));
+        for (int j = lo[1]; j <= hi[1]; j++)
+          for (int i = lo[0]; i <= hi[0]; i++) copy(kGCopy, p, cl(i, j, 1 - ibc), p, cl(i, j, P.mx[2] + 1 - ibc));
+      }
+  }
+
+  // Dirichlet-variable mask of the plugin's UserBC (CH/problem.f90:770-881,
+  // BioGrowth/problem.f90:623-736): 2D CH reflects both variables, 2D
+  // BioGrowth reflects phi and sets n = 2 - n, both 3D plugins set 2 - q.
+  int bc_mask() const {
+    if (H.ndims == 3) return (1 << H.nrvars) - 1;
+    return H.problem == kCH ? 0 : 2;
+  }
+
+  // SetPhysicalBC2D/3D (boundary.f90:614-802) -> UserBC on each face with
+  // mthbc = 10, faces in order 1..2*ndims.
+  void physical_bc(int p) {
+    const HostPatch& P = H.patches[p];
+    int nd = H.ndims, mbc = H.mbc, ll = 1 - mbc;
+    int ul[3];
+    for (int d = 0; d < 3; d++) ul[d] = P.mx[d] + mbc;
+    int kl = nd == 3 ? ll : 0, ku = nd == 3 ? ul[2] : 0;
+    int mask = bc_mask();
+    for (int face = 1; face <= 2 * nd; face++) {
+      if (P.mthbc[face - 1] != 10) continue;
+      int d = (face - 1) / 2, hi = (face - 1) % 2;
+      for (int ibc = 1; ibc <= mbc; ibc++) {
+        int gd = hi ? P.mx[d] + ibc : 1 - ibc;
+        int gs = hi ? P.mx[d] - ibc + 1 : ibc;
+        if (d == 0) {
+          for (int k = kl; k <= ku; k++)
+            for (int j = ll; j <= ul[1]; j++) bc(p, cell(p, gd, j, k), cell(p, gs, j, k), mask);
+        } else if (d == 1) {
+          for (int k = kl; k <= ku; k++)
+            for (int i = ll; i <= ul[0]; i++) bc(p, cell(p, i, gd, k), cell(p, i, gs, k), mask);
+        } else {
+          for (int j = ll; j <= ul[1]; j++)
+            for (int i = ll; i <= ul[0]; i++) bc(p, cell(p, i, j, gd), cell(p, i, j, gs), mask);
+        }
+      }
+    }
+  }
+
+  // GetPeriodicOffsets, boundary.f90:875-954
+  void periodic_offsets(int level, int poff[13][3]) const {
+    const int* mm = H.mxmax[level];
+    for (int o = 0; o < H.nperoff; o++) {
+      int a = 0, b = 0, c = 0;
+      switch (H.peroffidx[o]) {
+        case 1: a = mm[0]; break;
+        case 2: b = mm[1]; break;
+        case 3: c = mm[2]; break;
+        case 4: a = mm[0]; b = mm[1]; break;
+        case 5: a = -mm[0]; b = mm[1]; break;
+        case 6: b = mm[1]; c = mm[2]; break;
+        case 7: b = mm[1]; c = -mm[2]; break;
+        case 8: a = mm[0]; c = mm[2]; break;
+        case 9: a = -mm[0]; c = mm[2]; break;
+        case 10: a = mm[0]; b = mm[1]; c = mm[2]; break;
+        case 11: a = mm[0]; b = mm[1]; c = -mm[2]; break;
+        case 12: a = -mm[0]; b = mm[1]; c = mm[2]; break;
+        case 13: a = mm[0]; b = -mm[1]; c = mm[2]; break;
+      }
+      poff[o][0] = a;
+      poff[o][1] = b;
+      poff[o][2] = c;
+    }
+  }
+};
+
+}  // namespace
+
+std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std::vector<int>& stage_off) {
+  Emitter E(H);
+  const LevelT& L = H.L(level);
+  const std::vector<int>& ps = L.patches;
+  int n = (int)ps.size();
+  if (level > 0) {
+    if (H.ndims == 2)
+      for (int a = 0; a < n; a++) E.interpolate2d(ps[a], ipass);
+    for (int a = 0; a < n; a++)
+      for (int b = a + 1; b < n; b++) E.ghost_overlap(ps[a], ps[b], nullptr);
+  }
+  if (H.periodic) {
+    for (int a = 0; a < n; a++) E.self_periodic(ps[a]);
+    if (level > 0) {
+      int poff[13][3];
+      E.periodic_offsets(level, poff);
+      for (int a = 0; a < n; a++)
+        for (int b = a + 1; b < n; b++)
+          for (int pol = -1; pol <= 1; pol += 2)
+            for (int o = 0; o < H.nperoff; o++) {
+              int off[3] = {pol * poff[o][0], pol * poff[o][1], pol * poff[o][2]};
+              E.ghost_overlap(ps[a], ps[b], off);
+            }
+    }
+  }
+  for (int a = 0; a < n; a++) E.physical_bc(ps[a]);
+
+  // pass 1: drop writes overwritten before any read
+  std::vector<Em>& ops = E.out;
+  int m = (int)ops.size();
+  std::vector<char> dead(m, 0), readf(m, 0);
+  std::unordered_map<int64_t, int> last;
+  last.reserve(m * 2 + 16);
+  for (int x = 0; x < m; x++) {
+    for (int s = 0; s < ops[x].nsrc; s++) {
+      auto it = last.find(ops[x].src[s]);
+      if (it != last.end()) readf[it->second] = 1;
+    }
+    auto it = last.find(ops[x].dst);
+    if (it != last.end() && !readf[it->second]) dead[it->second] = 1;
+    last[ops[x].dst] = x;
+  }
+  // pass 2: stage = 1 + latest conflicting live predecessor
+  std::unordered_map<int64_t, int> wst, rst;
+  wst.reserve(m * 2 + 16);
+  rst.reserve(m * 2 + 16);
+  std::vector<int> stage(m, -1);
+  int nst = 0;
+  for (int x = 0; x < m; x++) {
+    if (dead[x]) continue;
+    int st = 0;
+    for (int s = 0; s < ops[x].nsrc; s++) {
+      auto it = wst.find(ops[x].src[s]);
+      if (it != wst.end()) st = std::max(st, it->second + 1);
+    }
+    auto r = rst.find(ops[x].dst);
+    if (r != rst.end()) st = std::max(st, r->second + 1);
+    auto w = wst.find(ops[x].dst);
+    if (w != wst.end()) st = std::max(st, w->second + 1);
+    stage[x] = st;
+    for (int s = 0; s < ops[x].nsrc; s++) {
+      auto it = rst.find(ops[x].src[s]);
+      if (it == rst.end()) rst[ops[x].src[s]] = st;
+      else it->second = std::max(it->second, st);
+    }
+    wst[ops[x].dst] = st;
+    rst.erase(ops[x].dst);
+    nst = std::max(nst, st + 1);
+  }
+  std::vector<GhostOp> res;
+  stage_off.assign(nst + 1, 0);
+  for (int x = 0; x < m; x++)
+    if (!dead[x]) stage_off[stage[x] + 1]++;
+  for (int s = 0; s < nst; s++) stage_off[s + 1] += stage_off[s];
+  res.resize(stage_off[nst]);
+  std::vector<int> fill(stage_off.begin(), stage_off.end() - 1);
+  for (int x = 0; x < m; x++)
+    if (!dead[x]) res[fill[stage[x]]++] = ops[x].op;
+  return res;
+}
+
+}  // namespace bsamg

@@ -1,0 +1,823 @@
+// Host side of libbsamg: context, hierarchy tables, device pool, launch
+// schedule of the FAS V-cycle, CUDA-graph replay and the C ABI.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "hier.h"
+#include "mixed.h"
+
+using namespace bsamg;
+
+namespace {
+
+thread_local std::string g_detail;
+
+int cuda_fail(cudaError_t e, const char* what) {
+  g_detail = std::string(what) + ": " + cudaGetErrorString(e);
+  return BSAMG_ERR_CUDA;
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t e__ = (call);                      \
+    if (e__ != cudaSuccess) return cuda_fail(e__, #call); \
+  } while (0)
+
+#define RET(x)                 \
+  do {                         \
+    int r__ = (x);             \
+    if (r__ != BSAMG_OK) return r__; \
+  } while (0)
+
+// count launches and check the launch status
+int after_launch(Hier& H, int n) {
+  if (n <= 0) return BSAMG_OK;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  if (H.capturing) H.capture_launches += n;
+  else H.launches += n;
+  return BSAMG_OK;
+}
+
+int set_device(const Hier& H) {
+  CK(cudaSetDevice(H.ctx->device));
+  return BSAMG_OK;
+}
+
+long long align32(long long x) { return (x + 31) & ~31LL; }
+
+// ---------------------------------------------------------------------------
+// schedule pieces (plain FP64)
+
+int enq_relax(Hier& H, int level, int ipass) {
+  LevelT& L = H.L(level);
+  return after_launch(H, launch_relax(H.lc(), L.d_blk[kKindColor], L.nblk[kKindColor], ipass));
+}
+
+int enq_set_ghost(Hier& H, int level, int ipass) {
+  LevelT& L = H.L(level);
+  GhostProg& g = L.gp[ipass];
+  int nst = (int)g.stage_off.size() - 1;
+  if (nst <= 0) return BSAMG_OK;
+  int nops = g.stage_off[nst];
+  LaunchCtx c = H.lc();
+  if (nops <= 2048) return after_launch(H, launch_ghost_program_1cta(c, g.d_ops, g.d_stage_off, nst));
+  for (int s = 0; s < nst; s++)
+    RET(after_launch(H, launch_ghost_stage(c, g.d_ops + g.stage_off[s], g.stage_off[s + 1] - g.stage_off[s])));
+  return BSAMG_OK;
+}
+
+int enq_level_relax(Hier& H, int level, int nsmooth) {
+  for (int pass = 1; pass <= nsmooth; pass++)
+    for (int rb = 1; rb <= 2; rb++) {
+      RET(enq_relax(H, level, rb));
+      RET(enq_set_ghost(H, level, rb));
+    }
+  return BSAMG_OK;
+}
+
+// AFASVcycle, afasroutines.f90:495-529
+int enq_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
+  RET(enq_level_relax(H, level, nsmooth));
+  if (level > minlevel) {
+    LevelT& L = H.L(level);
+    LaunchCtx c = H.lc();
+    RET(after_launch(H, launch_restrict_q(c, L.d_blk[kKindCoarse], L.nblk[kKindCoarse])));
+    RET(enq_set_ghost(H, level - 1, 0));
+    RET(after_launch(H, launch_coarse_ghost(c, L.d_blk[kKindCGhost], L.nblk[kKindCGhost])));
+    RET(after_launch(H, launch_coarse_load(c, L.d_blk[kKindCoarse], L.nblk[kKindCoarse])));
+    RET(enq_vcycle(H, level - 1, minlevel, nsmooth));
+    RET(after_launch(H, launch_correct_a(c, L.d_blk[kKindCGhost], L.nblk[kKindCGhost])));
+    RET(after_launch(H, launch_correct_b(c, L.d_blk[kKindFGhost], L.nblk[kKindFGhost])));
+    RET(enq_set_ghost(H, level, 0));
+    RET(enq_level_relax(H, level, nsmooth));
+  }
+  return BSAMG_OK;
+}
+
+// FillDown, afasroutines.f90:236-254 (field 1 = source, 2 = solution)
+int enq_fill_down(Hier& H, int field, int finest, int minlevel) {
+  for (int level = finest; level >= minlevel + 1; level--) {
+    LevelT& L = H.L(level);
+    RET(after_launch(H, launch_fill_down(H.lc(), L.d_blk[kKindCoarse], L.nblk[kKindCoarse], field)));
+    if (field == 2) RET(enq_set_ghost(H, level - 1, 0));
+  }
+  return BSAMG_OK;
+}
+
+int enq_get_source(Hier& H, int finest) {
+  for (int level = finest; level >= 0; level--) {
+    LevelT& L = H.L(level);
+    RET(after_launch(H, launch_get_source(H.lc(), L.d_blk[kKindInterior], L.nblk[kKindInterior])));
+  }
+  return BSAMG_OK;
+}
+
+int enq_update_source(Hier& H, int finest) {
+  for (int level = finest; level >= 0; level--) {
+    LevelT& L = H.L(level);
+    RET(after_launch(H, launch_update_source(H.lc(), L.d_blk[kKindInterior], L.nblk[kKindInterior])));
+  }
+  return BSAMG_OK;
+}
+
+// ErrorAFAS on `level` -> H.d_norm[0] (device)
+int enq_norm(Hier& H, int level, int errortype) {
+  LevelT& L = H.L(level);
+  RET(after_launch(H, launch_norm_partial(H.lc(), L.d_blk[kKindInterior], L.nblk[kKindInterior], H.d_partial, 1)));
+  return after_launch(H, launch_norm_finish(H.s, H.d_partial, L.nblk[kKindInterior], H.nrvars, L.count, errortype,
+                                            H.d_norm, H.d_nonfinite));
+}
+
+int enq_copy_q_to_qold(Hier& H, int minlevel, int finest) {
+  bool all = minlevel <= H.minlevel && finest >= H.maxlevel;
+  if (all) {
+    CK(cudaMemcpyAsync(H.pool + H.qold_region, H.pool + H.q_region, sizeof(double) * H.q_len,
+                       cudaMemcpyDeviceToDevice, H.s));
+    return BSAMG_OK;
+  }
+  for (int level = minlevel; level <= finest; level++)
+    for (int p : H.L(level).patches) {
+      HostPatch& P = H.patches[p];
+      CK(cudaMemcpyAsync(H.pool + P.oqold, H.pool + P.oq, sizeof(double) * P.sq * H.nrvars,
+                         cudaMemcpyDeviceToDevice, H.s));
+    }
+  return BSAMG_OK;
+}
+
+// One V-cycle iteration body of MultigridIterations (afasroutines.f90:81-104)
+// followed by a copy of the norm to pinned host memory.
+int enq_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype) {
+  RET(enq_vcycle(H, finest, minlevel, nsmooth));
+  RET(enq_fill_down(H, 2, finest, minlevel));
+  RET(enq_update_source(H, finest));
+  RET(enq_fill_down(H, 1, finest, minlevel));
+  RET(enq_norm(H, finest, errortype));
+  CK(cudaMemcpyAsync(H.h_norm, H.d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, H.s));
+  CK(cudaMemcpyAsync(H.h_nonfinite, H.d_nonfinite, sizeof(int), cudaMemcpyDeviceToHost, H.s));
+  return BSAMG_OK;
+}
+
+int get_graph(Hier& H, int mode, int finest, int minlevel, int nsmooth, int errortype, Hier::GraphRec** out) {
+  auto key = std::make_tuple(mode, finest, minlevel, nsmooth, errortype);
+  auto it = H.graphs.find(key);
+  if (it != H.graphs.end()) {
+    *out = &it->second;
+    return BSAMG_OK;
+  }
+  CK(cudaStreamBeginCapture(H.s, cudaStreamCaptureModeThreadLocal));
+  H.capturing = true;
+  H.capture_launches = 0;
+  int rc = mode == BSAMG_MODE_FP64 ? enq_iteration(H, finest, minlevel, nsmooth, errortype)
+                                   : mixed_enq_iteration(H, finest, minlevel, nsmooth, errortype);
+  H.capturing = false;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(H.s, &g);
+  if (rc != BSAMG_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  Hier::GraphRec rec;
+  e = cudaGraphInstantiate(&rec.exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  rec.nlaunch = H.capture_launches;
+  H.graphs[key] = rec;
+  *out = &H.graphs[key];
+  return BSAMG_OK;
+}
+
+int check_nonfinite(Hier& H) { return *H.h_nonfinite ? BSAMG_ERR_NONFINITE : BSAMG_OK; }
+
+int multigrid_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol,
+                         int errortype, int mode, int strict, int* ncycles, double* residuals) {
+  if (finest > H.maxlevel || minlevel < H.minlevel || finest < 0 || minlevel > 0) return BSAMG_ERR_ARG;
+  if (maxvcycles < 1 || nsmooth < 1 || (errortype != 1 && errortype != 2)) return BSAMG_ERR_ARG;
+  if (mode != BSAMG_MODE_FP64 && mode != BSAMG_MODE_MIXED) return BSAMG_ERR_ARG;
+  RET(set_device(H));
+  // afasroutines.f90:57-76
+  RET(enq_fill_down(H, 2, finest, minlevel));
+  RET(enq_get_source(H, finest));
+  RET(enq_update_source(H, finest));
+  RET(enq_fill_down(H, 1, finest, minlevel));
+  if (mode == BSAMG_MODE_MIXED) RET(mixed_prepare(H, finest, minlevel));
+  Hier::GraphRec* gr = nullptr;
+  RET(get_graph(H, mode, finest, minlevel, nsmooth, errortype, &gr));
+  int it;
+  double r = 0.0;
+  for (it = 1; it <= maxvcycles; it++) {
+    CK(cudaGraphLaunch(gr->exec, H.s));
+    H.launches += gr->nlaunch;
+    CK(cudaStreamSynchronize(H.s));
+    r = H.h_norm[0];
+    if (residuals) residuals[it - 1] = r;
+    RET(check_nonfinite(H));
+    if (r < tol) break;
+  }
+  bool conv = it <= maxvcycles;
+  if (ncycles) *ncycles = conv ? it : maxvcycles;
+  if (!conv && strict) return BSAMG_ERR_NOT_CONVERGED;
+  return BSAMG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// construction
+
+int add_patch(Hier& H, int level, int id, int parent_id, const int mx[3], const int mglobal[6], const int mbounds[6],
+              const int mthbc[6], const double dx[3], const double xlower[3]) {
+  if (H.committed || level < -kMaxDepth || level > kMaxDepth) return BSAMG_ERR_ARG;
+  if (H.id2idx.count(id)) return BSAMG_ERR_ARG;
+  HostPatch P{};
+  P.level = level;
+  P.id = id;
+  P.parent_id = parent_id;
+  P.parent = -1;
+  for (int d = 0; d < 3; d++) {
+    bool u = d < H.ndims;
+    P.mx[d] = u ? mx[d] : 1;
+    P.mglobal[d][0] = u ? mglobal[2 * d] : 1;
+    P.mglobal[d][1] = u ? mglobal[2 * d + 1] : 1;
+    P.mbounds[d][0] = u ? mbounds[2 * d] : 1;
+    P.mbounds[d][1] = u ? mbounds[2 * d + 1] : 1;
+    P.dx[d] = u ? dx[d] : 0.0;
+    P.xlower[d] = u ? xlower[d] : 0.0;
+    if (u && P.mx[d] < 1) return BSAMG_ERR_ARG;
+  }
+  for (int f = 0; f < 6; f++) P.mthbc[f] = f < 2 * H.ndims ? mthbc[f] : 10;
+  H.id2idx[id] = (int)H.patches.size();
+  H.patches.push_back(P);
+  return BSAMG_OK;
+}
+
+// RootInit + InitSeed, bsamroutines.f90:226-510
+int build_uniform(Hier& H, const int mx[3], int minlevel, const int mthbc[6], const double xlower[3],
+                  const double xupper[3]) {
+  if (H.committed || !H.patches.empty() || minlevel > 0 || minlevel < -kMaxDepth) return BSAMG_ERR_ARG;
+  int nd = H.ndims;
+  int cmx[3] = {1, 1, 1}, mg[6] = {1, 1, 1, 1, 1, 1}, mb[6] = {1, 1, 1, 1, 1, 1};
+  double dx[3] = {0, 0, 0}, xl[3] = {0, 0, 0};
+  for (int d = 0; d < nd; d++) {
+    if (mx[d] <= 0 || mx[d] % 2) return BSAMG_ERR_ARG;
+    if (!(xupper[d] > xlower[d])) return BSAMG_ERR_ARG;
+    cmx[d] = mx[d];
+    mg[2 * d + 1] = mx[d];
+    dx[d] = (xupper[d] - xlower[d]) / (double)mx[d];
+    xl[d] = xlower[d];
+  }
+  for (int d = 1; d < nd; d++)
+    if (std::fabs(dx[0] - dx[d]) > 1.0e-10) return BSAMG_ERR_ARG;
+  for (int d = 0; d < nd; d++) {
+    mb[2 * d] = 1;
+    mb[2 * d + 1] = minlevel < 0 ? mx[d] / 2 : mx[d];
+  }
+  RET(add_patch(H, 0, 0, minlevel < 0 ? 1 : -1, cmx, mg, mb, mthbc, dx, xl));
+  for (int l = -1; l >= minlevel; l--) {
+    int nmx[3] = {1, 1, 1}, nmg[6] = {1, 1, 1, 1, 1, 1}, nmb[6] = {1, 1, 1, 1, 1, 1};
+    double ndx[3] = {0, 0, 0};
+    for (int d = 0; d < nd; d++) {
+      if (cmx[d] % 2) return BSAMG_ERR_ARG;
+      nmx[d] = cmx[d] / 2;
+      ndx[d] = dx[d] * 2.0;
+      nmg[2 * d] = 1;
+      nmg[2 * d + 1] = mg[2 * d + 1] / 2;
+      nmb[2 * d] = 1;
+      nmb[2 * d + 1] = l > minlevel ? nmx[d] / 2 : nmx[d];
+    }
+    RET(add_patch(H, l, -l, l > minlevel ? -l + 1 : -1, nmx, nmg, nmb, mthbc, ndx, xl));
+    memcpy(cmx, nmx, sizeof(cmx));
+    memcpy(mg, nmg, sizeof(mg));
+    memcpy(dx, ndx, sizeof(dx));
+  }
+  return BSAMG_OK;
+}
+
+// PeriodicSetup, boundary.f90:805-872
+void periodic_setup(Hier& H, const int* mthbc) {
+  int m[6];
+  for (int f = 0; f < 6; f++) m[f] = f < 2 * H.ndims ? mthbc[f] : 10;
+  static const int i13[13] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13};
+  static const int i1245[4] = {1, 2, 4, 5}, i1389[4] = {1, 3, 8, 9}, i2367[4] = {2, 3, 6, 7};
+  static const int i1[1] = {1}, i2[1] = {2}, i3[1] = {3};
+  const int* src = nullptr;
+  int n = 0;
+  H.periodic = 1;
+  if (m[0] == 2) {
+    if (m[2] == 2) {
+      if (m[4] == 2) { src = i13; n = 13; } else { src = i1245; n = 4; }
+    } else {
+      if (m[4] == 2) { src = i1389; n = 4; } else { src = i1; n = 1; }
+    }
+  } else {
+    if (m[2] == 2) {
+      if (m[4] == 2) { src = i2367; n = 4; } else { src = i2; n = 1; }
+    } else {
+      if (m[4] == 2) { src = i3; n = 1; } else { H.periodic = 0; }
+    }
+  }
+  H.nperoff = n;
+  for (int i = 0; i < n; i++) H.peroffidx[i] = src[i];
+}
+
+// plugin coefficients for a spacing h (see PatchDev::c)
+void coefficients(const Hier& H, double h, double* c) {
+  double h2 = h * h;
+  if (H.problem == kCH) {
+    double k = H.ndims == 2 ? 4.0 : 6.0;
+    c[0] = H.pp.dt / h2;       // tmp1, CH/problem.f90:341
+    c[1] = H.pp.eps2 / h2;     // tmp2, :342
+    c[2] = k * H.pp.eps2 / h2; // tmp3, :343 (:579)
+    c[3] = k * c[0];           // a(1,2), :346 (:582)
+  } else {
+    c[0] = H.pp.dt * H.pp.eps2 / h2;  // tmp1, BioGrowth/problem.f90:277
+    c[1] = 1.0 / h2;                  // tmp3, :278
+    c[2] = 4.0 * c[0] + 1.0;          // first two terms of tmp2, :282
+    c[3] = 4.0 * c[1];                // first term of tmp4, :288
+  }
+}
+
+int upload_blocks(Hier& H, LevelT& L, int kind) {
+  std::vector<Blk> v;
+  for (int p : L.patches) {
+    HostPatch& P = H.patches[p];
+    long long units = 0;
+    switch (kind) {
+      case kKindColor: units = (long long)((P.mx[0] + 1) / 2) * P.mx[1] * P.mx[2]; break;
+      case kKindInterior: units = (long long)P.mx[0] * P.mx[1] * P.mx[2]; break;
+      case kKindCoarse: units = P.parent >= 0 ? (long long)P.cmx[0] * P.cmx[1] * P.cmx[2] : 0; break;
+      case kKindCGhost: units = P.parent >= 0 ? (long long)P.cn[0] * P.cn[1] * P.cn[2] : 0; break;
+      case kKindFGhost: units = (long long)P.qn[0] * P.qn[1] * P.qn[2]; break;
+    }
+    for (long long s = 0; s < units; s += kBlock) v.push_back(Blk{p, (int)s});
+  }
+  L.nblk[kind] = (int)v.size();
+  if (v.empty()) return BSAMG_OK;
+  CK(cudaMalloc(&L.d_blk[kind], sizeof(Blk) * v.size()));
+  H.bytes += sizeof(Blk) * v.size();
+  CK(cudaMemcpy(L.d_blk[kind], v.data(), sizeof(Blk) * v.size(), cudaMemcpyHostToDevice));
+  return BSAMG_OK;
+}
+
+// every cell an operation touches must lie inside its patch's ghosted
+// plane (parent plane for the coarse cells of C/F operations)
+bool ghost_ops_in_bounds(const Hier& H, const GhostProg& g) {
+  int np = (int)H.patches.size();
+  for (const GhostOp& o : g.ops) {
+    if (o.dp < 0 || o.dp >= np || o.sp < 0 || o.sp >= np) return false;
+    long long nd = H.patches[o.dp].sq, ns = H.patches[o.sp].sq;
+    if (o.dcell < 0 || o.dcell >= nd) return false;
+    if (o.type <= kGBC) {
+      if (o.s0 < 0 || o.s0 >= ns) return false;
+    } else {
+      if (o.s0 < 0 || o.s0 >= nd || o.s1 < 0 || o.s1 >= nd) return false;
+      int nc = o.type == kGCfA ? 1 : (o.type == kGCfAB ? 3 : 4);
+      int c[4] = {o.c0, o.c1, o.c2, o.c3};
+      for (int x = 0; x < nc; x++)
+        if (c[x] < 0 || c[x] >= ns) return false;
+    }
+  }
+  return true;
+}
+
+int upload_ghost(Hier& H, GhostProg& g) {
+  if (g.ops.empty()) return BSAMG_OK;
+  if (!ghost_ops_in_bounds(H, g)) return BSAMG_ERR_ARG;
+  CK(cudaMalloc(&g.d_ops, sizeof(GhostOp) * g.ops.size()));
+  CK(cudaMalloc(&g.d_stage_off, sizeof(int) * g.stage_off.size()));
+  H.bytes += sizeof(GhostOp) * g.ops.size() + sizeof(int) * g.stage_off.size();
+  CK(cudaMemcpy(g.d_ops, g.ops.data(), sizeof(GhostOp) * g.ops.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(g.d_stage_off, g.stage_off.data(), sizeof(int) * g.stage_off.size(), cudaMemcpyHostToDevice));
+  return BSAMG_OK;
+}
+
+int commit(Hier& H) {
+  if (H.committed) return BSAMG_ERR_ARG;
+  RET(set_device(H));
+  int root = -1;
+  H.minlevel = 0;
+  H.maxlevel = 0;
+  for (size_t n = 0; n < H.patches.size(); n++) {
+    HostPatch& P = H.patches[n];
+    if (P.level == 0 && root < 0) root = (int)n;
+    H.minlevel = std::min(H.minlevel, P.level);
+    H.maxlevel = std::max(H.maxlevel, P.level);
+  }
+  if (root < 0) return BSAMG_ERR_ARG;
+  for (HostPatch& P : H.patches) {
+    if (P.parent_id >= 0) {
+      auto it = H.id2idx.find(P.parent_id);
+      if (it == H.id2idx.end()) return BSAMG_ERR_NOT_FOUND;
+      if (H.patches[it->second].level != P.level - 1) return BSAMG_ERR_ARG;
+      P.parent = it->second;
+    }
+    if (P.level > H.minlevel && P.parent < 0) return BSAMG_ERR_ARG;
+    for (int d = 0; d < H.ndims; d++)  // RootInit's check, bsamroutines.f90:361-366
+      if (P.mglobal[d][1] - P.mglobal[d][0] + 1 != P.mx[d]) return BSAMG_ERR_ARG;
+    for (int f = 0; f < 2 * H.ndims; f++)
+      if (P.mthbc[f] != 2 && P.mthbc[f] != 10 && P.mthbc[f] != kInternalBC) return BSAMG_ERR_UNSUPPORTED;
+    for (int d = 0; d < 3; d++) {
+      bool u = d < H.ndims;
+      P.cmx[d] = (u && P.mx[d] % 2 == 0) ? P.mx[d] / 2 : 1;
+      P.qn[d] = u ? P.mx[d] + 2 * H.mbc : 1;
+      P.cn[d] = u ? P.cmx[d] + 2 * H.mbc : 1;
+    }
+    if (P.parent >= 0) {
+      for (int d = 0; d < H.ndims; d++) {
+        if (P.mx[d] % 2) return BSAMG_ERR_ARG;
+        const HostPatch& Q = H.patches[P.parent];
+        if (P.mbounds[d][0] < 1 || P.mbounds[d][1] > Q.mx[d] || P.mbounds[d][1] - P.mbounds[d][0] + 1 != P.cmx[d])
+          return BSAMG_ERR_ARG;
+      }
+    }
+    if (H.ndims == 2 && P.level > 0 && P.parent >= 0 && (P.mx[0] < 4 || P.mx[1] < 4))
+      return BSAMG_ERR_UNSUPPORTED;  // Interpolate2D reads cells 1..2 from each side
+  }
+  // level lists in insertion (visiting) order
+  for (size_t n = 0; n < H.patches.size(); n++) H.L(H.patches[n].level).patches.push_back((int)n);
+  const HostPatch& R = H.patches[root];
+  for (int l = 0; l <= kMaxDepth; l++)
+    for (int d = 0; d < 3; d++) H.mxmax[l][d] = d < H.ndims ? (R.mx[d] << l) : 1;
+  periodic_setup(H, R.mthbc);
+
+  // pool layout: [q...][qold...][qc...][f...][rf...][ftmp...]
+  long long off = 0;
+  for (HostPatch& P : H.patches) {
+    P.sq = (long long)P.qn[0] * P.qn[1] * P.qn[2];
+    P.sc = (long long)P.cn[0] * P.cn[1] * P.cn[2];
+    P.sf = (long long)P.mx[0] * P.mx[1] * P.mx[2];
+  }
+  H.q_region = off;
+  for (HostPatch& P : H.patches) { P.oq = off; off = align32(off + P.sq * H.nrvars); }
+  H.q_len = off - H.q_region;
+  H.qold_region = off;
+  for (HostPatch& P : H.patches) P.oqold = P.oq + H.qold_region - H.q_region;
+  off += H.q_len;
+  for (HostPatch& P : H.patches) { P.oqc = off; off = align32(off + P.sc * H.nrvars); }
+  for (HostPatch& P : H.patches) { P.of = off; off = align32(off + P.sf * H.nrvars); }
+  for (HostPatch& P : H.patches) { P.orf = off; off = align32(off + P.sf * H.nrvars); }
+  for (HostPatch& P : H.patches) { P.oftmp = off; off = align32(off + P.sf * H.nrvars); }
+  H.pool_elems = (size_t)off;
+  size_t need = H.pool_elems * sizeof(double) + mixed_pool_bytes(H);
+  {
+    std::lock_guard<std::mutex> lk(H.ctx->mu);
+    if (H.ctx->budget && H.ctx->used + need > H.ctx->budget) return BSAMG_ERR_BUDGET;
+    H.ctx->used += need;
+  }
+  H.bytes += need;
+  CK(cudaStreamCreateWithFlags(&H.s, cudaStreamNonBlocking));
+  CK(cudaMalloc(&H.pool, H.pool_elems * sizeof(double)));
+  CK(cudaMemsetAsync(H.pool, 0, H.pool_elems * sizeof(double), H.s));
+  RET(mixed_alloc(H));
+
+  std::vector<PatchDev> pd(H.patches.size());
+  for (size_t n = 0; n < H.patches.size(); n++) {
+    const HostPatch& P = H.patches[n];
+    PatchDev& D = pd[n];
+    memset(&D, 0, sizeof(D));
+    for (int d = 0; d < 3; d++) {
+      D.mx[d] = P.mx[d];
+      D.qn[d] = P.qn[d];
+      D.cmx[d] = P.cmx[d];
+      D.cn[d] = P.cn[d];
+      D.mb[d] = P.mbounds[d][0];
+    }
+    D.parent = P.parent;
+    D.level = P.level;
+    D.oq = P.oq; D.oqold = P.oqold; D.oqc = P.oqc; D.of = P.of; D.orf = P.orf; D.oftmp = P.oftmp;
+    D.sq = P.sq; D.sc = P.sc; D.sf = P.sf;
+    D.h = P.dx[0];
+    coefficients(H, P.dx[0], D.c);
+  }
+  CK(cudaMalloc(&H.dP, sizeof(PatchDev) * pd.size()));
+  CK(cudaMemcpy(H.dP, pd.data(), sizeof(PatchDev) * pd.size(), cudaMemcpyHostToDevice));
+  H.bytes += sizeof(PatchDev) * pd.size();
+
+  int maxblk = 1;
+  for (int l = H.minlevel; l <= H.maxlevel; l++) {
+    LevelT& L = H.L(l);
+    for (int k = 0; k < kNKind; k++) RET(upload_blocks(H, L, k));
+    maxblk = std::max(maxblk, L.nblk[kKindInterior]);
+    L.count = 0.0;
+    for (int p : L.patches) {
+      const HostPatch& P = H.patches[p];
+      L.count = (double)(H.nrvars * P.mx[0] * P.mx[1] * P.mx[2]) + L.count;
+    }
+    for (int ip = 0; ip < 3; ip++) {
+      // below and at the root the program does not depend on the colour
+      if (l <= 0 && ip > 0) {
+        L.gp[ip].ops = L.gp[0].ops;
+        L.gp[ip].stage_off = L.gp[0].stage_off;
+        L.gp[ip].d_ops = L.gp[0].d_ops;
+        L.gp[ip].d_stage_off = L.gp[0].d_stage_off;
+        continue;
+      }
+      L.gp[ip].ops = compile_set_ghost(H, l, ip, L.gp[ip].stage_off);
+      RET(upload_ghost(H, L.gp[ip]));
+    }
+  }
+  H.partial_cap = maxblk;
+  CK(cudaMalloc(&H.d_partial, sizeof(double) * 2 * (size_t)maxblk * std::max(1, H.nrvars)));
+  CK(cudaMalloc(&H.d_norm, sizeof(double) * 8));
+  CK(cudaMalloc(&H.d_nonfinite, sizeof(int) * 4));
+  CK(cudaMallocHost(&H.h_norm, sizeof(double) * 8));
+  CK(cudaMallocHost(&H.h_nonfinite, sizeof(int) * 4));
+  CK(cudaStreamSynchronize(H.s));
+  H.committed = true;
+  return BSAMG_OK;
+}
+
+void release(Hier& H) {
+  cudaSetDevice(H.ctx->device);
+  if (H.s) cudaStreamSynchronize(H.s);
+  for (auto& kv : H.graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  H.graphs.clear();
+  for (int l = 0; l < kNLev; l++) {
+    LevelT& L = H.lev[l];
+    for (int k = 0; k < kNKind; k++) cudaFree(L.d_blk[k]);
+    for (int ip = 0; ip < 3; ip++) {
+      bool shared = ip > 0 && L.gp[ip].d_ops == L.gp[0].d_ops;
+      if (!shared) {
+        cudaFree(L.gp[ip].d_ops);
+        cudaFree(L.gp[ip].d_stage_off);
+      }
+    }
+  }
+  mixed_free(H);
+  cudaFree(H.dP);
+  cudaFree(H.pool);
+  cudaFree(H.d_partial);
+  cudaFree(H.d_norm);
+  cudaFree(H.d_nonfinite);
+  if (H.h_norm) cudaFreeHost(H.h_norm);
+  if (H.h_nonfinite) cudaFreeHost(H.h_nonfinite);
+  if (H.s) cudaStreamDestroy(H.s);
+  if (H.committed) {
+    std::lock_guard<std::mutex> lk(H.ctx->mu);
+    size_t need = H.pool_elems * sizeof(double) + mixed_pool_bytes(H);
+    H.ctx->used -= std::min(H.ctx->used, need);
+  }
+}
+
+HostPatch* find(Hier& H, int id) {
+  auto it = H.id2idx.find(id);
+  return it == H.id2idx.end() ? nullptr : &H.patches[it->second];
+}
+
+double* field_ptr(Hier& H, HostPatch& P, int field, size_t* n) {
+  switch (field) {
+    case BSAMG_FIELD_Q: *n = P.sq * H.nrvars; return H.pool + P.oq;
+    case BSAMG_FIELD_QOLD: *n = P.sq * H.nrvars; return H.pool + P.oqold;
+    case BSAMG_FIELD_QC: *n = P.sc * H.nrvars; return H.pool + P.oqc;
+    case BSAMG_FIELD_F: *n = P.sf * H.nrvars; return H.pool + P.of;
+    case BSAMG_FIELD_RF: *n = P.sf * H.nrvars; return H.pool + P.orf;
+    case BSAMG_FIELD_FTMP: *n = P.sf * H.nrvars; return H.pool + P.oftmp;
+  }
+  *n = 0;
+  return nullptr;
+}
+
+bool level_ok(const Hier& H, int level) { return level >= H.minlevel && level <= H.maxlevel; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+int bsamg_init(int device, size_t hbm_budget_bytes, bsamg_ctx** out) {
+  if (!out) return BSAMG_ERR_ARG;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+  if (device < 0 || device >= n) return BSAMG_ERR_ARG;
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  bsamg_ctx* c = new (std::nothrow) bsamg_ctx();
+  if (!c) return BSAMG_ERR_ARG;
+  c->device = device;
+  c->budget = hbm_budget_bytes;
+  *out = c;
+  return BSAMG_OK;
+}
+
+int bsamg_finalize(bsamg_ctx* ctx) {
+  delete ctx;
+  return BSAMG_OK;
+}
+
+int bsamg_ctx_usage(const bsamg_ctx* ctx, size_t* used, size_t* budget) {
+  if (!ctx) return BSAMG_ERR_ARG;
+  if (used) *used = ctx->used;
+  if (budget) *budget = ctx->budget;
+  return BSAMG_OK;
+}
+
+int bsamg_hier_create(bsamg_ctx* ctx, int ndims, int nrvars, int mbc, int problem_kind, const double* params,
+                      int nparams, const double* qpo, bsamg_hier** out) {
+  if (!ctx || !out || !params) return BSAMG_ERR_ARG;
+  if (ndims < 2 || ndims > 3) return BSAMG_ERR_ARG;
+  if (mbc != 1) return BSAMG_ERR_UNSUPPORTED;
+  if (problem_kind != BSAMG_PROBLEM_CH && problem_kind != BSAMG_PROBLEM_BIOGROWTH) return BSAMG_ERR_ARG;
+  if (nrvars != 2) return BSAMG_ERR_UNSUPPORTED;  // both plugins carry two variables
+  if (nparams < 2 || (problem_kind == BSAMG_PROBLEM_BIOGROWTH && nparams < 5)) return BSAMG_ERR_ARG;
+  bsamg_hier* h = new (std::nothrow) bsamg_hier();
+  if (!h) return BSAMG_ERR_ARG;
+  h->ctx = ctx;
+  h->ndims = ndims;
+  h->nrvars = nrvars;
+  h->mbc = mbc;
+  h->problem = problem_kind;
+  h->pp.dt = params[0];
+  h->pp.eps2 = params[1] * params[1];  // SetProb, CH/problem.f90:32
+  h->pp.gamma = nparams > 2 ? params[2] : 0.0;
+  h->pp.lambda = nparams > 3 ? params[3] : 0.0;
+  h->pp.czero = nparams > 4 ? params[4] : 0.0;
+  for (int v = 0; v < kMaxVars; v++) h->pp.qpo[v] = (qpo && v < nrvars) ? qpo[v] : 0.0;
+  h->pp.nrvars = nrvars;
+  h->pp.problem = problem_kind;
+  *out = h;
+  return BSAMG_OK;
+}
+
+int bsamg_hier_destroy(bsamg_hier* h) {
+  if (!h) return BSAMG_OK;
+  release(*h);
+  delete h;
+  return BSAMG_OK;
+}
+
+int bsamg_patch_add(bsamg_hier* h, int level, int id, int parent_id, const int mx[3], const int mglobal[6],
+                    const int mbounds[6], const int mthbc[6], const double dx[3], const double xlower[3]) {
+  if (!h || !mx || !mglobal || !mbounds || !mthbc || !dx || !xlower) return BSAMG_ERR_ARG;
+  return add_patch(*h, level, id, parent_id, mx, mglobal, mbounds, mthbc, dx, xlower);
+}
+
+int bsamg_build_uniform(bsamg_hier* h, const int mx[3], int minlevel, const int mthbc[6], const double xlower[3],
+                        const double xupper[3]) {
+  if (!h || !mx || !mthbc || !xlower || !xupper) return BSAMG_ERR_ARG;
+  return build_uniform(*h, mx, minlevel, mthbc, xlower, xupper);
+}
+
+int bsamg_commit(bsamg_hier* h) {
+  if (!h) return BSAMG_ERR_ARG;
+  return commit(*h);
+}
+
+int bsamg_num_patches(const bsamg_hier* h, int* n) {
+  if (!h || !n) return BSAMG_ERR_ARG;
+  *n = (int)h->patches.size();
+  return BSAMG_OK;
+}
+
+size_t bsamg_field_size(const bsamg_hier* h, int id, int field) {
+  if (!h || !h->committed) return 0;
+  bsamg_hier* hh = const_cast<bsamg_hier*>(h);
+  HostPatch* P = find(*hh, id);
+  if (!P) return 0;
+  size_t n;
+  field_ptr(*hh, *P, field, &n);
+  return n;
+}
+
+int bsamg_put_field(bsamg_hier* h, int id, int field, const double* a, size_t n) {
+  if (!h || !h->committed || !a) return BSAMG_ERR_ARG;
+  HostPatch* P = find(*h, id);
+  if (!P) return BSAMG_ERR_NOT_FOUND;
+  size_t nn;
+  double* d = field_ptr(*h, *P, field, &nn);
+  if (!d || nn != n) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  CK(cudaMemcpyAsync(d, a, n * sizeof(double), cudaMemcpyHostToDevice, h->s));
+  CK(cudaStreamSynchronize(h->s));
+  return BSAMG_OK;
+}
+
+int bsamg_get_field(bsamg_hier* h, int id, int field, double* a, size_t n) {
+  if (!h || !h->committed || !a) return BSAMG_ERR_ARG;
+  HostPatch* P = find(*h, id);
+  if (!P) return BSAMG_ERR_NOT_FOUND;
+  size_t nn;
+  double* d = field_ptr(*h, *P, field, &nn);
+  if (!d || nn != n) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  CK(cudaMemcpyAsync(a, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+  CK(cudaStreamSynchronize(h->s));
+  return BSAMG_OK;
+}
+
+int bsamg_relax_level_color(bsamg_hier* h, int level, int ipass) {
+  if (!h || !h->committed || !level_ok(*h, level) || (ipass != 1 && ipass != 2)) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  return enq_relax(*h, level, ipass);
+}
+
+int bsamg_set_ghost(bsamg_hier* h, int level, int ipass) {
+  if (!h || !h->committed || !level_ok(*h, level) || ipass < 0 || ipass > 2) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  return enq_set_ghost(*h, level, ipass);
+}
+
+int bsamg_level_relax(bsamg_hier* h, int level, int nsmooth) {
+  if (!h || !h->committed || !level_ok(*h, level) || nsmooth < 0) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  return enq_level_relax(*h, level, nsmooth);
+}
+
+int bsamg_fill_down(bsamg_hier* h, int field, int finestlevel, int minlevel) {
+  if (!h || !h->committed || (field != 1 && field != 2)) return BSAMG_ERR_ARG;
+  if (!level_ok(*h, finestlevel) || !level_ok(*h, minlevel)) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  return enq_fill_down(*h, field, finestlevel, minlevel);
+}
+
+int bsamg_copy_q_to_qold(bsamg_hier* h, int minlevel, int finestlevel) {
+  if (!h || !h->committed) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  return enq_copy_q_to_qold(*h, minlevel, finestlevel);
+}
+
+int bsamg_vcycle(bsamg_hier* h, int level, int minlevel, int nsmooth) {
+  if (!h || !h->committed || !level_ok(*h, level) || !level_ok(*h, minlevel) || minlevel > level)
+    return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  return enq_vcycle(*h, level, minlevel, nsmooth);
+}
+
+int bsamg_residual_norm(bsamg_hier* h, int level, int errortype, double* out) {
+  if (!h || !h->committed || !level_ok(*h, level) || !out || (errortype != 1 && errortype != 2))
+    return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  RET(enq_norm(*h, level, errortype));
+  CK(cudaMemcpyAsync(h->h_norm, h->d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+  CK(cudaStreamSynchronize(h->s));
+  *out = h->h_norm[0];
+  return BSAMG_OK;
+}
+
+int bsamg_multigrid_iterations(bsamg_hier* h, int finestlevel, int minlevel, int nsmooth, int maxvcycles,
+                               double qerrortol, int updateauxfreq, int errortype, int mode, int strict,
+                               int* ncycles, double* residuals) {
+  if (!h || !h->committed) return BSAMG_ERR_ARG;
+  (void)updateauxfreq;  // both plugins have maux = 0: UpdateAuxInVcycle returns at :417
+  return multigrid_iterations(*h, finestlevel, minlevel, nsmooth, maxvcycles, qerrortol, errortype, mode, strict,
+                              ncycles, residuals);
+}
+
+int bsamg_time_step(bsamg_hier* h, int first, int finestlevel, int minlevel, int nsmooth, int maxvcycles,
+                    double qerrortol, int updateauxfreq, int errortype, int mode, int strict, int* ncycles,
+                    double* residuals) {
+  if (!h || !h->committed) return BSAMG_ERR_ARG;
+  if (!level_ok(*h, finestlevel) || !level_ok(*h, minlevel)) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  for (int level = 0; level <= finestlevel; level++) RET(enq_set_ghost(*h, level, 0));
+  if (first) RET(enq_fill_down(*h, 2, finestlevel, minlevel));
+  RET(enq_copy_q_to_qold(*h, minlevel, finestlevel));
+  (void)updateauxfreq;
+  return multigrid_iterations(*h, finestlevel, minlevel, nsmooth, maxvcycles, qerrortol, errortype, mode, strict,
+                              ncycles, residuals);
+}
+
+int bsamg_sync(bsamg_hier* h) {
+  if (!h || !h->s) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  CK(cudaStreamSynchronize(h->s));
+  return BSAMG_OK;
+}
+
+int bsamg_stream(bsamg_hier* h, void** stream) {
+  if (!h || !stream || !h->committed) return BSAMG_ERR_ARG;
+  *stream = (void*)h->s;
+  return BSAMG_OK;
+}
+
+int bsamg_launch_count(const bsamg_hier* h, long long* n) {
+  if (!h || !n) return BSAMG_ERR_ARG;
+  *n = h->launches;
+  return BSAMG_OK;
+}
+
+const char* bsamg_strerror(int status) {
+  switch (status) {
+    case BSAMG_OK: return "ok";
+    case BSAMG_ERR_ARG: return "bad argument or call order";
+    case BSAMG_ERR_CUDA: return "CUDA runtime error";
+    case BSAMG_ERR_BUDGET: return "allocation exceeds the context HBM budget";
+    case BSAMG_ERR_NOT_CONVERGED: return "maxvcycles reached above qerrortol";
+    case BSAMG_ERR_NONFINITE: return "residual norm is not finite";
+    case BSAMG_ERR_UNSUPPORTED: return "configuration not supported";
+    case BSAMG_ERR_NOT_FOUND: return "unknown patch id";
+  }
+  return "unknown status";
+}
+
+const char* bsamg_last_error_detail(void) { return g_detail.c_str(); }
+
+}  // extern "C"

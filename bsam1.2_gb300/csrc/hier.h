@@ -1,0 +1,108 @@
+// Host-side hierarchy state of libbsamg (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/bsamg.h"
+#include "internal.h"
+#include "launch.h"
+
+namespace bsamg {
+
+struct HostPatch {
+  int level, id, parent_id, parent;
+  int mx[3], mglobal[3][2], mbounds[3][2], mthbc[6];
+  double dx[3], xlower[3];
+  int cmx[3], qn[3], cn[3];
+  long long oq, oqold, oqc, of, orf, oftmp;
+  long long sq, sc, sf;
+  // mixed-path FP32 offsets (into the float pool)
+  long long e_oq, e_oqc, e_of, e_orf, e_ophi;
+};
+
+// A compiled SetGhost(level, ipass): operations sorted by stage.
+struct GhostProg {
+  std::vector<GhostOp> ops;
+  std::vector<int> stage_off;  // size nstages+1
+  GhostOp* d_ops = nullptr;
+  int* d_stage_off = nullptr;
+};
+
+struct LevelT {
+  std::vector<int> patches;  // visiting order
+  Blk* d_blk[kNKind] = {};
+  int nblk[kNKind] = {};
+  GhostProg gp[3];           // ipass 0, 1, 2
+  double count = 0.0;        // nrvars * cells (ErrorAFAS denominator)
+};
+
+struct Hier;
+// Inputs of the ghost compiler.
+std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std::vector<int>& stage_off);
+
+struct Hier {
+  bsamg_ctx* ctx = nullptr;
+  int ndims = 2, nrvars = 2, mbc = 1, problem = 1;
+  ProbParams pp{};
+  std::vector<HostPatch> patches;
+  std::unordered_map<int, int> id2idx;
+  bool committed = false;
+  int minlevel = 0, maxlevel = 0;
+  int periodic = 0, nperoff = 0, peroffidx[13] = {};
+  int mxmax[kMaxDepth + 1][3] = {};
+
+  PatchDev* dP = nullptr;
+  double* pool = nullptr;
+  size_t pool_elems = 0;
+  long long q_region = 0, q_len = 0, qold_region = 0;
+  float* fpool = nullptr;
+  size_t fpool_elems = 0;
+  size_t bytes = 0;
+
+  LevelT lev[kNLev];
+  cudaStream_t s = nullptr;
+  double* d_partial = nullptr;
+  int partial_cap = 0;
+  double* d_norm = nullptr;      // [0] norm, [1] raw sum, plus scratch
+  int* d_nonfinite = nullptr;
+  double* h_norm = nullptr;      // pinned
+  int* h_nonfinite = nullptr;    // pinned
+  long long launches = 0;
+  bool capturing = false;
+  long long capture_launches = 0;
+
+  struct GraphRec {
+    cudaGraphExec_t exec = nullptr;
+    long long nlaunch = 0;
+  };
+  std::map<std::tuple<int, int, int, int, int>, GraphRec> graphs;
+
+  LevelT& L(int level) { return lev[level + kMaxDepth]; }
+  const LevelT& L(int level) const { return lev[level + kMaxDepth]; }
+  LaunchCtx lc() const {
+    LaunchCtx c;
+    c.P = dP;
+    c.pool = pool;
+    c.fpool = fpool;
+    c.s = s;
+    c.pp = pp;
+    c.ndims = ndims;
+    return c;
+  }
+};
+
+}  // namespace bsamg
+
+struct bsamg_ctx {
+  int device = 0;
+  size_t budget = 0;
+  size_t used = 0;
+  std::mutex mu;
+};
+
+struct bsamg_hier : bsamg::Hier {};

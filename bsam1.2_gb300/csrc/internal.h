@@ -1,0 +1,79 @@
+// Internal types shared by the host side and the kernels of libbsamg.
+//
+// Device data model (replaces the pointer-linked nodeinfo records of
+// LIBRARY/nodeinfodef.f90:118-220 and the per-node ALLOCATEs of
+// LIBRARY/bsamstorage.f90:54-144): every field of every patch lives in one
+// pooled allocation, addressed by element offsets held in a flat PatchDev
+// table.  Each field keeps the reference's Fortran layout, so a whole node
+// array moves between host and device with one copy.  All q arrays of a
+// hierarchy are contiguous and followed by all qold arrays in the same order,
+// so CopyQToQold is a single device-to-device copy.
+#pragma once
+#include <cstdint>
+
+namespace bsamg {
+
+constexpr int kMaxDepth = 10;            // nodeinfodef.f90:62
+constexpr int kNLev = 2 * kMaxDepth + 1; // levels -10..10
+constexpr int kInternalBC = 999;         // nodeinfodef.f90:59
+constexpr int kMaxVars = 10;             // nodeinfodef.f90:64
+constexpr int kBlock = 256;              // threads per block of the cell kernels
+
+enum Problem : int { kCH = 1, kBio = 2 };
+
+struct PatchDev {
+  int mx[3];   // interior extents (1 for the unused dimension in 2D)
+  int qn[3];   // ghosted extents of q/qold (1 for the unused dimension)
+  int cmx[3];  // coarse extents (mx/2, or 1)
+  int cn[3];   // ghosted extents of qc
+  int mb[3];   // lower mbounds in the parent (1-based)
+  int parent;  // index into the patch table, -1 if none
+  int level;
+  int pad;
+  long long oq, oqold, oqc, of, orf, oftmp;  // element offsets into the pool
+  long long sq, sc, sf;                      // elements per variable plane
+  // Plugin coefficients for this patch's spacing, computed on the host with
+  // the reference's expressions (CH/problem.f90:339-347, :411-413,
+  // BioGrowth/problem.f90:276-278, :333-336):
+  //   CH : c0 = dt/h^2, c1 = eps^2/h^2, c2 = (4|6)*eps^2/h^2, c3 = (4|6)*c0
+  //   Bio: c0 = dt*eps^2/h^2, c1 = 1/h^2, c2 = 4*c0 + 1, c3 = 4*c1
+  double c[4];
+  double h;
+};
+
+// One block of a level's work list: block covers units [start, start+kBlock)
+// of patch `patch`.
+struct Blk {
+  int patch;
+  int start;
+};
+
+// Ghost program operations (see ghost.cu).
+enum GhostType : int {
+  kGCopy = 0,     // dst = src
+  kGCopyAdd = 1,  // dst = src + qpo[v]
+  kGCopySub = 2,  // dst = src - qpo[v]
+  kGBC = 3,       // dst = (mask bit v) ? 2 - src : src
+  kGCfA = 4,      // a1*s0 + a2*s1 + a3*c0
+  kGCfAB = 5,     // a1*s0 + a2*s1 + a3*(b1*c0 + b2*c1 + b3*c2)
+  kGCfAC = 6,     // a1*s0 + a2*s1 + a3*(c1*c0 + c2*c1 + c3*c2 + c4*c3)
+};
+
+struct GhostOp {
+  int type;
+  int dp;     // destination patch index
+  int dcell;  // destination cell offset within a q plane of dp
+  int sp;     // source patch for copies, parent patch for CF ops
+  int s0, s1; // source cells (copies: in sp; CF: fine cells in dp)
+  int c0, c1, c2, c3;  // coarse cells in sp (CF ops)
+  int mask;   // BC: Dirichlet-variable mask
+};
+
+struct ProbParams {
+  double dt, eps2, gamma, lambda, czero;
+  double qpo[kMaxVars];
+  int nrvars;
+  int problem;
+};
+
+}  // namespace bsamg

@@ -1,0 +1,52 @@
+// Launchers of the device kernels (one function per kernel family).  Every
+// launcher enqueues on the given stream and returns the number of kernel
+// launches it issued; the caller checks cudaGetLastError().
+#pragma once
+#include <cuda_runtime.h>
+
+#include "internal.h"
+
+namespace bsamg {
+
+struct LaunchCtx {
+  const PatchDev* P;  // device patch table
+  double* pool;       // device FP64 pool
+  float* fpool;       // device FP32 pool (mixed path), may be null
+  cudaStream_t s;
+  ProbParams pp;
+  int ndims;
+};
+
+// work-list kinds: what one unit of a level's block list is
+enum Kind : int {
+  kKindColor = 0,     // one slot of a colour row: ceil(mx1/2) * mx2 * mx3
+  kKindInterior = 1,  // one interior cell: mx1*mx2*mx3
+  kKindCoarse = 2,    // one coarse cell under a child: cmx1*cmx2*cmx3
+  kKindCGhost = 3,    // one ghosted coarse cell: (cmx+2)^d
+  kKindFGhost = 4,    // one ghosted fine cell: (mx+2)^d
+  kNKind = 5
+};
+
+// ---- plain FP64 path (fp64.cu, built with --fmad=false) ----
+int launch_relax(const LaunchCtx& c, const Blk* blk, int nblk, int ipass);
+int launch_restrict_q(const LaunchCtx& c, const Blk* blk, int nblk);
+int launch_coarse_ghost(const LaunchCtx& c, const Blk* blk, int nblk);
+int launch_coarse_load(const LaunchCtx& c, const Blk* blk, int nblk);
+int launch_correct_a(const LaunchCtx& c, const Blk* blk, int nblk);
+int launch_correct_b(const LaunchCtx& c, const Blk* blk, int nblk);
+int launch_fill_down(const LaunchCtx& c, const Blk* blk, int nblk, int field);
+int launch_get_source(const LaunchCtx& c, const Blk* blk, int nblk);
+int launch_update_source(const LaunchCtx& c, const Blk* blk, int nblk);
+// per-block partial sums of rf^2 (nrvars per block) -> partial[nblk*nrvars]
+int launch_norm_partial(const LaunchCtx& c, const Blk* blk, int nblk,
+                        double* partial, int store_rf);
+// deterministic final sum; writes out[0] = norm, out[1] = raw sum,
+// and ok[0] = 0 when the norm is finite, 1 otherwise
+int launch_norm_finish(cudaStream_t s, const double* partial, int nblk,
+                       int nrvars, double count, int errortype, double* out,
+                       int* nonfinite);
+int launch_ghost_stage(const LaunchCtx& c, const GhostOp* ops, int n);
+int launch_ghost_program_1cta(const LaunchCtx& c, const GhostOp* ops,
+                              const int* stage_off, int nstages);
+
+}  // namespace bsamg

@@ -1,0 +1,155 @@
+/*
+ * bsamg -- GB300 (sm_103a) FAS multigrid V-cycle for BSAM 1.2 patch
+ * hierarchies.  C ABI: plain ints, doubles, pointers and sizes; no C++ or
+ * torch types.  Every function returns an int status: 0 = OK, negative =
+ * error (see bsamg_strerror).  Nothing in the library aborts, traps or
+ * prints; a device-side failure is reported through the status of the call
+ * that observes it.
+ *
+ * The entry points replace the following reference routines (paths within
+ * the BSAM 1.2 project):
+ *
+ *   bsamg_hier_create / bsamg_patch_add / bsamg_commit
+ *       -> LIBRARY/bsamstorage.f90:54-144 (AllocFields) and the patch
+ *          descriptor of LIBRARY/nodeinfodef.f90:118-220; the Fortran host
+ *          calls bsamg_patch_add once per node it visits with ApplyOnLevel
+ *          (LIBRARY/treeops.f90:515-552) after a regrid
+ *          (LIBRARY/bsamroutines.f90:682-702).
+ *   bsamg_build_uniform
+ *       -> RootInit + InitSeed, LIBRARY/bsamroutines.f90:226-510.
+ *   bsamg_put_field / bsamg_get_field
+ *       -> direct access to info%q, info%qold, ... of a node (the Fortran
+ *          arrays are passed whole, ghost layers included).
+ *   bsamg_multigrid_iterations
+ *       -> MultigridIterations, LIBRARY/afasroutines.f90:48-110.
+ *   bsamg_time_step
+ *       -> one pass of the TakeTimeSteps loop body on a fixed mesh,
+ *          LIBRARY/bsamroutines.f90:657-797.
+ *   bsamg_copy_q_to_qold -> CopyQToQold, LIBRARY/bsamroutines.f90:592-605.
+ *   bsamg_fill_down      -> FillDown, LIBRARY/afasroutines.f90:236-254.
+ *   bsamg_vcycle         -> AFASVcycle, LIBRARY/afasroutines.f90:495-529.
+ *   bsamg_level_relax    -> LevelRelax, LIBRARY/afasroutines.f90:532-557.
+ *   bsamg_relax_level_color -> ApplyOnLevel(level, RelaxPatch) for one
+ *          colour, LIBRARY/afasroutines.f90:549-550 / :560-607.
+ *   bsamg_set_ghost      -> SetGhost, LIBRARY/boundary.f90:67-97.
+ *   bsamg_residual_norm  -> ErrorAFAS, LIBRARY/afasroutines.f90:113-160.
+ *
+ * Field layout of put/get: the reference's Fortran layout
+ * (LIBRARY/bsamstorage.f90:81-90, :106-115), column-major, variable index
+ * slowest: q(1-mbc:mx1+mbc, 1-mbc:mx2+mbc, [1-mbc:mx3+mbc | 1:1], 1:nrvars).
+ */
+#ifndef BSAMG_H
+#define BSAMG_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct bsamg_ctx bsamg_ctx;
+typedef struct bsamg_hier bsamg_hier;
+
+/* status codes */
+#define BSAMG_OK 0
+#define BSAMG_ERR_ARG -1         /* bad argument or call order */
+#define BSAMG_ERR_CUDA -2        /* a CUDA runtime call failed */
+#define BSAMG_ERR_BUDGET -3      /* allocation above the context's HBM budget */
+#define BSAMG_ERR_NOT_CONVERGED -4 /* maxvcycles reached above qerrortol (returned only when requested) */
+#define BSAMG_ERR_NONFINITE -5   /* the residual norm is NaN or Inf */
+#define BSAMG_ERR_UNSUPPORTED -6 /* configuration not implemented */
+#define BSAMG_ERR_NOT_FOUND -7   /* unknown patch id */
+
+/* problem kinds: the device form of a PROBLEM/<name> plugin */
+#define BSAMG_PROBLEM_CH 1        /* PROBLEM/CH/problem.f90 */
+#define BSAMG_PROBLEM_BIOGROWTH 2 /* PROBLEM/BioGrowth/problem.f90 */
+
+/* fields of a patch (nodeinfodef.f90:184-214) */
+#define BSAMG_FIELD_Q 0
+#define BSAMG_FIELD_QOLD 1
+#define BSAMG_FIELD_QC 2
+#define BSAMG_FIELD_F 3
+#define BSAMG_FIELD_RF 4
+#define BSAMG_FIELD_FTMP 5
+
+/* arithmetic modes of bsamg_multigrid_iterations */
+#define BSAMG_MODE_FP64 0  /* plain FP64 path: the drop-in, same order as the reference */
+#define BSAMG_MODE_MIXED 1 /* FP32 smoothing/prolongation in an FP64 defect-correction loop */
+
+/* Context: one device, one HBM budget.  hbm_budget_bytes = 0 means no
+ * limit beyond the device's own memory. */
+int bsamg_init(int device, size_t hbm_budget_bytes, bsamg_ctx** out);
+int bsamg_finalize(bsamg_ctx* ctx);
+/* bytes currently allocated by hierarchies of this context */
+int bsamg_ctx_usage(const bsamg_ctx* ctx, size_t* used, size_t* budget);
+
+/* Hierarchy.  params: [0]=dt [1]=eps, then for BIOGROWTH [2]=gamma
+ * [3]=lambda [4]=czero.  qpo: nrvars quasi-periodic offsets (nodeinfodef
+ * qpo), may be NULL.  Only mbc = 1 is supported. */
+int bsamg_hier_create(bsamg_ctx* ctx, int ndims, int nrvars, int mbc,
+                      int problem_kind, const double* params, int nparams,
+                      const double* qpo, bsamg_hier** out);
+int bsamg_hier_destroy(bsamg_hier* h);
+
+/* One patch (node).  Patches of a level are visited in the order they are
+ * added, which the caller makes the reference's ApplyOnLevel order
+ * (youngest first).  mglobal/mbounds are (lo,hi) pairs per dimension;
+ * parent_id = -1 for the coarsest level. */
+int bsamg_patch_add(bsamg_hier* h, int level, int id, int parent_id,
+                    const int mx[3], const int mglobal[6],
+                    const int mbounds[6], const int mthbc[6],
+                    const double dx[3], const double xlower[3]);
+/* Root grid (id 0) plus one grid per level -1..minlevel (id = -level). */
+int bsamg_build_uniform(bsamg_hier* h, const int mx[3], int minlevel,
+                        const int mthbc[6], const double xlower[3],
+                        const double xupper[3]);
+/* Builds tables, allocates the device pool (zero-filled) and the launch
+ * schedule.  No patch may be added afterwards. */
+int bsamg_commit(bsamg_hier* h);
+int bsamg_num_patches(const bsamg_hier* h, int* n);
+size_t bsamg_field_size(const bsamg_hier* h, int id, int field);
+/* synchronous host <-> device copies of a whole field array (n doubles) */
+int bsamg_put_field(bsamg_hier* h, int id, int field, const double* a,
+                    size_t n);
+int bsamg_get_field(bsamg_hier* h, int id, int field, double* a, size_t n);
+
+/* single operations, FP64 */
+int bsamg_relax_level_color(bsamg_hier* h, int level, int ipass);
+int bsamg_set_ghost(bsamg_hier* h, int level, int ipass);
+int bsamg_level_relax(bsamg_hier* h, int level, int nsmooth);
+int bsamg_fill_down(bsamg_hier* h, int field /*1=f, 2=q*/, int finestlevel,
+                    int minlevel);
+int bsamg_copy_q_to_qold(bsamg_hier* h, int minlevel, int finestlevel);
+int bsamg_vcycle(bsamg_hier* h, int level, int minlevel, int nsmooth);
+int bsamg_residual_norm(bsamg_hier* h, int level, int errortype,
+                        double* out);
+
+/* MultigridIterations.  residuals (may be NULL) receives up to maxvcycles
+ * norms; *ncycles the number of V-cycles run.  Reaching maxvcycles without
+ * convergence returns BSAMG_OK, as the reference does, unless
+ * strict != 0, in which case it returns BSAMG_ERR_NOT_CONVERGED. */
+int bsamg_multigrid_iterations(bsamg_hier* h, int finestlevel, int minlevel,
+                               int nsmooth, int maxvcycles, double qerrortol,
+                               int updateauxfreq, int errortype, int mode,
+                               int strict, int* ncycles, double* residuals);
+/* SetGhost(l,0) for l = 0..finest, FillDown(q) if first, CopyQToQold,
+ * MultigridIterations. */
+int bsamg_time_step(bsamg_hier* h, int first, int finestlevel, int minlevel,
+                    int nsmooth, int maxvcycles, double qerrortol,
+                    int updateauxfreq, int errortype, int mode, int strict,
+                    int* ncycles, double* residuals);
+
+/* Wait for all work of the hierarchy; returns the first deferred error. */
+int bsamg_sync(bsamg_hier* h);
+/* CUDA stream the hierarchy launches on (cudaStream_t as void*), for
+ * callers that time or order work around it. */
+int bsamg_stream(bsamg_hier* h, void** stream);
+/* Kernel launches issued by this hierarchy since creation. */
+int bsamg_launch_count(const bsamg_hier* h, long long* n);
+
+const char* bsamg_strerror(int status);
+/* Last CUDA error text seen by the library (thread-local), or "". */
+const char* bsamg_last_error_detail(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

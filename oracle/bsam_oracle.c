@@ -1,0 +1,1246 @@
+/*
+ * CPU oracle: plain-C restatement of the BSAM 1.2 FAS V-cycle.
+ * TEST INFRASTRUCTURE ONLY -- see bsam_oracle.h for scope and parity status.
+ *
+ * Every routine cites the reference routine it restates (file:line, paths
+ * within the reference project).  Evaluation order of each floating-point
+ * expression follows the Fortran source left to right; build with
+ * -ffp-contract=off so that no multiply-add is fused.
+ */
+#include "bsam_oracle.h"
+
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MAXDEPTH 10 /* nodeinfodef.f90:62 */
+#define INTERNALBC 999 /* nodeinfodef.f90:59 */
+#define NLEV (2 * MAXDEPTH + 1)
+
+/* C/F interpolation weights, boundary.f90:54-63 */
+static const double A1 = -01.0 / 05.0;
+static const double A2 = 02.0 / 03.0;
+static const double A3 = 08.0 / 15.0;
+static const double B1 = 05.0 / 32.0;
+static const double B2 = 15.0 / 16.0;
+static const double B3 = -03.0 / 32.0;
+static const double C1 = 09.0 / 16.0;
+static const double C2 = 03.0 / 16.0;
+static const double C3 = 03.0 / 16.0;
+static const double C4 = 01.0 / 16.0;
+
+typedef struct {
+  int level, id, parent_id, parent;
+  int mx[3], mglobal[3][2], mbounds[3][2], mthbc[6];
+  double dx[3], xlower[3];
+  int cmx[3];
+  int qlo[3], qn[3]; /* q, qold: ghosted */
+  int clo[3], cn[3]; /* qc: ghosted, coarse */
+  int fn[3];         /* f, rf, ftmp: interior, lower bound 1 */
+  double *q, *qold, *qc, *f, *rf, *ftmp;
+} OPatch;
+
+struct bsamo_hier {
+  int ndims, nrvars, mbc, problem;
+  double dt, eps, eps2, gamma, lambda, czero;
+  double qpo[10];
+  int np, cap;
+  OPatch* p;
+  int committed;
+  int lev_n[NLEV];
+  int* lev_list[NLEV];
+  int periodic, nperoff, peroffidx[13];
+  int mxmax[MAXDEPTH + 1][3];
+  int minlevel_present, maxlevel_present;
+  double integral[2];
+};
+
+/* ------------------------------------------------------------------ */
+/* indexing                                                            */
+
+static inline size_t iq(const OPatch* p, int i, int j, int k, int v) {
+  return (((size_t)v * p->qn[2] + (size_t)(k - p->qlo[2])) * p->qn[1] +
+          (size_t)(j - p->qlo[1])) * p->qn[0] + (size_t)(i - p->qlo[0]);
+}
+static inline size_t ic(const OPatch* p, int i, int j, int k, int v) {
+  return (((size_t)v * p->cn[2] + (size_t)(k - p->clo[2])) * p->cn[1] +
+          (size_t)(j - p->clo[1])) * p->cn[0] + (size_t)(i - p->clo[0]);
+}
+static inline size_t iff(const OPatch* p, int i, int j, int k, int v) {
+  return (((size_t)v * p->fn[2] + (size_t)(k - 1)) * p->fn[1] +
+          (size_t)(j - 1)) * p->fn[0] + (size_t)(i - 1);
+}
+#define Q(p, i, j, k, v) ((p)->q[iq((p), (i), (j), (k), (v))])
+#define QO(p, i, j, k, v) ((p)->qold[iq((p), (i), (j), (k), (v))])
+#define QC(p, i, j, k, v) ((p)->qc[ic((p), (i), (j), (k), (v))])
+#define FF(p, i, j, k, v) ((p)->f[iff((p), (i), (j), (k), (v))])
+#define RF(p, i, j, k, v) ((p)->rf[iff((p), (i), (j), (k), (v))])
+#define FT(p, i, j, k, v) ((p)->ftmp[iff((p), (i), (j), (k), (v))])
+
+static OPatch* find_patch(const bsamo_hier* h, int id) {
+  for (int n = 0; n < h->np; n++)
+    if (h->p[n].id == id) return &h->p[n];
+  return NULL;
+}
+static OPatch* parent_of(bsamo_hier* h, const OPatch* p) {
+  return p->parent >= 0 ? &h->p[p->parent] : NULL;
+}
+static int nlev(const bsamo_hier* h, int level) {
+  if (level < -MAXDEPTH || level > MAXDEPTH) return 0;
+  return h->lev_n[level + MAXDEPTH];
+}
+static OPatch* lev_patch(bsamo_hier* h, int level, int n) {
+  return &h->p[h->lev_list[level + MAXDEPTH][n]];
+}
+static inline int imod(int a, int b) { int r = a % b; return r < 0 ? r + b : r; }
+
+/* ------------------------------------------------------------------ */
+/* construction                                                        */
+
+int bsamo_create(int ndims, int nrvars, int mbc, int problem,
+                 const double* params, int nparams, const double* qpo,
+                 bsamo_hier** out) {
+  if (!out) return -1;
+  if (ndims < 2 || ndims > 3) return -2;
+  if (nrvars < 1 || nrvars > 10) return -2;
+  if (mbc != 1) return -2; /* mbc = 2 (P2 prolongation) not restated */
+  if (problem != BSAMO_PROBLEM_CH && problem != BSAMO_PROBLEM_BIOGROWTH)
+    return -2;
+  if (nparams < 2) return -2;
+  bsamo_hier* h = (bsamo_hier*)calloc(1, sizeof(*h));
+  h->ndims = ndims;
+  h->nrvars = nrvars;
+  h->mbc = mbc;
+  h->problem = problem;
+  h->dt = params[0];
+  h->eps = params[1];
+  h->eps2 = h->eps * h->eps; /* SetProb, CH/problem.f90:32 */
+  h->gamma = nparams > 2 ? params[2] : 0.0;
+  h->lambda = nparams > 3 ? params[3] : 0.0;
+  h->czero = nparams > 4 ? params[4] : 0.0;
+  for (int v = 0; v < 10; v++) h->qpo[v] = (qpo && v < nrvars) ? qpo[v] : 0.0;
+  *out = h;
+  return 0;
+}
+
+int bsamo_destroy(bsamo_hier* h) {
+  if (!h) return 0;
+  for (int n = 0; n < h->np; n++) {
+    OPatch* p = &h->p[n];
+    free(p->q); free(p->qold); free(p->qc); free(p->f); free(p->rf);
+    free(p->ftmp);
+  }
+  for (int l = 0; l < NLEV; l++) free(h->lev_list[l]);
+  free(h->p);
+  free(h);
+  return 0;
+}
+
+int bsamo_patch_add(bsamo_hier* h, int level, int id, int parent_id,
+                    const int mx[3], const int mglobal[6],
+                    const int mbounds[6], const int mthbc[6],
+                    const double dx[3], const double xlower[3]) {
+  if (!h || h->committed) return -1;
+  if (level < -MAXDEPTH || level > MAXDEPTH) return -2;
+  if (find_patch(h, id)) return -2;
+  if (h->np == h->cap) {
+    h->cap = h->cap ? 2 * h->cap : 16;
+    h->p = (OPatch*)realloc(h->p, sizeof(OPatch) * h->cap);
+  }
+  OPatch* p = &h->p[h->np++];
+  memset(p, 0, sizeof(*p));
+  p->level = level;
+  p->id = id;
+  p->parent_id = parent_id;
+  p->parent = -1;
+  for (int d = 0; d < 3; d++) {
+    p->mx[d] = d < h->ndims ? mx[d] : 1;
+    p->mglobal[d][0] = d < h->ndims ? mglobal[2 * d] : 1;
+    p->mglobal[d][1] = d < h->ndims ? mglobal[2 * d + 1] : 1;
+    p->mbounds[d][0] = d < h->ndims ? mbounds[2 * d] : 1;
+    p->mbounds[d][1] = d < h->ndims ? mbounds[2 * d + 1] : 1;
+    p->dx[d] = d < h->ndims ? dx[d] : 0.0;
+    p->xlower[d] = d < h->ndims ? xlower[d] : 0.0;
+  }
+  for (int f = 0; f < 6; f++) p->mthbc[f] = f < 2 * h->ndims ? mthbc[f] : 10;
+  return 0;
+}
+
+/* RootInit (bsamroutines.f90:226-440) and InitSeed (:443-510).  Patch ids:
+ * root = 0, level l < 0 has id = -l. */
+int bsamo_build_uniform(bsamo_hier* h, const int mx[3], int minlevel,
+                        const int mthbc[6], const double xlower[3],
+                        const double xupper[3]) {
+  if (!h || h->committed || h->np) return -1;
+  int nd = h->ndims;
+  int cmx[3] = {1, 1, 1}, mg[6] = {1, 1, 1, 1, 1, 1}, mb[6] = {1, 1, 1, 1, 1, 1};
+  double dx[3] = {0, 0, 0}, xl[3] = {0, 0, 0};
+  for (int d = 0; d < nd; d++) {
+    if (mx[d] <= 0 || mx[d] % 2) return -2; /* :345-359 */
+    cmx[d] = mx[d];
+    mg[2 * d + 1] = mx[d];
+    dx[d] = (xupper[d] - xlower[d]) / (double)mx[d]; /* :388 */
+    xl[d] = xlower[d];
+  }
+  for (int d = 1; d < nd; d++)
+    if (fabs(dx[0] - dx[d]) > 1.0e-10) return -2; /* :390-395 */
+  /* root mbounds are set to (1, mx/2) by InitSeed of level -1 (:482) */
+  for (int d = 0; d < nd; d++) {
+    mb[2 * d] = 1;
+    mb[2 * d + 1] = minlevel < 0 ? mx[d] / 2 : mx[d];
+  }
+  int rc = bsamo_patch_add(h, 0, 0, minlevel < 0 ? 1 : -1, cmx, mg, mb, mthbc,
+                           dx, xl);
+  if (rc) return rc;
+  for (int l = -1; l >= minlevel; l--) {
+    int nmx[3] = {1, 1, 1}, nmg[6] = {1, 1, 1, 1, 1, 1}, nmb[6] = {1, 1, 1, 1, 1, 1};
+    double ndx[3] = {0, 0, 0};
+    for (int d = 0; d < nd; d++) {
+      if (cmx[d] % 2) return -3; /* :472-475 */
+      nmx[d] = cmx[d] / 2;
+      ndx[d] = dx[d] * 2.0; /* :478 */
+      nmg[2 * d] = 1;
+      nmg[2 * d + 1] = mg[2 * d + 1] / 2; /* :480 */
+      nmb[2 * d] = 1;
+      nmb[2 * d + 1] = l > minlevel ? nmx[d] / 2 : nmx[d];
+      if (nmx[d] != nmg[2 * d + 1]) return -3; /* :486 */
+    }
+    rc = bsamo_patch_add(h, l, -l, l > minlevel ? -l + 1 : -1, nmx, nmg, nmb,
+                         mthbc, ndx, xl);
+    if (rc) return rc;
+    memcpy(cmx, nmx, sizeof(cmx));
+    memcpy(mg, nmg, sizeof(mg));
+    memcpy(dx, ndx, sizeof(dx));
+  }
+  return 0;
+}
+
+/* PeriodicSetup, boundary.f90:805-872 */
+static void periodic_setup(bsamo_hier* h, const int mthbc_in[6]) {
+  int m[6];
+  for (int f = 0; f < 6; f++) m[f] = 10;
+  for (int f = 0; f < 2 * h->ndims; f++) m[f] = mthbc_in[f];
+  static const int i13[13] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13};
+  static const int i1245[4] = {1, 2, 4, 5};
+  static const int i1389[4] = {1, 3, 8, 9};
+  static const int i2367[4] = {2, 3, 6, 7};
+  h->periodic = 1;
+  const int* src = NULL;
+  int n = 0;
+  if (m[0] == 2) {
+    if (m[2] == 2) {
+      if (m[4] == 2) { src = i13; n = 13; } else { src = i1245; n = 4; }
+    } else {
+      if (m[4] == 2) { src = i1389; n = 4; } else { static const int a[1] = {1}; src = a; n = 1; }
+    }
+  } else {
+    if (m[2] == 2) {
+      if (m[4] == 2) { src = i2367; n = 4; } else { static const int a[1] = {2}; src = a; n = 1; }
+    } else {
+      if (m[4] == 2) { static const int a[1] = {3}; src = a; n = 1; } else { h->periodic = 0; }
+    }
+  }
+  h->nperoff = n;
+  for (int i = 0; i < n; i++) h->peroffidx[i] = src[i];
+}
+
+int bsamo_commit(bsamo_hier* h) {
+  if (!h || h->committed) return -1;
+  OPatch* root = NULL;
+  for (int n = 0; n < h->np; n++)
+    if (h->p[n].level == 0) { root = &h->p[n]; break; }
+  if (!root) return -2;
+  h->minlevel_present = 0;
+  h->maxlevel_present = 0;
+  for (int n = 0; n < h->np; n++) {
+    OPatch* p = &h->p[n];
+    if (p->level < h->minlevel_present) h->minlevel_present = p->level;
+    if (p->level > h->maxlevel_present) h->maxlevel_present = p->level;
+    if (p->parent_id >= 0) {
+      OPatch* par = find_patch(h, p->parent_id);
+      if (!par || par->level != p->level - 1) return -3;
+      p->parent = (int)(par - h->p);
+    }
+    for (int f = 0; f < 2 * h->ndims; f++)
+      if (p->mthbc[f] != 2 && p->mthbc[f] != 10 && p->mthbc[f] != INTERNALBC)
+        return -4;
+    for (int d = 0; d < 3; d++) {
+      int used = d < h->ndims;
+      p->cmx[d] = (used && p->mx[d] % 2 == 0) ? p->mx[d] / 2 : 1; /* bsamstorage.f90:67-73 */
+      p->qlo[d] = used ? 1 - h->mbc : 1;
+      p->qn[d] = used ? p->mx[d] + 2 * h->mbc : 1;
+      p->clo[d] = used ? 1 - h->mbc : 1;
+      p->cn[d] = used ? p->cmx[d] + 2 * h->mbc : 1;
+      p->fn[d] = used ? p->mx[d] : 1;
+    }
+    size_t nq = (size_t)p->qn[0] * p->qn[1] * p->qn[2] * h->nrvars;
+    size_t nc = (size_t)p->cn[0] * p->cn[1] * p->cn[2] * h->nrvars;
+    size_t nf = (size_t)p->fn[0] * p->fn[1] * p->fn[2] * h->nrvars;
+    p->q = (double*)calloc(nq, sizeof(double)); /* zero fill, bsamstorage.f90:136-140 */
+    p->qold = (double*)calloc(nq, sizeof(double));
+    p->qc = (double*)calloc(nc, sizeof(double));
+    p->f = (double*)calloc(nf, sizeof(double));
+    p->rf = (double*)calloc(nf, sizeof(double));
+    p->ftmp = (double*)calloc(nf, sizeof(double));
+  }
+  for (int l = 0; l < NLEV; l++) {
+    h->lev_n[l] = 0;
+    free(h->lev_list[l]);
+    h->lev_list[l] = (int*)malloc(sizeof(int) * (h->np + 1));
+  }
+  for (int n = 0; n < h->np; n++) {
+    int l = h->p[n].level + MAXDEPTH;
+    h->lev_list[l][h->lev_n[l]++] = n;
+  }
+  /* mxmax, bsamroutines.f90:397-401 */
+  for (int l = 0; l <= MAXDEPTH; l++)
+    for (int d = 0; d < 3; d++)
+      h->mxmax[l][d] = d < h->ndims ? root->mx[d] << l : 1;
+  periodic_setup(h, root->mthbc);
+  h->committed = 1;
+  return 0;
+}
+
+int bsamo_num_patches(const bsamo_hier* h) { return h ? h->np : -1; }
+
+int bsamo_patch_info(const bsamo_hier* h, int index, int* out, double* dxl) {
+  if (!h || index < 0 || index >= h->np) return -1;
+  const OPatch* p = &h->p[index];
+  out[0] = p->level; out[1] = p->id; out[2] = p->parent_id;
+  for (int d = 0; d < 3; d++) {
+    out[3 + d] = p->mx[d];
+    out[6 + 2 * d] = p->mglobal[d][0];
+    out[7 + 2 * d] = p->mglobal[d][1];
+    out[12 + 2 * d] = p->mbounds[d][0];
+    out[13 + 2 * d] = p->mbounds[d][1];
+  }
+  for (int f = 0; f < 6; f++) out[18 + f] = p->mthbc[f];
+  if (dxl)
+    for (int d = 0; d < 3; d++) { dxl[d] = p->dx[d]; dxl[3 + d] = p->xlower[d]; }
+  return 0;
+}
+
+static double* field_ptr(const OPatch* p, int field, size_t* n, int nrvars) {
+  size_t nq = (size_t)p->qn[0] * p->qn[1] * p->qn[2] * nrvars;
+  size_t nc = (size_t)p->cn[0] * p->cn[1] * p->cn[2] * nrvars;
+  size_t nf = (size_t)p->fn[0] * p->fn[1] * p->fn[2] * nrvars;
+  switch (field) {
+    case BSAMO_FIELD_Q: *n = nq; return p->q;
+    case BSAMO_FIELD_QOLD: *n = nq; return p->qold;
+    case BSAMO_FIELD_QC: *n = nc; return p->qc;
+    case BSAMO_FIELD_F: *n = nf; return p->f;
+    case BSAMO_FIELD_RF: *n = nf; return p->rf;
+    case BSAMO_FIELD_FTMP: *n = nf; return p->ftmp;
+  }
+  *n = 0;
+  return NULL;
+}
+
+size_t bsamo_field_size(const bsamo_hier* h, int id, int field) {
+  if (!h || !h->committed) return 0;
+  const OPatch* p = find_patch(h, id);
+  if (!p) return 0;
+  size_t n;
+  field_ptr(p, field, &n, h->nrvars);
+  return n;
+}
+
+int bsamo_put_field(bsamo_hier* h, int id, int field, const double* a, size_t n) {
+  if (!h || !h->committed) return -1;
+  OPatch* p = find_patch(h, id);
+  if (!p) return -2;
+  size_t nn;
+  double* d = field_ptr(p, field, &nn, h->nrvars);
+  if (!d || nn != n) return -3;
+  memcpy(d, a, n * sizeof(double));
+  return 0;
+}
+
+int bsamo_get_field(const bsamo_hier* h, int id, int field, double* a, size_t n) {
+  if (!h || !h->committed) return -1;
+  const OPatch* p = find_patch(h, id);
+  if (!p) return -2;
+  size_t nn;
+  double* d = field_ptr(p, field, &nn, h->nrvars);
+  if (!d || nn != n) return -3;
+  memcpy(a, d, n * sizeof(double));
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* grid utilities (LIBRARY/gridutilities.f90)                           */
+
+static inline double cube(double c) { return c * c * c; } /* CH/problem.f90:918-928 */
+static inline double sqr(double c) { return c * c; }      /* :931-941 */
+
+/* ULap2D, gridutilities.f90:50-72, on plane v of a ghosted q-like array */
+static inline double ulap2(const OPatch* p, const double* a, int i, int j, int v,
+                           int coarse) {
+  size_t (*ix)(const OPatch*, int, int, int, int) = coarse ? ic : iq;
+  return a[ix(p, i + 1, j, 1, v)] + a[ix(p, i - 1, j, 1, v)] +
+         a[ix(p, i, j + 1, 1, v)] + a[ix(p, i, j - 1, 1, v)] -
+         4.0 * a[ix(p, i, j, 1, v)];
+}
+/* ULap3D, gridutilities.f90:372-399 */
+static inline double ulap3(const OPatch* p, const double* a, int i, int j, int k,
+                           int v, int coarse) {
+  size_t (*ix)(const OPatch*, int, int, int, int) = coarse ? ic : iq;
+  return a[ix(p, i + 1, j, k, v)] + a[ix(p, i - 1, j, k, v)] +
+         a[ix(p, i, j + 1, k, v)] + a[ix(p, i, j - 1, k, v)] +
+         a[ix(p, i, j, k + 1, v)] + a[ix(p, i, j, k - 1, v)] -
+         6.0 * a[ix(p, i, j, k, v)];
+}
+
+/* ------------------------------------------------------------------ */
+/* problem plugins                                                     */
+
+/* Growth / Uptake, BioGrowth/problem.f90:743-766 */
+static inline double growth(const bsamo_hier* h, double p) {
+  return h->gamma * 0.5 * (p + 1.0);
+}
+static inline double uptake(const bsamo_hier* h, double p) {
+  return h->lambda * 0.5 * (p + 1.0);
+}
+
+/* RelaxGrid2D, CH/problem.f90:318-369 */
+static void relax_ch2d(const bsamo_hier* h, OPatch* p, int ipass) {
+  double hh = p->dx[0];
+  double h2 = hh * hh;
+  double tmp1 = h->dt / h2, tmp2 = h->eps2 / h2, tmp3 = 4.0 * h->eps2 / h2;
+  double a12 = 4.0 * tmp1;
+  for (int j = 1; j <= p->mx[1]; j++)
+    for (int i = 1 + imod(j + ipass, 2); i <= p->mx[0]; i += 2) {
+      double a21 = -3.0 * sqr(Q(p, i, j, 1, 0)) - tmp3;
+      double b1 = FF(p, i, j, 1, 0) +
+                  tmp1 * (Q(p, i - 1, j, 1, 1) + Q(p, i + 1, j, 1, 1) +
+                          Q(p, i, j - 1, 1, 1) + Q(p, i, j + 1, 1, 1));
+      double b2 = FF(p, i, j, 1, 1) -
+                  tmp2 * (Q(p, i + 1, j, 1, 0) + Q(p, i - 1, j, 1, 0) +
+                          Q(p, i, j + 1, 1, 0) + Q(p, i, j - 1, 1, 0)) -
+                  2.0 * cube(Q(p, i, j, 1, 0));
+      double det = 1.0 - a12 * a21;
+      Q(p, i, j, 1, 0) = (b1 - a12 * b2) / det;
+      Q(p, i, j, 1, 1) = (b2 - a21 * b1) / det;
+    }
+}
+
+/* RelaxGrid3D, CH/problem.f90:554-614 */
+static void relax_ch3d(const bsamo_hier* h, OPatch* p, int ipass) {
+  double hh = p->dx[0];
+  double h2 = hh * hh;
+  double tmp1 = h->dt / h2, tmp2 = h->eps2 / h2, tmp3 = 6.0 * h->eps2 / h2;
+  double a12 = 6.0 * tmp1;
+  for (int k = 1; k <= p->mx[2]; k++)
+    for (int j = 1; j <= p->mx[1]; j++)
+      for (int i = 1 + imod(k + j + ipass, 2); i <= p->mx[0]; i += 2) {
+        double a21 = -3.0 * sqr(Q(p, i, j, k, 0)) - tmp3;
+        double b1 = FF(p, i, j, k, 0) +
+                    tmp1 * (Q(p, i - 1, j, k, 1) + Q(p, i + 1, j, k, 1) +
+                            Q(p, i, j - 1, k, 1) + Q(p, i, j + 1, k, 1) +
+                            Q(p, i, j, k - 1, 1) + Q(p, i, j, k + 1, 1));
+        double b2 = FF(p, i, j, k, 1) -
+                    tmp2 * (Q(p, i + 1, j, k, 0) + Q(p, i - 1, j, k, 0) +
+                            Q(p, i, j + 1, k, 0) + Q(p, i, j - 1, k, 0) +
+                            Q(p, i, j, k + 1, 0) + Q(p, i, j, k - 1, 0)) -
+                    2.0 * cube(Q(p, i, j, k, 0));
+        double det = 1.0 - a12 * a21;
+        Q(p, i, j, k, 0) = (b1 - a12 * b2) / det;
+        Q(p, i, j, k, 1) = (b2 - a21 * b1) / det;
+      }
+}
+
+/* RelaxGrid2D, BioGrowth/problem.f90:255-296 */
+static void relax_bio2d(const bsamo_hier* h, OPatch* p, int ipass) {
+  double hh = p->dx[0];
+  double h2 = hh * hh;
+  double dt = h->dt;
+  double tmp1 = dt * h->eps2 / h2, tmp3 = 1.0 / h2;
+  for (int j = 1; j <= p->mx[1]; j++)
+    for (int i = 1 + imod(j + ipass, 2); i <= p->mx[0]; i += 2) {
+      double tmp2 = 4.0 * tmp1 + 1.0 + dt * sqr(Q(p, i, j, 1, 0));
+      Q(p, i, j, 1, 0) =
+          (FF(p, i, j, 1, 0) +
+           dt * growth(h, QO(p, i, j, 1, 0)) * (Q(p, i, j, 1, 1) - h->czero) +
+           tmp1 * (Q(p, i - 1, j, 1, 0) + Q(p, i + 1, j, 1, 0) +
+                   Q(p, i, j - 1, 1, 0) + Q(p, i, j + 1, 1, 0))) / tmp2;
+      double tmp4 = 4.0 * tmp3 + uptake(h, QO(p, i, j, 1, 0));
+      Q(p, i, j, 1, 1) =
+          (FF(p, i, j, 1, 1) +
+           tmp3 * (Q(p, i + 1, j, 1, 1) + Q(p, i - 1, j, 1, 1) +
+                   Q(p, i, j + 1, 1, 1) + Q(p, i, j - 1, 1, 1))) / tmp4;
+    }
+}
+
+/* RelaxGrid3D, BioGrowth/problem.f90:445-478 (zero stub) */
+static void relax_bio3d(const bsamo_hier* h, OPatch* p, int ipass) {
+  (void)h;
+  for (int k = 1; k <= p->mx[2]; k++)
+    for (int j = 1; j <= p->mx[1]; j++)
+      for (int i = 1 + imod(k + j + ipass, 2); i <= p->mx[0]; i += 2) {
+        Q(p, i, j, k, 0) = 0.0;
+        Q(p, i, j, k, 1) = 0.0;
+      }
+}
+
+/* Operator2D/3D of the plugin evaluated on a ghosted array `a` described by
+ * patch `p` (coarse=1 selects the qc extents), with qold `ao` (may equal
+ * NULL when the plugin does not read qold at these cells), spacing hh; the
+ * result for interior cell (i,j,k) of variable v. */
+typedef struct {
+  const OPatch* p;
+  const double* a;
+  int coarse;
+  /* qold view: patch + offset mapping from (i,j,k) of `a` to qold indices */
+  const OPatch* po;
+  const double* ao;
+  int ooff[3];
+  double hh;
+} OpView;
+
+static inline double opA(const OpView* w, int i, int j, int k, int v) {
+  return w->a[(w->coarse ? ic : iq)(w->p, i, j, k, v)];
+}
+static inline double opO(const OpView* w, int i, int j, int k, int v) {
+  return w->ao[iq(w->po, i + w->ooff[0], j + w->ooff[1], k + w->ooff[2], v)];
+}
+
+/* Operator2D CH/problem.f90:393-422, Operator3D :638-669,
+ * Operator2D BioGrowth/problem.f90:320-353, Operator3D :518-520 (zero) */
+static void op_eval(const bsamo_hier* h, const OpView* w, int i, int j, int k,
+                    double* out) {
+  double h2 = w->hh * w->hh;
+  if (h->problem == BSAMO_PROBLEM_CH) {
+    double tmp1 = h->dt / h2, tmp2 = h->eps2 / h2;
+    if (h->ndims == 2) {
+      out[0] = opA(w, i, j, 1, 0) - tmp1 * ulap2(w->p, w->a, i, j, 1, w->coarse);
+      out[1] = opA(w, i, j, 1, 1) - cube(opA(w, i, j, 1, 0)) +
+               tmp2 * ulap2(w->p, w->a, i, j, 0, w->coarse);
+    } else {
+      out[0] = opA(w, i, j, k, 0) - tmp1 * ulap3(w->p, w->a, i, j, k, 1, w->coarse);
+      out[1] = opA(w, i, j, k, 1) - cube(opA(w, i, j, k, 0)) +
+               tmp2 * ulap3(w->p, w->a, i, j, k, 0, w->coarse);
+    }
+  } else {
+    if (h->ndims == 2) {
+      double dt = h->dt;
+      double tmp1 = dt * h->eps2 / h2, tmp3 = 1.0 / h2;
+      out[0] = opA(w, i, j, 1, 0) - tmp1 * ulap2(w->p, w->a, i, j, 0, w->coarse) +
+               dt * cube(opA(w, i, j, 1, 0)) -
+               dt * growth(h, opO(w, i, j, 1, 0)) * (opA(w, i, j, 1, 1) - h->czero);
+      out[1] = -tmp3 * ulap2(w->p, w->a, i, j, 1, w->coarse) +
+               uptake(h, opO(w, i, j, 1, 0)) * opA(w, i, j, 1, 1);
+    } else {
+      out[0] = 0.0;
+      out[1] = 0.0;
+    }
+  }
+}
+
+/* Source2D/3D + SourceUpdate2D/3D (CH :425-476 / :672-721, BioGrowth
+ * :356-405): value of the source at interior cell for variable v. */
+static inline double source_val(const bsamo_hier* h, const OPatch* p, int i,
+                                int j, int k, int v) {
+  if (h->problem == BSAMO_PROBLEM_CH) {
+    return v == 0 ? QO(p, i, j, k, 0) : -QO(p, i, j, k, 0);
+  }
+  if (h->ndims == 2) return v == 0 ? (1.0 + h->dt) * QO(p, i, j, k, 0) : 0.0;
+  return 0.0;
+}
+
+/* UserBC2D/3D (CH :770-881, BioGrowth :623-736) on face `bc` (1..2*ndims) */
+static void user_bc(const bsamo_hier* h, OPatch* p, int bc) {
+  int nd = h->ndims, mbc = h->mbc, ll = 1 - mbc;
+  int ul[3];
+  for (int d = 0; d < 3; d++) ul[d] = p->mx[d] + mbc;
+  int kl = nd == 3 ? ll : 1, ku = nd == 3 ? ul[2] : 1;
+  for (int v = 0; v < h->nrvars; v++) {
+    /* per variable: reflect (0) or Dirichlet 2-q (1) */
+    int dir;
+    if (h->problem == BSAMO_PROBLEM_CH) dir = nd == 3 ? 1 : 0;
+    else dir = nd == 3 ? 1 : (v == 1);
+    for (int ibc = 1; ibc <= mbc; ibc++) {
+      int d = (bc - 1) / 2, hi = (bc - 1) % 2;
+      int gdst = hi ? p->mx[d] + ibc : 1 - ibc;
+      int gsrc = hi ? p->mx[d] - ibc + 1 : ibc;
+      if (d == 0) {
+        for (int k = kl; k <= ku; k++)
+          for (int j = ll; j <= ul[1]; j++) {
+            double s = Q(p, gsrc, j, k, v);
+            Q(p, gdst, j, k, v) = dir ? 2.0 - s : s;
+          }
+      } else if (d == 1) {
+        for (int k = kl; k <= ku; k++)
+          for (int i = ll; i <= ul[0]; i++) {
+            double s = Q(p, i, gsrc, k, v);
+            Q(p, i, gdst, k, v) = dir ? 2.0 - s : s;
+          }
+      } else {
+        for (int j = ll; j <= ul[1]; j++)
+          for (int i = ll; i <= ul[0]; i++) {
+            double s = Q(p, i, j, gsrc, v);
+            Q(p, i, j, gdst, v) = dir ? 2.0 - s : s;
+          }
+      }
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* boundary.f90                                                        */
+
+/* Interpolate2D, boundary.f90:143-333.  qf = child q, qc = parent q. */
+static void interpolate2d(const bsamo_hier* h, OPatch* f, const OPatch* c,
+                          int ipass) {
+  int mx1 = f->mx[0], mx2 = f->mx[1];
+  int mb11 = f->mbounds[0][0], mb12 = f->mbounds[0][1];
+  int mb21 = f->mbounds[1][0], mb22 = f->mbounds[1][1];
+  const int* m = f->mthbc;
+#define QF(i, j) Q(f, i, j, 1, v)
+#define QCC(i, j) Q(c, i, j, 1, v)
+  for (int v = 0; v < h->nrvars; v++) {
+    if (ipass == 1 || ipass == 0) { /* red corners :158-168 */
+      QF(mx1 + 1, mx2 + 1) = A1 * QF(mx1 - 1, mx2 - 1) + A2 * QF(mx1, mx2) +
+                             A3 * QCC(mb12 + 1, mb22 + 1);
+      QF(0, 0) = A1 * QF(2, 2) + A2 * QF(1, 1) + A3 * QCC(mb11 - 1, mb21 - 1);
+    }
+    if (ipass == 2 || ipass == 0) { /* black corners :171-181 */
+      QF(mx1 + 1, 0) = A1 * QF(mx1 - 1, 2) + A2 * QF(mx1, 1) +
+                       A3 * QCC(mb12 + 1, mb21 - 1);
+      QF(0, mx2 + 1) = A1 * QF(2, mx2 - 1) + A2 * QF(1, mx2) +
+                       A3 * QCC(mb11 - 1, mb22 + 1);
+    }
+  }
+  for (int v = 0; v < h->nrvars; v++) {
+    if (m[0] == 2 || m[0] == INTERNALBC) { /* face 1 :185-216 */
+      if (ipass == 1 || ipass == 0) {
+        for (int j = 2, n = 0; j <= mx2 - 2; j += 2, n++)
+          QF(0, j) = A1 * QF(2, j + 2) + A2 * QF(1, j + 1) + A3 * QCC(mb11 - 1, mb21 + n);
+        QF(0, mx2) = A1 * QF(2, mx2) + A2 * QF(1, mx2) +
+                     A3 * (B1 * QCC(mb11 - 1, mb22 + 1) + B2 * QCC(mb11 - 1, mb22) +
+                           B3 * QCC(mb11 - 1, mb22 - 1));
+      }
+      if (ipass == 2 || ipass == 0) {
+        for (int j = 3, n = 0; j <= mx2 - 1; j += 2, n++)
+          QF(0, j) = A1 * QF(2, j - 2) + A2 * QF(1, j - 1) + A3 * QCC(mb11 - 1, mb21 + 1 + n);
+        QF(0, 1) = A1 * QF(2, 1) + A2 * QF(1, 1) +
+                   A3 * (B1 * QCC(mb11 - 1, mb21 - 1) + B2 * QCC(mb11 - 1, mb21) +
+                         B3 * QCC(mb11 - 1, mb21 + 1));
+      }
+    }
+    if (m[1] == 2 || m[1] == INTERNALBC) { /* face 2 :222-257 */
+      if (ipass == 1 || ipass == 0) {
+        for (int j = 3, n = 0; j <= mx2 - 1; j += 2, n++)
+          QF(mx1 + 1, j) = A1 * QF(mx1 - 1, j - 2) + A2 * QF(mx1, j - 1) +
+                           A3 * QCC(mb12 + 1, mb21 + 1 + n);
+        QF(mx1 + 1, 1) = A1 * QF(mx1 - 1, 1) + A2 * QF(mx1, 1) +
+                         A3 * (B1 * QCC(mb12 + 1, mb21 - 1) + B2 * QCC(mb12 + 1, mb21) +
+                               B3 * QCC(mb12 + 1, mb21 + 1));
+      }
+      if (ipass == 2 || ipass == 0) {
+        for (int j = 2, n = 0; j <= mx2 - 2; j += 2, n++)
+          QF(mx1 + 1, j) = A1 * QF(mx1 - 1, j + 2) + A2 * QF(mx1, j + 1) +
+                           A3 * QCC(mb12 + 1, mb21 + n);
+        QF(mx1 + 1, mx2) = A1 * QF(mx1 - 1, mx2) + A2 * QF(mx1, mx2) +
+                           A3 * (B1 * QCC(mb12 + 1, mb22 + 1) + B2 * QCC(mb12 + 1, mb22) +
+                                 B3 * QCC(mb12 + 1, mb22 - 1));
+      }
+    }
+    if (m[2] == 2 || m[2] == INTERNALBC) { /* face 3 :259-294 */
+      if (ipass == 1 || ipass == 0) {
+        for (int i = 2, n = 0; i <= mx1 - 2; i += 2, n++)
+          QF(i, 0) = A1 * QF(i + 2, 2) + A2 * QF(i + 1, 1) + A3 * QCC(mb11 + n, mb21 - 1);
+        QF(mx1, 0) = A1 * QF(mx1, 2) + A2 * QF(mx1, 1) +
+                     A3 * (B1 * QCC(mb12 + 1, mb21 - 1) + B2 * QCC(mb12, mb21 - 1) +
+                           B3 * QCC(mb12 - 1, mb21 - 1));
+      }
+      if (ipass == 2 || ipass == 0) {
+        for (int i = 3, n = 0; i <= mx1 - 1; i += 2, n++)
+          QF(i, 0) = A1 * QF(i - 2, 2) + A2 * QF(i - 1, 1) + A3 * QCC(mb11 + 1 + n, mb21 - 1);
+        QF(1, 0) = A1 * QF(1, 2) + A2 * QF(1, 1) +
+                   A3 * (B1 * QCC(mb11 - 1, mb21 - 1) + B2 * QCC(mb11, mb21 - 1) +
+                         B3 * QCC(mb11 + 1, mb21 - 1));
+      }
+    }
+    if (m[3] == 2 || m[3] == INTERNALBC) { /* face 4 :296-331 */
+      if (ipass == 1 || ipass == 0) {
+        for (int i = 3, n = 0; i <= mx1 - 1; i += 2, n++)
+          QF(i, mx2 + 1) = A1 * QF(i - 2, mx2 - 1) + A2 * QF(i - 1, mx2) +
+                           A3 * QCC(mb11 + 1 + n, mb22 + 1);
+        QF(1, mx2 + 1) = A1 * QF(1, mx2 - 1) + A2 * QF(1, mx2) +
+                         A3 * (B1 * QCC(mb11 - 1, mb22 + 1) + B2 * QCC(mb11, mb22 + 1) +
+                               B3 * QCC(mb11 + 1, mb22 + 1));
+      }
+      if (ipass == 2 || ipass == 0) {
+        for (int i = 2, n = 0; i <= mx1 - 2; i += 2, n++)
+          QF(i, mx2 + 1) = A1 * QF(i + 2, mx2 - 1) + A2 * QF(i + 1, mx2) +
+                           A3 * QCC(mb11 + n, mb22 + 1);
+        QF(mx1, mx2 + 1) = A1 * QF(mx1, mx2 - 1) + A2 * QF(mx1, mx2) +
+                           A3 * (B1 * QCC(mb12 + 1, mb22 + 1) + B2 * QCC(mb12, mb22 + 1) +
+                                 B3 * QCC(mb12 - 1, mb22 + 1));
+      }
+    }
+  }
+#undef QF
+#undef QCC
+}
+
+/* GhostOverlap, boundary.f90:359-431 (the level-landscape part, :434-475, is
+ * only used while the mesh is being built and is not restated). */
+static void ghost_overlap(const bsamo_hier* h, OPatch* g1, OPatch* g2,
+                          const int* off) {
+  int nd = h->ndims, mbc = h->mbc;
+  int mg1[3][2], mg2[3][2], ovg[3][2], ovg1[3][2], ovg2[3][2];
+  for (int n = 0; n < 3; n++) {
+    mg1[n][0] = mg1[n][1] = mg2[n][0] = mg2[n][1] = 1;
+    ovg[n][0] = ovg[n][1] = ovg1[n][0] = ovg1[n][1] = ovg2[n][0] = ovg2[n][1] = 1;
+  }
+  for (int n = 0; n < nd; n++) {
+    mg1[n][0] = g1->mglobal[n][0];
+    mg1[n][1] = g1->mglobal[n][1];
+    mg2[n][0] = g2->mglobal[n][0] + (off ? off[n] : 0);
+    mg2[n][1] = g2->mglobal[n][1] + (off ? off[n] : 0);
+  }
+  for (int n = 0; n < nd; n++) {
+    ovg[n][0] = mg1[n][0] - mbc > mg2[n][0] - mbc ? mg1[n][0] - mbc : mg2[n][0] - mbc;
+    ovg[n][1] = mg1[n][1] + mbc < mg2[n][1] + mbc ? mg1[n][1] + mbc : mg2[n][1] + mbc;
+  }
+  for (int n = 0; n < nd; n++)
+    if (ovg[n][1] - ovg[n][0] < 0) return;
+  for (int n = 0; n < nd; n++) {
+    ovg1[n][0] = ovg[n][0] > mg2[n][0] ? ovg[n][0] : mg2[n][0];
+    ovg1[n][1] = ovg[n][1] < mg2[n][1] ? ovg[n][1] : mg2[n][1];
+    ovg2[n][0] = ovg[n][0] > mg1[n][0] ? ovg[n][0] : mg1[n][0];
+    ovg2[n][1] = ovg[n][1] < mg1[n][1] ? ovg[n][1] : mg1[n][1];
+  }
+  /* grid2 interior -> grid1 (:412-420) */
+  int ml1[3][2], ml2[3][2];
+  for (int n = 0; n < 3; n++) ml1[n][0] = ml1[n][1] = ml2[n][0] = ml2[n][1] = 1;
+  for (int n = 0; n < nd; n++) {
+    ml1[n][0] = ovg1[n][0] - mg1[n][0] + 1;
+    ml1[n][1] = ovg1[n][1] - mg1[n][0] + 1;
+    ml2[n][0] = ovg1[n][0] - mg2[n][0] + 1;
+    ml2[n][1] = ovg1[n][1] - mg2[n][0] + 1;
+  }
+  for (int v = 0; v < h->nrvars; v++)
+    for (int k = 0; k <= ml1[2][1] - ml1[2][0]; k++)
+      for (int j = 0; j <= ml1[1][1] - ml1[1][0]; j++)
+        for (int i = 0; i <= ml1[0][1] - ml1[0][0]; i++)
+          Q(g1, ml1[0][0] + i, ml1[1][0] + j, ml1[2][0] + k, v) =
+              Q(g2, ml2[0][0] + i, ml2[1][0] + j, ml2[2][0] + k, v);
+  /* grid1 interior -> grid2 (:422-430) */
+  for (int n = 0; n < nd; n++) {
+    ml1[n][0] = ovg2[n][0] - mg1[n][0] + 1;
+    ml1[n][1] = ovg2[n][1] - mg1[n][0] + 1;
+    ml2[n][0] = ovg2[n][0] - mg2[n][0] + 1;
+    ml2[n][1] = ovg2[n][1] - mg2[n][0] + 1;
+  }
+  for (int v = 0; v < h->nrvars; v++)
+    for (int k = 0; k <= ml2[2][1] - ml2[2][0]; k++)
+      for (int j = 0; j <= ml2[1][1] - ml2[1][0]; j++)
+        for (int i = 0; i <= ml2[0][1] - ml2[0][0]; i++)
+          Q(g2, ml2[0][0] + i, ml2[1][0] + j, ml2[2][0] + k, v) =
+              Q(g1, ml1[0][0] + i, ml1[1][0] + j, ml1[2][0] + k, v);
+}
+
+/* SelfPeriodicBC, boundary.f90:480-577 */
+static void self_periodic(const bsamo_hier* h, OPatch* p) {
+  int mbc = h->mbc, nd = h->ndims;
+  int lo[3], hi[3];
+  for (int d = 0; d < 3; d++) {
+    lo[d] = d < nd ? 1 - mbc : 1;
+    hi[d] = d < nd ? p->mx[d] + mbc : 1;
+  }
+  if (p->mthbc[0] == 2 && p->mthbc[1] == 2) {
+    for (int ibc = 1; ibc <= mbc; ibc++)
+      for (int v = 0; v < h->nrvars; v++) {
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++)
+            Q(p, p->mx[0] + ibc, j, k, v) = Q(p, ibc, j, k, v) + h->qpo[v];
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++)
+            Q(p, 1 - ibc, j, k, v) = Q(p, p->mx[0] + 1 - ibc, j, k, v) - h->qpo[v];
+      }
+  }
+  if (p->mthbc[2] == 2 && p->mthbc[3] == 2) {
+    for (int ibc = 1; ibc <= mbc; ibc++)
+      for (int v = 0; v < h->nrvars; v++) {
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int i = lo[0]; i <= hi[0]; i++)
+            Q(p, i, p->mx[1] + ibc, k, v) = Q(p, i, ibc, k, v);
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int i = lo[0]; i <= hi[0]; i++)
+            Q(p, i, 1 - ibc, k, v) = Q(p, i, p->mx[1] + 1 - ibc, k, v);
+      }
+  }
+  if (nd == 3 && p->mthbc[4] == 2 && p->mthbc[5] == 2) {
+    for (int ibc = 1; ibc <= mbc; ibc++)
+      for (int v = 0; v < h->nrvars; v++) {
+        for (int j = lo[1]; j <= hi[1]; j++)
+          for (int i = lo[0]; i <= hi[0]; i++)
+            Q(p, i, j, p->mx[2] + ibc, v) = Q(p, i, j, ibc, v);
+        for (int j = lo[1]; j <= hi[1]; j++)
+          for (int i = lo[0]; i <= hi[0]; i++)
+            Q(p, i, j, 1 - ibc, v) = Q(p, i, j, p->mx[2] + 1 - ibc, v);
+      }
+  }
+}
+
+/* GetPeriodicOffsets, boundary.f90:875-954 */
+static void periodic_offsets(const bsamo_hier* h, int level, int poff[13][3]) {
+  const int* mm = h->mxmax[level];
+  for (int o = 0; o < h->nperoff; o++) {
+    int a = 0, b = 0, c = 0;
+    switch (h->peroffidx[o]) {
+      case 1: a = mm[0]; break;
+      case 2: b = mm[1]; break;
+      case 3: c = mm[2]; break;
+      case 4: a = mm[0]; b = mm[1]; break;
+      case 5: a = -mm[0]; b = mm[1]; break;
+      case 6: b = mm[1]; c = mm[2]; break;
+      case 7: b = mm[1]; c = -mm[2]; break;
+      case 8: a = mm[0]; c = mm[2]; break;
+      case 9: a = -mm[0]; c = mm[2]; break;
+      case 10: a = mm[0]; b = mm[1]; c = mm[2]; break;
+      case 11: a = mm[0]; b = mm[1]; c = -mm[2]; break;
+      case 12: a = -mm[0]; b = mm[1]; c = mm[2]; break;
+      case 13: a = mm[0]; b = -mm[1]; c = mm[2]; break;
+    }
+    poff[o][0] = a; poff[o][1] = b; poff[o][2] = c;
+  }
+}
+
+/* SetPhysicalBC2D/3D, boundary.f90:614-802 */
+static void set_physical_bc(const bsamo_hier* h, OPatch* p) {
+  for (int face = 1; face <= 2 * h->ndims; face++)
+    if (p->mthbc[face - 1] == 10) user_bc(h, p, face);
+}
+
+/* SetGhost, boundary.f90:67-97 */
+static void set_ghost(bsamo_hier* h, int level, int ipass) {
+  int n = nlev(h, level);
+  if (level > 0) {
+    for (int a = 0; a < n; a++) { /* InterpolateCoarseFine :100-140 */
+      OPatch* p = lev_patch(h, level, a);
+      OPatch* c = parent_of(h, p);
+      if (h->ndims == 2) interpolate2d(h, p, c, ipass);
+      /* Interpolate3D (boundary.f90:1048-1550) is not restated */
+    }
+    for (int a = 0; a < n; a++) /* ApplyOnLevelPairs(TransferBC) */
+      for (int b = a + 1; b < n; b++)
+        ghost_overlap(h, lev_patch(h, level, a), lev_patch(h, level, b), NULL);
+  }
+  if (h->periodic) {
+    for (int a = 0; a < n; a++) self_periodic(h, lev_patch(h, level, a));
+    if (level > 0) { /* TransferPeriodicBC :580-611 */
+      int poff[13][3];
+      periodic_offsets(h, level, poff);
+      for (int a = 0; a < n; a++)
+        for (int b = a + 1; b < n; b++)
+          for (int pol = -1; pol <= 1; pol += 2)
+            for (int o = 0; o < h->nperoff; o++) {
+              int off[3] = {pol * poff[o][0], pol * poff[o][1], pol * poff[o][2]};
+              ghost_overlap(h, lev_patch(h, level, a), lev_patch(h, level, b), off);
+            }
+    }
+  }
+  for (int a = 0; a < n; a++) set_physical_bc(h, lev_patch(h, level, a));
+}
+
+/* GetCoarseGhostPoints, boundary.f90:957-1015 */
+static void get_coarse_ghost_points(const bsamo_hier* h, OPatch* p) {
+  OPatch* par = &((bsamo_hier*)h)->p[p->parent];
+  int nd = h->ndims;
+  int il[3] = {1, 1, 1}, ih[3] = {1, 1, 1}, jl[3] = {1, 1, 1}, jh[3] = {1, 1, 1};
+  int mb[3][2];
+  for (int d = 0; d < 3; d++) { mb[d][0] = mb[d][1] = 1; }
+  for (int d = 0; d < nd; d++) {
+    il[d] = 0; ih[d] = p->cmx[d] + 1;
+    mb[d][0] = p->mbounds[d][0]; mb[d][1] = p->mbounds[d][1];
+    jl[d] = mb[d][0] - 1; jh[d] = mb[d][1] + 1;
+  }
+  for (int v = 0; v < h->nrvars; v++) {
+    /* face 1 and 2 */
+    for (int k = il[2]; k <= ih[2]; k++)
+      for (int j = il[1]; j <= ih[1]; j++) {
+        QC(p, il[0], j, k, v) = Q(par, jl[0], jl[1] + (j - il[1]), jl[2] + (k - il[2]), v);
+      }
+    for (int k = il[2]; k <= ih[2]; k++)
+      for (int j = il[1]; j <= ih[1]; j++) {
+        QC(p, ih[0], j, k, v) = Q(par, jh[0], jl[1] + (j - il[1]), jl[2] + (k - il[2]), v);
+      }
+    /* face 3 and 4 */
+    for (int k = il[2]; k <= ih[2]; k++)
+      for (int i = 1; i <= p->cmx[0]; i++)
+        QC(p, i, il[1], k, v) = Q(par, mb[0][0] + i - 1, jl[1], jl[2] + (k - il[2]), v);
+    for (int k = il[2]; k <= ih[2]; k++)
+      for (int i = 1; i <= p->cmx[0]; i++)
+        QC(p, i, ih[1], k, v) = Q(par, mb[0][0] + i - 1, jh[1], jl[2] + (k - il[2]), v);
+    if (nd >= 3) { /* face 5 and 6 */
+      for (int j = 1; j <= p->cmx[1]; j++)
+        for (int i = 1; i <= p->cmx[0]; i++)
+          QC(p, i, j, il[2], v) = Q(par, mb[0][0] + i - 1, mb[1][0] + j - 1, jl[2], v);
+      for (int j = 1; j <= p->cmx[1]; j++)
+        for (int i = 1; i <= p->cmx[0]; i++)
+          QC(p, i, j, ih[2], v) = Q(par, mb[0][0] + i - 1, mb[1][0] + j - 1, jh[2], v);
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* afasroutines.f90                                                     */
+
+static void relax_patch(const bsamo_hier* h, OPatch* p, int ipass) {
+  /* RelaxPatch, afasroutines.f90:560-607 */
+  if (h->problem == BSAMO_PROBLEM_CH) {
+    if (h->ndims == 2) relax_ch2d(h, p, ipass); else relax_ch3d(h, p, ipass);
+  } else {
+    if (h->ndims == 2) relax_bio2d(h, p, ipass); else relax_bio3d(h, p, ipass);
+  }
+}
+
+int bsamo_relax_level_color(bsamo_hier* h, int level, int ipass) {
+  if (!h || !h->committed) return -1;
+  for (int a = 0; a < nlev(h, level); a++) relax_patch(h, lev_patch(h, level, a), ipass);
+  return 0;
+}
+
+int bsamo_set_ghost(bsamo_hier* h, int level, int ipass) {
+  if (!h || !h->committed) return -1;
+  set_ghost(h, level, ipass);
+  return 0;
+}
+
+/* LevelRelax, afasroutines.f90:532-557 */
+static void level_relax(bsamo_hier* h, int level, int nsmooth) {
+  for (int pass = 1; pass <= nsmooth; pass++)
+    for (int rb = 1; rb <= 2; rb++) {
+      for (int a = 0; a < nlev(h, level); a++) relax_patch(h, lev_patch(h, level, a), rb);
+      set_ghost(h, level, rb);
+    }
+}
+
+int bsamo_level_relax(bsamo_hier* h, int level, int nsmooth) {
+  if (!h || !h->committed) return -1;
+  level_relax(h, level, nsmooth);
+  return 0;
+}
+
+/* Residual, afasroutines.f90:817-857: rf = f - Operator(q) */
+static void residual(const bsamo_hier* h, OPatch* p) {
+  OpView w = {p, p->q, 0, p, p->qold, {0, 0, 0}, p->dx[0]};
+  double out[3];
+  int kmx = h->ndims == 3 ? p->mx[2] : 1;
+  for (int k = 1; k <= kmx; k++)
+    for (int j = 1; j <= p->mx[1]; j++)
+      for (int i = 1; i <= p->mx[0]; i++) {
+        op_eval(h, &w, i, j, k, out);
+        for (int v = 0; v < h->nrvars; v++) RF(p, i, j, k, v) = FF(p, i, j, k, v) - out[v];
+      }
+}
+
+/* Restriction2D/3D, gridutilities.f90:103-126, :437-466, of an interior
+ * array accessor. */
+typedef double (*Getter)(const OPatch*, int, int, int, int);
+static double get_q(const OPatch* p, int i, int j, int k, int v) { return Q(p, i, j, k, v); }
+static double get_f(const OPatch* p, int i, int j, int k, int v) { return FF(p, i, j, k, v); }
+static double get_rf(const OPatch* p, int i, int j, int k, int v) { return RF(p, i, j, k, v); }
+
+static inline double restrict_at(const bsamo_hier* h, const OPatch* p, Getter g,
+                                 int ci, int cj, int ck, int v) {
+  int i = 2 * ci, j = 2 * cj;
+  if (h->ndims == 2)
+    return 0.25 * (g(p, i, j, 1, v) + g(p, i - 1, j, 1, v) + g(p, i, j - 1, 1, v) +
+                   g(p, i - 1, j - 1, 1, v));
+  int k = 2 * ck;
+  return 0.125 * (g(p, i, j, k, v) + g(p, i - 1, j, k, v) + g(p, i, j - 1, k, v) +
+                  g(p, i - 1, j - 1, k, v) + g(p, i, j, k - 1, v) +
+                  g(p, i - 1, j, k - 1, v) + g(p, i, j - 1, k - 1, v) +
+                  g(p, i - 1, j - 1, k - 1, v));
+}
+
+/* RestrictSolution, afasroutines.f90:610-652 */
+static void restrict_solution(bsamo_hier* h, OPatch* p) {
+  OPatch* par = parent_of(h, p);
+  int kc = h->ndims == 3 ? p->cmx[2] : 1;
+  for (int v = 0; v < h->nrvars; v++)
+    for (int k = 1; k <= kc; k++)
+      for (int j = 1; j <= p->cmx[1]; j++)
+        for (int i = 1; i <= p->cmx[0]; i++)
+          QC(p, i, j, k, v) = restrict_at(h, p, get_q, i, j, k, v);
+  for (int v = 0; v < h->nrvars; v++)
+    for (int k = 1; k <= kc; k++)
+      for (int j = 1; j <= p->cmx[1]; j++)
+        for (int i = 1; i <= p->cmx[0]; i++)
+          Q(par, p->mbounds[0][0] + i - 1, p->mbounds[1][0] + j - 1,
+            h->ndims == 3 ? p->mbounds[2][0] + k - 1 : 1, v) = QC(p, i, j, k, v);
+}
+
+/* CoarseLoadingFunction, afasroutines.f90:673-736 */
+static void coarse_loading(bsamo_hier* h, OPatch* p) {
+  OPatch* par = parent_of(h, p);
+  double ch = par->dx[0];
+  residual(h, p);
+  /* qold of the parent offset so that qc index (i,j,k) maps to parent
+   * index mb-1+i (the section parent%qold(mb-1:mb+1)) */
+  OpView w = {p, p->qc, 1, par, par->qold,
+              {p->mbounds[0][0] - 1, p->mbounds[1][0] - 1,
+               h->ndims == 3 ? p->mbounds[2][0] - 1 : 0}, ch};
+  double out[3];
+  int kc = h->ndims == 3 ? p->cmx[2] : 1;
+  for (int k = 1; k <= kc; k++)
+    for (int j = 1; j <= p->cmx[1]; j++)
+      for (int i = 1; i <= p->cmx[0]; i++) {
+        op_eval(h, &w, i, j, k, out);
+        for (int v = 0; v < h->nrvars; v++)
+          FF(par, p->mbounds[0][0] + i - 1, p->mbounds[1][0] + j - 1,
+             h->ndims == 3 ? p->mbounds[2][0] + k - 1 : 1, v) =
+              restrict_at(h, p, get_rf, i, j, k, v) + out[v];
+      }
+}
+
+/* CorrectFine, afasroutines.f90:860-980 with BiLinProlongationP1
+ * (gridutilities.f90:156-195) / TriLinProlongationP1 (:510-566). */
+static void correct_fine(bsamo_hier* h, OPatch* p) {
+  OPatch* par = parent_of(h, p);
+  int nd = h->ndims;
+  int c0 = p->cmx[0], c1 = p->cmx[1], c2 = nd == 3 ? p->cmx[2] : 1;
+  int mb0 = p->mbounds[0][0], mb1 = p->mbounds[1][0], mb2 = nd == 3 ? p->mbounds[2][0] : 1;
+  int klo = nd == 3 ? 0 : 1, khi = nd == 3 ? c2 + 1 : 1;
+  for (int v = 0; v < h->nrvars; v++)
+    for (int k = klo; k <= khi; k++)
+      for (int j = 0; j <= c1 + 1; j++)
+        for (int i = 0; i <= c0 + 1; i++)
+          QC(p, i, j, k, v) =
+              Q(par, mb0 - 1 + i, mb1 - 1 + j, nd == 3 ? mb2 - 1 + k : 1, v) - QC(p, i, j, k, v);
+  int m0 = p->mx[0], m1 = p->mx[1], m2 = nd == 3 ? p->mx[2] : 1;
+  if (nd == 2) {
+    size_t nb = (size_t)(m0 + 2) * (c1 + 2);
+    double* b = (double*)malloc(sizeof(double) * nb);
+#define B(i, j) b[(size_t)(j) * (m0 + 2) + (i)]
+    for (int v = 0; v < h->nrvars; v++) {
+      for (int cj = 0; cj <= c1 + 1; cj++)
+        for (int c = 0; c <= c0; c++) {
+          B(2 * c, cj) = 3.0 * QC(p, c, cj, 1, v) + QC(p, c + 1, cj, 1, v);
+          B(2 * c + 1, cj) = QC(p, c, cj, 1, v) + 3.0 * QC(p, c + 1, cj, 1, v);
+        }
+      for (int c = 0; c <= c1; c++)
+        for (int i = 0; i <= m0 + 1; i++) {
+          double pe = (3.0 * B(i, c) + B(i, c + 1)) / 16.0;
+          double po = (B(i, c) + 3.0 * B(i, c + 1)) / 16.0;
+          Q(p, i, 2 * c, 1, v) = Q(p, i, 2 * c, 1, v) + pe;
+          Q(p, i, 2 * c + 1, 1, v) = Q(p, i, 2 * c + 1, 1, v) + po;
+        }
+    }
+#undef B
+    free(b);
+  } else {
+    size_t nb = (size_t)(m0 + 2) * (c1 + 2) * (c2 + 2);
+    size_t ncc = (size_t)(m0 + 2) * (m1 + 2) * (c2 + 2);
+    double* b = (double*)malloc(sizeof(double) * nb);
+    double* cc = (double*)malloc(sizeof(double) * ncc);
+#define B(i, j, k) b[((size_t)(k) * (c1 + 2) + (j)) * (m0 + 2) + (i)]
+#define CC(i, j, k) cc[((size_t)(k) * (m1 + 2) + (j)) * (m0 + 2) + (i)]
+    for (int v = 0; v < h->nrvars; v++) {
+      for (int ck = 0; ck <= c2 + 1; ck++)
+        for (int cj = 0; cj <= c1 + 1; cj++)
+          for (int c = 0; c <= c0; c++) {
+            B(2 * c, cj, ck) = 3.0 * QC(p, c, cj, ck, v) + QC(p, c + 1, cj, ck, v);
+            B(2 * c + 1, cj, ck) = QC(p, c, cj, ck, v) + 3.0 * QC(p, c + 1, cj, ck, v);
+          }
+      for (int ck = 0; ck <= c2 + 1; ck++)
+        for (int c = 0; c <= c1; c++)
+          for (int i = 0; i <= m0 + 1; i++) {
+            CC(i, 2 * c, ck) = 3.0 * B(i, c, ck) + B(i, c + 1, ck);
+            CC(i, 2 * c + 1, ck) = B(i, c, ck) + 3.0 * B(i, c + 1, ck);
+          }
+      for (int c = 0; c <= c2; c++)
+        for (int j = 0; j <= m1 + 1; j++)
+          for (int i = 0; i <= m0 + 1; i++) {
+            double pe = (3.0 * CC(i, j, c) + CC(i, j, c + 1)) / 64.0;
+            double po = (CC(i, j, c) + 3.0 * CC(i, j, c + 1)) / 64.0;
+            Q(p, i, j, 2 * c, v) = Q(p, i, j, 2 * c, v) + pe;
+            Q(p, i, j, 2 * c + 1, v) = Q(p, i, j, 2 * c + 1, v) + po;
+          }
+    }
+#undef B
+#undef CC
+    free(b);
+    free(cc);
+  }
+  (void)m2;
+}
+
+/* AFASVcycle, afasroutines.f90:495-529 */
+static void afas_vcycle(bsamo_hier* h, int level, int minlevel, int nsmooth) {
+  level_relax(h, level, nsmooth);
+  if (level > minlevel) {
+    int n = nlev(h, level);
+    for (int a = 0; a < n; a++) restrict_solution(h, lev_patch(h, level, a));
+    set_ghost(h, level - 1, 0);
+    for (int a = 0; a < n; a++) get_coarse_ghost_points(h, lev_patch(h, level, a));
+    for (int a = 0; a < n; a++) coarse_loading(h, lev_patch(h, level, a));
+    afas_vcycle(h, level - 1, minlevel, nsmooth);
+    for (int a = 0; a < n; a++) correct_fine(h, lev_patch(h, level, a));
+    set_ghost(h, level, 0);
+    level_relax(h, level, nsmooth);
+  }
+}
+
+int bsamo_vcycle(bsamo_hier* h, int level, int minlevel, int nsmooth) {
+  if (!h || !h->committed) return -1;
+  afas_vcycle(h, level, minlevel, nsmooth);
+  return 0;
+}
+
+/* FillDown / FillDownLevel, afasroutines.f90:236-327 (1 = source, 2 = q) */
+static void fill_down(bsamo_hier* h, int field, int finest, int minlevel) {
+  for (int level = finest; level >= minlevel + 1; level--) {
+    for (int a = 0; a < nlev(h, level); a++) {
+      OPatch* p = lev_patch(h, level, a);
+      OPatch* par = parent_of(h, p);
+      int kc = h->ndims == 3 ? p->cmx[2] : 1;
+      for (int v = 0; v < h->nrvars; v++)
+        for (int k = 1; k <= kc; k++)
+          for (int j = 1; j <= p->cmx[1]; j++)
+            for (int i = 1; i <= p->cmx[0]; i++) {
+              int pi = p->mbounds[0][0] + i - 1, pj = p->mbounds[1][0] + j - 1;
+              int pk = h->ndims == 3 ? p->mbounds[2][0] + k - 1 : 1;
+              if (field == 1) FF(par, pi, pj, pk, v) = restrict_at(h, p, get_f, i, j, k, v);
+              else Q(par, pi, pj, pk, v) = restrict_at(h, p, get_q, i, j, k, v);
+            }
+    }
+    if (field == 2) set_ghost(h, level - 1, 0);
+  }
+}
+
+int bsamo_fill_down(bsamo_hier* h, int field, int finestlevel, int minlevel) {
+  if (!h || !h->committed || (field != 1 && field != 2)) return -1;
+  fill_down(h, field, finestlevel, minlevel);
+  return 0;
+}
+
+/* CopyQToQold, bsamroutines.f90:592-605 */
+int bsamo_copy_q_to_qold(bsamo_hier* h, int minlevel, int finestlevel) {
+  if (!h || !h->committed) return -1;
+  for (int level = minlevel; level <= finestlevel; level++)
+    for (int a = 0; a < nlev(h, level); a++) {
+      OPatch* p = lev_patch(h, level, a);
+      size_t nq = (size_t)p->qn[0] * p->qn[1] * p->qn[2] * h->nrvars;
+      memcpy(p->qold, p->q, nq * sizeof(double));
+    }
+  return 0;
+}
+
+/* GetSourceFunction (:330-381) then UpdateSourceFunction (:438-492) */
+static void get_source(bsamo_hier* h, OPatch* p) {
+  int kmx = h->ndims == 3 ? p->mx[2] : 1;
+  for (int v = 0; v < h->nrvars; v++)
+    for (int k = 1; k <= kmx; k++)
+      for (int j = 1; j <= p->mx[1]; j++)
+        for (int i = 1; i <= p->mx[0]; i++) FT(p, i, j, k, v) = source_val(h, p, i, j, k, v);
+}
+static void update_source(bsamo_hier* h, OPatch* p) {
+  int kmx = h->ndims == 3 ? p->mx[2] : 1;
+  for (int v = 0; v < h->nrvars; v++)
+    for (int k = 1; k <= kmx; k++)
+      for (int j = 1; j <= p->mx[1]; j++)
+        for (int i = 1; i <= p->mx[0]; i++) FF(p, i, j, k, v) = FT(p, i, j, k, v) + 0.0;
+}
+
+/* ErrorAFAS, afasroutines.f90:113-160, with L2Error (:163-189) and
+ * L2ComponentErrors (:192-219) */
+static double error_afas(bsamo_hier* h, int level, int errortype) {
+  if (errortype == 1) {
+    h->integral[0] = 0.0;
+    h->integral[1] = 0.0;
+    for (int a = 0; a < nlev(h, level); a++) {
+      OPatch* p = lev_patch(h, level, a);
+      residual(h, p);
+      double s = 0.0; /* SquareSum in array-element order */
+      size_t nf = (size_t)p->fn[0] * p->fn[1] * p->fn[2] * h->nrvars;
+      for (size_t n = 0; n < nf; n++) s = s + p->rf[n] * p->rf[n];
+      h->integral[0] = s + h->integral[0];
+      h->integral[1] = (double)(h->nrvars * p->mx[0] * p->mx[1] * p->mx[2]) + h->integral[1];
+    }
+    return sqrt(h->integral[0] / h->integral[1]);
+  }
+  double comp[10] = {0};
+  h->integral[1] = 0.0;
+  for (int a = 0; a < nlev(h, level); a++) {
+    OPatch* p = lev_patch(h, level, a);
+    residual(h, p);
+    size_t nc = (size_t)p->fn[0] * p->fn[1] * p->fn[2];
+    for (int v = 0; v < h->nrvars; v++) {
+      double s = 0.0;
+      for (size_t n = 0; n < nc; n++) s = s + p->rf[v * nc + n] * p->rf[v * nc + n];
+      comp[v] = s + comp[v];
+    }
+    h->integral[1] = (double)(p->mx[0] * p->mx[1] * p->mx[2]) + h->integral[1];
+  }
+  double mx = 0.0;
+  for (int v = 0; v < h->nrvars; v++) {
+    double e = sqrt(comp[v] / h->integral[1]);
+    if (v == 0 || e > mx) mx = e;
+  }
+  return mx;
+}
+
+int bsamo_residual_norm(bsamo_hier* h, int level, int errortype, double* out) {
+  if (!h || !h->committed || !out) return -1;
+  *out = error_afas(h, level, errortype);
+  return 0;
+}
+
+/* MultigridIterations, afasroutines.f90:48-110 (the plugins' aux updates
+ * are empty for maux = 0 and are skipped) */
+int bsamo_multigrid_iterations(bsamo_hier* h, int finest, int minlevel,
+                               int nsmooth, int maxvcycles, double qerrortol,
+                               int updateauxfreq, int errortype,
+                               int* ncycles, double* residuals) {
+  if (!h || !h->committed) return -1;
+  (void)updateauxfreq;
+  fill_down(h, 2, finest, minlevel);
+  for (int level = finest; level >= 0; level--)
+    for (int a = 0; a < nlev(h, level); a++) get_source(h, lev_patch(h, level, a));
+  for (int level = finest; level >= 0; level--)
+    for (int a = 0; a < nlev(h, level); a++) update_source(h, lev_patch(h, level, a));
+  fill_down(h, 1, finest, minlevel);
+  int it;
+  for (it = 1; it <= maxvcycles; it++) {
+    afas_vcycle(h, finest, minlevel, nsmooth);
+    fill_down(h, 2, finest, minlevel);
+    for (int level = finest; level >= 0; level--)
+      for (int a = 0; a < nlev(h, level); a++) update_source(h, lev_patch(h, level, a));
+    fill_down(h, 1, finest, minlevel);
+    double r = error_afas(h, finest, errortype);
+    if (residuals) residuals[it - 1] = r;
+    if (r < qerrortol) break;
+  }
+  if (ncycles) *ncycles = it > maxvcycles ? maxvcycles : it;
+  return 0;
+}
+
+int bsamo_time_step(bsamo_hier* h, int first, int finest, int minlevel,
+                    int nsmooth, int maxvcycles, double qerrortol,
+                    int updateauxfreq, int errortype, int* ncycles,
+                    double* residuals) {
+  if (!h || !h->committed) return -1;
+  for (int level = 0; level <= finest; level++) set_ghost(h, level, 0);
+  if (first) fill_down(h, 2, finest, minlevel);
+  bsamo_copy_q_to_qold(h, minlevel, finest);
+  return bsamo_multigrid_iterations(h, finest, minlevel, nsmooth, maxvcycles,
+                                    qerrortol, updateauxfreq, errortype,
+                                    ncycles, residuals);
+}
+
+/* splitmix64 (Steele, Lea, Flood 2014) on seed ^ (gidx * golden gamma) */
+double bsamo_uniform_pm1(unsigned long long seed, unsigned long long gidx) {
+  uint64_t z = (uint64_t)seed ^ ((uint64_t)gidx * 0x9E3779B97F4A7C15ULL);
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  z = z ^ (z >> 31);
+  return 2.0 * ((double)(z >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+}

@@ -1,0 +1,102 @@
+/*
+ * CPU oracle for the BSAM 1.2 FAS V-cycle on block-structured patches.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * Fortran (LIBRARY/afasroutines.f90, LIBRARY/boundary.f90,
+ * LIBRARY/gridutilities.f90, LIBRARY/bsamroutines.f90 RootInit/InitSeed/
+ * CopyQToQold/TakeTimeSteps, PROBLEM/CH/problem.f90, PROBLEM/BioGrowth/
+ * problem.f90).  Only the tests, the smoke check and the CPU-baseline leg of
+ * the benchmark may load it; the product library never links it.
+ *
+ * Parity status: UNPINNED by the reference itself.  The reference ships no
+ * tests, golden vectors or fixtures, and no Fortran compiler exists on the
+ * build or GPU machines, so the reference cannot be run.  The oracle is pinned
+ * instead by math-derived known-answer tests (tests/test_oracle_kat.py).
+ *
+ * Arithmetic follows the reference's evaluation order term by term and is
+ * compiled with -ffp-contract=off (no FMA contraction), so the CUDA plain-FP64
+ * path, which uses the same order with explicit round-to-nearest intrinsics,
+ * is expected to agree bit for bit except in reductions.
+ *
+ * Field layout is the reference's Fortran layout (bsamstorage.f90:81-90,
+ * :106-115): q(1-mbc:mx1+mbc, 1-mbc:mx2+mbc, [1-mbc:mx3+mbc | 1], 1:nrvars),
+ * column-major, variable index slowest.  The same layout is used by the CUDA
+ * library's put/get calls, so arrays move between the two unchanged.
+ */
+#ifndef BSAM_ORACLE_H
+#define BSAM_ORACLE_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct bsamo_hier bsamo_hier;
+
+/* problem kinds (same codes as include/bsamg.h) */
+#define BSAMO_PROBLEM_CH 1
+#define BSAMO_PROBLEM_BIOGROWTH 2
+
+/* field codes (same codes as include/bsamg.h) */
+#define BSAMO_FIELD_Q 0
+#define BSAMO_FIELD_QOLD 1
+#define BSAMO_FIELD_QC 2
+#define BSAMO_FIELD_F 3
+#define BSAMO_FIELD_RF 4
+#define BSAMO_FIELD_FTMP 5
+
+/* params: [0]=dt [1]=eps [2]=gamma [3]=lambda [4]=czero; qpo[nrvars] */
+int bsamo_create(int ndims, int nrvars, int mbc, int problem,
+                 const double* params, int nparams, const double* qpo,
+                 bsamo_hier** out);
+int bsamo_destroy(bsamo_hier* h);
+int bsamo_patch_add(bsamo_hier* h, int level, int id, int parent_id,
+                    const int mx[3], const int mglobal[6],
+                    const int mbounds[6], const int mthbc[6],
+                    const double dx[3], const double xlower[3]);
+/* RootInit (bsamroutines.f90:226-440) + InitSeed (:443-510) for one root
+ * grid and levels -1..minlevel below it. */
+int bsamo_build_uniform(bsamo_hier* h, const int mx[3], int minlevel,
+                        const int mthbc[6], const double xlower[3],
+                        const double xupper[3]);
+int bsamo_commit(bsamo_hier* h);
+int bsamo_num_patches(const bsamo_hier* h);
+/* out[0..27]: level,id,parent_id,mx[3],mglobal[6],mbounds[6],mthbc[6],
+ * then 4 unused */
+int bsamo_patch_info(const bsamo_hier* h, int index, int* out, double* dxl);
+size_t bsamo_field_size(const bsamo_hier* h, int id, int field);
+int bsamo_put_field(bsamo_hier* h, int id, int field, const double* a,
+                    size_t n);
+int bsamo_get_field(const bsamo_hier* h, int id, int field, double* a,
+                    size_t n);
+
+/* single operations (tier-(i)/(ii) parity) */
+int bsamo_relax_level_color(bsamo_hier* h, int level, int ipass);
+int bsamo_set_ghost(bsamo_hier* h, int level, int ipass);
+int bsamo_level_relax(bsamo_hier* h, int level, int nsmooth);
+int bsamo_fill_down(bsamo_hier* h, int field, int finestlevel, int minlevel);
+int bsamo_copy_q_to_qold(bsamo_hier* h, int minlevel, int finestlevel);
+int bsamo_vcycle(bsamo_hier* h, int level, int minlevel, int nsmooth);
+int bsamo_residual_norm(bsamo_hier* h, int level, int errortype,
+                        double* out);
+
+/* MultigridIterations (afasroutines.f90:48-110).  residuals[maxvcycles]
+ * receives ErrorAFAS per V-cycle; *ncycles the number run. */
+int bsamo_multigrid_iterations(bsamo_hier* h, int finestlevel, int minlevel,
+                               int nsmooth, int maxvcycles, double qerrortol,
+                               int updateauxfreq, int errortype,
+                               int* ncycles, double* residuals);
+/* One TakeTimeSteps step (bsamroutines.f90:657-797) on a fixed mesh:
+ * SetGhost(l,0) for l=0..finest, FillDown(q) if first, CopyQToQold,
+ * MultigridIterations. */
+int bsamo_time_step(bsamo_hier* h, int first, int finestlevel, int minlevel,
+                    int nsmooth, int maxvcycles, double qerrortol,
+                    int updateauxfreq, int errortype, int* ncycles,
+                    double* residuals);
+
+/* seeded inputs: U(-1,1) from splitmix64 on a global cell index */
+double bsamo_uniform_pm1(unsigned long long seed, unsigned long long gidx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

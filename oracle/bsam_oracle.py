@@ -1,0 +1,172 @@
+"""ctypes view of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py
+import this module.  The method names mirror the CUDA library's Python host
+class (bsam1.2_gb300.Hierarchy) so a parity test can drive both the same way.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .build import build_oracle  # noqa: F401  (package-relative when imported as oracle.*)
+
+FIELD = {"q": 0, "qold": 1, "qc": 2, "f": 3, "rf": 4, "ftmp": 5}
+PROBLEM = {"ch": 1, "biogrowth": 2}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle()
+        L = ctypes.CDLL(path)
+        I, D, P = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+        IP = ctypes.POINTER(ctypes.c_int)
+        DP = ctypes.POINTER(ctypes.c_double)
+        L.bsamo_create.argtypes = [I, I, I, I, DP, I, DP, ctypes.POINTER(P)]
+        L.bsamo_destroy.argtypes = [P]
+        L.bsamo_patch_add.argtypes = [P, I, I, I, IP, IP, IP, IP, DP, DP]
+        L.bsamo_build_uniform.argtypes = [P, IP, I, IP, DP, DP]
+        L.bsamo_commit.argtypes = [P]
+        L.bsamo_num_patches.argtypes = [P]
+        L.bsamo_patch_info.argtypes = [P, I, IP, DP]
+        L.bsamo_field_size.argtypes = [P, I, I]
+        L.bsamo_field_size.restype = ctypes.c_size_t
+        L.bsamo_put_field.argtypes = [P, I, I, DP, ctypes.c_size_t]
+        L.bsamo_get_field.argtypes = [P, I, I, DP, ctypes.c_size_t]
+        L.bsamo_relax_level_color.argtypes = [P, I, I]
+        L.bsamo_set_ghost.argtypes = [P, I, I]
+        L.bsamo_level_relax.argtypes = [P, I, I]
+        L.bsamo_fill_down.argtypes = [P, I, I, I]
+        L.bsamo_copy_q_to_qold.argtypes = [P, I, I]
+        L.bsamo_vcycle.argtypes = [P, I, I, I]
+        L.bsamo_residual_norm.argtypes = [P, I, I, DP]
+        L.bsamo_multigrid_iterations.argtypes = [P, I, I, I, I, D, I, I, IP, DP]
+        L.bsamo_time_step.argtypes = [P, I, I, I, I, I, D, I, I, IP, DP]
+        L.bsamo_uniform_pm1.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong]
+        L.bsamo_uniform_pm1.restype = D
+        _lib = L
+    return _lib
+
+
+def _ia(x, n):
+    a = (ctypes.c_int * n)(*[int(v) for v in x])
+    return a
+
+
+def _da(x, n):
+    return (ctypes.c_double * n)(*[float(v) for v in x])
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError(f"oracle {what} failed with status {rc}")
+
+
+class OracleHierarchy:
+    """A patch hierarchy held by the CPU oracle."""
+
+    def __init__(self, ndims, nrvars, problem, params, qpo=None, mbc=1):
+        L = lib()
+        self.ndims, self.nrvars = ndims, nrvars
+        h = ctypes.c_void_p()
+        p = _da(params, len(params))
+        q = _da(qpo if qpo is not None else [0.0] * nrvars, nrvars)
+        _check(L.bsamo_create(ndims, nrvars, mbc, PROBLEM[problem], p, len(params), q,
+                              ctypes.byref(h)), "create")
+        self.h = h
+        self.patches = []
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().bsamo_destroy(self.h)
+            self.h = None
+
+    def add_patch(self, level, id, parent_id, mx, mglobal, mbounds, mthbc, dx, xlower):
+        _check(lib().bsamo_patch_add(self.h, level, id, parent_id, _ia(mx, 3), _ia(mglobal, 6),
+                                     _ia(mbounds, 6), _ia(mthbc, 6), _da(dx, 3),
+                                     _da(xlower, 3)), "patch_add")
+
+    def build_uniform(self, mx, minlevel, mthbc, xlower, xupper):
+        _check(lib().bsamo_build_uniform(self.h, _ia(mx, 3), minlevel, _ia(mthbc, 6),
+                                         _da(xlower, 3), _da(xupper, 3)), "build_uniform")
+
+    def commit(self):
+        _check(lib().bsamo_commit(self.h), "commit")
+
+    def patch_table(self):
+        L = lib()
+        out = []
+        for n in range(L.bsamo_num_patches(self.h)):
+            a = (ctypes.c_int * 28)()
+            d = (ctypes.c_double * 6)()
+            _check(L.bsamo_patch_info(self.h, n, a, d), "patch_info")
+            a = list(a)
+            out.append(dict(level=a[0], id=a[1], parent_id=a[2], mx=a[3:6], mglobal=a[6:12],
+                            mbounds=a[12:18], mthbc=a[18:24], dx=list(d)[0:3],
+                            xlower=list(d)[3:6]))
+        return out
+
+    def field_size(self, pid, field):
+        return lib().bsamo_field_size(self.h, pid, FIELD[field])
+
+    def put(self, pid, field, arr):
+        a = np.ascontiguousarray(np.asarray(arr, dtype=np.float64).ravel(order="F"))
+        _check(lib().bsamo_put_field(self.h, pid, FIELD[field],
+                                     a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), a.size),
+               "put_field")
+
+    def get(self, pid, field):
+        n = self.field_size(pid, field)
+        a = np.empty(n, dtype=np.float64)
+        _check(lib().bsamo_get_field(self.h, pid, FIELD[field],
+                                     a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n),
+               "get_field")
+        return a
+
+    def relax_level_color(self, level, ipass):
+        _check(lib().bsamo_relax_level_color(self.h, level, ipass), "relax")
+
+    def set_ghost(self, level, ipass):
+        _check(lib().bsamo_set_ghost(self.h, level, ipass), "set_ghost")
+
+    def level_relax(self, level, nsmooth):
+        _check(lib().bsamo_level_relax(self.h, level, nsmooth), "level_relax")
+
+    def fill_down(self, field, finest, minlevel):
+        _check(lib().bsamo_fill_down(self.h, {"f": 1, "q": 2}[field], finest, minlevel), "fill_down")
+
+    def copy_q_to_qold(self, minlevel, finest):
+        _check(lib().bsamo_copy_q_to_qold(self.h, minlevel, finest), "copy_q_to_qold")
+
+    def vcycle(self, level, minlevel, nsmooth):
+        _check(lib().bsamo_vcycle(self.h, level, minlevel, nsmooth), "vcycle")
+
+    def residual_norm(self, level, errortype=1):
+        r = ctypes.c_double()
+        _check(lib().bsamo_residual_norm(self.h, level, errortype, ctypes.byref(r)), "resid")
+        return r.value
+
+    def multigrid_iterations(self, finest, minlevel, nsmooth=2, maxvcycles=20, tol=1e-9,
+                             updateauxfreq=1, errortype=1):
+        n = ctypes.c_int()
+        res = (ctypes.c_double * maxvcycles)()
+        _check(lib().bsamo_multigrid_iterations(self.h, finest, minlevel, nsmooth, maxvcycles,
+                                                tol, updateauxfreq, errortype, ctypes.byref(n),
+                                                res), "multigrid_iterations")
+        return n.value, list(res)[: n.value]
+
+    def time_step(self, first, finest, minlevel, nsmooth=2, maxvcycles=20, tol=1e-9,
+                  updateauxfreq=1, errortype=1):
+        n = ctypes.c_int()
+        res = (ctypes.c_double * maxvcycles)()
+        _check(lib().bsamo_time_step(self.h, int(bool(first)), finest, minlevel, nsmooth,
+                                     maxvcycles, tol, updateauxfreq, errortype, ctypes.byref(n),
+                                     res), "time_step")
+        return n.value, list(res)[: n.value]
+
+
+def uniform_pm1(seed, gidx):
+    return lib().bsamo_uniform_pm1(seed, gidx)
