@@ -1,0 +1,388 @@
+"""Benchmark: Cahn-Hilliard time steps per second at residual <= tol, on one
+GB300 per rank, batched + mixed precision vs the plain FP64 path.
+
+Default workload (ch3d-256): 3D CH on a uniform 256^3 periodic grid,
+eps = 0.02, dt = 5e-4, FAS V(2,2), levels 256^3 .. 2^3 (minlevel -7),
+residual tolerance 1e-8, spinodal start phi0 = 0.1 + 0.05*U(-1,1) from a
+seeded splitmix64 stream, mu0 from phi0.  A step is one CH time step
+(CopyQToQold + MultigridIterations to tolerance).  --warmup + --steps time
+steps run in each arm (3 + 17 = 20 by default, the configuration's 20 time
+steps); the max-norm difference of phi between the mixed arm and the plain
+FP64 arm (which is bit-identical to the CPU oracle) after those steps is
+reported as error_vs_fp64.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Under torchrun with N > 1 every rank runs an independent replica on its own
+GPU (the path does not shard); value is the sum over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "CH steps/s at resid≤1e-8: batched+mixed vs plain FP64, 1 GB300; p50/p99 ms"
+
+WORKLOADS = {
+    "ch3d-256": dict(ndims=3, n=256, minlevel=-7, mthbc=[2, 2, 2, 2, 2, 2], eps=0.02, dt=5e-4, tol=1e-8,
+                     mean=0.1, amp=0.05, seed=20240503,
+                     desc="3D Cahn-Hilliard 256^3 periodic, eps=0.02, dt=5e-4, V(2,2), resid<=1e-8"),
+    "ch2d-128": dict(ndims=2, n=128, minlevel=-6, mthbc=[2, 2, 2, 2, 10, 10], eps=0.01, dt=1e-3, tol=1e-9,
+                     mean=0.0, amp=0.05, seed=20240503,
+                     desc="2D Cahn-Hilliard 128^2 periodic, eps=0.01, dt=1e-3, V(2,2), resid<=1e-9"),
+}
+NSMOOTH = 2
+MAXV = 30
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-reduce across ranks (gloo on CPU tensors); no-op at N=1."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo")
+            self.td = td
+            self.pg = True
+
+    def barrier(self):
+        if self.pg:
+            self.td.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.td.destroy_process_group()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(workload, kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return d.get(workload, {}).get(kernel)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        rows = [r.split(",") for r in out.strip().splitlines() if r.strip()]
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def make_hierarchy(pkg, ctx, w):
+    nd, n = w["ndims"], w["n"]
+    h = pkg.Hierarchy(ctx, nd, 2, "ch", [w["dt"], w["eps"]])
+    h.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
+    h.commit()
+    return h
+
+
+def initial_q(pkg, w):
+    nd, n = w["ndims"], w["n"]
+    q = pkg.initial.ch_spinodal((n,) * nd, w["eps"], 1.0 / n, seed=w["seed"], mean=w["mean"], amp=w["amp"])
+    return np.asfortranarray(q).ravel(order="F")
+
+
+def reset(h, q0, w):
+    h.put_flat(0, "q", q0)
+    h.set_ghost(0, 0)
+    h.copy_q_to_qold(w["minlevel"], 0)
+
+
+def run_arm(h, q0, w, mode, steps, warmup, dist, clocks=None):
+    """warmup + timed steps; returns dict of timings and the V-cycle counts."""
+    reset(h, q0, w)
+    vc = []
+    for s in range(warmup):
+        n, _ = h.time_step(s == 0, 0, w["minlevel"], NSMOOTH, MAXV, w["tol"], mode=mode, strict=True)
+        vc.append(n)
+    h.sync()
+    dist.barrier()
+    if clocks:
+        clocks.start()
+    l0 = h.launch_count()
+    h.mark(0)
+    per = []
+    for s in range(steps):
+        n, res = h.time_step(warmup == 0 and s == 0, 0, w["minlevel"], NSMOOTH, MAXV, w["tol"], mode=mode,
+                             strict=True)
+        h.mark(1 + (s % 60))
+        vc.append(n)
+        per.append(h.elapsed_ms(0 if s == 0 else 1 + ((s - 1) % 60), 1 + (s % 60)))
+    h.sync()
+    ck = clocks.stop() if clocks else None
+    total = h.elapsed_ms(0, 1 + ((steps - 1) % 60))
+    launches = h.launch_count() - l0
+    dist.barrier()
+    return dict(total_ms=total, per_ms=per, vcycles=vc, launches=launches, clocks=ck,
+                final_resid=res[-1])
+
+
+def run_e2e(pkg, h, q0, w, mode, steps, warmup, dist):
+    """Public-API end to end: per step, H2D of q from pinned host memory,
+    the time step, D2H of q into pinned host memory (two pinned buffers
+    alternate as input and output, as a host that keeps its state would)."""
+    bufs = [pkg.pin(np.array(q0, copy=True)), pkg.pin(np.empty_like(q0))]
+    reset(h, q0, w)
+    first = True
+    cur = 0
+    for s in range(warmup + steps):
+        if s == warmup:
+            dist.barrier()
+            h.mark(10)
+        h.put_flat(0, "q", bufs[cur])
+        h.time_step(first, 0, w["minlevel"], NSMOOTH, MAXV, w["tol"], mode=mode, strict=True)
+        h.get(0, "q", out=bufs[1 - cur])
+        cur = 1 - cur
+        first = False
+    h.mark(11)
+    ms = h.elapsed_ms(10, 11)
+    dist.barrier()
+    for b in bufs:
+        pkg.unpin(b)
+    return ms, bufs[0].nbytes
+
+
+def pct(x, p):
+    return float(np.percentile(np.asarray(x), p))
+
+
+def cpu_baseline(pkg, w, vcycles_per_step, nvc=2):
+    """The CPU oracle (C restatement of the reference, 1 thread) on the same
+    workload: nvc V-cycles of the first step, scaled to steps/s with the
+    V-cycle count per step of the FP64 run."""
+    from oracle.bsam_oracle import OracleHierarchy
+    nd, n = w["ndims"], w["n"]
+    o = OracleHierarchy(nd, 2, "ch", [w["dt"], w["eps"]])
+    o.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
+    o.commit()
+    o.put(0, "q", initial_q(pkg, w))
+    o.set_ghost(0, 0)
+    o.fill_down("q", 0, w["minlevel"])
+    o.copy_q_to_qold(w["minlevel"], 0)
+    t = time.perf_counter()
+    o.multigrid_iterations(0, w["minlevel"], NSMOOTH, nvc, 0.0)
+    dt = time.perf_counter() - t
+    per_v = dt / nvc
+    return per_v, dict(value=1.0 / (per_v * vcycles_per_step), unit="steps/s", cores=1, kind="port",
+                       sample=f"oracle (C restatement of the reference, 1 thread, -O2 -ffp-contract=off) "
+                              f"running {nvc} V-cycles of the first time step of the same {w['n']}^{nd} "
+                              f"workload ({dt:.1f} s); steps/s = 1/(t_vcycle x {vcycles_per_step:.2f} "
+                              f"V-cycles per step of the FP64 run)")
+
+
+def reference_arm(args, w, dist):
+    """--impl reference: the reference algorithm on the host cores (the CPU
+    oracle; the reference itself is Fortran and no Fortran compiler exists
+    on these machines).  Each step is a bounded sample: one V-cycle of the
+    workload's first time step; a full first time step during warm-up gives
+    the V-cycles per step used to convert to steps/s."""
+    if dist.rank != 0:
+        return
+    import __graft_entry__ as ge
+    pkg_initial = ge.load_package().initial  # numpy input generator only; libbsamg is not loaded
+    from oracle.bsam_oracle import OracleHierarchy
+    nd, n = w["ndims"], w["n"]
+    o = OracleHierarchy(nd, 2, "ch", [w["dt"], w["eps"]])
+    o.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
+    o.commit()
+    q = pkg_initial.ch_spinodal((n,) * nd, w["eps"], 1.0 / n, seed=w["seed"], mean=w["mean"], amp=w["amp"])
+    o.put(0, "q", q)
+    o.set_ghost(0, 0)
+    o.copy_q_to_qold(w["minlevel"], 0)
+    t = time.perf_counter()
+    nv, _ = o.time_step(True, 0, w["minlevel"], NSMOOTH, MAXV, w["tol"])
+    t_step = time.perf_counter() - t
+    for _ in range(max(0, args.warmup - 1)):
+        o.multigrid_iterations(0, w["minlevel"], NSMOOTH, 1, 0.0)
+    ts = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        o.multigrid_iterations(0, w["minlevel"], NSMOOTH, 1, 0.0)
+        ts.append(time.perf_counter() - t)
+    per_v = statistics.mean(ts)
+    value = 1.0 / (per_v * nv)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_v * nv * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded splitmix64 spinodal start)",
+        "config": {"workload": args.workload, "desc": w["desc"]},
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": 1, "kind": "port",
+                         "sample": f"each step = one V-cycle of the first time step; a full first step "
+                                   f"({nv} V-cycles, {t_step:.1f} s) measured during warm-up"},
+        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "vcycles_per_step": nv, "first_step_s": t_step,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=17)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ch3d-256", choices=list(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    dist = Dist()
+    if args.impl == "reference":
+        reference_arm(args, w, dist)
+        dist.close()
+        return
+    import __graft_entry__ as ge
+    ge._load_build_module().build()
+    pkg = ge.load_package()
+    ctx = pkg.Context(dist.local)
+    h = make_hierarchy(pkg, ctx, w)
+    q0 = pkg.pin(initial_q(pkg, w))
+    N = w["n"] ** w["ndims"]
+
+    clocks = Clocks(dist.local)
+    mixed = run_arm(h, q0, w, "mixed", args.steps, args.warmup, dist, clocks)
+    q_mixed = h.get(0, "q")
+    ms_mixed = h.time_smoother(0, "mixed", reps=20)
+    fp64 = run_arm(h, q0, w, "fp64", args.steps, args.warmup, dist)
+    q_fp64 = h.get(0, "q")
+    ms_fp64 = h.time_smoother(0, "fp64", reps=10)
+    e2e_ms, qbytes = (None, 0) if args.no_e2e else run_e2e(pkg, h, q0, w, "mixed", args.steps,
+                                                           min(args.warmup, 1), dist)
+
+    t_mixed = dist.max(mixed["total_ms"])
+    t_fp64 = dist.max(fp64["total_ms"])
+    value = dist.ws * args.steps / (t_mixed * 1e-3)
+    v_fp64 = dist.ws * args.steps / (t_fp64 * 1e-3)
+    nphi = q_fp64.size // 2
+    err = float(np.max(np.abs(q_mixed[:nphi] - q_fp64[:nphi])) / np.max(np.abs(q_fp64[:nphi])))
+    peak, peak_kind = peaks()
+    b_mixed = 18.0 * N  # e read (N*2*4) + g,phib,e-write of one colour (N/2*(2*4+4+2*4))
+    b_fp64 = 32.0 * N   # q read (N*2*8) + f read and q write of one colour (N/2*(2*8+2*8))
+    ach = b_mixed / (ms_mixed * 1e-3) / 1e9
+    ach64 = b_fp64 / (ms_fp64 * 1e-3) / 1e9
+    vps_m = statistics.mean(mixed["vcycles"][args.warmup:])
+    vps_f = statistics.mean(fp64["vcycles"][args.warmup:])
+    if dist.rank != 0:
+        dist.close()
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": dist.ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_mixed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded splitmix64 spinodal start, mu0 from phi0)",
+        "config": {"workload": args.workload, "desc": w["desc"], "n": w["n"], "ndims": w["ndims"],
+                   "minlevel": w["minlevel"], "nsmooth": NSMOOTH, "tol": w["tol"],
+                   "parallelism": f"replicas x{dist.ws}",
+                   "l2": "inputs larger than L2 (q+qold 550 MB FP64 at 256^3)"},
+        "p50_ms": pct(mixed["per_ms"], 50), "p99_ms": pct(mixed["per_ms"], 99),
+        "vcycles_per_step": vps_m,
+        "plain_fp64": {"value": v_fp64, "unit": "steps/s", "ms_per_step": t_fp64 / args.steps,
+                       "p50_ms": pct(fp64["per_ms"], 50), "p99_ms": pct(fp64["per_ms"], 99),
+                       "vcycles_per_step": vps_f, "gpu_launches": fp64["launches"]},
+        "speedup_mixed_vs_fp64": value / v_fp64,
+        "error_vs_fp64": {"max_rel_phi": err, "after_steps": args.warmup + args.steps},
+        "dof_sweeps_per_s": None,
+        "roofline": {"bound": "hbm", "kernel": "k_mx_relax (FP32 colour sweep, finest level)",
+                     "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                     "peak_kind": peak_kind, "bytes_per_launch": b_mixed, "ms_per_launch": ms_mixed,
+                     "traffic": ncu_traffic(args.workload, "k_mx_relax")},
+        "roofline_fp64": {"bound": "fp64 pipe", "kernel": "k_relax (FP64 colour sweep, finest level)",
+                          "achieved_hbm": ach64, "peak_hbm": peak, "frac_hbm": ach64 / peak,
+                          "bytes_per_launch": b_fp64, "ms_per_launch": ms_fp64,
+                          "traffic": ncu_traffic(args.workload, "k_relax")},
+        "gpu_launches": mixed["launches"],
+        "clocks": mixed["clocks"],
+    }
+    # 4 colour sweeps of the finest level per pass pair, 2*NSMOOTH*2 sweeps per V-cycle on the finest level
+    line["dof_sweeps_per_s"] = 2 * N * (2 * NSMOOTH) * vps_m * value
+    if e2e_ms is not None:
+        line["e2e"] = {"value": dist.ws * args.steps / (e2e_ms * 1e-3), "unit": "steps/s",
+                       "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes}
+    if not args.no_cpu_baseline:
+        per_v, cb = cpu_baseline(pkg, w, vps_f)
+        line["cpu_baseline"] = cb
+    print(json.dumps(line), flush=True)
+    h.close()
+    ctx.close()
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -3,5 +3,5 @@
 The compute path is libbsamg.so (CUDA C++ behind the C ABI in
 include/bsamg.h); this package is its Python host mirror.
 """
-from .api import BsamgError, Context, Hierarchy, exported_symbols, lib  # noqa: F401
+from .api import BsamgError, Context, Hierarchy, exported_symbols, lib, pin, unpin  # noqa: F401
 from . import initial  # noqa: F401

@@ -65,6 +65,11 @@ def lib():
         "bsamg_sync": ([P], I),
         "bsamg_stream": ([P, ctypes.POINTER(P)], I),
         "bsamg_launch_count": ([P, ctypes.POINTER(ctypes.c_longlong)], I),
+        "bsamg_mark": ([P, I], I),
+        "bsamg_elapsed_ms": ([P, I, I, DP], I),
+        "bsamg_time_smoother": ([P, I, I, I, DP], I),
+        "bsamg_host_register": ([P, SZ], I),
+        "bsamg_host_unregister": ([P], I),
         "bsamg_strerror": ([I], ctypes.c_char_p),
         "bsamg_last_error_detail": ([], ctypes.c_char_p),
     }
@@ -222,7 +227,31 @@ class Hierarchy:
         _ck(lib().bsamg_stream(self.h, ctypes.byref(s)), "bsamg_stream")
         return s.value
 
+    def mark(self, slot):
+        _ck(lib().bsamg_mark(self.h, slot), "bsamg_mark")
+
+    def elapsed_ms(self, a, b):
+        ms = ctypes.c_double()
+        _ck(lib().bsamg_elapsed_ms(self.h, a, b, ctypes.byref(ms)), "bsamg_elapsed_ms")
+        return ms.value
+
+    def time_smoother(self, level, mode="fp64", reps=20):
+        ms = ctypes.c_double()
+        _ck(lib().bsamg_time_smoother(self.h, level, MODE[mode], reps, ctypes.byref(ms)),
+            "bsamg_time_smoother")
+        return ms.value
+
     def launch_count(self):
         n = ctypes.c_longlong()
         _ck(lib().bsamg_launch_count(self.h, ctypes.byref(n)), "bsamg_launch_count")
         return n.value
+
+
+def pin(arr):
+    """Page-lock a numpy array's memory (for fast put/get); returns arr."""
+    _ck(lib().bsamg_host_register(arr.ctypes.data_as(ctypes.c_void_p), arr.nbytes), "bsamg_host_register")
+    return arr
+
+
+def unpin(arr):
+    _ck(lib().bsamg_host_unregister(arr.ctypes.data_as(ctypes.c_void_p)), "bsamg_host_unregister")

@@ -15,8 +15,10 @@
 using namespace bsamg;
 
 namespace {
-
 thread_local std::string g_detail;
+}  // namespace
+
+namespace bsamg {
 
 int cuda_fail(cudaError_t e, const char* what) {
   g_detail = std::string(what) + ": " + cudaGetErrorString(e);
@@ -163,6 +165,10 @@ int enq_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype)
   CK(cudaMemcpyAsync(H.h_nonfinite, H.d_nonfinite, sizeof(int), cudaMemcpyDeviceToHost, H.s));
   return BSAMG_OK;
 }
+
+}  // namespace bsamg
+
+namespace {
 
 int get_graph(Hier& H, int mode, int finest, int minlevel, int nsmooth, int errortype, Hier::GraphRec** out) {
   auto key = std::make_tuple(mode, finest, minlevel, nsmooth, errortype);
@@ -491,6 +497,7 @@ int commit(Hier& H) {
     D.level = P.level;
     D.oq = P.oq; D.oqold = P.oqold; D.oqc = P.oqc; D.of = P.of; D.orf = P.orf; D.oftmp = P.oftmp;
     D.sq = P.sq; D.sc = P.sc; D.sf = P.sf;
+    D.eq = P.e_oq; D.ecq = P.e_oqc; D.eg = P.e_of; D.ephi = P.e_ophi;
     D.h = P.dx[0];
     coefficients(H, P.dx[0], D.c);
   }
@@ -535,6 +542,8 @@ int commit(Hier& H) {
 void release(Hier& H) {
   cudaSetDevice(H.ctx->device);
   if (H.s) cudaStreamSynchronize(H.s);
+  for (int m = 0; m < 64; m++)
+    if (H.marks[m]) cudaEventDestroy(H.marks[m]);
   for (auto& kv : H.graphs)
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
   H.graphs.clear();
@@ -801,6 +810,50 @@ int bsamg_stream(bsamg_hier* h, void** stream) {
 int bsamg_launch_count(const bsamg_hier* h, long long* n) {
   if (!h || !n) return BSAMG_ERR_ARG;
   *n = h->launches;
+  return BSAMG_OK;
+}
+
+int bsamg_mark(bsamg_hier* h, int slot) {
+  if (!h || !h->committed || slot < 0 || slot >= 64) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  if (!h->marks[slot]) CK(cudaEventCreate(&h->marks[slot]));
+  CK(cudaEventRecord(h->marks[slot], h->s));
+  return BSAMG_OK;
+}
+
+int bsamg_elapsed_ms(bsamg_hier* h, int a, int b, double* ms) {
+  if (!h || !ms || a < 0 || b < 0 || a >= 64 || b >= 64 || !h->marks[a] || !h->marks[b]) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  CK(cudaEventSynchronize(h->marks[b]));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, h->marks[a], h->marks[b]));
+  *ms = t;
+  return BSAMG_OK;
+}
+
+int bsamg_time_smoother(bsamg_hier* h, int level, int mode, int reps, double* ms_per_launch) {
+  if (!h || !h->committed || !level_ok(*h, level) || reps < 1 || !ms_per_launch) return BSAMG_ERR_ARG;
+  if (mode != BSAMG_MODE_FP64 && mode != BSAMG_MODE_MIXED) return BSAMG_ERR_ARG;
+  RET(set_device(*h));
+  RET(bsamg_mark(h, 62));
+  for (int r = 0; r < reps; r++)
+    RET(mode == BSAMG_MODE_FP64 ? enq_relax(*h, level, 1 + (r & 1)) : mixed_enq_relax(*h, level, 1 + (r & 1)));
+  RET(bsamg_mark(h, 63));
+  double ms;
+  RET(bsamg_elapsed_ms(h, 62, 63, &ms));
+  *ms_per_launch = ms / reps;
+  return BSAMG_OK;
+}
+
+int bsamg_host_register(void* ptr, size_t bytes) {
+  if (!ptr || !bytes) return BSAMG_ERR_ARG;
+  CK(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  return BSAMG_OK;
+}
+
+int bsamg_host_unregister(void* ptr) {
+  if (!ptr) return BSAMG_ERR_ARG;
+  CK(cudaHostUnregister(ptr));
   return BSAMG_OK;
 }
 

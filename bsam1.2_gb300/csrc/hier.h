@@ -62,6 +62,7 @@ struct Hier {
   long long q_region = 0, q_len = 0, qold_region = 0;
   float* fpool = nullptr;
   size_t fpool_elems = 0;
+  size_t e_len = 0;  // leading FP32 elements holding every patch's correction e
   size_t bytes = 0;
 
   LevelT lev[kNLev];
@@ -81,6 +82,7 @@ struct Hier {
     long long nlaunch = 0;
   };
   std::map<std::tuple<int, int, int, int, int>, GraphRec> graphs;
+  cudaEvent_t marks[64] = {};
 
   LevelT& L(int level) { return lev[level + kMaxDepth]; }
   const LevelT& L(int level) const { return lev[level + kMaxDepth]; }
@@ -95,6 +97,16 @@ struct Hier {
     return c;
   }
 };
+
+// schedule helpers shared by the FP64 and mixed paths (hier.cu)
+int cuda_fail(cudaError_t e, const char* what);
+int after_launch(Hier& H, int n);
+int set_device(const Hier& H);
+int enq_set_ghost(Hier& H, int level, int ipass);
+int enq_fill_down(Hier& H, int field, int finest, int minlevel);
+int enq_update_source(Hier& H, int finest);
+int enq_norm(Hier& H, int level, int errortype);
+int enq_relax(Hier& H, int level, int ipass);
 
 }  // namespace bsamg
 

@@ -32,6 +32,10 @@ struct PatchDev {
   int pad;
   long long oq, oqold, oqc, of, orf, oftmp;  // element offsets into the pool
   long long sq, sc, sf;                      // elements per variable plane
+  // mixed path, offsets into the FP32 pool: correction e (ghosted, like q),
+  // its coarse image ec (like qc), correction right-hand side g (interior,
+  // like f) and the frozen base phase field phib (interior, one plane)
+  long long eq, ecq, eg, ephi;
   // Plugin coefficients for this patch's spacing, computed on the host with
   // the reference's expressions (CH/problem.f90:339-347, :411-413,
   // BioGrowth/problem.f90:276-278, :333-336):

@@ -15,5 +15,7 @@ int mixed_prepare(Hier& H, int finest, int minlevel);
 // one outer defect-correction iteration, ending with the FP64 norm copied
 // to H.h_norm (captured into a CUDA graph by the caller)
 int mixed_enq_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype);
+// one FP32 colour sweep of the correction smoother on `level`
+int mixed_enq_relax(Hier& H, int level, int ipass);
 
 }  // namespace bsamg

@@ -145,6 +145,22 @@ int bsamg_stream(bsamg_hier* h, void** stream);
 /* Kernel launches issued by this hierarchy since creation. */
 int bsamg_launch_count(const bsamg_hier* h, long long* n);
 
+/* Timing support (no reference counterpart: measurement hooks).
+ * bsamg_mark records CUDA event `slot` (0..63) on the hierarchy's stream;
+ * bsamg_elapsed_ms waits for event b and returns the time from a to b. */
+int bsamg_mark(bsamg_hier* h, int slot);
+int bsamg_elapsed_ms(bsamg_hier* h, int a, int b, double* ms);
+/* Launches the colour smoother of `level` reps times (alternating red and
+ * black) in the given mode on the current state and returns the mean device
+ * time of one launch; the state is modified. */
+int bsamg_time_smoother(bsamg_hier* h, int level, int mode, int reps,
+                        double* ms_per_launch);
+
+/* Page-locks (pins) an existing host buffer so put/get copies run at full
+ * PCIe/NVLink-C2C speed; a Fortran host can pin its node arrays once. */
+int bsamg_host_register(void* ptr, size_t bytes);
+int bsamg_host_unregister(void* ptr);
+
 const char* bsamg_strerror(int status);
 /* Last CUDA error text seen by the library (thread-local), or "". */
 const char* bsamg_last_error_detail(void);
