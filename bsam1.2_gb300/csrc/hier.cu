@@ -443,6 +443,8 @@ int commit(Hier& H) {
     }
     if (H.ndims == 2 && P.level > 0 && P.parent >= 0 && (P.mx[0] < 4 || P.mx[1] < 4))
       return BSAMG_ERR_UNSUPPORTED;  // Interpolate2D reads cells 1..2 from each side
+    if (H.ndims == 3 && P.level > 0)
+      return BSAMG_ERR_UNSUPPORTED;  // 3D coarse-fine interpolation (Interpolate3D) is not built yet
   }
   // level lists in insertion (visiting) order
   for (size_t n = 0; n < H.patches.size(); n++) H.L(H.patches[n].level).patches.push_back((int)n);
