@@ -68,6 +68,7 @@ def lib():
         "bsamg_mark": ([P, I], I),
         "bsamg_elapsed_ms": ([P, I, I, DP], I),
         "bsamg_time_smoother": ([P, I, I, I, DP], I),
+        "bsamg_ch_residual_norm_noalloc": ([P, P, I, IP, D, D, D, I, P, P], I),
         "bsamg_host_register": ([P, SZ], I),
         "bsamg_host_unregister": ([P], I),
         "bsamg_strerror": ([I], ctypes.c_char_p),
@@ -255,3 +256,13 @@ def pin(arr):
 
 def unpin(arr):
     _ck(lib().bsamg_host_unregister(arr.ctypes.data_as(ctypes.c_void_p)), "bsamg_host_unregister")
+
+
+def ch_residual_norm_noalloc(q_dev, f_dev, ndims, mx, h, dt, eps, norm_out_dev, errortype=1, stream=None):
+    """Allocation-free ErrorAFAS of one CH patch on caller-owned device buffers
+    (raw device addresses as ints); writes the norm to the device double at
+    norm_out_dev.  See bsamg_ch_residual_norm_noalloc in include/bsamg.h."""
+    _ck(lib().bsamg_ch_residual_norm_noalloc(ctypes.c_void_p(q_dev), ctypes.c_void_p(f_dev), ndims,
+                                              _ia(list(mx) + [1] * (3 - len(mx)), 3), h, dt, eps, errortype,
+                                              ctypes.c_void_p(norm_out_dev), ctypes.c_void_p(stream)),
+        "bsamg_ch_residual_norm_noalloc")

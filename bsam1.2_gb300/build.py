@@ -18,6 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 UNITS = {
     "fp64.cu": ["--fmad=false"],
+    "noalloc.cu": ["--fmad=false"],
     "mixed.cu": [],
     "hier.cu": [],
     "ghostc.cpp": [],

@@ -156,6 +156,28 @@ int bsamg_elapsed_ms(bsamg_hier* h, int a, int b, double* ms);
 int bsamg_time_smoother(bsamg_hier* h, int level, int mode, int reps,
                         double* ms_per_launch);
 
+/* Allocation-free convergence norm of one CH patch.  No counterpart in the
+ * reference: it exists for callers that cannot let a library call
+ * cudaMalloc -- hosts whose device memory is owned by their own allocator
+ * (a PyTorch caching allocator, a Fortran code with a fixed device-memory
+ * plan) and serving loops that must not trigger the device-wide
+ * synchronisation cudaMalloc/cudaFree imply while other streams run.
+ * q (ghosted, nrvars = 2) and f (interior) are the caller's device arrays in
+ * the Fortran layout above; the ErrorAFAS norm (errortype 1 or 2) is written
+ * to the caller's device double *norm_out, on `stream` (a cudaStream_t, or
+ * NULL for the default stream).  The call allocates nothing: its block
+ * partial sums live in a fixed file-scope device array, so a patch may have
+ * at most BSAMG_NOALLOC_MAX_CELLS interior cells (larger patches return
+ * BSAMG_ERR_ARG).  Every call on a device shares that array, so calls whose
+ * kernels overlap on the GPU race; order them on one stream.  The first call
+ * on a device looks up the array's address: make it before any stream
+ * capture.  Agrees bit for bit with bsamg_residual_norm on the same data. */
+#define BSAMG_NOALLOC_MAX_CELLS 16777216
+int bsamg_ch_residual_norm_noalloc(const double* q, const double* f,
+                                   int ndims, const int mx[3], double h,
+                                   double dt, double eps, int errortype,
+                                   double* norm_out, void* stream);
+
 /* Page-locks (pins) an existing host buffer so put/get copies run at full
  * PCIe/NVLink-C2C speed; a Fortran host can pin its node arrays once. */
 int bsamg_host_register(void* ptr, size_t bytes);
