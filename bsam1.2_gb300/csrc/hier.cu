@@ -166,12 +166,7 @@ int enq_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype)
   return BSAMG_OK;
 }
 
-}  // namespace bsamg
-
-namespace {
-
-int get_graph(Hier& H, int mode, int finest, int minlevel, int nsmooth, int errortype, Hier::GraphRec** out) {
-  auto key = std::make_tuple(mode, finest, minlevel, nsmooth, errortype);
+int capture_graph(Hier& H, const GraphKey& key, const std::function<int()>& body, Hier::GraphRec** out) {
   auto it = H.graphs.find(key);
   if (it != H.graphs.end()) {
     *out = &it->second;
@@ -180,8 +175,7 @@ int get_graph(Hier& H, int mode, int finest, int minlevel, int nsmooth, int erro
   CK(cudaStreamBeginCapture(H.s, cudaStreamCaptureModeThreadLocal));
   H.capturing = true;
   H.capture_launches = 0;
-  int rc = mode == BSAMG_MODE_FP64 ? enq_iteration(H, finest, minlevel, nsmooth, errortype)
-                                   : mixed_enq_iteration(H, finest, minlevel, nsmooth, errortype);
+  int rc = body();
   H.capturing = false;
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(H.s, &g);
@@ -200,6 +194,17 @@ int get_graph(Hier& H, int mode, int finest, int minlevel, int nsmooth, int erro
   return BSAMG_OK;
 }
 
+int replay(Hier& H, Hier::GraphRec* g) {
+  CK(cudaGraphLaunch(g->exec, H.s));
+  H.launches += g->nlaunch;
+  CK(cudaStreamSynchronize(H.s));
+  return BSAMG_OK;
+}
+
+}  // namespace bsamg
+
+namespace {
+
 int check_nonfinite(Hier& H) { return *H.h_nonfinite ? BSAMG_ERR_NONFINITE : BSAMG_OK; }
 
 int multigrid_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol,
@@ -213,15 +218,15 @@ int multigrid_iterations(Hier& H, int finest, int minlevel, int nsmooth, int max
   RET(enq_get_source(H, finest));
   RET(enq_update_source(H, finest));
   RET(enq_fill_down(H, 1, finest, minlevel));
-  if (mode == BSAMG_MODE_MIXED) RET(mixed_prepare(H, finest, minlevel));
+  if (mode == BSAMG_MODE_MIXED)
+    return mixed_iterations(H, finest, minlevel, nsmooth, maxvcycles, tol, errortype, strict, ncycles, residuals);
   Hier::GraphRec* gr = nullptr;
-  RET(get_graph(H, mode, finest, minlevel, nsmooth, errortype, &gr));
+  RET(capture_graph(H, std::make_tuple(mode, finest, minlevel, nsmooth, errortype),
+                    [&] { return enq_iteration(H, finest, minlevel, nsmooth, errortype); }, &gr));
   int it;
   double r = 0.0;
   for (it = 1; it <= maxvcycles; it++) {
-    CK(cudaGraphLaunch(gr->exec, H.s));
-    H.launches += gr->nlaunch;
-    CK(cudaStreamSynchronize(H.s));
+    RET(replay(H, gr));
     r = H.h_norm[0];
     if (residuals) residuals[it - 1] = r;
     RET(check_nonfinite(H));
@@ -452,6 +457,14 @@ int commit(Hier& H) {
   for (int l = 0; l <= kMaxDepth; l++)
     for (int d = 0; d < 3; d++) H.mxmax[l][d] = d < H.ndims ? (R.mx[d] << l) : 1;
   periodic_setup(H, R.mthbc);
+  {
+    bool w = true;
+    for (int l = H.minlevel; l <= H.maxlevel; l++) w = w && H.L(l).patches.size() == 1;
+    for (const HostPatch& P : H.patches)
+      for (int f = 0; f < 2 * H.ndims; f++) w = w && P.mthbc[f] == 2;
+    for (int v = 0; v < H.nrvars; v++) w = w && H.pp.qpo[v] == 0.0;
+    H.wrap_all = w;
+  }
 
   // pool layout: [q...][qold...][qc...][f...][rf...][ftmp...]
   long long off = 0;
@@ -502,6 +515,7 @@ int commit(Hier& H) {
     D.eq = P.e_oq; D.ecq = P.e_oqc; D.eg = P.e_of; D.ephi = P.e_ophi;
     D.h = P.dx[0];
     coefficients(H, P.dx[0], D.c);
+    for (int x = 0; x < 4; x++) D.cf[x] = (float)D.c[x];
   }
   CK(cudaMalloc(&H.dP, sizeof(PatchDev) * pd.size()));
   CK(cudaMemcpy(H.dP, pd.data(), sizeof(PatchDev) * pd.size(), cudaMemcpyHostToDevice));
@@ -530,6 +544,7 @@ int commit(Hier& H) {
       RET(upload_ghost(H, L.gp[ip]));
     }
   }
+  RET(mixed_tables(H));
   H.partial_cap = maxblk;
   CK(cudaMalloc(&H.d_partial, sizeof(double) * 2 * (size_t)maxblk * std::max(1, H.nrvars)));
   CK(cudaMalloc(&H.d_norm, sizeof(double) * 8));

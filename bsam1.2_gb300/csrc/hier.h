@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -52,6 +53,9 @@ struct Hier {
   std::vector<HostPatch> patches;
   std::unordered_map<int, int> id2idx;
   bool committed = false;
+  // every level is one fully periodic patch and qpo = 0: the mixed path
+  // addresses neighbours with periodic wrap instead of ghost cells
+  bool wrap_all = false;
   int minlevel = 0, maxlevel = 0;
   int periodic = 0, nperoff = 0, peroffidx[13] = {};
   int mxmax[kMaxDepth + 1][3] = {};
@@ -63,6 +67,8 @@ struct Hier {
   float* fpool = nullptr;
   size_t fpool_elems = 0;
   size_t e_len = 0;  // leading FP32 elements holding every patch's correction e
+  size_t e_coarse_off = 0, e_coarse_len = 0;  // the part of it on levels < 0
+  Blk* mx_norm_blk[kNLev] = {};               // padded interior lists (mixed norm)
   size_t bytes = 0;
 
   LevelT lev[kNLev];
@@ -107,6 +113,10 @@ int enq_fill_down(Hier& H, int field, int finest, int minlevel);
 int enq_update_source(Hier& H, int finest);
 int enq_norm(Hier& H, int level, int errortype);
 int enq_relax(Hier& H, int level, int ipass);
+using GraphKey = std::tuple<int, int, int, int, int>;
+// capture what `body` enqueues as a CUDA graph (once per key) and replay it
+int capture_graph(Hier& H, const GraphKey& key, const std::function<int()>& body, Hier::GraphRec** out);
+int replay(Hier& H, Hier::GraphRec* g);
 
 }  // namespace bsamg
 

@@ -42,6 +42,7 @@ struct PatchDev {
   //   CH : c0 = dt/h^2, c1 = eps^2/h^2, c2 = (4|6)*eps^2/h^2, c3 = (4|6)*c0
   //   Bio: c0 = dt*eps^2/h^2, c1 = 1/h^2, c2 = 4*c0 + 1, c3 = 4*c1
   double c[4];
+  float cf[4];  // the same coefficients rounded to FP32 on the host (mixed path)
   double h;
 };
 

@@ -96,27 +96,56 @@ __device__ __forceinline__ T ulap(const T* a, long long c, long long sy, long lo
   return a[c + 1] + a[c - 1] + a[c + sy] + a[c - sy] + a[c + sz] + a[c - sz] - T(6) * a[c];
 }
 
-// correction operator M(e) = N(qbar+e) - N(qbar) of the CH plugin
-// (Operator2D/3D, CH/problem.f90:393-422, :638-669), cube difference
-// written as e*(3 pb (pb + e) + e^2) to keep the small terms exact.
-template <int DIM>
-__device__ __forceinline__ void mop(const float* e, long long c, long long sy, long long sz, long long ps, float pb,
-                                    float c0, float c1, float& m0, float& m1) {
+// ---------------------------------------------------------------------------
+// Neighbour addressing.  WRAP = true on hierarchies whose every level is one
+// fully periodic patch (and qpo = 0): neighbours of boundary cells are read
+// from the opposite side of the interior, so the correction cycle needs no
+// ghost fills at all; the FP64 ghosts are refreshed once after the loop.
+
+template <int DIM, bool WRAP>
+struct Nbr {
+  long long xm, xp, ym, yp, zm, zp;
+  __device__ __forceinline__ Nbr(long long c, int i, int j, int k, const int* mx, long long sy, long long sz) {
+    xm = c - 1; xp = c + 1; ym = c - sy; yp = c + sy; zm = c - sz; zp = c + sz;
+    if (WRAP) {
+      if (i == 1) xm = c + (mx[0] - 1);
+      if (i == mx[0]) xp = c - (mx[0] - 1);
+      if (j == 1) ym = c + (long long)(mx[1] - 1) * sy;
+      if (j == mx[1]) yp = c - (long long)(mx[1] - 1) * sy;
+      if (DIM == 3) {
+        if (k == 1) zm = c + (long long)(mx[2] - 1) * sz;
+        if (k == mx[2]) zp = c - (long long)(mx[2] - 1) * sz;
+      }
+    }
+  }
+};
+
+template <int DIM, bool WRAP, typename T>
+__device__ __forceinline__ T ulapn(const T* a, long long c, const Nbr<DIM, WRAP>& n) {
+  if (DIM == 2) return a[n.xp] + a[n.xm] + a[n.yp] + a[n.ym] - T(4) * a[c];
+  return a[n.xp] + a[n.xm] + a[n.yp] + a[n.ym] + a[n.zp] + a[n.zm] - T(6) * a[c];
+}
+
+// correction operator at a fine cell with neighbour set n
+template <int DIM, bool WRAP>
+__device__ __forceinline__ void mopn(const float* e, long long c, const Nbr<DIM, WRAP>& n, long long ps, float pb,
+                                     float c0, float c1, float& m0, float& m1) {
   const float* e0 = e;
   const float* e1 = e + ps;
   float x = e0[c];
-  m0 = x - c0 * ulap<DIM>(e1, c, sy, sz);
-  m1 = e1[c] - x * (3.0f * pb * (pb + x) + x * x) + c1 * ulap<DIM>(e0, c, sy, sz);
+  m0 = x - c0 * ulapn<DIM, WRAP>(e1, c, n);
+  m1 = e1[c] - x * (3.0f * pb * (pb + x) + x * x) + c1 * ulapn<DIM, WRAP>(e0, c, n);
 }
 
-// ---------------------------------------------------------------------------
+constexpr int kNormCells = 8;  // interior blocks per CTA in k_mx_norm
 
-// step 1: phib = (float)qbar_phi everywhere; on levels >= 0 the FP64
-// residual g = f - N(qbar) (or the stored rf) as FP32.
+__device__ __forceinline__ int wrap1(int x, int n) { return x < 1 ? x + n : (x > n ? x - n : x); }
+
+// step 1: phib = (float)qbar_phi everywhere; g = FP32 of the FP64 residual:
+// mode 0: phib only, 1: g from the stored rf, 2: g = f - N(qbar) recomputed
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_prep(const PatchDev* __restrict__ P, const double* __restrict__ pool,
-                                                    float* __restrict__ fpool, const Blk* __restrict__ blk,
-                                                    int mode /*0 phib only, 1 from rf, 2 recompute*/) {
+                                                    float* __restrict__ fpool, const Blk* __restrict__ blk, int mode) {
   const Blk b = blk[blockIdx.x];
   const PatchDev& p = P[b.patch];
   int i, j, k;
@@ -147,7 +176,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_prep(const PatchDev* __restrict__
 //   a21 = -3 (pb + e)^2 - tmp3
 //   b1  = g1 + tmp1 * sum(e_mu neighbours)
 //   b2  = g2 - tmp2 * sum(e_phi neighbours) - e^2 (3 pb + 2 e)
-template <int DIM>
+template <int DIM, bool WRAP>
 __global__ void __launch_bounds__(kBlock) k_mx_relax(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                      const Blk* __restrict__ blk, int ipass) {
   const Blk b = blk[blockIdx.x];
@@ -159,18 +188,19 @@ __global__ void __launch_bounds__(kBlock) k_mx_relax(const PatchDev* __restrict_
   long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
   long long c = gofs<DIM>(p.qn, i, j, k);
   long long fc = iofs<DIM>(p.mx, i, j, k);
-  float tmp1 = (float)p.c[0], tmp2 = (float)p.c[1], tmp3 = (float)p.c[2], a12 = (float)p.c[3];
+  Nbr<DIM, WRAP> n(c, i, j, k, p.mx, sy, sz);
+  float tmp1 = p.cf[0], tmp2 = p.cf[1], tmp3 = p.cf[2], a12 = p.cf[3];
   float pb = fpool[p.ephi + fc];
   float x = e0[c];
   float w = pb + x;
   float a21 = -3.0f * w * w - tmp3;
   float s1, s0;
   if (DIM == 2) {
-    s1 = e1[c - 1] + e1[c + 1] + e1[c - sy] + e1[c + sy];
-    s0 = e0[c + 1] + e0[c - 1] + e0[c + sy] + e0[c - sy];
+    s1 = e1[n.xm] + e1[n.xp] + e1[n.ym] + e1[n.yp];
+    s0 = e0[n.xp] + e0[n.xm] + e0[n.yp] + e0[n.ym];
   } else {
-    s1 = e1[c - 1] + e1[c + 1] + e1[c - sy] + e1[c + sy] + e1[c - sz] + e1[c + sz];
-    s0 = e0[c + 1] + e0[c - 1] + e0[c + sy] + e0[c - sy] + e0[c + sz] + e0[c - sz];
+    s1 = e1[n.xm] + e1[n.xp] + e1[n.ym] + e1[n.yp] + e1[n.zm] + e1[n.zp];
+    s0 = e0[n.xp] + e0[n.xm] + e0[n.yp] + e0[n.ym] + e0[n.zp] + e0[n.zm];
   }
   float b1 = fpool[p.eg + fc] + tmp1 * s1;
   float b2 = fpool[p.eg + p.sf + fc] - tmp2 * s0 - x * x * (3.0f * pb + 2.0f * x);
@@ -209,8 +239,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_restrict(const PatchDev* __restri
 
 // GetCoarseGhostPoints on e (ring of ec <- parent e) when corr == 0;
 // CorrectFine step 1 (ec = parent e - ec over the whole ghosted ec) when
-// corr == 1.
-template <int DIM>
+// corr == 1.  With WRAP the parent index wraps around the parent's interior.
+template <int DIM, bool WRAP>
 __global__ void __launch_bounds__(kBlock) k_mx_coarse_ring(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                            const Blk* __restrict__ blk, int nrvars, int corr) {
   const Blk b = blk[blockIdx.x];
@@ -223,7 +253,13 @@ __global__ void __launch_bounds__(kBlock) k_mx_coarse_ring(const PatchDev* __res
     if (!ring) return;
   }
   const PatchDev& par = P[p.parent];
-  long long src = gofs<DIM>(par.qn, p.mb[0] - 1 + i, p.mb[1] - 1 + j, DIM == 3 ? p.mb[2] - 1 + k : 0);
+  int pi = p.mb[0] - 1 + i, pj = p.mb[1] - 1 + j, pk = DIM == 3 ? p.mb[2] - 1 + k : 0;
+  if (WRAP) {
+    pi = wrap1(pi, par.mx[0]);
+    pj = wrap1(pj, par.mx[1]);
+    if (DIM == 3) pk = wrap1(pk, par.mx[2]);
+  }
+  long long src = gofs<DIM>(par.qn, pi, pj, pk);
   long long dst = gofs<DIM>(p.cn, i, j, k);
   for (int v = 0; v < nrvars; v++) {
     float* ec = fpool + p.ecq + v * p.sc;
@@ -234,7 +270,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_coarse_ring(const PatchDev* __res
 
 // CoarseLoadingFunction on the correction: fine r = g - M(e) under each
 // coarse cell; parent g(mb) = R(r) + M_c(ec) with the parent's base field.
-template <int DIM>
+template <int DIM, bool WRAP>
 __global__ void __launch_bounds__(kBlock) k_mx_coarse_load(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                            const Blk* __restrict__ blk) {
   const Blk b = blk[blockIdx.x];
@@ -244,48 +280,44 @@ __global__ void __launch_bounds__(kBlock) k_mx_coarse_load(const PatchDev* __res
   const PatchDev& par = P[p.parent];
   const float* e = fpool + p.eq;
   long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
-  float c0 = (float)p.c[0], c1 = (float)p.c[1];
-  float r0[8], r1[8];
+  float c0 = p.cf[0], c1 = p.cf[1];
+  float R0 = 0.f, R1 = 0.f;
   const int nk = DIM == 3 ? 2 : 1;
-  // children in the reference's restriction order: (2i,2j,2k), (2i-1,2j,2k),
-  // (2i,2j-1,2k), (2i-1,2j-1,2k), then the k-1 layer
-  int n = 0;
   for (int dk = 0; dk < nk; dk++)
     for (int dj = 0; dj < 2; dj++)
-      for (int di = 0; di < 2; di++, n++) {
+      for (int di = 0; di < 2; di++) {
         int i = 2 * ci - di, j = 2 * cj - dj, k = DIM == 3 ? 2 * ck - dk : 1;
         long long c = gofs<DIM>(p.qn, i, j, k);
         long long fc = iofs<DIM>(p.mx, i, j, k);
+        Nbr<DIM, WRAP> n(c, i, j, k, p.mx, sy, sz);
         float m0, m1;
-        mop<DIM>(e, c, sy, sz, p.sq, fpool[p.ephi + fc], c0, c1, m0, m1);
-        r0[n] = fpool[p.eg + fc] - m0;
-        r1[n] = fpool[p.eg + p.sf + fc] - m1;
+        mopn<DIM, WRAP>(e, c, n, p.sq, fpool[p.ephi + fc], c0, c1, m0, m1);
+        R0 += fpool[p.eg + fc] - m0;
+        R1 += fpool[p.eg + p.sf + fc] - m1;
       }
-  float R0 = 0.f, R1 = 0.f;
-  for (int x = 0; x < 2 * 2 * nk; x++) {
-    R0 += r0[x];
-    R1 += r1[x];
-  }
   R0 *= DIM == 2 ? 0.25f : 0.125f;
   R1 *= DIM == 2 ? 0.25f : 0.125f;
   const float* ec = fpool + p.ecq;
   long long csy = p.cn[0], csz = (long long)p.cn[0] * p.cn[1];
   long long cc = gofs<DIM>(p.cn, ci, cj, ck);
   long long pf = iofs<DIM>(par.mx, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 1);
+  // the coarse operator reads the ec ring, which coarse_ring has filled
+  Nbr<DIM, false> n(cc, ci, cj, ck, p.cmx, csy, csz);
   float m0, m1;
-  mop<DIM>(ec, cc, csy, csz, p.sc, fpool[par.ephi + pf], (float)par.c[0], (float)par.c[1], m0, m1);
+  mopn<DIM, false>(ec, cc, n, p.sc, fpool[par.ephi + pf], par.cf[0], par.cf[1], m0, m1);
   fpool[par.eg + pf] = R0 + m0;
   fpool[par.eg + par.sf + pf] = R1 + m1;
 }
 
-// CorrectFine step 2 on e: e(0:mx+1) += P(ec)
-template <int DIM>
+// CorrectFine step 2 on e: e(0:mx+1) += P(ec) (interior only with WRAP)
+template <int DIM, bool WRAP>
 __global__ void __launch_bounds__(kBlock) k_mx_prolong(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                        const Blk* __restrict__ blk, int nrvars) {
   const Blk b = blk[blockIdx.x];
   const PatchDev& p = P[b.patch];
   int i, j, k;
   if (!ghosted_cell<DIM>(p.qn, b.start + threadIdx.x, i, j, k)) return;
+  if (WRAP && (i == 0 || i > p.mx[0] || j == 0 || j > p.mx[1] || (DIM == 3 && (k == 0 || k > p.mx[2])))) return;
   int ci = i >> 1, cj = j >> 1, ck = k >> 1;
   bool ei = (i & 1) == 0, ej = (j & 1) == 0, ek = (k & 1) == 0;
   long long dst = gofs<DIM>(p.qn, i, j, k);
@@ -311,17 +343,27 @@ __global__ void __launch_bounds__(kBlock) k_mx_prolong(const PatchDev* __restric
   }
 }
 
-// step 3: qbar += e over the whole ghosted q of a level
-template <int DIM>
+// step 3: qbar += e (whole ghosted array; interior only with WRAP).  The
+// same pass refreshes the base field phib of the next cycle and clears e,
+// so the next cycle needs neither a separate prep pass over q nor a memset
+// on this level.
+template <int DIM, bool WRAP>
 __global__ void __launch_bounds__(kBlock) k_mx_update(const PatchDev* __restrict__ P, double* __restrict__ pool,
-                                                      const float* __restrict__ fpool, const Blk* __restrict__ blk,
+                                                      float* __restrict__ fpool, const Blk* __restrict__ blk,
                                                       int nrvars) {
   const Blk b = blk[blockIdx.x];
   const PatchDev& p = P[b.patch];
   int i, j, k;
   if (!ghosted_cell<DIM>(p.qn, b.start + threadIdx.x, i, j, k)) return;
+  bool interior = i >= 1 && i <= p.mx[0] && j >= 1 && j <= p.mx[1] && (DIM == 2 || (k >= 1 && k <= p.mx[2]));
+  if (WRAP && !interior) return;
   long long c = gofs<DIM>(p.qn, i, j, k);
-  for (int v = 0; v < nrvars; v++) pool[p.oq + v * p.sq + c] += (double)fpool[p.eq + v * p.sq + c];
+  for (int v = 0; v < nrvars; v++) {
+    double nq = pool[p.oq + v * p.sq + c] + (double)fpool[p.eq + v * p.sq + c];
+    pool[p.oq + v * p.sq + c] = nq;
+    fpool[p.eq + v * p.sq + c] = 0.0f;
+    if (v == 0 && interior) fpool[p.ephi + iofs<DIM>(p.mx, i, j, k)] = (float)nq;
+  }
 }
 
 // FP64 residual rf = f - N(q) of the finest level and per-block sums of rf^2
@@ -329,29 +371,35 @@ __global__ void __launch_bounds__(kBlock) k_mx_update(const PatchDev* __restrict
 // path's norm kernel, but this translation unit lets the compiler fuse
 // multiply-adds, which cuts FP64 pipe work by about a third; the mixed path
 // needs the true residual to ~1e-15 relative, not bit-identical rounding.
-template <int DIM>
+template <int DIM, bool WRAP>
 __global__ void __launch_bounds__(kBlock) k_mx_norm(const PatchDev* __restrict__ P, double* __restrict__ pool,
                                                     const Blk* __restrict__ blk, double* __restrict__ partial) {
+  // kNormCells consecutive blocks of the interior list per CTA, so the
+  // shuffle reduction (FP64 adds on every lane) is paid once per kNormCells
+  // cells instead of once per cell
   __shared__ double red[2][kBlock / 32];
-  const Blk b = blk[blockIdx.x];
-  const PatchDev& p = P[b.patch];
-  int i, j, k;
   double s0 = 0.0, s1 = 0.0;
-  if (interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) {
+  for (int sub = 0; sub < kNormCells; sub++) {
+    const Blk b = blk[blockIdx.x * kNormCells + sub];
+    if (b.patch < 0) break;
+    const PatchDev& p = P[b.patch];
+    int i, j, k;
+    if (!interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) continue;
     const double* q0 = pool + p.oq;
     const double* q1 = q0 + p.sq;
     long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
     long long c = gofs<DIM>(p.qn, i, j, k);
     long long fc = iofs<DIM>(p.mx, i, j, k);
+    Nbr<DIM, WRAP> n(c, i, j, k, p.mx, sy, sz);
     double phi = q0[c];
-    double o0 = phi - p.c[0] * ulap<DIM>(q1, c, sy, sz);
-    double o1 = q1[c] - phi * phi * phi + p.c[1] * ulap<DIM>(q0, c, sy, sz);
+    double o0 = phi - p.c[0] * ulapn<DIM, WRAP>(q1, c, n);
+    double o1 = q1[c] - phi * phi * phi + p.c[1] * ulapn<DIM, WRAP>(q0, c, n);
     double e0 = pool[p.of + fc] - o0;
     double e1 = pool[p.of + p.sf + fc] - o1;
     pool[p.orf + fc] = e0;
     pool[p.orf + p.sf + fc] = e1;
-    s0 = e0 * e0;
-    s1 = e1 * e1;
+    s0 = fma(e0, e0, s0);
+    s1 = fma(e1, e1, s1);
   }
   for (int o = 16; o > 0; o >>= 1) {
     s0 += __shfl_down_sync(0xffffffffu, s0, o);
@@ -365,9 +413,57 @@ __global__ void __launch_bounds__(kBlock) k_mx_norm(const PatchDev* __restrict__
   __syncthreads();
   if (threadIdx.x == 0) {
     double t0 = 0.0, t1 = 0.0;
-    for (int n = 0; n < kBlock / 32; n++) {
-      t0 += red[0][n];
-      t1 += red[1][n];
+    for (int m = 0; m < kBlock / 32; m++) {
+      t0 += red[0][m];
+      t1 += red[1][m];
+    }
+    partial[2 * blockIdx.x] = t0;
+    partial[2 * blockIdx.x + 1] = t1;
+  }
+}
+
+// Residual tracked in FP32 between FP64 evaluations: after qbar += e the
+// new residual is exactly g - M(e) (M is the difference N(qbar+e) - N(qbar)),
+// so g <- g - M(e) on the finest level gives the next right-hand side and,
+// summed, the tracked norm.
+template <int DIM, bool WRAP>
+__global__ void __launch_bounds__(kBlock) k_mx_track(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                     const Blk* __restrict__ blk, double* __restrict__ partial) {
+  __shared__ double red[2][kBlock / 32];
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  double s0 = 0.0, s1 = 0.0;
+  if (interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) {
+    const float* e = fpool + p.eq;
+    long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
+    long long c = gofs<DIM>(p.qn, i, j, k);
+    long long fc = iofs<DIM>(p.mx, i, j, k);
+    Nbr<DIM, WRAP> n(c, i, j, k, p.mx, sy, sz);
+    float m0, m1;
+    mopn<DIM, WRAP>(e, c, n, p.sq, fpool[p.ephi + fc], p.cf[0], p.cf[1], m0, m1);
+    float g0 = fpool[p.eg + fc] - m0;
+    float g1 = fpool[p.eg + p.sf + fc] - m1;
+    fpool[p.eg + fc] = g0;
+    fpool[p.eg + p.sf + fc] = g1;
+    s0 = (double)g0 * g0;
+    s1 = (double)g1 * g1;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+  }
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    red[0][w] = s0;
+    red[1][w] = s1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0.0, t1 = 0.0;
+    for (int m = 0; m < kBlock / 32; m++) {
+      t0 += red[0][m];
+      t1 += red[1][m];
     }
     partial[2 * blockIdx.x] = t0;
     partial[2 * blockIdx.x + 1] = t1;
@@ -434,7 +530,24 @@ __global__ void __launch_bounds__(kBlock) k_ghost32_program(const PatchDev* __re
     }                                                                                       \
   } while (0)
 
+#define MX_LAUNCH_W(H, kind, KER, ...)                                                      \
+  do {                                                                                      \
+    int nb__ = L.nblk[kind];                                                                \
+    if (nb__ > 0) {                                                                         \
+      if ((H).ndims == 2) {                                                                 \
+        if ((H).wrap_all) KER<2, true><<<nb__, kBlock, 0, (H).s>>>(__VA_ARGS__);            \
+        else KER<2, false><<<nb__, kBlock, 0, (H).s>>>(__VA_ARGS__);                        \
+      } else {                                                                              \
+        if ((H).wrap_all) KER<3, true><<<nb__, kBlock, 0, (H).s>>>(__VA_ARGS__);            \
+        else KER<3, false><<<nb__, kBlock, 0, (H).s>>>(__VA_ARGS__);                        \
+      }                                                                                     \
+      int r__ = after_launch(H, 1);                                                         \
+      if (r__) return r__;                                                                  \
+    }                                                                                       \
+  } while (0)
+
 int mx_set_ghost(Hier& H, int level, int ipass) {
+  if (H.wrap_all) return BSAMG_OK;  // every consumer wraps
   GhostProg& g = H.L(level).gp[ipass];
   int nst = (int)g.stage_off.size() - 1;
   if (nst <= 0) return BSAMG_OK;
@@ -458,7 +571,7 @@ int mx_level_relax(Hier& H, int level, int nsmooth) {
   LevelT& L = H.L(level);
   for (int pass = 1; pass <= nsmooth; pass++)
     for (int rb = 1; rb <= 2; rb++) {
-      MX_LAUNCH(H, kKindColor, k_mx_relax, H.dP, H.fpool, L.d_blk[kKindColor], rb);
+      MX_LAUNCH_W(H, kKindColor, k_mx_relax, H.dP, H.fpool, L.d_blk[kKindColor], rb);
       int r = mx_set_ghost(H, level, rb);
       if (r) return r;
     }
@@ -472,25 +585,33 @@ int mx_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
     LevelT& L = H.L(level);
     MX_LAUNCH(H, kKindCoarse, k_mx_restrict, H.dP, H.fpool, L.d_blk[kKindCoarse], H.nrvars);
     if ((r = mx_set_ghost(H, level - 1, 0))) return r;
-    MX_LAUNCH(H, kKindCGhost, k_mx_coarse_ring, H.dP, H.fpool, L.d_blk[kKindCGhost], H.nrvars, 0);
-    MX_LAUNCH(H, kKindCoarse, k_mx_coarse_load, H.dP, H.fpool, L.d_blk[kKindCoarse]);
+    MX_LAUNCH_W(H, kKindCGhost, k_mx_coarse_ring, H.dP, H.fpool, L.d_blk[kKindCGhost], H.nrvars, 0);
+    MX_LAUNCH_W(H, kKindCoarse, k_mx_coarse_load, H.dP, H.fpool, L.d_blk[kKindCoarse]);
     if ((r = mx_vcycle(H, level - 1, minlevel, nsmooth))) return r;
-    MX_LAUNCH(H, kKindCGhost, k_mx_coarse_ring, H.dP, H.fpool, L.d_blk[kKindCGhost], H.nrvars, 1);
-    MX_LAUNCH(H, kKindFGhost, k_mx_prolong, H.dP, H.fpool, L.d_blk[kKindFGhost], H.nrvars);
+    MX_LAUNCH_W(H, kKindCGhost, k_mx_coarse_ring, H.dP, H.fpool, L.d_blk[kKindCGhost], H.nrvars, 1);
+    MX_LAUNCH_W(H, kKindFGhost, k_mx_prolong, H.dP, H.fpool, L.d_blk[kKindFGhost], H.nrvars);
     if ((r = mx_set_ghost(H, level, 0))) return r;
     if ((r = mx_level_relax(H, level, nsmooth))) return r;
   }
   return BSAMG_OK;
 }
 
-std::vector<long long> layout(const Hier& H, size_t* total, size_t* e_len) {
-  // region order: all e (sq*V), all ec (sc*V), all g (sf*V), all phib (sf);
-  // e is one contiguous region so one memset clears every correction
+// FP32 pool layout.  Region order: e of levels >= 0, e of levels < 0 (so
+// the coarse corrections can be cleared with one memset), all ec, all g, all
+// phib.  Returns per patch {e, ec, g, phib} offsets.
+std::vector<long long> layout(const Hier& H, size_t* total, size_t* e_len, size_t* e_coarse_off) {
   size_t np = H.patches.size();
   std::vector<long long> off(4 * np);
   long long o = 0;
   auto al = [](long long x) { return (x + 63) & ~63LL; };
-  for (size_t p = 0; p < np; p++) { off[4 * p] = o; o = al(o + H.patches[p].sq * H.nrvars); }
+  for (int pass = 0; pass < 2; pass++) {
+    if (pass == 1) *e_coarse_off = (size_t)o;
+    for (size_t p = 0; p < np; p++)
+      if ((H.patches[p].level < 0) == (pass == 1)) {
+        off[4 * p] = o;
+        o = al(o + H.patches[p].sq * H.nrvars);
+      }
+  }
   *e_len = (size_t)o;
   for (size_t p = 0; p < np; p++) { off[4 * p + 1] = o; o = al(o + H.patches[p].sc * H.nrvars); }
   for (size_t p = 0; p < np; p++) { off[4 * p + 2] = o; o = al(o + H.patches[p].sf * H.nrvars); }
@@ -499,20 +620,106 @@ std::vector<long long> layout(const Hier& H, size_t* total, size_t* e_len) {
   return off;
 }
 
+int mx_norm(Hier& H, int level, int errortype) {
+  LevelT& L = H.L(level);
+  int nb = (L.nblk[kKindInterior] + kNormCells - 1) / kNormCells;
+  if (nb <= 0) return BSAMG_OK;
+  // the interior list is padded with patch = -1 entries to a multiple of
+  // kNormCells (see mixed_alloc)
+  if (H.ndims == 2) {
+    if (H.wrap_all) k_mx_norm<2, true><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.mx_norm_blk[level + kMaxDepth], H.d_partial);
+    else k_mx_norm<2, false><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.mx_norm_blk[level + kMaxDepth], H.d_partial);
+  } else {
+    if (H.wrap_all) k_mx_norm<3, true><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.mx_norm_blk[level + kMaxDepth], H.d_partial);
+    else k_mx_norm<3, false><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.mx_norm_blk[level + kMaxDepth], H.d_partial);
+  }
+  int r = after_launch(H, 1);
+  if (r) return r;
+  return after_launch(H, launch_norm_finish(H.s, H.d_partial, nb, H.nrvars, L.count, errortype, H.d_norm,
+                                            H.d_nonfinite));
+}
+
+int to_host(Hier& H) {
+  cudaError_t ce = cudaMemcpyAsync(H.h_norm, H.d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, H.s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(norm)");
+  ce = cudaMemcpyAsync(H.h_nonfinite, H.d_nonfinite, sizeof(int), cudaMemcpyDeviceToHost, H.s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(nonfinite)");
+  return BSAMG_OK;
+}
+
+// FillDown of q in FP64 (restriction to the parents); with WRAP the coarse
+// ghosts are not needed inside the loop, so the ghost fills are skipped
+int mx_fill_down_q(Hier& H, int finest, int minlevel) {
+  if (!H.wrap_all) return enq_fill_down(H, 2, finest, minlevel);
+  for (int level = finest; level >= minlevel + 1; level--) {
+    LevelT& L = H.L(level);
+    int r = after_launch(H, launch_fill_down(H.lc(), L.d_blk[kKindCoarse], L.nblk[kKindCoarse], 2));
+    if (r) return r;
+  }
+  return BSAMG_OK;
+}
+
+// one outer iteration; resync: take g on the finest level from the FP64 rf
+int mx_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype, bool resync) {
+  // e of levels >= 0 was cleared by the previous update pass (or by
+  // mixed_iterations before the first cycle); clear the coarse ones
+  if (H.e_coarse_len) {
+    cudaError_t ce = cudaMemsetAsync(H.fpool + H.e_coarse_off, 0, H.e_coarse_len * sizeof(float), H.s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemsetAsync(e)");
+  }
+  for (int level = finest; level >= minlevel; level--) {
+    LevelT& L = H.L(level);
+    // phib of levels >= 0 comes from the update pass; g of the finest level
+    // from the FP64 rf after a resync, else from the tracked update
+    if (level == finest && !resync) continue;
+    int mode = level < 0 ? 0 : (level == finest ? 1 : 2);
+    MX_LAUNCH(H, kKindInterior, k_mx_prep, H.dP, H.pool, H.fpool, L.d_blk[kKindInterior], mode);
+  }
+  int r = mx_vcycle(H, finest, minlevel, nsmooth);
+  if (r) return r;
+  // tracked residual g - M(e): M needs this cycle's base field, so it runs
+  // before the update pass replaces phib with the new base
+  {
+    LevelT& L = H.L(finest);
+    MX_LAUNCH_W(H, kKindInterior, k_mx_track, H.dP, H.fpool, L.d_blk[kKindInterior], H.d_partial);
+    if ((r = after_launch(H, launch_norm_finish(H.s, H.d_partial, L.nblk[kKindInterior], H.nrvars, L.count,
+                                                 errortype, H.d_norm, H.d_nonfinite))))
+      return r;
+  }
+  for (int level = finest; level >= 0; level--) {
+    LevelT& L = H.L(level);
+    MX_LAUNCH_W(H, kKindFGhost, k_mx_update, H.dP, H.pool, H.fpool, L.d_blk[kKindFGhost], H.nrvars);
+  }
+  if ((r = mx_fill_down_q(H, finest, minlevel))) return r;
+  // refinement levels: ghosts from the updated FP64 state (coarse-fine
+  // interpolation reads the parent values FillDown just restricted)
+  for (int level = 1; level <= finest; level++)
+    if ((r = enq_set_ghost(H, level, 0))) return r;
+  return to_host(H);
+}
+
+int mx_verify(Hier& H, int finest, int errortype) {
+  int r = mx_norm(H, finest, errortype);
+  if (r) return r;
+  return to_host(H);
+}
+
 }  // namespace
 
 size_t mixed_pool_bytes(const Hier& H) {
   if (H.problem != kCH) return 0;
-  size_t n, ne;
-  layout(H, &n, &ne);
+  size_t n, ne, ec;
+  layout(H, &n, &ne, &ec);
   return n * sizeof(float);
 }
 
 int mixed_alloc(Hier& H) {
   if (H.problem != kCH) return BSAMG_OK;
-  size_t n, ne;
-  std::vector<long long> off = layout(H, &n, &ne);
+  size_t n, ne, ec;
+  std::vector<long long> off = layout(H, &n, &ne, &ec);
   H.e_len = ne;
+  H.e_coarse_off = ec;
+  H.e_coarse_len = ne - ec;
   for (size_t p = 0; p < H.patches.size(); p++) {
     HostPatch& P = H.patches[p];
     P.e_oq = off[4 * p];
@@ -531,57 +738,103 @@ int mixed_alloc(Hier& H) {
 void mixed_free(Hier& H) {
   if (H.fpool) cudaFree(H.fpool);
   H.fpool = nullptr;
+  for (int l = 0; l < kNLev; l++) {
+    if (H.mx_norm_blk[l]) cudaFree(H.mx_norm_blk[l]);
+    H.mx_norm_blk[l] = nullptr;
+  }
 }
 
-int mx_norm(Hier& H, int level, int errortype) {
-  LevelT& L = H.L(level);
-  MX_LAUNCH(H, kKindInterior, k_mx_norm, H.dP, H.pool, L.d_blk[kKindInterior], H.d_partial);
-  return after_launch(H, launch_norm_finish(H.s, H.d_partial, L.nblk[kKindInterior], H.nrvars, L.count, errortype,
-                                            H.d_norm, H.d_nonfinite));
+int mixed_tables(Hier& H) {
+  if (H.problem != kCH || !H.fpool) return BSAMG_OK;
+  for (int l = H.minlevel; l <= H.maxlevel; l++) {
+    // interior work list padded with patch = -1 to a multiple of kNormCells
+    std::vector<Blk> v;
+    for (int p : H.L(l).patches) {
+      const HostPatch& P = H.patches[p];
+      long long units = (long long)P.mx[0] * P.mx[1] * P.mx[2];
+      for (long long s = 0; s < units; s += kBlock) v.push_back(Blk{p, (int)s});
+    }
+    while (v.size() % kNormCells) v.push_back(Blk{-1, 0});
+    Blk* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(Blk) * v.size());
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(norm list)");
+    e = cudaMemcpy(d, v.data(), sizeof(Blk) * v.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(norm list)");
+    H.mx_norm_blk[l + kMaxDepth] = d;
+    H.bytes += sizeof(Blk) * v.size();
+  }
+  return BSAMG_OK;
 }
 
 int mixed_enq_relax(Hier& H, int level, int ipass) {
   if (H.problem != kCH || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
   LevelT& L = H.L(level);
-  MX_LAUNCH(H, kKindColor, k_mx_relax, H.dP, H.fpool, L.d_blk[kKindColor], ipass);
+  MX_LAUNCH_W(H, kKindColor, k_mx_relax, H.dP, H.fpool, L.d_blk[kKindColor], ipass);
   return BSAMG_OK;
 }
 
-int mixed_prepare(Hier& H, int finest, int minlevel) {
+int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,
+                     int strict, int* ncycles, double* residuals) {
   if (H.problem != kCH || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
-  (void)minlevel;
-  // the first outer iteration needs the FP64 residual of the finest level
-  return mx_norm(H, finest, 1);
-}
-
-int mixed_enq_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype) {
-  if (H.problem != kCH || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
-  // 1. FP64 residuals -> g, phib, e = 0
-  cudaError_t ce = cudaMemsetAsync(H.fpool, 0, H.e_len * sizeof(float), H.s);
-  if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemsetAsync(e)");
-  for (int level = finest; level >= minlevel; level--) {
-    LevelT& L = H.L(level);
-    int mode = level < 0 ? 0 : (level == finest ? 1 : 2);
-    MX_LAUNCH(H, kKindInterior, k_mx_prep, H.dP, H.pool, H.fpool, L.d_blk[kKindInterior], mode);
-  }
-  // 2. FP32 correction V-cycle
-  int r = mx_vcycle(H, finest, minlevel, nsmooth);
+  // the first outer iteration takes its right-hand side from the FP64
+  // residual of the finest level
+  int r = mx_norm(H, finest, errortype);
   if (r) return r;
-  // 3. FP64 update, FillDown(q), norm (stores rf for the next iteration)
-  for (int level = finest; level >= 0; level--) {
-    LevelT& L = H.L(level);
-    MX_LAUNCH(H, kKindFGhost, k_mx_update, H.dP, H.pool, H.fpool, L.d_blk[kKindFGhost], H.nrvars);
+  if ((r = to_host(H))) return r;
+  cudaError_t ce = cudaStreamSynchronize(H.s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize");
+  double r_sync = H.h_norm[0];  // FP64 residual the current g was taken from
+  Hier::GraphRec *ga = nullptr, *gt = nullptr, *gv = nullptr;
+  auto key = [&](int m) { return std::make_tuple(m, finest, minlevel, nsmooth, errortype); };
+  if ((r = capture_graph(H, key(11), [&] { return mx_iteration(H, finest, minlevel, nsmooth, errortype, true); },
+                         &ga)))
+    return r;
+  if ((r = capture_graph(H, key(12), [&] { return mx_iteration(H, finest, minlevel, nsmooth, errortype, false); },
+                         &gt)))
+    return r;
+  if ((r = capture_graph(H, key(13), [&] { return mx_verify(H, finest, errortype); }, &gv))) return r;
+  // With refinement levels the coarse-fine ghosts of the finest level are
+  // re-interpolated from the updated parents after every cycle, which
+  // g - M(e) does not see; there the FP64 residual is evaluated every cycle.
+  bool track = finest == 0;
+  // every update pass leaves e = 0; clear it anyway in case an earlier call
+  // stopped between cycles
+  cudaError_t ce0 = cudaMemsetAsync(H.fpool, 0, H.e_len * sizeof(float), H.s);
+  if (ce0 != cudaSuccess) return cuda_fail(ce0, "cudaMemsetAsync(e)");
+  bool resync = true, conv = false;
+  int it;
+  double res = 0.0;
+  for (it = 1; it <= maxvcycles; it++) {
+    if ((r = replay(H, resync ? ga : gt))) return r;
+    if (*H.h_nonfinite) return BSAMG_ERR_NONFINITE;
+    double tracked = H.h_norm[0];
+    res = tracked;
+    resync = false;
+    // Re-evaluate the residual in FP64 when the FP32-tracked one says the
+    // iterate has converged, on the last cycle, and
+    // once the tracked value has fallen 1e5 below the FP64 residual it
+    // started from -- about where FP32 rounding of g stops being negligible.
+    if (!track || tracked < tol || tracked < 1e-5 * r_sync || it == maxvcycles) {
+      if ((r = replay(H, gv))) return r;
+      if (*H.h_nonfinite) return BSAMG_ERR_NONFINITE;
+      res = H.h_norm[0];
+      r_sync = res;
+      resync = true;  // the next cycle starts from this FP64 residual
+    }
+    if (residuals) residuals[it - 1] = res;
+    if (resync && res < tol) {
+      conv = true;
+      break;
+    }
   }
-  if ((r = enq_fill_down(H, 2, finest, minlevel))) return r;
-  // refinement levels: ghosts from the updated FP64 state (coarse-fine
-  // interpolation reads the parent values FillDown just restricted)
-  for (int level = 1; level <= finest; level++)
-    if ((r = enq_set_ghost(H, level, 0))) return r;
-  if ((r = mx_norm(H, finest, errortype))) return r;
-  ce = cudaMemcpyAsync(H.h_norm, H.d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, H.s);
-  if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(norm)");
-  ce = cudaMemcpyAsync(H.h_nonfinite, H.d_nonfinite, sizeof(int), cudaMemcpyDeviceToHost, H.s);
-  if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(nonfinite)");
+  if (ncycles) *ncycles = conv ? it : maxvcycles;
+  // leave the state as the FP64 path leaves it: fresh ghosts, coarse levels
+  // restricted from the finest (FillDown, afasroutines.f90:83)
+  if (H.wrap_all || finest == 0)
+    if ((r = enq_set_ghost(H, finest, 0))) return r;
+  if (H.wrap_all)
+    if ((r = enq_fill_down(H, 2, finest, minlevel))) return r;
+  if (!conv && strict) return BSAMG_ERR_NOT_CONVERGED;
   return BSAMG_OK;
 }
 

@@ -10,11 +10,12 @@ namespace bsamg {
 size_t mixed_pool_bytes(const Hier& H);
 int mixed_alloc(Hier& H);
 void mixed_free(Hier& H);
-// once per MultigridIterations call, after the FP64 sources are in place
-int mixed_prepare(Hier& H, int finest, int minlevel);
-// one outer defect-correction iteration, ending with the FP64 norm copied
-// to H.h_norm (captured into a CUDA graph by the caller)
-int mixed_enq_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype);
+// work lists of the mixed path, after the level tables exist
+int mixed_tables(Hier& H);
+// MultigridIterations in the mixed mode (after the common prologue:
+// FillDown(q), sources, FillDown(f)); same contract as the FP64 loop
+int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,
+                     int strict, int* ncycles, double* residuals);
 // one FP32 colour sweep of the correction smoother on `level`
 int mixed_enq_relax(Hier& H, int level, int ipass);
 

@@ -1,9 +1,12 @@
 """Mixed-precision path (FP32 correction V-cycle in an FP64 defect-correction
 loop) against the FP64 oracle (needs a GB300).
 
-Both paths stop when the FP64 residual norm falls below the tolerance, so
-they stop at slightly different iterates; the stated error bound is the
-max-norm difference of phi after the time steps, relative to max |phi|.
+Both paths stop when the FP64 residual norm of the finest level falls below
+the tolerance, so at the configuration tolerance they stop at different
+iterates and differ by about what the tolerance allows (the FP64 path's own
+error against a fully converged solve is 3e-8 relative in 2D at 1e-9 and
+2e-7 in 3D at 1e-8).  Converged tightly, both must reach the same discrete
+solution; that is the parity statement for this path.
 """
 import numpy as np
 import pytest
@@ -13,19 +16,17 @@ from tests.test_parity_gpu import CH2, CH3, uniform_spec, make_pair, PERIODIC2, 
 
 pytestmark = pytest.mark.gpu
 
+# case: (config, hierarchy, config tolerance, its error bound, tight tolerance, tight bound)
 MIXED_CASES = {
-    "ch2d-periodic-64": (CH2, lambda: uniform_spec(2, 64, PERIODIC2), 1e-9, 2e-7),
-    "ch2d-neumann-64": (CH2, lambda: uniform_spec(2, 64, NEUMANN2), 1e-9, 2e-7),
-    "ch3d-periodic-32": (CH3, lambda: uniform_spec(3, 32, PERIODIC3), 1e-8, 2e-6),
-    "ch3d-dirichlet-16": (CH3, lambda: uniform_spec(3, 16, DIRICHLET3), 1e-8, 2e-6),
-    "ch2d-amr-periodic": (CH2, lambda: H.amr2d(periodic=True), 1e-9, 2e-6),
+    "ch2d-periodic-64": (CH2, lambda: uniform_spec(2, 64, PERIODIC2), 1e-9, 2e-6, 1e-12, 1e-9),
+    "ch2d-neumann-64": (CH2, lambda: uniform_spec(2, 64, NEUMANN2), 1e-9, 2e-6, 1e-12, 1e-9),
+    "ch3d-periodic-32": (CH3, lambda: uniform_spec(3, 32, PERIODIC3), 1e-8, 1e-5, 1e-11, 1e-8),
+    "ch3d-dirichlet-16": (CH3, lambda: uniform_spec(3, 16, DIRICHLET3), 1e-8, 1e-5, 1e-11, 1e-8),
+    "ch2d-amr-periodic": (CH2, lambda: H.amr2d(periodic=True), 1e-9, 2e-6, 1e-12, 1e-9),
 }
 
 
-@pytest.mark.parametrize("case", list(MIXED_CASES))
-def test_mixed_converges_to_fp64_solution(pkg, ctx, oracle_mod, case):
-    cfg, mk, tol, bound = MIXED_CASES[case]
-    spec = mk()
+def _run(pkg, ctx, oracle_mod, cfg, spec, tol):
     g, o = make_pair(pkg, ctx, oracle_mod, cfg, spec)
     nd = cfg["ndims"]
     for p in spec.patches:
@@ -35,8 +36,8 @@ def test_mixed_converges_to_fp64_solution(pkg, ctx, oracle_mod, case):
         o.put(p["id"], "q", q)
     fin, mn = spec.finest(), spec.minlevel()
     for step in range(3):
-        ng, rg = g.time_step(step == 0, fin, mn, tol=tol, maxvcycles=30, mode="mixed")
-        no, ro = o.time_step(step == 0, fin, mn, tol=tol, maxvcycles=30)
+        ng, rg = g.time_step(step == 0, fin, mn, tol=tol, maxvcycles=40, mode="mixed", strict=True)
+        no, ro = o.time_step(step == 0, fin, mn, tol=tol, maxvcycles=40)
         assert rg[-1] < tol, (step, rg)
         assert ng <= no + 3, (step, ng, no, rg, ro)
     worst = 0.0
@@ -44,5 +45,15 @@ def test_mixed_converges_to_fp64_solution(pkg, ctx, oracle_mod, case):
         a, b = g.get(p["id"], "q"), o.get(p["id"], "q")
         n = a.size // 2
         worst = max(worst, float(np.max(np.abs(a[:n] - b[:n])) / np.max(np.abs(b[:n]))))
-    print(f"{case}: mixed vs FP64 oracle, max rel error of phi = {worst:.3e}")
-    assert worst <= bound
+    return worst
+
+
+@pytest.mark.parametrize("case", list(MIXED_CASES))
+def test_mixed_reaches_the_fp64_solution(pkg, ctx, oracle_mod, case):
+    cfg, mk, tol, bound, tight, tight_bound = MIXED_CASES[case]
+    err_tight = _run(pkg, ctx, oracle_mod, cfg, mk(), tight)
+    err = _run(pkg, ctx, oracle_mod, cfg, mk(), tol)
+    print(f"{case}: max rel error of phi vs FP64 oracle: {err:.3e} at tol {tol:g}, "
+          f"{err_tight:.3e} at tol {tight:g}")
+    assert err_tight <= tight_bound
+    assert err <= bound
