@@ -320,6 +320,7 @@ def main():
     mixed = run_arm(h, q0, w, "mixed", args.steps, args.warmup, dist, clocks)
     q_mixed = h.get(0, "q")
     ms_mixed = h.time_smoother(0, "mixed", reps=20)
+    col_mixed = h.smoother_colours(0, "mixed")
     fp64 = run_arm(h, q0, w, "fp64", args.steps, args.warmup, dist)
     q_fp64 = h.get(0, "q")
     ms_fp64 = h.time_smoother(0, "fp64", reps=10)
@@ -333,7 +334,9 @@ def main():
     nphi = q_fp64.size // 2
     err = float(np.max(np.abs(q_mixed[:nphi] - q_fp64[:nphi])) / np.max(np.abs(q_fp64[:nphi])))
     peak, peak_kind = peaks()
-    b_mixed = 18.0 * N  # e read (N*2*4) + g,phib,e-write of one colour (N/2*(2*4+4+2*4))
+    # per colour: e read (N*2*4) + g, phib and e write of that colour (N/2*(2*4+4+2*4)) = 18 N;
+    # a fused launch does both colours: 36 N (the per-sweep figure 4*N*V*s + N*s)
+    b_mixed = 18.0 * N * col_mixed
     b_fp64 = 32.0 * N   # q read (N*2*8) + f read and q write of one colour (N/2*(2*8+2*8))
     ach = b_mixed / (ms_mixed * 1e-3) / 1e9
     ach64 = b_fp64 / (ms_fp64 * 1e-3) / 1e9
@@ -359,10 +362,12 @@ def main():
         "speedup_mixed_vs_fp64": value / v_fp64,
         "error_vs_fp64": {"max_rel_phi": err, "after_steps": args.warmup + args.steps},
         "dof_sweeps_per_s": None,
-        "roofline": {"bound": "hbm", "kernel": "k_mx_relax (FP32 colour sweep, finest level)",
+        "roofline": {"bound": "hbm",
+                     "kernel": ("k_mx_rb3 (fused FP32 red+black sweep, finest level)" if col_mixed == 2
+                                else "k_mx_relax (FP32 colour sweep, finest level)"),
                      "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                      "peak_kind": peak_kind, "bytes_per_launch": b_mixed, "ms_per_launch": ms_mixed,
-                     "traffic": ncu_traffic(args.workload, "k_mx_relax")},
+                     "traffic": ncu_traffic(args.workload, "k_mx_rb3" if col_mixed == 2 else "k_mx_relax")},
         "roofline_fp64": {"bound": "fp64 pipe", "kernel": "k_relax (FP64 colour sweep, finest level)",
                           "achieved_hbm": ach64, "peak_hbm": peak, "frac_hbm": ach64 / peak,
                           "bytes_per_launch": b_fp64, "ms_per_launch": ms_fp64,

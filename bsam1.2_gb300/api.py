@@ -68,6 +68,7 @@ def lib():
         "bsamg_mark": ([P, I], I),
         "bsamg_elapsed_ms": ([P, I, I, DP], I),
         "bsamg_time_smoother": ([P, I, I, I, DP], I),
+        "bsamg_smoother_colours": ([P, I, I, IP], I),
         "bsamg_ch_residual_norm_noalloc": ([P, P, I, IP, D, D, D, I, P, P], I),
         "bsamg_host_register": ([P, SZ], I),
         "bsamg_host_unregister": ([P], I),
@@ -241,6 +242,11 @@ class Hierarchy:
         _ck(lib().bsamg_time_smoother(self.h, level, MODE[mode], reps, ctypes.byref(ms)),
             "bsamg_time_smoother")
         return ms.value
+
+    def smoother_colours(self, level, mode="fp64"):
+        n = ctypes.c_int()
+        _ck(lib().bsamg_smoother_colours(self.h, level, MODE[mode], ctypes.byref(n)), "bsamg_smoother_colours")
+        return n.value
 
     def launch_count(self):
         n = ctypes.c_longlong()

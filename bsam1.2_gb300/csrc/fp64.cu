@@ -316,40 +316,48 @@ __global__ void __launch_bounds__(kBlock) k_correct_a(const PatchDev* __restrict
 }
 
 // CorrectFine step 2: q(0:mx+1) += BiLinProlongationP1(qc)
-// (gridutilities.f90:156-195) / TriLinProlongationP1 (:510-566).  Each
-// thread recomputes the intermediate b (and c) entries it needs with the
-// reference's expressions, so the sums match the array form exactly.
+// (gridutilities.f90:156-195) / TriLinProlongationP1 (:510-566).  One
+// thread per coarse index (ci,cj,ck) in 0..cmx produces fine cells
+// 2ci..2ci+1 (and likewise in y, z): it forms the reference's intermediate
+// b (and c) entries for its 2x2(x2) coarse values with the reference's
+// expressions, so every fine value is bit-identical to the array form.
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_correct_b(const PatchDev* __restrict__ P, double* __restrict__ pool,
                                                       const Blk* __restrict__ blk, int nrvars) {
   const Blk b = blk[blockIdx.x];
   const PatchDev& p = P[b.patch];
-  int i, j, k;
-  if (!ghosted_cell<DIM>(p.qn, b.start + threadIdx.x, i, j, k)) return;
-  int ci = i >> 1, cj = j >> 1, ck = k >> 1;
-  bool ei = (i & 1) == 0, ej = (j & 1) == 0, ek = (k & 1) == 0;
-  long long dst = gofs<DIM>(p.qn, i, j, k);
+  int cpn[3] = {p.cmx[0] + 1, p.cmx[1] + 1, DIM == 3 ? p.cmx[2] + 1 : 1};
+  int t = b.start + threadIdx.x;
+  int ci = t % cpn[0], r = t / cpn[0];
+  int cj = r % cpn[1], ck = r / cpn[1];
+  if (ck >= cpn[2]) return;
+  const int nz = DIM == 3 ? 2 : 1;
   for (int v = 0; v < nrvars; v++) {
     const double* a = pool + p.oqc + v * p.sc;
-    // x-direction: b(i, cy, cz) from a(ci, cy, cz), a(ci+1, cy, cz)
-    auto bx = [&](int cy, int cz) {
-      double lo = a[gofs<DIM>(p.cn, ci, cy, cz)], hi = a[gofs<DIM>(p.cn, ci + 1, cy, cz)];
-      return ei ? 3.0 * lo + hi : lo + 3.0 * hi;
-    };
-    double add;
-    if (DIM == 2) {
-      double blo = bx(cj, 0), bhi = bx(cj + 1, 0);
-      add = ej ? (3.0 * blo + bhi) / 16.0 : (blo + 3.0 * bhi) / 16.0;
-    } else {
-      auto cy = [&](int cz) {
-        double blo = bx(cj, cz), bhi = bx(cj + 1, cz);
-        return ej ? 3.0 * blo + bhi : blo + 3.0 * bhi;
-      };
-      double clo = cy(ck), chi = cy(ck + 1);
-      add = ek ? (3.0 * clo + chi) / 64.0 : (clo + 3.0 * chi) / 64.0;
-    }
     double* q = pool + p.oq + v * p.sq;
-    q[dst] = q[dst] + add;
+    double bxv[2][2][2];
+    for (int dz = 0; dz < nz; dz++)
+      for (int dy = 0; dy < 2; dy++) {
+        double lo = a[gofs<DIM>(p.cn, ci, cj + dy, ck + dz)], hi = a[gofs<DIM>(p.cn, ci + 1, cj + dy, ck + dz)];
+        bxv[dz][dy][0] = 3.0 * lo + hi;
+        bxv[dz][dy][1] = lo + 3.0 * hi;
+      }
+    for (int fz = 0; fz < nz; fz++)
+      for (int fy = 0; fy < 2; fy++)
+        for (int fx = 0; fx < 2; fx++) {
+          int i = 2 * ci + fx, j = 2 * cj + fy, k = DIM == 3 ? 2 * ck + fz : 0;
+          double add;
+          if (DIM == 2) {
+            double blo = bxv[0][0][fx], bhi = bxv[0][1][fx];
+            add = fy == 0 ? (3.0 * blo + bhi) / 16.0 : (blo + 3.0 * bhi) / 16.0;
+          } else {
+            double c0 = fy == 0 ? 3.0 * bxv[0][0][fx] + bxv[0][1][fx] : bxv[0][0][fx] + 3.0 * bxv[0][1][fx];
+            double c1 = fy == 0 ? 3.0 * bxv[1][0][fx] + bxv[1][1][fx] : bxv[1][0][fx] + 3.0 * bxv[1][1][fx];
+            add = fz == 0 ? (3.0 * c0 + c1) / 64.0 : (c0 + 3.0 * c1) / 64.0;
+          }
+          long long dst = gofs<DIM>(p.qn, i, j, k);
+          q[dst] = q[dst] + add;
+        }
   }
 }
 

@@ -96,7 +96,7 @@ int enq_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
     RET(after_launch(H, launch_coarse_load(c, L.d_blk[kKindCoarse], L.nblk[kKindCoarse])));
     RET(enq_vcycle(H, level - 1, minlevel, nsmooth));
     RET(after_launch(H, launch_correct_a(c, L.d_blk[kKindCGhost], L.nblk[kKindCGhost])));
-    RET(after_launch(H, launch_correct_b(c, L.d_blk[kKindFGhost], L.nblk[kKindFGhost])));
+    RET(after_launch(H, launch_correct_b(c, L.d_blk[kKindProl], L.nblk[kKindProl])));
     RET(enq_set_ghost(H, level, 0));
     RET(enq_level_relax(H, level, nsmooth));
   }
@@ -364,6 +364,9 @@ int upload_blocks(Hier& H, LevelT& L, int kind) {
       case kKindCoarse: units = P.parent >= 0 ? (long long)P.cmx[0] * P.cmx[1] * P.cmx[2] : 0; break;
       case kKindCGhost: units = P.parent >= 0 ? (long long)P.cn[0] * P.cn[1] * P.cn[2] : 0; break;
       case kKindFGhost: units = (long long)P.qn[0] * P.qn[1] * P.qn[2]; break;
+      case kKindProl:
+        units = P.parent >= 0 ? (long long)(P.cmx[0] + 1) * (P.cmx[1] + 1) * (H.ndims == 3 ? P.cmx[2] + 1 : 1) : 0;
+        break;
     }
     for (long long s = 0; s < units; s += kBlock) v.push_back(Blk{p, (int)s});
   }
@@ -871,6 +874,13 @@ int bsamg_host_register(void* ptr, size_t bytes) {
 int bsamg_host_unregister(void* ptr) {
   if (!ptr) return BSAMG_ERR_ARG;
   CK(cudaHostUnregister(ptr));
+  return BSAMG_OK;
+}
+
+int bsamg_smoother_colours(bsamg_hier* h, int level, int mode, int* colours) {
+  if (!h || !h->committed || !level_ok(*h, level) || !colours) return BSAMG_ERR_ARG;
+  (void)mode;
+  *colours = 1;  // every smoother launch updates one colour
   return BSAMG_OK;
 }
 

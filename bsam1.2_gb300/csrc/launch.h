@@ -24,7 +24,8 @@ enum Kind : int {
   kKindCoarse = 2,    // one coarse cell under a child: cmx1*cmx2*cmx3
   kKindCGhost = 3,    // one ghosted coarse cell: (cmx+2)^d
   kKindFGhost = 4,    // one ghosted fine cell: (mx+2)^d
-  kNKind = 5
+  kKindProl = 5,      // one coarse index 0..cmx per dimension under a child: (cmx+1)^d
+  kNKind = 6
 };
 
 // ---- plain FP64 path (fp64.cu, built with --fmad=false) ----

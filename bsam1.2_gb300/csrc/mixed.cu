@@ -309,37 +309,50 @@ __global__ void __launch_bounds__(kBlock) k_mx_coarse_load(const PatchDev* __res
   fpool[par.eg + par.sf + pf] = R1 + m1;
 }
 
-// CorrectFine step 2 on e: e(0:mx+1) += P(ec) (interior only with WRAP)
+// CorrectFine step 2 on e: e(0:mx+1) += P(ec) (interior only with WRAP).
+// One thread per coarse index (ci,cj,ck) in 0..cmx: it produces the fine
+// cells 2ci..2ci+1 (x) etc. from the 2x2(x2) coarse values they share, with
+// the same per-direction (3,1)/4 weights as BiLin/TriLinProlongationP1
+// (gridutilities.f90:156-195, :510-566).
 template <int DIM, bool WRAP>
 __global__ void __launch_bounds__(kBlock) k_mx_prolong(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                        const Blk* __restrict__ blk, int nrvars) {
   const Blk b = blk[blockIdx.x];
   const PatchDev& p = P[b.patch];
-  int i, j, k;
-  if (!ghosted_cell<DIM>(p.qn, b.start + threadIdx.x, i, j, k)) return;
-  if (WRAP && (i == 0 || i > p.mx[0] || j == 0 || j > p.mx[1] || (DIM == 3 && (k == 0 || k > p.mx[2])))) return;
-  int ci = i >> 1, cj = j >> 1, ck = k >> 1;
-  bool ei = (i & 1) == 0, ej = (j & 1) == 0, ek = (k & 1) == 0;
-  long long dst = gofs<DIM>(p.qn, i, j, k);
+  int cpn[3] = {p.cmx[0] + 1, p.cmx[1] + 1, DIM == 3 ? p.cmx[2] + 1 : 1};
+  int t = b.start + threadIdx.x;
+  int ci = t % cpn[0], r = t / cpn[0];
+  int cj = r % cpn[1], ck = r / cpn[1];
+  if (ck >= cpn[2]) return;
+  const int nz = DIM == 3 ? 2 : 1;
   for (int v = 0; v < nrvars; v++) {
     const float* a = fpool + p.ecq + v * p.sc;
-    auto bx = [&](int cy, int cz) {
-      float lo = a[gofs<DIM>(p.cn, ci, cy, cz)], hi = a[gofs<DIM>(p.cn, ci + 1, cy, cz)];
-      return ei ? 3.0f * lo + hi : lo + 3.0f * hi;
-    };
-    float add;
-    if (DIM == 2) {
-      float blo = bx(cj, 0), bhi = bx(cj + 1, 0);
-      add = (ej ? 3.0f * blo + bhi : blo + 3.0f * bhi) * (1.0f / 16.0f);
-    } else {
-      auto cy = [&](int cz) {
-        float blo = bx(cj, cz), bhi = bx(cj + 1, cz);
-        return ej ? 3.0f * blo + bhi : blo + 3.0f * bhi;
-      };
-      float clo = cy(ck), chi = cy(ck + 1);
-      add = (ek ? 3.0f * clo + chi : clo + 3.0f * chi) * (1.0f / 64.0f);
-    }
-    fpool[p.eq + v * p.sq + dst] += add;
+    float* e = fpool + p.eq + v * p.sq;
+    // x-direction values b[dz][dy][fx] for coarse rows (cj+dy, ck+dz)
+    float bxv[2][2][2];
+    for (int dz = 0; dz < nz; dz++)
+      for (int dy = 0; dy < 2; dy++) {
+        float lo = a[gofs<DIM>(p.cn, ci, cj + dy, ck + dz)], hi = a[gofs<DIM>(p.cn, ci + 1, cj + dy, ck + dz)];
+        bxv[dz][dy][0] = 3.0f * lo + hi;
+        bxv[dz][dy][1] = lo + 3.0f * hi;
+      }
+    for (int fz = 0; fz < nz; fz++)
+      for (int fy = 0; fy < 2; fy++)
+        for (int fx = 0; fx < 2; fx++) {
+          int i = 2 * ci + fx, j = 2 * cj + fy, k = DIM == 3 ? 2 * ck + fz : 0;
+          if (WRAP && (i == 0 || i > p.mx[0] || j == 0 || j > p.mx[1] || (DIM == 3 && (k == 0 || k > p.mx[2]))))
+            continue;
+          float add;
+          if (DIM == 2) {
+            float blo = bxv[0][0][fx], bhi = bxv[0][1][fx];
+            add = (fy == 0 ? 3.0f * blo + bhi : blo + 3.0f * bhi) * (1.0f / 16.0f);
+          } else {
+            float c0 = fy == 0 ? 3.0f * bxv[0][0][fx] + bxv[0][1][fx] : bxv[0][0][fx] + 3.0f * bxv[0][1][fx];
+            float c1 = fy == 0 ? 3.0f * bxv[1][0][fx] + bxv[1][1][fx] : bxv[1][0][fx] + 3.0f * bxv[1][1][fx];
+            add = (fz == 0 ? 3.0f * c0 + c1 : c0 + 3.0f * c1) * (1.0f / 64.0f);
+          }
+          e[gofs<DIM>(p.qn, i, j, k)] += add;
+        }
   }
 }
 
@@ -429,11 +442,13 @@ __global__ void __launch_bounds__(kBlock) k_mx_norm(const PatchDev* __restrict__
 template <int DIM, bool WRAP>
 __global__ void __launch_bounds__(kBlock) k_mx_track(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                      const Blk* __restrict__ blk, double* __restrict__ partial) {
-  __shared__ double red[2][kBlock / 32];
+  // sums of squares in FP32 (the tracked norm only decides when to
+  // re-evaluate in FP64); one conversion per block, no FP64 shuffles
+  __shared__ float red[2][kBlock / 32];
   const Blk b = blk[blockIdx.x];
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  double s0 = 0.0, s1 = 0.0;
+  float s0 = 0.f, s1 = 0.f;
   if (interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) {
     const float* e = fpool + p.eq;
     long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
@@ -446,8 +461,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_track(const PatchDev* __restrict_
     float g1 = fpool[p.eg + p.sf + fc] - m1;
     fpool[p.eg + fc] = g0;
     fpool[p.eg + p.sf + fc] = g1;
-    s0 = (double)g0 * g0;
-    s1 = (double)g1 * g1;
+    s0 = g0 * g0;
+    s1 = g1 * g1;
   }
   for (int o = 16; o > 0; o >>= 1) {
     s0 += __shfl_down_sync(0xffffffffu, s0, o);
@@ -460,13 +475,13 @@ __global__ void __launch_bounds__(kBlock) k_mx_track(const PatchDev* __restrict_
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t0 = 0.0, t1 = 0.0;
+    float t0 = 0.f, t1 = 0.f;
     for (int m = 0; m < kBlock / 32; m++) {
       t0 += red[0][m];
       t1 += red[1][m];
     }
-    partial[2 * blockIdx.x] = t0;
-    partial[2 * blockIdx.x + 1] = t1;
+    partial[2 * blockIdx.x] = (double)t0;
+    partial[2 * blockIdx.x + 1] = (double)t1;
   }
 }
 
@@ -589,7 +604,7 @@ int mx_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
     MX_LAUNCH_W(H, kKindCoarse, k_mx_coarse_load, H.dP, H.fpool, L.d_blk[kKindCoarse]);
     if ((r = mx_vcycle(H, level - 1, minlevel, nsmooth))) return r;
     MX_LAUNCH_W(H, kKindCGhost, k_mx_coarse_ring, H.dP, H.fpool, L.d_blk[kKindCGhost], H.nrvars, 1);
-    MX_LAUNCH_W(H, kKindFGhost, k_mx_prolong, H.dP, H.fpool, L.d_blk[kKindFGhost], H.nrvars);
+    MX_LAUNCH_W(H, kKindProl, k_mx_prolong, H.dP, H.fpool, L.d_blk[kKindProl], H.nrvars);
     if ((r = mx_set_ghost(H, level, 0))) return r;
     if ((r = mx_level_relax(H, level, nsmooth))) return r;
   }

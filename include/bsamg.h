@@ -155,6 +155,9 @@ int bsamg_elapsed_ms(bsamg_hier* h, int a, int b, double* ms);
  * time of one launch; the state is modified. */
 int bsamg_time_smoother(bsamg_hier* h, int level, int mode, int reps,
                         double* ms_per_launch);
+/* Colours one launch of that smoother updates (1: each launch is one
+ * colour half-sweep). */
+int bsamg_smoother_colours(bsamg_hier* h, int level, int mode, int* colours);
 
 /* Allocation-free convergence norm of one CH patch.  No counterpart in the
  * reference: it exists for callers that cannot let a library call

@@ -21,6 +21,7 @@ MIXED_CASES = {
     "ch2d-periodic-64": (CH2, lambda: uniform_spec(2, 64, PERIODIC2), 1e-9, 2e-6, 1e-12, 1e-9),
     "ch2d-neumann-64": (CH2, lambda: uniform_spec(2, 64, NEUMANN2), 1e-9, 2e-6, 1e-12, 1e-9),
     "ch3d-periodic-32": (CH3, lambda: uniform_spec(3, 32, PERIODIC3), 1e-8, 1e-5, 1e-11, 1e-8),
+    "ch3d-periodic-64": (CH3, lambda: uniform_spec(3, 64, PERIODIC3), 1e-8, 1e-5, 1e-11, 1e-8),
     "ch3d-dirichlet-16": (CH3, lambda: uniform_spec(3, 16, DIRICHLET3), 1e-8, 1e-5, 1e-11, 1e-8),
     "ch2d-amr-periodic": (CH2, lambda: H.amr2d(periodic=True), 1e-9, 2e-6, 1e-12, 1e-9),
 }
