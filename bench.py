@@ -292,18 +292,64 @@ def reference_arm(args, w, dist):
     print(json.dumps(line), flush=True)
 
 
+def serve_arm(args, dist):
+    """--workload serve: the serving configuration.  Poisson arrivals (mean
+    200/s, seeded) of independent CH requests, replayed in real time against
+    the continuous-batching loop, once with the mixed path and once with the
+    plain FP64 path; value = completed time steps per second of the mixed run."""
+    import __graft_entry__ as ge
+    ge._load_build_module().build()
+    pkg = ge.load_package()
+    duration = max(0.5, args.steps / 10.0)
+    out = {}
+    for mode in ("mixed", "fp64"):
+        ctx = pkg.Context(dist.local, hbm_budget=int(args.serve_budget_gb * 2**30))
+        warm = pkg.serve.poisson_stream(200.0, 0.05, seed=7, mode=mode)
+        pkg.serve.serve(ctx, warm, slots=args.serve_slots)
+        reqs = pkg.serve.poisson_stream(200.0, duration, seed=2024, mode=mode)
+        stats = {}
+        done, wall = pkg.serve.serve(ctx, reqs, slots=args.serve_slots, stats=stats)
+        ctx.close()
+        out[mode] = dict(pkg.serve.summarize(done, wall), **stats)
+    m, f = out["mixed"], out["fp64"]
+    line = {
+        "metric": METRIC, "value": m["steps_per_s"], "unit": "steps/s", "n_gpus": dist.ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 / m["steps_per_s"] if m["steps_per_s"] else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded Poisson arrivals and spinodal starts)",
+        "config": {"workload": "serve", "arrival_rate_per_s": 200.0, "arrival_window_s": duration,
+                   "slots": args.serve_slots, "hbm_budget_gb": args.serve_budget_gb,
+                   "mix": "2D roots {32,64,128,256}^2 with 0-3 nested levels, 3D roots {32,64}^3, 1-20 steps"},
+        "p50_ms": m["p50_ms"], "p99_ms": m["p99_ms"], "serving_mixed": m, "serving_fp64": f,
+        "speedup_mixed_vs_fp64": m["steps_per_s"] / f["steps_per_s"] if f["steps_per_s"] else None,
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=17)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ch3d-256", choices=list(WORKLOADS))
+    ap.add_argument("--workload", default="ch3d-256", choices=list(WORKLOADS) + ["serve"])
+    ap.add_argument("--serve-slots", type=int, default=32)
+    ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
-    w = WORKLOADS[args.workload]
     dist = Dist()
+    if args.workload == "serve":
+        if args.impl == "reference":
+            if dist.rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the serving loop has no CPU counterpart in "
+                                  "the reference (a single serial solve per run)"}), flush=True)
+        else:
+            serve_arm(args, dist)
+        dist.close()
+        return
+    w = WORKLOADS[args.workload]
     if args.impl == "reference":
         reference_arm(args, w, dist)
         dist.close()

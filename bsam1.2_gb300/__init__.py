@@ -5,3 +5,4 @@ include/bsamg.h); this package is its Python host mirror.
 """
 from .api import BsamgError, Context, Hierarchy, exported_symbols, lib, pin, unpin  # noqa: F401
 from . import initial  # noqa: F401
+from . import serve  # noqa: F401

@@ -372,9 +372,10 @@ int upload_blocks(Hier& H, LevelT& L, int kind) {
   }
   L.nblk[kind] = (int)v.size();
   if (v.empty()) return BSAMG_OK;
-  CK(cudaMalloc(&L.d_blk[kind], sizeof(Blk) * v.size()));
+  CK(cudaMallocAsync((void**)&L.d_blk[kind], sizeof(Blk) * v.size(), H.s));
   H.bytes += sizeof(Blk) * v.size();
-  CK(cudaMemcpy(L.d_blk[kind], v.data(), sizeof(Blk) * v.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(L.d_blk[kind], v.data(), sizeof(Blk) * v.size(), cudaMemcpyHostToDevice, H.s));
+  CK(cudaStreamSynchronize(H.s));  // v is freed on return
   return BSAMG_OK;
 }
 
@@ -402,12 +403,42 @@ bool ghost_ops_in_bounds(const Hier& H, const GhostProg& g) {
 int upload_ghost(Hier& H, GhostProg& g) {
   if (g.ops.empty()) return BSAMG_OK;
   if (!ghost_ops_in_bounds(H, g)) return BSAMG_ERR_ARG;
-  CK(cudaMalloc(&g.d_ops, sizeof(GhostOp) * g.ops.size()));
-  CK(cudaMalloc(&g.d_stage_off, sizeof(int) * g.stage_off.size()));
+  CK(cudaMallocAsync((void**)&g.d_ops, sizeof(GhostOp) * g.ops.size(), H.s));
+  CK(cudaMallocAsync((void**)&g.d_stage_off, sizeof(int) * g.stage_off.size(), H.s));
   H.bytes += sizeof(GhostOp) * g.ops.size() + sizeof(int) * g.stage_off.size();
-  CK(cudaMemcpy(g.d_ops, g.ops.data(), sizeof(GhostOp) * g.ops.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(g.d_stage_off, g.stage_off.data(), sizeof(int) * g.stage_off.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(g.d_ops, g.ops.data(), sizeof(GhostOp) * g.ops.size(), cudaMemcpyHostToDevice, H.s));
+  CK(cudaMemcpyAsync(g.d_stage_off, g.stage_off.data(), sizeof(int) * g.stage_off.size(), cudaMemcpyHostToDevice,
+                     H.s));
   return BSAMG_OK;
+}
+
+// Pinned host words for the norm read-back come from a per-context pool, so
+// hierarchies never call cudaMallocHost/cudaFreeHost (the latter
+// synchronises the device) while other hierarchies run.
+constexpr int kPinnedSlots = 1024, kSlotDoubles = 16;
+
+int pinned_slot_take(Hier& H) {
+  bsamg_ctx* c = H.ctx;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->pinned) {
+    CK(cudaMallocHost((void**)&c->pinned, sizeof(double) * kSlotDoubles * kPinnedSlots));
+    for (int i = kPinnedSlots - 1; i >= 0; i--) c->free_slots.push_back(i);
+  }
+  if (c->free_slots.empty()) return BSAMG_ERR_BUDGET;
+  H.pinned_slot = c->free_slots.back();
+  c->free_slots.pop_back();
+  H.h_norm = c->pinned + (size_t)H.pinned_slot * kSlotDoubles;
+  H.h_nonfinite = reinterpret_cast<int*>(H.h_norm + 8);
+  return BSAMG_OK;
+}
+
+void pinned_slot_give(Hier& H) {
+  if (H.pinned_slot < 0) return;
+  std::lock_guard<std::mutex> lk(H.ctx->mu);
+  H.ctx->free_slots.push_back(H.pinned_slot);
+  H.pinned_slot = -1;
+  H.h_norm = nullptr;
+  H.h_nonfinite = nullptr;
 }
 
 int commit(Hier& H) {
@@ -492,10 +523,13 @@ int commit(Hier& H) {
     std::lock_guard<std::mutex> lk(H.ctx->mu);
     if (H.ctx->budget && H.ctx->used + need > H.ctx->budget) return BSAMG_ERR_BUDGET;
     H.ctx->used += need;
+    H.reserved = need;
   }
   H.bytes += need;
   CK(cudaStreamCreateWithFlags(&H.s, cudaStreamNonBlocking));
-  CK(cudaMalloc(&H.pool, H.pool_elems * sizeof(double)));
+  // stream-ordered allocations: creating or destroying a hierarchy never
+  // synchronises the device, so other hierarchies' work keeps running
+  CK(cudaMallocAsync((void**)&H.pool, H.pool_elems * sizeof(double), H.s));
   CK(cudaMemsetAsync(H.pool, 0, H.pool_elems * sizeof(double), H.s));
   RET(mixed_alloc(H));
 
@@ -520,8 +554,9 @@ int commit(Hier& H) {
     coefficients(H, P.dx[0], D.c);
     for (int x = 0; x < 4; x++) D.cf[x] = (float)D.c[x];
   }
-  CK(cudaMalloc(&H.dP, sizeof(PatchDev) * pd.size()));
-  CK(cudaMemcpy(H.dP, pd.data(), sizeof(PatchDev) * pd.size(), cudaMemcpyHostToDevice));
+  CK(cudaMallocAsync((void**)&H.dP, sizeof(PatchDev) * pd.size(), H.s));
+  CK(cudaMemcpyAsync(H.dP, pd.data(), sizeof(PatchDev) * pd.size(), cudaMemcpyHostToDevice, H.s));
+  CK(cudaStreamSynchronize(H.s));  // pd is freed on return
   H.bytes += sizeof(PatchDev) * pd.size();
 
   int maxblk = 1;
@@ -549,11 +584,10 @@ int commit(Hier& H) {
   }
   RET(mixed_tables(H));
   H.partial_cap = maxblk;
-  CK(cudaMalloc(&H.d_partial, sizeof(double) * 2 * (size_t)maxblk * std::max(1, H.nrvars)));
-  CK(cudaMalloc(&H.d_norm, sizeof(double) * 8));
-  CK(cudaMalloc(&H.d_nonfinite, sizeof(int) * 4));
-  CK(cudaMallocHost(&H.h_norm, sizeof(double) * 8));
-  CK(cudaMallocHost(&H.h_nonfinite, sizeof(int) * 4));
+  CK(cudaMallocAsync((void**)&H.d_partial, sizeof(double) * 2 * (size_t)maxblk * std::max(1, H.nrvars), H.s));
+  CK(cudaMallocAsync((void**)&H.d_norm, sizeof(double) * 8, H.s));
+  CK(cudaMallocAsync((void**)&H.d_nonfinite, sizeof(int) * 4, H.s));
+  RET(pinned_slot_take(H));
   CK(cudaStreamSynchronize(H.s));
   H.committed = true;
   return BSAMG_OK;
@@ -569,28 +603,31 @@ void release(Hier& H) {
   H.graphs.clear();
   for (int l = 0; l < kNLev; l++) {
     LevelT& L = H.lev[l];
-    for (int k = 0; k < kNKind; k++) cudaFree(L.d_blk[k]);
+    for (int k = 0; k < kNKind; k++)
+      if (L.d_blk[k]) cudaFreeAsync(L.d_blk[k], H.s);
     for (int ip = 0; ip < 3; ip++) {
       bool shared = ip > 0 && L.gp[ip].d_ops == L.gp[0].d_ops;
       if (!shared) {
-        cudaFree(L.gp[ip].d_ops);
-        cudaFree(L.gp[ip].d_stage_off);
+        if (L.gp[ip].d_ops) cudaFreeAsync(L.gp[ip].d_ops, H.s);
+        if (L.gp[ip].d_stage_off) cudaFreeAsync(L.gp[ip].d_stage_off, H.s);
       }
     }
   }
   mixed_free(H);
-  cudaFree(H.dP);
-  cudaFree(H.pool);
-  cudaFree(H.d_partial);
-  cudaFree(H.d_norm);
-  cudaFree(H.d_nonfinite);
-  if (H.h_norm) cudaFreeHost(H.h_norm);
-  if (H.h_nonfinite) cudaFreeHost(H.h_nonfinite);
-  if (H.s) cudaStreamDestroy(H.s);
-  if (H.committed) {
+  if (H.dP) cudaFreeAsync(H.dP, H.s);
+  if (H.pool) cudaFreeAsync(H.pool, H.s);
+  if (H.d_partial) cudaFreeAsync(H.d_partial, H.s);
+  if (H.d_norm) cudaFreeAsync(H.d_norm, H.s);
+  if (H.d_nonfinite) cudaFreeAsync(H.d_nonfinite, H.s);
+  pinned_slot_give(H);
+  if (H.s) {
+    cudaStreamSynchronize(H.s);
+    cudaStreamDestroy(H.s);
+  }
+  if (H.reserved) {
     std::lock_guard<std::mutex> lk(H.ctx->mu);
-    size_t need = H.pool_elems * sizeof(double) + mixed_pool_bytes(H);
-    H.ctx->used -= std::min(H.ctx->used, need);
+    H.ctx->used -= std::min(H.ctx->used, H.reserved);
+    H.reserved = 0;
   }
 }
 
@@ -638,6 +675,10 @@ int bsamg_init(int device, size_t hbm_budget_bytes, bsamg_ctx** out) {
 }
 
 int bsamg_finalize(bsamg_ctx* ctx) {
+  if (ctx && ctx->pinned) {
+    cudaSetDevice(ctx->device);
+    cudaFreeHost(ctx->pinned);
+  }
   delete ctx;
   return BSAMG_OK;
 }

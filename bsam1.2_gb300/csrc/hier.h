@@ -70,6 +70,7 @@ struct Hier {
   size_t e_coarse_off = 0, e_coarse_len = 0;  // the part of it on levels < 0
   Blk* mx_norm_blk[kNLev] = {};               // padded interior lists (mixed norm)
   size_t bytes = 0;
+  size_t reserved = 0;  // bytes counted against the context budget
 
   LevelT lev[kNLev];
   cudaStream_t s = nullptr;
@@ -77,7 +78,8 @@ struct Hier {
   int partial_cap = 0;
   double* d_norm = nullptr;      // [0] norm, [1] raw sum, plus scratch
   int* d_nonfinite = nullptr;
-  double* h_norm = nullptr;      // pinned
+  int pinned_slot = -1;
+  double* h_norm = nullptr;      // pinned (a slot of the context's pool)
   int* h_nonfinite = nullptr;    // pinned
   long long launches = 0;
   bool capturing = false;
@@ -125,6 +127,8 @@ struct bsamg_ctx {
   size_t budget = 0;
   size_t used = 0;
   std::mutex mu;
+  double* pinned = nullptr;     // pinned read-back words, one slot per hierarchy
+  std::vector<int> free_slots;
 };
 
 struct bsamg_hier : bsamg::Hier {};

@@ -743,18 +743,18 @@ int mixed_alloc(Hier& H) {
     P.e_ophi = off[4 * p + 3];
   }
   H.fpool_elems = n;
-  cudaError_t e = cudaMalloc(&H.fpool, n * sizeof(float));
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(fpool)");
+  cudaError_t e = cudaMallocAsync((void**)&H.fpool, n * sizeof(float), H.s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(fpool)");
   e = cudaMemsetAsync(H.fpool, 0, n * sizeof(float), H.s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(fpool)");
   return BSAMG_OK;
 }
 
 void mixed_free(Hier& H) {
-  if (H.fpool) cudaFree(H.fpool);
+  if (H.fpool) cudaFreeAsync(H.fpool, H.s);
   H.fpool = nullptr;
   for (int l = 0; l < kNLev; l++) {
-    if (H.mx_norm_blk[l]) cudaFree(H.mx_norm_blk[l]);
+    if (H.mx_norm_blk[l]) cudaFreeAsync(H.mx_norm_blk[l], H.s);
     H.mx_norm_blk[l] = nullptr;
   }
 }
@@ -771,10 +771,12 @@ int mixed_tables(Hier& H) {
     }
     while (v.size() % kNormCells) v.push_back(Blk{-1, 0});
     Blk* d = nullptr;
-    cudaError_t e = cudaMalloc(&d, sizeof(Blk) * v.size());
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(norm list)");
-    e = cudaMemcpy(d, v.data(), sizeof(Blk) * v.size(), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(norm list)");
+    cudaError_t e = cudaMallocAsync((void**)&d, sizeof(Blk) * v.size(), H.s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(norm list)");
+    e = cudaMemcpyAsync(d, v.data(), sizeof(Blk) * v.size(), cudaMemcpyHostToDevice, H.s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(norm list)");
+    e = cudaStreamSynchronize(H.s);  // v is freed at the end of the iteration
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
     H.mx_norm_blk[l + kMaxDepth] = d;
     H.bytes += sizeof(Blk) * v.size();
   }
