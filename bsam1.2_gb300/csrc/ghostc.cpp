@@ -164,6 +164,188 @@ struct Emitter {
     }
   }
 
+  // GetFaceIndex, boundary.f90:1018-1045: [0] ghost index, [1] second fine
+  // cell, [2] first fine cell, [3] parent cell beyond the patch, [4] parent
+  // cell at the patch edge, for the low (parity 1) or high (2) side of d.
+  void face_index(const HostPatch& F, int d, int parity, int fi[5]) const {
+    if (parity == 1) {
+      fi[0] = 0, fi[1] = 2, fi[2] = 1, fi[3] = F.mbounds[d][0] - 1, fi[4] = F.mbounds[d][0];
+    } else {
+      fi[0] = F.mx[d] + 1, fi[1] = F.mx[d] - 1, fi[2] = F.mx[d], fi[3] = F.mbounds[d][1] + 1,
+      fi[4] = F.mbounds[d][1];
+    }
+  }
+  // one 3D interpolated ghost cell; kind 0: kGCfA, 1: kGCfAB, 2: kGCfAC
+  void cf3(int f, int c, int kind, const int* g, const int* s1, const int* s2, const int (*cc)[3]) {
+    static const int types[3] = {kGCfA, kGCfAB, kGCfAC};
+    int nc = kind == 0 ? 1 : kind == 1 ? 3 : 4;
+    int co[4] = {0, 0, 0, 0};
+    for (int x = 0; x < nc; x++) co[x] = cell(c, cc[x][0], cc[x][1], cc[x][2]);
+    cf(types[kind], f, cell(f, g[0], g[1], g[2]), cell(f, s1[0], s1[1], s1[2]), cell(f, s2[0], s2[1], s2[2]), c,
+       co[0], co[1], co[2], co[3]);
+  }
+  // an edge: dimensions d1, d2 fixed by the face indices fa, fb; t runs
+  // (the four statements of each edge group, boundary.f90:1107-1126)
+  void cf3_edge(int f, int c, int d1, const int* fa, int d2, const int* fb, int t) {
+    const HostPatch& F = H.patches[f];
+    int mx = F.mx[t], lo = F.mbounds[t][0], hi = F.mbounds[t][1];
+    int g[3], s1[3], s2[3], cc[4][3];
+    g[d1] = fa[0], s1[d1] = fa[1], s2[d1] = fa[2];
+    g[d2] = fb[0], s1[d2] = fb[1], s2[d2] = fb[2];
+    for (int x = 0; x < 4; x++) cc[x][d1] = fa[3], cc[x][d2] = fb[3];
+    for (int i = 3, n = 0; i <= mx - 1; i += 2, n++) {
+      g[t] = i, s1[t] = i - 2, s2[t] = i - 1, cc[0][t] = lo + 1 + n;
+      cf3(f, c, 0, g, s1, s2, cc);
+    }
+    g[t] = s1[t] = s2[t] = 1;
+    cc[0][t] = lo - 1, cc[1][t] = lo, cc[2][t] = lo + 1;
+    cf3(f, c, 1, g, s1, s2, cc);
+    for (int i = 2, n = 0; i <= mx - 2; i += 2, n++) {
+      g[t] = i, s1[t] = i + 2, s2[t] = i + 1, cc[0][t] = lo + n;
+      cf3(f, c, 0, g, s1, s2, cc);
+    }
+    g[t] = s1[t] = s2[t] = mx;
+    cc[0][t] = hi + 1, cc[1][t] = hi, cc[2][t] = hi - 1;
+    cf3(f, c, 1, g, s1, s2, cc);
+  }
+  // one colour class of a face with normal n (index fn) and tangential
+  // dimensions t1 < t2.  cls 0 yellow (t1, t2 even), 1 blue (odd, odd),
+  // 2 green (odd, even), 3 red (even, odd); each is its strided bulk and its
+  // two edge rows, where the parent value is a b-combination along the
+  // dimension that sits at its end (boundary.f90:1236-1320 and analogues).
+  void cf3_face_class(int f, int c, int n, const int* fn, int t1, int t2, int cls) {
+    const HostPatch& F = H.patches[f];
+    int m1 = F.mx[t1], m2 = F.mx[t2];
+    int l1 = F.mbounds[t1][0], h1 = F.mbounds[t1][1], l2 = F.mbounds[t2][0], h2 = F.mbounds[t2][1];
+    int g[3], s1[3], s2[3], cc[4][3];
+    g[n] = fn[0], s1[n] = fn[1], s2[n] = fn[2];
+    for (int x = 0; x < 4; x++) cc[x][n] = fn[3];
+    bool e1 = cls == 0 || cls == 3, e2 = cls == 0 || cls == 2;
+    int a1lo = e1 ? 2 : 3, a1hi = e1 ? m1 - 2 : m1 - 1, a2lo = e2 ? 2 : 3, a2hi = e2 ? m2 - 2 : m2 - 1;
+    int d1 = e1 ? 1 : -1, d2 = e2 ? 1 : -1;
+    auto par1 = [&](int i) { return e1 ? l1 + i / 2 - 1 : l1 + (i - 1) / 2; };
+    auto par2 = [&](int j) { return e2 ? l2 + j / 2 - 1 : l2 + (j - 1) / 2; };
+    for (int j = a2lo; j <= a2hi; j += 2)
+      for (int i = a1lo; i <= a1hi; i += 2) {
+        g[t1] = i, g[t2] = j;
+        s1[t1] = i + 2 * d1, s1[t2] = j + 2 * d2;
+        s2[t1] = i + d1, s2[t2] = j + d2;
+        cc[0][t1] = par1(i), cc[0][t2] = par2(j);
+        cf3(f, c, 0, g, s1, s2, cc);
+      }
+    for (int j = a2lo; j <= a2hi; j += 2) {
+      int i = e1 ? m1 : 1;
+      g[t1] = s1[t1] = s2[t1] = i;
+      g[t2] = j, s1[t2] = j + 2 * d2, s2[t2] = j + d2;
+      for (int x = 0; x < 3; x++) cc[x][t2] = par2(j);
+      if (e1) cc[0][t1] = h1 + 1, cc[1][t1] = h1, cc[2][t1] = h1 - 1;
+      else cc[0][t1] = l1 - 1, cc[1][t1] = l1, cc[2][t1] = l1 + 1;
+      cf3(f, c, 1, g, s1, s2, cc);
+    }
+    for (int i = a1lo; i <= a1hi; i += 2) {
+      int j = e2 ? m2 : 1;
+      g[t2] = s1[t2] = s2[t2] = j;
+      g[t1] = i, s1[t1] = i + 2 * d1, s2[t1] = i + d1;
+      for (int x = 0; x < 3; x++) cc[x][t1] = par1(i);
+      if (e2) cc[0][t2] = h2 + 1, cc[1][t2] = h2, cc[2][t2] = h2 - 1;
+      else cc[0][t2] = l2 - 1, cc[1][t2] = l2, cc[2][t2] = l2 + 1;
+      cf3(f, c, 1, g, s1, s2, cc);
+    }
+  }
+  // the four grey corner cells of a face, written on every pass
+  // (boundary.f90:1322-1333 and analogues)
+  void cf3_face_grey(int f, int c, int n, const int* fn, int t1, int t2) {
+    const HostPatch& F = H.patches[f];
+    for (int p1 = 1; p1 <= 2; p1++) {
+      int fa[5];
+      face_index(F, t1, p1, fa);
+      for (int p2 = 1; p2 <= 2; p2++) {
+        int fb[5];
+        face_index(F, t2, p2, fb);
+        int g[3], s1[3], s2[3], cc[4][3];
+        g[n] = fn[0], s1[n] = fn[1], s2[n] = fn[2];
+        g[t1] = s1[t1] = s2[t1] = fa[2];
+        g[t2] = s1[t2] = s2[t2] = fb[2];
+        for (int x = 0; x < 4; x++) cc[x][n] = fn[3];
+        cc[0][t1] = fa[4], cc[0][t2] = fb[4];
+        cc[1][t1] = fa[3], cc[1][t2] = fb[4];
+        cc[2][t1] = fa[4], cc[2][t2] = fb[3];
+        cc[3][t1] = fa[3], cc[3][t2] = fb[3];
+        cf3(f, c, 2, g, s1, s2, cc);
+      }
+    }
+  }
+
+  // Interpolate3D, boundary.f90:1048-1550: corners, the twelve edges, then
+  // the six faces.  Corners and edges skip non-interface faces on pass 1
+  // only; the face-5/6 test of edges 1-4 compares with 99 where every other
+  // test compares with 999 (boundary.f90:1104), kept as the reference has it.
+  void interpolate3d(int f, int ipass) {
+    const HostPatch& F = H.patches[f];
+    int c = F.parent;
+    const int* m = F.mthbc;
+    auto iface = [](int v) { return v == 2 || v == 999; };
+    int fa[5], fb[5], fc[5];
+    for (int p1 = 1; p1 <= 2; p1++) {
+      if (!iface(m[p1 - 1]) && ipass == 1) continue;
+      face_index(F, 0, p1, fa);
+      for (int p2 = 1; p2 <= 2; p2++) {
+        if (!iface(m[p2 + 1]) && ipass == 1) continue;
+        face_index(F, 1, p2, fb);
+        for (int p3 = 1; p3 <= 2; p3++) {
+          if (!iface(m[p3 + 3]) && ipass == 1) continue;
+          face_index(F, 2, p3, fc);
+          int g[3] = {fa[0], fb[0], fc[0]}, s1[3] = {fa[1], fb[1], fc[1]}, s2[3] = {fa[2], fb[2], fc[2]};
+          int cc[4][3] = {{fa[3], fb[3], fc[3]}};
+          cf3(f, c, 0, g, s1, s2, cc);
+        }
+      }
+    }
+    for (int p1 = 1; p1 <= 2; p1++) {  // edges 1-4
+      if (!iface(m[p1 - 1]) && ipass == 1) continue;
+      face_index(F, 0, p1, fa);
+      for (int p3 = 1; p3 <= 2; p3++) {
+        if (m[p3 + 3] != 2 && m[p3 + 3] != 99 && ipass == 1) continue;
+        face_index(F, 2, p3, fc);
+        cf3_edge(f, c, 0, fa, 2, fc, 1);
+      }
+    }
+    for (int p1 = 1; p1 <= 2; p1++) {  // edges 5-8
+      if (!iface(m[p1 - 1]) && ipass == 1) continue;
+      face_index(F, 0, p1, fa);
+      for (int p2 = 1; p2 <= 2; p2++) {
+        if (!iface(m[p2 + 1]) && ipass == 1) continue;
+        face_index(F, 1, p2, fb);
+        cf3_edge(f, c, 0, fa, 1, fb, 2);
+      }
+    }
+    for (int p2 = 1; p2 <= 2; p2++) {  // edges 9-12
+      if (!iface(m[p2 + 1]) && ipass == 1) continue;
+      face_index(F, 1, p2, fb);
+      for (int p3 = 1; p3 <= 2; p3++) {
+        if (!iface(m[p3 + 3]) && ipass == 1) continue;
+        face_index(F, 2, p3, fc);
+        cf3_edge(f, c, 1, fb, 2, fc, 0);
+      }
+    }
+    static const int T[3][2] = {{1, 2}, {0, 2}, {0, 1}};
+    for (int n = 0; n < 3; n++)
+      for (int par = 1; par <= 2; par++) {
+        if (!iface(m[2 * n + par - 1])) continue;
+        int fn[5];
+        face_index(F, n, par, fn);
+        if (ipass == 0 || (par + ipass) % 2 == 0) {
+          cf3_face_class(f, c, n, fn, T[n][0], T[n][1], 0);
+          cf3_face_class(f, c, n, fn, T[n][0], T[n][1], 1);
+        }
+        if (ipass == 0 || (par + ipass) % 2 == 1) {
+          cf3_face_class(f, c, n, fn, T[n][0], T[n][1], 2);
+          cf3_face_class(f, c, n, fn, T[n][0], T[n][1], 3);
+        }
+        cf3_face_grey(f, c, n, fn, T[n][0], T[n][1]);
+      }
+  }
+
   // GhostOverlap, boundary.f90:359-431 (the landscape part is mesh-build
   // only).  Ghost cells of g1 that lie in the interior of g2 (shifted by
   // off) take g2's values, then the converse.
@@ -320,8 +502,10 @@ std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std:
   const std::vector<int>& ps = L.patches;
   int n = (int)ps.size();
   if (level > 0) {
-    if (H.ndims == 2)
-      for (int a = 0; a < n; a++) E.interpolate2d(ps[a], ipass);
+    for (int a = 0; a < n; a++) {
+      if (H.ndims == 2) E.interpolate2d(ps[a], ipass);
+      else E.interpolate3d(ps[a], ipass);
+    }
     for (int a = 0; a < n; a++)
       for (int b = a + 1; b < n; b++) E.ghost_overlap(ps[a], ps[b], nullptr);
   }

@@ -480,10 +480,9 @@ int commit(Hier& H) {
           return BSAMG_ERR_ARG;
       }
     }
-    if (H.ndims == 2 && P.level > 0 && P.parent >= 0 && (P.mx[0] < 4 || P.mx[1] < 4))
-      return BSAMG_ERR_UNSUPPORTED;  // Interpolate2D reads cells 1..2 from each side
-    if (H.ndims == 3 && P.level > 0)
-      return BSAMG_ERR_UNSUPPORTED;  // 3D coarse-fine interpolation (Interpolate3D) is not built yet
+    if (P.level > 0 && P.parent >= 0)
+      for (int d = 0; d < H.ndims; d++)
+        if (P.mx[d] < 4) return BSAMG_ERR_UNSUPPORTED;  // Interpolate2D/3D read cells 1..2 from each side
   }
   // level lists in insertion (visiting) order
   for (size_t n = 0; n < H.patches.size(); n++) H.L(H.patches[n].level).patches.push_back((int)n);

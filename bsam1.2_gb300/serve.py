@@ -1,7 +1,7 @@
 """Continuous-batching request loop over independent CH time-step requests.
 
 A request asks for `steps` CH time steps on its own mesh (2D or 3D root,
-optionally with nested refinement levels in 2D) from its own seeded start.
+optionally with nested refinement levels) from its own seeded start.
 Requests are admitted as worker slots and device memory free up: a slot
 builds the request's hierarchy, and if the context's HBM budget is exhausted
 (`bsamg_commit` returns BSAMG_ERR_BUDGET) it waits until another request
@@ -172,9 +172,8 @@ class Server:
 
 def poisson_stream(rate, duration, seed, mode="mixed", max_requests=None):
     """Requests of the serving configuration: Poisson arrivals at `rate`/s;
-    2D root from {32,64,128,256}^2 with 0-3 nested levels, or 3D root from
-    {32,64}^3 (no refinement: 3D coarse-fine interpolation is not built);
-    1-20 steps; eps ~ U(0.01, 0.03); own seed."""
+    2D root from {32,64,128,256}^2 or 3D root from {32,64}^3, each with 0-3
+    nested levels; 1-20 steps; eps ~ U(0.01, 0.03); own seed."""
     rng = np.random.default_rng(seed)
     t, out = 0.0, []
     while True:
@@ -185,7 +184,8 @@ def poisson_stream(rate, duration, seed, mode="mixed", max_requests=None):
             nd, n = 2, int(rng.choice([32, 64, 128, 256]))
             levels = int(rng.integers(0, 4))
         else:
-            nd, n, levels = 3, int(rng.choice([32, 64])), 0
+            nd, n = 3, int(rng.choice([32, 64]))
+            levels = int(rng.integers(0, 4))
         steps = int(rng.integers(1, 21))
         eps = float(rng.uniform(0.01, 0.03))
         # the time steps of the 2D and 3D benchmark configurations

@@ -686,6 +686,211 @@ static void interpolate2d(const bsamo_hier* h, OPatch* f, const OPatch* c,
 #undef QCC
 }
 
+/* ---- Interpolate3D, boundary.f90:1048-1550 ---------------------------- */
+
+/* GetFaceIndex, boundary.f90:1018-1045: for dimension d and parity 1 (low) or
+ * 2 (high): [0] ghost index, [1] second fine cell, [2] first fine cell,
+ * [3] coarse cell beyond the patch, [4] coarse cell at the patch edge. */
+static void face_index(const OPatch* f, int d, int parity, int fi[5]) {
+  if (parity == 1) {
+    fi[0] = 0; fi[1] = 2; fi[2] = 1;
+    fi[3] = f->mbounds[d][0] - 1; fi[4] = f->mbounds[d][0];
+  } else {
+    fi[0] = f->mx[d] + 1; fi[1] = f->mx[d] - 1; fi[2] = f->mx[d];
+    fi[3] = f->mbounds[d][1] + 1; fi[4] = f->mbounds[d][1];
+  }
+}
+
+/* one interpolated ghost value, all variables:
+ * q(g) = a1*q(s1) + a2*q(s2) + a3*coarse, coarse one of
+ *   kind 0: qc(c[0]);  kind 1: b1*qc(c[0]) + b2*qc(c[1]) + b3*qc(c[2]);
+ *   kind 2: c1*qc(c[0]) + c2*qc(c[1]) + c3*qc(c[2]) + c4*qc(c[3]) */
+static void cf3_put(const bsamo_hier* h, OPatch* f, const OPatch* pc, const int g[3], const int s1[3],
+                    const int s2[3], int kind, int c[4][3]) {
+  for (int v = 0; v < h->nrvars; v++) {
+    double co;
+    if (kind == 0) co = Q(pc, c[0][0], c[0][1], c[0][2], v);
+    else if (kind == 1)
+      co = B1 * Q(pc, c[0][0], c[0][1], c[0][2], v) + B2 * Q(pc, c[1][0], c[1][1], c[1][2], v) +
+           B3 * Q(pc, c[2][0], c[2][1], c[2][2], v);
+    else
+      co = C1 * Q(pc, c[0][0], c[0][1], c[0][2], v) + C2 * Q(pc, c[1][0], c[1][1], c[1][2], v) +
+           C3 * Q(pc, c[2][0], c[2][1], c[2][2], v) + C4 * Q(pc, c[3][0], c[3][1], c[3][2], v);
+    Q(f, g[0], g[1], g[2], v) = A1 * Q(f, s1[0], s1[1], s1[2], v) + A2 * Q(f, s2[0], s2[1], s2[2], v) + A3 * co;
+  }
+}
+
+static int cf_face(int m) { return m == 2 || m == INTERNALBC; }
+
+/* An edge with dimensions d1, d2 fixed at the faces given by fa, fb (face
+ * index arrays) and dimension t running; the four statements of each edge
+ * block (boundary.f90:1096-1126 and the two groups after it). */
+static void cf3_edge(const bsamo_hier* h, OPatch* f, const OPatch* pc, int d1, const int* fa, int d2,
+                     const int* fb, int t) {
+  int mx = f->mx[t], lo = f->mbounds[t][0], hi = f->mbounds[t][1];
+  int g[3], s1[3], s2[3], c[4][3];
+  g[d1] = fa[0]; s1[d1] = fa[1]; s2[d1] = fa[2];
+  g[d2] = fb[0]; s1[d2] = fb[1]; s2[d2] = fb[2];
+  for (int x = 0; x < 4; x++) { c[x][d1] = fa[3]; c[x][d2] = fb[3]; }
+  for (int i = 3, n = 0; i <= mx - 1; i += 2, n++) { /* 3:mx-1:2 */
+    g[t] = i; s1[t] = i - 2; s2[t] = i - 1; c[0][t] = lo + 1 + n;
+    cf3_put(h, f, pc, g, s1, s2, 0, c);
+  }
+  g[t] = 1; s1[t] = 1; s2[t] = 1;
+  c[0][t] = lo - 1; c[1][t] = lo; c[2][t] = lo + 1;
+  cf3_put(h, f, pc, g, s1, s2, 1, c);
+  for (int i = 2, n = 0; i <= mx - 2; i += 2, n++) { /* 2:mx-2:2 */
+    g[t] = i; s1[t] = i + 2; s2[t] = i + 1; c[0][t] = lo + n;
+    cf3_put(h, f, pc, g, s1, s2, 0, c);
+  }
+  g[t] = mx; s1[t] = mx; s2[t] = mx;
+  c[0][t] = hi + 1; c[1][t] = hi; c[2][t] = hi - 1;
+  cf3_put(h, f, pc, g, s1, s2, 1, c);
+}
+
+/* The tangential classes of one face (normal n fixed by fn, tangential
+ * dimensions t1 < t2), boundary.f90:1209-1335 and its two analogues.
+ * cls 0: yellow (t1, t2 even) with its edge rows; 1: blue (odd, odd);
+ * 2: green (t1 odd, t2 even); 3: red (t1 even, t2 odd). */
+static void cf3_face_class(const bsamo_hier* h, OPatch* f, const OPatch* pc, int n, const int* fn, int t1, int t2,
+                           int cls) {
+  int m1 = f->mx[t1], m2 = f->mx[t2];
+  int l1 = f->mbounds[t1][0], h1 = f->mbounds[t1][1], l2 = f->mbounds[t2][0], h2 = f->mbounds[t2][1];
+  int g[3], s1[3], s2[3], c[4][3];
+  g[n] = fn[0]; s1[n] = fn[1]; s2[n] = fn[2];
+  for (int x = 0; x < 4; x++) c[x][n] = fn[3];
+  /* direction of the diagonal in t1 and t2: +1 for even classes, -1 for odd */
+  int e1 = (cls == 0 || cls == 3), e2 = (cls == 0 || cls == 2);
+  int a1lo = e1 ? 2 : 3, a1hi = e1 ? m1 - 2 : m1 - 1, a2lo = e2 ? 2 : 3, a2hi = e2 ? m2 - 2 : m2 - 1;
+  int d1 = e1 ? 1 : -1, d2 = e2 ? 1 : -1;
+  /* bulk: both coordinates in the strided ranges */
+  for (int j = a2lo; j <= a2hi; j += 2)
+    for (int i = a1lo; i <= a1hi; i += 2) {
+      g[t1] = i; g[t2] = j;
+      s1[t1] = i + 2 * d1; s1[t2] = j + 2 * d2;
+      s2[t1] = i + d1; s2[t2] = j + d2;
+      c[0][t1] = e1 ? l1 + i / 2 - 1 : l1 + (i - 1) / 2;
+      c[0][t2] = e2 ? l2 + j / 2 - 1 : l2 + (j - 1) / 2;
+      cf3_put(h, f, pc, g, s1, s2, 0, c);
+    }
+  /* edge row with t1 at its end (even class: t1 = m1, odd class: t1 = 1),
+   * t2 in its strided range; coarse b-combination along t1 */
+  for (int j = a2lo; j <= a2hi; j += 2) {
+    int i = e1 ? m1 : 1;
+    g[t1] = i; g[t2] = j;
+    s1[t1] = i; s1[t2] = j + 2 * d2;
+    s2[t1] = i; s2[t2] = j + d2;
+    int ct2 = e2 ? l2 + j / 2 - 1 : l2 + (j - 1) / 2;
+    for (int x = 0; x < 3; x++) c[x][t2] = ct2;
+    if (e1) { c[0][t1] = h1 + 1; c[1][t1] = h1; c[2][t1] = h1 - 1; }
+    else { c[0][t1] = l1 - 1; c[1][t1] = l1; c[2][t1] = l1 + 1; }
+    cf3_put(h, f, pc, g, s1, s2, 1, c);
+  }
+  /* edge row with t2 at its end, t1 in its strided range; b along t2 */
+  for (int i = a1lo; i <= a1hi; i += 2) {
+    int j = e2 ? m2 : 1;
+    g[t1] = i; g[t2] = j;
+    s1[t1] = i + 2 * d1; s1[t2] = j;
+    s2[t1] = i + d1; s2[t2] = j;
+    int ct1 = e1 ? l1 + i / 2 - 1 : l1 + (i - 1) / 2;
+    for (int x = 0; x < 3; x++) c[x][t1] = ct1;
+    if (e2) { c[0][t2] = h2 + 1; c[1][t2] = h2; c[2][t2] = h2 - 1; }
+    else { c[0][t2] = l2 - 1; c[1][t2] = l2; c[2][t2] = l2 + 1; }
+    cf3_put(h, f, pc, g, s1, s2, 1, c);
+  }
+}
+
+/* grey corner cells of a face, boundary.f90:1322-1333 and analogues */
+static void cf3_face_grey(const bsamo_hier* h, OPatch* f, const OPatch* pc, int n, const int* fn, int t1, int t2) {
+  for (int p1 = 1; p1 <= 2; p1++) {
+    int fa[5];
+    face_index(f, t1, p1, fa);
+    for (int p2 = 1; p2 <= 2; p2++) {
+      int fb[5];
+      face_index(f, t2, p2, fb);
+      int g[3], s1[3], s2[3], c[4][3];
+      g[n] = fn[0]; s1[n] = fn[1]; s2[n] = fn[2];
+      g[t1] = s1[t1] = s2[t1] = fa[2];
+      g[t2] = s1[t2] = s2[t2] = fb[2];
+      for (int x = 0; x < 4; x++) c[x][n] = fn[3];
+      c[0][t1] = fa[4]; c[0][t2] = fb[4];
+      c[1][t1] = fa[3]; c[1][t2] = fb[4];
+      c[2][t1] = fa[4]; c[2][t2] = fb[3];
+      c[3][t1] = fa[3]; c[3][t2] = fb[3];
+      cf3_put(h, f, pc, g, s1, s2, 2, c);
+    }
+  }
+}
+
+static void interpolate3d(const bsamo_hier* h, OPatch* f, const OPatch* pc, int ipass) {
+  const int* m = f->mthbc;
+  int fa[5], fb[5], fcc[5];
+  /* (1) corners */
+  for (int p1 = 1; p1 <= 2; p1++) {
+    if (!cf_face(m[p1 - 1]) && ipass == 1) continue;
+    face_index(f, 0, p1, fa);
+    for (int p2 = 1; p2 <= 2; p2++) {
+      if (!cf_face(m[p2 + 1]) && ipass == 1) continue;
+      face_index(f, 1, p2, fb);
+      for (int p3 = 1; p3 <= 2; p3++) {
+        if (!cf_face(m[p3 + 3]) && ipass == 1) continue;
+        face_index(f, 2, p3, fcc);
+        int g[3] = {fa[0], fb[0], fcc[0]}, s1[3] = {fa[1], fb[1], fcc[1]}, s2[3] = {fa[2], fb[2], fcc[2]};
+        int c[4][3] = {{fa[3], fb[3], fcc[3]}};
+        cf3_put(h, f, pc, g, s1, s2, 0, c);
+      }
+    }
+  }
+  /* (2) edges 1-4: dimensions 1 and 3 fixed; the face-5/6 test of the
+   * reference compares with 99, not 999 (boundary.f90:1104) */
+  for (int p1 = 1; p1 <= 2; p1++) {
+    if (!cf_face(m[p1 - 1]) && ipass == 1) continue;
+    face_index(f, 0, p1, fa);
+    for (int p3 = 1; p3 <= 2; p3++) {
+      if (m[p3 + 3] != 2 && m[p3 + 3] != 99 && ipass == 1) continue;
+      face_index(f, 2, p3, fcc);
+      cf3_edge(h, f, pc, 0, fa, 2, fcc, 1);
+    }
+  }
+  /* edges 5-8: dimensions 1 and 2 fixed */
+  for (int p1 = 1; p1 <= 2; p1++) {
+    if (!cf_face(m[p1 - 1]) && ipass == 1) continue;
+    face_index(f, 0, p1, fa);
+    for (int p2 = 1; p2 <= 2; p2++) {
+      if (!cf_face(m[p2 + 1]) && ipass == 1) continue;
+      face_index(f, 1, p2, fb);
+      cf3_edge(h, f, pc, 0, fa, 1, fb, 2);
+    }
+  }
+  /* edges 9-12: dimensions 2 and 3 fixed */
+  for (int p2 = 1; p2 <= 2; p2++) {
+    if (!cf_face(m[p2 + 1]) && ipass == 1) continue;
+    face_index(f, 1, p2, fb);
+    for (int p3 = 1; p3 <= 2; p3++) {
+      if (!cf_face(m[p3 + 3]) && ipass == 1) continue;
+      face_index(f, 2, p3, fcc);
+      cf3_edge(h, f, pc, 1, fb, 2, fcc, 0);
+    }
+  }
+  /* (3) faces, normal dimension n with tangential dimensions (t1, t2) */
+  static const int T[3][2] = {{1, 2}, {0, 2}, {0, 1}};
+  for (int n = 0; n < 3; n++)
+    for (int par = 1; par <= 2; par++) {
+      if (!cf_face(m[2 * n + par - 1])) continue;
+      int fn[5];
+      face_index(f, n, par, fn);
+      if (ipass == 0 || (par + ipass) % 2 == 0) {
+        cf3_face_class(h, f, pc, n, fn, T[n][0], T[n][1], 0);
+        cf3_face_class(h, f, pc, n, fn, T[n][0], T[n][1], 1);
+      }
+      if (ipass == 0 || (par + ipass) % 2 == 1) {
+        cf3_face_class(h, f, pc, n, fn, T[n][0], T[n][1], 2);
+        cf3_face_class(h, f, pc, n, fn, T[n][0], T[n][1], 3);
+      }
+      cf3_face_grey(h, f, pc, n, fn, T[n][0], T[n][1]);
+    }
+}
+
 /* GhostOverlap, boundary.f90:359-431 (the level-landscape part, :434-475, is
  * only used while the mesh is being built and is not restated). */
 static void ghost_overlap(const bsamo_hier* h, OPatch* g1, OPatch* g2,
@@ -825,7 +1030,7 @@ static void set_ghost(bsamo_hier* h, int level, int ipass) {
       OPatch* p = lev_patch(h, level, a);
       OPatch* c = parent_of(h, p);
       if (h->ndims == 2) interpolate2d(h, p, c, ipass);
-      /* Interpolate3D (boundary.f90:1048-1550) is not restated */
+      else interpolate3d(h, p, c, ipass);
     }
     for (int a = 0; a < n; a++) /* ApplyOnLevelPairs(TransferBC) */
       for (int b = a + 1; b < n; b++)

@@ -92,3 +92,19 @@ def amr2d(periodic=True, n=32):
     s.child(101, 201, [3, 3], [10, 8])     # level 2 inside 101
     s.child(101, 202, [11, 3], [14, 10])   # sibling of 201
     return s
+
+
+def amr3d(periodic=True, n=16):
+    """root n^3 + below-root levels + two refined levels in 3D: siblings that
+    touch each other, the boundary, each other's periodic images, and a
+    level-2 pair inside one level-1 patch."""
+    s = Spec(3)
+    mthbc = [2] * 6 if periodic else [10] * 6
+    s.root_and_below(n, -int(math.log2(n)) + 1, mthbc)
+    s.child(0, 101, [3, 3, 3], [8, 6, 7])        # 12 x 8 x 10
+    s.child(0, 102, [9, 3, 3], [12, 6, 6])       # 8 x 8 x 8, touches 101 at x
+    s.child(0, 103, [1, 10, 4], [4, 13, 7])      # touches the low-x boundary
+    s.child(0, 104, [13, 10, 4], [16, 13, 7])    # touches the high-x boundary (image of 103)
+    s.child(101, 201, [3, 3, 3], [6, 6, 6])      # level 2 inside 101
+    s.child(101, 202, [7, 3, 2], [10, 6, 8])     # sibling of 201, 8 x 8 x 14
+    return s

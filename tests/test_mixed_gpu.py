@@ -24,6 +24,7 @@ MIXED_CASES = {
     "ch3d-periodic-64": (CH3, lambda: uniform_spec(3, 64, PERIODIC3), 1e-8, 1e-5, 1e-11, 1e-8),
     "ch3d-dirichlet-16": (CH3, lambda: uniform_spec(3, 16, DIRICHLET3), 1e-8, 1e-5, 1e-11, 1e-8),
     "ch2d-amr-periodic": (CH2, lambda: H.amr2d(periodic=True), 1e-9, 2e-6, 1e-12, 1e-9),
+    "ch3d-amr-periodic": (CH3, lambda: H.amr3d(periodic=True), 1e-8, 1e-5, 1e-11, 1e-8),
 }
 
 

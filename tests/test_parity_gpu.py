@@ -77,6 +77,8 @@ CASES = {
     "ch2d-amr-periodic": (CH2, lambda: H.amr2d(periodic=True)),
     "ch2d-amr-neumann": (CH2, lambda: H.amr2d(periodic=False)),
     "bio2d-amr": (BIO2, lambda: H.amr2d(periodic=False)),
+    "ch3d-amr-periodic": (CH3, lambda: H.amr3d(periodic=True)),
+    "ch3d-amr-dirichlet": (CH3, lambda: H.amr3d(periodic=False)),
 }
 
 

@@ -14,7 +14,8 @@ def _requests(serve, mode):
             R(2, 3, 32, 0, 2, 0.025, 5e-4 * 64, seed=13, mode=mode),
             R(3, 2, 128, 1, 2, 0.015, 1e-3, seed=14, mode=mode),
             R(4, 2, 64, 3, 2, 0.03, 2.5e-4 * 4, seed=15, mode=mode),
-            R(5, 3, 64, 0, 2, 0.01, 5e-4 * 16, seed=16, mode=mode)]
+            R(5, 3, 64, 0, 2, 0.01, 5e-4 * 16, seed=16, mode=mode),
+            R(6, 3, 32, 2, 2, 0.02, 5e-4, seed=17, mode=mode)]
 
 
 @pytest.mark.parametrize("mode", ["fp64", "mixed"])
@@ -28,7 +29,7 @@ def test_same_result_alone_and_in_the_mix(pkg, mode):
         assert r.error is None and r.result is not None
     srv.close()
     ctx.close()
-    # the mix: six requests, three slots, all submitted at once, and a budget
+    # the mix: seven requests, three slots, all submitted at once, and a budget
     # below their sum (the 64^3 request alone takes about 31 MB) so that
     # admission has to wait for memory
     mixed = _requests(serve, mode)
