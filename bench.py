@@ -319,7 +319,7 @@ def serve_arm(args, dist):
         "data": "synthetic (seeded Poisson arrivals and spinodal starts)",
         "config": {"workload": "serve", "arrival_rate_per_s": 200.0, "arrival_window_s": duration,
                    "slots": args.serve_slots, "hbm_budget_gb": args.serve_budget_gb,
-                   "mix": "2D roots {32,64,128,256}^2 with 0-3 nested levels, 3D roots {32,64}^3, 1-20 steps"},
+                   "mix": "2D roots {32,64,128,256}^2 or 3D roots {32,64}^3, each with 0-3 nested levels, 1-20 steps"},
         "p50_ms": m["p50_ms"], "p99_ms": m["p99_ms"], "serving_mixed": m, "serving_fp64": f,
         "speedup_mixed_vs_fp64": m["steps_per_s"] / f["steps_per_s"] if f["steps_per_s"] else None,
     }

@@ -20,6 +20,7 @@ UNITS = {
     "fp64.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
     "mixed.cu": [],
+    "box.cu": [],
     "hier.cu": [],
     "ghostc.cpp": [],
 }

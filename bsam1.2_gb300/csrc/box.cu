@@ -1,0 +1,797 @@
+// Mixed-precision MultigridIterations on periodic boxes.
+//
+// Applies when every level of the hierarchy is one fully periodic patch with
+// even extents that covers its parent (a uniform periodic grid and its
+// below-root levels, RootInit/InitSeed, bsamroutines.f90:226-510).  The
+// algorithm is the one of mixed.cu -- an FP32 FAS V-cycle on the correction
+// equation M(e) = N(qbar + e) - N(qbar) = g inside an outer loop that updates
+// qbar and confirms convergence on the true residual f - N(qbar) -- with a
+// data layout and precision split chosen for GB300:
+//
+//  * No ghost cells and no work lists.  Neighbours wrap around the box, and
+//    every kernel derives its cell from a 3D grid, so a thread's first loads
+//    are its data (no dependent table lookups).
+//  * Colour-split FP32 arrays (BoxLev).  A red half-sweep reads whole
+//    sectors of black values and writes whole sectors of red ones, instead
+//    of touching every sector of an interleaved array for half its bytes.
+//  * The FP64 iterate is held for the whole solve as a pair of floats
+//    (hi + lo, about 48 significant bits).  qbar += e is a TwoSum, and the
+//    residual f - N(qbar) is evaluated in double-float arithmetic, all on the
+//    FP32 pipe; GB300's FP64 rate is 1/64 of its FP32 rate.  The rounding
+//    error of the double-float residual is about 2^-47 times the largest
+//    term (|c0 ulap(mu)|, |phi^3| ~ 1-100 here), i.e. ~1e-12, four orders
+//    below the 1e-8..1e-9 tolerances the residual is tested against.  FP64 is
+//    used only to split q at the start (integer bit operations, exact) and
+//    to write it back at the end (one FP64 add per value).
+//  * The tracked residual update g <- g - M(e) and qbar += e are one pass,
+//    and e is never cleared: the first two half-sweeps of a cycle on the
+//    finest level treat the previous cycle's e as zero.
+//
+// Plugin: CH (CH/problem.f90), whose source is f = (phi_old, -phi_old)
+// (Source2D/3D, :425-450, :672-695) and whose operator is
+// N(q) = (phi - dt/h^2 ULap(mu), mu - phi^3 + eps^2/h^2 ULap(phi))
+// (Operator2D/3D, :393-422, :638-669).
+#include <algorithm>
+
+#include "box.h"
+#include "launch.h"
+
+namespace bsamg {
+
+namespace {
+
+// colour of 0-based cell (x, y, z): parity of the 1-based i + j (+ k)
+template <int DIM>
+__device__ __forceinline__ int colour(int x, int y, int z) {
+  return DIM == 3 ? (x + y + z + 1) & 1 : (x + y) & 1;
+}
+
+// Index of a cell and its six neighbours within the colour arrays.  own is
+// in the cell's colour array, the neighbours in the other colour's array.
+template <int DIM>
+struct Loc {
+  int c;
+  int own, xm, xp, ym, yp, zm, zp;
+  __device__ __forceinline__ Loc(const BoxLev& L, int x, int y, int z) {
+    c = colour<DIM>(x, y, z);
+    int h = x >> 1, b = x & 1, hh = L.hh, n1 = L.n[1];
+    int r = z * n1 + y;
+    own = r * hh + h;
+    int hxm = b ? h : (h ? h - 1 : hh - 1);
+    int hxp = b ? (h + 1 < hh ? h + 1 : 0) : h;
+    xm = r * hh + hxm;
+    xp = r * hh + hxp;
+    ym = (r - y + (y ? y - 1 : n1 - 1)) * hh + h;
+    yp = (r - y + (y + 1 < n1 ? y + 1 : 0)) * hh + h;
+    if (DIM == 3) {
+      int n2 = L.n[2];
+      zm = ((z ? z - 1 : n2 - 1) * n1 + y) * hh + h;
+      zp = ((z + 1 < n2 ? z + 1 : 0) * n1 + y) * hh + h;
+    } else {
+      zm = zp = 0;
+    }
+  }
+};
+
+template <int DIM>
+__device__ __forceinline__ float nsum(const float* a, const Loc<DIM>& l) {
+  float s = a[l.xm] + a[l.xp] + a[l.ym] + a[l.yp];
+  if (DIM == 3) s += a[l.zm] + a[l.zp];
+  return s;
+}
+
+// variable v, colour c of a two-variable colour-split array
+__device__ __forceinline__ float* arr(float* fp, long long off, long long half, int v, int c) {
+  return fp + off + (long long)(v * 2 + c) * half;
+}
+
+// correction operator M(e) at a cell (see mixed.cu, mopn)
+template <int DIM>
+__device__ __forceinline__ void mop(float* fp, const BoxLev& L, const Loc<DIM>& l, float pb, float& m0, float& m1) {
+  const float* e0 = arr(fp, L.oe, L.half, 0, l.c);
+  const float* e1 = arr(fp, L.oe, L.half, 1, l.c);
+  const float* o0 = arr(fp, L.oe, L.half, 0, 1 - l.c);
+  const float* o1 = arr(fp, L.oe, L.half, 1, 1 - l.c);
+  float x = e0[l.own], y = e1[l.own];
+  float k = DIM == 2 ? 4.0f : 6.0f;
+  m0 = x - L.c0 * (nsum<DIM>(o1, l) - k * y);
+  m1 = y - x * (3.0f * pb * (pb + x) + x * x) + L.c1 * (nsum<DIM>(o0, l) - k * x);
+}
+
+// ---------------------------------------------------------------------------
+// double-float arithmetic (value = h + l, |l| <= ulp(h)/2 after
+// normalisation): Dekker/Knuth error-free transformations
+
+struct DF {
+  float h, l;
+};
+__device__ __forceinline__ DF two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DF fast_two_sum(float a, float b) {
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+  DF s = two_sum(x.h, y.h);
+  return fast_two_sum(s.h, s.l + (x.l + y.l));
+}
+__device__ __forceinline__ DF df_neg(DF x) { return {-x.h, -x.l}; }
+__device__ __forceinline__ DF df_mul(DF x, DF y) {
+  float p = x.h * y.h;
+  float e = fmaf(x.h, y.h, -p);
+  e = fmaf(x.h, y.l, e);
+  e = fmaf(x.l, y.h, e);
+  return fast_two_sum(p, e);
+}
+// undivided Laplacian sum(neighbours) - k*centre of double-float values
+template <int DIM>
+__device__ __forceinline__ DF df_lap(const DF* nb, DF c) {
+  float sh = nb[0].h, el = nb[0].l;
+  for (int m = 1; m < 2 * DIM; m++) {
+    DF t = two_sum(sh, nb[m].h);
+    sh = t.h;
+    el += t.l + nb[m].l;
+  }
+  const float k = DIM == 2 ? 4.0f : 6.0f;
+  float p = k * c.h;
+  float pe = fmaf(k, c.h, -p);  // k*c.h = p + pe exactly
+  DF t = two_sum(sh, -p);
+  el += t.l - pe - k * c.l;
+  return fast_two_sum(t.h, el);
+}
+
+// Split a double into hi + lo floats with integer operations only (no FP64
+// instructions).  hi keeps the leading 24 significant bits (truncated), lo
+// the next 29 rounded to 24, so hi + lo carries 48 of the 53 bits.  Values
+// whose magnitude is outside [2^-70, 2^120] (zero, denormals, infinities,
+// NaN, extremes) take the conversion instructions instead.
+__device__ __forceinline__ DF split64(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  unsigned int top = (unsigned int)(b >> 32);
+  int e = (int)((top >> 20) & 0x7FFu) - 1023;
+  if (e >= -70 && e <= 120) {
+    unsigned int s = top & 0x80000000u;
+    float hi = __uint_as_float(s | ((unsigned int)(e + 127) << 23) | ((unsigned int)(b >> 29) & 0x7FFFFFu));
+    float rf = __uint2float_rn((unsigned int)b & 0x1FFFFFFFu);
+    float lo = rf * __uint_as_float((unsigned int)(e - 52 + 127) << 23);
+    return {hi, s ? -lo : lo};
+  }
+  if ((b << 1) == 0) return {__uint_as_float(top & 0x80000000u), 0.0f};
+  float hi = (float)x;
+  return {hi, (float)(x - (double)hi)};
+}
+// float -> double by bit operations for normal floats and zeros
+__device__ __forceinline__ double f2d(float f) {
+  unsigned int u = __float_as_uint(f);
+  unsigned int ex = (u >> 23) & 0xFFu;
+  if (ex != 0 && ex != 0xFFu)
+    return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                            ((unsigned long long)(ex + 896u) << 52) |
+                                            ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+  if ((u << 1) == 0) return __longlong_as_double((long long)((unsigned long long)u << 32));
+  return (double)f;
+}
+
+// deterministic per-CTA sums of two values -> partial[2*cta], [2*cta+1]
+// (shared-memory tree: block sizes need not be a multiple of the warp size)
+__device__ __forceinline__ void cta_sum2(float s0, float s1, double* partial) {
+  __shared__ float red[2][256];
+  int t = threadIdx.y * blockDim.x + threadIdx.x;
+  int nt = blockDim.x * blockDim.y;
+  red[0][t] = s0;
+  red[1][t] = s1;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (t < w && t + w < nt) {
+      red[0][t] += red[0][t + w];
+      red[1][t] += red[1][t + w];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    long long cta = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    partial[2 * cta] = (double)red[0][0];
+    partial[2 * cta + 1] = (double)red[1][0];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// kernels.  Grid (x, y, z) = (position in a colour row or coarse x,
+// y, z); blockDim.z = 1.
+
+// Colour half-sweep of the correction smoother (RelaxGrid2D/3D in
+// correction form, see mixed.cu k_mx_relax).  first = 1: e of both colours
+// counts as zero (first half-sweep of a cycle); first = 2: the own colour's
+// e counts as zero (second half-sweep).
+template <int DIM>
+__device__ __forceinline__ void relax_at(float* __restrict__ fp, const BoxLev& L, int c, int first, int h, int y,
+                                         int z) {
+  int x = 2 * h + ((c + y + z + (DIM == 3 ? 1 : 0)) & 1);
+  Loc<DIM> l(L, x, y, z);
+  float* e0 = arr(fp, L.oe, L.half, 0, c);
+  float* e1 = arr(fp, L.oe, L.half, 1, c);
+  const float* g0 = arr(fp, L.og, L.half, 0, c);
+  const float* g1 = arr(fp, L.og, L.half, 1, c);
+  float pb = fp[L.opb + (long long)c * L.half + l.own];
+  float s0 = 0.f, s1 = 0.f, xv = 0.f;
+  if (first != 1) {
+    s0 = nsum<DIM>(arr(fp, L.oe, L.half, 0, 1 - c), l);
+    s1 = nsum<DIM>(arr(fp, L.oe, L.half, 1, 1 - c), l);
+    if (first == 0) xv = e0[l.own];
+  }
+  float w = pb + xv;
+  float a21 = -3.0f * w * w - L.tmp3;
+  float b1 = g0[l.own] + L.c0 * s1;
+  float b2 = g1[l.own] - L.c1 * s0 - xv * xv * (3.0f * pb + 2.0f * xv);
+  float rdet = 1.0f / (1.0f - L.a12 * a21);
+  e0[l.own] = (b1 - L.a12 * b2) * rdet;
+  e1[l.own] = (b2 - a21 * b1) * rdet;
+}
+// Full-grid sweep: each thread takes position h of rows 2yp and 2yp+1 (n1
+// is even), loading both cells' data before either is stored so that twice
+// the loads are in flight per thread.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_relax(float* __restrict__ fp, BoxLev L, int c, int first) {
+  int h = blockIdx.x * blockDim.x + threadIdx.x;
+  int yp = blockIdx.y * blockDim.y + threadIdx.y;
+  int z = blockIdx.z;
+  if (h >= L.hh || 2 * yp >= L.n[1]) return;
+  float* e0 = arr(fp, L.oe, L.half, 0, c);
+  float* e1 = arr(fp, L.oe, L.half, 1, c);
+  const float* g0 = arr(fp, L.og, L.half, 0, c);
+  const float* g1 = arr(fp, L.og, L.half, 1, c);
+  const float* o0 = arr(fp, L.oe, L.half, 0, 1 - c);
+  const float* o1 = arr(fp, L.oe, L.half, 1, 1 - c);
+  const float* pbc = fp + L.opb + (long long)c * L.half;
+  int own[2];
+  float pb[2], xv[2], s0[2], s1[2], b1[2], gg1[2];
+  for (int k = 0; k < 2; k++) {
+    int y = 2 * yp + k;
+    int x = 2 * h + ((c + y + z + (DIM == 3 ? 1 : 0)) & 1);
+    Loc<DIM> l(L, x, y, z);
+    own[k] = l.own;
+    pb[k] = pbc[l.own];
+    s0[k] = s1[k] = xv[k] = 0.f;
+    if (first != 1) {
+      s0[k] = nsum<DIM>(o0, l);
+      s1[k] = nsum<DIM>(o1, l);
+      if (first == 0) xv[k] = e0[l.own];
+    }
+    b1[k] = g0[l.own];
+    gg1[k] = g1[l.own];
+  }
+  for (int k = 0; k < 2; k++) {
+    float w = pb[k] + xv[k];
+    float a21 = -3.0f * w * w - L.tmp3;
+    float bb1 = b1[k] + L.c0 * s1[k];
+    float bb2 = gg1[k] - L.c1 * s0[k] - xv[k] * xv[k] * (3.0f * pb[k] + 2.0f * xv[k]);
+    float rdet = 1.0f / (1.0f - L.a12 * a21);
+    e0[own[k]] = (bb1 - L.a12 * bb2) * rdet;
+    e1[own[k]] = (bb2 - a21 * bb1) * rdet;
+  }
+}
+
+// RestrictSolution on e and on the base field: coarse e = ec = R(e_fine),
+// coarse pb = R(pb_fine); one thread per coarse cell
+template <int DIM>
+__device__ __forceinline__ void restrict_at(float* __restrict__ fp, const BoxLev& F, const BoxLev& C, int X, int Y,
+                                            int Z) {
+  Loc<DIM> lc(C, X, Y, Z);
+  float s[3] = {0.f, 0.f, 0.f};
+  const int nz = DIM == 3 ? 2 : 1;
+  for (int dz = 0; dz < nz; dz++)
+    for (int dy = 0; dy < 2; dy++) {
+      int y = 2 * Y + dy, z = DIM == 3 ? 2 * Z + dz : 0;
+      int r = (z * F.n[1] + y) * F.hh + X;  // both fine cells of the row sit at x/2 = X
+      for (int c = 0; c < 2; c++) {
+        s[0] += arr(fp, F.oe, F.half, 0, c)[r];
+        s[1] += arr(fp, F.oe, F.half, 1, c)[r];
+        s[2] += fp[F.opb + (long long)c * F.half + r];
+      }
+    }
+  const float w = DIM == 2 ? 0.25f : 0.125f;
+  for (int v = 0; v < 2; v++) {
+    arr(fp, C.oe, C.half, v, lc.c)[lc.own] = s[v] * w;
+    arr(fp, C.oec, C.half, v, lc.c)[lc.own] = s[v] * w;
+  }
+  fp[C.opb + (long long)lc.c * C.half + lc.own] = s[2] * w;
+}
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_restrict(float* __restrict__ fp, BoxLev F, BoxLev C) {
+  int X = blockIdx.x * blockDim.x + threadIdx.x;
+  int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (X < C.n[0] && Y < C.n[1]) restrict_at<DIM>(fp, F, C, X, Y, blockIdx.z);
+}
+
+// CoarseLoadingFunction on the correction: coarse g = R(g - M(e)) + M_c(ec)
+template <int DIM>
+__device__ __forceinline__ void coarse_load_at(float* __restrict__ fp, const BoxLev& F, const BoxLev& C, int X, int Y,
+                                               int Z) {
+  float R0 = 0.f, R1 = 0.f;
+  const int nz = DIM == 3 ? 2 : 1;
+  for (int dz = 0; dz < nz; dz++)
+    for (int dy = 0; dy < 2; dy++)
+      for (int dx = 0; dx < 2; dx++) {
+        Loc<DIM> l(F, 2 * X + dx, 2 * Y + dy, DIM == 3 ? 2 * Z + dz : 0);
+        float pb = fp[F.opb + (long long)l.c * F.half + l.own];
+        float m0, m1;
+        mop<DIM>(fp, F, l, pb, m0, m1);
+        R0 += arr(fp, F.og, F.half, 0, l.c)[l.own] - m0;
+        R1 += arr(fp, F.og, F.half, 1, l.c)[l.own] - m1;
+      }
+  const float w = DIM == 2 ? 0.25f : 0.125f;
+  Loc<DIM> lc(C, X, Y, Z);
+  // M_c(ec): the coarse operator on the restricted correction
+  BoxLev Cec = C;
+  Cec.oe = C.oec;
+  float pbc = fp[C.opb + (long long)lc.c * C.half + lc.own];
+  float m0, m1;
+  mop<DIM>(fp, Cec, lc, pbc, m0, m1);
+  arr(fp, C.og, C.half, 0, lc.c)[lc.own] = R0 * w + m0;
+  arr(fp, C.og, C.half, 1, lc.c)[lc.own] = R1 * w + m1;
+}
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_coarse_load(float* __restrict__ fp, BoxLev F, BoxLev C) {
+  int X = blockIdx.x * blockDim.x + threadIdx.x;
+  int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (X < C.n[0] && Y < C.n[1]) coarse_load_at<DIM>(fp, F, C, X, Y, blockIdx.z);
+}
+
+// CorrectFine on e: e_fine += P(e_c - ec), per-direction (3,1)/4 weights
+// (Bi/TriLinProlongationP1, gridutilities.f90:156-195, :510-566).  Thread T
+// (per dimension 0..nc-1) owns fine cells 2T-1 (wrapped) and 2T, between
+// coarse cells T-1 (wrapped) and T.
+template <int DIM>
+__device__ __forceinline__ void prolong_at(float* __restrict__ fp, const BoxLev& F, const BoxLev& C, int T0, int T1,
+                                           int T2) {
+  const int T[3] = {T0, T1, T2};
+  int cx[2][3], fx[2][3];
+  for (int d = 0; d < 3; d++) {
+    int n = C.n[d];
+    cx[0][d] = T[d] ? T[d] - 1 : n - 1;
+    cx[1][d] = T[d];
+    fx[0][d] = T[d] ? 2 * T[d] - 1 : 2 * n - 1;
+    fx[1][d] = 2 * T[d];
+  }
+  constexpr int NZ = DIM == 3 ? 2 : 1;
+  // corrections e_c - ec at the 2x2(x2) coarse corners, both variables
+  float a[2][NZ][2][2];
+  for (int dz = 0; dz < NZ; dz++)
+    for (int dy = 0; dy < 2; dy++)
+      for (int dx = 0; dx < 2; dx++) {
+        Loc<DIM> l(C, cx[dx][0], cx[dy][1], DIM == 3 ? cx[dz][2] : 0);
+        for (int v = 0; v < 2; v++)
+          a[v][dz][dy][dx] = arr(fp, C.oe, C.half, v, l.c)[l.own] - arr(fp, C.oec, C.half, v, l.c)[l.own];
+      }
+  // weight 3/4 on the near coarse cell (f = 0: the first, f = 1: the second)
+  auto w1 = [](float lo, float hi, int f) { return f == 0 ? 3.0f * lo + hi : lo + 3.0f * hi; };
+  // every fine value is loaded before the first store, so the loads of one
+  // thread are in flight together (a store to fp could alias a later load)
+  constexpr int NF = 4 * NZ;
+  float* dst[NF][2];
+  float val[NF][2];
+  for (int m = 0; m < NF; m++) {
+    int fxi = m & 1, fy = (m >> 1) & 1, fz = m >> 2;
+    Loc<DIM> l(F, fx[fxi][0], fx[fy][1], DIM == 3 ? fx[fz][2] : 0);
+    for (int v = 0; v < 2; v++) {
+      dst[m][v] = arr(fp, F.oe, F.half, v, l.c) + l.own;
+      val[m][v] = *dst[m][v];
+    }
+  }
+  for (int m = 0; m < NF; m++) {
+    int fxi = m & 1, fy = (m >> 1) & 1, fz = m >> 2;
+    for (int v = 0; v < 2; v++) {
+      float r0 = w1(w1(a[v][0][0][0], a[v][0][0][1], fxi), w1(a[v][0][1][0], a[v][0][1][1], fxi), fy);
+      float add;
+      if (DIM == 2) {
+        add = r0 * (1.0f / 16.0f);
+      } else {
+        float r1 =
+            w1(w1(a[v][NZ - 1][0][0], a[v][NZ - 1][0][1], fxi), w1(a[v][NZ - 1][1][0], a[v][NZ - 1][1][1], fxi), fy);
+        add = w1(r0, r1, fz) * (1.0f / 64.0f);
+      }
+      val[m][v] += add;
+    }
+  }
+  for (int m = 0; m < NF; m++)
+    for (int v = 0; v < 2; v++) *dst[m][v] = val[m][v];
+}
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_prolong(float* __restrict__ fp, BoxLev F, BoxLev C) {
+  int X = blockIdx.x * blockDim.x + threadIdx.x;
+  int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (X < C.n[0] && Y < C.n[1]) prolong_at<DIM>(fp, F, C, X, Y, blockIdx.z);
+}
+
+// The V-cycle on the coarse end of the hierarchy (levels with at most
+// kSmallCells cells) in one CTA: the same phases as bx_vcycle, separated by
+// __syncthreads() instead of kernel boundaries, so a cycle spends one launch
+// instead of eleven per level on grids too small to fill the GPU.
+constexpr int kSmallCells = 8192;
+constexpr int kSmallThreads = 1024;
+struct SmallLevels {
+  BoxLev L[kNLev];  // L[0] the top (finest) small level, then coarser
+  int n;
+};
+
+template <int DIM>
+__device__ __forceinline__ void small_relax(float* fp, const BoxLev& L, int nsmooth, bool fresh) {
+  int cnt = L.hh * L.n[1] * L.n[2];
+  for (int pass = 1; pass <= nsmooth; pass++)
+    for (int c = 0; c < 2; c++) {
+      int first = (fresh && pass == 1) ? c + 1 : 0;
+      for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+        int h = i % L.hh, r = i / L.hh;
+        relax_at<DIM>(fp, L, c, first, h, r % L.n[1], r / L.n[1]);
+      }
+      __syncthreads();
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kSmallThreads) k_bx_small_vcycle(float* __restrict__ fp, SmallLevels S, int nsmooth,
+                                                                   int fresh) {
+  for (int i = 0; i < S.n; i++) {
+    const BoxLev& F = S.L[i];
+    small_relax<DIM>(fp, F, nsmooth, fresh && i == 0);
+    if (i == S.n - 1) break;
+    const BoxLev& C = S.L[i + 1];
+    int cnt = C.n[0] * C.n[1] * C.n[2];
+    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+      int X = j % C.n[0], r = j / C.n[0];
+      restrict_at<DIM>(fp, F, C, X, r % C.n[1], r / C.n[1]);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+      int X = j % C.n[0], r = j / C.n[0];
+      coarse_load_at<DIM>(fp, F, C, X, r % C.n[1], r / C.n[1]);
+    }
+    __syncthreads();
+  }
+  for (int i = S.n - 2; i >= 0; i--) {
+    const BoxLev &F = S.L[i], &C = S.L[i + 1];
+    int cnt = C.n[0] * C.n[1] * C.n[2];
+    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+      int X = j % C.n[0], r = j / C.n[0];
+      prolong_at<DIM>(fp, F, C, X, r % C.n[1], r / C.n[1]);
+    }
+    __syncthreads();
+    small_relax<DIM>(fp, F, nsmooth, false);
+  }
+}
+
+// After a cycle on the finest level: tracked residual g <- g - M(e) (M at
+// this cycle's base field), its per-CTA sums of squares, then qbar += e as
+// double-float.  One thread per cell; every load precedes every store.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_track_update(float* __restrict__ fp, BoxLev L, long long oqlo,
+                                                         double* __restrict__ partial) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int y = blockIdx.y * blockDim.y + threadIdx.y;
+  int z = blockIdx.z;
+  float s0 = 0.f, s1 = 0.f;
+  if (x < L.n[0] && y < L.n[1]) {
+    Loc<DIM> l(L, x, y, z);
+    float* qh0 = arr(fp, L.opb, L.half, 0, l.c) + l.own;  // the base field is qhi(phi)
+    float* qh1 = arr(fp, L.opb, L.half, 1, l.c) + l.own;
+    float* ql0 = arr(fp, oqlo, L.half, 0, l.c) + l.own;
+    float* ql1 = arr(fp, oqlo, L.half, 1, l.c) + l.own;
+    float* g0 = arr(fp, L.og, L.half, 0, l.c) + l.own;
+    float* g1 = arr(fp, L.og, L.half, 1, l.c) + l.own;
+    float h0 = *qh0, h1 = *qh1, lo0 = *ql0, lo1 = *ql1, a0 = *g0, a1 = *g1;
+    float e0 = arr(fp, L.oe, L.half, 0, l.c)[l.own], e1 = arr(fp, L.oe, L.half, 1, l.c)[l.own];
+    float m0, m1;
+    mop<DIM>(fp, L, l, h0, m0, m1);
+    a0 -= m0;
+    a1 -= m1;
+    DF t0 = two_sum(h0, e0);
+    t0 = fast_two_sum(t0.h, t0.l + lo0);
+    DF t1 = two_sum(h1, e1);
+    t1 = fast_two_sum(t1.h, t1.l + lo1);
+    *g0 = a0;
+    *g1 = a1;
+    *qh0 = t0.h;
+    *ql0 = t0.l;
+    *qh1 = t1.h;
+    *ql1 = t1.l;
+    s0 = a0 * a0;
+    s1 = a1 * a1;
+  }
+  cta_sum2(s0, s1, partial);
+}
+
+// The true residual r = f - N(qbar) of the finest level in double-float
+// (ErrorAFAS, afasroutines.f90:113-233, with f = (phi_old, -phi_old)); g is
+// set to r and the per-CTA sums of r^2 go to partial.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_resid(float* __restrict__ fp, BoxLev L, long long oqlo, long long ofhi,
+                                                  long long oflo, double* __restrict__ partial) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int y = blockIdx.y * blockDim.y + threadIdx.y;
+  int z = blockIdx.z;
+  float s0 = 0.f, s1 = 0.f;
+  if (x < L.n[0] && y < L.n[1]) {
+    const DF c0 = {L.c0h, L.c0l}, c1 = {L.c1h, L.c1l};
+    Loc<DIM> l(L, x, y, z);
+    const int o = 1 - l.c;
+    const int nbi[6] = {l.xm, l.xp, l.ym, l.yp, l.zm, l.zp};
+    DF v[2], nb[2][6];
+    for (int q = 0; q < 2; q++) {
+      const float* hi = arr(fp, L.opb, L.half, q, l.c);
+      const float* lo = arr(fp, oqlo, L.half, q, l.c);
+      v[q] = {hi[l.own], lo[l.own]};
+      const float* ho = arr(fp, L.opb, L.half, q, o);
+      const float* lo2 = arr(fp, oqlo, L.half, q, o);
+      for (int m = 0; m < 2 * DIM; m++) nb[q][m] = {ho[nbi[m]], lo2[nbi[m]]};
+    }
+    DF f1 = {fp[ofhi + (long long)l.c * L.half + l.own], fp[oflo + (long long)l.c * L.half + l.own]};
+    DF lphi = df_lap<DIM>(nb[0], v[0]);
+    DF lmu = df_lap<DIM>(nb[1], v[1]);
+    // r1 = f1 - (phi - c0 lap(mu)); r2 = -f1 - (mu - phi^3 + c1 lap(phi))
+    DF r1 = df_add(df_add(f1, df_neg(v[0])), df_mul(c0, lmu));
+    DF p3 = df_mul(df_mul(v[0], v[0]), v[0]);
+    DF r2 = df_add(df_add(df_neg(df_add(f1, v[1])), p3), df_neg(df_mul(c1, lphi)));
+    float a0 = r1.h + r1.l, a1 = r2.h + r2.l;
+    arr(fp, L.og, L.half, 0, l.c)[l.own] = a0;
+    arr(fp, L.og, L.half, 1, l.c)[l.own] = a1;
+    s0 = a0 * a0;
+    s1 = a1 * a1;
+  }
+  cta_sum2(s0, s1, partial);
+}
+
+// FP64 q (ghosted Fortran layout) -> qhi/qlo, and f = (phi_old, -phi_old) as
+// fhi/flo, on the finest level
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_split(const double* __restrict__ pool, long long oq, long long oqold,
+                                                  long long sq, int qn0, int qn1, float* __restrict__ fp, BoxLev L,
+                                                  long long oqlo, long long ofhi, long long oflo) {
+  int h = blockIdx.x * blockDim.x + threadIdx.x;
+  int y = blockIdx.y * blockDim.y + threadIdx.y;
+  int z = blockIdx.z;
+  if (h >= L.hh || y >= L.n[1]) return;
+  long long g = (2 * h + 1) + (long long)(y + 1) * qn0 + (DIM == 3 ? (long long)(z + 1) * qn0 * qn1 : 0);
+  double in[2][3];  // the two cells' phi, mu, phi_old, loaded before any store
+  for (int b = 0; b < 2; b++) {
+    in[b][0] = pool[oq + g + b];
+    in[b][1] = pool[oq + sq + g + b];
+    in[b][2] = pool[oqold + g + b];
+  }
+  for (int b = 0; b < 2; b++) {
+    Loc<DIM> l(L, 2 * h + b, y, z);
+    for (int v = 0; v < 2; v++) {
+      DF s = split64(in[b][v]);
+      arr(fp, L.opb, L.half, v, l.c)[l.own] = s.h;
+      arr(fp, oqlo, L.half, v, l.c)[l.own] = s.l;
+    }
+    DF f = split64(in[b][2]);
+    fp[ofhi + (long long)l.c * L.half + l.own] = f.h;
+    fp[oflo + (long long)l.c * L.half + l.own] = f.l;
+  }
+}
+
+// qhi + qlo -> FP64 q (interior of the finest level)
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_merge(double* __restrict__ pool, long long oq, long long sq, int qn0,
+                                                  int qn1, const float* __restrict__ fp, BoxLev L, long long oqlo) {
+  int h = blockIdx.x * blockDim.x + threadIdx.x;
+  int y = blockIdx.y * blockDim.y + threadIdx.y;
+  int z = blockIdx.z;
+  if (h >= L.hh || y >= L.n[1]) return;
+  long long g = (2 * h + 1) + (long long)(y + 1) * qn0 + (DIM == 3 ? (long long)(z + 1) * qn0 * qn1 : 0);
+  float hi[2][2], lo[2][2];  // loaded before any store
+  for (int b = 0; b < 2; b++) {
+    Loc<DIM> l(L, 2 * h + b, y, z);
+    for (int v = 0; v < 2; v++) {
+      hi[b][v] = fp[L.opb + (long long)(v * 2 + l.c) * L.half + l.own];
+      lo[b][v] = fp[oqlo + (long long)(v * 2 + l.c) * L.half + l.own];
+    }
+  }
+  for (int b = 0; b < 2; b++)
+    for (int v = 0; v < 2; v++) pool[oq + v * sq + g + b] = f2d(hi[b][v]) + f2d(lo[b][v]);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+struct Launch {
+  dim3 g, b;
+};
+// threads over (nx, ny, nz) with up to 128 along x and 256 per block
+Launch shape(int nx, int ny, int nz) {
+  int tx = nx >= 128 ? 128 : nx;
+  int ty = std::max(1, 256 / tx);
+  if (ty > ny) ty = ny;
+  return {dim3((nx + tx - 1) / tx, (ny + ty - 1) / ty, nz), dim3(tx, ty, 1)};
+}
+long long ctas(const Launch& s) { return (long long)s.g.x * s.g.y * s.g.z; }
+
+#define BX_LAUNCH(H, SH, KER, ...)                                            \
+  do {                                                                        \
+    if ((H).ndims == 2) KER<2><<<(SH).g, (SH).b, 0, (H).s>>>(__VA_ARGS__);    \
+    else KER<3><<<(SH).g, (SH).b, 0, (H).s>>>(__VA_ARGS__);                   \
+    int r__ = after_launch(H, 1);                                             \
+    if (r__) return r__;                                                      \
+  } while (0)
+
+BoxLev& B(Hier& H, int level) { return H.blev[level + kMaxDepth]; }
+
+int bx_relax(Hier& H, int level, int c, int first) {
+  BoxLev& L = B(H, level);
+  Launch sh = shape(L.hh, L.n[1] / 2, L.n[2]);
+  BX_LAUNCH(H, sh, k_bx_relax, H.fpool, L, c, first);
+  return BSAMG_OK;
+}
+
+int bx_level_relax(Hier& H, int level, int nsmooth, bool fresh) {
+  for (int pass = 1; pass <= nsmooth; pass++)
+    for (int c = 0; c < 2; c++) {
+      int r = bx_relax(H, level, c, (fresh && pass == 1) ? c + 1 : 0);
+      if (r) return r;
+    }
+  return BSAMG_OK;
+}
+
+// AFASVcycle (afasroutines.f90:495-529) on the correction
+int bx_vcycle(Hier& H, int level, int minlevel, int nsmooth, bool fresh) {
+  if (2 * B(H, level).half <= kSmallCells) {
+    SmallLevels S{};
+    for (int l = level; l >= minlevel; l--) S.L[S.n++] = B(H, l);
+    if (H.ndims == 2) k_bx_small_vcycle<2><<<1, kSmallThreads, 0, H.s>>>(H.fpool, S, nsmooth, fresh ? 1 : 0);
+    else k_bx_small_vcycle<3><<<1, kSmallThreads, 0, H.s>>>(H.fpool, S, nsmooth, fresh ? 1 : 0);
+    return after_launch(H, 1);
+  }
+  int r = bx_level_relax(H, level, nsmooth, fresh);
+  if (r) return r;
+  if (level > minlevel) {
+    BoxLev &F = B(H, level), &C = B(H, level - 1);
+    Launch sc = shape(C.n[0], C.n[1], C.n[2]);
+    BX_LAUNCH(H, sc, k_bx_restrict, H.fpool, F, C);
+    BX_LAUNCH(H, sc, k_bx_coarse_load, H.fpool, F, C);
+    if ((r = bx_vcycle(H, level - 1, minlevel, nsmooth, false))) return r;
+    BX_LAUNCH(H, sc, k_bx_prolong, H.fpool, F, C);
+    if ((r = bx_level_relax(H, level, nsmooth, false))) return r;
+  }
+  return BSAMG_OK;
+}
+
+int bx_finish(Hier& H, int finest, long long nparts, int errortype) {
+  int r = after_launch(H, launch_norm_finish(H.s, H.d_partial, (int)nparts, H.nrvars, H.L(finest).count, errortype,
+                                             H.d_norm, H.d_nonfinite));
+  if (r) return r;
+  cudaError_t ce = cudaMemcpyAsync(H.h_norm, H.d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, H.s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(norm)");
+  ce = cudaMemcpyAsync(H.h_nonfinite, H.d_nonfinite, sizeof(int), cudaMemcpyDeviceToHost, H.s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(nonfinite)");
+  return BSAMG_OK;
+}
+
+int bx_resid(Hier& H, int finest, int errortype) {
+  BoxLev& L = B(H, finest);
+  Launch sh = shape(L.n[0], L.n[1], L.n[2]);
+  BX_LAUNCH(H, sh, k_bx_resid, H.fpool, L, H.b_oqlo, H.b_ofhi, H.b_oflo, H.d_partial);
+  return bx_finish(H, finest, ctas(sh), errortype);
+}
+
+int bx_cycle(Hier& H, int finest, int minlevel, int nsmooth, int errortype) {
+  int r = bx_vcycle(H, finest, minlevel, nsmooth, true);
+  if (r) return r;
+  BoxLev& L = B(H, finest);
+  Launch sh = shape(L.n[0], L.n[1], L.n[2]);
+  BX_LAUNCH(H, sh, k_bx_track_update, H.fpool, L, H.b_oqlo, H.d_partial);
+  return bx_finish(H, finest, ctas(sh), errortype);
+}
+
+}  // namespace
+
+bool box_eligible(const Hier& H, bool periodic_single) {
+  if (H.problem != kCH || !periodic_single) return false;
+  for (int l = H.minlevel; l <= H.maxlevel; l++) {
+    const HostPatch& P = H.patches[H.L(l).patches[0]];
+    for (int d = 0; d < H.ndims; d++) {
+      if (P.mx[d] % 2) return false;
+      if (l > H.minlevel && P.mx[d] != 2 * H.patches[P.parent].mx[d]) return false;
+    }
+  }
+  return true;
+}
+
+// float pool of the box path: per level e, g, pb (not on the finest level,
+// where pb is qhi(phi)), ec (below the finest); on the finest level qhi,
+// qlo, fhi, flo
+size_t box_layout(Hier& H) {
+  long long o = 0;
+  auto al = [](long long x) { return (x + 63) & ~63LL; };
+  for (int l = H.maxlevel; l >= H.minlevel; l--) {
+    const HostPatch& P = H.patches[H.L(l).patches[0]];
+    BoxLev& L = H.blev[l + kMaxDepth];
+    for (int d = 0; d < 3; d++) L.n[d] = P.mx[d];
+    L.hh = P.mx[0] / 2;
+    L.half = (long long)P.mx[0] * P.mx[1] * P.mx[2] / 2;
+    L.oe = o; o = al(o + 4 * L.half);
+    L.og = o; o = al(o + 4 * L.half);
+    if (l == H.maxlevel) {
+      L.opb = o; o = al(o + 4 * L.half);    // qhi (both variables)
+      H.b_oqlo = o; o = al(o + 4 * L.half);
+      H.b_ofhi = o; o = al(o + 2 * L.half);
+      H.b_oflo = o; o = al(o + 2 * L.half);
+      L.oec = -1;
+    } else {
+      L.opb = o; o = al(o + 2 * L.half);
+      L.oec = o; o = al(o + 4 * L.half);
+    }
+    double c[4];
+    coefficients(H, P.dx[0], c);
+    L.c0 = (float)c[0];
+    L.c1 = (float)c[1];
+    L.tmp3 = (float)c[2];
+    L.a12 = (float)c[3];
+    L.c0h = (float)c[0];
+    L.c0l = (float)(c[0] - (double)L.c0h);
+    L.c1h = (float)c[1];
+    L.c1l = (float)(c[1] - (double)L.c1h);
+  }
+  const BoxLev& F = H.blev[H.maxlevel + kMaxDepth];
+  H.b_partials = (size_t)ctas(shape(F.n[0], F.n[1], F.n[2]));
+  return (size_t)o;
+}
+
+int box_enq_relax(Hier& H, int level, int ipass) { return bx_relax(H, level, ipass - 1, 0); }
+
+int box_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,
+                   int strict, int* ncycles, double* residuals) {
+  if (finest != H.maxlevel || minlevel < H.minlevel) return BSAMG_ERR_UNSUPPORTED;
+  const HostPatch& P = H.patches[H.L(finest).patches[0]];
+  BoxLev& L = B(H, finest);
+  Launch sh = shape(L.hh, L.n[1], L.n[2]);
+  BX_LAUNCH(H, sh, k_bx_split, H.pool, P.oq, P.oqold, P.sq, P.qn[0], P.qn[1], H.fpool, L, H.b_oqlo, H.b_ofhi,
+            H.b_oflo);
+  int r = bx_resid(H, finest, errortype);
+  if (r) return r;
+  cudaError_t ce = cudaStreamSynchronize(H.s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize");
+  if (*H.h_nonfinite) return BSAMG_ERR_NONFINITE;
+  double r_sync = H.h_norm[0];
+  Hier::GraphRec *gc = nullptr, *gv = nullptr;
+  auto key = [&](int m) { return std::make_tuple(m, finest, minlevel, nsmooth, errortype); };
+  if ((r = capture_graph(H, key(21), [&] { return bx_cycle(H, finest, minlevel, nsmooth, errortype); }, &gc)))
+    return r;
+  if ((r = capture_graph(H, key(22), [&] { return bx_resid(H, finest, errortype); }, &gv))) return r;
+  bool conv = false;
+  int it;
+  for (it = 1; it <= maxvcycles; it++) {
+    if ((r = replay(H, gc))) return r;
+    if (*H.h_nonfinite) return BSAMG_ERR_NONFINITE;
+    double tracked = H.h_norm[0], res = tracked;
+    // confirm on the true residual when the tracked one says converged, on
+    // the last cycle, and once the tracked value is 1e5 below the residual
+    // it started from (where FP32 rounding of g - M(e) stops being negligible)
+    if (tracked < tol || tracked < 1e-5 * r_sync || it == maxvcycles) {
+      if ((r = replay(H, gv))) return r;
+      if (*H.h_nonfinite) return BSAMG_ERR_NONFINITE;
+      res = H.h_norm[0];
+      r_sync = res;
+      if (residuals) residuals[it - 1] = res;
+      if (res < tol) {
+        conv = true;
+        break;
+      }
+      continue;
+    }
+    if (residuals) residuals[it - 1] = res;
+  }
+  if (ncycles) *ncycles = conv ? it : maxvcycles;
+  // leave the state as the FP64 path leaves it: q in FP64 with fresh ghosts
+  // and the coarse levels restricted from the finest (FillDown,
+  // afasroutines.f90:83)
+  BX_LAUNCH(H, sh, k_bx_merge, H.pool, P.oq, P.sq, P.qn[0], P.qn[1], H.fpool, L, H.b_oqlo);
+  if ((r = enq_set_ghost(H, finest, 0))) return r;
+  if ((r = enq_fill_down(H, 2, finest, minlevel))) return r;
+  if (!conv && strict) return BSAMG_ERR_NOT_CONVERGED;
+  return BSAMG_OK;
+}
+
+}  // namespace bsamg

@@ -11,6 +11,8 @@
 // 32 bytes of algorithmic traffic, and the part issues FP64 at ~1.2 TFLOP/s.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "internal.h"
 #include "launch.h"
 
@@ -463,24 +465,83 @@ __global__ void __launch_bounds__(kBlock) k_norm_partial(const PatchDev* __restr
 }
 
 // Final deterministic reduction of the block partials in block order.
-__global__ void k_norm_finish(const double* __restrict__ partial, int nblk, int nrvars, double count,
-                              int errortype, double* out, int* nonfinite) {
+// First stage of a long final sum: CTA g adds the partial pairs
+// [g*chunk, min((g+1)*chunk, nblk)) in a fixed order and writes one pair to
+// stage[2g], stage[2g+1].  Spreading the FP64 additions over many SMs
+// matters on GB300, whose FP64 rate is two additions per clock per SM.
+constexpr int kStageBlocks = (kNormOutLen - 8) / 2;
+__global__ void __launch_bounds__(kBlock) k_norm_stage(const double* __restrict__ partial, int nblk, int chunk,
+                                                       double* __restrict__ stage) {
   __shared__ double red[2][kBlock];
-  double t0 = 0.0, t1 = 0.0;
-  for (int n = threadIdx.x; n < nblk; n += blockDim.x) {
-    t0 = t0 + partial[2 * n];
-    t1 = t1 + partial[2 * n + 1];
+  int lo = blockIdx.x * chunk, hi = min(lo + chunk, nblk);
+  double a = 0.0, c = 0.0;
+  for (int n = lo + threadIdx.x; n < hi; n += kBlock) {
+    a = a + partial[2 * n];
+    c = c + partial[2 * n + 1];
   }
-  red[0][threadIdx.x] = t0;
-  red[1][threadIdx.x] = t1;
+  red[0][threadIdx.x] = a;
+  red[1][threadIdx.x] = c;
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      red[0][threadIdx.x] = red[0][threadIdx.x] + red[0][threadIdx.x + s];
-      red[1][threadIdx.x] = red[1][threadIdx.x] + red[1][threadIdx.x + s];
+  for (int w = kBlock / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      red[0][threadIdx.x] = red[0][threadIdx.x] + red[0][threadIdx.x + w];
+      red[1][threadIdx.x] = red[1][threadIdx.x] + red[1][threadIdx.x + w];
     }
     __syncthreads();
   }
+  if (threadIdx.x == 0) {
+    stage[2 * blockIdx.x] = red[0][0];
+    stage[2 * blockIdx.x + 1] = red[1][0];
+  }
+}
+
+// One CTA of 1024 threads; each thread keeps eight independent partial sums
+// so that eight loads are in flight, then a fixed-shape tree.  The order of
+// the additions depends only on nblk, so the result is deterministic.
+constexpr int kFinishThreads = 1024;
+__global__ void __launch_bounds__(kFinishThreads) k_norm_finish(const double* __restrict__ partial, int nblk,
+                                                                int nrvars, double count, int errortype, double* out,
+                                                                int* nonfinite) {
+  __shared__ double red[2][kFinishThreads / 32];
+  double a[8], c[8];
+  for (int u = 0; u < 8; u++) a[u] = c[u] = 0.0;
+  int n = threadIdx.x;
+  for (; n + 7 * kFinishThreads < nblk; n += 8 * kFinishThreads)
+    for (int u = 0; u < 8; u++) {
+      a[u] = a[u] + partial[2 * (n + u * kFinishThreads)];
+      c[u] = c[u] + partial[2 * (n + u * kFinishThreads) + 1];
+    }
+  // the remaining (at most seven) partials of this thread; a constant index
+  // keeps a[] and c[] in registers
+  for (; n < nblk; n += kFinishThreads) {
+    a[0] = a[0] + partial[2 * n];
+    c[0] = c[0] + partial[2 * n + 1];
+  }
+  double t0 = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+  double t1 = ((c[0] + c[1]) + (c[2] + c[3])) + ((c[4] + c[5]) + (c[6] + c[7]));
+  for (int o = 16; o > 0; o >>= 1) {
+    t0 = t0 + __shfl_down_sync(0xffffffffu, t0, o);
+    t1 = t1 + __shfl_down_sync(0xffffffffu, t1, o);
+  }
+  int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[0][w] = t0;
+    red[1][w] = t1;
+  }
+  __syncthreads();
+  if (w == 0) {
+    t0 = red[0][threadIdx.x];
+    t1 = red[1][threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) {
+      t0 = t0 + __shfl_down_sync(0xffffffffu, t0, o);
+      t1 = t1 + __shfl_down_sync(0xffffffffu, t1, o);
+    }
+    if (threadIdx.x == 0) {
+      red[0][0] = t0;
+      red[1][0] = t1;
+    }
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
     double a = red[0][0], c = red[1][0];
     double r;
@@ -622,7 +683,16 @@ int launch_norm_partial(const LaunchCtx& c, const Blk* blk, int nblk, double* pa
 }
 int launch_norm_finish(cudaStream_t s, const double* partial, int nblk, int nrvars, double count, int errortype,
                        double* out, int* nonfinite) {
-  k_norm_finish<<<1, kBlock, 0, s>>>(partial, nblk, nrvars, count, errortype, out, nonfinite);
+  if (nblk > 2048) {
+    // two stages; out[8 ..] holds the stage sums
+    int g = std::min(kStageBlocks, (nblk + 511) / 512);
+    int chunk = (nblk + g - 1) / g;
+    g = (nblk + chunk - 1) / chunk;
+    k_norm_stage<<<g, kBlock, 0, s>>>(partial, nblk, chunk, out + 8);
+    k_norm_finish<<<1, kFinishThreads, 0, s>>>(out + 8, g, nrvars, count, errortype, out, nonfinite);
+    return 2;
+  }
+  k_norm_finish<<<1, kFinishThreads, 0, s>>>(partial, nblk, nrvars, count, errortype, out, nonfinite);
   return 1;
 }
 int launch_ghost_stage(const LaunchCtx& c, const GhostOp* ops, int n) {

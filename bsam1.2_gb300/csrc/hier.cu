@@ -10,6 +10,7 @@
 #include <string>
 
 #include "hier.h"
+#include "box.h"
 #include "mixed.h"
 
 using namespace bsamg;
@@ -201,6 +202,23 @@ int replay(Hier& H, Hier::GraphRec* g) {
   return BSAMG_OK;
 }
 
+// plugin coefficients for a spacing h (see PatchDev::c)
+void coefficients(const Hier& H, double h, double* c) {
+  double h2 = h * h;
+  if (H.problem == kCH) {
+    double k = H.ndims == 2 ? 4.0 : 6.0;
+    c[0] = H.pp.dt / h2;       // tmp1, CH/problem.f90:341
+    c[1] = H.pp.eps2 / h2;     // tmp2, :342
+    c[2] = k * H.pp.eps2 / h2; // tmp3, :343 (:579)
+    c[3] = k * c[0];           // a(1,2), :346 (:582)
+  } else {
+    c[0] = H.pp.dt * H.pp.eps2 / h2;  // tmp1, BioGrowth/problem.f90:277
+    c[1] = 1.0 / h2;                  // tmp3, :278
+    c[2] = 4.0 * c[0] + 1.0;          // first two terms of tmp2, :282
+    c[3] = 4.0 * c[1];                // first term of tmp4, :288
+  }
+}
+
 }  // namespace bsamg
 
 namespace {
@@ -214,6 +232,9 @@ int multigrid_iterations(Hier& H, int finest, int minlevel, int nsmooth, int max
   if (mode != BSAMG_MODE_FP64 && mode != BSAMG_MODE_MIXED) return BSAMG_ERR_ARG;
   RET(set_device(H));
   // afasroutines.f90:57-76
+  // the periodic-box mixed path forms f from qold itself
+  if (mode == BSAMG_MODE_MIXED && H.box)
+    return box_iterations(H, finest, minlevel, nsmooth, maxvcycles, tol, errortype, strict, ncycles, residuals);
   RET(enq_fill_down(H, 2, finest, minlevel));
   RET(enq_get_source(H, finest));
   RET(enq_update_source(H, finest));
@@ -336,22 +357,6 @@ void periodic_setup(Hier& H, const int* mthbc) {
   for (int i = 0; i < n; i++) H.peroffidx[i] = src[i];
 }
 
-// plugin coefficients for a spacing h (see PatchDev::c)
-void coefficients(const Hier& H, double h, double* c) {
-  double h2 = h * h;
-  if (H.problem == kCH) {
-    double k = H.ndims == 2 ? 4.0 : 6.0;
-    c[0] = H.pp.dt / h2;       // tmp1, CH/problem.f90:341
-    c[1] = H.pp.eps2 / h2;     // tmp2, :342
-    c[2] = k * H.pp.eps2 / h2; // tmp3, :343 (:579)
-    c[3] = k * c[0];           // a(1,2), :346 (:582)
-  } else {
-    c[0] = H.pp.dt * H.pp.eps2 / h2;  // tmp1, BioGrowth/problem.f90:277
-    c[1] = 1.0 / h2;                  // tmp3, :278
-    c[2] = 4.0 * c[0] + 1.0;          // first two terms of tmp2, :282
-    c[3] = 4.0 * c[1];                // first term of tmp4, :288
-  }
-}
 
 int upload_blocks(Hier& H, LevelT& L, int kind) {
   std::vector<Blk> v;
@@ -496,7 +501,7 @@ int commit(Hier& H) {
     for (const HostPatch& P : H.patches)
       for (int f = 0; f < 2 * H.ndims; f++) w = w && P.mthbc[f] == 2;
     for (int v = 0; v < H.nrvars; v++) w = w && H.pp.qpo[v] == 0.0;
-    H.wrap_all = w;
+    H.box = box_eligible(H, w);
   }
 
   // pool layout: [q...][qold...][qc...][f...][rf...][ftmp...]
@@ -517,7 +522,7 @@ int commit(Hier& H) {
   for (HostPatch& P : H.patches) { P.orf = off; off = align32(off + P.sf * H.nrvars); }
   for (HostPatch& P : H.patches) { P.oftmp = off; off = align32(off + P.sf * H.nrvars); }
   H.pool_elems = (size_t)off;
-  size_t need = H.pool_elems * sizeof(double) + mixed_pool_bytes(H);
+  size_t need = H.pool_elems * sizeof(double) + (H.box ? box_layout(H) * sizeof(float) : mixed_pool_bytes(H));
   {
     std::lock_guard<std::mutex> lk(H.ctx->mu);
     if (H.ctx->budget && H.ctx->used + need > H.ctx->budget) return BSAMG_ERR_BUDGET;
@@ -582,9 +587,10 @@ int commit(Hier& H) {
     }
   }
   RET(mixed_tables(H));
+  maxblk = std::max(maxblk, (int)H.b_partials);
   H.partial_cap = maxblk;
   CK(cudaMallocAsync((void**)&H.d_partial, sizeof(double) * 2 * (size_t)maxblk * std::max(1, H.nrvars), H.s));
-  CK(cudaMallocAsync((void**)&H.d_norm, sizeof(double) * 8, H.s));
+  CK(cudaMallocAsync((void**)&H.d_norm, sizeof(double) * kNormOutLen, H.s));
   CK(cudaMallocAsync((void**)&H.d_nonfinite, sizeof(int) * 4, H.s));
   RET(pinned_slot_take(H));
   CK(cudaStreamSynchronize(H.s));

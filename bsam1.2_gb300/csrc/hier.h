@@ -53,9 +53,6 @@ struct Hier {
   std::vector<HostPatch> patches;
   std::unordered_map<int, int> id2idx;
   bool committed = false;
-  // every level is one fully periodic patch and qpo = 0: the mixed path
-  // addresses neighbours with periodic wrap instead of ghost cells
-  bool wrap_all = false;
   int minlevel = 0, maxlevel = 0;
   int periodic = 0, nperoff = 0, peroffidx[13] = {};
   int mxmax[kMaxDepth + 1][3] = {};
@@ -69,6 +66,12 @@ struct Hier {
   size_t e_len = 0;  // leading FP32 elements holding every patch's correction e
   size_t e_coarse_off = 0, e_coarse_len = 0;  // the part of it on levels < 0
   Blk* mx_norm_blk[kNLev] = {};               // padded interior lists (mixed norm)
+  // periodic-box mixed path (box.cu): every level one periodic box with even
+  // extents covering its parent; FP64 iterate held as float pairs
+  bool box = false;
+  BoxLev blev[kNLev] = {};
+  long long b_oqlo = 0, b_ofhi = 0, b_oflo = 0;  // float offsets (qhi is blev[finest].opb)
+  size_t b_partials = 0;                         // partial-sum slots the box kernels need
   size_t bytes = 0;
   size_t reserved = 0;  // bytes counted against the context budget
 
@@ -115,6 +118,8 @@ int enq_fill_down(Hier& H, int field, int finest, int minlevel);
 int enq_update_source(Hier& H, int finest);
 int enq_norm(Hier& H, int level, int errortype);
 int enq_relax(Hier& H, int level, int ipass);
+// plugin coefficients for a spacing h (PatchDev::c)
+void coefficients(const Hier& H, double h, double* c);
 using GraphKey = std::tuple<int, int, int, int, int>;
 // capture what `body` enqueues as a CUDA graph (once per key) and replay it
 int capture_graph(Hier& H, const GraphKey& key, const std::function<int()>& body, Hier::GraphRec** out);

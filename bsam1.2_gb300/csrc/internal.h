@@ -46,6 +46,22 @@ struct PatchDev {
   double h;
 };
 
+// One level of the periodic-box mixed path (box.cu): the level is a single
+// fully periodic n0 x n1 x n2 box with even extents.  Its FP32 arrays are
+// stored colour-split: for variable v and colour c (c = parity of the
+// 1-based i+j(+k), so ipass 1 is c = 0) the cells of that colour follow row
+// by row (row = (z, y)), hh = n0/2 of them per row; element
+// (v*2 + c)*half + row*hh + x/2.  pb (the base phase field) has one variable.
+struct BoxLev {
+  int n[3];        // cells per dimension (n[2] = 1 in 2D)
+  int hh;          // n[0] / 2
+  int pad;
+  long long half;  // cells of one colour
+  long long oe, og, opb, oec;   // float offsets: e, g, pb, ec (ec: levels below the finest)
+  float c0, c1, tmp3, a12;      // dt/h^2, eps^2/h^2, (4|6) eps^2/h^2, (4|6) dt/h^2
+  float c0h, c0l, c1h, c1l;     // dt/h^2 and eps^2/h^2 as float pairs (hi + lo)
+};
+
 // One block of a level's work list: block covers units [start, start+kBlock)
 // of patch `patch`.
 struct Blk {

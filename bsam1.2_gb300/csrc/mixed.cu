@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "launch.h"
+#include "box.h"
 #include "mixed.h"
 
 namespace bsamg {
@@ -97,49 +98,34 @@ __device__ __forceinline__ T ulap(const T* a, long long c, long long sy, long lo
 }
 
 // ---------------------------------------------------------------------------
-// Neighbour addressing.  WRAP = true on hierarchies whose every level is one
-// fully periodic patch (and qpo = 0): neighbours of boundary cells are read
-// from the opposite side of the interior, so the correction cycle needs no
-// ghost fills at all; the FP64 ghosts are refreshed once after the loop.
+// Neighbour offsets of a cell in a ghosted array.
 
-template <int DIM, bool WRAP>
+template <int DIM>
 struct Nbr {
   long long xm, xp, ym, yp, zm, zp;
-  __device__ __forceinline__ Nbr(long long c, int i, int j, int k, const int* mx, long long sy, long long sz) {
+  __device__ __forceinline__ Nbr(long long c, long long sy, long long sz) {
     xm = c - 1; xp = c + 1; ym = c - sy; yp = c + sy; zm = c - sz; zp = c + sz;
-    if (WRAP) {
-      if (i == 1) xm = c + (mx[0] - 1);
-      if (i == mx[0]) xp = c - (mx[0] - 1);
-      if (j == 1) ym = c + (long long)(mx[1] - 1) * sy;
-      if (j == mx[1]) yp = c - (long long)(mx[1] - 1) * sy;
-      if (DIM == 3) {
-        if (k == 1) zm = c + (long long)(mx[2] - 1) * sz;
-        if (k == mx[2]) zp = c - (long long)(mx[2] - 1) * sz;
-      }
-    }
   }
 };
 
-template <int DIM, bool WRAP, typename T>
-__device__ __forceinline__ T ulapn(const T* a, long long c, const Nbr<DIM, WRAP>& n) {
+template <int DIM, typename T>
+__device__ __forceinline__ T ulapn(const T* a, long long c, const Nbr<DIM>& n) {
   if (DIM == 2) return a[n.xp] + a[n.xm] + a[n.yp] + a[n.ym] - T(4) * a[c];
   return a[n.xp] + a[n.xm] + a[n.yp] + a[n.ym] + a[n.zp] + a[n.zm] - T(6) * a[c];
 }
 
 // correction operator at a fine cell with neighbour set n
-template <int DIM, bool WRAP>
-__device__ __forceinline__ void mopn(const float* e, long long c, const Nbr<DIM, WRAP>& n, long long ps, float pb,
+template <int DIM>
+__device__ __forceinline__ void mopn(const float* e, long long c, const Nbr<DIM>& n, long long ps, float pb,
                                      float c0, float c1, float& m0, float& m1) {
   const float* e0 = e;
   const float* e1 = e + ps;
   float x = e0[c];
-  m0 = x - c0 * ulapn<DIM, WRAP>(e1, c, n);
-  m1 = e1[c] - x * (3.0f * pb * (pb + x) + x * x) + c1 * ulapn<DIM, WRAP>(e0, c, n);
+  m0 = x - c0 * ulapn<DIM>(e1, c, n);
+  m1 = e1[c] - x * (3.0f * pb * (pb + x) + x * x) + c1 * ulapn<DIM>(e0, c, n);
 }
 
 constexpr int kNormCells = 8;  // interior blocks per CTA in k_mx_norm
-
-__device__ __forceinline__ int wrap1(int x, int n) { return x < 1 ? x + n : (x > n ? x - n : x); }
 
 // step 1: phib = (float)qbar_phi everywhere; g = FP32 of the FP64 residual:
 // mode 0: phib only, 1: g from the stored rf, 2: g = f - N(qbar) recomputed
@@ -176,7 +162,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_prep(const PatchDev* __restrict__
 //   a21 = -3 (pb + e)^2 - tmp3
 //   b1  = g1 + tmp1 * sum(e_mu neighbours)
 //   b2  = g2 - tmp2 * sum(e_phi neighbours) - e^2 (3 pb + 2 e)
-template <int DIM, bool WRAP>
+template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_relax(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                      const Blk* __restrict__ blk, int ipass) {
   const Blk b = blk[blockIdx.x];
@@ -188,7 +174,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_relax(const PatchDev* __restrict_
   long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
   long long c = gofs<DIM>(p.qn, i, j, k);
   long long fc = iofs<DIM>(p.mx, i, j, k);
-  Nbr<DIM, WRAP> n(c, i, j, k, p.mx, sy, sz);
+  Nbr<DIM> n(c, sy, sz);
   float tmp1 = p.cf[0], tmp2 = p.cf[1], tmp3 = p.cf[2], a12 = p.cf[3];
   float pb = fpool[p.ephi + fc];
   float x = e0[c];
@@ -239,8 +225,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_restrict(const PatchDev* __restri
 
 // GetCoarseGhostPoints on e (ring of ec <- parent e) when corr == 0;
 // CorrectFine step 1 (ec = parent e - ec over the whole ghosted ec) when
-// corr == 1.  With WRAP the parent index wraps around the parent's interior.
-template <int DIM, bool WRAP>
+// corr == 1.
+template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_coarse_ring(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                            const Blk* __restrict__ blk, int nrvars, int corr) {
   const Blk b = blk[blockIdx.x];
@@ -254,11 +240,6 @@ __global__ void __launch_bounds__(kBlock) k_mx_coarse_ring(const PatchDev* __res
   }
   const PatchDev& par = P[p.parent];
   int pi = p.mb[0] - 1 + i, pj = p.mb[1] - 1 + j, pk = DIM == 3 ? p.mb[2] - 1 + k : 0;
-  if (WRAP) {
-    pi = wrap1(pi, par.mx[0]);
-    pj = wrap1(pj, par.mx[1]);
-    if (DIM == 3) pk = wrap1(pk, par.mx[2]);
-  }
   long long src = gofs<DIM>(par.qn, pi, pj, pk);
   long long dst = gofs<DIM>(p.cn, i, j, k);
   for (int v = 0; v < nrvars; v++) {
@@ -270,7 +251,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_coarse_ring(const PatchDev* __res
 
 // CoarseLoadingFunction on the correction: fine r = g - M(e) under each
 // coarse cell; parent g(mb) = R(r) + M_c(ec) with the parent's base field.
-template <int DIM, bool WRAP>
+template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_coarse_load(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                            const Blk* __restrict__ blk) {
   const Blk b = blk[blockIdx.x];
@@ -289,9 +270,9 @@ __global__ void __launch_bounds__(kBlock) k_mx_coarse_load(const PatchDev* __res
         int i = 2 * ci - di, j = 2 * cj - dj, k = DIM == 3 ? 2 * ck - dk : 1;
         long long c = gofs<DIM>(p.qn, i, j, k);
         long long fc = iofs<DIM>(p.mx, i, j, k);
-        Nbr<DIM, WRAP> n(c, i, j, k, p.mx, sy, sz);
+        Nbr<DIM> n(c, sy, sz);
         float m0, m1;
-        mopn<DIM, WRAP>(e, c, n, p.sq, fpool[p.ephi + fc], c0, c1, m0, m1);
+        mopn<DIM>(e, c, n, p.sq, fpool[p.ephi + fc], c0, c1, m0, m1);
         R0 += fpool[p.eg + fc] - m0;
         R1 += fpool[p.eg + p.sf + fc] - m1;
       }
@@ -302,19 +283,19 @@ __global__ void __launch_bounds__(kBlock) k_mx_coarse_load(const PatchDev* __res
   long long cc = gofs<DIM>(p.cn, ci, cj, ck);
   long long pf = iofs<DIM>(par.mx, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 1);
   // the coarse operator reads the ec ring, which coarse_ring has filled
-  Nbr<DIM, false> n(cc, ci, cj, ck, p.cmx, csy, csz);
+  Nbr<DIM> n(cc, csy, csz);
   float m0, m1;
-  mopn<DIM, false>(ec, cc, n, p.sc, fpool[par.ephi + pf], par.cf[0], par.cf[1], m0, m1);
+  mopn<DIM>(ec, cc, n, p.sc, fpool[par.ephi + pf], par.cf[0], par.cf[1], m0, m1);
   fpool[par.eg + pf] = R0 + m0;
   fpool[par.eg + par.sf + pf] = R1 + m1;
 }
 
-// CorrectFine step 2 on e: e(0:mx+1) += P(ec) (interior only with WRAP).
+// CorrectFine step 2 on e: e(0:mx+1) += P(ec).
 // One thread per coarse index (ci,cj,ck) in 0..cmx: it produces the fine
 // cells 2ci..2ci+1 (x) etc. from the 2x2(x2) coarse values they share, with
 // the same per-direction (3,1)/4 weights as BiLin/TriLinProlongationP1
 // (gridutilities.f90:156-195, :510-566).
-template <int DIM, bool WRAP>
+template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_prolong(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                        const Blk* __restrict__ blk, int nrvars) {
   const Blk b = blk[blockIdx.x];
@@ -340,8 +321,6 @@ __global__ void __launch_bounds__(kBlock) k_mx_prolong(const PatchDev* __restric
       for (int fy = 0; fy < 2; fy++)
         for (int fx = 0; fx < 2; fx++) {
           int i = 2 * ci + fx, j = 2 * cj + fy, k = DIM == 3 ? 2 * ck + fz : 0;
-          if (WRAP && (i == 0 || i > p.mx[0] || j == 0 || j > p.mx[1] || (DIM == 3 && (k == 0 || k > p.mx[2]))))
-            continue;
           float add;
           if (DIM == 2) {
             float blo = bxv[0][0][fx], bhi = bxv[0][1][fx];
@@ -356,11 +335,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_prolong(const PatchDev* __restric
   }
 }
 
-// step 3: qbar += e (whole ghosted array; interior only with WRAP).  The
+// step 3: qbar += e (whole ghosted array).  The
 // same pass refreshes the base field phib of the next cycle and clears e,
 // so the next cycle needs neither a separate prep pass over q nor a memset
 // on this level.
-template <int DIM, bool WRAP>
+template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_update(const PatchDev* __restrict__ P, double* __restrict__ pool,
                                                       float* __restrict__ fpool, const Blk* __restrict__ blk,
                                                       int nrvars) {
@@ -369,7 +348,6 @@ __global__ void __launch_bounds__(kBlock) k_mx_update(const PatchDev* __restrict
   int i, j, k;
   if (!ghosted_cell<DIM>(p.qn, b.start + threadIdx.x, i, j, k)) return;
   bool interior = i >= 1 && i <= p.mx[0] && j >= 1 && j <= p.mx[1] && (DIM == 2 || (k >= 1 && k <= p.mx[2]));
-  if (WRAP && !interior) return;
   long long c = gofs<DIM>(p.qn, i, j, k);
   for (int v = 0; v < nrvars; v++) {
     double nq = pool[p.oq + v * p.sq + c] + (double)fpool[p.eq + v * p.sq + c];
@@ -384,7 +362,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_update(const PatchDev* __restrict
 // path's norm kernel, but this translation unit lets the compiler fuse
 // multiply-adds, which cuts FP64 pipe work by about a third; the mixed path
 // needs the true residual to ~1e-15 relative, not bit-identical rounding.
-template <int DIM, bool WRAP>
+template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_norm(const PatchDev* __restrict__ P, double* __restrict__ pool,
                                                     const Blk* __restrict__ blk, double* __restrict__ partial) {
   // kNormCells consecutive blocks of the interior list per CTA, so the
@@ -403,10 +381,10 @@ __global__ void __launch_bounds__(kBlock) k_mx_norm(const PatchDev* __restrict__
     long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
     long long c = gofs<DIM>(p.qn, i, j, k);
     long long fc = iofs<DIM>(p.mx, i, j, k);
-    Nbr<DIM, WRAP> n(c, i, j, k, p.mx, sy, sz);
+    Nbr<DIM> n(c, sy, sz);
     double phi = q0[c];
-    double o0 = phi - p.c[0] * ulapn<DIM, WRAP>(q1, c, n);
-    double o1 = q1[c] - phi * phi * phi + p.c[1] * ulapn<DIM, WRAP>(q0, c, n);
+    double o0 = phi - p.c[0] * ulapn<DIM>(q1, c, n);
+    double o1 = q1[c] - phi * phi * phi + p.c[1] * ulapn<DIM>(q0, c, n);
     double e0 = pool[p.of + fc] - o0;
     double e1 = pool[p.of + p.sf + fc] - o1;
     pool[p.orf + fc] = e0;
@@ -439,7 +417,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_norm(const PatchDev* __restrict__
 // new residual is exactly g - M(e) (M is the difference N(qbar+e) - N(qbar)),
 // so g <- g - M(e) on the finest level gives the next right-hand side and,
 // summed, the tracked norm.
-template <int DIM, bool WRAP>
+template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_track(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                      const Blk* __restrict__ blk, double* __restrict__ partial) {
   // sums of squares in FP32 (the tracked norm only decides when to
@@ -454,9 +432,9 @@ __global__ void __launch_bounds__(kBlock) k_mx_track(const PatchDev* __restrict_
     long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
     long long c = gofs<DIM>(p.qn, i, j, k);
     long long fc = iofs<DIM>(p.mx, i, j, k);
-    Nbr<DIM, WRAP> n(c, i, j, k, p.mx, sy, sz);
+    Nbr<DIM> n(c, sy, sz);
     float m0, m1;
-    mopn<DIM, WRAP>(e, c, n, p.sq, fpool[p.ephi + fc], p.cf[0], p.cf[1], m0, m1);
+    mopn<DIM>(e, c, n, p.sq, fpool[p.ephi + fc], p.cf[0], p.cf[1], m0, m1);
     float g0 = fpool[p.eg + fc] - m0;
     float g1 = fpool[p.eg + p.sf + fc] - m1;
     fpool[p.eg + fc] = g0;
@@ -545,24 +523,9 @@ __global__ void __launch_bounds__(kBlock) k_ghost32_program(const PatchDev* __re
     }                                                                                       \
   } while (0)
 
-#define MX_LAUNCH_W(H, kind, KER, ...)                                                      \
-  do {                                                                                      \
-    int nb__ = L.nblk[kind];                                                                \
-    if (nb__ > 0) {                                                                         \
-      if ((H).ndims == 2) {                                                                 \
-        if ((H).wrap_all) KER<2, true><<<nb__, kBlock, 0, (H).s>>>(__VA_ARGS__);            \
-        else KER<2, false><<<nb__, kBlock, 0, (H).s>>>(__VA_ARGS__);                        \
-      } else {                                                                              \
-        if ((H).wrap_all) KER<3, true><<<nb__, kBlock, 0, (H).s>>>(__VA_ARGS__);            \
-        else KER<3, false><<<nb__, kBlock, 0, (H).s>>>(__VA_ARGS__);                        \
-      }                                                                                     \
-      int r__ = after_launch(H, 1);                                                         \
-      if (r__) return r__;                                                                  \
-    }                                                                                       \
-  } while (0)
+#define MX_LAUNCH_W MX_LAUNCH
 
 int mx_set_ghost(Hier& H, int level, int ipass) {
-  if (H.wrap_all) return BSAMG_OK;  // every consumer wraps
   GhostProg& g = H.L(level).gp[ipass];
   int nst = (int)g.stage_off.size() - 1;
   if (nst <= 0) return BSAMG_OK;
@@ -642,11 +605,9 @@ int mx_norm(Hier& H, int level, int errortype) {
   // the interior list is padded with patch = -1 entries to a multiple of
   // kNormCells (see mixed_alloc)
   if (H.ndims == 2) {
-    if (H.wrap_all) k_mx_norm<2, true><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.mx_norm_blk[level + kMaxDepth], H.d_partial);
-    else k_mx_norm<2, false><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.mx_norm_blk[level + kMaxDepth], H.d_partial);
+    k_mx_norm<2><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.mx_norm_blk[level + kMaxDepth], H.d_partial);
   } else {
-    if (H.wrap_all) k_mx_norm<3, true><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.mx_norm_blk[level + kMaxDepth], H.d_partial);
-    else k_mx_norm<3, false><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.mx_norm_blk[level + kMaxDepth], H.d_partial);
+    k_mx_norm<3><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.mx_norm_blk[level + kMaxDepth], H.d_partial);
   }
   int r = after_launch(H, 1);
   if (r) return r;
@@ -662,17 +623,8 @@ int to_host(Hier& H) {
   return BSAMG_OK;
 }
 
-// FillDown of q in FP64 (restriction to the parents); with WRAP the coarse
-// ghosts are not needed inside the loop, so the ghost fills are skipped
-int mx_fill_down_q(Hier& H, int finest, int minlevel) {
-  if (!H.wrap_all) return enq_fill_down(H, 2, finest, minlevel);
-  for (int level = finest; level >= minlevel + 1; level--) {
-    LevelT& L = H.L(level);
-    int r = after_launch(H, launch_fill_down(H.lc(), L.d_blk[kKindCoarse], L.nblk[kKindCoarse], 2));
-    if (r) return r;
-  }
-  return BSAMG_OK;
-}
+// FillDown of q in FP64 (restriction to the parents, with their ghosts)
+int mx_fill_down_q(Hier& H, int finest, int minlevel) { return enq_fill_down(H, 2, finest, minlevel); }
 
 // one outer iteration; resync: take g on the finest level from the FP64 rf
 int mx_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype, bool resync) {
@@ -730,6 +682,14 @@ size_t mixed_pool_bytes(const Hier& H) {
 
 int mixed_alloc(Hier& H) {
   if (H.problem != kCH) return BSAMG_OK;
+  if (H.box) {
+    H.fpool_elems = box_layout(H);
+    cudaError_t e = cudaMallocAsync((void**)&H.fpool, H.fpool_elems * sizeof(float), H.s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(fpool)");
+    e = cudaMemsetAsync(H.fpool, 0, H.fpool_elems * sizeof(float), H.s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(fpool)");
+    return BSAMG_OK;
+  }
   size_t n, ne, ec;
   std::vector<long long> off = layout(H, &n, &ne, &ec);
   H.e_len = ne;
@@ -760,7 +720,7 @@ void mixed_free(Hier& H) {
 }
 
 int mixed_tables(Hier& H) {
-  if (H.problem != kCH || !H.fpool) return BSAMG_OK;
+  if (H.problem != kCH || !H.fpool || H.box) return BSAMG_OK;
   for (int l = H.minlevel; l <= H.maxlevel; l++) {
     // interior work list padded with patch = -1 to a multiple of kNormCells
     std::vector<Blk> v;
@@ -785,6 +745,7 @@ int mixed_tables(Hier& H) {
 
 int mixed_enq_relax(Hier& H, int level, int ipass) {
   if (H.problem != kCH || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
+  if (H.box) return box_enq_relax(H, level, ipass);
   LevelT& L = H.L(level);
   MX_LAUNCH_W(H, kKindColor, k_mx_relax, H.dP, H.fpool, L.d_blk[kKindColor], ipass);
   return BSAMG_OK;
@@ -847,10 +808,8 @@ int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcyc
   if (ncycles) *ncycles = conv ? it : maxvcycles;
   // leave the state as the FP64 path leaves it: fresh ghosts, coarse levels
   // restricted from the finest (FillDown, afasroutines.f90:83)
-  if (H.wrap_all || finest == 0)
+  if (finest == 0)
     if ((r = enq_set_ghost(H, finest, 0))) return r;
-  if (H.wrap_all)
-    if ((r = enq_fill_down(H, 2, finest, minlevel))) return r;
   if (!conv && strict) return BSAMG_ERR_NOT_CONVERGED;
   return BSAMG_OK;
 }
