@@ -46,27 +46,32 @@ __device__ __forceinline__ int colour(int x, int y, int z) {
   return DIM == 3 ? (x + y + z + 1) & 1 : (x + y) & 1;
 }
 
-// Index of a cell and its six neighbours within the colour arrays.  own is
-// in the cell's colour array, the neighbours in the other colour's array.
+// A cell and its six neighbours as 32-bit indices into a colour-split array
+// of one variable, the colour offset included: own = c*half + row*hh + x/2,
+// the neighbours in the other colour's half.  A kernel forms one base
+// pointer per array and variable (fp + offset + v*2*half), the same for all
+// its threads, so that a load costs one address instruction.
 template <int DIM>
 struct Loc {
   int c;
-  int own, xm, xp, ym, yp, zm, zp;
+  unsigned own, xm, xp, ym, yp, zm, zp;
   __device__ __forceinline__ Loc(const BoxLev& L, int x, int y, int z) {
     c = colour<DIM>(x, y, z);
-    int h = x >> 1, b = x & 1, hh = L.hh, n1 = L.n[1];
-    int r = z * n1 + y;
-    own = r * hh + h;
-    int hxm = b ? h : (h ? h - 1 : hh - 1);
-    int hxp = b ? (h + 1 < hh ? h + 1 : 0) : h;
-    xm = r * hh + hxm;
-    xp = r * hh + hxp;
-    ym = (r - y + (y ? y - 1 : n1 - 1)) * hh + h;
-    yp = (r - y + (y + 1 < n1 ? y + 1 : 0)) * hh + h;
+    unsigned hh = (unsigned)L.hh, n1 = (unsigned)L.n[1], half = (unsigned)L.half;
+    unsigned h = (unsigned)x >> 1, b = (unsigned)x & 1u;
+    unsigned r = (unsigned)z * n1 + (unsigned)y;
+    unsigned on = c ? 0u : half;  // start of the other colour
+    own = (c ? half : 0u) + r * hh + h;
+    unsigned row = on + r * hh;
+    xm = row + (b ? h : (h ? h - 1 : hh - 1));
+    xp = row + (b ? (h + 1 < hh ? h + 1 : 0u) : h);
+    unsigned rz = r - (unsigned)y;  // z * n1
+    ym = on + (rz + (y ? (unsigned)y - 1 : n1 - 1)) * hh + h;
+    yp = on + (rz + ((unsigned)y + 1 < n1 ? (unsigned)y + 1 : 0u)) * hh + h;
     if (DIM == 3) {
-      int n2 = L.n[2];
-      zm = ((z ? z - 1 : n2 - 1) * n1 + y) * hh + h;
-      zp = ((z + 1 < n2 ? z + 1 : 0) * n1 + y) * hh + h;
+      unsigned n2 = (unsigned)L.n[2];
+      zm = on + ((z ? (unsigned)z - 1 : n2 - 1) * n1 + (unsigned)y) * hh + h;
+      zp = on + (((unsigned)z + 1 < n2 ? (unsigned)z + 1 : 0u) * n1 + (unsigned)y) * hh + h;
     } else {
       zm = zp = 0;
     }
@@ -80,22 +85,22 @@ __device__ __forceinline__ float nsum(const float* a, const Loc<DIM>& l) {
   return s;
 }
 
-// variable v, colour c of a two-variable colour-split array
-__device__ __forceinline__ float* arr(float* fp, long long off, long long half, int v, int c) {
-  return fp + off + (long long)(v * 2 + c) * half;
+// bases of variables 0 and 1 of a two-variable colour-split array
+struct V2 {
+  float* v0;
+  float* v1;
+};
+__device__ __forceinline__ V2 var2(float* fp, long long off, long long half) {
+  return {fp + off, fp + off + 2 * half};
 }
 
 // correction operator M(e) at a cell (see mixed.cu, mopn)
 template <int DIM>
-__device__ __forceinline__ void mop(float* fp, const BoxLev& L, const Loc<DIM>& l, float pb, float& m0, float& m1) {
-  const float* e0 = arr(fp, L.oe, L.half, 0, l.c);
-  const float* e1 = arr(fp, L.oe, L.half, 1, l.c);
-  const float* o0 = arr(fp, L.oe, L.half, 0, 1 - l.c);
-  const float* o1 = arr(fp, L.oe, L.half, 1, 1 - l.c);
-  float x = e0[l.own], y = e1[l.own];
-  float k = DIM == 2 ? 4.0f : 6.0f;
-  m0 = x - L.c0 * (nsum<DIM>(o1, l) - k * y);
-  m1 = y - x * (3.0f * pb * (pb + x) + x * x) + L.c1 * (nsum<DIM>(o0, l) - k * x);
+__device__ __forceinline__ void mop(V2 E, const BoxLev& L, const Loc<DIM>& l, float pb, float& m0, float& m1) {
+  float x = E.v0[l.own], y = E.v1[l.own];
+  const float k = DIM == 2 ? 4.0f : 6.0f;
+  m0 = x - L.c0 * (nsum<DIM>(E.v1, l) - k * y);
+  m1 = y - x * (3.0f * pb * (pb + x) + x * x) + L.c1 * (nsum<DIM>(E.v0, l) - k * x);
 }
 
 // ---------------------------------------------------------------------------
@@ -175,21 +180,39 @@ __device__ __forceinline__ double f2d(float f) {
   return (double)f;
 }
 
-// deterministic per-CTA sums of two values -> partial[2*cta], [2*cta+1]
-// (shared-memory tree: block sizes need not be a multiple of the warp size)
+// deterministic per-CTA sums of two values -> partial[2*cta], [2*cta+1]:
+// warp shuffles then one thread over the warp sums when the block is whole
+// warps, else a shared-memory tree
 __device__ __forceinline__ void cta_sum2(float s0, float s1, double* partial) {
   __shared__ float red[2][256];
   int t = threadIdx.y * blockDim.x + threadIdx.x;
   int nt = blockDim.x * blockDim.y;
-  red[0][t] = s0;
-  red[1][t] = s1;
-  __syncthreads();
-  for (int w = 128; w > 0; w >>= 1) {
-    if (t < w && t + w < nt) {
-      red[0][t] += red[0][t + w];
-      red[1][t] += red[1][t + w];
+  if ((nt & 31) == 0) {
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 += __shfl_down_sync(0xffffffffu, s0, o);
+      s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    }
+    if ((t & 31) == 0) {
+      red[0][t >> 5] = s0;
+      red[1][t >> 5] = s1;
     }
     __syncthreads();
+    if (t == 0)
+      for (int w = 1; w < (nt >> 5); w++) {
+        red[0][0] += red[0][w];
+        red[1][0] += red[1][w];
+      }
+  } else {
+    red[0][t] = s0;
+    red[1][t] = s1;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if (t < w && t + w < nt) {
+        red[0][t] += red[0][t + w];
+        red[1][t] += red[1][t + w];
+      }
+      __syncthreads();
+    }
   }
   if (t == 0) {
     long long cta = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
@@ -202,102 +225,98 @@ __device__ __forceinline__ void cta_sum2(float s0, float s1, double* partial) {
 // kernels.  Grid (x, y, z) = (position in a colour row or coarse x,
 // y, z); blockDim.z = 1.
 
-// Colour half-sweep of the correction smoother (RelaxGrid2D/3D in
-// correction form, see mixed.cu k_mx_relax).  first = 1: e of both colours
-// counts as zero (first half-sweep of a cycle); first = 2: the own colour's
-// e counts as zero (second half-sweep).
+// One cell of a colour half-sweep of the correction smoother (RelaxGrid2D/3D
+// in correction form, see mixed.cu k_mx_relax).  first = 1: e of both
+// colours counts as zero (first half-sweep of a cycle); first = 2: the own
+// colour's e counts as zero (second half-sweep).
 template <int DIM>
 __device__ __forceinline__ void relax_at(float* __restrict__ fp, const BoxLev& L, int c, int first, int h, int y,
                                          int z) {
+  V2 E = var2(fp, L.oe, L.half), G = var2(fp, L.og, L.half);
+  const float* PB = fp + L.opb;
   int x = 2 * h + ((c + y + z + (DIM == 3 ? 1 : 0)) & 1);
   Loc<DIM> l(L, x, y, z);
-  float* e0 = arr(fp, L.oe, L.half, 0, c);
-  float* e1 = arr(fp, L.oe, L.half, 1, c);
-  const float* g0 = arr(fp, L.og, L.half, 0, c);
-  const float* g1 = arr(fp, L.og, L.half, 1, c);
-  float pb = fp[L.opb + (long long)c * L.half + l.own];
+  float pb = PB[l.own];
   float s0 = 0.f, s1 = 0.f, xv = 0.f;
   if (first != 1) {
-    s0 = nsum<DIM>(arr(fp, L.oe, L.half, 0, 1 - c), l);
-    s1 = nsum<DIM>(arr(fp, L.oe, L.half, 1, 1 - c), l);
-    if (first == 0) xv = e0[l.own];
+    s0 = nsum<DIM>(E.v0, l);
+    s1 = nsum<DIM>(E.v1, l);
+    if (first == 0) xv = E.v0[l.own];
   }
   float w = pb + xv;
   float a21 = -3.0f * w * w - L.tmp3;
-  float b1 = g0[l.own] + L.c0 * s1;
-  float b2 = g1[l.own] - L.c1 * s0 - xv * xv * (3.0f * pb + 2.0f * xv);
+  float b1 = G.v0[l.own] + L.c0 * s1;
+  float b2 = G.v1[l.own] - L.c1 * s0 - xv * xv * (3.0f * pb + 2.0f * xv);
   float rdet = 1.0f / (1.0f - L.a12 * a21);
-  e0[l.own] = (b1 - L.a12 * b2) * rdet;
-  e1[l.own] = (b2 - a21 * b1) * rdet;
+  E.v0[l.own] = (b1 - L.a12 * b2) * rdet;
+  E.v1[l.own] = (b2 - a21 * b1) * rdet;
 }
+
 // Full-grid sweep: each thread takes position h of rows 2yp and 2yp+1 (n1
 // is even), loading both cells' data before either is stored so that twice
 // the loads are in flight per thread.
 template <int DIM>
-__global__ void __launch_bounds__(256) k_bx_relax(float* __restrict__ fp, BoxLev L, int c, int first) {
+__global__ void __launch_bounds__(256, 8) k_bx_relax(float* __restrict__ fp, BoxLev L, int c, int first) {
   int h = blockIdx.x * blockDim.x + threadIdx.x;
   int yp = blockIdx.y * blockDim.y + threadIdx.y;
   int z = blockIdx.z;
   if (h >= L.hh || 2 * yp >= L.n[1]) return;
-  float* e0 = arr(fp, L.oe, L.half, 0, c);
-  float* e1 = arr(fp, L.oe, L.half, 1, c);
-  const float* g0 = arr(fp, L.og, L.half, 0, c);
-  const float* g1 = arr(fp, L.og, L.half, 1, c);
-  const float* o0 = arr(fp, L.oe, L.half, 0, 1 - c);
-  const float* o1 = arr(fp, L.oe, L.half, 1, 1 - c);
-  const float* pbc = fp + L.opb + (long long)c * L.half;
-  int own[2];
-  float pb[2], xv[2], s0[2], s1[2], b1[2], gg1[2];
+  V2 E = var2(fp, L.oe, L.half), G = var2(fp, L.og, L.half);
+  const float* PB = fp + L.opb;
+  unsigned own[2];
+  float pb[2], xv[2], s0[2], s1[2], g0[2], g1[2];
   for (int k = 0; k < 2; k++) {
     int y = 2 * yp + k;
     int x = 2 * h + ((c + y + z + (DIM == 3 ? 1 : 0)) & 1);
     Loc<DIM> l(L, x, y, z);
     own[k] = l.own;
-    pb[k] = pbc[l.own];
+    pb[k] = PB[l.own];
     s0[k] = s1[k] = xv[k] = 0.f;
     if (first != 1) {
-      s0[k] = nsum<DIM>(o0, l);
-      s1[k] = nsum<DIM>(o1, l);
-      if (first == 0) xv[k] = e0[l.own];
+      s0[k] = nsum<DIM>(E.v0, l);
+      s1[k] = nsum<DIM>(E.v1, l);
+      if (first == 0) xv[k] = E.v0[l.own];
     }
-    b1[k] = g0[l.own];
-    gg1[k] = g1[l.own];
+    g0[k] = G.v0[l.own];
+    g1[k] = G.v1[l.own];
   }
   for (int k = 0; k < 2; k++) {
     float w = pb[k] + xv[k];
     float a21 = -3.0f * w * w - L.tmp3;
-    float bb1 = b1[k] + L.c0 * s1[k];
-    float bb2 = gg1[k] - L.c1 * s0[k] - xv[k] * xv[k] * (3.0f * pb[k] + 2.0f * xv[k]);
+    float b1 = g0[k] + L.c0 * s1[k];
+    float b2 = g1[k] - L.c1 * s0[k] - xv[k] * xv[k] * (3.0f * pb[k] + 2.0f * xv[k]);
     float rdet = 1.0f / (1.0f - L.a12 * a21);
-    e0[own[k]] = (bb1 - L.a12 * bb2) * rdet;
-    e1[own[k]] = (bb2 - a21 * bb1) * rdet;
+    E.v0[own[k]] = (b1 - L.a12 * b2) * rdet;
+    E.v1[own[k]] = (b2 - a21 * b1) * rdet;
   }
 }
 
 // RestrictSolution on e and on the base field: coarse e = ec = R(e_fine),
-// coarse pb = R(pb_fine); one thread per coarse cell
+// coarse pb = R(pb_fine); one coarse cell
 template <int DIM>
 __device__ __forceinline__ void restrict_at(float* __restrict__ fp, const BoxLev& F, const BoxLev& C, int X, int Y,
                                             int Z) {
-  Loc<DIM> lc(C, X, Y, Z);
+  V2 Ef = var2(fp, F.oe, F.half);
+  const float* PBf = fp + F.opb;
   float s[3] = {0.f, 0.f, 0.f};
   const int nz = DIM == 3 ? 2 : 1;
   for (int dz = 0; dz < nz; dz++)
     for (int dy = 0; dy < 2; dy++) {
-      int y = 2 * Y + dy, z = DIM == 3 ? 2 * Z + dz : 0;
-      int r = (z * F.n[1] + y) * F.hh + X;  // both fine cells of the row sit at x/2 = X
+      unsigned y = 2 * Y + dy, z = DIM == 3 ? 2 * Z + dz : 0;
+      unsigned r = (z * (unsigned)F.n[1] + y) * (unsigned)F.hh + (unsigned)X;  // both fine cells sit at x/2 = X
       for (int c = 0; c < 2; c++) {
-        s[0] += arr(fp, F.oe, F.half, 0, c)[r];
-        s[1] += arr(fp, F.oe, F.half, 1, c)[r];
-        s[2] += fp[F.opb + (long long)c * F.half + r];
+        unsigned i = r + (c ? (unsigned)F.half : 0u);
+        s[0] += Ef.v0[i];
+        s[1] += Ef.v1[i];
+        s[2] += PBf[i];
       }
     }
   const float w = DIM == 2 ? 0.25f : 0.125f;
-  for (int v = 0; v < 2; v++) {
-    arr(fp, C.oe, C.half, v, lc.c)[lc.own] = s[v] * w;
-    arr(fp, C.oec, C.half, v, lc.c)[lc.own] = s[v] * w;
-  }
-  fp[C.opb + (long long)lc.c * C.half + lc.own] = s[2] * w;
+  Loc<DIM> lc(C, X, Y, Z);
+  V2 Ec = var2(fp, C.oe, C.half), ECc = var2(fp, C.oec, C.half);
+  Ec.v0[lc.own] = ECc.v0[lc.own] = s[0] * w;
+  Ec.v1[lc.own] = ECc.v1[lc.own] = s[1] * w;
+  fp[C.opb + lc.own] = s[2] * w;
 }
 template <int DIM>
 __global__ void __launch_bounds__(256) k_bx_restrict(float* __restrict__ fp, BoxLev F, BoxLev C) {
@@ -310,28 +329,27 @@ __global__ void __launch_bounds__(256) k_bx_restrict(float* __restrict__ fp, Box
 template <int DIM>
 __device__ __forceinline__ void coarse_load_at(float* __restrict__ fp, const BoxLev& F, const BoxLev& C, int X, int Y,
                                                int Z) {
+  V2 Ef = var2(fp, F.oe, F.half), Gf = var2(fp, F.og, F.half);
+  const float* PBf = fp + F.opb;
   float R0 = 0.f, R1 = 0.f;
   const int nz = DIM == 3 ? 2 : 1;
   for (int dz = 0; dz < nz; dz++)
     for (int dy = 0; dy < 2; dy++)
       for (int dx = 0; dx < 2; dx++) {
         Loc<DIM> l(F, 2 * X + dx, 2 * Y + dy, DIM == 3 ? 2 * Z + dz : 0);
-        float pb = fp[F.opb + (long long)l.c * F.half + l.own];
         float m0, m1;
-        mop<DIM>(fp, F, l, pb, m0, m1);
-        R0 += arr(fp, F.og, F.half, 0, l.c)[l.own] - m0;
-        R1 += arr(fp, F.og, F.half, 1, l.c)[l.own] - m1;
+        mop<DIM>(Ef, F, l, PBf[l.own], m0, m1);
+        R0 += Gf.v0[l.own] - m0;
+        R1 += Gf.v1[l.own] - m1;
       }
   const float w = DIM == 2 ? 0.25f : 0.125f;
   Loc<DIM> lc(C, X, Y, Z);
   // M_c(ec): the coarse operator on the restricted correction
-  BoxLev Cec = C;
-  Cec.oe = C.oec;
-  float pbc = fp[C.opb + (long long)lc.c * C.half + lc.own];
+  V2 ECc = var2(fp, C.oec, C.half), Gc = var2(fp, C.og, C.half);
   float m0, m1;
-  mop<DIM>(fp, Cec, lc, pbc, m0, m1);
-  arr(fp, C.og, C.half, 0, lc.c)[lc.own] = R0 * w + m0;
-  arr(fp, C.og, C.half, 1, lc.c)[lc.own] = R1 * w + m1;
+  mop<DIM>(ECc, C, lc, fp[C.opb + lc.own], m0, m1);
+  Gc.v0[lc.own] = R0 * w + m0;
+  Gc.v1[lc.own] = R1 * w + m1;
 }
 template <int DIM>
 __global__ void __launch_bounds__(256) k_bx_coarse_load(float* __restrict__ fp, BoxLev F, BoxLev C) {
@@ -357,29 +375,29 @@ __device__ __forceinline__ void prolong_at(float* __restrict__ fp, const BoxLev&
     fx[1][d] = 2 * T[d];
   }
   constexpr int NZ = DIM == 3 ? 2 : 1;
+  V2 Ec = var2(fp, C.oe, C.half), ECc = var2(fp, C.oec, C.half), Ef = var2(fp, F.oe, F.half);
   // corrections e_c - ec at the 2x2(x2) coarse corners, both variables
   float a[2][NZ][2][2];
   for (int dz = 0; dz < NZ; dz++)
     for (int dy = 0; dy < 2; dy++)
       for (int dx = 0; dx < 2; dx++) {
         Loc<DIM> l(C, cx[dx][0], cx[dy][1], DIM == 3 ? cx[dz][2] : 0);
-        for (int v = 0; v < 2; v++)
-          a[v][dz][dy][dx] = arr(fp, C.oe, C.half, v, l.c)[l.own] - arr(fp, C.oec, C.half, v, l.c)[l.own];
+        a[0][dz][dy][dx] = Ec.v0[l.own] - ECc.v0[l.own];
+        a[1][dz][dy][dx] = Ec.v1[l.own] - ECc.v1[l.own];
       }
   // weight 3/4 on the near coarse cell (f = 0: the first, f = 1: the second)
   auto w1 = [](float lo, float hi, int f) { return f == 0 ? 3.0f * lo + hi : lo + 3.0f * hi; };
   // every fine value is loaded before the first store, so the loads of one
   // thread are in flight together (a store to fp could alias a later load)
   constexpr int NF = 4 * NZ;
-  float* dst[NF][2];
+  unsigned own[NF];
   float val[NF][2];
   for (int m = 0; m < NF; m++) {
     int fxi = m & 1, fy = (m >> 1) & 1, fz = m >> 2;
     Loc<DIM> l(F, fx[fxi][0], fx[fy][1], DIM == 3 ? fx[fz][2] : 0);
-    for (int v = 0; v < 2; v++) {
-      dst[m][v] = arr(fp, F.oe, F.half, v, l.c) + l.own;
-      val[m][v] = *dst[m][v];
-    }
+    own[m] = l.own;
+    val[m][0] = Ef.v0[l.own];
+    val[m][1] = Ef.v1[l.own];
   }
   for (int m = 0; m < NF; m++) {
     int fxi = m & 1, fy = (m >> 1) & 1, fz = m >> 2;
@@ -396,8 +414,10 @@ __device__ __forceinline__ void prolong_at(float* __restrict__ fp, const BoxLev&
       val[m][v] += add;
     }
   }
-  for (int m = 0; m < NF; m++)
-    for (int v = 0; v < 2; v++) *dst[m][v] = val[m][v];
+  for (int m = 0; m < NF; m++) {
+    Ef.v0[own[m]] = val[m][0];
+    Ef.v1[own[m]] = val[m][1];
+  }
 }
 template <int DIM>
 __global__ void __launch_bounds__(256) k_bx_prolong(float* __restrict__ fp, BoxLev F, BoxLev C) {
@@ -474,29 +494,26 @@ __global__ void __launch_bounds__(256) k_bx_track_update(float* __restrict__ fp,
   int z = blockIdx.z;
   float s0 = 0.f, s1 = 0.f;
   if (x < L.n[0] && y < L.n[1]) {
+    V2 E = var2(fp, L.oe, L.half), G = var2(fp, L.og, L.half);
+    V2 QH = var2(fp, L.opb, L.half), QL = var2(fp, oqlo, L.half);  // the base field is qhi(phi)
     Loc<DIM> l(L, x, y, z);
-    float* qh0 = arr(fp, L.opb, L.half, 0, l.c) + l.own;  // the base field is qhi(phi)
-    float* qh1 = arr(fp, L.opb, L.half, 1, l.c) + l.own;
-    float* ql0 = arr(fp, oqlo, L.half, 0, l.c) + l.own;
-    float* ql1 = arr(fp, oqlo, L.half, 1, l.c) + l.own;
-    float* g0 = arr(fp, L.og, L.half, 0, l.c) + l.own;
-    float* g1 = arr(fp, L.og, L.half, 1, l.c) + l.own;
-    float h0 = *qh0, h1 = *qh1, lo0 = *ql0, lo1 = *ql1, a0 = *g0, a1 = *g1;
-    float e0 = arr(fp, L.oe, L.half, 0, l.c)[l.own], e1 = arr(fp, L.oe, L.half, 1, l.c)[l.own];
+    unsigned i = l.own;
+    float h0 = QH.v0[i], h1 = QH.v1[i], lo0 = QL.v0[i], lo1 = QL.v1[i], a0 = G.v0[i], a1 = G.v1[i];
+    float e0 = E.v0[i], e1 = E.v1[i];
     float m0, m1;
-    mop<DIM>(fp, L, l, h0, m0, m1);
+    mop<DIM>(E, L, l, h0, m0, m1);
     a0 -= m0;
     a1 -= m1;
     DF t0 = two_sum(h0, e0);
     t0 = fast_two_sum(t0.h, t0.l + lo0);
     DF t1 = two_sum(h1, e1);
     t1 = fast_two_sum(t1.h, t1.l + lo1);
-    *g0 = a0;
-    *g1 = a1;
-    *qh0 = t0.h;
-    *ql0 = t0.l;
-    *qh1 = t1.h;
-    *ql1 = t1.l;
+    G.v0[i] = a0;
+    G.v1[i] = a1;
+    QH.v0[i] = t0.h;
+    QL.v0[i] = t0.l;
+    QH.v1[i] = t1.h;
+    QL.v1[i] = t1.l;
     s0 = a0 * a0;
     s1 = a1 * a1;
   }
@@ -515,19 +532,17 @@ __global__ void __launch_bounds__(256) k_bx_resid(float* __restrict__ fp, BoxLev
   float s0 = 0.f, s1 = 0.f;
   if (x < L.n[0] && y < L.n[1]) {
     const DF c0 = {L.c0h, L.c0l}, c1 = {L.c1h, L.c1l};
+    V2 QH = var2(fp, L.opb, L.half), QL = var2(fp, oqlo, L.half), G = var2(fp, L.og, L.half);
     Loc<DIM> l(L, x, y, z);
-    const int o = 1 - l.c;
-    const int nbi[6] = {l.xm, l.xp, l.ym, l.yp, l.zm, l.zp};
+    const unsigned nbi[6] = {l.xm, l.xp, l.ym, l.yp, l.zm, l.zp};
     DF v[2], nb[2][6];
     for (int q = 0; q < 2; q++) {
-      const float* hi = arr(fp, L.opb, L.half, q, l.c);
-      const float* lo = arr(fp, oqlo, L.half, q, l.c);
+      const float* hi = q ? QH.v1 : QH.v0;
+      const float* lo = q ? QL.v1 : QL.v0;
       v[q] = {hi[l.own], lo[l.own]};
-      const float* ho = arr(fp, L.opb, L.half, q, o);
-      const float* lo2 = arr(fp, oqlo, L.half, q, o);
-      for (int m = 0; m < 2 * DIM; m++) nb[q][m] = {ho[nbi[m]], lo2[nbi[m]]};
+      for (int m = 0; m < 2 * DIM; m++) nb[q][m] = {hi[nbi[m]], lo[nbi[m]]};
     }
-    DF f1 = {fp[ofhi + (long long)l.c * L.half + l.own], fp[oflo + (long long)l.c * L.half + l.own]};
+    DF f1 = {fp[ofhi + l.own], fp[oflo + l.own]};
     DF lphi = df_lap<DIM>(nb[0], v[0]);
     DF lmu = df_lap<DIM>(nb[1], v[1]);
     // r1 = f1 - (phi - c0 lap(mu)); r2 = -f1 - (mu - phi^3 + c1 lap(phi))
@@ -535,8 +550,8 @@ __global__ void __launch_bounds__(256) k_bx_resid(float* __restrict__ fp, BoxLev
     DF p3 = df_mul(df_mul(v[0], v[0]), v[0]);
     DF r2 = df_add(df_add(df_neg(df_add(f1, v[1])), p3), df_neg(df_mul(c1, lphi)));
     float a0 = r1.h + r1.l, a1 = r2.h + r2.l;
-    arr(fp, L.og, L.half, 0, l.c)[l.own] = a0;
-    arr(fp, L.og, L.half, 1, l.c)[l.own] = a1;
+    G.v0[l.own] = a0;
+    G.v1[l.own] = a1;
     s0 = a0 * a0;
     s1 = a1 * a1;
   }
@@ -544,7 +559,7 @@ __global__ void __launch_bounds__(256) k_bx_resid(float* __restrict__ fp, BoxLev
 }
 
 // FP64 q (ghosted Fortran layout) -> qhi/qlo, and f = (phi_old, -phi_old) as
-// fhi/flo, on the finest level
+// fhi/flo, on the finest level; two cells (x = 2h, 2h+1) per thread
 template <int DIM>
 __global__ void __launch_bounds__(256) k_bx_split(const double* __restrict__ pool, long long oq, long long oqold,
                                                   long long sq, int qn0, int qn1, float* __restrict__ fp, BoxLev L,
@@ -560,35 +575,36 @@ __global__ void __launch_bounds__(256) k_bx_split(const double* __restrict__ poo
     in[b][1] = pool[oq + sq + g + b];
     in[b][2] = pool[oqold + g + b];
   }
+  V2 QH = var2(fp, L.opb, L.half), QL = var2(fp, oqlo, L.half);
   for (int b = 0; b < 2; b++) {
     Loc<DIM> l(L, 2 * h + b, y, z);
-    for (int v = 0; v < 2; v++) {
-      DF s = split64(in[b][v]);
-      arr(fp, L.opb, L.half, v, l.c)[l.own] = s.h;
-      arr(fp, oqlo, L.half, v, l.c)[l.own] = s.l;
-    }
-    DF f = split64(in[b][2]);
-    fp[ofhi + (long long)l.c * L.half + l.own] = f.h;
-    fp[oflo + (long long)l.c * L.half + l.own] = f.l;
+    DF s0 = split64(in[b][0]), s1 = split64(in[b][1]), f = split64(in[b][2]);
+    QH.v0[l.own] = s0.h;
+    QL.v0[l.own] = s0.l;
+    QH.v1[l.own] = s1.h;
+    QL.v1[l.own] = s1.l;
+    fp[ofhi + l.own] = f.h;
+    fp[oflo + l.own] = f.l;
   }
 }
 
 // qhi + qlo -> FP64 q (interior of the finest level)
 template <int DIM>
 __global__ void __launch_bounds__(256) k_bx_merge(double* __restrict__ pool, long long oq, long long sq, int qn0,
-                                                  int qn1, const float* __restrict__ fp, BoxLev L, long long oqlo) {
+                                                  int qn1, float* __restrict__ fp, BoxLev L, long long oqlo) {
   int h = blockIdx.x * blockDim.x + threadIdx.x;
   int y = blockIdx.y * blockDim.y + threadIdx.y;
   int z = blockIdx.z;
   if (h >= L.hh || y >= L.n[1]) return;
   long long g = (2 * h + 1) + (long long)(y + 1) * qn0 + (DIM == 3 ? (long long)(z + 1) * qn0 * qn1 : 0);
+  V2 QH = var2(fp, L.opb, L.half), QL = var2(fp, oqlo, L.half);
   float hi[2][2], lo[2][2];  // loaded before any store
   for (int b = 0; b < 2; b++) {
     Loc<DIM> l(L, 2 * h + b, y, z);
-    for (int v = 0; v < 2; v++) {
-      hi[b][v] = fp[L.opb + (long long)(v * 2 + l.c) * L.half + l.own];
-      lo[b][v] = fp[oqlo + (long long)(v * 2 + l.c) * L.half + l.own];
-    }
+    hi[b][0] = QH.v0[l.own];
+    hi[b][1] = QH.v1[l.own];
+    lo[b][0] = QL.v0[l.own];
+    lo[b][1] = QL.v1[l.own];
   }
   for (int b = 0; b < 2; b++)
     for (int v = 0; v < 2; v++) pool[oq + v * sq + g + b] = f2d(hi[b][v]) + f2d(lo[b][v]);
@@ -695,6 +711,8 @@ bool box_eligible(const Hier& H, bool periodic_single) {
       if (P.mx[d] % 2) return false;
       if (l > H.minlevel && P.mx[d] != 2 * H.patches[P.parent].mx[d]) return false;
     }
+    // cell indices (both colours) are 32-bit
+    if ((long long)P.mx[0] * P.mx[1] * P.mx[2] >= (1LL << 31)) return false;
   }
   return true;
 }
