@@ -30,6 +30,51 @@ class BsamgError(RuntimeError):
         self.status = status
 
 
+class RegridParams(ctypes.Structure):
+    """bsamg_regrid_params (include/bsamg.h)."""
+    _fields_ = [("maxlevel", ctypes.c_int), ("tagging", ctypes.c_int), ("initial", ctypes.c_int),
+                ("maxside", ctypes.c_int), ("first_id", ctypes.c_int), ("ibuffer", ctypes.c_int * 11),
+                ("minimumgridpoints", ctypes.c_int * 11), ("qtolerance", ctypes.c_double * 11),
+                ("desiredfillratio", ctypes.c_double * 11)]
+
+
+TAGGING = {"ch": 0, "gradient": 1}
+# bsamg_qinit_fn: (user, level, mx[3], dx[3], xlower[3], q)
+QINIT = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                         ctypes.POINTER(ctypes.c_double))
+
+
+def regrid_params(maxlevel, tagging="ch", initial=False, maxside=0, first_id=1000, ibuffer=1,
+                  minimumgridpoints=4, qtolerance=1e-2, desiredfillratio=0.9):
+    """bsamg_regrid_params; scalars apply to every level, lists per level
+    (the griddata namelist entries of the reference)."""
+    r = RegridParams()
+    r.maxlevel, r.tagging, r.initial, r.maxside, r.first_id = (maxlevel, TAGGING[tagging], int(initial), maxside,
+                                                              first_id)
+    per = lambda x, l: x[l] if isinstance(x, (list, tuple)) else x
+    for l in range(11):
+        r.ibuffer[l] = per(ibuffer, l)
+        r.minimumgridpoints[l] = per(minimumgridpoints, l)
+        r.qtolerance[l] = per(qtolerance, l)
+        r.desiredfillratio[l] = per(desiredfillratio, l)
+    return r
+
+
+def qinit_callback(fn, ndims, nrvars):
+    """bsamg_qinit_fn around fn(level, mx, dx, xlower) -> the new patch's
+    ghosted Fortran-layout array (only its interior is used)."""
+    def cb(user, level, mx, dx, xl, q):
+        m = [mx[d] for d in range(ndims)]
+        a = np.asarray(fn(level, m, [dx[d] for d in range(ndims)], [xl[d] for d in range(ndims)]),
+                       dtype=np.float64).ravel(order="F")
+        n = int(np.prod([v + 2 for v in m])) * nrvars
+        if a.size != n:
+            raise ValueError(f"qinit returned {a.size} values for a patch of {n}")
+        ctypes.memmove(q, a.ctypes.data, n * 8)
+    return QINIT(cb)
+
+
 def lib():
     """Load libbsamg.so (built by __graft_entry__.build()); fail loudly if absent."""
     global _lib
@@ -50,6 +95,8 @@ def lib():
         "bsamg_build_uniform": ([P, IP, I, IP, DP, DP], I),
         "bsamg_commit": ([P], I),
         "bsamg_num_patches": ([P, IP], I),
+        "bsamg_patch_info": ([P, I, IP, DP], I),
+        "bsamg_regrid": ([P, ctypes.POINTER(RegridParams), QINIT, P, ctypes.POINTER(P)], I),
         "bsamg_field_size": ([P, I, I], SZ),
         "bsamg_put_field": ([P, I, I, DP, SZ], I),
         "bsamg_get_field": ([P, I, I, DP, SZ], I),
@@ -153,6 +200,31 @@ class Hierarchy:
     def build_uniform(self, mx, minlevel, mthbc, xlower, xupper):
         _ck(lib().bsamg_build_uniform(self.h, _ia(mx, 3), minlevel, _ia(mthbc, 6), _da(xlower, 3),
                                       _da(xupper, 3)), "bsamg_build_uniform")
+
+    def patch_table(self):
+        """Geometry of every patch in visiting order (bsamg_patch_info)."""
+        L = lib()
+        n = ctypes.c_int()
+        _ck(L.bsamg_num_patches(self.h, ctypes.byref(n)), "bsamg_num_patches")
+        out = []
+        for i in range(n.value):
+            a = (ctypes.c_int * 24)()
+            d = (ctypes.c_double * 6)()
+            _ck(L.bsamg_patch_info(self.h, i, a, d), "bsamg_patch_info")
+            a = list(a)
+            out.append(dict(level=a[0], id=a[1], parent_id=a[2], mx=a[3:6], mglobal=a[6:12], mbounds=a[12:18],
+                            mthbc=a[18:24], dx=list(d)[0:3], xlower=list(d)[3:6]))
+        return out
+
+    def regrid(self, params, qinit=None):
+        """AMR regrid (bsamg_regrid): a new Hierarchy on the same context;
+        this one is unchanged."""
+        cb = qinit_callback(qinit, self.ndims, self.nrvars) if qinit is not None else QINIT()
+        h = ctypes.c_void_p()
+        _ck(lib().bsamg_regrid(self.h, ctypes.byref(params), cb, None, ctypes.byref(h)), "bsamg_regrid")
+        new = Hierarchy.__new__(Hierarchy)
+        new.ctx, new.ndims, new.nrvars, new.h = self.ctx, self.ndims, self.nrvars, h
+        return new
 
     def commit(self):
         _ck(lib().bsamg_commit(self.h), "bsamg_commit")

@@ -23,6 +23,7 @@ UNITS = {
     "box.cu": [],
     "hier.cu": [],
     "ghostc.cpp": [],
+    "regrid.cpp": [],
 }
 
 

@@ -219,6 +219,86 @@ void coefficients(const Hier& H, double h, double* c) {
   }
 }
 
+// PeriodicSetup, boundary.f90:805-872
+void periodic_setup(Hier& H, const int* mthbc) {
+  int m[6];
+  for (int f = 0; f < 6; f++) m[f] = f < 2 * H.ndims ? mthbc[f] : 10;
+  static const int i13[13] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13};
+  static const int i1245[4] = {1, 2, 4, 5}, i1389[4] = {1, 3, 8, 9}, i2367[4] = {2, 3, 6, 7};
+  static const int i1[1] = {1}, i2[1] = {2}, i3[1] = {3};
+  const int* src = nullptr;
+  int n = 0;
+  H.periodic = 1;
+  if (m[0] == 2) {
+    if (m[2] == 2) {
+      if (m[4] == 2) { src = i13; n = 13; } else { src = i1245; n = 4; }
+    } else {
+      if (m[4] == 2) { src = i1389; n = 4; } else { src = i1; n = 1; }
+    }
+  } else {
+    if (m[2] == 2) {
+      if (m[4] == 2) { src = i2367; n = 4; } else { src = i2; n = 1; }
+    } else {
+      if (m[4] == 2) { src = i3; n = 1; } else { H.periodic = 0; }
+    }
+  }
+  H.nperoff = n;
+  for (int i = 0; i < n; i++) H.peroffidx[i] = src[i];
+}
+
+// Host tables of a hierarchy (no device work): parent links, extents,
+// validation, level lists, periodic offsets.  commit() runs it first; the
+// regrid runs it on host-only hierarchies to compile their ghost programs.
+int build_tables(Hier& H) {
+  int root = -1;
+  H.minlevel = 0;
+  H.maxlevel = 0;
+  for (size_t n = 0; n < H.patches.size(); n++) {
+    HostPatch& P = H.patches[n];
+    if (P.level == 0 && root < 0) root = (int)n;
+    H.minlevel = std::min(H.minlevel, P.level);
+    H.maxlevel = std::max(H.maxlevel, P.level);
+  }
+  if (root < 0) return BSAMG_ERR_ARG;
+  for (HostPatch& P : H.patches) {
+    if (P.parent_id >= 0) {
+      auto it = H.id2idx.find(P.parent_id);
+      if (it == H.id2idx.end()) return BSAMG_ERR_NOT_FOUND;
+      if (H.patches[it->second].level != P.level - 1) return BSAMG_ERR_ARG;
+      P.parent = it->second;
+    }
+    if (P.level > H.minlevel && P.parent < 0) return BSAMG_ERR_ARG;
+    for (int d = 0; d < H.ndims; d++)  // RootInit's check, bsamroutines.f90:361-366
+      if (P.mglobal[d][1] - P.mglobal[d][0] + 1 != P.mx[d]) return BSAMG_ERR_ARG;
+    for (int f = 0; f < 2 * H.ndims; f++)
+      if (P.mthbc[f] != 2 && P.mthbc[f] != 10 && P.mthbc[f] != kInternalBC) return BSAMG_ERR_UNSUPPORTED;
+    for (int d = 0; d < 3; d++) {
+      bool u = d < H.ndims;
+      P.cmx[d] = (u && P.mx[d] % 2 == 0) ? P.mx[d] / 2 : 1;
+      P.qn[d] = u ? P.mx[d] + 2 * H.mbc : 1;
+      P.cn[d] = u ? P.cmx[d] + 2 * H.mbc : 1;
+    }
+    if (P.parent >= 0) {
+      for (int d = 0; d < H.ndims; d++) {
+        if (P.mx[d] % 2) return BSAMG_ERR_ARG;
+        const HostPatch& Q = H.patches[P.parent];
+        if (P.mbounds[d][0] < 1 || P.mbounds[d][1] > Q.mx[d] || P.mbounds[d][1] - P.mbounds[d][0] + 1 != P.cmx[d])
+          return BSAMG_ERR_ARG;
+      }
+    }
+    if (P.level > 0 && P.parent >= 0)
+      for (int d = 0; d < H.ndims; d++)
+        if (P.mx[d] < 4) return BSAMG_ERR_UNSUPPORTED;  // Interpolate2D/3D read cells 1..2 from each side
+  }
+  // level lists in insertion (visiting) order
+  for (size_t n = 0; n < H.patches.size(); n++) H.L(H.patches[n].level).patches.push_back((int)n);
+  const HostPatch& R = H.patches[root];
+  for (int l = 0; l <= kMaxDepth; l++)
+    for (int d = 0; d < 3; d++) H.mxmax[l][d] = d < H.ndims ? (R.mx[d] << l) : 1;
+  periodic_setup(H, R.mthbc);
+  return BSAMG_OK;
+}
+
 }  // namespace bsamg
 
 namespace {
@@ -330,32 +410,6 @@ int build_uniform(Hier& H, const int mx[3], int minlevel, const int mthbc[6], co
   return BSAMG_OK;
 }
 
-// PeriodicSetup, boundary.f90:805-872
-void periodic_setup(Hier& H, const int* mthbc) {
-  int m[6];
-  for (int f = 0; f < 6; f++) m[f] = f < 2 * H.ndims ? mthbc[f] : 10;
-  static const int i13[13] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13};
-  static const int i1245[4] = {1, 2, 4, 5}, i1389[4] = {1, 3, 8, 9}, i2367[4] = {2, 3, 6, 7};
-  static const int i1[1] = {1}, i2[1] = {2}, i3[1] = {3};
-  const int* src = nullptr;
-  int n = 0;
-  H.periodic = 1;
-  if (m[0] == 2) {
-    if (m[2] == 2) {
-      if (m[4] == 2) { src = i13; n = 13; } else { src = i1245; n = 4; }
-    } else {
-      if (m[4] == 2) { src = i1389; n = 4; } else { src = i1; n = 1; }
-    }
-  } else {
-    if (m[2] == 2) {
-      if (m[4] == 2) { src = i2367; n = 4; } else { src = i2; n = 1; }
-    } else {
-      if (m[4] == 2) { src = i3; n = 1; } else { H.periodic = 0; }
-    }
-  }
-  H.nperoff = n;
-  for (int i = 0; i < n; i++) H.peroffidx[i] = src[i];
-}
 
 
 int upload_blocks(Hier& H, LevelT& L, int kind) {
@@ -449,52 +503,7 @@ void pinned_slot_give(Hier& H) {
 int commit(Hier& H) {
   if (H.committed) return BSAMG_ERR_ARG;
   RET(set_device(H));
-  int root = -1;
-  H.minlevel = 0;
-  H.maxlevel = 0;
-  for (size_t n = 0; n < H.patches.size(); n++) {
-    HostPatch& P = H.patches[n];
-    if (P.level == 0 && root < 0) root = (int)n;
-    H.minlevel = std::min(H.minlevel, P.level);
-    H.maxlevel = std::max(H.maxlevel, P.level);
-  }
-  if (root < 0) return BSAMG_ERR_ARG;
-  for (HostPatch& P : H.patches) {
-    if (P.parent_id >= 0) {
-      auto it = H.id2idx.find(P.parent_id);
-      if (it == H.id2idx.end()) return BSAMG_ERR_NOT_FOUND;
-      if (H.patches[it->second].level != P.level - 1) return BSAMG_ERR_ARG;
-      P.parent = it->second;
-    }
-    if (P.level > H.minlevel && P.parent < 0) return BSAMG_ERR_ARG;
-    for (int d = 0; d < H.ndims; d++)  // RootInit's check, bsamroutines.f90:361-366
-      if (P.mglobal[d][1] - P.mglobal[d][0] + 1 != P.mx[d]) return BSAMG_ERR_ARG;
-    for (int f = 0; f < 2 * H.ndims; f++)
-      if (P.mthbc[f] != 2 && P.mthbc[f] != 10 && P.mthbc[f] != kInternalBC) return BSAMG_ERR_UNSUPPORTED;
-    for (int d = 0; d < 3; d++) {
-      bool u = d < H.ndims;
-      P.cmx[d] = (u && P.mx[d] % 2 == 0) ? P.mx[d] / 2 : 1;
-      P.qn[d] = u ? P.mx[d] + 2 * H.mbc : 1;
-      P.cn[d] = u ? P.cmx[d] + 2 * H.mbc : 1;
-    }
-    if (P.parent >= 0) {
-      for (int d = 0; d < H.ndims; d++) {
-        if (P.mx[d] % 2) return BSAMG_ERR_ARG;
-        const HostPatch& Q = H.patches[P.parent];
-        if (P.mbounds[d][0] < 1 || P.mbounds[d][1] > Q.mx[d] || P.mbounds[d][1] - P.mbounds[d][0] + 1 != P.cmx[d])
-          return BSAMG_ERR_ARG;
-      }
-    }
-    if (P.level > 0 && P.parent >= 0)
-      for (int d = 0; d < H.ndims; d++)
-        if (P.mx[d] < 4) return BSAMG_ERR_UNSUPPORTED;  // Interpolate2D/3D read cells 1..2 from each side
-  }
-  // level lists in insertion (visiting) order
-  for (size_t n = 0; n < H.patches.size(); n++) H.L(H.patches[n].level).patches.push_back((int)n);
-  const HostPatch& R = H.patches[root];
-  for (int l = 0; l <= kMaxDepth; l++)
-    for (int d = 0; d < 3; d++) H.mxmax[l][d] = d < H.ndims ? (R.mx[d] << l) : 1;
-  periodic_setup(H, R.mthbc);
+  RET(build_tables(H));
   {
     bool w = true;
     for (int l = H.minlevel; l <= H.maxlevel; l++) w = w && H.L(l).patches.size() == 1;
@@ -710,6 +719,7 @@ int bsamg_hier_create(bsamg_ctx* ctx, int ndims, int nrvars, int mbc, int proble
   h->nrvars = nrvars;
   h->mbc = mbc;
   h->problem = problem_kind;
+  h->params.assign(params, params + nparams);
   h->pp.dt = params[0];
   h->pp.eps2 = params[1] * params[1];  // SetProb, CH/problem.f90:32
   h->pp.gamma = nparams > 2 ? params[2] : 0.0;
@@ -720,6 +730,11 @@ int bsamg_hier_create(bsamg_ctx* ctx, int ndims, int nrvars, int mbc, int proble
   h->pp.problem = problem_kind;
   *out = h;
   return BSAMG_OK;
+}
+
+int bsamg_regrid(bsamg_hier* h, const bsamg_regrid_params* prm, bsamg_qinit_fn qinit, void* user, bsamg_hier** out) {
+  if (!h || !prm || !out) return BSAMG_ERR_ARG;
+  return regrid(*h, *prm, qinit, user, out);
 }
 
 int bsamg_hier_destroy(bsamg_hier* h) {
@@ -749,6 +764,25 @@ int bsamg_commit(bsamg_hier* h) {
 int bsamg_num_patches(const bsamg_hier* h, int* n) {
   if (!h || !n) return BSAMG_ERR_ARG;
   *n = (int)h->patches.size();
+  return BSAMG_OK;
+}
+
+int bsamg_patch_info(const bsamg_hier* h, int index, int* out, double* dxl) {
+  if (!h || !out || !dxl || index < 0 || index >= (int)h->patches.size()) return BSAMG_ERR_ARG;
+  const HostPatch& P = h->patches[index];
+  out[0] = P.level;
+  out[1] = P.id;
+  out[2] = P.parent_id;
+  for (int d = 0; d < 3; d++) {
+    out[3 + d] = P.mx[d];
+    out[6 + 2 * d] = P.mglobal[d][0];
+    out[7 + 2 * d] = P.mglobal[d][1];
+    out[12 + 2 * d] = P.mbounds[d][0];
+    out[13 + 2 * d] = P.mbounds[d][1];
+    dxl[d] = P.dx[d];
+    dxl[3 + d] = P.xlower[d];
+  }
+  for (int f = 0; f < 6; f++) out[18 + f] = P.mthbc[f];
   return BSAMG_OK;
 }
 

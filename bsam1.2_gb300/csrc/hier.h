@@ -50,6 +50,7 @@ struct Hier {
   bsamg_ctx* ctx = nullptr;
   int ndims = 2, nrvars = 2, mbc = 1, problem = 1;
   ProbParams pp{};
+  std::vector<double> params;  // as given to bsamg_hier_create
   std::vector<HostPatch> patches;
   std::unordered_map<int, int> id2idx;
   bool committed = false;
@@ -120,6 +121,11 @@ int enq_norm(Hier& H, int level, int errortype);
 int enq_relax(Hier& H, int level, int ipass);
 // plugin coefficients for a spacing h (PatchDev::c)
 void coefficients(const Hier& H, double h, double* c);
+// host tables of an uncommitted hierarchy (parent links, extents, level
+// lists, periodic offsets); commit() starts with it
+int build_tables(Hier& H);
+// AMR regrid of a committed hierarchy into a new one (regrid.cpp)
+int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* user, bsamg_hier** out);
 using GraphKey = std::tuple<int, int, int, int, int>;
 // capture what `body` enqueues as a CUDA graph (once per key) and replay it
 int capture_graph(Hier& H, const GraphKey& key, const std::function<int()>& body, Hier::GraphRec** out);

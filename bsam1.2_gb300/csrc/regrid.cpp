@@ -1,0 +1,616 @@
+// AMR regrid: the AMR(rootlevel) pass that TakeTimeSteps runs before every
+// time step (LIBRARY/bsamroutines.f90:657-689, AMR :966-991).
+//
+// The clustering is inherently sequential and branchy host work on small
+// integer arrays, so it runs on the host, as in the reference; the library
+// downloads the solution once, builds the new mesh level by level, and
+// uploads the new hierarchy once.  Level by level from the root:
+//   SetGhost(l, 0)                       ghost programs executed on host arrays
+//   tag (ErrFlag :1059-1131)             CH SetErrFlagsUser2D/3D or |grad phi|
+//   buffer (BufferAndList :1206-1247, InflateEdgeTags :1267-1308)
+//   cluster (NewSubGrids :1408-1605)     modified Berger-Rigoutsos per patch
+//   MakeNewGrid (:1663-1784) + InitFields (:1787-1856)
+//   TransferValues (:1859-1951)          previous level-(l+1) values
+// Floating-point work (ghost interpolation, mass-corrected prolongation) is
+// evaluated in the reference's order and built with -ffp-contract=off, so
+// the new mesh and its values equal a sequential restatement bit for bit.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "hier.h"
+
+namespace bsamg {
+
+namespace {
+
+constexpr int kMaxSubgrids = 1024;  // nodeinfodef.f90:62
+
+struct Model {
+  const Hier& src;                     // the hierarchy being regridded
+  std::vector<HostPatch> g;            // geometry, in visiting order
+  std::vector<std::vector<double>> q;  // ghosted q of levels >= 0 (empty below)
+  std::vector<std::vector<double>> qold;
+  std::vector<int> src_idx;            // index in src, or -1 for new patches
+  explicit Model(const Hier& h) : src(h) {}
+  int nd() const { return src.ndims; }
+  size_t nq(const HostPatch& P) const { return (size_t)P.qn[0] * P.qn[1] * P.qn[2]; }
+  double& Q(int p, int i, int j, int k, int v) {
+    const HostPatch& P = g[p];
+    return q[p][(((size_t)v * P.qn[2] + k) * P.qn[1] + j) * P.qn[0] + i];
+  }
+};
+
+// a host-only hierarchy with the model's geometry (tables, no device memory)
+int host_tables(const Model& M, Hier& T) {
+  T.ctx = M.src.ctx;
+  T.ndims = M.src.ndims;
+  T.nrvars = M.src.nrvars;
+  T.mbc = M.src.mbc;
+  T.problem = M.src.problem;
+  T.pp = M.src.pp;
+  for (const HostPatch& P : M.g) {
+    HostPatch c = P;
+    c.parent = -1;
+    T.id2idx[c.id] = (int)T.patches.size();
+    T.patches.push_back(c);
+  }
+  return build_tables(T);
+}
+
+// SetGhost(level, 0) on the model's host arrays: the compiled ghost program
+// of the level, stage by stage (the operations of a stage are independent)
+int host_set_ghost(Model& M, int level) {
+  Hier T;
+  int r = host_tables(M, T);
+  if (r) return r;
+  std::vector<int> stage_off;
+  std::vector<GhostOp> ops = compile_set_ghost(T, level, 0, stage_off);
+  const double a1 = -01.0 / 05.0, a2 = 02.0 / 03.0, a3 = 08.0 / 15.0;   // boundary.f90:54-63
+  const double b1 = 05.0 / 32.0, b2 = 15.0 / 16.0, b3 = -03.0 / 32.0;
+  const double c1 = 09.0 / 16.0, c2 = 03.0 / 16.0, c3 = 03.0 / 16.0, c4 = 01.0 / 16.0;
+  for (const GhostOp& o : ops) {
+    if (M.q[o.dp].empty() || M.q[o.sp].empty()) return BSAMG_ERR_ARG;  // below-root data is not on the host
+    for (int v = 0; v < M.src.nrvars; v++) {
+      double* dq = M.q[o.dp].data() + v * M.nq(M.g[o.dp]);
+      const double* sq = M.q[o.sp].data() + v * M.nq(M.g[o.sp]);
+      double val;
+      switch (o.type) {
+        case kGCopy: val = sq[o.s0]; break;
+        case kGCopyAdd: val = sq[o.s0] + M.src.pp.qpo[v]; break;
+        case kGCopySub: val = sq[o.s0] - M.src.pp.qpo[v]; break;
+        case kGBC: val = ((o.mask >> v) & 1) ? 2.0 - sq[o.s0] : sq[o.s0]; break;
+        case kGCfA: val = a1 * dq[o.s0] + a2 * dq[o.s1] + a3 * sq[o.c0]; break;
+        case kGCfAB: val = a1 * dq[o.s0] + a2 * dq[o.s1] + a3 * (b1 * sq[o.c0] + b2 * sq[o.c1] + b3 * sq[o.c2]); break;
+        default:
+          val = a1 * dq[o.s0] + a2 * dq[o.s1] + a3 * (c1 * sq[o.c0] + c2 * sq[o.c1] + c3 * sq[o.c2] + c4 * sq[o.c3]);
+          break;
+      }
+      dq[o.dcell] = val;
+    }
+  }
+  return BSAMG_OK;
+}
+
+// error flags of one patch, interior cells, x fastest
+struct Flags {
+  int mx[3];
+  std::vector<int> f;
+  int& at(int i, int j, int k) { return f[((size_t)(k - 1) * mx[1] + (j - 1)) * mx[0] + (i - 1)]; }
+};
+
+// SetErrFlagsUser2D/3D (CH/problem.f90:248-308): second differences of phi
+// above (2|3) qtolerance; or the gradient rule |grad phi| h > qtolerance
+void tag_patch(Model& M, int p, const bsamg_regrid_params& prm, Flags& F) {
+  const HostPatch& P = M.g[p];
+  int nd = M.nd();
+  double tol = prm.qtolerance[P.level];
+  for (int d = 0; d < 3; d++) F.mx[d] = P.mx[d];
+  F.f.assign((size_t)P.mx[0] * P.mx[1] * P.mx[2], 0);
+  int ko = nd == 3 ? 1 : 0;  // ghost offset of the third index
+  auto q = [&](int i, int j, int k) { return M.Q(p, i, j, k - 1 + ko, 0); };
+  for (int k = 1; k <= P.mx[2]; k++)
+    for (int j = 1; j <= P.mx[1]; j++)
+      for (int i = 1; i <= P.mx[0]; i++) {
+        bool t;
+        if (prm.tagging == BSAMG_TAG_CH) {
+          double s = std::fabs(q(i + 1, j, k) - 2.0 * q(i, j, k) + q(i - 1, j, k)) +
+                     std::fabs(q(i, j + 1, k) - 2.0 * q(i, j, k) + q(i, j - 1, k));
+          if (nd == 3) s = s + std::fabs(q(i, j, k + 1) - 2.0 * q(i, j, k) + q(i, j, k - 1));
+          t = s > (nd == 3 ? 3.0 : 2.0) * tol;
+        } else {
+          double gx = (q(i + 1, j, k) - q(i - 1, j, k)) * 0.5;
+          double gy = (q(i, j + 1, k) - q(i, j - 1, k)) * 0.5;
+          double gs = gx * gx + gy * gy;
+          if (nd == 3) {
+            double gz = (q(i, j, k + 1) - q(i, j, k - 1)) * 0.5;
+            gs = gs + gz * gz;
+          }
+          t = gs > tol * tol;
+        }
+        F.at(i, j, k) = t ? 1 : 0;
+      }
+}
+
+struct Tag {
+  int c[3];
+};
+
+// BufferAndList (:1206-1247): buffer inside the patch, list the tags whose
+// buffer crosses its edge (global coordinates)
+void buffer_and_list(const Model& M, const HostPatch& P, int ib, Flags& F, std::vector<Tag>& list) {
+  std::vector<int> tmp = F.f;
+  int nd = M.nd();
+  for (int k = 1; k <= P.mx[2]; k++)
+    for (int j = 1; j <= P.mx[1]; j++)
+      for (int i = 1; i <= P.mx[0]; i++) {
+        if (tmp[((size_t)(k - 1) * P.mx[1] + (j - 1)) * P.mx[0] + (i - 1)] != 1) continue;
+        int idx[3] = {i, j, k}, lo[3] = {1, 1, 1}, hi[3] = {1, 1, 1};
+        bool out = false;
+        for (int d = 0; d < nd; d++) lo[d] = idx[d] - ib, hi[d] = idx[d] + ib;
+        for (int d = 0; d < 3; d++) out = out || lo[d] < 1 || hi[d] > P.mx[d];
+        if (out) {
+          Tag t;
+          for (int d = 0; d < 3; d++) t.c[d] = d < nd ? idx[d] + P.mglobal[d][0] - 1 : 1;
+          list.push_back(t);
+        } else {
+          for (int c = lo[2]; c <= hi[2]; c++)
+            for (int b = lo[1]; b <= hi[1]; b++)
+              for (int a = lo[0]; a <= hi[0]; a++) F.at(a, b, c) = 1;
+        }
+      }
+}
+
+// BufferTaggedCells (:1311-1349)
+void buffer_tagged(int nd, const HostPatch& P, const int* tag, int ib, Flags& F) {
+  int lo[3] = {1, 1, 1}, hi[3] = {1, 1, 1};
+  for (int d = 0; d < nd; d++) {
+    lo[d] = std::max(tag[d] - ib, P.mglobal[d][0]);
+    hi[d] = std::min(tag[d] + ib, P.mglobal[d][1]);
+    if (hi[d] < lo[d]) return;
+    lo[d] -= P.mglobal[d][0] - 1;
+    hi[d] -= P.mglobal[d][0] - 1;
+  }
+  for (int c = lo[2]; c <= hi[2]; c++)
+    for (int b = lo[1]; b <= hi[1]; b++)
+      for (int a = lo[0]; a <= hi[0]; a++) F.at(a, b, c) = 1;
+}
+
+using Box = int[3][2];
+
+// GetSignatures (:1608-1632) along dimension n over box b
+void signature(Flags& F, const Box& b, int n, std::vector<int>& sig) {
+  for (int i = b[n][0]; i <= b[n][1]; i++) {
+    int lo[3], hi[3], s = 0;
+    for (int d = 0; d < 3; d++) lo[d] = b[d][0], hi[d] = b[d][1];
+    lo[n] = hi[n] = i;
+    for (int c = lo[2]; c <= hi[2]; c++)
+      for (int y = lo[1]; y <= hi[1]; y++)
+        for (int x = lo[0]; x <= hi[0]; x++) s += F.at(x, y, c);
+    sig[i] = s;
+  }
+}
+
+// GridFlagRatio (:1635-1660)
+double flag_ratio(Flags& F, Box& b, int nd) {
+  double total = 1.0;
+  for (int d = 0; d < nd; d++) total = total * (double)(b[d][1] - b[d][0] + 1);
+  for (int d = nd; d < 3; d++) b[d][0] = b[d][1] = 1;
+  long long s = 0;
+  for (int c = b[2][0]; c <= b[2][1]; c++)
+    for (int y = b[1][0]; y <= b[1][1]; y++)
+      for (int x = b[0][0]; x <= b[0][1]; x++) s += F.at(x, y, c);
+  return (double)s / total;
+}
+
+struct Sub {
+  Box b;
+};
+
+// NewSubGrids (:1408-1605), the modified Berger-Rigoutsos algorithm; false
+// on the reference's error stops
+bool new_sub_grids(int nd, const HostPatch& P, Flags& F, const bsamg_regrid_params& prm, std::vector<Sub>& out) {
+  out.clear();
+  int level = P.level;
+  double desfill = prm.desiredfillratio[level];
+  int mgp = prm.minimumgridpoints[level];
+  if (mgp < 4 || mgp % 2) return false;
+  Sub whole;
+  for (int d = 0; d < 3; d++) whole.b[d][0] = 1, whole.b[d][1] = d < nd ? P.mx[d] : 1;
+  if (flag_ratio(F, whole.b, nd) < 1.0e-10) return true;
+  int maxm = 0;
+  for (int d = 0; d < nd; d++) maxm = std::max(maxm, P.mx[d]);
+  std::vector<std::vector<int>> sig(3, std::vector<int>(maxm + 2, 0)), dds(3, std::vector<int>(maxm + 2, 0));
+  std::vector<char> cansplit(kMaxSubgrids + 1, 1);
+  out.push_back(whole);
+  int igrid = 1;
+  auto imod2 = [](int a) { return ((a % 2) + 2) % 2; };
+  while ((int)out.size() < kMaxSubgrids && igrid <= (int)out.size()) {
+    int npass = 0;
+    while (cansplit[igrid] && npass < 15) {
+      npass++;
+      Box& b = out[igrid - 1].b;
+      for (int n = 0; n < nd; n++) signature(F, b, n, sig[n]);
+      for (int n = 0; n < nd; n++) {  // trim unflagged edges
+        int i1 = b[n][0], i2 = b[n][1];
+        while (sig[n][i1] == 0 && i1 < b[n][1] && i2 - i1 + 1 > mgp) i1++;
+        while (sig[n][i2] == 0 && i2 > b[n][0] && i2 - i1 + 1 > mgp) i2--;
+        b[n][0] = i1 - imod2(i1 + 1);
+        b[n][1] = i2 + imod2(i2);
+      }
+      if (flag_ratio(F, b, nd) >= desfill) {
+        cansplit[igrid] = 0;
+        continue;
+      }
+      for (int n = 0; n < nd; n++) signature(F, b, n, sig[n]);
+      int isplit[3] = {0, 0, 0};
+      bool have = false;
+      for (int n = 0; n < nd && !have; n++) {  // holes
+        int i1 = b[n][0], i2 = b[n][1];
+        for (int i = i1 + mgp - 1; i <= i2 - mgp; i += 2)
+          if (sig[n][i] == 0 && std::min(i - i1 + 1, i2 - i) >= mgp) {
+            isplit[n] = i;
+            have = true;
+            break;
+          }
+      }
+      if (!have) {  // inflection points
+        for (int n = 0; n < nd; n++)
+          for (int i = b[n][0] + 1; i <= b[n][1] - 1; i++) dds[n][i] = sig[n][i - 1] - 2 * sig[n][i] + sig[n][i + 1];
+        int inflect = 0, dist0 = 0;
+        for (int n = 0; n < nd; n++) {
+          int i1 = b[n][0], i2 = b[n][1];
+          for (int i = i1 + mgp; i <= i2 - mgp + 1; i += 2) {
+            int del = std::abs(dds[n][i] - dds[n][i - 1]);
+            if (del > inflect) {
+              inflect = del;
+              isplit[0] = isplit[1] = isplit[2] = 0;
+              isplit[n] = i - 1;
+              have = true;
+              dist0 = std::min(i - i1, i2 - i + 1);
+            } else if (del == inflect && inflect > 0) {
+              int dist1 = std::min(i - i1, i2 - i + 1);
+              if (dist1 > dist0) {
+                isplit[0] = isplit[1] = isplit[2] = 0;
+                isplit[n] = i - 1;
+                have = true;
+                dist0 = dist1;
+              }
+            }
+          }
+        }
+      }
+      if (!have) {
+        cansplit[igrid] = 0;
+        continue;
+      }
+      for (int n = 0; n < nd; n++)
+        if (isplit[n] > 0 && std::min(b[n][1] - isplit[n], isplit[n] - b[n][0] + 1) >= mgp) {
+          Sub s = out[igrid - 1];
+          s.b[n][0] = isplit[n] + 1;
+          out[igrid - 1].b[n][1] = isplit[n];
+          out.push_back(s);
+          cansplit[out.size()] = 1;
+          break;
+        }
+    }
+    igrid++;
+  }
+  for (const Sub& s : out)  // the reference's checks, :1565-1595
+    for (int n = 0; n < nd; n++) {
+      int len = s.b[n][1] - s.b[n][0] + 1;
+      if (len < mgp || len % 2 || s.b[n][0] % 2 == 0 || s.b[n][1] % 2 == 1) return false;
+    }
+  return true;
+}
+
+// Patches longer than maxside child cells are cut into nearly equal even
+// pieces (not a reference feature: it bounds patch sizes for the batched
+// kernels)
+void split_long(int nd, int maxside, std::vector<Sub>& subs) {
+  if (maxside <= 0) return;
+  int P = maxside / 2;
+  for (size_t g = 0; g < subs.size(); g++)
+    for (int n = 0; n < nd; n++) {
+      int len = subs[g].b[n][1] - subs[g].b[n][0] + 1;
+      if (len <= P) continue;
+      int pieces = (len + P - 1) / P, half = len / 2, base = half / pieces, extra = half % pieces;
+      int lo = subs[g].b[n][0];
+      Sub tmpl = subs[g];
+      for (int k = 0; k < pieces; k++) {
+        int plen = 2 * (base + (k < extra ? 1 : 0));
+        Sub piece = tmpl;
+        piece.b[n][0] = lo;
+        piece.b[n][1] = lo + plen - 1;
+        if (k == 0) subs[g] = piece;
+        else subs.push_back(piece);
+        lo += plen;
+      }
+    }
+}
+
+// BiLin/TriLinProlongationP1MC (gridutilities.f90:242-369, :628-727): a is
+// the coarse block with one ghost layer (cmx+2 per dimension), out the fine
+// block with one ghost layer (2*cmx+2)
+void prolong_mc(int nd, const std::vector<double>& a, const int cmx[3], double* out) {
+  int cn0 = cmx[0] + 2, cn1 = cmx[1] + 2, cn2 = nd == 3 ? cmx[2] + 2 : 1;
+  int fn0 = 2 * cmx[0] + 2, fn1 = 2 * cmx[1] + 2;
+  auto A = [&](int i, int j, int k) { return a[((size_t)k * cn1 + j) * cn0 + i]; };
+  auto O = [&](int i, int j, int k) -> double& { return out[((size_t)k * fn1 + j) * fn0 + i]; };
+  std::vector<double> b((size_t)fn0 * cn1 * cn2);
+  auto Bx = [&](int i, int j, int k) -> double& { return b[((size_t)k * cn1 + j) * fn0 + i]; };
+  for (int k = 0; k < cn2; k++)
+    for (int j = 0; j < cn1; j++)
+      for (int I = 0; I <= cmx[0]; I++) {
+        Bx(2 * I, j, k) = 3.0 * A(I, j, k) + A(I + 1, j, k);
+        Bx(2 * I + 1, j, k) = A(I, j, k) + 3.0 * A(I + 1, j, k);
+      }
+  if (nd == 2) {
+    for (int J = 0; J <= cmx[1]; J++)
+      for (int i = 0; i < fn0; i++) {
+        O(i, 2 * J, 0) = (3.0 * Bx(i, J, 0) + Bx(i, J + 1, 0)) / 16.0;
+        O(i, 2 * J + 1, 0) = (Bx(i, J, 0) + 3.0 * Bx(i, J + 1, 0)) / 16.0;
+      }
+    for (int J = 1; J <= cmx[1]; J++)
+      for (int I = 1; I <= cmx[0]; I++) {
+        double cor = A(I, J, 0) - 0.25 * (O(2 * I, 2 * J, 0) + O(2 * I - 1, 2 * J, 0) + O(2 * I, 2 * J - 1, 0) +
+                                          O(2 * I - 1, 2 * J - 1, 0));
+        O(2 * I, 2 * J, 0) = O(2 * I, 2 * J, 0) + cor;
+        O(2 * I - 1, 2 * J, 0) = O(2 * I - 1, 2 * J, 0) + cor;
+        O(2 * I, 2 * J - 1, 0) = O(2 * I, 2 * J - 1, 0) + cor;
+        O(2 * I - 1, 2 * J - 1, 0) = O(2 * I - 1, 2 * J - 1, 0) + cor;
+      }
+    return;
+  }
+  std::vector<double> c((size_t)fn0 * fn1 * cn2);
+  auto Cy = [&](int i, int j, int k) -> double& { return c[((size_t)k * fn1 + j) * fn0 + i]; };
+  for (int k = 0; k < cn2; k++)
+    for (int J = 0; J <= cmx[1]; J++)
+      for (int i = 0; i < fn0; i++) {
+        Cy(i, 2 * J, k) = 3.0 * Bx(i, J, k) + Bx(i, J + 1, k);
+        Cy(i, 2 * J + 1, k) = Bx(i, J, k) + 3.0 * Bx(i, J + 1, k);
+      }
+  for (int K = 0; K <= cmx[2]; K++)
+    for (int j = 0; j < fn1; j++)
+      for (int i = 0; i < fn0; i++) {
+        O(i, j, 2 * K) = (3.0 * Cy(i, j, K) + Cy(i, j, K + 1)) / 64.0;
+        O(i, j, 2 * K + 1) = (Cy(i, j, K) + 3.0 * Cy(i, j, K + 1)) / 64.0;
+      }
+  for (int K = 1; K <= cmx[2]; K++)
+    for (int J = 1; J <= cmx[1]; J++)
+      for (int I = 1; I <= cmx[0]; I++) {
+        double cor = A(I, J, K) - 0.125 * (O(2 * I, 2 * J, 2 * K) + O(2 * I - 1, 2 * J, 2 * K) +
+                                           O(2 * I, 2 * J - 1, 2 * K) + O(2 * I - 1, 2 * J - 1, 2 * K) +
+                                           O(2 * I, 2 * J, 2 * K - 1) + O(2 * I - 1, 2 * J, 2 * K - 1) +
+                                           O(2 * I, 2 * J - 1, 2 * K - 1) + O(2 * I - 1, 2 * J - 1, 2 * K - 1));
+        for (int dk = 0; dk < 2; dk++)
+          for (int dj = 0; dj < 2; dj++)
+            for (int di = 0; di < 2; di++)
+              O(2 * I - di, 2 * J - dj, 2 * K - dk) = O(2 * I - di, 2 * J - dj, 2 * K - dk) + cor;
+      }
+}
+
+// MakeNewGrid (:1663-1784) and InitFields (:1787-1856) for box b of patch p
+void make_new_grid(Model& M, int p, const Box& b, int id, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit,
+                   void* user) {
+  int nd = M.nd();
+  HostPatch C{};
+  const HostPatch& P = M.g[p];
+  C.level = P.level + 1;
+  C.id = id;
+  C.parent_id = P.id;
+  C.parent = p;
+  for (int d = 0; d < 3; d++) {
+    C.mx[d] = 1;
+    C.mglobal[d][0] = C.mglobal[d][1] = C.mbounds[d][0] = C.mbounds[d][1] = 1;
+    C.dx[d] = C.xlower[d] = 0.0;
+    if (d >= nd) continue;
+    C.mx[d] = (b[d][1] - b[d][0] + 1) * 2;
+    C.mbounds[d][0] = b[d][0];
+    C.mbounds[d][1] = b[d][1];
+    int g0 = P.mglobal[d][0] + b[d][0] - 1, g1 = g0 + b[d][1] - b[d][0];
+    C.mglobal[d][0] = (g0 - 1) * 2 + 1;
+    C.mglobal[d][1] = g1 * 2;
+    C.xlower[d] = (double)(b[d][0] - 1) * P.dx[d] + P.xlower[d];
+    C.dx[d] = P.dx[d] / 2.0;
+  }
+  for (int f = 0; f < 6; f++) C.mthbc[f] = f < 2 * nd ? kInternalBC : 10;
+  for (int n = 0; n < nd; n++) {
+    if (P.mthbc[2 * n] < kInternalBC && C.mbounds[n][0] == 1) C.mthbc[2 * n] = P.mthbc[2 * n];
+    if (P.mthbc[2 * n + 1] < kInternalBC && C.mbounds[n][1] == P.mx[n]) C.mthbc[2 * n + 1] = P.mthbc[2 * n + 1];
+  }
+  for (int d = 0; d < 3; d++) {
+    C.cmx[d] = d < nd ? C.mx[d] / 2 : 1;
+    C.qn[d] = d < nd ? C.mx[d] + 2 : 1;
+    C.cn[d] = d < nd ? C.cmx[d] + 2 : 1;
+  }
+  size_t nq = (size_t)C.qn[0] * C.qn[1] * C.qn[2];
+  std::vector<double> q(nq * M.src.nrvars, 0.0);
+  if (prm.initial) {
+    qinit(user, C.level, C.mx, C.dx, C.xlower, q.data());
+  } else {
+    int cmx[3] = {C.cmx[0], C.cmx[1], nd == 3 ? C.cmx[2] : 0};
+    int k0 = nd == 3 ? b[2][0] - 1 : 0, k1 = nd == 3 ? b[2][1] + 1 : 0;  // ghost-shifted third index
+    std::vector<double> a;
+    for (int v = 0; v < M.src.nrvars; v++) {
+      a.clear();
+      for (int k = k0; k <= k1; k++)
+        for (int j = b[1][0] - 1; j <= b[1][1] + 1; j++)
+          for (int i = b[0][0] - 1; i <= b[0][1] + 1; i++) a.push_back(M.Q(p, i, j, k, v));
+      prolong_mc(nd, a, cmx, q.data() + v * nq);
+    }
+  }
+  M.g.push_back(C);
+  M.src_idx.push_back(-1);
+  M.qold.push_back(q);  // child%qold = child%q (:1782)
+  M.q.push_back(std::move(q));
+}
+
+// TransferOverlap (:1919-1951): interior q of src onto dst
+void transfer_overlap(int nrvars, const HostPatch& S, const std::vector<double>& sq, const HostPatch& D,
+                      std::vector<double>& dq, int nd) {
+  int lo[3], hi[3];
+  for (int d = 0; d < 3; d++) {
+    lo[d] = std::max(S.mglobal[d][0], D.mglobal[d][0]);
+    hi[d] = std::min(S.mglobal[d][1], D.mglobal[d][1]);
+    if (hi[d] < lo[d]) return;
+  }
+  size_t ns = (size_t)S.qn[0] * S.qn[1] * S.qn[2], ndd = (size_t)D.qn[0] * D.qn[1] * D.qn[2];
+  int ko = nd == 3 ? 1 : 0;
+  auto at = [&](const HostPatch& P, int i, int j, int k) {
+    return ((size_t)(k - P.mglobal[2][0] + ko) * P.qn[1] + (j - P.mglobal[1][0] + 1)) * P.qn[0] +
+           (i - P.mglobal[0][0] + 1);
+  };
+  for (int v = 0; v < nrvars; v++)
+    for (int k = lo[2]; k <= hi[2]; k++)
+      for (int j = lo[1]; j <= hi[1]; j++)
+        for (int i = lo[0]; i <= hi[0]; i++) dq[v * ndd + at(D, i, j, k)] = sq[v * ns + at(S, i, j, k)];
+}
+
+int download(const Hier& H, int idx, std::vector<double>& out, long long off) {
+  const HostPatch& P = H.patches[idx];
+  out.resize((size_t)P.sq * H.nrvars);
+  cudaError_t e = cudaMemcpyAsync(out.data(), H.pool + off, out.size() * sizeof(double), cudaMemcpyDeviceToHost, H.s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(regrid download)");
+  return BSAMG_OK;
+}
+
+}  // namespace
+
+int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* user, bsamg_hier** out) {
+  if (!H.committed || prm.maxlevel < 0 || prm.maxlevel > kMaxDepth || (prm.initial && !qinit)) return BSAMG_ERR_ARG;
+  if (prm.tagging != BSAMG_TAG_CH && prm.tagging != BSAMG_TAG_GRADIENT) return BSAMG_ERR_ARG;
+  int r = set_device(H);
+  if (r) return r;
+  int nd = H.ndims, nv = H.nrvars;
+  Model M(H);
+  // the root and the levels below persist; q of level 0 comes to the host
+  for (size_t n = 0; n < H.patches.size(); n++) {
+    const HostPatch& P = H.patches[n];
+    if (P.level > 0) continue;
+    M.g.push_back(P);
+    M.src_idx.push_back((int)n);
+    M.q.emplace_back();
+    M.qold.emplace_back();
+    if (P.level == 0 && (r = download(H, (int)n, M.q.back(), P.oq))) return r;
+  }
+  // previous refinement levels, for TransferValues
+  std::vector<std::vector<double>> oldq(H.patches.size());
+  for (size_t n = 0; n < H.patches.size(); n++)
+    if (H.patches[n].level > 0 && (r = download(H, (int)n, oldq[n], H.patches[n].oq))) return r;
+  cudaError_t ce = cudaStreamSynchronize(H.s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize(regrid)");
+
+  int next_id = prm.first_id;
+  int level;
+  std::vector<Sub> subs;
+  auto level_patches = [&](int l) {
+    std::vector<int> v;
+    for (size_t p = 0; p < M.g.size(); p++)
+      if (M.g[p].level == l) v.push_back((int)p);
+    return v;
+  };
+  for (level = 0; level < prm.maxlevel; level++) {  // AMR(level), :966-991
+    std::vector<int> lp = level_patches(level);
+    if (lp.empty()) break;
+    if ((r = host_set_ghost(M, level))) return r;
+    std::vector<Flags> fl(lp.size());
+    std::vector<Tag> list;
+    int ib = prm.ibuffer[level];
+    for (size_t a = 0; a < lp.size(); a++) {  // ErrFlag
+      tag_patch(M, lp[a], prm, fl[a]);
+      if (ib > 0) buffer_and_list(M, M.g[lp[a]], ib, fl[a], list);
+    }
+    if (!list.empty()) {  // InflateEdgeTags
+      Hier T;
+      if ((r = host_tables(M, T))) return r;
+      int poff[13][3] = {};
+      for (int o = 0; o < T.nperoff; o++) {
+        const int* mm = T.mxmax[level];
+        int a = 0, b = 0, c = 0;
+        switch (T.peroffidx[o]) {  // GetPeriodicOffsets, boundary.f90:875-954
+          case 1: a = mm[0]; break;
+          case 2: b = mm[1]; break;
+          case 3: c = mm[2]; break;
+          case 4: a = mm[0]; b = mm[1]; break;
+          case 5: a = -mm[0]; b = mm[1]; break;
+          case 6: b = mm[1]; c = mm[2]; break;
+          case 7: b = mm[1]; c = -mm[2]; break;
+          case 8: a = mm[0]; c = mm[2]; break;
+          case 9: a = -mm[0]; c = mm[2]; break;
+          case 10: a = mm[0]; b = mm[1]; c = mm[2]; break;
+          case 11: a = mm[0]; b = mm[1]; c = -mm[2]; break;
+          case 12: a = -mm[0]; b = mm[1]; c = mm[2]; break;
+          case 13: a = mm[0]; b = -mm[1]; c = mm[2]; break;
+        }
+        poff[o][0] = a, poff[o][1] = b, poff[o][2] = c;
+      }
+      for (int t = (int)list.size() - 1; t >= 0; t--) {
+        for (size_t a = 0; a < lp.size(); a++) buffer_tagged(nd, M.g[lp[a]], list[t].c, ib, fl[a]);
+        if (T.periodic)
+          for (int pol = -1; pol <= 1; pol += 2)
+            for (int o = 0; o < T.nperoff; o++) {
+              int c[3];
+              for (int d = 0; d < 3; d++) c[d] = list[t].c[d] + pol * poff[o][d];
+              for (size_t a = 0; a < lp.size(); a++) buffer_tagged(nd, M.g[lp[a]], c, ib, fl[a]);
+            }
+      }
+    }
+    size_t first_new = M.g.size();
+    for (size_t a = 0; a < lp.size(); a++) {  // GridAdapt -> RefineGrid
+      if (!new_sub_grids(nd, M.g[lp[a]], fl[a], prm, subs)) return BSAMG_ERR_ARG;
+      split_long(nd, prm.maxside, subs);
+      for (const Sub& s : subs) make_new_grid(M, lp[a], s.b, next_id++, prm, qinit, user);
+    }
+    for (size_t c = first_new; c < M.g.size(); c++)  // TransferValues
+      for (size_t n = 0; n < H.patches.size(); n++)
+        if (H.patches[n].level == level + 1) transfer_overlap(nv, H.patches[n], oldq[n], M.g[c], M.q[c], nd);
+  }
+  if (!level_patches(level).empty() && (r = host_set_ghost(M, level))) return r;  // AMR(finest)
+
+  // the new hierarchy, on the same context
+  bsamg_hier* nh = nullptr;
+  r = bsamg_hier_create(H.ctx, nd, nv, H.mbc, H.problem, H.params.data(), (int)H.params.size(), H.pp.qpo, &nh);
+  if (r) return r;
+  auto fail = [&](int rc) {
+    bsamg_hier_destroy(nh);
+    return rc;
+  };
+  for (const HostPatch& P : M.g) {
+    int mg[6], mb[6];
+    for (int d = 0; d < 3; d++) {
+      mg[2 * d] = P.mglobal[d][0], mg[2 * d + 1] = P.mglobal[d][1];
+      mb[2 * d] = P.mbounds[d][0], mb[2 * d + 1] = P.mbounds[d][1];
+    }
+    if ((r = bsamg_patch_add(nh, P.level, P.id, P.parent_id, P.mx, mg, mb, P.mthbc, P.dx, P.xlower))) return fail(r);
+  }
+  if ((r = bsamg_commit(nh))) return fail(r);
+  Hier& N = *nh;
+  for (size_t p = 0; p < M.g.size(); p++) {
+    const HostPatch& D = N.patches[p];
+    size_t bytes = (size_t)D.sq * nv * sizeof(double);
+    cudaError_t e;
+    if (M.src_idx[p] >= 0 && M.g[p].level < 0) {  // unchanged below the root
+      const HostPatch& S = H.patches[M.src_idx[p]];
+      e = cudaMemcpyAsync(N.pool + D.oq, H.pool + S.oq, bytes, cudaMemcpyDeviceToDevice, N.s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(N.pool + D.oqold, H.pool + S.oqold, bytes, cudaMemcpyDeviceToDevice, N.s);
+    } else if (M.src_idx[p] >= 0) {  // the root: new ghosts, same qold
+      const HostPatch& S = H.patches[M.src_idx[p]];
+      e = cudaMemcpyAsync(N.pool + D.oq, M.q[p].data(), bytes, cudaMemcpyHostToDevice, N.s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(N.pool + D.oqold, H.pool + S.oqold, bytes, cudaMemcpyDeviceToDevice, N.s);
+    } else {
+      e = cudaMemcpyAsync(N.pool + D.oq, M.q[p].data(), bytes, cudaMemcpyHostToDevice, N.s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(N.pool + D.oqold, M.qold[p].data(), bytes, cudaMemcpyHostToDevice, N.s);
+    }
+    if (e != cudaSuccess) return fail(cuda_fail(e, "cudaMemcpyAsync(regrid upload)"));
+  }
+  ce = cudaStreamSynchronize(N.s);  // the host arrays are freed on return
+  if (ce != cudaSuccess) return fail(cuda_fail(ce, "cudaStreamSynchronize(regrid upload)"));
+  *out = nh;
+  return BSAMG_OK;
+}
+
+}  // namespace bsamg

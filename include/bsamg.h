@@ -89,6 +89,45 @@ int bsamg_hier_create(bsamg_ctx* ctx, int ndims, int nrvars, int mbc,
                       const double* qpo, bsamg_hier** out);
 int bsamg_hier_destroy(bsamg_hier* h);
 
+/* ---- AMR regrid ------------------------------------------------------
+ * The AMR(rootlevel) pass that TakeTimeSteps runs before every time step
+ * (LIBRARY/bsamroutines.f90:657-689, AMR :966-991): level by level from the
+ * root, SetGhost(l,0); tag (ErrFlag :1059-1131 with the plugin rule
+ * SetErrFlagsUser2D/3D, PROBLEM/CH/problem.f90:248-308, or the gradient
+ * rule); buffer the tags (BufferAndList :1206-1247, InflateEdgeTags
+ * :1267-1308, periodic images included); cluster the tags of every patch
+ * (NewSubGrids :1408-1605, modified Berger-Rigoutsos); make the children
+ * (MakeNewGrid :1663-1784) and fill them (InitFields :1787-1856: the
+ * initial condition through `qinit` when `initial`, else mass-corrected
+ * bilinear/trilinear prolongation from the parent); copy the previous
+ * level-(l+1) values over them (TransferValues :1859-1951).  The per-level
+ * arrays are the griddata namelist entries (bsamroutines.f90:243-266).
+ * The result is a new committed hierarchy on the same context: the levels
+ * <= 0 of h (q and qold) and the new levels > 0; h is left unchanged and
+ * stays valid.  New patch ids are first_id, first_id+1, ... in creation
+ * order (parents in visiting order, children in NewSubGrids order).
+ * maxside > 0 splits new patches to at most maxside cells per side (not a
+ * reference feature). */
+#define BSAMG_TAG_CH 0       /* |second differences of phi| > (2|3) qtolerance */
+#define BSAMG_TAG_GRADIENT 1 /* |grad phi| h > qtolerance (central differences) */
+typedef struct {
+  int maxlevel;
+  int tagging;
+  int initial;
+  int maxside;
+  int first_id;
+  int ibuffer[11];
+  int minimumgridpoints[11];
+  double qtolerance[11];
+  double desiredfillratio[11];
+} bsamg_regrid_params;
+/* Fill the interior of q (ghosted Fortran layout, nrvars variables) of a
+ * new patch with the initial condition (the plugin's QInit2D/3D). */
+typedef void (*bsamg_qinit_fn)(void* user, int level, const int* mx, const double* dx, const double* xlower,
+                               double* q);
+int bsamg_regrid(bsamg_hier* h, const bsamg_regrid_params* prm, bsamg_qinit_fn qinit, void* user,
+                 bsamg_hier** out);
+
 /* One patch (node).  Patches of a level are visited in the order they are
  * added, which the caller makes the reference's ApplyOnLevel order
  * (youngest first).  mglobal/mbounds are (lo,hi) pairs per dimension;
@@ -105,6 +144,11 @@ int bsamg_build_uniform(bsamg_hier* h, const int mx[3], int minlevel,
  * schedule.  No patch may be added afterwards. */
 int bsamg_commit(bsamg_hier* h);
 int bsamg_num_patches(const bsamg_hier* h, int* n);
+/* Geometry of the patch at `index` in visiting order: out[0..23] = level,
+ * id, parent_id, mx[3], mglobal[6], mbounds[6], mthbc[6]; dxl[0..5] =
+ * dx[3], xlower[3] -- the nodeinfo fields a host walks after a regrid
+ * (LIBRARY/nodeinfodef.f90:118-220). */
+int bsamg_patch_info(const bsamg_hier* h, int index, int* out, double* dxl);
 size_t bsamg_field_size(const bsamg_hier* h, int id, int field);
 /* synchronous host <-> device copies of a whole field array (n doubles) */
 int bsamg_put_field(bsamg_hier* h, int id, int field, const double* a,

@@ -1449,3 +1449,535 @@ double bsamo_uniform_pm1(unsigned long long seed, unsigned long long gidx) {
   z = z ^ (z >> 31);
   return 2.0 * ((double)(z >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
 }
+
+/* ------------------------------------------------------------------ */
+/* AMR regrid (bsamroutines.f90:657-689, :966-1951)                    */
+
+/* a patch added to a committed hierarchy, fields allocated (zero) */
+static int add_live_patch(bsamo_hier* h, int level, int id, int parent, const int mx[3], const int mg[3][2],
+                          const int mb[3][2], const int thbc[6], const double dx[3], const double xl[3]) {
+  if (h->np == h->cap) {
+    h->cap = h->cap ? 2 * h->cap : 16;
+    h->p = (OPatch*)realloc(h->p, sizeof(OPatch) * h->cap);
+  }
+  int n = h->np++;
+  OPatch* p = &h->p[n];
+  memset(p, 0, sizeof(*p));
+  p->level = level;
+  p->id = id;
+  p->parent = parent;
+  p->parent_id = parent >= 0 ? h->p[parent].id : -1;
+  for (int d = 0; d < 3; d++) {
+    int used = d < h->ndims;
+    p->mx[d] = mx[d];
+    p->mglobal[d][0] = mg[d][0];
+    p->mglobal[d][1] = mg[d][1];
+    p->mbounds[d][0] = mb[d][0];
+    p->mbounds[d][1] = mb[d][1];
+    p->dx[d] = dx[d];
+    p->xlower[d] = xl[d];
+    p->cmx[d] = (used && p->mx[d] % 2 == 0) ? p->mx[d] / 2 : 1;
+    p->qlo[d] = used ? 1 - h->mbc : 1;
+    p->qn[d] = used ? p->mx[d] + 2 * h->mbc : 1;
+    p->clo[d] = used ? 1 - h->mbc : 1;
+    p->cn[d] = used ? p->cmx[d] + 2 * h->mbc : 1;
+    p->fn[d] = used ? p->mx[d] : 1;
+  }
+  for (int f = 0; f < 6; f++) p->mthbc[f] = thbc[f];
+  size_t nq = (size_t)p->qn[0] * p->qn[1] * p->qn[2] * h->nrvars;
+  size_t nc = (size_t)p->cn[0] * p->cn[1] * p->cn[2] * h->nrvars;
+  size_t nf = (size_t)p->fn[0] * p->fn[1] * p->fn[2] * h->nrvars;
+  p->q = (double*)calloc(nq, sizeof(double));
+  p->qold = (double*)calloc(nq, sizeof(double));
+  p->qc = (double*)calloc(nc, sizeof(double));
+  p->f = (double*)calloc(nf, sizeof(double));
+  p->rf = (double*)calloc(nf, sizeof(double));
+  p->ftmp = (double*)calloc(nf, sizeof(double));
+  int l = level + MAXDEPTH;
+  h->lev_list[l] = (int*)realloc(h->lev_list[l], sizeof(int) * (h->lev_n[l] + 1));
+  h->lev_list[l][h->lev_n[l]++] = n;
+  if (level > h->maxlevel_present) h->maxlevel_present = level;
+  return n;
+}
+
+static inline size_t fidx(const OPatch* p, int i, int j, int k) {
+  return ((size_t)(k - 1) * p->mx[1] + (size_t)(j - 1)) * p->mx[0] + (size_t)(i - 1);
+}
+
+/* SetErrFlagsUser2D/3D (CH/problem.f90:248-308) or the gradient rule */
+static void tag_patch(const bsamo_hier* h, const OPatch* p, const bsamo_regrid_params* prm, int* fl) {
+  double tol = prm->qtolerance[p->level];
+  int nd = h->ndims;
+  for (int k = 1; k <= p->mx[2]; k++)
+    for (int j = 1; j <= p->mx[1]; j++)
+      for (int i = 1; i <= p->mx[0]; i++) {
+        int t;
+        if (prm->tagging == BSAMO_TAG_CH) {
+          double s = fabs(Q(p, i + 1, j, k, 0) - 2.0 * Q(p, i, j, k, 0) + Q(p, i - 1, j, k, 0)) +
+                     fabs(Q(p, i, j + 1, k, 0) - 2.0 * Q(p, i, j, k, 0) + Q(p, i, j - 1, k, 0));
+          if (nd == 3) s = s + fabs(Q(p, i, j, k + 1, 0) - 2.0 * Q(p, i, j, k, 0) + Q(p, i, j, k - 1, 0));
+          t = s > (nd == 3 ? 3.0 : 2.0) * tol;
+        } else {
+          double gx = (Q(p, i + 1, j, k, 0) - Q(p, i - 1, j, k, 0)) * 0.5;
+          double gy = (Q(p, i, j + 1, k, 0) - Q(p, i, j - 1, k, 0)) * 0.5;
+          double g = gx * gx + gy * gy;
+          if (nd == 3) {
+            double gz = (Q(p, i, j, k + 1, 0) - Q(p, i, j, k - 1, 0)) * 0.5;
+            g = g + gz * gz;
+          }
+          t = g > tol * tol;
+        }
+        fl[fidx(p, i, j, k)] = t;
+      }
+}
+
+typedef struct {
+  int n, cap;
+  int (*c)[3];
+} TagList;
+
+/* BufferAndList, bsamroutines.f90:1206-1247 */
+static void buffer_and_list(const bsamo_hier* h, const OPatch* p, int ib, int* fl, TagList* tl) {
+  size_t n = (size_t)p->mx[0] * p->mx[1] * p->mx[2];
+  int* tmp = (int*)malloc(sizeof(int) * n);
+  memcpy(tmp, fl, sizeof(int) * n);
+  for (int k = 1; k <= p->mx[2]; k++)
+    for (int j = 1; j <= p->mx[1]; j++)
+      for (int i = 1; i <= p->mx[0]; i++) {
+        if (tmp[fidx(p, i, j, k)] != 1) continue;
+        int idx[3] = {i, j, k}, lo[3] = {1, 1, 1}, hi[3] = {1, 1, 1}, out = 0;
+        for (int d = 0; d < h->ndims; d++) {
+          lo[d] = idx[d] - ib;
+          hi[d] = idx[d] + ib;
+        }
+        for (int d = 0; d < 3; d++)
+          if (lo[d] < 1 || hi[d] > p->mx[d]) out = 1;
+        if (out) { /* AddTaggedCellToList, :1250-1264 */
+          if (tl->n == tl->cap) {
+            tl->cap = tl->cap ? 2 * tl->cap : 64;
+            tl->c = realloc(tl->c, sizeof(*tl->c) * tl->cap);
+          }
+          for (int d = 0; d < 3; d++) tl->c[tl->n][d] = d < h->ndims ? idx[d] + p->mglobal[d][0] - 1 : 1;
+          tl->n++;
+        } else {
+          for (int c = lo[2]; c <= hi[2]; c++)
+            for (int b = lo[1]; b <= hi[1]; b++)
+              for (int a = lo[0]; a <= hi[0]; a++) fl[fidx(p, a, b, c)] = 1;
+        }
+      }
+  free(tmp);
+}
+
+/* BufferTaggedCells, bsamroutines.f90:1311-1349 */
+static void buffer_tagged(const bsamo_hier* h, const OPatch* p, const int tag[3], int ib, int* fl) {
+  int lo[3] = {1, 1, 1}, hi[3] = {1, 1, 1};
+  for (int d = 0; d < h->ndims; d++) {
+    lo[d] = tag[d] - ib > p->mglobal[d][0] ? tag[d] - ib : p->mglobal[d][0];
+    hi[d] = tag[d] + ib < p->mglobal[d][1] ? tag[d] + ib : p->mglobal[d][1];
+    if (hi[d] < lo[d]) return;
+    lo[d] = lo[d] - p->mglobal[d][0] + 1;
+    hi[d] = hi[d] - p->mglobal[d][0] + 1;
+  }
+  for (int c = lo[2]; c <= hi[2]; c++)
+    for (int b = lo[1]; b <= hi[1]; b++)
+      for (int a = lo[0]; a <= hi[0]; a++) fl[fidx(p, a, b, c)] = 1;
+}
+
+/* GetSignatures, :1608-1632; signature of dimension n over box mb */
+static void signatures(const OPatch* p, const int* fl, int mb[3][2], int nd, int* sig /* [3][maxm+1] */, int maxm) {
+  for (int n = 0; n < nd; n++)
+    for (int i = mb[n][0]; i <= mb[n][1]; i++) {
+      int lo[3], hi[3], s = 0;
+      for (int d = 0; d < 3; d++) { lo[d] = mb[d][0]; hi[d] = mb[d][1]; }
+      lo[n] = hi[n] = i;
+      for (int c = lo[2]; c <= hi[2]; c++)
+        for (int b = lo[1]; b <= hi[1]; b++)
+          for (int a = lo[0]; a <= hi[0]; a++) s += fl[fidx(p, a, b, c)];
+      sig[n * (maxm + 2) + i] = s;
+    }
+}
+
+/* GridFlagRatio, :1635-1660 */
+static double flag_ratio(const OPatch* p, const int* fl, int mb[3][2], int nd) {
+  double total = 1.0;
+  for (int d = 0; d < nd; d++) total = total * (double)(mb[d][1] - mb[d][0] + 1);
+  for (int d = nd; d < 3; d++) mb[d][0] = mb[d][1] = 1;
+  double flagged = 0.0;
+  long long s = 0;
+  for (int c = mb[2][0]; c <= mb[2][1]; c++)
+    for (int b = mb[1][0]; b <= mb[1][1]; b++)
+      for (int a = mb[0][0]; a <= mb[0][1]; a++) s += fl[fidx(p, a, b, c)];
+  flagged = (double)s;
+  return flagged / total;
+}
+
+#define MAXSUBGRIDS 1024 /* nodeinfodef.f90:62 */
+
+/* NewSubGrids, :1408-1605 (modified Berger-Rigoutsos).  Returns the number
+ * of subgrids written to sub[][3][2] (parent index space), or -1 on the
+ * reference's error stops. */
+static int new_sub_grids(const bsamo_hier* h, const OPatch* p, const int* fl, const bsamo_regrid_params* prm,
+                         int (*sub)[3][2]) {
+  int nd = h->ndims, level = p->level;
+  double desfill = prm->desiredfillratio[level];
+  int mgp = prm->minimumgridpoints[level];
+  if (mgp < 4 || mgp % 2) return -1;
+  int mb[3][2];
+  for (int d = 0; d < 3; d++) { mb[d][0] = 1; mb[d][1] = d < nd ? p->mx[d] : 1; }
+  if (flag_ratio(p, fl, mb, nd) < 1.0e-10) return 0;
+  int maxm = 0;
+  for (int d = 0; d < nd; d++) if (p->mx[d] > maxm) maxm = p->mx[d];
+  int* sig = (int*)calloc((size_t)3 * (maxm + 2), sizeof(int));
+  int* dds = (int*)calloc((size_t)3 * (maxm + 2), sizeof(int));
+  static char cansplit[MAXSUBGRIDS + 1];
+  int ngrid = 1;
+  for (int g = 0; g <= MAXSUBGRIDS; g++) cansplit[g] = 1;
+  memcpy(sub[0], mb, sizeof(mb));
+  int igrid = 1;
+  while (ngrid < MAXSUBGRIDS && igrid <= ngrid) {
+    int (*b)[2] = sub[igrid - 1];
+    int npass = 0;
+    while (cansplit[igrid] && npass < 15) {
+      npass++;
+      signatures(p, fl, b, nd, sig, maxm);
+      for (int n = 0; n < nd; n++) { /* trim unflagged edges */
+        int* sg = sig + n * (maxm + 2);
+        int i1 = b[n][0], i2 = b[n][1];
+        while (sg[i1] == 0 && i1 < b[n][1] && i2 - i1 + 1 > mgp) i1++;
+        while (sg[i2] == 0 && i2 > b[n][0] && i2 - i1 + 1 > mgp) i2--;
+        b[n][0] = i1 - imod(i1 + 1, 2);
+        b[n][1] = i2 + imod(i2, 2);
+      }
+      double fill = flag_ratio(p, fl, b, nd);
+      if (fill < desfill) {
+        signatures(p, fl, b, nd, sig, maxm);
+        int isplit[3] = {0, 0, 0}, have = 0;
+        for (int n = 0; n < nd && !have; n++) { /* holes */
+          int* sg = sig + n * (maxm + 2);
+          int i1 = b[n][0], i2 = b[n][1];
+          for (int i = i1 + mgp - 1; i <= i2 - mgp; i += 2) {
+            int m = i - i1 + 1 < i2 - i ? i - i1 + 1 : i2 - i;
+            if (sg[i] == 0 && m >= mgp) {
+              isplit[n] = i;
+              have = 1;
+              break;
+            }
+          }
+        }
+        if (!have) { /* inflection points */
+          for (int n = 0; n < nd; n++) {
+            int *sg = sig + n * (maxm + 2), *dd = dds + n * (maxm + 2);
+            for (int i = b[n][0] + 1; i <= b[n][1] - 1; i++) dd[i] = sg[i - 1] - 2 * sg[i] + sg[i + 1];
+          }
+          int inflect = 0, dist0 = 0;
+          for (int n = 0; n < nd; n++) {
+            int* dd = dds + n * (maxm + 2);
+            int i1 = b[n][0], i2 = b[n][1];
+            for (int i = i1 + mgp; i <= i2 - mgp + 1; i += 2) {
+              int del = abs(dd[i] - dd[i - 1]);
+              if (del > inflect) {
+                inflect = del;
+                isplit[0] = isplit[1] = isplit[2] = 0;
+                isplit[n] = i - 1;
+                have = 1;
+                dist0 = i - i1 < i2 - i + 1 ? i - i1 : i2 - i + 1;
+              } else if (del == inflect && inflect > 0) {
+                int dist1 = i - i1 < i2 - i + 1 ? i - i1 : i2 - i + 1;
+                if (dist1 > dist0) {
+                  isplit[0] = isplit[1] = isplit[2] = 0;
+                  isplit[n] = i - 1;
+                  have = 1;
+                  dist0 = dist1;
+                }
+              }
+            }
+          }
+        }
+        if (have) {
+          for (int n = 0; n < nd; n++) {
+            int m = b[n][1] - isplit[n] < isplit[n] - b[n][0] + 1 ? b[n][1] - isplit[n] : isplit[n] - b[n][0] + 1;
+            if (isplit[n] > 0 && m >= mgp) {
+              ngrid++;
+              cansplit[ngrid] = 1;
+              memcpy(sub[ngrid - 1], b, sizeof(int) * 6);
+              sub[ngrid - 1][n][0] = isplit[n] + 1;
+              b[n][1] = isplit[n];
+              break;
+            }
+          }
+        } else {
+          cansplit[igrid] = 0;
+        }
+      } else {
+        cansplit[igrid] = 0;
+      }
+    }
+    igrid++;
+  }
+  free(sig);
+  free(dds);
+  for (int g = 0; g < ngrid; g++)
+    for (int n = 0; n < nd; n++) { /* the reference's checks, :1565-1595 */
+      int len = sub[g][n][1] - sub[g][n][0] + 1;
+      if (len < mgp || len % 2 || sub[g][n][0] % 2 == 0 || sub[g][n][1] % 2 == 1) return -1;
+    }
+  return ngrid;
+}
+
+/* Patches longer than maxside child cells (maxside/2 parent cells) are cut
+ * into nearly equal even pieces along that dimension (not a reference
+ * feature: it bounds the patch size for the batched kernels). */
+static int split_long(int nd, int maxside, int (*sub)[3][2], int ng, int cap) {
+  if (maxside <= 0) return ng;
+  int P = maxside / 2;
+  for (int g = 0; g < ng; g++)
+    for (int n = 0; n < nd; n++) {
+      int len = sub[g][n][1] - sub[g][n][0] + 1;
+      if (len <= P) continue;
+      int pieces = (len + P - 1) / P;
+      int lo = sub[g][n][0];
+      for (int k = 0; k < pieces; k++) {
+        /* even lengths, the remainder spread from the first piece on */
+        int half = len / 2, base = half / pieces, extra = half % pieces;
+        int plen = 2 * (base + (k < extra ? 1 : 0));
+        int (*t)[2];
+        if (k == 0) t = sub[g];
+        else {
+          if (ng == cap) return -1;
+          memcpy(sub[ng], sub[g], sizeof(int) * 6);
+          t = sub[ng++];
+        }
+        t[n][0] = lo;
+        t[n][1] = lo + plen - 1;
+        lo += plen;
+      }
+    }
+  return ng;
+}
+
+/* BiLinProlongationP1MC / TriLinProlongationP1MC (gridutilities.f90:242-369,
+ * :628-727): a = coarse values with one ghost layer, cn = cmx+2 per
+ * dimension; out = fine values with one ghost layer, fn = 2*cmx+2. */
+static void prolong_mc(int nd, const double* a, const int cmx[3], double* out) {
+  int cn0 = cmx[0] + 2, cn1 = cmx[1] + 2, cn2 = nd == 3 ? cmx[2] + 2 : 1;
+  int fn0 = 2 * cmx[0] + 2, fn1 = 2 * cmx[1] + 2, fn2 = nd == 3 ? 2 * cmx[2] + 2 : 1;
+#define A(i, j, k) a[((size_t)(k) * cn1 + (j)) * cn0 + (i)]
+#define O(i, j, k) out[((size_t)(k) * fn1 + (j)) * fn0 + (i)]
+  double* b = (double*)malloc(sizeof(double) * fn0 * cn1 * cn2);
+#define Bx(i, j, k) b[((size_t)(k) * cn1 + (j)) * fn0 + (i)]
+  for (int k = 0; k < cn2; k++)
+    for (int j = 0; j < cn1; j++)
+      for (int I = 0; I <= cmx[0]; I++) {
+        Bx(2 * I, j, k) = 3.0 * A(I, j, k) + A(I + 1, j, k);
+        Bx(2 * I + 1, j, k) = A(I, j, k) + 3.0 * A(I + 1, j, k);
+      }
+  if (nd == 2) {
+    for (int J = 0; J <= cmx[1]; J++)
+      for (int i = 0; i < fn0; i++) {
+        O(i, 2 * J, 0) = (3.0 * Bx(i, J, 0) + Bx(i, J + 1, 0)) / 16.0;
+        O(i, 2 * J + 1, 0) = (Bx(i, J, 0) + 3.0 * Bx(i, J + 1, 0)) / 16.0;
+      }
+    for (int J = 1; J <= cmx[1]; J++)
+      for (int I = 1; I <= cmx[0]; I++) {
+        double cor = A(I, J, 0) - 0.25 * (O(2 * I, 2 * J, 0) + O(2 * I - 1, 2 * J, 0) + O(2 * I, 2 * J - 1, 0) +
+                                          O(2 * I - 1, 2 * J - 1, 0));
+        O(2 * I, 2 * J, 0) = O(2 * I, 2 * J, 0) + cor;
+        O(2 * I - 1, 2 * J, 0) = O(2 * I - 1, 2 * J, 0) + cor;
+        O(2 * I, 2 * J - 1, 0) = O(2 * I, 2 * J - 1, 0) + cor;
+        O(2 * I - 1, 2 * J - 1, 0) = O(2 * I - 1, 2 * J - 1, 0) + cor;
+      }
+  } else {
+    double* c = (double*)malloc(sizeof(double) * fn0 * fn1 * cn2);
+#define Cy(i, j, k) c[((size_t)(k) * fn1 + (j)) * fn0 + (i)]
+    for (int k = 0; k < cn2; k++)
+      for (int J = 0; J <= cmx[1]; J++)
+        for (int i = 0; i < fn0; i++) {
+          Cy(i, 2 * J, k) = 3.0 * Bx(i, J, k) + Bx(i, J + 1, k);
+          Cy(i, 2 * J + 1, k) = Bx(i, J, k) + 3.0 * Bx(i, J + 1, k);
+        }
+    for (int K = 0; K <= cmx[2]; K++)
+      for (int j = 0; j < fn1; j++)
+        for (int i = 0; i < fn0; i++) {
+          O(i, j, 2 * K) = (3.0 * Cy(i, j, K) + Cy(i, j, K + 1)) / 64.0;
+          O(i, j, 2 * K + 1) = (Cy(i, j, K) + 3.0 * Cy(i, j, K + 1)) / 64.0;
+        }
+    for (int K = 1; K <= cmx[2]; K++)
+      for (int J = 1; J <= cmx[1]; J++)
+        for (int I = 1; I <= cmx[0]; I++) {
+          double cor = A(I, J, K) -
+                       0.125 * (O(2 * I, 2 * J, 2 * K) + O(2 * I - 1, 2 * J, 2 * K) + O(2 * I, 2 * J - 1, 2 * K) +
+                                O(2 * I - 1, 2 * J - 1, 2 * K) + O(2 * I, 2 * J, 2 * K - 1) +
+                                O(2 * I - 1, 2 * J, 2 * K - 1) + O(2 * I, 2 * J - 1, 2 * K - 1) +
+                                O(2 * I - 1, 2 * J - 1, 2 * K - 1));
+          for (int dk = 0; dk < 2; dk++)
+            for (int dj = 0; dj < 2; dj++)
+              for (int di = 0; di < 2; di++)
+                O(2 * I - di, 2 * J - dj, 2 * K - dk) = O(2 * I - di, 2 * J - dj, 2 * K - dk) + cor;
+        }
+    free(c);
+#undef Cy
+  }
+  free(b);
+#undef A
+#undef O
+#undef Bx
+}
+
+/* MakeNewGrid (:1663-1784) + InitFields (:1787-1856); returns the index */
+static int make_new_grid(bsamo_hier* h, int pidx, int mbp[3][2], int id, const bsamo_regrid_params* prm,
+                         bsamo_qinit_fn qinit, void* user) {
+  int nd = h->ndims;
+  int mx[3] = {1, 1, 1}, mg[3][2], mb[3][2], thbc[6];
+  double dx[3] = {0, 0, 0}, xl[3] = {0, 0, 0};
+  const OPatch* par = &h->p[pidx];
+  for (int d = 0; d < 3; d++) {
+    mg[d][0] = mg[d][1] = mb[d][0] = mb[d][1] = 1;
+    if (d >= nd) continue;
+    mx[d] = (mbp[d][1] - mbp[d][0] + 1) * 2;
+    mb[d][0] = mbp[d][0];
+    mb[d][1] = mbp[d][1];
+    int g0 = par->mglobal[d][0] + mbp[d][0] - 1;
+    int g1 = g0 + mbp[d][1] - mbp[d][0];
+    mg[d][0] = (g0 - 1) * 2 + 1;
+    mg[d][1] = g1 * 2;
+    xl[d] = (double)(mbp[d][0] - 1) * par->dx[d] + par->xlower[d];
+    dx[d] = par->dx[d] / 2.0;
+  }
+  for (int f = 0; f < 6; f++) thbc[f] = f < 2 * nd ? INTERNALBC : 10;
+  for (int n = 0; n < nd; n++) {
+    if (par->mthbc[2 * n] < INTERNALBC && mb[n][0] == 1) thbc[2 * n] = par->mthbc[2 * n];
+    if (par->mthbc[2 * n + 1] < INTERNALBC && mb[n][1] == par->mx[n]) thbc[2 * n + 1] = par->mthbc[2 * n + 1];
+  }
+  int c = add_live_patch(h, par->level + 1, id, pidx, mx, mg, mb, thbc, dx, xl);
+  OPatch* ch = &h->p[c];
+  par = &h->p[pidx];
+  if (prm->initial) {
+    qinit(user, ch->level, ch->mx, ch->dx, ch->xlower, ch->q);
+  } else {
+    int cmx[3] = {ch->cmx[0], ch->cmx[1], nd == 3 ? ch->cmx[2] : 0};
+    size_t na = (size_t)(cmx[0] + 2) * (cmx[1] + 2) * (nd == 3 ? cmx[2] + 2 : 1);
+    size_t nfine = (size_t)ch->qn[0] * ch->qn[1] * ch->qn[2];
+    double* a = (double*)malloc(sizeof(double) * na);
+    for (int v = 0; v < h->nrvars; v++) {
+      size_t t = 0;
+      int k0 = nd == 3 ? mb[2][0] - 1 : 1, k1 = nd == 3 ? mb[2][1] + 1 : 1;
+      for (int k = k0; k <= k1; k++)
+        for (int j = mb[1][0] - 1; j <= mb[1][1] + 1; j++)
+          for (int i = mb[0][0] - 1; i <= mb[0][1] + 1; i++) a[t++] = Q(par, i, j, k, v);
+      prolong_mc(nd, a, cmx, ch->q + v * nfine);
+    }
+    free(a);
+  }
+  /* child%rf = parent%rf = child%f = parent%f = 0 (:1773-1776); SetSrc is
+   * empty for CH; child%qold = child%q (:1782) */
+  size_t nf = (size_t)ch->fn[0] * ch->fn[1] * ch->fn[2] * h->nrvars;
+  size_t npf = (size_t)par->fn[0] * par->fn[1] * par->fn[2] * h->nrvars;
+  memset(ch->f, 0, nf * sizeof(double));
+  memset(ch->rf, 0, nf * sizeof(double));
+  memset(par->f, 0, npf * sizeof(double));
+  memset(par->rf, 0, npf * sizeof(double));
+  memcpy(ch->qold, ch->q, sizeof(double) * (size_t)ch->qn[0] * ch->qn[1] * ch->qn[2] * h->nrvars);
+  return c;
+}
+
+/* TransferOverlap (:1919-1951): interior q values of src onto dst */
+static void transfer_overlap(const bsamo_hier* h, const OPatch* src, OPatch* dst) {
+  int lo[3], hi[3];
+  for (int d = 0; d < 3; d++) {
+    lo[d] = src->mglobal[d][0] > dst->mglobal[d][0] ? src->mglobal[d][0] : dst->mglobal[d][0];
+    hi[d] = src->mglobal[d][1] < dst->mglobal[d][1] ? src->mglobal[d][1] : dst->mglobal[d][1];
+    if (hi[d] < lo[d]) return;
+  }
+  for (int v = 0; v < h->nrvars; v++)
+    for (int k = lo[2]; k <= hi[2]; k++)
+      for (int j = lo[1]; j <= hi[1]; j++)
+        for (int i = lo[0]; i <= hi[0]; i++)
+          Q(dst, i - dst->mglobal[0][0] + 1, j - dst->mglobal[1][0] + 1, k - dst->mglobal[2][0] + 1, v) =
+              Q(src, i - src->mglobal[0][0] + 1, j - src->mglobal[1][0] + 1, k - src->mglobal[2][0] + 1, v);
+}
+
+int bsamo_regrid(const bsamo_hier* old, const bsamo_regrid_params* prm, bsamo_qinit_fn qinit, void* user,
+                 bsamo_hier** out) {
+  if (!old || !old->committed || !prm || !out) return -1;
+  if (prm->maxlevel < 0 || prm->maxlevel > MAXDEPTH || (prm->initial && !qinit)) return -2;
+  double params[5] = {old->dt, old->eps, old->gamma, old->lambda, old->czero};
+  bsamo_hier* h = NULL;
+  int rc = bsamo_create(old->ndims, old->nrvars, old->mbc, old->problem, params, 5, old->qpo, &h);
+  if (rc) return rc;
+  for (int n = 0; n < old->np; n++) { /* the root and the levels below persist */
+    const OPatch* p = &old->p[n];
+    if (p->level > 0) continue;
+    int mg[6], mb[6];
+    for (int d = 0; d < 3; d++) {
+      mg[2 * d] = p->mglobal[d][0]; mg[2 * d + 1] = p->mglobal[d][1];
+      mb[2 * d] = p->mbounds[d][0]; mb[2 * d + 1] = p->mbounds[d][1];
+    }
+    bsamo_patch_add(h, p->level, p->id, p->parent_id, p->mx, mg, mb, p->mthbc, p->dx, p->xlower);
+  }
+  if ((rc = bsamo_commit(h))) { bsamo_destroy(h); return rc; }
+  for (int n = 0; n < h->np; n++) {
+    OPatch* p = &h->p[n];
+    const OPatch* o = find_patch(old, p->id);
+    size_t nq = (size_t)p->qn[0] * p->qn[1] * p->qn[2] * h->nrvars;
+    size_t nc = (size_t)p->cn[0] * p->cn[1] * p->cn[2] * h->nrvars;
+    size_t nf = (size_t)p->fn[0] * p->fn[1] * p->fn[2] * h->nrvars;
+    memcpy(p->q, o->q, nq * sizeof(double));
+    memcpy(p->qold, o->qold, nq * sizeof(double));
+    memcpy(p->qc, o->qc, nc * sizeof(double));
+    memcpy(p->f, o->f, nf * sizeof(double));
+    memcpy(p->rf, o->rf, nf * sizeof(double));
+    memcpy(p->ftmp, o->ftmp, nf * sizeof(double));
+  }
+  int next_id = prm->first_id;
+  int (*sub)[3][2] = malloc(sizeof(*sub) * 4 * MAXSUBGRIDS);
+  int level;
+  for (level = 0; level < prm->maxlevel && nlev(h, level) > 0; level++) { /* AMR(level), :966-991 */
+    set_ghost(h, level, 0);
+    int np = nlev(h, level);
+    int** fl = (int**)calloc(np, sizeof(int*));
+    TagList tl = {0, 0, NULL};
+    int ib = prm->ibuffer[level];
+    for (int a = 0; a < np; a++) { /* ErrFlag, :1059-1131 */
+      OPatch* p = lev_patch(h, level, a);
+      fl[a] = (int*)calloc((size_t)p->mx[0] * p->mx[1] * p->mx[2], sizeof(int));
+      tag_patch(h, p, prm, fl[a]);
+      if (ib > 0) buffer_and_list(h, p, ib, fl[a], &tl);
+    }
+    if (tl.n > 0) { /* InflateEdgeTags, :1267-1308 */
+      int poff[13][3];
+      if (h->periodic) periodic_offsets(h, level, poff);
+      for (int t = tl.n - 1; t >= 0; t--) {
+        for (int a = 0; a < np; a++) buffer_tagged(h, lev_patch(h, level, a), tl.c[t], ib, fl[a]);
+        if (h->periodic)
+          for (int pol = -1; pol <= 1; pol += 2)
+            for (int o = 0; o < h->nperoff; o++) {
+              int c[3];
+              for (int d = 0; d < 3; d++) c[d] = tl.c[t][d] + pol * poff[o][d];
+              for (int a = 0; a < np; a++) buffer_tagged(h, lev_patch(h, level, a), c, ib, fl[a]);
+            }
+      }
+    }
+    free(tl.c);
+    int first_new = h->np;
+    for (int a = 0; a < np && rc == 0; a++) { /* GridAdapt -> RefineGrid, :1366-1405 */
+      int pidx = h->lev_list[level + MAXDEPTH][a];
+      int ng = new_sub_grids(h, &h->p[pidx], fl[a], prm, sub);
+      if (ng < 0) { rc = -5; break; }
+      ng = split_long(h->ndims, prm->maxside, sub, ng, 4 * MAXSUBGRIDS);
+      if (ng < 0) { rc = -5; break; }
+      for (int g = 0; g < ng; g++) make_new_grid(h, pidx, sub[g], next_id++, prm, qinit, user);
+    }
+    for (int a = 0; a < np; a++) free(fl[a]);
+    free(fl);
+    if (rc) break;
+    /* TransferValues (:1859-1951): previous level-(l+1) grids onto new ones */
+    for (int c = first_new; c < h->np; c++)
+      for (int n = 0; n < old->np; n++)
+        if (old->p[n].level == level + 1) transfer_overlap(h, &old->p[n], &h->p[c]);
+  }
+  free(sub);
+  if (rc) { bsamo_destroy(h); return rc; }
+  if (nlev(h, level) > 0) set_ghost(h, level, 0); /* AMR(finest) */
+  *out = h;
+  return 0;
+}

@@ -93,6 +93,36 @@ int bsamo_time_step(bsamo_hier* h, int first, int finestlevel, int minlevel,
                     int updateauxfreq, int errortype, int* ncycles,
                     double* residuals);
 
+/* AMR regrid: the AMR(rootlevel) pass that TakeTimeSteps runs before every
+ * step (bsamroutines.f90:657-689, :966-1951).  Level by level from the root:
+ * SetGhost(l,0), tag (CH SetErrFlagsUser2D/3D or the gradient rule), buffer
+ * the tags (BufferAndList, InflateEdgeTags with periodic images), cluster
+ * the tags of each patch with the modified Berger-Rigoutsos algorithm
+ * (NewSubGrids), make the children (MakeNewGrid), fill them (InitFields:
+ * the initial condition, or mass-corrected bilinear/trilinear prolongation
+ * from the parent) and copy the previous level-(l+1) values over them
+ * (TransferValues).  The result is a new committed hierarchy: the levels
+ * <= 0 of `old` (all fields copied) and the new levels > 0. */
+#define BSAMO_TAG_CH 0       /* CH/problem.f90:248-308: second differences of phi */
+#define BSAMO_TAG_GRADIENT 1 /* |grad phi| h > qtolerance, central differences */
+typedef struct {
+  int maxlevel;
+  int tagging;
+  int initial;  /* new grids take the initial condition (InitFields :1804) */
+  int maxside;  /* 0, or split new patches to at most maxside cells per side */
+  int first_id; /* ids of the new patches: first_id, first_id + 1, ... */
+  int ibuffer[11];
+  int minimumgridpoints[11];
+  double qtolerance[11];
+  double desiredfillratio[11];
+} bsamo_regrid_params;
+/* fill the interior of q (ghosted Fortran layout) of a new patch */
+typedef void (*bsamo_qinit_fn)(void* user, int level, const int* mx,
+                               const double* dx, const double* xlower,
+                               double* q);
+int bsamo_regrid(const bsamo_hier* old, const bsamo_regrid_params* prm,
+                 bsamo_qinit_fn qinit, void* user, bsamo_hier** out);
+
 /* seeded inputs: U(-1,1) from splitmix64 on a global cell index */
 double bsamo_uniform_pm1(unsigned long long seed, unsigned long long gidx);
 

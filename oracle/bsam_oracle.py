@@ -17,6 +17,48 @@ PROBLEM = {"ch": 1, "biogrowth": 2}
 _lib = None
 
 
+class RegridParams(ctypes.Structure):
+    """bsamo_regrid_params (the same layout as bsamg_regrid_params)."""
+    _fields_ = [("maxlevel", ctypes.c_int), ("tagging", ctypes.c_int), ("initial", ctypes.c_int),
+                ("maxside", ctypes.c_int), ("first_id", ctypes.c_int), ("ibuffer", ctypes.c_int * 11),
+                ("minimumgridpoints", ctypes.c_int * 11), ("qtolerance", ctypes.c_double * 11),
+                ("desiredfillratio", ctypes.c_double * 11)]
+
+
+TAGGING = {"ch": 0, "gradient": 1}
+QINIT = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                         ctypes.POINTER(ctypes.c_double))
+
+
+def regrid_params(maxlevel, tagging="ch", initial=False, maxside=0, first_id=1000, ibuffer=1,
+                  minimumgridpoints=4, qtolerance=1e-2, desiredfillratio=0.9):
+    """RegridParams with one value for every level (lists are taken per level)."""
+    r = RegridParams()
+    r.maxlevel, r.tagging, r.initial, r.maxside, r.first_id = (maxlevel, TAGGING[tagging], int(initial), maxside,
+                                                              first_id)
+    per = lambda x, l: x[l] if isinstance(x, (list, tuple)) else x
+    for l in range(11):
+        r.ibuffer[l] = per(ibuffer, l)
+        r.minimumgridpoints[l] = per(minimumgridpoints, l)
+        r.qtolerance[l] = per(qtolerance, l)
+        r.desiredfillratio[l] = per(desiredfillratio, l)
+    return r
+
+
+def make_qinit(fn, ndims, nrvars):
+    """C callback around fn(level, mx, dx, xlower) -> ghosted Fortran-layout
+    array of the new patch (only its interior is used)."""
+    def cb(user, level, mx, dx, xl, q):
+        m = [mx[d] for d in range(3)]
+        a = np.asarray(fn(level, m[:ndims], [dx[d] for d in range(3)][:ndims], [xl[d] for d in range(3)][:ndims]),
+                       dtype=np.float64).ravel(order="F")
+        n = int(np.prod([v + 2 for v in m[:ndims]])) * nrvars
+        assert a.size == n, (a.size, n)
+        ctypes.memmove(q, a.ctypes.data, n * 8)
+    return QINIT(cb)
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -45,6 +87,7 @@ def lib():
         L.bsamo_residual_norm.argtypes = [P, I, I, DP]
         L.bsamo_multigrid_iterations.argtypes = [P, I, I, I, I, D, I, I, IP, DP]
         L.bsamo_time_step.argtypes = [P, I, I, I, I, I, D, I, I, IP, DP]
+        L.bsamo_regrid.argtypes = [P, ctypes.POINTER(RegridParams), QINIT, P, ctypes.POINTER(P)]
         L.bsamo_uniform_pm1.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong]
         L.bsamo_uniform_pm1.restype = D
         _lib = L
@@ -166,6 +209,20 @@ class OracleHierarchy:
                                      maxvcycles, tol, updateauxfreq, errortype, ctypes.byref(n),
                                      res), "time_step")
         return n.value, list(res)[: n.value]
+
+
+def _wrap(h, ndims, nrvars):
+    o = OracleHierarchy.__new__(OracleHierarchy)
+    o.h, o.ndims, o.nrvars, o.patches = h, ndims, nrvars, []
+    return o
+
+
+def regrid(old, params, qinit=None):
+    """AMR regrid of an oracle hierarchy (bsamo_regrid); returns a new one."""
+    cb = make_qinit(qinit, old.ndims, old.nrvars) if qinit is not None else QINIT()
+    h = ctypes.c_void_p()
+    _check(lib().bsamo_regrid(old.h, ctypes.byref(params), cb, None, ctypes.byref(h)), "regrid")
+    return _wrap(h, old.ndims, old.nrvars)
 
 
 def uniform_pm1(seed, gidx):
