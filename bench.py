@@ -40,6 +40,17 @@ WORKLOADS = {
                      mean=0.0, amp=0.05, seed=20240503,
                      desc="2D Cahn-Hilliard 128^2 periodic, eps=0.01, dt=1e-3, V(2,2), resid<=1e-9"),
 }
+# cfg2: adaptive mesh rebuilt before every step by the regrid (TakeTimeSteps'
+# AMR pass).  With eps = 0.01 the interface gradient is 1/(sqrt(2) eps) = 71,
+# so |grad phi| h exceeds 0.5 on levels 0-1 only; 0.25 lets three levels form.
+AMR_WORKLOADS = {
+    "ch2d-amr": dict(ndims=2, n=64, minlevel=-5, mthbc=[2, 2, 2, 2, 10, 10], eps=0.01, dt=1e-3, tol=1e-9,
+                     maxlevel=3, tagging="gradient", qtol=0.25, ibuffer=1, mgp=4, fill=0.9, maxside=64,
+                     radius=0.25, noise=0.01, seed=20240503,
+                     desc="2D Cahn-Hilliard AMR: 64^2 periodic root + 3 levels (|grad phi| h > 0.25, "
+                          "Berger-Rigoutsos, <= 64 cells per side, regrid every step), circle r=0.25 + 1% "
+                          "noise, eps=0.01, dt=1e-3, V(2,2), resid<=1e-9"),
+}
 NSMOOTH = 2
 MAXV = 30
 
@@ -292,6 +303,198 @@ def reference_arm(args, w, dist):
     print(json.dumps(line), flush=True)
 
 
+def amr_params(api, w, step):
+    return api.regrid_params(w["maxlevel"], tagging=w["tagging"], initial=step == 0, maxside=w["maxside"],
+                             first_id=100000 * (step + 1), ibuffer=w["ibuffer"], minimumgridpoints=w["mgp"],
+                             qtolerance=w["qtol"], desiredfillratio=w["fill"])
+
+
+def amr_run(api, make_root, w, mode, steps, warmup, use_events=True):
+    """warmup + timed steps of regrid + time step; returns timings, V-cycle
+    counts and the final mesh."""
+    qinit = api_qinit(w)
+    h = make_root()
+    wall, solve, vc = [], [], []
+    t_start = None
+    for s in range(warmup + steps):
+        if s == warmup:
+            if use_events:
+                h.sync()
+            t_start = time.perf_counter()
+        t0 = time.perf_counter()
+        old = h
+        h = h.regrid(amr_params(api, w, s), qinit if s == 0 else None)
+        if use_events:
+            old.close()
+        t1 = time.perf_counter()
+        fin = max(p["level"] for p in h.patch_table())
+        kw = dict(mode=mode, strict=True) if use_events else {}
+        n, res = h.time_step(s == 0, fin, w["minlevel"], NSMOOTH, MAXV, w["tol"], **kw)
+        if use_events:
+            h.sync()
+        t2 = time.perf_counter()
+        if s >= warmup:
+            wall.append(t2 - t0)
+            solve.append(t2 - t1)
+        vc.append(n)
+    total = time.perf_counter() - t_start
+    return dict(total_s=total, wall=wall, solve=solve, vcycles=vc[warmup:], h=h)
+
+
+def api_qinit(w):
+    import __graft_entry__ as ge
+    return ge.load_package().initial.ch_circle_patch(w["eps"], w["seed"], radius=w["radius"], noise=w["noise"])
+
+
+def mesh_stats(tab):
+    levels = {}
+    for p in tab:
+        if p["level"] < 0:
+            continue
+        d = levels.setdefault(p["level"], {"patches": 0, "cells": 0})
+        d["patches"] += 1
+        d["cells"] += int(np.prod(p["mx"][:2]))
+    sides = [max(p["mx"][:2]) for p in tab if p["level"] > 0]
+    hist = {}
+    for b in (8, 16, 32, 64, 128):
+        hist[f"<={b}"] = sum(1 for x in sides if x <= b) - sum(v for v in hist.values())
+    return {"levels": levels, "patch_side_histogram": hist}
+
+
+def amr_arm(args, w, dist):
+    """--workload ch2d-amr: cfg2.  Each step is the reference's TakeTimeSteps
+    body with AMR: the regrid (host clustering, new device hierarchy) then
+    CopyQToQold + MultigridIterations.  Timed on the host clock with the
+    device synchronised after each step, because the regrid is host work."""
+    import __graft_entry__ as ge
+    ge._load_build_module().build()
+    pkg = ge.load_package()
+    ctx = pkg.Context(dist.local)
+    nd, n = w["ndims"], w["n"]
+
+    def make_root():
+        h = pkg.Hierarchy(ctx, nd, 2, "ch", [w["dt"], w["eps"]])
+        h.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
+        h.commit()
+        h.put(0, "q", api_qinit(w)(0, [n] * nd, [1.0 / n] * nd, [0.0] * nd))
+        return h
+
+    out = {}
+    for mode in ("mixed", "fp64"):
+        dist.barrier()
+        r = amr_run(pkg, make_root, w, mode, args.steps, args.warmup)
+        r["tab"] = r["h"].patch_table()
+        out[mode] = r
+    m, f = out["mixed"], out["fp64"]
+    same_mesh = [(p["level"], p["mglobal"]) for p in m["tab"]] == [(p["level"], p["mglobal"]) for p in f["tab"]]
+    err = None
+    if same_mesh:
+        worst = 0.0
+        for p in f["tab"]:
+            if p["level"] < 0:
+                continue
+            a, b = m["h"].get(p["id"], "q"), f["h"].get(p["id"], "q")
+            k = a.size // 2
+            worst = max(worst, float(np.max(np.abs(a[:k] - b[:k])) / np.max(np.abs(b[:k]))))
+        err = worst
+    t_m = dist.max(m["total_s"])
+    t_f = dist.max(f["total_s"])
+    value = dist.ws * args.steps / t_m
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": dist.ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_m / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded splitmix64 noise on a tanh circle)",
+        "config": {"workload": args.workload, "desc": w["desc"], "regrid": "every step (host clustering)",
+                   "l2": "L2-resident, launch- and host-bound (2D, < 1 MB per level)"},
+        "p50_ms": 1e3 * pct(m["wall"], 50), "p99_ms": 1e3 * pct(m["wall"], 99),
+        "regrid_ms_per_step": 1e3 * (statistics.mean(m["wall"]) - statistics.mean(m["solve"])),
+        "solve_ms_per_step": 1e3 * statistics.mean(m["solve"]),
+        "vcycles_per_step": statistics.mean(m["vcycles"]),
+        "plain_fp64": {"value": dist.ws * args.steps / t_f, "unit": "steps/s", "ms_per_step": 1e3 * t_f / args.steps,
+                       "solve_ms_per_step": 1e3 * statistics.mean(f["solve"]),
+                       "vcycles_per_step": statistics.mean(f["vcycles"])},
+        "speedup_mixed_vs_fp64": t_f / t_m,
+        "error_vs_fp64": {"max_rel_phi": err, "same_mesh": same_mesh, "after_steps": args.warmup + args.steps},
+        "mesh": mesh_stats(f["tab"]),
+        "timing": "host clock around regrid + time step, device synchronised after each step",
+    }
+    if not args.no_cpu_baseline:
+        from oracle import bsam_oracle as om
+
+        def oracle_root():
+            o = om.OracleHierarchy(nd, 2, "ch", [w["dt"], w["eps"]])
+            o.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
+            o.commit()
+            o.put(0, "q", api_qinit(w)(0, [n] * nd, [1.0 / n] * nd, [0.0] * nd))
+            return o
+
+        class OAPI:  # the oracle behind the same regrid/time-step calls
+            regrid_params = staticmethod(om.regrid_params)
+
+        def wrap(o):
+            class W:
+                def __init__(self, o):
+                    self.o = o
+
+                def regrid(self, prm, qinit=None):
+                    return W(om.regrid(self.o, prm, qinit))
+
+                def patch_table(self):
+                    return self.o.patch_table()
+
+                def time_step(self, *a, **k):
+                    return self.o.time_step(*a, **k)
+            return W(o)
+
+        ns = 3
+        r = amr_run(OAPI, lambda: wrap(oracle_root()), w, "fp64", ns, 1, use_events=False)
+        line["cpu_baseline"] = {"value": ns / r["total_s"], "unit": "steps/s", "cores": 1, "kind": "port",
+                                "sample": f"oracle (C restatement, 1 thread): regrid + time step, steps 2-{ns + 1} "
+                                          f"of the same run ({r['total_s']:.1f} s)"}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    for r in out.values():
+        r["h"].close()
+    ctx.close()
+
+
+def amr_reference_arm(args, w, dist):
+    """--impl reference for the AMR workload: the oracle (the reference
+    algorithm restated in C; the Fortran cannot be built here) runs the
+    same steps -- regrid, then the time step -- on one host core."""
+    if dist.rank != 0:
+        return
+    from oracle import bsam_oracle as om
+    nd, n = w["ndims"], w["n"]
+    qinit = api_qinit(w)
+    o = om.OracleHierarchy(nd, 2, "ch", [w["dt"], w["eps"]])
+    o.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
+    o.commit()
+    o.put(0, "q", qinit(0, [n] * nd, [1.0 / n] * nd, [0.0] * nd))
+    ts, vc = [], []
+    for s in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        o = om.regrid(o, amr_params(om, w, s), qinit if s == 0 else None)
+        fin = max(p["level"] for p in o.patch_table())
+        nv, _ = o.time_step(s == 0, fin, w["minlevel"], NSMOOTH, MAXV, w["tol"])
+        if s >= args.warmup:
+            ts.append(time.perf_counter() - t)
+            vc.append(nv)
+    value = len(ts) / sum(ts)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(ts),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded splitmix64 noise on a tanh circle)",
+        "config": {"workload": args.workload, "desc": w["desc"]},
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": 1, "kind": "port",
+                         "sample": "every step in full: regrid + CopyQToQold + MultigridIterations"},
+        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "vcycles_per_step": statistics.mean(vc),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def serve_arm(args, dist):
     """--workload serve: the serving configuration.  Poisson arrivals (mean
     200/s, seeded) of independent CH requests, replayed in real time against
@@ -333,7 +536,7 @@ def main():
     ap.add_argument("--steps", type=int, default=17)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ch3d-256", choices=list(WORKLOADS) + ["serve"])
+    ap.add_argument("--workload", default="ch3d-256", choices=list(WORKLOADS) + list(AMR_WORKLOADS) + ["serve"])
     ap.add_argument("--serve-slots", type=int, default=32)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -347,6 +550,14 @@ def main():
                                   "the reference (a single serial solve per run)"}), flush=True)
         else:
             serve_arm(args, dist)
+        dist.close()
+        return
+    if args.workload in AMR_WORKLOADS:
+        w = AMR_WORKLOADS[args.workload]
+        if args.impl == "reference":
+            amr_reference_arm(args, w, dist)
+        else:
+            amr_arm(args, w, dist)
         dist.close()
         return
     w = WORKLOADS[args.workload]

@@ -496,8 +496,10 @@ struct Emitter {
 
 }  // namespace
 
-std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std::vector<int>& stage_off) {
-  Emitter E(H);
+namespace {
+
+// the writer sequence of SetGhost(level, ipass), in the reference's order
+void emit_set_ghost(const Hier& H, int level, int ipass, Emitter& E) {
   const LevelT& L = H.L(level);
   const std::vector<int>& ps = L.patches;
   int n = (int)ps.size();
@@ -514,8 +516,19 @@ std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std:
     if (level > 0) {
       int poff[13][3];
       E.periodic_offsets(level, poff);
+      // Only patches within 2*mbc of the domain edge can meet another
+      // patch's periodic image (for offset +N in dimension d the ghost boxes
+      // meet only if (N - hi_a) + (lo_b - 1) <= 2*mbc); other pairs emit
+      // nothing, so skipping them leaves the operation sequence unchanged.
+      std::vector<char> edge(n, 0);
+      for (int a = 0; a < n; a++) {
+        const HostPatch& P = H.patches[ps[a]];
+        for (int d = 0; d < H.ndims; d++)
+          if (P.mglobal[d][0] - 1 <= 2 * H.mbc || H.mxmax[level][d] - P.mglobal[d][1] <= 2 * H.mbc) edge[a] = 1;
+      }
       for (int a = 0; a < n; a++)
         for (int b = a + 1; b < n; b++)
+          if (edge[a] && edge[b])
           for (int pol = -1; pol <= 1; pol += 2)
             for (int o = 0; o < H.nperoff; o++) {
               int off[3] = {pol * poff[o][0], pol * poff[o][1], pol * poff[o][2]};
@@ -524,47 +537,75 @@ std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std:
     }
   }
   for (int a = 0; a < n; a++) E.physical_bc(ps[a]);
+}
 
-  // pass 1: drop writes overwritten before any read
+}  // namespace
+
+std::vector<GhostOp> set_ghost_sequence(const Hier& H, int level, int ipass) {
+  Emitter E(H);
+  emit_set_ghost(H, level, ipass, E);
+  std::vector<GhostOp> res(E.out.size());
+  for (size_t x = 0; x < E.out.size(); x++) res[x] = E.out[x].op;
+  return res;
+}
+
+std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std::vector<int>& stage_off) {
+  Emitter E(H);
+  emit_set_ghost(H, level, ipass, E);
+  // Cells are keyed by patch and cell offset; the passes below use flat
+  // arrays over the ghosted cells of the patches the operations touch.
   std::vector<Em>& ops = E.out;
   int m = (int)ops.size();
+  std::unordered_map<int, long long> base;
+  long long slots = 0;
+  auto slot_base = [&](int p) {
+    auto it = base.find(p);
+    if (it != base.end()) return it->second;
+    const HostPatch& P = H.patches[p];
+    long long b = slots;
+    slots += (long long)P.qn[0] * P.qn[1] * P.qn[2];
+    base[p] = b;
+    return b;
+  };
+  std::vector<long long> dkey(m), skey(2 * (size_t)m);
+  for (int x = 0; x < m; x++) {
+    dkey[x] = slot_base((int)(ops[x].dst >> 32)) + (uint32_t)ops[x].dst;
+    for (int s = 0; s < ops[x].nsrc; s++)
+      skey[2 * (size_t)x + s] = slot_base((int)(ops[x].src[s] >> 32)) + (uint32_t)ops[x].src[s];
+  }
+  // pass 1: drop writes overwritten before any read
   std::vector<char> dead(m, 0), readf(m, 0);
-  std::unordered_map<int64_t, int> last;
-  last.reserve(m * 2 + 16);
+  std::vector<int> last(slots, -1);
   for (int x = 0; x < m; x++) {
     for (int s = 0; s < ops[x].nsrc; s++) {
-      auto it = last.find(ops[x].src[s]);
-      if (it != last.end()) readf[it->second] = 1;
+      int w = last[skey[2 * (size_t)x + s]];
+      if (w >= 0) readf[w] = 1;
     }
-    auto it = last.find(ops[x].dst);
-    if (it != last.end() && !readf[it->second]) dead[it->second] = 1;
-    last[ops[x].dst] = x;
+    int w = last[dkey[x]];
+    if (w >= 0 && !readf[w]) dead[w] = 1;
+    last[dkey[x]] = x;
   }
-  // pass 2: stage = 1 + latest conflicting live predecessor
-  std::unordered_map<int64_t, int> wst, rst;
-  wst.reserve(m * 2 + 16);
-  rst.reserve(m * 2 + 16);
-  std::vector<int> stage(m, -1);
+  // pass 2: stage = 1 + latest conflicting live predecessor (wst: stage of
+  // the last write of a cell, rst: latest stage reading it since)
+  std::vector<int> wst(slots, -1), rst(slots, -1), stage(m, -1);
   int nst = 0;
   for (int x = 0; x < m; x++) {
     if (dead[x]) continue;
     int st = 0;
     for (int s = 0; s < ops[x].nsrc; s++) {
-      auto it = wst.find(ops[x].src[s]);
-      if (it != wst.end()) st = std::max(st, it->second + 1);
+      int w = wst[skey[2 * (size_t)x + s]];
+      if (w >= 0) st = std::max(st, w + 1);
     }
-    auto r = rst.find(ops[x].dst);
-    if (r != rst.end()) st = std::max(st, r->second + 1);
-    auto w = wst.find(ops[x].dst);
-    if (w != wst.end()) st = std::max(st, w->second + 1);
+    long long d = dkey[x];
+    if (rst[d] >= 0) st = std::max(st, rst[d] + 1);
+    if (wst[d] >= 0) st = std::max(st, wst[d] + 1);
     stage[x] = st;
     for (int s = 0; s < ops[x].nsrc; s++) {
-      auto it = rst.find(ops[x].src[s]);
-      if (it == rst.end()) rst[ops[x].src[s]] = st;
-      else it->second = std::max(it->second, st);
+      int& r = rst[skey[2 * (size_t)x + s]];
+      r = std::max(r, st);
     }
-    wst[ops[x].dst] = st;
-    rst.erase(ops[x].dst);
+    wst[d] = st;
+    rst[d] = -1;
     nst = std::max(nst, st + 1);
   }
   std::vector<GhostOp> res;

@@ -45,6 +45,9 @@ struct LevelT {
 struct Hier;
 // Inputs of the ghost compiler.
 std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std::vector<int>& stage_off);
+// the same writes unprocessed, in the reference's order (for sequential
+// execution on the host)
+std::vector<GhostOp> set_ghost_sequence(const Hier& H, int level, int ipass);
 
 struct Hier {
   bsamg_ctx* ctx = nullptr;

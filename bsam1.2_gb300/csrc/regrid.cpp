@@ -61,14 +61,13 @@ int host_tables(const Model& M, Hier& T) {
   return build_tables(T);
 }
 
-// SetGhost(level, 0) on the model's host arrays: the compiled ghost program
-// of the level, stage by stage (the operations of a stage are independent)
+// SetGhost(level, 0) on the model's host arrays: the level's writer
+// sequence executed in order
 int host_set_ghost(Model& M, int level) {
   Hier T;
   int r = host_tables(M, T);
   if (r) return r;
-  std::vector<int> stage_off;
-  std::vector<GhostOp> ops = compile_set_ghost(T, level, 0, stage_off);
+  std::vector<GhostOp> ops = set_ghost_sequence(T, level, 0);
   const double a1 = -01.0 / 05.0, a2 = 02.0 / 03.0, a3 = 08.0 / 15.0;   // boundary.f90:54-63
   const double b1 = 05.0 / 32.0, b2 = 15.0 / 16.0, b3 = -03.0 / 32.0;
   const double c1 = 09.0 / 16.0, c2 = 03.0 / 16.0, c3 = 03.0 / 16.0, c4 = 01.0 / 16.0;
@@ -470,13 +469,6 @@ void transfer_overlap(int nrvars, const HostPatch& S, const std::vector<double>&
         for (int i = lo[0]; i <= hi[0]; i++) dq[v * ndd + at(D, i, j, k)] = sq[v * ns + at(S, i, j, k)];
 }
 
-int download(const Hier& H, int idx, std::vector<double>& out, long long off) {
-  const HostPatch& P = H.patches[idx];
-  out.resize((size_t)P.sq * H.nrvars);
-  cudaError_t e = cudaMemcpyAsync(out.data(), H.pool + off, out.size() * sizeof(double), cudaMemcpyDeviceToHost, H.s);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(regrid download)");
-  return BSAMG_OK;
-}
 
 }  // namespace
 
@@ -487,22 +479,31 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   if (r) return r;
   int nd = H.ndims, nv = H.nrvars;
   Model M(H);
-  // the root and the levels below persist; q of level 0 comes to the host
+  // one copy of the whole q region (every patch, ghosts included)
+  std::vector<double> qreg((size_t)H.q_len);
+  cudaError_t ce = cudaMemcpyAsync(qreg.data(), H.pool + H.q_region, qreg.size() * sizeof(double),
+                                   cudaMemcpyDeviceToHost, H.s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(regrid download)");
+  ce = cudaStreamSynchronize(H.s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize(regrid)");
+  auto slice = [&](int n) {
+    const HostPatch& P = H.patches[n];
+    const double* b = qreg.data() + (P.oq - H.q_region);
+    return std::vector<double>(b, b + (size_t)P.sq * nv);
+  };
+  // the root and the levels below persist; q of level 0 is regridded on the host
   for (size_t n = 0; n < H.patches.size(); n++) {
     const HostPatch& P = H.patches[n];
     if (P.level > 0) continue;
     M.g.push_back(P);
     M.src_idx.push_back((int)n);
-    M.q.emplace_back();
+    M.q.push_back(P.level == 0 ? slice((int)n) : std::vector<double>());
     M.qold.emplace_back();
-    if (P.level == 0 && (r = download(H, (int)n, M.q.back(), P.oq))) return r;
   }
   // previous refinement levels, for TransferValues
   std::vector<std::vector<double>> oldq(H.patches.size());
   for (size_t n = 0; n < H.patches.size(); n++)
-    if (H.patches[n].level > 0 && (r = download(H, (int)n, oldq[n], H.patches[n].oq))) return r;
-  cudaError_t ce = cudaStreamSynchronize(H.s);
-  if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize(regrid)");
+    if (H.patches[n].level > 0) oldq[n] = slice((int)n);
 
   int next_id = prm.first_id;
   int level;
@@ -589,24 +590,33 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   }
   if ((r = bsamg_commit(nh))) return fail(r);
   Hier& N = *nh;
+  // q: one image of the new q region; qold: one image (new patches) and a
+  // device-to-device copy for the persisting levels <= 0
+  std::vector<double> qimg((size_t)N.q_len, 0.0), oimg((size_t)N.q_len, 0.0);
   for (size_t p = 0; p < M.g.size(); p++) {
     const HostPatch& D = N.patches[p];
-    size_t bytes = (size_t)D.sq * nv * sizeof(double);
-    cudaError_t e;
-    if (M.src_idx[p] >= 0 && M.g[p].level < 0) {  // unchanged below the root
+    double* dq = qimg.data() + (D.oq - N.q_region);
+    size_t n = (size_t)D.sq * nv;
+    if (M.src_idx[p] >= 0 && M.g[p].level < 0) {
       const HostPatch& S = H.patches[M.src_idx[p]];
-      e = cudaMemcpyAsync(N.pool + D.oq, H.pool + S.oq, bytes, cudaMemcpyDeviceToDevice, N.s);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(N.pool + D.oqold, H.pool + S.oqold, bytes, cudaMemcpyDeviceToDevice, N.s);
-    } else if (M.src_idx[p] >= 0) {  // the root: new ghosts, same qold
-      const HostPatch& S = H.patches[M.src_idx[p]];
-      e = cudaMemcpyAsync(N.pool + D.oq, M.q[p].data(), bytes, cudaMemcpyHostToDevice, N.s);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(N.pool + D.oqold, H.pool + S.oqold, bytes, cudaMemcpyDeviceToDevice, N.s);
+      std::memcpy(dq, qreg.data() + (S.oq - H.q_region), n * sizeof(double));
     } else {
-      e = cudaMemcpyAsync(N.pool + D.oq, M.q[p].data(), bytes, cudaMemcpyHostToDevice, N.s);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(N.pool + D.oqold, M.qold[p].data(), bytes, cudaMemcpyHostToDevice, N.s);
+      std::memcpy(dq, M.q[p].data(), n * sizeof(double));
     }
-    if (e != cudaSuccess) return fail(cuda_fail(e, "cudaMemcpyAsync(regrid upload)"));
+    if (M.src_idx[p] < 0) std::memcpy(oimg.data() + (D.oq - N.q_region), M.qold[p].data(), n * sizeof(double));
   }
+  ce = cudaMemcpyAsync(N.pool + N.q_region, qimg.data(), qimg.size() * sizeof(double), cudaMemcpyHostToDevice, N.s);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(N.pool + N.qold_region, oimg.data(), oimg.size() * sizeof(double), cudaMemcpyHostToDevice,
+                         N.s);
+  for (size_t p = 0; p < M.g.size() && ce == cudaSuccess; p++)
+    if (M.src_idx[p] >= 0) {
+      const HostPatch& D = N.patches[p];
+      const HostPatch& S = H.patches[M.src_idx[p]];
+      ce = cudaMemcpyAsync(N.pool + D.oqold, H.pool + S.oqold, (size_t)D.sq * nv * sizeof(double),
+                           cudaMemcpyDeviceToDevice, N.s);
+    }
+  if (ce != cudaSuccess) return fail(cuda_fail(ce, "cudaMemcpyAsync(regrid upload)"));
   ce = cudaStreamSynchronize(N.s);  // the host arrays are freed on return
   if (ce != cudaSuccess) return fail(cuda_fail(ce, "cudaStreamSynchronize(regrid upload)"));
   *out = nh;

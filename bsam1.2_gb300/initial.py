@@ -81,3 +81,30 @@ def ch_circle(shape, eps, h, seed, radius=0.25, noise=0.01, center=None):
     q[sl + (0,)] = phi
     q[sl + (1,)] = mu
     return q
+
+
+def ch_circle_patch(eps, seed, radius=0.25, noise=0.01, center=(0.5, 0.5, 0.5), length=1.0):
+    """Initial condition of a patch of any level (a QInit for the regrid):
+    phi0 = tanh((r - radius)/(sqrt(2) eps)) + noise*U(-1,1), U from splitmix64
+    on the cell's global index on its level (so every level sees the same
+    field whatever the patching), mu0 = 0 as the CH plugin's QInit2D/3D
+    (CH/problem.f90:60-61).  Returns fn(level, mx, dx, xlower) -> ghosted
+    Fortran-layout array."""
+    def fn(level, mx, dx, xl):
+        nd = len(mx)
+        nglob = [int(round(length / dx[d])) for d in range(nd)]
+        i0 = [int(round(xl[d] / dx[d])) for d in range(nd)]
+        ax = [(np.arange(mx[d]) + 0.5) * dx[d] + xl[d] for d in range(nd)]
+        coords = np.meshgrid(*ax, indexing="ij")
+        r = np.sqrt(sum((c - center[d]) ** 2 for d, c in enumerate(coords)))
+        idx = np.meshgrid(*[np.arange(mx[d], dtype=np.uint64) + np.uint64(i0[d]) for d in range(nd)], indexing="ij")
+        g = idx[0]
+        stride = np.uint64(1)
+        for d in range(1, nd):
+            stride = stride * np.uint64(nglob[d - 1])
+            g = g + idx[d] * stride
+        phi = np.tanh((r - radius) / (np.sqrt(2.0) * eps)) + noise * splitmix_pm1(seed, g)
+        q = np.zeros(tuple(m + 2 for m in mx) + (2,), order="F")
+        q[tuple(slice(1, -1) for _ in mx) + (0,)] = phi
+        return q
+    return fn
