@@ -36,6 +36,11 @@ WORKLOADS = {
     "ch3d-256": dict(ndims=3, n=256, minlevel=-7, mthbc=[2, 2, 2, 2, 2, 2], eps=0.02, dt=5e-4, tol=1e-8,
                      mean=0.1, amp=0.05, seed=20240503,
                      desc="3D Cahn-Hilliard 256^3 periodic, eps=0.02, dt=5e-4, V(2,2), resid<=1e-8"),
+    # a smaller 3D box with the same kernels and a working set still above
+    # L2 (relax ~150 MB per sweep): the case the detailed ncu profiles use
+    "ch3d-256x256x128": dict(ndims=3, n=256, mx=[256, 256, 128], minlevel=-6, mthbc=[2, 2, 2, 2, 2, 2], eps=0.02,
+                             dt=5e-4, tol=1e-8, mean=0.1, amp=0.05, seed=20240503,
+                             desc="3D Cahn-Hilliard 256x256x128 periodic, eps=0.02, dt=5e-4, V(2,2), resid<=1e-8"),
     "ch2d-128": dict(ndims=2, n=128, minlevel=-6, mthbc=[2, 2, 2, 2, 10, 10], eps=0.01, dt=1e-3, tol=1e-9,
                      mean=0.0, amp=0.05, seed=20240503,
                      desc="2D Cahn-Hilliard 128^2 periodic, eps=0.01, dt=1e-3, V(2,2), resid<=1e-9"),
@@ -155,17 +160,25 @@ class Clocks:
                 "reasons": sorted(reasons)}
 
 
-def make_hierarchy(pkg, ctx, w):
+def root_mx(w):
+    """root extents (3 entries) and upper domain corner of a uniform workload"""
     nd, n = w["ndims"], w["n"]
-    h = pkg.Hierarchy(ctx, nd, 2, "ch", [w["dt"], w["eps"]])
-    h.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
+    mx = list(w.get("mx", [n] * nd)) + [1] * (3 - nd)
+    return mx, [mx[d] / n if d < nd else 1 for d in range(3)]
+
+
+def make_hierarchy(pkg, ctx, w):
+    mx, up = root_mx(w)
+    h = pkg.Hierarchy(ctx, w["ndims"], 2, "ch", [w["dt"], w["eps"]])
+    h.build_uniform(mx, w["minlevel"], w["mthbc"], [0, 0, 0], up)
     h.commit()
     return h
 
 
 def initial_q(pkg, w):
     nd, n = w["ndims"], w["n"]
-    q = pkg.initial.ch_spinodal((n,) * nd, w["eps"], 1.0 / n, seed=w["seed"], mean=w["mean"], amp=w["amp"])
+    mx, _ = root_mx(w)
+    q = pkg.initial.ch_spinodal(tuple(mx[:nd]), w["eps"], 1.0 / n, seed=w["seed"], mean=w["mean"], amp=w["amp"])
     return np.asfortranarray(q).ravel(order="F")
 
 
@@ -239,8 +252,9 @@ def cpu_baseline(pkg, w, vcycles_per_step, nvc=2):
     V-cycle count per step of the FP64 run."""
     from oracle.bsam_oracle import OracleHierarchy
     nd, n = w["ndims"], w["n"]
+    mx, up = root_mx(w)
     o = OracleHierarchy(nd, 2, "ch", [w["dt"], w["eps"]])
-    o.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
+    o.build_uniform(mx, w["minlevel"], w["mthbc"], [0, 0, 0], up)
     o.commit()
     o.put(0, "q", initial_q(pkg, w))
     o.set_ghost(0, 0)
@@ -252,7 +266,7 @@ def cpu_baseline(pkg, w, vcycles_per_step, nvc=2):
     per_v = dt / nvc
     return per_v, dict(value=1.0 / (per_v * vcycles_per_step), unit="steps/s", cores=1, kind="port",
                        sample=f"oracle (C restatement of the reference, 1 thread, -O2 -ffp-contract=off) "
-                              f"running {nvc} V-cycles of the first time step of the same {w['n']}^{nd} "
+                              f"running {nvc} V-cycles of the first time step of the same "
                               f"workload ({dt:.1f} s); steps/s = 1/(t_vcycle x {vcycles_per_step:.2f} "
                               f"V-cycles per step of the FP64 run)")
 
@@ -269,10 +283,11 @@ def reference_arm(args, w, dist):
     pkg_initial = ge.load_package().initial  # numpy input generator only; libbsamg is not loaded
     from oracle.bsam_oracle import OracleHierarchy
     nd, n = w["ndims"], w["n"]
+    mx, up = root_mx(w)
     o = OracleHierarchy(nd, 2, "ch", [w["dt"], w["eps"]])
-    o.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
+    o.build_uniform(mx, w["minlevel"], w["mthbc"], [0, 0, 0], up)
     o.commit()
-    q = pkg_initial.ch_spinodal((n,) * nd, w["eps"], 1.0 / n, seed=w["seed"], mean=w["mean"], amp=w["amp"])
+    q = pkg_initial.ch_spinodal(tuple(mx[:nd]), w["eps"], 1.0 / n, seed=w["seed"], mean=w["mean"], amp=w["amp"])
     o.put(0, "q", q)
     o.set_ghost(0, 0)
     o.copy_q_to_qold(w["minlevel"], 0)
@@ -571,7 +586,7 @@ def main():
     ctx = pkg.Context(dist.local)
     h = make_hierarchy(pkg, ctx, w)
     q0 = pkg.pin(initial_q(pkg, w))
-    N = w["n"] ** w["ndims"]
+    N = int(np.prod(root_mx(w)[0]))
 
     clocks = Clocks(dist.local)
     mixed = run_arm(h, q0, w, "mixed", args.steps, args.warmup, dist, clocks)
