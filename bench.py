@@ -55,6 +55,16 @@ AMR_WORKLOADS = {
                      desc="2D Cahn-Hilliard AMR: 64^2 periodic root + 3 levels (|grad phi| h > 0.25, "
                           "Berger-Rigoutsos, <= 64 cells per side, regrid every step), circle r=0.25 + 1% "
                           "noise, eps=0.01, dt=1e-3, V(2,2), resid<=1e-9"),
+    # cfg4: the three-variable growth plugin (phi, nutrient, pressure) on a
+    # 32^3 root with two refinement levels; the mixed path's correction
+    # smoother is the CH one, so this workload runs the FP64 path only
+    "growth3d-amr": dict(ndims=3, n=32, minlevel=-4, mthbc=[10] * 6, problem="growth", nrvars=3,
+                         params=[0.01, 0.025, 1.5, 2.0, 0.5, 1.0], eps=0.025, dt=0.01, tol=1e-8, maxlevel=2,
+                         tagging="gradient", qtol=0.25, ibuffer=1, mgp=4, fill=0.9, maxside=64, radius=0.1,
+                         noise=0.02, seed=20240503, modes=("fp64",), init="sphere",
+                         desc="3D growth (phi, nutrient, pressure; no reference counterpart): 32^3 root + 2 levels "
+                              "(|grad phi| h > 0.25, regrid every step), sphere r = 0.1 + 0.02 U(-1,1), "
+                              "eps=0.025, dt=0.01, gamma=1.5, lambda=2, c0=0.5, cpress=1, V(2,2), resid<=1e-8"),
 }
 NSMOOTH = 2
 MAXV = 30
@@ -358,18 +368,25 @@ def amr_run(api, make_root, w, mode, steps, warmup, use_events=True):
 
 def api_qinit(w):
     import __graft_entry__ as ge
-    return ge.load_package().initial.ch_circle_patch(w["eps"], w["seed"], radius=w["radius"], noise=w["noise"])
+    ini = ge.load_package().initial
+    if w.get("init") == "sphere":
+        return ini.growth_sphere(w["eps"], w["seed"], radius=w["radius"], noise=w["noise"])
+    return ini.ch_circle_patch(w["eps"], w["seed"], radius=w["radius"], noise=w["noise"])
 
 
-def mesh_stats(tab):
+def amr_hier_args(w):
+    return w["ndims"], w.get("nrvars", 2), w.get("problem", "ch"), w.get("params", [w["dt"], w["eps"]])
+
+
+def mesh_stats(tab, nd=2):
     levels = {}
     for p in tab:
         if p["level"] < 0:
             continue
         d = levels.setdefault(p["level"], {"patches": 0, "cells": 0})
         d["patches"] += 1
-        d["cells"] += int(np.prod(p["mx"][:2]))
-    sides = [max(p["mx"][:2]) for p in tab if p["level"] > 0]
+        d["cells"] += int(np.prod(p["mx"][:nd]))
+    sides = [max(p["mx"][:nd]) for p in tab if p["level"] > 0]
     hist = {}
     for b in (8, 16, 32, 64, 128):
         hist[f"<={b}"] = sum(1 for x in sides if x <= b) - sum(v for v in hist.values())
@@ -388,19 +405,20 @@ def amr_arm(args, w, dist):
     nd, n = w["ndims"], w["n"]
 
     def make_root():
-        h = pkg.Hierarchy(ctx, nd, 2, "ch", [w["dt"], w["eps"]])
+        h = pkg.Hierarchy(ctx, *amr_hier_args(w))
         h.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
         h.commit()
         h.put(0, "q", api_qinit(w)(0, [n] * nd, [1.0 / n] * nd, [0.0] * nd))
         return h
 
     out = {}
-    for mode in ("mixed", "fp64"):
+    modes = w.get("modes", ("mixed", "fp64"))
+    for mode in modes:
         dist.barrier()
         r = amr_run(pkg, make_root, w, mode, args.steps, args.warmup)
         r["tab"] = r["h"].patch_table()
         out[mode] = r
-    m, f = out["mixed"], out["fp64"]
+    m, f = out[modes[0]], out["fp64"]
     same_mesh = [(p["level"], p["mglobal"]) for p in m["tab"]] == [(p["level"], p["mglobal"]) for p in f["tab"]]
     err = None
     if same_mesh:
@@ -409,7 +427,7 @@ def amr_arm(args, w, dist):
             if p["level"] < 0:
                 continue
             a, b = m["h"].get(p["id"], "q"), f["h"].get(p["id"], "q")
-            k = a.size // 2
+            k = a.size // w.get("nrvars", 2)
             worst = max(worst, float(np.max(np.abs(a[:k] - b[:k])) / np.max(np.abs(b[:k]))))
         err = worst
     t_m = dist.max(m["total_s"])
@@ -418,9 +436,10 @@ def amr_arm(args, w, dist):
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": dist.ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_m / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded splitmix64 noise on a tanh circle)",
+        "vs_baseline": None, "dtype": "f32+f64" if modes[0] == "mixed" else "f64",
+        "data": "synthetic (seeded splitmix64 noise on a tanh " + ("sphere)" if w.get("init") == "sphere" else "circle)"),
         "config": {"workload": args.workload, "desc": w["desc"], "regrid": "every step (host clustering)",
-                   "l2": "L2-resident, launch- and host-bound (2D, < 1 MB per level)"},
+                   "l2": "L2-resident, launch- and host-bound (working set of a few MB per level)"},
         "p50_ms": 1e3 * pct(m["wall"], 50), "p99_ms": 1e3 * pct(m["wall"], 99),
         "regrid_ms_per_step": 1e3 * (statistics.mean(m["wall"]) - statistics.mean(m["solve"])),
         "solve_ms_per_step": 1e3 * statistics.mean(m["solve"]),
@@ -428,16 +447,17 @@ def amr_arm(args, w, dist):
         "plain_fp64": {"value": dist.ws * args.steps / t_f, "unit": "steps/s", "ms_per_step": 1e3 * t_f / args.steps,
                        "solve_ms_per_step": 1e3 * statistics.mean(f["solve"]),
                        "vcycles_per_step": statistics.mean(f["vcycles"])},
-        "speedup_mixed_vs_fp64": t_f / t_m,
+        "speedup_mixed_vs_fp64": t_f / t_m if modes[0] == "mixed" else None,
+        "mixed": "run" if modes[0] == "mixed" else "not built for this plugin (the correction smoother is CH's)",
         "error_vs_fp64": {"max_rel_phi": err, "same_mesh": same_mesh, "after_steps": args.warmup + args.steps},
-        "mesh": mesh_stats(f["tab"]),
+        "mesh": mesh_stats(f["tab"], nd),
         "timing": "host clock around regrid + time step, device synchronised after each step",
     }
     if not args.no_cpu_baseline:
         from oracle import bsam_oracle as om
 
         def oracle_root():
-            o = om.OracleHierarchy(nd, 2, "ch", [w["dt"], w["eps"]])
+            o = om.OracleHierarchy(*amr_hier_args(w))
             o.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
             o.commit()
             o.put(0, "q", api_qinit(w)(0, [n] * nd, [1.0 / n] * nd, [0.0] * nd))
@@ -482,7 +502,7 @@ def amr_reference_arm(args, w, dist):
     from oracle import bsam_oracle as om
     nd, n = w["ndims"], w["n"]
     qinit = api_qinit(w)
-    o = om.OracleHierarchy(nd, 2, "ch", [w["dt"], w["eps"]])
+    o = om.OracleHierarchy(*amr_hier_args(w))
     o.build_uniform([n] * nd + [1] * (3 - nd), w["minlevel"], w["mthbc"], [0, 0, 0], [1, 1, 1])
     o.commit()
     o.put(0, "q", qinit(0, [n] * nd, [1.0 / n] * nd, [0.0] * nd))
@@ -500,7 +520,7 @@ def amr_reference_arm(args, w, dist):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(ts),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded splitmix64 noise on a tanh circle)",
+        "data": "synthetic (seeded splitmix64 noise on a tanh " + ("sphere)" if w.get("init") == "sphere" else "circle)"),
         "config": {"workload": args.workload, "desc": w["desc"]},
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": 1, "kind": "port",
                          "sample": "every step in full: regrid + CopyQToQold + MultigridIterations"},

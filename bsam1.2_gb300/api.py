@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libbsamg.so")
 
 FIELD = {"q": 0, "qold": 1, "qc": 2, "f": 3, "rf": 4, "ftmp": 5}
-PROBLEM = {"ch": 1, "biogrowth": 2}
+PROBLEM = {"ch": 1, "biogrowth": 2, "growth": 3}
 MODE = {"fp64": 0, "mixed": 1}
 
 _lib = None

@@ -55,43 +55,54 @@ __device__ __forceinline__ double ulap(const double* a, long long c, long long s
 
 // Operator2D/3D of the plugin at ghosted offset c of array a (planes of ps
 // elements), with qold value o0 (variable 1 at the same cell) and patch
-// coefficients cf.  CH: CH/problem.f90:393-422, :638-669; BioGrowth:
-// BioGrowth/problem.f90:320-353 (3D: zero stub, :497-522).
+// coefficients cf; r receives one value per variable.  CH:
+// CH/problem.f90:393-422, :638-669; BioGrowth: BioGrowth/problem.f90:320-353
+// (3D: zero stub, :497-522); growth (three variables, no reference
+// counterpart): phi as BioGrowth's with 2*ndims neighbours, n the BioGrowth
+// uptake equation, p: -Lap(p)/h^2 - cpress*phi*n.
 template <int PROB, int DIM>
 __device__ __forceinline__ void op_eval(const double* a, long long c, long long sy, long long sz,
                                         long long ps, double o0, const double* cf,
-                                        const ProbParams& pp, double& r0, double& r1) {
+                                        const ProbParams& pp, double* r) {
   const double* a0 = a;
   const double* a1 = a + ps;
   if (PROB == kCH) {
-    r0 = a0[c] - cf[0] * ulap<DIM>(a1, c, sy, sz);
-    r1 = a1[c] - cube(a0[c]) + cf[1] * ulap<DIM>(a0, c, sy, sz);
-  } else {
+    r[0] = a0[c] - cf[0] * ulap<DIM>(a1, c, sy, sz);
+    r[1] = a1[c] - cube(a0[c]) + cf[1] * ulap<DIM>(a0, c, sy, sz);
+  } else if (PROB == kBio) {
     if (DIM == 2) {
       double dt = pp.dt;
-      r0 = a0[c] - cf[0] * ulap<DIM>(a0, c, sy, sz) + dt * cube(a0[c]) -
-           dt * (pp.gamma * 0.5 * (o0 + 1.0)) * (a1[c] - pp.czero);
-      r1 = -cf[1] * ulap<DIM>(a1, c, sy, sz) + (pp.lambda * 0.5 * (o0 + 1.0)) * a1[c];
+      r[0] = a0[c] - cf[0] * ulap<DIM>(a0, c, sy, sz) + dt * cube(a0[c]) -
+             dt * (pp.gamma * 0.5 * (o0 + 1.0)) * (a1[c] - pp.czero);
+      r[1] = -cf[1] * ulap<DIM>(a1, c, sy, sz) + (pp.lambda * 0.5 * (o0 + 1.0)) * a1[c];
     } else {
-      r0 = 0.0;
-      r1 = 0.0;
+      r[0] = 0.0;
+      r[1] = 0.0;
     }
+  } else {
+    const double* a2 = a + 2 * ps;
+    double dt = pp.dt;
+    r[0] = a0[c] - cf[0] * ulap<DIM>(a0, c, sy, sz) + dt * cube(a0[c]) -
+           dt * (pp.gamma * 0.5 * (o0 + 1.0)) * (a1[c] - pp.czero);
+    r[1] = -cf[1] * ulap<DIM>(a1, c, sy, sz) + (pp.lambda * 0.5 * (o0 + 1.0)) * a1[c];
+    r[2] = -cf[1] * ulap<DIM>(a2, c, sy, sz) - pp.cpress * a0[c] * a1[c];
   }
 }
 
 // Source2D/3D + SourceUpdate2D/3D values (CH/problem.f90:425-476, :672-721;
-// BioGrowth/problem.f90:356-405, :525-575)
+// BioGrowth/problem.f90:356-405, :525-575; growth as BioGrowth, p zero)
 template <int PROB, int DIM>
-__device__ __forceinline__ void source_eval(double o0, const ProbParams& pp, double& s0, double& s1) {
+__device__ __forceinline__ void source_eval(double o0, const ProbParams& pp, double* s) {
   if (PROB == kCH) {
-    s0 = o0;
-    s1 = -o0;
-  } else if (DIM == 2) {
-    s0 = (1.0 + pp.dt) * o0;
-    s1 = 0.0;
+    s[0] = o0;
+    s[1] = -o0;
+  } else if (PROB == kBio) {
+    s[0] = DIM == 2 ? (1.0 + pp.dt) * o0 : 0.0;
+    s[1] = 0.0;
   } else {
-    s0 = 0.0;
-    s1 = 0.0;
+    s[0] = (1.0 + pp.dt) * o0;
+    s[1] = 0.0;
+    s[2] = 0.0;
   }
 }
 
@@ -179,7 +190,7 @@ __global__ void __launch_bounds__(kBlock) k_relax(const PatchDev* __restrict__ P
     double det = 1.0 - p.c[3] * a21;
     q0[c] = (b1 - p.c[3] * b2) / det;
     q1[c] = (b2 - a21 * b1) / det;
-  } else {
+  } else if (PROB == kBio) {
     if (DIM == 2) {
       // RelaxGrid2D BioGrowth/problem.f90:280-294
       const double* o0 = pool + p.oqold;
@@ -196,6 +207,30 @@ __global__ void __launch_bounds__(kBlock) k_relax(const PatchDev* __restrict__ P
       q0[c] = 0.0;
       q1[c] = 0.0;
     }
+  } else {
+    // growth: phi and n as BioGrowth's RelaxGrid2D with 2*ndims neighbours,
+    // then p from the updated phi and n
+    double* q2 = q1 + p.sq;
+    const double* f2 = f1 + p.sf;
+    const double* o0 = pool + p.oqold;
+    double dt = pp.dt;
+    double phi = q0[c];
+    double ol = o0[c];
+    double tmp2 = p.c[2] + dt * sqr(phi);
+    double s0 = q0[c - 1] + q0[c + 1] + q0[c - sy] + q0[c + sy];
+    double s1 = q1[c + 1] + q1[c - 1] + q1[c + sy] + q1[c - sy];
+    double s2 = q2[c + 1] + q2[c - 1] + q2[c + sy] + q2[c - sy];
+    if (DIM == 3) {
+      s0 = s0 + q0[c - sz] + q0[c + sz];
+      s1 = s1 + q1[c + sz] + q1[c - sz];
+      s2 = s2 + q2[c + sz] + q2[c - sz];
+    }
+    double np = (f0[fc] + dt * (pp.gamma * 0.5 * (ol + 1.0)) * (q1[c] - pp.czero) + p.c[0] * s0) / tmp2;
+    double tmp4 = p.c[3] + (pp.lambda * 0.5 * (ol + 1.0));
+    double nn = (f1[fc] + p.c[1] * s1) / tmp4;
+    q0[c] = np;
+    q1[c] = nn;
+    q2[c] = (f2[fc] + p.c[1] * s2 + pp.cpress * np * nn) / p.c[3];
   }
 }
 
@@ -264,10 +299,9 @@ __global__ void __launch_bounds__(kBlock) k_coarse_load(const PatchDev* __restri
   const double* q = pool + p.oq;
   const double* qo = pool + p.oqold;
   long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
-  double* rf0 = pool + p.orf;
-  double* rf1 = rf0 + p.sf;
-  const double* f0 = pool + p.of;
-  const double* f1 = f0 + p.sf;
+  constexpr int NV = PROB == kGrowth ? 3 : 2;
+  double* rf = pool + p.orf;
+  const double* f = pool + p.of;
   const int nk = DIM == 3 ? 2 : 1;
   for (int dk = 0; dk < nk; dk++)
     for (int dj = 0; dj < 2; dj++)
@@ -275,16 +309,17 @@ __global__ void __launch_bounds__(kBlock) k_coarse_load(const PatchDev* __restri
         int i = 2 * ci - di, j = 2 * cj - dj, k = DIM == 3 ? 2 * ck - dk : 1;
         long long c = gofs<DIM>(p.qn, i, j, k);
         long long fc = iofs<DIM>(p.mx, i, j, k);
-        double r0, r1;
-        op_eval<PROB, DIM>(q, c, sy, sz, p.sq, qo[c], p.c, pp, r0, r1);
-        rf0[fc] = f0[fc] - r0;
-        rf1[fc] = f1[fc] - r1;
+        double r[NV];
+        op_eval<PROB, DIM>(q, c, sy, sz, p.sq, qo[c], p.c, pp, r);
+        for (int v = 0; v < NV; v++) rf[v * p.sf + fc] = f[v * p.sf + fc] - r[v];
       }
   // the restriction reads rf written above by this same thread
-  auto at0 = [&](int i, int j, int k) { return rf0[iofs<DIM>(p.mx, i, j, k)]; };
-  auto at1 = [&](int i, int j, int k) { return rf1[iofs<DIM>(p.mx, i, j, k)]; };
-  double R0 = restrict_at<DIM>(at0, ci, cj, ck);
-  double R1 = restrict_at<DIM>(at1, ci, cj, ck);
+  double R[NV];
+  for (int v = 0; v < NV; v++) {
+    const double* rv = rf + v * p.sf;
+    auto at = [&](int i, int j, int k) { return rv[iofs<DIM>(p.mx, i, j, k)]; };
+    R[v] = restrict_at<DIM>(at, ci, cj, ck);
+  }
   // coarse operator on qc with the parent's spacing; parent qold at the
   // section parent%qold(mb-1:mb+1)
   const double* qc = pool + p.oqc;
@@ -292,11 +327,10 @@ __global__ void __launch_bounds__(kBlock) k_coarse_load(const PatchDev* __restri
   long long cc = gofs<DIM>(p.cn, ci, cj, ck);
   long long pc = gofs<DIM>(par.qn, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 0);
   double o0 = pool[par.oqold + pc];
-  double c0, c1;
-  op_eval<PROB, DIM>(qc, cc, csy, csz, p.sc, o0, par.c, pp, c0, c1);
+  double cr[NV];
+  op_eval<PROB, DIM>(qc, cc, csy, csz, p.sc, o0, par.c, pp, cr);
   long long pf = iofs<DIM>(par.mx, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 1);
-  pool[par.of + pf] = R0 + c0;
-  pool[par.of + par.sf + pf] = R1 + c1;
+  for (int v = 0; v < NV; v++) pool[par.of + v * par.sf + pf] = R[v] + cr[v];
 }
 
 // CorrectFine step 1, afasroutines.f90:892-895 / :934-938:
@@ -396,11 +430,11 @@ __global__ void __launch_bounds__(kBlock) k_get_source(const PatchDev* __restric
   int i, j, k;
   if (!interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) return;
   double o0 = pool[p.oqold + gofs<DIM>(p.qn, i, j, k)];
-  double s0, s1;
-  source_eval<PROB, DIM>(o0, pp, s0, s1);
+  constexpr int NV = PROB == kGrowth ? 3 : 2;
+  double s[NV];
+  source_eval<PROB, DIM>(o0, pp, s);
   long long fc = iofs<DIM>(p.mx, i, j, k);
-  pool[p.oftmp + fc] = s0;
-  pool[p.oftmp + p.sf + fc] = s1;
+  for (int v = 0; v < NV; v++) pool[p.oftmp + v * p.sf + fc] = s[v];
 }
 
 // UpdateSourceFunction, afasroutines.f90:438-492: f = ftmp + SourceUpdate
@@ -422,46 +456,38 @@ template <int PROB, int DIM>
 __global__ void __launch_bounds__(kBlock) k_norm_partial(const PatchDev* __restrict__ P, double* __restrict__ pool,
                                                          const Blk* __restrict__ blk, ProbParams pp,
                                                          double* __restrict__ partial, int store_rf) {
-  __shared__ double red[2][kBlock / 32];
+  constexpr int NV = PROB == kGrowth ? 3 : 2;
+  __shared__ double red[NV][kBlock / 32];
   const Blk b = blk[blockIdx.x];
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  double s0 = 0.0, s1 = 0.0;
+  double s[NV];
+  for (int v = 0; v < NV; v++) s[v] = 0.0;
   if (interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) {
     const double* q = pool + p.oq;
     long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
     long long c = gofs<DIM>(p.qn, i, j, k);
     long long fc = iofs<DIM>(p.mx, i, j, k);
-    double r0, r1;
-    op_eval<PROB, DIM>(q, c, sy, sz, p.sq, pool[p.oqold + c], p.c, pp, r0, r1);
-    double e0 = pool[p.of + fc] - r0;
-    double e1 = pool[p.of + p.sf + fc] - r1;
-    if (store_rf) {
-      pool[p.orf + fc] = e0;
-      pool[p.orf + p.sf + fc] = e1;
+    double r[NV];
+    op_eval<PROB, DIM>(q, c, sy, sz, p.sq, pool[p.oqold + c], p.c, pp, r);
+    for (int v = 0; v < NV; v++) {
+      double e = pool[p.of + v * p.sf + fc] - r[v];
+      if (store_rf) pool[p.orf + v * p.sf + fc] = e;
+      s[v] = e * e;
     }
-    s0 = e0 * e0;
-    s1 = e1 * e1;
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    s0 = s0 + __shfl_down_sync(0xffffffffu, s0, o);
-    s1 = s1 + __shfl_down_sync(0xffffffffu, s1, o);
-  }
+  for (int o = 16; o > 0; o >>= 1)
+    for (int v = 0; v < NV; v++) s[v] = s[v] + __shfl_down_sync(0xffffffffu, s[v], o);
   int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) {
-    red[0][w] = s0;
-    red[1][w] = s1;
-  }
+  if (l == 0)
+    for (int v = 0; v < NV; v++) red[v][w] = s[v];
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double t0 = 0.0, t1 = 0.0;
-    for (int n = 0; n < kBlock / 32; n++) {
-      t0 = t0 + red[0][n];
-      t1 = t1 + red[1][n];
+  if (threadIdx.x == 0)
+    for (int v = 0; v < NV; v++) {
+      double t = 0.0;
+      for (int n = 0; n < kBlock / 32; n++) t = t + red[v][n];
+      partial[NV * blockIdx.x + v] = t;
     }
-    partial[2 * blockIdx.x] = t0;
-    partial[2 * blockIdx.x + 1] = t1;
-  }
 }
 
 // Final deterministic reduction of the block partials in block order.
@@ -469,91 +495,81 @@ __global__ void __launch_bounds__(kBlock) k_norm_partial(const PatchDev* __restr
 // [g*chunk, min((g+1)*chunk, nblk)) in a fixed order and writes one pair to
 // stage[2g], stage[2g+1].  Spreading the FP64 additions over many SMs
 // matters on GB300, whose FP64 rate is two additions per clock per SM.
-constexpr int kStageBlocks = (kNormOutLen - 8) / 2;
+constexpr int kStageBlocks = (kNormOutLen - 8) / 3;
+template <int NV>
 __global__ void __launch_bounds__(kBlock) k_norm_stage(const double* __restrict__ partial, int nblk, int chunk,
                                                        double* __restrict__ stage) {
-  __shared__ double red[2][kBlock];
+  __shared__ double red[NV][kBlock];
   int lo = blockIdx.x * chunk, hi = min(lo + chunk, nblk);
-  double a = 0.0, c = 0.0;
-  for (int n = lo + threadIdx.x; n < hi; n += kBlock) {
-    a = a + partial[2 * n];
-    c = c + partial[2 * n + 1];
-  }
-  red[0][threadIdx.x] = a;
-  red[1][threadIdx.x] = c;
+  double a[NV];
+  for (int v = 0; v < NV; v++) a[v] = 0.0;
+  for (int n = lo + threadIdx.x; n < hi; n += kBlock)
+    for (int v = 0; v < NV; v++) a[v] = a[v] + partial[NV * n + v];
+  for (int v = 0; v < NV; v++) red[v][threadIdx.x] = a[v];
   __syncthreads();
   for (int w = kBlock / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) {
-      red[0][threadIdx.x] = red[0][threadIdx.x] + red[0][threadIdx.x + w];
-      red[1][threadIdx.x] = red[1][threadIdx.x] + red[1][threadIdx.x + w];
-    }
+    if (threadIdx.x < w)
+      for (int v = 0; v < NV; v++) red[v][threadIdx.x] = red[v][threadIdx.x] + red[v][threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    stage[2 * blockIdx.x] = red[0][0];
-    stage[2 * blockIdx.x + 1] = red[1][0];
-  }
+  if (threadIdx.x == 0)
+    for (int v = 0; v < NV; v++) stage[NV * blockIdx.x + v] = red[v][0];
 }
 
 // One CTA of 1024 threads; each thread keeps eight independent partial sums
-// so that eight loads are in flight, then a fixed-shape tree.  The order of
-// the additions depends only on nblk, so the result is deterministic.
+// per variable so that eight loads are in flight, then a fixed-shape tree.
+// The order of the additions depends only on nblk, so the result is
+// deterministic.  Partials hold NV values per block.
 constexpr int kFinishThreads = 1024;
+template <int NV>
 __global__ void __launch_bounds__(kFinishThreads) k_norm_finish(const double* __restrict__ partial, int nblk,
-                                                                int nrvars, double count, int errortype, double* out,
+                                                                double count, int errortype, double* out,
                                                                 int* nonfinite) {
-  __shared__ double red[2][kFinishThreads / 32];
-  double a[8], c[8];
-  for (int u = 0; u < 8; u++) a[u] = c[u] = 0.0;
+  __shared__ double red[NV][kFinishThreads / 32];
+  double a[NV][8];
+  for (int v = 0; v < NV; v++)
+    for (int u = 0; u < 8; u++) a[v][u] = 0.0;
   int n = threadIdx.x;
   for (; n + 7 * kFinishThreads < nblk; n += 8 * kFinishThreads)
-    for (int u = 0; u < 8; u++) {
-      a[u] = a[u] + partial[2 * (n + u * kFinishThreads)];
-      c[u] = c[u] + partial[2 * (n + u * kFinishThreads) + 1];
-    }
+    for (int u = 0; u < 8; u++)
+      for (int v = 0; v < NV; v++) a[v][u] = a[v][u] + partial[NV * (n + u * kFinishThreads) + v];
   // the remaining (at most seven) partials of this thread; a constant index
-  // keeps a[] and c[] in registers
-  for (; n < nblk; n += kFinishThreads) {
-    a[0] = a[0] + partial[2 * n];
-    c[0] = c[0] + partial[2 * n + 1];
-  }
-  double t0 = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
-  double t1 = ((c[0] + c[1]) + (c[2] + c[3])) + ((c[4] + c[5]) + (c[6] + c[7]));
-  for (int o = 16; o > 0; o >>= 1) {
-    t0 = t0 + __shfl_down_sync(0xffffffffu, t0, o);
-    t1 = t1 + __shfl_down_sync(0xffffffffu, t1, o);
-  }
+  // keeps a[][] in registers
+  for (; n < nblk; n += kFinishThreads)
+    for (int v = 0; v < NV; v++) a[v][0] = a[v][0] + partial[NV * n + v];
+  double t[NV];
+  for (int v = 0; v < NV; v++)
+    t[v] = ((a[v][0] + a[v][1]) + (a[v][2] + a[v][3])) + ((a[v][4] + a[v][5]) + (a[v][6] + a[v][7]));
+  for (int o = 16; o > 0; o >>= 1)
+    for (int v = 0; v < NV; v++) t[v] = t[v] + __shfl_down_sync(0xffffffffu, t[v], o);
   int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) {
-    red[0][w] = t0;
-    red[1][w] = t1;
-  }
+  if ((threadIdx.x & 31) == 0)
+    for (int v = 0; v < NV; v++) red[v][w] = t[v];
   __syncthreads();
   if (w == 0) {
-    t0 = red[0][threadIdx.x];
-    t1 = red[1][threadIdx.x];
-    for (int o = 16; o > 0; o >>= 1) {
-      t0 = t0 + __shfl_down_sync(0xffffffffu, t0, o);
-      t1 = t1 + __shfl_down_sync(0xffffffffu, t1, o);
-    }
-    if (threadIdx.x == 0) {
-      red[0][0] = t0;
-      red[1][0] = t1;
-    }
+    for (int v = 0; v < NV; v++) t[v] = red[v][threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1)
+      for (int v = 0; v < NV; v++) t[v] = t[v] + __shfl_down_sync(0xffffffffu, t[v], o);
+    if (threadIdx.x == 0)
+      for (int v = 0; v < NV; v++) red[v][0] = t[v];
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double a = red[0][0], c = red[1][0];
+    double sum = red[0][0];
+    for (int v = 1; v < NV; v++) sum = sum + red[v][0];
     double r;
     if (errortype == 1) {
-      r = sqrt((a + c) / count);  // integralresult(1)/integralresult(2), :135
+      r = sqrt(sum / count);  // integralresult(1)/integralresult(2), :135
     } else {
-      double cells = count / nrvars;
-      double e0 = sqrt(a / cells), e1 = sqrt(c / cells);
-      r = e1 > e0 ? e1 : e0;  // MAXVAL of component errors, :146-153
+      double cells = count / NV;
+      r = sqrt(red[0][0] / cells);
+      for (int v = 1; v < NV; v++) {  // MAXVAL of component errors, :146-153
+        double e = sqrt(red[v][0] / cells);
+        r = e > r ? e : r;
+      }
     }
     out[0] = r;
-    out[1] = a + c;
+    out[1] = sum;
     nonfinite[0] = isfinite(r) ? 0 : 1;
   }
 }
@@ -574,7 +590,7 @@ __device__ __forceinline__ void ghost_apply(const PatchDev* __restrict__ P, doub
       case kGCopy: val = sq[g.s0]; break;
       case kGCopyAdd: val = sq[g.s0] + pp.qpo[v]; break;
       case kGCopySub: val = sq[g.s0] - pp.qpo[v]; break;
-      case kGBC: val = ((g.mask >> v) & 1) ? 2.0 - sq[g.s0] : sq[g.s0]; break;
+      case kGBC: val = ((g.mask >> v) & 1) ? 2.0 - sq[g.s0] : (((g.mask >> (8 + v)) & 1) ? -sq[g.s0] : sq[g.s0]); break;
       case kGCfA: val = kA1 * dq[g.s0] + kA2 * dq[g.s1] + kA3 * sq[g.c0]; break;
       case kGCfAB:
         val = kA1 * dq[g.s0] + kA2 * dq[g.s1] + kA3 * (kB1 * sq[g.c0] + kB2 * sq[g.c1] + kB3 * sq[g.c2]);
@@ -625,9 +641,12 @@ __global__ void __launch_bounds__(kBlock) k_ghost_program(const PatchDev* __rest
     if ((c).pp.problem == kCH) {                                                      \
       if ((c).ndims == 2) KER<kCH, 2><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__);       \
       else KER<kCH, 3><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__);                      \
-    } else {                                                                          \
+    } else if ((c).pp.problem == kBio) {                                              \
       if ((c).ndims == 2) KER<kBio, 2><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__);      \
       else KER<kBio, 3><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__);                     \
+    } else {                                                                          \
+      if ((c).ndims == 2) KER<kGrowth, 2><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__);   \
+      else KER<kGrowth, 3><<<nblk, kBlock, 0, (c).s>>>(__VA_ARGS__);                  \
     }                                                                                 \
   } while (0)
 
@@ -683,17 +702,21 @@ int launch_norm_partial(const LaunchCtx& c, const Blk* blk, int nblk, double* pa
 }
 int launch_norm_finish(cudaStream_t s, const double* partial, int nblk, int nrvars, double count, int errortype,
                        double* out, int* nonfinite) {
+  int n = 1;
   if (nblk > 2048) {
     // two stages; out[8 ..] holds the stage sums
     int g = std::min(kStageBlocks, (nblk + 511) / 512);
     int chunk = (nblk + g - 1) / g;
     g = (nblk + chunk - 1) / chunk;
-    k_norm_stage<<<g, kBlock, 0, s>>>(partial, nblk, chunk, out + 8);
-    k_norm_finish<<<1, kFinishThreads, 0, s>>>(out + 8, g, nrvars, count, errortype, out, nonfinite);
-    return 2;
+    if (nrvars == 3) k_norm_stage<3><<<g, kBlock, 0, s>>>(partial, nblk, chunk, out + 8);
+    else k_norm_stage<2><<<g, kBlock, 0, s>>>(partial, nblk, chunk, out + 8);
+    partial = out + 8;
+    nblk = g;
+    n = 2;
   }
-  k_norm_finish<<<1, kFinishThreads, 0, s>>>(partial, nblk, nrvars, count, errortype, out, nonfinite);
-  return 1;
+  if (nrvars == 3) k_norm_finish<3><<<1, kFinishThreads, 0, s>>>(partial, nblk, count, errortype, out, nonfinite);
+  else k_norm_finish<2><<<1, kFinishThreads, 0, s>>>(partial, nblk, count, errortype, out, nonfinite);
+  return n;
 }
 int launch_ghost_stage(const LaunchCtx& c, const GhostOp* ops, int n) {
   if (n <= 0) return 0;

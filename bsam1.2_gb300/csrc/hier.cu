@@ -212,10 +212,12 @@ void coefficients(const Hier& H, double h, double* c) {
     c[2] = k * H.pp.eps2 / h2; // tmp3, :343 (:579)
     c[3] = k * c[0];           // a(1,2), :346 (:582)
   } else {
+    // BioGrowth's 2D expressions; the growth plugin uses 2*ndims neighbours
+    double k = H.problem == kGrowth ? 2.0 * H.ndims : 4.0;
     c[0] = H.pp.dt * H.pp.eps2 / h2;  // tmp1, BioGrowth/problem.f90:277
     c[1] = 1.0 / h2;                  // tmp3, :278
-    c[2] = 4.0 * c[0] + 1.0;          // first two terms of tmp2, :282
-    c[3] = 4.0 * c[1];                // first term of tmp4, :288
+    c[2] = k * c[0] + 1.0;            // first two terms of tmp2, :282
+    c[3] = k * c[1];                  // first term of tmp4, :288
   }
 }
 
@@ -709,9 +711,13 @@ int bsamg_hier_create(bsamg_ctx* ctx, int ndims, int nrvars, int mbc, int proble
   if (!ctx || !out || !params) return BSAMG_ERR_ARG;
   if (ndims < 2 || ndims > 3) return BSAMG_ERR_ARG;
   if (mbc != 1) return BSAMG_ERR_UNSUPPORTED;
-  if (problem_kind != BSAMG_PROBLEM_CH && problem_kind != BSAMG_PROBLEM_BIOGROWTH) return BSAMG_ERR_ARG;
-  if (nrvars != 2) return BSAMG_ERR_UNSUPPORTED;  // both plugins carry two variables
-  if (nparams < 2 || (problem_kind == BSAMG_PROBLEM_BIOGROWTH && nparams < 5)) return BSAMG_ERR_ARG;
+  if (problem_kind != BSAMG_PROBLEM_CH && problem_kind != BSAMG_PROBLEM_BIOGROWTH &&
+      problem_kind != BSAMG_PROBLEM_GROWTH)
+    return BSAMG_ERR_ARG;
+  if (nrvars != nvars_of(problem_kind)) return BSAMG_ERR_UNSUPPORTED;  // CH, BioGrowth: 2; growth: 3
+  if (nparams < 2 || (problem_kind == BSAMG_PROBLEM_BIOGROWTH && nparams < 5) ||
+      (problem_kind == BSAMG_PROBLEM_GROWTH && nparams < 6))
+    return BSAMG_ERR_ARG;
   bsamg_hier* h = new (std::nothrow) bsamg_hier();
   if (!h) return BSAMG_ERR_ARG;
   h->ctx = ctx;
@@ -725,6 +731,7 @@ int bsamg_hier_create(bsamg_ctx* ctx, int ndims, int nrvars, int mbc, int proble
   h->pp.gamma = nparams > 2 ? params[2] : 0.0;
   h->pp.lambda = nparams > 3 ? params[3] : 0.0;
   h->pp.czero = nparams > 4 ? params[4] : 0.0;
+  h->pp.cpress = nparams > 5 ? params[5] : 0.0;
   for (int v = 0; v < kMaxVars; v++) h->pp.qpo[v] = (qpo && v < nrvars) ? qpo[v] : 0.0;
   h->pp.nrvars = nrvars;
   h->pp.problem = problem_kind;

@@ -19,7 +19,9 @@ constexpr int kInternalBC = 999;         // nodeinfodef.f90:59
 constexpr int kMaxVars = 10;             // nodeinfodef.f90:64
 constexpr int kBlock = 256;              // threads per block of the cell kernels
 
-enum Problem : int { kCH = 1, kBio = 2 };
+enum Problem : int { kCH = 1, kBio = 2, kGrowth = 3 };
+// variables of a plugin
+constexpr int nvars_of(int problem) { return problem == kGrowth ? 3 : 2; }
 
 struct PatchDev {
   int mx[3];   // interior extents (1 for the unused dimension in 2D)
@@ -74,7 +76,7 @@ enum GhostType : int {
   kGCopy = 0,     // dst = src
   kGCopyAdd = 1,  // dst = src + qpo[v]
   kGCopySub = 2,  // dst = src - qpo[v]
-  kGBC = 3,       // dst = (mask bit v) ? 2 - src : src
+  kGBC = 3,       // dst = (mask bit v) ? 2 - src : (mask bit 8+v) ? -src : src
   kGCfA = 4,      // a1*s0 + a2*s1 + a3*c0
   kGCfAB = 5,     // a1*s0 + a2*s1 + a3*(b1*c0 + b2*c1 + b3*c2)
   kGCfAC = 6,     // a1*s0 + a2*s1 + a3*(c1*c0 + c2*c1 + c3*c2 + c4*c3)
@@ -87,11 +89,12 @@ struct GhostOp {
   int sp;     // source patch for copies, parent patch for CF ops
   int s0, s1; // source cells (copies: in sp; CF: fine cells in dp)
   int c0, c1, c2, c3;  // coarse cells in sp (CF ops)
-  int mask;   // BC: Dirichlet-variable mask
+  int mask;   // BC: bits 0-7 variables with value 1 on the face (2 - q), bits 8-15 value 0 (-q)
 };
 
 struct ProbParams {
   double dt, eps2, gamma, lambda, czero;
+  double cpress;  // growth plugin: pressure source coefficient
   double qpo[kMaxVars];
   int nrvars;
   int problem;

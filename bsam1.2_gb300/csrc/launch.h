@@ -8,7 +8,7 @@
 
 namespace bsamg {
 
-constexpr int kNormOutLen = 8 + 2 * 128;
+constexpr int kNormOutLen = 8 + 3 * 128;
 
 struct LaunchCtx {
   const PatchDev* P;  // device patch table
@@ -45,7 +45,8 @@ int launch_norm_partial(const LaunchCtx& c, const Blk* blk, int nblk,
                         double* partial, int store_rf);
 // deterministic final sum; writes out[0] = norm, out[1] = raw sum,
 // and ok[0] = 0 when the norm is finite, 1 otherwise.  out must hold
-// kNormOutLen doubles (out[8 ..] is scratch of the two-stage sum).
+// kNormOutLen doubles (out[8 ..] is scratch of the two-stage sum); the
+// partials hold nrvars values per block.
 int launch_norm_finish(cudaStream_t s, const double* partial, int nblk,
                        int nrvars, double count, int errortype, double* out,
                        int* nonfinite);

@@ -476,7 +476,7 @@ __device__ __forceinline__ void ghost32_apply(const PatchDev* __restrict__ P, fl
       case kGCopy:
       case kGCopyAdd:
       case kGCopySub: val = sq[g.s0]; break;  // the qpo offset cancels in a correction
-      case kGBC: val = ((g.mask >> v) & 1) ? -sq[g.s0] : sq[g.s0]; break;  // 2 - q -> -e
+      case kGBC: val = ((g.mask >> v) & 0x101) ? -sq[g.s0] : sq[g.s0]; break;  // 2 - q, -q -> -e
       case kGCfA: val = fA1 * dq[g.s0] + fA2 * dq[g.s1] + fA3 * sq[g.c0]; break;
       case kGCfAB: val = fA1 * dq[g.s0] + fA2 * dq[g.s1] + fA3 * (fB1 * sq[g.c0] + fB2 * sq[g.c1] + fB3 * sq[g.c2]); break;
       default:

@@ -81,7 +81,7 @@ int host_set_ghost(Model& M, int level) {
         case kGCopy: val = sq[o.s0]; break;
         case kGCopyAdd: val = sq[o.s0] + M.src.pp.qpo[v]; break;
         case kGCopySub: val = sq[o.s0] - M.src.pp.qpo[v]; break;
-        case kGBC: val = ((o.mask >> v) & 1) ? 2.0 - sq[o.s0] : sq[o.s0]; break;
+        case kGBC: val = ((o.mask >> v) & 1) ? 2.0 - sq[o.s0] : (((o.mask >> (8 + v)) & 1) ? -sq[o.s0] : sq[o.s0]); break;
         case kGCfA: val = a1 * dq[o.s0] + a2 * dq[o.s1] + a3 * sq[o.c0]; break;
         case kGCfAB: val = a1 * dq[o.s0] + a2 * dq[o.s1] + a3 * (b1 * sq[o.c0] + b2 * sq[o.c1] + b3 * sq[o.c2]); break;
         default:

@@ -108,3 +108,31 @@ def ch_circle_patch(eps, seed, radius=0.25, noise=0.01, center=(0.5, 0.5, 0.5), 
         q[tuple(slice(1, -1) for _ in mx) + (0,)] = phi
         return q
     return fn
+
+
+def growth_sphere(eps, seed, radius=0.1, noise=0.02, center=(0.5, 0.5, 0.5), length=1.0):
+    """Initial condition of the three-variable growth plugin on a patch of
+    any level: phi = tanh((r0 - r)/(sqrt(2) eps)) with r0 = radius +
+    noise*U(-1,1) per cell (U from splitmix64 on the cell's global index on
+    its level), nutrient n = 1, pressure p = 0.  Returns fn(level, mx, dx,
+    xlower) -> ghosted Fortran-layout array with three variables."""
+    def fn(level, mx, dx, xl):
+        nd = len(mx)
+        nglob = [int(round(length / dx[d])) for d in range(nd)]
+        i0 = [int(round(xl[d] / dx[d])) for d in range(nd)]
+        ax = [(np.arange(mx[d]) + 0.5) * dx[d] + xl[d] for d in range(nd)]
+        coords = np.meshgrid(*ax, indexing="ij")
+        r = np.sqrt(sum((c - center[d]) ** 2 for d, c in enumerate(coords)))
+        idx = np.meshgrid(*[np.arange(mx[d], dtype=np.uint64) + np.uint64(i0[d]) for d in range(nd)], indexing="ij")
+        g = idx[0]
+        stride = np.uint64(1)
+        for d in range(1, nd):
+            stride = stride * np.uint64(nglob[d - 1])
+            g = g + idx[d] * stride
+        r0 = radius + noise * splitmix_pm1(seed, g)
+        q = np.zeros(tuple(m + 2 for m in mx) + (3,), order="F")
+        inner = tuple(slice(1, -1) for _ in mx)
+        q[inner + (0,)] = np.tanh((r0 - r) / (np.sqrt(2.0) * eps))
+        q[inner + (1,)] = 1.0
+        return q
+    return fn

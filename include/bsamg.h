@@ -61,6 +61,13 @@ typedef struct bsamg_hier bsamg_hier;
 /* problem kinds: the device form of a PROBLEM/<name> plugin */
 #define BSAMG_PROBLEM_CH 1        /* PROBLEM/CH/problem.f90 */
 #define BSAMG_PROBLEM_BIOGROWTH 2 /* PROBLEM/BioGrowth/problem.f90 */
+/* Three-variable growth plugin (phi, nutrient n, pressure p; nrvars = 3);
+ * no reference counterpart (the reference's 3D BioGrowth is a stub,
+ * BioGrowth/problem.f90:445-478, and has no pressure).  phi and n follow
+ * BioGrowth's equations with 2*ndims neighbours; p solves
+ * -Lap(p)/h^2 - cpress*phi*n = 0.  params: dt, eps, gamma, lambda, czero,
+ * cpress.  Physical faces: phi reflected, n = 1, p = 0. */
+#define BSAMG_PROBLEM_GROWTH 3
 
 /* fields of a patch (nodeinfodef.f90:184-214) */
 #define BSAMG_FIELD_Q 0

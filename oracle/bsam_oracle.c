@@ -45,6 +45,7 @@ typedef struct {
 struct bsamo_hier {
   int ndims, nrvars, mbc, problem;
   double dt, eps, eps2, gamma, lambda, czero;
+  double cpress; /* growth plugin: pressure source coefficient */
   double qpo[10];
   int np, cap;
   OPatch* p;
@@ -106,9 +107,12 @@ int bsamo_create(int ndims, int nrvars, int mbc, int problem,
   if (ndims < 2 || ndims > 3) return -2;
   if (nrvars < 1 || nrvars > 10) return -2;
   if (mbc != 1) return -2; /* mbc = 2 (P2 prolongation) not restated */
-  if (problem != BSAMO_PROBLEM_CH && problem != BSAMO_PROBLEM_BIOGROWTH)
+  if (problem != BSAMO_PROBLEM_CH && problem != BSAMO_PROBLEM_BIOGROWTH &&
+      problem != BSAMO_PROBLEM_GROWTH)
     return -2;
   if (nparams < 2) return -2;
+  if ((problem == BSAMO_PROBLEM_GROWTH) != (nrvars == 3)) return -2;
+  if (problem == BSAMO_PROBLEM_GROWTH && nparams < 6) return -2;
   bsamo_hier* h = (bsamo_hier*)calloc(1, sizeof(*h));
   h->ndims = ndims;
   h->nrvars = nrvars;
@@ -120,6 +124,7 @@ int bsamo_create(int ndims, int nrvars, int mbc, int problem,
   h->gamma = nparams > 2 ? params[2] : 0.0;
   h->lambda = nparams > 3 ? params[3] : 0.0;
   h->czero = nparams > 4 ? params[4] : 0.0;
+  h->cpress = nparams > 5 ? params[5] : 0.0;
   for (int v = 0; v < 10; v++) h->qpo[v] = (qpo && v < nrvars) ? qpo[v] : 0.0;
   *out = h;
   return 0;
@@ -473,6 +478,40 @@ static void relax_bio2d(const bsamo_hier* h, OPatch* p, int ipass) {
     }
 }
 
+/* Growth plugin (no reference counterpart): phi and n as BioGrowth's
+ * RelaxGrid2D with 2*ndims neighbours, then p = (f3 + Sum p_nb/h^2 +
+ * cpress*phi*n) / (2*ndims/h^2) from the updated phi and n. */
+static void relax_growth(const bsamo_hier* h, OPatch* p, int ipass) {
+  double hh = p->dx[0];
+  double h2 = hh * hh;
+  double dt = h->dt;
+  int nd = h->ndims;
+  double kk = 2.0 * nd;
+  double tmp1 = dt * h->eps2 / h2, tmp3 = 1.0 / h2;
+  double c2 = kk * tmp1 + 1.0, c3 = kk * tmp3;
+  int kmx = nd == 3 ? p->mx[2] : 1;
+  for (int k = 1; k <= kmx; k++)
+    for (int j = 1; j <= p->mx[1]; j++)
+      for (int i = 1 + imod((nd == 3 ? k : 0) + j + ipass, 2); i <= p->mx[0]; i += 2) {
+        double phi = Q(p, i, j, k, 0), ol = QO(p, i, j, k, 0);
+        double tmp2 = c2 + dt * sqr(phi);
+        double s0 = Q(p, i - 1, j, k, 0) + Q(p, i + 1, j, k, 0) + Q(p, i, j - 1, k, 0) + Q(p, i, j + 1, k, 0);
+        double s1 = Q(p, i + 1, j, k, 1) + Q(p, i - 1, j, k, 1) + Q(p, i, j + 1, k, 1) + Q(p, i, j - 1, k, 1);
+        double s2 = Q(p, i + 1, j, k, 2) + Q(p, i - 1, j, k, 2) + Q(p, i, j + 1, k, 2) + Q(p, i, j - 1, k, 2);
+        if (nd == 3) {
+          s0 = s0 + Q(p, i, j, k - 1, 0) + Q(p, i, j, k + 1, 0);
+          s1 = s1 + Q(p, i, j, k + 1, 1) + Q(p, i, j, k - 1, 1);
+          s2 = s2 + Q(p, i, j, k + 1, 2) + Q(p, i, j, k - 1, 2);
+        }
+        double np = (FF(p, i, j, k, 0) + dt * growth(h, ol) * (Q(p, i, j, k, 1) - h->czero) + tmp1 * s0) / tmp2;
+        double tmp4 = c3 + uptake(h, ol);
+        double nn = (FF(p, i, j, k, 1) + tmp3 * s1) / tmp4;
+        Q(p, i, j, k, 0) = np;
+        Q(p, i, j, k, 1) = nn;
+        Q(p, i, j, k, 2) = (FF(p, i, j, k, 2) + tmp3 * s2 + h->cpress * np * nn) / c3;
+      }
+}
+
 /* RelaxGrid3D, BioGrowth/problem.f90:445-478 (zero stub) */
 static void relax_bio3d(const bsamo_hier* h, OPatch* p, int ipass) {
   (void)h;
@@ -522,6 +561,24 @@ static void op_eval(const bsamo_hier* h, const OpView* w, int i, int j, int k,
       out[1] = opA(w, i, j, k, 1) - cube(opA(w, i, j, k, 0)) +
                tmp2 * ulap3(w->p, w->a, i, j, k, 0, w->coarse);
     }
+  } else if (h->problem == BSAMO_PROBLEM_GROWTH) {
+    double dt = h->dt;
+    double tmp1 = dt * h->eps2 / h2, tmp3 = 1.0 / h2;
+    int kk = h->ndims == 3 ? k : 1;
+    double l0, l1, l2;
+    if (h->ndims == 2) {
+      l0 = ulap2(w->p, w->a, i, j, 0, w->coarse);
+      l1 = ulap2(w->p, w->a, i, j, 1, w->coarse);
+      l2 = ulap2(w->p, w->a, i, j, 2, w->coarse);
+    } else {
+      l0 = ulap3(w->p, w->a, i, j, k, 0, w->coarse);
+      l1 = ulap3(w->p, w->a, i, j, k, 1, w->coarse);
+      l2 = ulap3(w->p, w->a, i, j, k, 2, w->coarse);
+    }
+    double a0 = opA(w, i, j, kk, 0), a1 = opA(w, i, j, kk, 1), o0 = opO(w, i, j, kk, 0);
+    out[0] = a0 - tmp1 * l0 + dt * cube(a0) - dt * growth(h, o0) * (a1 - h->czero);
+    out[1] = -tmp3 * l1 + uptake(h, o0) * a1;
+    out[2] = -tmp3 * l2 - h->cpress * a0 * a1;
   } else {
     if (h->ndims == 2) {
       double dt = h->dt;
@@ -545,7 +602,8 @@ static inline double source_val(const bsamo_hier* h, const OPatch* p, int i,
   if (h->problem == BSAMO_PROBLEM_CH) {
     return v == 0 ? QO(p, i, j, k, 0) : -QO(p, i, j, k, 0);
   }
-  if (h->ndims == 2) return v == 0 ? (1.0 + h->dt) * QO(p, i, j, k, 0) : 0.0;
+  if (h->problem == BSAMO_PROBLEM_GROWTH || h->ndims == 2)
+    return v == 0 ? (1.0 + h->dt) * QO(p, i, j, k, 0) : 0.0;
   return 0.0;
 }
 
@@ -556,9 +614,10 @@ static void user_bc(const bsamo_hier* h, OPatch* p, int bc) {
   for (int d = 0; d < 3; d++) ul[d] = p->mx[d] + mbc;
   int kl = nd == 3 ? ll : 1, ku = nd == 3 ? ul[2] : 1;
   for (int v = 0; v < h->nrvars; v++) {
-    /* per variable: reflect (0) or Dirichlet 2-q (1) */
+    /* per variable: reflect (0), Dirichlet 2-q (1) or Dirichlet -q (2) */
     int dir;
     if (h->problem == BSAMO_PROBLEM_CH) dir = nd == 3 ? 1 : 0;
+    else if (h->problem == BSAMO_PROBLEM_GROWTH) dir = v;
     else dir = nd == 3 ? 1 : (v == 1);
     for (int ibc = 1; ibc <= mbc; ibc++) {
       int d = (bc - 1) / 2, hi = (bc - 1) % 2;
@@ -568,19 +627,19 @@ static void user_bc(const bsamo_hier* h, OPatch* p, int bc) {
         for (int k = kl; k <= ku; k++)
           for (int j = ll; j <= ul[1]; j++) {
             double s = Q(p, gsrc, j, k, v);
-            Q(p, gdst, j, k, v) = dir ? 2.0 - s : s;
+            Q(p, gdst, j, k, v) = dir == 1 ? 2.0 - s : (dir == 2 ? -s : s);
           }
       } else if (d == 1) {
         for (int k = kl; k <= ku; k++)
           for (int i = ll; i <= ul[0]; i++) {
             double s = Q(p, i, gsrc, k, v);
-            Q(p, i, gdst, k, v) = dir ? 2.0 - s : s;
+            Q(p, i, gdst, k, v) = dir == 1 ? 2.0 - s : (dir == 2 ? -s : s);
           }
       } else {
         for (int j = ll; j <= ul[1]; j++)
           for (int i = ll; i <= ul[0]; i++) {
             double s = Q(p, i, j, gsrc, v);
-            Q(p, i, j, gdst, v) = dir ? 2.0 - s : s;
+            Q(p, i, j, gdst, v) = dir == 1 ? 2.0 - s : (dir == 2 ? -s : s);
           }
       }
     }
@@ -1100,8 +1159,10 @@ static void relax_patch(const bsamo_hier* h, OPatch* p, int ipass) {
   /* RelaxPatch, afasroutines.f90:560-607 */
   if (h->problem == BSAMO_PROBLEM_CH) {
     if (h->ndims == 2) relax_ch2d(h, p, ipass); else relax_ch3d(h, p, ipass);
-  } else {
+  } else if (h->problem == BSAMO_PROBLEM_BIOGROWTH) {
     if (h->ndims == 2) relax_bio2d(h, p, ipass); else relax_bio3d(h, p, ipass);
+  } else {
+    relax_growth(h, p, ipass);
   }
 }
 
@@ -1900,9 +1961,9 @@ int bsamo_regrid(const bsamo_hier* old, const bsamo_regrid_params* prm, bsamo_qi
                  bsamo_hier** out) {
   if (!old || !old->committed || !prm || !out) return -1;
   if (prm->maxlevel < 0 || prm->maxlevel > MAXDEPTH || (prm->initial && !qinit)) return -2;
-  double params[5] = {old->dt, old->eps, old->gamma, old->lambda, old->czero};
+  double params[6] = {old->dt, old->eps, old->gamma, old->lambda, old->czero, old->cpress};
   bsamo_hier* h = NULL;
-  int rc = bsamo_create(old->ndims, old->nrvars, old->mbc, old->problem, params, 5, old->qpo, &h);
+  int rc = bsamo_create(old->ndims, old->nrvars, old->mbc, old->problem, params, 6, old->qpo, &h);
   if (rc) return rc;
   for (int n = 0; n < old->np; n++) { /* the root and the levels below persist */
     const OPatch* p = &old->p[n];

@@ -35,6 +35,7 @@ typedef struct bsamo_hier bsamo_hier;
 /* problem kinds (same codes as include/bsamg.h) */
 #define BSAMO_PROBLEM_CH 1
 #define BSAMO_PROBLEM_BIOGROWTH 2
+#define BSAMO_PROBLEM_GROWTH 3 /* three variables, no reference counterpart */
 
 /* field codes (same codes as include/bsamg.h) */
 #define BSAMO_FIELD_Q 0
@@ -44,7 +45,7 @@ typedef struct bsamo_hier bsamo_hier;
 #define BSAMO_FIELD_RF 4
 #define BSAMO_FIELD_FTMP 5
 
-/* params: [0]=dt [1]=eps [2]=gamma [3]=lambda [4]=czero; qpo[nrvars] */
+/* params: [0]=dt [1]=eps [2]=gamma [3]=lambda [4]=czero [5]=cpress; qpo[nrvars] */
 int bsamo_create(int ndims, int nrvars, int mbc, int problem,
                  const double* params, int nparams, const double* qpo,
                  bsamo_hier** out);

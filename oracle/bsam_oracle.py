@@ -12,7 +12,7 @@ import numpy as np
 from .build import build_oracle  # noqa: F401  (package-relative when imported as oracle.*)
 
 FIELD = {"q": 0, "qold": 1, "qc": 2, "f": 3, "rf": 4, "ftmp": 5}
-PROBLEM = {"ch": 1, "biogrowth": 2}
+PROBLEM = {"ch": 1, "biogrowth": 2, "growth": 3}
 
 _lib = None
 

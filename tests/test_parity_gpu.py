@@ -21,11 +21,13 @@ RTOL = 1e-12
 CH2 = dict(ndims=2, problem="ch", params=[1e-3, 0.01])
 CH3 = dict(ndims=3, problem="ch", params=[5e-4, 0.02])
 BIO2 = dict(ndims=2, problem="biogrowth", params=[0.1, 0.05, 1.5, 2.0, 0.5])
+GROWTH3 = dict(ndims=3, problem="growth", params=[0.01, 0.025, 1.5, 2.0, 0.5, 1.0], nrvars=3)
 
 
 def make_pair(pkg, ctx, oracle_mod, cfg, spec):
-    g = pkg.Hierarchy(ctx, cfg["ndims"], 2, cfg["problem"], cfg["params"])
-    o = oracle_mod.OracleHierarchy(cfg["ndims"], 2, cfg["problem"], cfg["params"])
+    nv = cfg.get("nrvars", 2)
+    g = pkg.Hierarchy(ctx, cfg["ndims"], nv, cfg["problem"], cfg["params"])
+    o = oracle_mod.OracleHierarchy(cfg["ndims"], nv, cfg["problem"], cfg["params"])
     spec.apply(g)
     spec.apply(o)
     return g, o
@@ -79,6 +81,8 @@ CASES = {
     "bio2d-amr": (BIO2, lambda: H.amr2d(periodic=False)),
     "ch3d-amr-periodic": (CH3, lambda: H.amr3d(periodic=True)),
     "ch3d-amr-dirichlet": (CH3, lambda: H.amr3d(periodic=False)),
+    "growth3d": (GROWTH3, lambda: uniform_spec(3, 16, DIRICHLET3)),
+    "growth3d-amr": (GROWTH3, lambda: H.amr3d(periodic=False)),
 }
 
 
@@ -131,6 +135,9 @@ def _init(pkg, spec, hs, cfg, seed):
         h = p["dx"][0]
         if cfg["problem"] == "ch":
             q = pkg.initial.ch_spinodal(shape, cfg["params"][1], h, seed=seed + p["id"] + 50)
+        elif cfg["problem"] == "growth":
+            q = pkg.initial.growth_sphere(cfg["params"][1], seed=seed, radius=0.3)(
+                p["level"], list(shape), p["dx"][:nd], p["xlower"][:nd])
         else:
             q = np.zeros(tuple(n + 2 for n in shape) + (2,), order="F")
             q[(slice(1, -1),) * nd + (0,)] = pkg.initial.splitmix_pm1(

@@ -130,3 +130,27 @@ def test_regrid_every_step_matches_oracle(pkg, ctx, oracle_mod):
             a, b = g.get(p["id"], "q"), o.get(p["id"], "q")
             worst = max(worst, float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)))
         assert worst <= RTOL, (step, worst)
+
+
+def test_growth3d_regrid_and_steps_match_oracle(pkg, ctx, oracle_mod):
+    """The three-variable growth plugin on a regridded 3D mesh (cfg4's shape
+    at 16^3): meshes, fields and time steps as the oracle's."""
+    params = [0.01, 0.025, 1.5, 2.0, 0.5, 1.0]
+    fn = pkg.initial.growth_sphere(0.025, seed=9, radius=0.25)
+    g = pkg.Hierarchy(ctx, 3, 3, "growth", params)
+    o = oracle_mod.OracleHierarchy(3, 3, "growth", params)
+    for h in (g, o):
+        h.build_uniform([16, 16, 16], -3, [10] * 6, [0, 0, 0], [1, 1, 1])
+        h.commit()
+        h.put(0, "q", fn(0, [16] * 3, [1 / 16] * 3, [0.0] * 3))
+    for step in range(3):
+        kw = dict(tagging="gradient", initial=step == 0, qtolerance=0.25, first_id=1000 * (step + 1))
+        g = g.regrid(pkg.regrid_params(2, **kw), fn if step == 0 else None)
+        o = oracle_mod.regrid(o, oracle_mod.regrid_params(2, **kw), fn if step == 0 else None)
+        tab = same(g, o)
+        fin = max(p["level"] for p in tab)
+        assert fin >= 1
+        ng, rg = g.time_step(step == 0, fin, -3, tol=1e-9, maxvcycles=30)
+        no, ro = o.time_step(step == 0, fin, -3, tol=1e-9, maxvcycles=30)
+        assert ng == no, (step, rg, ro)
+        np.testing.assert_allclose(rg, ro, rtol=1e-10, atol=0)
