@@ -119,6 +119,12 @@ def lib():
         "bsamg_ch_residual_norm_noalloc": ([P, P, I, IP, D, D, D, I, P, P], I),
         "bsamg_host_register": ([P, SZ], I),
         "bsamg_host_unregister": ([P], I),
+        "bsamg_after_step_stats": ([P, I, DP, ctypes.POINTER(ctypes.c_longlong)], I),
+        "bsamg_write_q": ([P, ctypes.c_char_p, D, I], I),
+        "bsamg_write_uniform_q": ([P, ctypes.c_char_p, D, I], I),
+        "bsamg_read_q": ([P, ctypes.c_char_p, I, DP, ctypes.POINTER(P)], I),
+        "bsamg_format_f25_12": ([D, ctypes.c_char_p], I),
+        "bsamg_format_stats_line": ([D, DP, ctypes.c_longlong, ctypes.c_char_p, SZ], I),
         "bsamg_strerror": ([I], ctypes.c_char_p),
         "bsamg_last_error_detail": ([], ctypes.c_char_p),
     }
@@ -226,6 +232,33 @@ class Hierarchy:
         new.ctx, new.ndims, new.nrvars, new.h = self.ctx, self.ndims, self.nrvars, h
         return new
 
+    def after_step_stats(self, finest):
+        """AfterStepStatistics + GetMeshSize (bsamg_after_step_stats):
+        (integral of phi, CH 2D energy, composite mesh size)."""
+        r = (ctypes.c_double * 2)()
+        m = ctypes.c_longlong()
+        _ck(lib().bsamg_after_step_stats(self.h, finest, r, ctypes.byref(m)), "bsamg_after_step_stats")
+        return r[0], r[1], m.value
+
+    def write_q(self, path, time, finest):
+        """WriteQ: the text frame file of levels 0..finest (bsamg_write_q)."""
+        _ck(lib().bsamg_write_q(self.h, os.fsencode(path), time, finest), "bsamg_write_q")
+
+    def write_uniform_q(self, path, time, finest):
+        """WriteUniformMeshQ: the composite on one uniform grid (bsamg_write_uniform_q)."""
+        _ck(lib().bsamg_write_uniform_q(self.h, os.fsencode(path), time, finest), "bsamg_write_uniform_q")
+
+    def read_q(self, path, first_id=1000):
+        """ReadQ: restart from a frame file, with this hierarchy as the root
+        grid (bsamg_read_q); returns (new Hierarchy, frame time)."""
+        h = ctypes.c_void_p()
+        t = ctypes.c_double()
+        _ck(lib().bsamg_read_q(self.h, os.fsencode(path), first_id, ctypes.byref(t), ctypes.byref(h)),
+            "bsamg_read_q")
+        new = Hierarchy.__new__(Hierarchy)
+        new.ctx, new.ndims, new.nrvars, new.h = self.ctx, self.ndims, self.nrvars, h
+        return new, t.value
+
     def commit(self):
         _ck(lib().bsamg_commit(self.h), "bsamg_commit")
 
@@ -324,6 +357,20 @@ class Hierarchy:
         n = ctypes.c_longlong()
         _ck(lib().bsamg_launch_count(self.h, ctypes.byref(n)), "bsamg_launch_count")
         return n.value
+
+
+def format_f25(x):
+    """One F25.12 field as the frame files hold it."""
+    b = ctypes.create_string_buffer(26)
+    _ck(lib().bsamg_format_f25_12(float(x), b), "bsamg_format_f25_12")
+    return b.value.decode()
+
+
+def format_stats_line(time, integral, meshsize):
+    """One OUT/stats.dat record (newline included)."""
+    b = ctypes.create_string_buffer(128)
+    _ck(lib().bsamg_format_stats_line(time, _da(integral, 2), meshsize, b, 128), "bsamg_format_stats_line")
+    return b.value.decode()
 
 
 def pin(arr):

@@ -24,6 +24,8 @@ UNITS = {
     "hier.cu": [],
     "ghostc.cpp": [],
     "regrid.cpp": [],
+    "io.cu": ["--fmad=false"],
+    "frames.cpp": [],
 }
 
 

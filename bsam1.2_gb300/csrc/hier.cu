@@ -26,6 +26,11 @@ int cuda_fail(cudaError_t e, const char* what) {
   return BSAMG_ERR_CUDA;
 }
 
+int io_fail(const char* what) {
+  g_detail = what;
+  return BSAMG_ERR_IO;
+}
+
 #define CK(call)                                   \
   do {                                             \
     cudaError_t e__ = (call);                      \
@@ -392,6 +397,8 @@ int build_uniform(Hier& H, const int mx[3], int minlevel, const int mthbc[6], co
     mb[2 * d + 1] = minlevel < 0 ? mx[d] / 2 : mx[d];
   }
   RET(add_patch(H, 0, 0, minlevel < 0 ? 1 : -1, cmx, mg, mb, mthbc, dx, xl));
+  H.has_root_xupper = true;
+  for (int d = 0; d < 3; d++) H.root_xupper[d] = d < nd ? xupper[d] : 0.0;
   for (int l = -1; l >= minlevel; l--) {
     int nmx[3] = {1, 1, 1}, nmg[6] = {1, 1, 1, 1, 1, 1}, nmb[6] = {1, 1, 1, 1, 1, 1};
     double ndx[3] = {0, 0, 0};
@@ -981,6 +988,7 @@ const char* bsamg_strerror(int status) {
     case BSAMG_ERR_NONFINITE: return "residual norm is not finite";
     case BSAMG_ERR_UNSUPPORTED: return "configuration not supported";
     case BSAMG_ERR_NOT_FOUND: return "unknown patch id";
+    case BSAMG_ERR_IO: return "frame file could not be read or written (see bsamg_last_error_detail)";
   }
   return "unknown status";
 }

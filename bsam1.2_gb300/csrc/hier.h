@@ -54,6 +54,8 @@ struct Hier {
   int ndims = 2, nrvars = 2, mbc = 1, problem = 1;
   ProbParams pp{};
   std::vector<double> params;  // as given to bsamg_hier_create
+  bool has_root_xupper = false;  // built by bsamg_build_uniform: the root's xupper
+  double root_xupper[3] = {};
   std::vector<HostPatch> patches;
   std::unordered_map<int, int> id2idx;
   bool committed = false;
@@ -127,6 +129,8 @@ void coefficients(const Hier& H, double h, double* c);
 // host tables of an uncommitted hierarchy (parent links, extents, level
 // lists, periodic offsets); commit() starts with it
 int build_tables(Hier& H);
+// xupper of a patch as the reference's frame files carry it (frames.cpp)
+double xupper_of(const Hier& H, const HostPatch& P, int d);
 // AMR regrid of a committed hierarchy into a new one (regrid.cpp)
 int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* user, bsamg_hier** out);
 using GraphKey = std::tuple<int, int, int, int, int>;

@@ -51,6 +51,18 @@ int launch_norm_finish(cudaStream_t s, const double* partial, int nblk,
                        int nrvars, double count, int errortype, double* out,
                        int* nonfinite);
 int launch_ghost_stage(const LaunchCtx& c, const GhostOp* ops, int n);
+
+// ---- after-step statistics and uniform-mesh output (io.cu, --fmad=false) ----
+// partial[2*(pofs + b)] = (mass, energy) of block b of a level's interior
+// list (coarse = false) or, negated, of the parent cells of its coarse list
+int launch_stats(const LaunchCtx& c, const Blk* blk, int nblk, bool coarse, int mass, int energy, double* partial,
+                 int pofs);
+int launch_stats_finish(cudaStream_t s, const double* partial, int n, double* out);
+// F = mass-corrected prolongation of the uniform (n+2)^d block A (one variable)
+int launch_uniform_prolong(cudaStream_t s, int ndims, const double* A, double* F, const int n[3]);
+// a patch's ghosted q (nv variables) into the uniform block U (extents un)
+int launch_uniform_scatter(cudaStream_t s, int ndims, const double* pool, long long oq, long long sq, const int qn[3],
+                           const int g[3], double* U, const int un[3], int nv);
 int launch_ghost_program_1cta(const LaunchCtx& c, const GhostOp* ops,
                               const int* stage_off, int nstages);
 

@@ -576,6 +576,8 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   bsamg_hier* nh = nullptr;
   r = bsamg_hier_create(H.ctx, nd, nv, H.mbc, H.problem, H.params.data(), (int)H.params.size(), H.pp.qpo, &nh);
   if (r) return r;
+  nh->has_root_xupper = H.has_root_xupper;
+  std::memcpy(nh->root_xupper, H.root_xupper, sizeof(H.root_xupper));
   auto fail = [&](int rc) {
     bsamg_hier_destroy(nh);
     return rc;

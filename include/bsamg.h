@@ -57,6 +57,7 @@ typedef struct bsamg_hier bsamg_hier;
 #define BSAMG_ERR_NONFINITE -5   /* the residual norm is NaN or Inf */
 #define BSAMG_ERR_UNSUPPORTED -6 /* configuration not implemented */
 #define BSAMG_ERR_NOT_FOUND -7   /* unknown patch id */
+#define BSAMG_ERR_IO -8          /* a frame file could not be opened, read, parsed or written */
 
 /* problem kinds: the device form of a PROBLEM/<name> plugin */
 #define BSAMG_PROBLEM_CH 1        /* PROBLEM/CH/problem.f90 */
@@ -187,6 +188,46 @@ int bsamg_time_step(bsamg_hier* h, int first, int finestlevel, int minlevel,
                     int nsmooth, int maxvcycles, double qerrortol,
                     int updateauxfreq, int errortype, int mode, int strict,
                     int* ncycles, double* residuals);
+
+/* ---- frame files, restart and after-step statistics ----
+ *
+ * bsamg_after_step_stats -> the AfterStepStatistics + GetMeshSize pass of
+ *     TakeTimeSteps (LIBRARY/bsamroutines.f90:763-775, :846-868, :918-963)
+ *     with the plugin's AfterStep2D/3D (PROBLEM/CH/problem.f90:149-215 and
+ *     Energy2D :518-547; PROBLEM/BioGrowth/problem.f90:107-152) as one
+ *     device reduction over levels 0..finestlevel: integral[0] = the
+ *     integral of phi (variable 1), integral[1] = the CH 2D energy (0 for
+ *     the other plugins), *meshsize = the composite cell count.  A level > 0
+ *     patch subtracts its parent's cells under it, as the reference does.
+ *     BioGrowth 3D reports zeros (its AfterStep3D is empty); the growth
+ *     plugin reports the integral of phi.  Sums are a fixed-order tree
+ *     (deterministic; equal to the reference's sequential SUM to rounding).
+ * bsamg_write_q -> WriteQ, LIBRARY/bsaminputoutput.f90:60-181: the text
+ *     frame file (F25.12 reals, I3/I8 integers, one record per ghosted cell)
+ *     of levels 0..finestlevel, patches in visiting order; the caller names
+ *     the file (the reference uses ./OUT/mNNNNN.dat).
+ * bsamg_write_uniform_q -> WriteUniformMeshQ, :446-572: the composite
+ *     solution on one uniform grid at the finest spacing (root prolonged with
+ *     the mass-corrected bilinear/trilinear operator, each level's patches
+ *     copied over it), computed on the device and written as one patch.
+ * bsamg_read_q -> ReadQ, :184-443: restart from a frame file.  `root` is a
+ *     committed hierarchy holding the run's root grid and the levels below it
+ *     (bsamg_build_uniform); the new hierarchy copies it, takes the root's q
+ *     from the file (ghost layers included) and adds the file's refinement
+ *     patches (ids first_id, first_id + 1, ...; each parented by the patch of
+ *     the level below that contains it; qold = q).  The root block is checked
+ *     as ReadQ checks it (ndims, ratio 2, nrvars, dx, xlower, xupper, mx,
+ *     mglobal); a mismatch or a malformed file returns BSAMG_ERR_IO.  *time
+ *     receives the frame's time.
+ * bsamg_format_f25_12 -> one F25.12 field (25 characters + NUL into out).
+ * bsamg_format_stats_line -> one OUT/stats.dat record,
+ *     '(3(F25.12),1x,I8)' (bsamroutines.f90:771-775), newline included. */
+int bsamg_after_step_stats(bsamg_hier* h, int finestlevel, double integral[2], long long* meshsize);
+int bsamg_write_q(bsamg_hier* h, const char* path, double time, int finestlevel);
+int bsamg_write_uniform_q(bsamg_hier* h, const char* path, double time, int finestlevel);
+int bsamg_read_q(bsamg_hier* root, const char* path, int first_id, double* time, bsamg_hier** out);
+int bsamg_format_f25_12(double x, char* out);
+int bsamg_format_stats_line(double time, const double integral[2], long long meshsize, char* out, size_t n);
 
 /* Wait for all work of the hierarchy; returns the first deferred error. */
 int bsamg_sync(bsamg_hier* h);

@@ -56,6 +56,8 @@ struct bsamo_hier {
   int mxmax[MAXDEPTH + 1][3];
   int minlevel_present, maxlevel_present;
   double integral[2];
+  int has_root_xupper; /* built by bsamo_build_uniform: the root's xupper */
+  double root_xupper[3];
 };
 
 /* ------------------------------------------------------------------ */
@@ -199,6 +201,8 @@ int bsamo_build_uniform(bsamo_hier* h, const int mx[3], int minlevel,
   int rc = bsamo_patch_add(h, 0, 0, minlevel < 0 ? 1 : -1, cmx, mg, mb, mthbc,
                            dx, xl);
   if (rc) return rc;
+  h->has_root_xupper = 1;
+  for (int d = 0; d < 3; d++) h->root_xupper[d] = d < nd ? xupper[d] : 0.0;
   for (int l = -1; l >= minlevel; l--) {
     int nmx[3] = {1, 1, 1}, nmg[6] = {1, 1, 1, 1, 1, 1}, nmb[6] = {1, 1, 1, 1, 1, 1};
     double ndx[3] = {0, 0, 0};
@@ -1965,6 +1969,8 @@ int bsamo_regrid(const bsamo_hier* old, const bsamo_regrid_params* prm, bsamo_qi
   bsamo_hier* h = NULL;
   int rc = bsamo_create(old->ndims, old->nrvars, old->mbc, old->problem, params, 6, old->qpo, &h);
   if (rc) return rc;
+  h->has_root_xupper = old->has_root_xupper;
+  memcpy(h->root_xupper, old->root_xupper, sizeof(h->root_xupper));
   for (int n = 0; n < old->np; n++) { /* the root and the levels below persist */
     const OPatch* p = &old->p[n];
     if (p->level > 0) continue;
@@ -2041,4 +2047,472 @@ int bsamo_regrid(const bsamo_hier* old, const bsamo_regrid_params* prm, bsamo_qi
   if (nlev(h, level) > 0) set_ghost(h, level, 0); /* AMR(finest) */
   *out = h;
   return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* after-step statistics, frame files and restart                      */
+
+/* one F25.12 field (the edit descriptor of every real in WriteQ,
+ * bsaminputoutput.f90:72, :106-120, :147): the C library's correctly rounded
+ * fixed notation, a field of 25 asterisks when the number needs more than
+ * 25 characters, NaN and Infinity right-justified. */
+void bsamo_format_f25_12(double x, char out[26]) {
+  char b[64];
+  int n;
+  if (isnan(x))
+    n = snprintf(b, sizeof b, "%25s", "NaN");
+  else if (isinf(x))
+    n = snprintf(b, sizeof b, "%25s", x < 0 ? "-Infinity" : "Infinity");
+  else
+    n = snprintf(b, sizeof b, "%25.12f", x);
+  if (n > 25) {
+    memset(b, '*', 25);
+    b[25] = 0;
+  }
+  memcpy(out, b, 26);
+}
+
+static void put_f25(FILE* f, double x) {
+  char b[26];
+  bsamo_format_f25_12(x, b);
+  fputs(b, f);
+}
+
+/* xupper of a patch: the root's as given to RootInit (bsamroutines.f90:
+ * 267-413) for levels <= 0 of a hierarchy built by bsamo_build_uniform;
+ * MakeNewGrid's mbounds(2)*parent%dx + parent%xlower (:1752) for a patch
+ * with a parent above the root; otherwise xlower + mx*dx. */
+static double xupper_of(const bsamo_hier* h, const OPatch* p, int d) {
+  if (p->level <= 0 && h->has_root_xupper) return h->root_xupper[d];
+  if (p->level > 0 && p->parent >= 0) {
+    const OPatch* q = &h->p[p->parent];
+    return (double)p->mbounds[d][1] * q->dx[d] + q->xlower[d];
+  }
+  return p->xlower[d] + (double)p->mx[d] * p->dx[d];
+}
+
+/* Ff (CH/problem.f90:901-915) */
+static inline double ff_energy(double c) {
+  double c2 = c * c;
+  return c2 * (c2 - 2.0) / 4.0;
+}
+
+/* SUM of variable 1 over m0 x m1 x m2 cells of p starting after (i0,j0,k0) */
+static double sum_var1(const OPatch* p, int i0, int j0, int k0, int m0, int m1, int m2) {
+  double s = 0.0;
+  for (int k = 1; k <= m2; k++)
+    for (int j = 1; j <= m1; j++)
+      for (int i = 1; i <= m0; i++) s = s + Q(p, i0 + i, j0 + j, k0 + k, 0);
+  return s;
+}
+
+/* Energy2D (CH/problem.f90:518-547) of variable 1 on the block
+ * c(0:m0+1, 0:m1+1) = q(i0:i0+m0+1, j0:j0+m1+1) of p, spacing hh */
+static double energy2d(const bsamo_hier* h, const OPatch* p, int i0, int j0, int m0, int m1, double hh) {
+#define CE(i, j) Q(p, i0 + (i), j0 + (j), 1, 0)
+  double h2 = hh * hh;
+  double sf = 0.0, sg = 0.0;
+  for (int j = 1; j <= m1; j++)
+    for (int i = 1; i <= m0; i++) sf = sf + ff_energy(CE(i, j));
+  for (int j = 1; j <= m1; j++)
+    for (int i = 1; i <= m0; i++) {
+      double a = CE(i + 1, j) - CE(i, j), b = CE(i, j) - CE(i - 1, j);
+      double c = CE(i, j + 1) - CE(i, j), d = CE(i, j) - CE(i, j - 1);
+      sg = sg + (((a * a + b * b) + c * c) + d * d);
+    }
+  double tmp = h->eps2 / h2 / 4.0;
+  return h2 * (sf + tmp * sg);
+#undef CE
+}
+
+/* AfterStepStatistics + GetMeshSize over levels finest..0 (bsamroutines.f90:
+ * 763-775, :846-868, :918-963) with the plugins' AfterStep2D/3D:
+ * CH 2D integral of phi and Energy2D (CH/problem.f90:149-183), CH 3D the
+ * integral of phi (:186-215), BioGrowth 2D the integral of phi
+ * (BioGrowth/problem.f90:107-136), BioGrowth 3D nothing (:139-152).  A level
+ * > 0 patch subtracts the same quantity of its parent's cells under it (the
+ * parent's q over mbounds).  The growth plugin, which has no reference
+ * counterpart, reports the integral of phi as CH in 3D. */
+int bsamo_after_step_stats(const bsamo_hier* h, int finest, double integral[2], long long* meshsize) {
+  if (!h || !h->committed || !integral) return -1;
+  int nd = h->ndims;
+  int mass = !(h->problem == BSAMO_PROBLEM_BIOGROWTH && nd == 3);
+  int energy = h->problem == BSAMO_PROBLEM_CH && nd == 2;
+  double r1 = 0.0, r2 = 0.0;
+  long long ms = 0;
+  for (int level = finest; level >= 0; level--)
+    for (int a = 0; a < nlev(h, level); a++) {
+      const OPatch* p = &h->p[h->lev_list[level + MAXDEPTH][a]];
+      double hh = p->dx[0], ch = hh * 2.0;
+      double hd = nd == 2 ? hh * hh : hh * hh * hh;
+      double chd = nd == 2 ? ch * ch : ch * ch * ch;
+      long long pm = 1, pc = 1;
+      for (int d = 0; d < nd; d++) {
+        pm *= p->mx[d];
+        pc *= p->mx[d] / 2;
+      }
+      if (level == 0) {
+        if (mass) r1 = r1 + hd * sum_var1(p, 0, 0, 0, p->mx[0], p->mx[1], p->mx[2]);
+        if (energy) r2 = r2 + energy2d(h, p, 0, 0, p->mx[0], p->mx[1], hh);
+        ms += pm;
+      } else {
+        if (p->parent < 0) return -3;
+        const OPatch* q = &h->p[p->parent];
+        int i0 = p->mbounds[0][0] - 1, j0 = p->mbounds[1][0] - 1, k0 = nd == 3 ? p->mbounds[2][0] - 1 : 0;
+        if (mass)
+          r1 = r1 + hd * sum_var1(p, 0, 0, 0, p->mx[0], p->mx[1], p->mx[2]) -
+               chd * sum_var1(q, i0, j0, k0, p->cmx[0], p->cmx[1], p->cmx[2]);
+        if (energy)
+          r2 = r2 + energy2d(h, p, 0, 0, p->mx[0], p->mx[1], hh) - energy2d(h, q, i0, j0, p->cmx[0], p->cmx[1], ch);
+        ms += pm - pc;
+      }
+    }
+  integral[0] = r1;
+  integral[1] = r2;
+  if (meshsize) *meshsize = ms;
+  return 0;
+}
+
+/* one patch block of a frame file: OutputQ (bsaminputoutput.f90:85-129),
+ * WriteQ2D/3D (:132-181).  q is the ghosted Fortran-layout array. */
+static void write_block(FILE* f, int nd, int nv, int level, const double* dx, const double* xl, const double* xu,
+                        const int* mx, const int mg[3][2], const double* q) {
+  fputs("  \n", f); /* WRITE(54,*) ' ': list-directed, a leading blank then ' ' */
+  fprintf(f, "%3d %3d %3d %3d\n", level, nd, 2, nv);
+  const double* rows[3] = {dx, xl, xu};
+  for (int r = 0; r < 3; r++) {
+    for (int d = 0; d < nd; d++) {
+      if (d) fputc(' ', f);
+      put_f25(f, rows[r][d]);
+    }
+    fputc('\n', f);
+  }
+  for (int d = 0; d < nd; d++) fprintf(f, d ? " %8d" : "%8d", mx[d]);
+  fputc('\n', f);
+  for (int d = 0; d < nd; d++) fprintf(f, d ? " %8d %8d" : "%8d %8d", mg[d][0], mg[d][1]);
+  fputc('\n', f);
+  int qn0 = mx[0] + 2, qn1 = mx[1] + 2, qn2 = nd == 3 ? mx[2] + 2 : 1;
+  size_t plane = (size_t)qn0 * qn1 * qn2;
+  for (int k = 0; k < qn2; k++)
+    for (int j = 0; j < qn1; j++)
+      for (int i = 0; i < qn0; i++) {
+        size_t c = ((size_t)k * qn1 + j) * qn0 + i;
+        for (int v = 0; v < nv; v++) { /* 10(F25.12,2X): no blanks after the last value */
+          if (v) fputs("  ", f);
+          put_f25(f, q[v * plane + c]);
+        }
+        fputc('\n', f);
+      }
+}
+
+/* WriteQ (bsaminputoutput.f90:60-82): time, finest level, then every patch
+ * of levels 0..finest in visiting order */
+int bsamo_write_q(const bsamo_hier* h, const char* path, double time, int finest) {
+  if (!h || !h->committed || !path || finest < 0 || finest > MAXDEPTH) return -1;
+  FILE* f = fopen(path, "w");
+  if (!f) return -8;
+  put_f25(f, time);
+  fprintf(f, "\n%3d\n", finest);
+  for (int level = 0; level <= finest; level++)
+    for (int a = 0; a < nlev(h, level); a++) {
+      const OPatch* p = &h->p[h->lev_list[level + MAXDEPTH][a]];
+      double xu[3];
+      int mg[3][2];
+      for (int d = 0; d < 3; d++) {
+        xu[d] = xupper_of(h, p, d);
+        mg[d][0] = p->mglobal[d][0];
+        mg[d][1] = p->mglobal[d][1];
+      }
+      write_block(f, h->ndims, h->nrvars, p->level, p->dx, p->xlower, xu, p->mx, mg, p->q);
+    }
+  return fclose(f) ? -8 : 0;
+}
+
+/* WriteUniformMeshQ (bsaminputoutput.f90:446-572): the root's q prolonged
+ * level by level with the mass-corrected bilinear/trilinear operator
+ * (gridutilities.f90 BiLinProlongationP1MC / TriLinProlongationP1MC) over the
+ * whole domain, each level's patches (ghost layers included) copied over it
+ * in visiting order (CopyPatchToUniformGrid), written as one level-0 patch
+ * at the finest spacing. */
+int bsamo_write_uniform_q(const bsamo_hier* h, const char* path, double time, int finest) {
+  if (!h || !h->committed || !path || finest < 0 || finest > MAXDEPTH) return -1;
+  if (nlev(h, 0) < 1) return -1;
+  int nd = h->ndims, nv = h->nrvars;
+  const OPatch* r = &h->p[h->lev_list[MAXDEPTH][0]];
+  int n[3] = {r->mx[0], r->mx[1], nd == 3 ? r->mx[2] : 1};
+  double dx[3] = {r->dx[0], r->dx[1], r->dx[2]};
+  size_t sz = (size_t)(n[0] + 2) * (n[1] + 2) * (nd == 3 ? n[2] + 2 : 1);
+  double* u = (double*)malloc(sizeof(double) * sz * nv);
+  memcpy(u, r->q, sizeof(double) * sz * nv);
+  for (int level = 1; level <= finest; level++) {
+    int nf[3] = {2 * n[0], 2 * n[1], nd == 3 ? 2 * n[2] : 1};
+    size_t szf = (size_t)(nf[0] + 2) * (nf[1] + 2) * (nd == 3 ? nf[2] + 2 : 1);
+    double* uf = (double*)malloc(sizeof(double) * szf * nv);
+    int cmx[3] = {n[0], n[1], nd == 3 ? n[2] : 0};
+    for (int v = 0; v < nv; v++) prolong_mc(nd, u + v * sz, cmx, uf + v * szf);
+    for (int d = 0; d < nd; d++) dx[d] = dx[d] / 2.0;
+    for (int a = 0; a < nlev(h, level); a++) { /* CopyPatchToUniformGrid */
+      const OPatch* p = &h->p[h->lev_list[level + MAXDEPTH][a]];
+      int k0 = nd == 3 ? p->mglobal[2][0] - 1 : 0;
+      for (int v = 0; v < nv; v++)
+        for (int k = 0; k < p->qn[2]; k++)
+          for (int j = 0; j < p->qn[1]; j++)
+            for (int i = 0; i < p->qn[0]; i++)
+              uf[v * szf + ((size_t)(k0 + k) * (nf[1] + 2) + (p->mglobal[1][0] - 1 + j)) * (nf[0] + 2) +
+                 (p->mglobal[0][0] - 1 + i)] =
+                  p->q[(((size_t)v * p->qn[2] + k) * p->qn[1] + j) * p->qn[0] + i];
+    }
+    free(u);
+    u = uf;
+    sz = szf;
+    memcpy(n, nf, sizeof(n));
+  }
+  FILE* f = fopen(path, "w");
+  if (!f) {
+    free(u);
+    return -8;
+  }
+  put_f25(f, time);
+  fprintf(f, "\n%3d\n", 0);
+  double xu[3];
+  int mg[3][2];
+  for (int d = 0; d < 3; d++) {
+    xu[d] = xupper_of(h, r, d);
+    mg[d][0] = 1;
+    mg[d][1] = n[d];
+  }
+  write_block(f, nd, nv, 0, dx, r->xlower, xu, n, mg, u);
+  free(u);
+  return fclose(f) ? -8 : 0;
+}
+
+/* ---- ReadQ (bsaminputoutput.f90:184-443) ---- */
+
+typedef struct {
+  char* buf;
+  size_t nlines;
+  char** line;
+  size_t* len;
+} Lines;
+
+static int read_lines(const char* path, Lines* L) {
+  memset(L, 0, sizeof(*L));
+  FILE* f = fopen(path, "rb");
+  if (!f) return -8;
+  fseek(f, 0, SEEK_END);
+  long sz = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  L->buf = (char*)malloc((size_t)sz + 1);
+  if (sz > 0 && fread(L->buf, 1, (size_t)sz, f) != (size_t)sz) {
+    fclose(f);
+    return -8;
+  }
+  fclose(f);
+  L->buf[sz] = 0;
+  size_t cap = 0;
+  for (long i = 0; i < sz;) {
+    long e = i;
+    while (e < sz && L->buf[e] != '\n') e++;
+    if (L->nlines == cap) {
+      cap = cap ? 2 * cap : 1024;
+      L->line = (char**)realloc(L->line, sizeof(char*) * cap);
+      L->len = (size_t*)realloc(L->len, sizeof(size_t) * cap);
+    }
+    size_t n = (size_t)(e - i);
+    if (n && L->buf[i + n - 1] == '\r') n--;
+    L->line[L->nlines] = L->buf + i;
+    L->len[L->nlines++] = n;
+    L->buf[e < sz ? e : sz] = 0;
+    i = e + 1;
+  }
+  return 0;
+}
+
+static void free_lines(Lines* L) {
+  free(L->buf);
+  free(L->line);
+  free(L->len);
+}
+
+/* the characters [col, col+w) of a record, blank-padded (PAD='YES') */
+static void field_of(const Lines* L, size_t ln, int col, int w, char* out) {
+  for (int c = 0; c < w; c++) out[c] = (size_t)(col + c) < L->len[ln] ? L->line[ln][col + c] : ' ';
+  out[w] = 0;
+}
+
+/* Iw input: a blank field is 0 */
+static int read_int(const Lines* L, size_t ln, int col, int w, int* v) {
+  char b[32], *e;
+  field_of(L, ln, col, w, b);
+  long x = strtol(b, &e, 10);
+  while (*e == ' ') e++;
+  if (*e) return -8;
+  *v = (int)x;
+  return 0;
+}
+
+/* F25.12 input of a field written by F25.12 output (a decimal point is
+ * required; a blank field is 0) */
+static int read_real(const Lines* L, size_t ln, int col, double* v) {
+  char b[32], *e;
+  field_of(L, ln, col, 25, b);
+  int blank = 1, point = 0;
+  for (int c = 0; c < 25; c++) {
+    if (b[c] != ' ') blank = 0;
+    if (b[c] == '.') point = 1;
+  }
+  if (blank) {
+    *v = 0.0;
+    return 0;
+  }
+  if (!point) return -8;
+  *v = strtod(b, &e);
+  while (*e == ' ') e++;
+  return *e ? -8 : 0;
+}
+
+/* Restart from a frame file.  `root` is a committed hierarchy with the
+ * run's root grid and the levels below it (RootInit); the result copies it,
+ * replaces the root's q (ghost layers included) by the file's and adds the
+ * file's refinement patches with ids first_id, first_id + 1, ...  The checks
+ * of the root block are ReadQ's (:296-336, including its one-sided dx test).
+ * Unlike ReadQ, whose restart patches all hang off the youngest patch of
+ * the level below (:246, "the usual parent-child relationship is broken"),
+ * each patch gets the patch of the level below that contains it as parent,
+ * with mbounds and mthbc as MakeNewGrid would set them; qold = q.  The
+ * restart patches only feed TransferValues of the first regrid, so the
+ * regrid result does not depend on that choice. */
+int bsamo_read_q(const bsamo_hier* root, const char* path, int first_id, double* time, bsamo_hier** out) {
+  if (!root || !root->committed || !path || !out) return -1;
+  Lines L;
+  int rc = read_lines(path, &L);
+  if (rc) {
+    free_lines(&L);
+    return rc;
+  }
+  double params[6] = {root->dt, root->eps, root->gamma, root->lambda, root->czero, root->cpress};
+  bsamo_hier* h = NULL;
+  if ((rc = bsamo_create(root->ndims, root->nrvars, root->mbc, root->problem, params, 6, root->qpo, &h))) {
+    free_lines(&L);
+    return rc;
+  }
+  h->has_root_xupper = root->has_root_xupper;
+  memcpy(h->root_xupper, root->root_xupper, sizeof(h->root_xupper));
+  for (int n = 0; n < root->np; n++) {
+    const OPatch* p = &root->p[n];
+    if (p->level > 0) continue;
+    int mg[6], mb[6];
+    for (int d = 0; d < 3; d++) {
+      mg[2 * d] = p->mglobal[d][0]; mg[2 * d + 1] = p->mglobal[d][1];
+      mb[2 * d] = p->mbounds[d][0]; mb[2 * d + 1] = p->mbounds[d][1];
+    }
+    bsamo_patch_add(h, p->level, p->id, p->parent_id, p->mx, mg, mb, p->mthbc, p->dx, p->xlower);
+  }
+  if ((rc = bsamo_commit(h))) goto fail;
+  for (int n = 0; n < h->np; n++) {
+    OPatch* p = &h->p[n];
+    const OPatch* o = find_patch(root, p->id);
+    size_t nq = (size_t)p->qn[0] * p->qn[1] * p->qn[2] * h->nrvars;
+    size_t nc = (size_t)p->cn[0] * p->cn[1] * p->cn[2] * h->nrvars;
+    size_t nf = (size_t)p->fn[0] * p->fn[1] * p->fn[2] * h->nrvars;
+    memcpy(p->q, o->q, nq * sizeof(double));
+    memcpy(p->qold, o->qold, nq * sizeof(double));
+    memcpy(p->qc, o->qc, nc * sizeof(double));
+    memcpy(p->f, o->f, nf * sizeof(double));
+    memcpy(p->rf, o->rf, nf * sizeof(double));
+    memcpy(p->ftmp, o->ftmp, nf * sizeof(double));
+  }
+  rc = -8;
+  int nd = h->ndims, finest, r0 = h->lev_list[MAXDEPTH][0];
+  double t;
+  if (L.nlines < 2 || read_real(&L, 0, 0, &t) || read_int(&L, 1, 0, 3, &finest)) goto fail;
+  if (finest < 0 || finest > MAXDEPTH) goto fail;
+  size_t ln = 2;
+  int next_id = first_id;
+  for (int lvl = 0; lvl <= finest; lvl++) {
+    for (;;) {
+      if (ln >= L.nlines) goto done; /* READ(54,'(A1)',IOSTAT=ioerror); ioerror < 0 */
+      int level, rnd, ratio, nv;
+      if (ln + 1 >= L.nlines) goto fail;
+      if (read_int(&L, ln + 1, 0, 3, &level) || read_int(&L, ln + 1, 4, 3, &rnd) ||
+          read_int(&L, ln + 1, 8, 3, &ratio) || read_int(&L, ln + 1, 12, 3, &nv))
+        goto fail;
+      if (level != lvl) break; /* BACKSPACE twice, next level */
+      ln += 2;
+      if (rnd != nd || ratio != 2 || nv != h->nrvars || ln + 5 > L.nlines) goto fail;
+      double dx[3] = {0, 0, 0}, xl[3] = {0, 0, 0}, xu[3] = {0, 0, 0};
+      int mx[3] = {1, 1, 1}, mg[3][2] = {{1, 1}, {1, 1}, {1, 1}};
+      for (int d = 0; d < nd; d++)
+        if (read_real(&L, ln, 26 * d, &dx[d]) || read_real(&L, ln + 1, 26 * d, &xl[d]) ||
+            read_real(&L, ln + 2, 26 * d, &xu[d]) || read_int(&L, ln + 3, 9 * d, 8, &mx[d]) ||
+            read_int(&L, ln + 4, 18 * d, 8, &mg[d][0]) || read_int(&L, ln + 4, 18 * d + 9, 8, &mg[d][1]))
+          goto fail;
+      ln += 5;
+      OPatch* tgt;
+      if (level == 0) {
+        tgt = &h->p[r0];
+        for (int d = 0; d < nd; d++) {
+          const double small = 1.0e-08;
+          if (dx[d] - tgt->dx[d] > small) goto fail;
+          if (fabs(xl[d] - tgt->xlower[d]) > small) goto fail;
+          if (fabs(xu[d] - xupper_of(h, tgt, d)) > small) goto fail;
+          if (mx[d] != tgt->mx[d] || mg[d][0] != 1 || mg[d][1] != tgt->mx[d]) goto fail;
+        }
+      } else {
+        int par = -1, mb[3][2] = {{1, 1}, {1, 1}, {1, 1}}, thbc[6];
+        for (int d = 0; d < nd; d++)
+          if (mx[d] < 2 || mg[d][0] % 2 != 1 || mg[d][1] % 2 != 0 || mg[d][1] - mg[d][0] + 1 != mx[d]) goto fail;
+        for (int a = 0; a < nlev(h, level - 1) && par < 0; a++) {
+          int c = h->lev_list[level - 1 + MAXDEPTH][a], in = 1;
+          const OPatch* q = &h->p[c];
+          for (int d = 0; d < nd; d++)
+            if ((mg[d][0] + 1) / 2 < q->mglobal[d][0] || mg[d][1] / 2 > q->mglobal[d][1]) in = 0;
+          if (in) par = c;
+        }
+        if (par < 0) goto fail;
+        const OPatch* q = &h->p[par];
+        for (int d = 0; d < nd; d++) {
+          mb[d][0] = (mg[d][0] + 1) / 2 - q->mglobal[d][0] + 1;
+          mb[d][1] = mg[d][1] / 2 - q->mglobal[d][0] + 1;
+        }
+        for (int f = 0; f < 6; f++) thbc[f] = f < 2 * nd ? INTERNALBC : 10;
+        for (int e = 0; e < nd; e++) {
+          if (q->mthbc[2 * e] < INTERNALBC && mb[e][0] == 1) thbc[2 * e] = q->mthbc[2 * e];
+          if (q->mthbc[2 * e + 1] < INTERNALBC && mb[e][1] == q->mx[e]) thbc[2 * e + 1] = q->mthbc[2 * e + 1];
+        }
+        int c = add_live_patch(h, level, next_id++, par, mx, mg, mb, thbc, dx, xl);
+        tgt = &h->p[c];
+      }
+      size_t plane = (size_t)tgt->qn[0] * tgt->qn[1] * tgt->qn[2];
+      if (ln + plane > L.nlines) goto fail;
+      for (size_t c = 0; c < plane; c++, ln++)
+        for (int v = 0; v < nv; v++)
+          if (read_real(&L, ln, 27 * v, &tgt->q[v * plane + c])) goto fail;
+      if (level > 0) memcpy(tgt->qold, tgt->q, sizeof(double) * plane * nv);
+    }
+  }
+done:
+  free_lines(&L);
+  if (time) *time = t;
+  *out = h;
+  return 0;
+fail:
+  free_lines(&L);
+  bsamo_destroy(h);
+  return rc ? rc : -8;
+}
+
+/* one record of OUT/stats.dat: WRITE(65,'(3(F25.12),1x,I8)') currenttime,
+ * integralresult(1:2), totalmeshsize (bsamroutines.f90:771-775) */
+int bsamo_format_stats_line(double time, const double integral[2], long long meshsize, char* out, size_t n) {
+  char a[26], b[26], c[26], m[16];
+  bsamo_format_f25_12(time, a);
+  bsamo_format_f25_12(integral[0], b);
+  bsamo_format_f25_12(integral[1], c);
+  if (meshsize < -9999999LL || meshsize > 99999999LL)
+    strcpy(m, "********");
+  else
+    snprintf(m, sizeof m, "%8lld", meshsize);
+  int k = snprintf(out, n, "%s%s%s %s\n", a, b, c, m);
+  return k < 0 || (size_t)k >= n ? -1 : 0;
 }

@@ -124,6 +124,23 @@ typedef void (*bsamo_qinit_fn)(void* user, int level, const int* mx,
 int bsamo_regrid(const bsamo_hier* old, const bsamo_regrid_params* prm,
                  bsamo_qinit_fn qinit, void* user, bsamo_hier** out);
 
+/* AfterStepStatistics + GetMeshSize over levels finest..0
+ * (bsamroutines.f90:763-775, :846-868, :918-963; CH/problem.f90:149-215,
+ * :518-547; BioGrowth/problem.f90:107-152): integral[0] = integral of phi,
+ * integral[1] = the CH 2D energy (0 elsewhere), *meshsize = composite cells */
+int bsamo_after_step_stats(const bsamo_hier* h, int finestlevel, double integral[2], long long* meshsize);
+/* WriteQ (bsaminputoutput.f90:60-181): the frame file of levels 0..finest */
+int bsamo_write_q(const bsamo_hier* h, const char* path, double time, int finestlevel);
+/* WriteUniformMeshQ (bsaminputoutput.f90:446-572) */
+int bsamo_write_uniform_q(const bsamo_hier* h, const char* path, double time, int finestlevel);
+/* ReadQ (bsaminputoutput.f90:184-443): restart from a frame file; `root`
+ * holds the root grid and the levels below it */
+int bsamo_read_q(const bsamo_hier* root, const char* path, int first_id, double* time, bsamo_hier** out);
+/* one F25.12 field (25 characters and a terminating zero) */
+void bsamo_format_f25_12(double x, char out[26]);
+/* one record of OUT/stats.dat (bsamroutines.f90:771-775), newline included */
+int bsamo_format_stats_line(double time, const double integral[2], long long meshsize, char* out, size_t n);
+
 /* seeded inputs: U(-1,1) from splitmix64 on a global cell index */
 double bsamo_uniform_pm1(unsigned long long seed, unsigned long long gidx);
 

@@ -88,6 +88,13 @@ def lib():
         L.bsamo_multigrid_iterations.argtypes = [P, I, I, I, I, D, I, I, IP, DP]
         L.bsamo_time_step.argtypes = [P, I, I, I, I, I, D, I, I, IP, DP]
         L.bsamo_regrid.argtypes = [P, ctypes.POINTER(RegridParams), QINIT, P, ctypes.POINTER(P)]
+        L.bsamo_after_step_stats.argtypes = [P, I, DP, ctypes.POINTER(ctypes.c_longlong)]
+        L.bsamo_write_q.argtypes = [P, ctypes.c_char_p, D, I]
+        L.bsamo_write_uniform_q.argtypes = [P, ctypes.c_char_p, D, I]
+        L.bsamo_read_q.argtypes = [P, ctypes.c_char_p, I, DP, ctypes.POINTER(P)]
+        L.bsamo_format_f25_12.argtypes = [D, ctypes.c_char_p]
+        L.bsamo_format_f25_12.restype = None
+        L.bsamo_format_stats_line.argtypes = [D, DP, ctypes.c_longlong, ctypes.c_char_p, ctypes.c_size_t]
         L.bsamo_uniform_pm1.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong]
         L.bsamo_uniform_pm1.restype = D
         _lib = L
@@ -209,6 +216,39 @@ class OracleHierarchy:
                                      maxvcycles, tol, updateauxfreq, errortype, ctypes.byref(n),
                                      res), "time_step")
         return n.value, list(res)[: n.value]
+
+    def after_step_stats(self, finest):
+        """(integral of phi, CH 2D energy, composite mesh size)."""
+        r = (ctypes.c_double * 2)()
+        m = ctypes.c_longlong()
+        _check(lib().bsamo_after_step_stats(self.h, finest, r, ctypes.byref(m)), "after_step_stats")
+        return r[0], r[1], m.value
+
+    def write_q(self, path, time, finest):
+        _check(lib().bsamo_write_q(self.h, os.fsencode(path), time, finest), "write_q")
+
+    def write_uniform_q(self, path, time, finest):
+        _check(lib().bsamo_write_uniform_q(self.h, os.fsencode(path), time, finest), "write_uniform_q")
+
+
+def read_q(root, path, first_id=1000):
+    """Restart from a frame file (bsamo_read_q); returns (hierarchy, time)."""
+    h = ctypes.c_void_p()
+    t = ctypes.c_double()
+    _check(lib().bsamo_read_q(root.h, os.fsencode(path), first_id, ctypes.byref(t), ctypes.byref(h)), "read_q")
+    return _wrap(h, root.ndims, root.nrvars), t.value
+
+
+def format_f25(x):
+    b = ctypes.create_string_buffer(26)
+    lib().bsamo_format_f25_12(float(x), b)
+    return b.value.decode()
+
+
+def format_stats_line(time, integral, meshsize):
+    b = ctypes.create_string_buffer(128)
+    _check(lib().bsamo_format_stats_line(time, _da(integral, 2), meshsize, b, 128), "format_stats_line")
+    return b.value.decode()
 
 
 def _wrap(h, ndims, nrvars):
