@@ -112,6 +112,9 @@ def lib():
         "bsamg_sync": ([P], I),
         "bsamg_stream": ([P, ctypes.POINTER(P)], I),
         "bsamg_launch_count": ([P, ctypes.POINTER(ctypes.c_longlong)], I),
+        "bsamg_set_tail_cells": ([P, ctypes.c_longlong], I),
+        "bsamg_set_params": ([P, DP, I], I),
+        "bsamg_hier_reset": ([P], I),
         "bsamg_mark": ([P, I], I),
         "bsamg_elapsed_ms": ([P, I, I, DP], I),
         "bsamg_time_smoother": ([P, I, I, I, DP], I),
@@ -124,6 +127,7 @@ def lib():
         "bsamg_write_uniform_q": ([P, ctypes.c_char_p, D, I], I),
         "bsamg_read_q": ([P, ctypes.c_char_p, I, DP, ctypes.POINTER(P)], I),
         "bsamg_format_f25_12": ([D, ctypes.c_char_p], I),
+        "bsamg_seed_spinodal": ([P, I, ctypes.c_ulonglong, D, D], I),
         "bsamg_format_stats_line": ([D, DP, ctypes.c_longlong, ctypes.c_char_p, SZ], I),
         "bsamg_strerror": ([I], ctypes.c_char_p),
         "bsamg_last_error_detail": ([], ctypes.c_char_p),
@@ -259,6 +263,11 @@ class Hierarchy:
         new.ctx, new.ndims, new.nrvars, new.h = self.ctx, self.ndims, self.nrvars, h
         return new, t.value
 
+    def seed_spinodal(self, pid, seed, mean=0.0, amp=0.05):
+        """The seeded spinodal start of patch pid, generated on the device
+        (bsamg_seed_spinodal; the same values as initial.ch_spinodal)."""
+        _ck(lib().bsamg_seed_spinodal(self.h, pid, seed, mean, amp), "bsamg_seed_spinodal")
+
     def commit(self):
         _ck(lib().bsamg_commit(self.h), "bsamg_commit")
 
@@ -352,6 +361,19 @@ class Hierarchy:
         n = ctypes.c_int()
         _ck(lib().bsamg_smoother_colours(self.h, level, MODE[mode], ctypes.byref(n)), "bsamg_smoother_colours")
         return n.value
+
+    def set_params(self, params):
+        """New plugin parameters for a committed hierarchy (bsamg_set_params)."""
+        _ck(lib().bsamg_set_params(self.h, _da(params, len(params)), len(params)), "bsamg_set_params")
+
+    def reset(self):
+        """Every field back to zero, as after commit (bsamg_hier_reset)."""
+        _ck(lib().bsamg_hier_reset(self.h), "bsamg_hier_reset")
+
+    def set_tail_cells(self, cells):
+        """Largest cumulative coarse-level size the mixed V-cycle runs inside
+        one thread block (bsamg_set_tail_cells; 0 disables)."""
+        _ck(lib().bsamg_set_tail_cells(self.h, cells), "bsamg_set_tail_cells")
 
     def launch_count(self):
         n = ctypes.c_longlong()

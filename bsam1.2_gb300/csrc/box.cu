@@ -720,6 +720,23 @@ bool box_eligible(const Hier& H, bool periodic_single) {
 // float pool of the box path: per level e, g, pb (not on the finest level,
 // where pb is qhi(phi)), ec (below the finest); on the finest level qhi,
 // qlo, fhi, flo
+void box_coefficients(Hier& H) {
+  for (int l = H.maxlevel; l >= H.minlevel; l--) {
+    const HostPatch& P = H.patches[H.L(l).patches[0]];
+    BoxLev& L = H.blev[l + kMaxDepth];
+    double c[4];
+    coefficients(H, P.dx[0], c);
+    L.c0 = (float)c[0];
+    L.c1 = (float)c[1];
+    L.tmp3 = (float)c[2];
+    L.a12 = (float)c[3];
+    L.c0h = (float)c[0];
+    L.c0l = (float)(c[0] - (double)L.c0h);
+    L.c1h = (float)c[1];
+    L.c1l = (float)(c[1] - (double)L.c1h);
+  }
+}
+
 size_t box_layout(Hier& H) {
   long long o = 0;
   auto al = [](long long x) { return (x + 63) & ~63LL; };
@@ -741,17 +758,8 @@ size_t box_layout(Hier& H) {
       L.opb = o; o = al(o + 2 * L.half);
       L.oec = o; o = al(o + 4 * L.half);
     }
-    double c[4];
-    coefficients(H, P.dx[0], c);
-    L.c0 = (float)c[0];
-    L.c1 = (float)c[1];
-    L.tmp3 = (float)c[2];
-    L.a12 = (float)c[3];
-    L.c0h = (float)c[0];
-    L.c0l = (float)(c[0] - (double)L.c0h);
-    L.c1h = (float)c[1];
-    L.c1l = (float)(c[1] - (double)L.c1h);
   }
+  box_coefficients(H);
   const BoxLev& F = H.blev[H.maxlevel + kMaxDepth];
   H.b_partials = (size_t)ctas(shape(F.n[0], F.n[1], F.n[2]));
   return (size_t)o;

@@ -11,6 +11,8 @@ namespace bsamg {
 bool box_eligible(const Hier& H, bool periodic_single);
 // fills H.blev / H.b_* offsets; returns the float-pool size in elements
 size_t box_layout(Hier& H);
+// the plugin coefficients of every box level (from the current parameters)
+void box_coefficients(Hier& H);
 // same contract as the FP64 loop; runs instead of the common prologue
 // (it forms f from qold itself); finest must be the hierarchy's finest level
 int box_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,

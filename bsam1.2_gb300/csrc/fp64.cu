@@ -161,12 +161,11 @@ __device__ __forceinline__ bool ghosted_cell(const int* n, int t, int& i, int& j
 // Red-black pointwise relaxation of one colour over all patches of a level.
 
 template <int PROB, int DIM>
-__global__ void __launch_bounds__(kBlock) k_relax(const PatchDev* __restrict__ P, double* __restrict__ pool,
-                                                  const Blk* __restrict__ blk, int ipass, ProbParams pp) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_relax(const PatchDev* __restrict__ P, double* __restrict__ pool, const Blk b,
+                                        int tid, int ipass, const ProbParams& pp) {
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  if (!color_cell<DIM>(p, b.start + threadIdx.x, ipass, i, j, k)) return;
+  if (!color_cell<DIM>(p, b.start + tid, ipass, i, j, k)) return;
   double* q0 = pool + p.oq;
   double* q1 = q0 + p.sq;
   const double* f0 = pool + p.of;
@@ -233,6 +232,11 @@ __global__ void __launch_bounds__(kBlock) k_relax(const PatchDev* __restrict__ P
     q2[c] = (f2[fc] + p.c[1] * s2 + pp.cpress * np * nn) / p.c[3];
   }
 }
+template <int PROB, int DIM>
+__global__ void __launch_bounds__(kBlock) k_relax(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                  const Blk* __restrict__ blk, int ipass, ProbParams pp) {
+  u_relax<PROB, DIM>(P, pool, blk[blockIdx.x], threadIdx.x, ipass, pp);
+}
 
 // ---------------------------------------------------------------------------
 // Restriction2D/3D (gridutilities.f90:103-126, :437-466) of plane `a`
@@ -250,12 +254,11 @@ __device__ __forceinline__ double restrict_at(F at, int ci, int cj, int ck) {
 // RestrictSolution, afasroutines.f90:610-652: qc(1:cmx) = R(q);
 // parent q(mb) = qc.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_restrict_q(const PatchDev* __restrict__ P, double* __restrict__ pool,
-                                                       const Blk* __restrict__ blk, int nrvars) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_restrict_q(const PatchDev* __restrict__ P, double* __restrict__ pool, const Blk b,
+                                             int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
   int ci, cj, ck;
-  if (!interior_cell<DIM>(p.cmx, b.start + threadIdx.x, ci, cj, ck)) return;
+  if (!interior_cell<DIM>(p.cmx, b.start + tid, ci, cj, ck)) return;
   const PatchDev& par = P[p.parent];
   for (int v = 0; v < nrvars; v++) {
     const double* q = pool + p.oq + v * p.sq;
@@ -265,17 +268,21 @@ __global__ void __launch_bounds__(kBlock) k_restrict_q(const PatchDev* __restric
     pool[par.oq + v * par.sq + gofs<DIM>(par.qn, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 0)] = val;
   }
 }
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_restrict_q(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                       const Blk* __restrict__ blk, int nrvars) {
+  u_restrict_q<DIM>(P, pool, blk[blockIdx.x], threadIdx.x, nrvars);
+}
 
 // GetCoarseGhostPoints, boundary.f90:957-1015.  Every ring cell of qc is
 // covered by exactly one of its face statements, each of which copies
 // parent%q(mb-1+i, mb-1+j, mb-1+k).
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_coarse_ghost(const PatchDev* __restrict__ P, double* __restrict__ pool,
-                                                         const Blk* __restrict__ blk, int nrvars) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_coarse_ghost(const PatchDev* __restrict__ P, double* __restrict__ pool, const Blk b,
+                                               int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  if (!ghosted_cell<DIM>(p.cn, b.start + threadIdx.x, i, j, k)) return;
+  if (!ghosted_cell<DIM>(p.cn, b.start + tid, i, j, k)) return;
   bool ring = i == 0 || i == p.cmx[0] + 1 || j == 0 || j == p.cmx[1] + 1 ||
               (DIM == 3 && (k == 0 || k == p.cmx[2] + 1));
   if (!ring) return;
@@ -284,17 +291,21 @@ __global__ void __launch_bounds__(kBlock) k_coarse_ghost(const PatchDev* __restr
   long long dst = gofs<DIM>(p.cn, i, j, k);
   for (int v = 0; v < nrvars; v++) pool[p.oqc + v * p.sc + dst] = pool[par.oq + v * par.sq + src];
 }
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_coarse_ghost(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                         const Blk* __restrict__ blk, int nrvars) {
+  u_coarse_ghost<DIM>(P, pool, blk[blockIdx.x], threadIdx.x, nrvars);
+}
 
 // CoarseLoadingFunction, afasroutines.f90:673-736, with Residual (:817-857):
 // rf = f - Op_h(q) on the children of a coarse cell;
 // parent f(mb) = R(rf) + Op_2h(qc, parent qold, h_parent).
 template <int PROB, int DIM>
-__global__ void __launch_bounds__(kBlock) k_coarse_load(const PatchDev* __restrict__ P, double* __restrict__ pool,
-                                                        const Blk* __restrict__ blk, ProbParams pp) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_coarse_load(const PatchDev* __restrict__ P, double* __restrict__ pool, const Blk b,
+                                              int tid, const ProbParams& pp) {
   const PatchDev& p = P[b.patch];
   int ci, cj, ck;
-  if (!interior_cell<DIM>(p.cmx, b.start + threadIdx.x, ci, cj, ck)) return;
+  if (!interior_cell<DIM>(p.cmx, b.start + tid, ci, cj, ck)) return;
   const PatchDev& par = P[p.parent];
   const double* q = pool + p.oq;
   const double* qo = pool + p.oqold;
@@ -332,16 +343,20 @@ __global__ void __launch_bounds__(kBlock) k_coarse_load(const PatchDev* __restri
   long long pf = iofs<DIM>(par.mx, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 1);
   for (int v = 0; v < NV; v++) pool[par.of + v * par.sf + pf] = R[v] + cr[v];
 }
+template <int PROB, int DIM>
+__global__ void __launch_bounds__(kBlock) k_coarse_load(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                        const Blk* __restrict__ blk, ProbParams pp) {
+  u_coarse_load<PROB, DIM>(P, pool, blk[blockIdx.x], threadIdx.x, pp);
+}
 
 // CorrectFine step 1, afasroutines.f90:892-895 / :934-938:
 // qc(0:cmx+1) = parent%q(mb-1:mb+1) - qc
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_correct_a(const PatchDev* __restrict__ P, double* __restrict__ pool,
-                                                      const Blk* __restrict__ blk, int nrvars) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_correct_a(const PatchDev* __restrict__ P, double* __restrict__ pool, const Blk b,
+                                            int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  if (!ghosted_cell<DIM>(p.cn, b.start + threadIdx.x, i, j, k)) return;
+  if (!ghosted_cell<DIM>(p.cn, b.start + tid, i, j, k)) return;
   const PatchDev& par = P[p.parent];
   long long src = gofs<DIM>(par.qn, p.mb[0] - 1 + i, p.mb[1] - 1 + j, DIM == 3 ? p.mb[2] - 1 + k : 0);
   long long dst = gofs<DIM>(p.cn, i, j, k);
@@ -349,6 +364,11 @@ __global__ void __launch_bounds__(kBlock) k_correct_a(const PatchDev* __restrict
     double* qc = pool + p.oqc + v * p.sc;
     qc[dst] = pool[par.oq + v * par.sq + src] - qc[dst];
   }
+}
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_correct_a(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                      const Blk* __restrict__ blk, int nrvars) {
+  u_correct_a<DIM>(P, pool, blk[blockIdx.x], threadIdx.x, nrvars);
 }
 
 // CorrectFine step 2: q(0:mx+1) += BiLinProlongationP1(qc)
@@ -358,12 +378,11 @@ __global__ void __launch_bounds__(kBlock) k_correct_a(const PatchDev* __restrict
 // b (and c) entries for its 2x2(x2) coarse values with the reference's
 // expressions, so every fine value is bit-identical to the array form.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_correct_b(const PatchDev* __restrict__ P, double* __restrict__ pool,
-                                                      const Blk* __restrict__ blk, int nrvars) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_correct_b(const PatchDev* __restrict__ P, double* __restrict__ pool, const Blk b,
+                                            int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
   int cpn[3] = {p.cmx[0] + 1, p.cmx[1] + 1, DIM == 3 ? p.cmx[2] + 1 : 1};
-  int t = b.start + threadIdx.x;
+  int t = b.start + tid;
   int ci = t % cpn[0], r = t / cpn[0];
   int cj = r % cpn[1], ck = r / cpn[1];
   if (ck >= cpn[2]) return;
@@ -396,15 +415,19 @@ __global__ void __launch_bounds__(kBlock) k_correct_b(const PatchDev* __restrict
         }
   }
 }
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_correct_b(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                      const Blk* __restrict__ blk, int nrvars) {
+  u_correct_b<DIM>(P, pool, blk[blockIdx.x], threadIdx.x, nrvars);
+}
 
 // FillDownLevel, afasroutines.f90:257-327: parent f or q (mb) = R(child).
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_fill_down(const PatchDev* __restrict__ P, double* __restrict__ pool,
-                                                      const Blk* __restrict__ blk, int nrvars, int field) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_fill_down(const PatchDev* __restrict__ P, double* __restrict__ pool, const Blk b,
+                                            int tid, int nrvars, int field) {
   const PatchDev& p = P[b.patch];
   int ci, cj, ck;
-  if (!interior_cell<DIM>(p.cmx, b.start + threadIdx.x, ci, cj, ck)) return;
+  if (!interior_cell<DIM>(p.cmx, b.start + tid, ci, cj, ck)) return;
   const PatchDev& par = P[p.parent];
   for (int v = 0; v < nrvars; v++) {
     if (field == 1) {
@@ -419,6 +442,11 @@ __global__ void __launch_bounds__(kBlock) k_fill_down(const PatchDev* __restrict
           restrict_at<DIM>(at, ci, cj, ck);
     }
   }
+}
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_fill_down(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                      const Blk* __restrict__ blk, int nrvars, int field) {
+  u_fill_down<DIM>(P, pool, blk[blockIdx.x], threadIdx.x, nrvars, field);
 }
 
 // GetSourceFunction, afasroutines.f90:330-381: ftmp = Source(q, qold)
@@ -627,6 +655,44 @@ __global__ void __launch_bounds__(kBlock) k_ghost_program(const PatchDev* __rest
   }
 }
 
+// The coarse tail of the V-cycle in one block (see TailPhase): the
+// operations the separate launches would run, phase by phase, each phase's
+// work-list blocks executed in turn by the block's 256 threads with a
+// barrier between phases.  Per-cell arithmetic and the order of dependent
+// updates are those of the separate kernels, so results are bit-identical.
+template <int PROB, int DIM>
+__global__ void __launch_bounds__(kBlock) k_tail(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                 const TailPhase* __restrict__ ph, int nph, ProbParams pp) {
+  for (int x = 0; x < nph; x++) {
+    const TailPhase f = ph[x];
+    if (f.op == kTGhost) {
+      for (int s = 0; s < f.nstages; s++) {
+        for (int t = f.stage_off[s] + threadIdx.x; t < f.stage_off[s + 1]; t += blockDim.x) {
+          GhostOp g = f.ops[t];
+          ghost_apply(P, pool, g, pp);
+        }
+        __syncthreads();
+      }
+      continue;
+    }
+    for (int b = 0; b < f.nblk; b++) {
+      const Blk bb = f.blk[b];
+      switch (f.op) {
+        case kTRelax: u_relax<PROB, DIM>(P, pool, bb, threadIdx.x, f.arg, pp); break;
+        case kTRestrict: u_restrict_q<DIM>(P, pool, bb, threadIdx.x, pp.nrvars); break;
+        case kTRing:
+          if (f.arg) u_correct_a<DIM>(P, pool, bb, threadIdx.x, pp.nrvars);
+          else u_coarse_ghost<DIM>(P, pool, bb, threadIdx.x, pp.nrvars);
+          break;
+        case kTLoad: u_coarse_load<PROB, DIM>(P, pool, bb, threadIdx.x, pp); break;
+        case kTFill: u_fill_down<DIM>(P, pool, bb, threadIdx.x, pp.nrvars, f.arg); break;
+        default: u_correct_b<DIM>(P, pool, bb, threadIdx.x, pp.nrvars); break;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 
@@ -727,6 +793,12 @@ int launch_ghost_stage(const LaunchCtx& c, const GhostOp* ops, int n) {
 int launch_ghost_program_1cta(const LaunchCtx& c, const GhostOp* ops, const int* stage_off, int nstages) {
   if (nstages <= 0) return 0;
   k_ghost_program<<<1, kBlock, 0, c.s>>>(c.P, c.pool, ops, stage_off, nstages, c.pp);
+  return 1;
+}
+int launch_tail(const LaunchCtx& c, const TailPhase* ph, int nph) {
+  if (nph <= 0) return 0;
+  const int nblk = 1;
+  DISPATCH_PD(c, k_tail, c.P, c.pool, ph, nph, c.pp);
   return 1;
 }
 

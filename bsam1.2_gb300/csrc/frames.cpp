@@ -308,8 +308,8 @@ int after_step_stats(Hier& H, int finest, double* integral, long long* meshsize)
   integral[0] = integral[1] = 0.0;
   if (total == 0) return BSAMG_OK;
   double* partial = nullptr;
-  cudaError_t e = cudaMallocAsync((void**)&partial, sizeof(double) * 2 * (size_t)total, H.s);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(stats)");
+  cudaError_t e = dev_alloc(H, (void**)&partial, sizeof(double) * 2 * (size_t)total);
+  if (e != cudaSuccess) return cuda_fail(e, "device allocation (stats)");
   LaunchCtx c = H.lc();
   int pofs = 0, n = 0;
   for (int l = finest; l >= 0; l--) {
@@ -374,8 +374,8 @@ int write_uniform_q(Hier& H, const char* path, double time, int finest) {
     H.ctx->used -= std::min(H.ctx->used, need);
   };
   double* buf[2] = {nullptr, nullptr};
-  cudaError_t e = cudaMallocAsync((void**)&buf[0], fine_elems * sizeof(double), H.s);
-  if (e == cudaSuccess) e = cudaMallocAsync((void**)&buf[1], fine_elems * sizeof(double), H.s);
+  cudaError_t e = dev_alloc(H, (void**)&buf[0], fine_elems * sizeof(double));
+  if (e == cudaSuccess) e = dev_alloc(H, (void**)&buf[1], fine_elems * sizeof(double));
   // uniform level 0 = the root's q, ghost layers included
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(buf[0], H.pool + R.oq, ghosted(n) * nv * sizeof(double), cudaMemcpyDeviceToDevice, H.s);
@@ -649,6 +649,17 @@ int bsamg_write_uniform_q(bsamg_hier* h, const char* path, double time, int fine
 int bsamg_read_q(bsamg_hier* root, const char* path, int first_id, double* time, bsamg_hier** out) {
   if (!root) return BSAMG_ERR_ARG;
   return read_q(*root, path, first_id, time, out);
+}
+
+int bsamg_seed_spinodal(bsamg_hier* h, int id, unsigned long long seed, double mean, double amp) {
+  if (!h || !h->committed || h->problem != kCH || h->nrvars != 2) return BSAMG_ERR_ARG;
+  auto it = h->id2idx.find(id);
+  if (it == h->id2idx.end()) return BSAMG_ERR_NOT_FOUND;
+  const HostPatch& P = h->patches[it->second];
+  int r = set_device(*h);
+  if (r) return r;
+  int n = launch_seed_spinodal(h->s, h->ndims, h->pool + P.oq, P.sq, P.mx, seed, mean, amp, h->pp.eps2, P.dx[0]);
+  return after_launch(*h, n);
 }
 
 int bsamg_format_f25_12(double x, char* out) {

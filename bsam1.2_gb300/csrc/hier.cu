@@ -63,16 +63,41 @@ long long align32(long long x) { return (x + 31) & ~31LL; }
 // ---------------------------------------------------------------------------
 // schedule pieces (plain FP64)
 
-int enq_relax(Hier& H, int level, int ipass) {
+// the tail program being recorded: the V-cycle schedule records its
+// operations instead of launching them
+std::vector<TailPhase>* recording(Hier& H) { return static_cast<std::vector<TailPhase>*>(H.rec); }
+
+// one work-list operation of the FP64 V-cycle, launched or recorded
+int enq_op(Hier& H, int level, int kind, int op, int arg) {
   LevelT& L = H.L(level);
-  return after_launch(H, launch_relax(H.lc(), L.d_blk[kKindColor], L.nblk[kKindColor], ipass));
+  if (auto* rec = recording(H)) {
+    if (L.nblk[kind] > 0) rec->push_back(TailPhase{op, arg, L.nblk[kind], 0, L.d_blk[kind], nullptr, nullptr});
+    return BSAMG_OK;
+  }
+  LaunchCtx c = H.lc();
+  const Blk* b = L.d_blk[kind];
+  int n = L.nblk[kind];
+  switch (op) {
+    case kTRelax: return after_launch(H, launch_relax(c, b, n, arg));
+    case kTRestrict: return after_launch(H, launch_restrict_q(c, b, n));
+    case kTRing: return after_launch(H, arg ? launch_correct_a(c, b, n) : launch_coarse_ghost(c, b, n));
+    case kTLoad: return after_launch(H, launch_coarse_load(c, b, n));
+    case kTFill: return after_launch(H, launch_fill_down(c, b, n, arg));
+    default: return after_launch(H, launch_correct_b(c, b, n));
+  }
 }
+
+int enq_relax(Hier& H, int level, int ipass) { return enq_op(H, level, kKindColor, kTRelax, ipass); }
 
 int enq_set_ghost(Hier& H, int level, int ipass) {
   LevelT& L = H.L(level);
   GhostProg& g = L.gp[ipass];
   int nst = (int)g.stage_off.size() - 1;
   if (nst <= 0) return BSAMG_OK;
+  if (auto* rec = recording(H)) {
+    rec->push_back(TailPhase{kTGhost, 0, 0, nst, nullptr, g.d_ops, g.d_stage_off});
+    return BSAMG_OK;
+  }
   int nops = g.stage_off[nst];
   LaunchCtx c = H.lc();
   if (nops <= 2048) return after_launch(H, launch_ghost_program_1cta(c, g.d_ops, g.d_stage_off, nst));
@@ -92,31 +117,69 @@ int enq_level_relax(Hier& H, int level, int nsmooth) {
 
 // AFASVcycle, afasroutines.f90:495-529
 int enq_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
+  if (!H.rec && level <= H.tail_level && level >= minlevel) {
+    auto it = H.fp_tail_progs.find(std::make_tuple(level, minlevel, nsmooth));
+    if (it != H.fp_tail_progs.end())  // the rest of the V-cycle in one block
+      return after_launch(H, launch_tail(H.lc(), static_cast<const TailPhase*>(it->second.first), it->second.second));
+  }
   RET(enq_level_relax(H, level, nsmooth));
   if (level > minlevel) {
-    LevelT& L = H.L(level);
-    LaunchCtx c = H.lc();
-    RET(after_launch(H, launch_restrict_q(c, L.d_blk[kKindCoarse], L.nblk[kKindCoarse])));
+    RET(enq_op(H, level, kKindCoarse, kTRestrict, 0));
     RET(enq_set_ghost(H, level - 1, 0));
-    RET(after_launch(H, launch_coarse_ghost(c, L.d_blk[kKindCGhost], L.nblk[kKindCGhost])));
-    RET(after_launch(H, launch_coarse_load(c, L.d_blk[kKindCoarse], L.nblk[kKindCoarse])));
+    RET(enq_op(H, level, kKindCGhost, kTRing, 0));
+    RET(enq_op(H, level, kKindCoarse, kTLoad, 0));
     RET(enq_vcycle(H, level - 1, minlevel, nsmooth));
-    RET(after_launch(H, launch_correct_a(c, L.d_blk[kKindCGhost], L.nblk[kKindCGhost])));
-    RET(after_launch(H, launch_correct_b(c, L.d_blk[kKindProl], L.nblk[kKindProl])));
+    RET(enq_op(H, level, kKindCGhost, kTRing, 1));
+    RET(enq_op(H, level, kKindProl, kTProlong, 0));
     RET(enq_set_ghost(H, level, 0));
     RET(enq_level_relax(H, level, nsmooth));
   }
   return BSAMG_OK;
 }
 
+int enq_fill_down_from(Hier& H, int field, int finest, int minlevel);
+
+// Record and upload the FP64 tail programs used by a run with these
+// levels once, outside any stream capture: the V-cycle (key nsmooth) and
+// FillDown of q and f (keys -2, -1) from the first level at or below the
+// tail level.
+int fp_prepare_tail(Hier& H, int finest, int minlevel, int nsmooth) {
+  int start = std::min(finest, H.tail_level);
+  if (start < minlevel) return BSAMG_OK;
+  for (int which : {nsmooth, -2, -1}) {
+    auto key = std::make_tuple(start, minlevel, which);
+    if (H.fp_tail_progs.count(key)) continue;
+    std::vector<TailPhase> prog;
+    H.rec = &prog;
+    int r = which > 0 ? enq_vcycle(H, start, minlevel, nsmooth) : enq_fill_down_from(H, -which, start, minlevel);
+    H.rec = nullptr;
+    if (r) return r;
+    void* d = nullptr;
+    if (!prog.empty()) {
+      CK(dev_alloc(H, &d, sizeof(TailPhase) * prog.size()));
+      CK(cudaMemcpyAsync(d, prog.data(), sizeof(TailPhase) * prog.size(), cudaMemcpyHostToDevice, H.s));  // staged
+    }
+    H.fp_tail_progs[key] = std::make_pair(d, (int)prog.size());
+  }
+  return BSAMG_OK;
+}
+
 // FillDown, afasroutines.f90:236-254 (field 1 = source, 2 = solution)
-int enq_fill_down(Hier& H, int field, int finest, int minlevel) {
+int enq_fill_down_from(Hier& H, int field, int finest, int minlevel) {
   for (int level = finest; level >= minlevel + 1; level--) {
-    LevelT& L = H.L(level);
-    RET(after_launch(H, launch_fill_down(H.lc(), L.d_blk[kKindCoarse], L.nblk[kKindCoarse], field)));
+    if (!H.rec && level <= H.tail_level) {
+      auto it = H.fp_tail_progs.find(std::make_tuple(level, minlevel, -field));
+      if (it != H.fp_tail_progs.end())  // the remaining levels in one block
+        return after_launch(H, launch_tail(H.lc(), static_cast<const TailPhase*>(it->second.first),
+                                           it->second.second));
+    }
+    RET(enq_op(H, level, kKindCoarse, kTFill, field));
     if (field == 2) RET(enq_set_ghost(H, level - 1, 0));
   }
   return BSAMG_OK;
+}
+int enq_fill_down(Hier& H, int field, int finest, int minlevel) {
+  return enq_fill_down_from(H, field, finest, minlevel);
 }
 
 int enq_get_source(Hier& H, int finest) {
@@ -322,6 +385,7 @@ int multigrid_iterations(Hier& H, int finest, int minlevel, int nsmooth, int max
   // the periodic-box mixed path forms f from qold itself
   if (mode == BSAMG_MODE_MIXED && H.box)
     return box_iterations(H, finest, minlevel, nsmooth, maxvcycles, tol, errortype, strict, ncycles, residuals);
+  RET(fp_prepare_tail(H, finest, minlevel, nsmooth));
   RET(enq_fill_down(H, 2, finest, minlevel));
   RET(enq_get_source(H, finest));
   RET(enq_update_source(H, finest));
@@ -440,10 +504,11 @@ int upload_blocks(Hier& H, LevelT& L, int kind) {
   }
   L.nblk[kind] = (int)v.size();
   if (v.empty()) return BSAMG_OK;
-  CK(cudaMallocAsync((void**)&L.d_blk[kind], sizeof(Blk) * v.size(), H.s));
+  CK(dev_alloc(H, (void**)&L.d_blk[kind], sizeof(Blk) * v.size()));
   H.bytes += sizeof(Blk) * v.size();
+  // a copy from pageable memory returns once the source has been staged, so
+  // v may be freed on return
   CK(cudaMemcpyAsync(L.d_blk[kind], v.data(), sizeof(Blk) * v.size(), cudaMemcpyHostToDevice, H.s));
-  CK(cudaStreamSynchronize(H.s));  // v is freed on return
   return BSAMG_OK;
 }
 
@@ -471,8 +536,8 @@ bool ghost_ops_in_bounds(const Hier& H, const GhostProg& g) {
 int upload_ghost(Hier& H, GhostProg& g) {
   if (g.ops.empty()) return BSAMG_OK;
   if (!ghost_ops_in_bounds(H, g)) return BSAMG_ERR_ARG;
-  CK(cudaMallocAsync((void**)&g.d_ops, sizeof(GhostOp) * g.ops.size(), H.s));
-  CK(cudaMallocAsync((void**)&g.d_stage_off, sizeof(int) * g.stage_off.size(), H.s));
+  CK(dev_alloc(H, (void**)&g.d_ops, sizeof(GhostOp) * g.ops.size()));
+  CK(dev_alloc(H, (void**)&g.d_stage_off, sizeof(int) * g.stage_off.size()));
   H.bytes += sizeof(GhostOp) * g.ops.size() + sizeof(int) * g.stage_off.size();
   CK(cudaMemcpyAsync(g.d_ops, g.ops.data(), sizeof(GhostOp) * g.ops.size(), cudaMemcpyHostToDevice, H.s));
   CK(cudaMemcpyAsync(g.d_stage_off, g.stage_off.data(), sizeof(int) * g.stage_off.size(), cudaMemcpyHostToDevice,
@@ -551,7 +616,7 @@ int commit(Hier& H) {
   CK(cudaStreamCreateWithFlags(&H.s, cudaStreamNonBlocking));
   // stream-ordered allocations: creating or destroying a hierarchy never
   // synchronises the device, so other hierarchies' work keeps running
-  CK(cudaMallocAsync((void**)&H.pool, H.pool_elems * sizeof(double), H.s));
+  CK(dev_alloc(H, (void**)&H.pool, H.pool_elems * sizeof(double)));
   CK(cudaMemsetAsync(H.pool, 0, H.pool_elems * sizeof(double), H.s));
   RET(mixed_alloc(H));
 
@@ -576,10 +641,10 @@ int commit(Hier& H) {
     coefficients(H, P.dx[0], D.c);
     for (int x = 0; x < 4; x++) D.cf[x] = (float)D.c[x];
   }
-  CK(cudaMallocAsync((void**)&H.dP, sizeof(PatchDev) * pd.size(), H.s));
-  CK(cudaMemcpyAsync(H.dP, pd.data(), sizeof(PatchDev) * pd.size(), cudaMemcpyHostToDevice, H.s));
-  CK(cudaStreamSynchronize(H.s));  // pd is freed on return
+  CK(dev_alloc(H, (void**)&H.dP, sizeof(PatchDev) * pd.size()));
+  CK(cudaMemcpyAsync(H.dP, pd.data(), sizeof(PatchDev) * pd.size(), cudaMemcpyHostToDevice, H.s));  // staged
   H.bytes += sizeof(PatchDev) * pd.size();
+  H.hP = std::move(pd);
 
   int maxblk = 1;
   for (int l = H.minlevel; l <= H.maxlevel; l++) {
@@ -605,11 +670,12 @@ int commit(Hier& H) {
     }
   }
   RET(mixed_tables(H));
+  set_tail(H, H.tail_cells);
   maxblk = std::max(maxblk, (int)H.b_partials);
   H.partial_cap = maxblk;
-  CK(cudaMallocAsync((void**)&H.d_partial, sizeof(double) * 2 * (size_t)maxblk * std::max(1, H.nrvars), H.s));
-  CK(cudaMallocAsync((void**)&H.d_norm, sizeof(double) * kNormOutLen, H.s));
-  CK(cudaMallocAsync((void**)&H.d_nonfinite, sizeof(int) * 4, H.s));
+  CK(dev_alloc(H, (void**)&H.d_partial, sizeof(double) * 2 * (size_t)maxblk * std::max(1, H.nrvars)));
+  CK(dev_alloc(H, (void**)&H.d_norm, sizeof(double) * kNormOutLen));
+  CK(dev_alloc(H, (void**)&H.d_nonfinite, sizeof(int) * 4));
   RET(pinned_slot_take(H));
   CK(cudaStreamSynchronize(H.s));
   H.committed = true;
@@ -637,6 +703,9 @@ void release(Hier& H) {
     }
   }
   mixed_free(H);
+  for (auto& kv : H.fp_tail_progs)
+    if (kv.second.first) cudaFreeAsync(kv.second.first, H.s);
+  H.fp_tail_progs.clear();
   if (H.dP) cudaFreeAsync(H.dP, H.s);
   if (H.pool) cudaFreeAsync(H.pool, H.s);
   if (H.d_partial) cudaFreeAsync(H.d_partial, H.s);
@@ -693,15 +762,28 @@ int bsamg_init(int device, size_t hbm_budget_bytes, bsamg_ctx** out) {
   if (!c) return BSAMG_ERR_ARG;
   c->device = device;
   c->budget = hbm_budget_bytes;
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  e = cudaMemPoolCreate(&c->mempool, &props);
+  if (e == cudaSuccess) {
+    unsigned long long keep = ~0ull;
+    e = cudaMemPoolSetAttribute(c->mempool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  if (e != cudaSuccess) {
+    if (c->mempool) cudaMemPoolDestroy(c->mempool);
+    delete c;
+    return cuda_fail(e, "cudaMemPoolCreate");
+  }
   *out = c;
   return BSAMG_OK;
 }
 
 int bsamg_finalize(bsamg_ctx* ctx) {
-  if (ctx && ctx->pinned) {
-    cudaSetDevice(ctx->device);
-    cudaFreeHost(ctx->pinned);
-  }
+  if (ctx) cudaSetDevice(ctx->device);
+  if (ctx && ctx->pinned) cudaFreeHost(ctx->pinned);
+  if (ctx && ctx->mempool) cudaMemPoolDestroy(ctx->mempool);
   delete ctx;
   return BSAMG_OK;
 }
@@ -924,6 +1006,69 @@ int bsamg_stream(bsamg_hier* h, void** stream) {
 int bsamg_launch_count(const bsamg_hier* h, long long* n) {
   if (!h || !n) return BSAMG_ERR_ARG;
   *n = h->launches;
+  return BSAMG_OK;
+}
+
+int bsamg_set_params(bsamg_hier* h, const double* params, int nparams) {
+  if (!h || !h->committed || !params) return BSAMG_ERR_ARG;
+  if (nparams < 2 || (h->problem == kBio && nparams < 5) || (h->problem == kGrowth && nparams < 6))
+    return BSAMG_ERR_ARG;
+  if ((int)h->params.size() == nparams && std::equal(params, params + nparams, h->params.begin())) return BSAMG_OK;
+  int r = set_device(*h);
+  if (r) return r;
+  h->params.assign(params, params + nparams);
+  h->pp.dt = params[0];
+  h->pp.eps2 = params[1] * params[1];  // SetProb, CH/problem.f90:32
+  h->pp.gamma = nparams > 2 ? params[2] : 0.0;
+  h->pp.lambda = nparams > 3 ? params[3] : 0.0;
+  h->pp.czero = nparams > 4 ? params[4] : 0.0;
+  h->pp.cpress = nparams > 5 ? params[5] : 0.0;
+  for (size_t n = 0; n < h->patches.size(); n++) {
+    PatchDev& D = h->hP[n];
+    coefficients(*h, h->patches[n].dx[0], D.c);
+    for (int x = 0; x < 4; x++) D.cf[x] = (float)D.c[x];
+  }
+  // stream-ordered after the work already enqueued; staged from pageable
+  // memory before the call returns
+  cudaError_t e = cudaMemcpyAsync(h->dP, h->hP.data(), sizeof(PatchDev) * h->hP.size(), cudaMemcpyHostToDevice,
+                                  h->s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(patch table)");
+  // Kernels read the coefficients from the patch table, except those of the
+  // periodic-box path and the BioGrowth/growth parameters, which are kernel
+  // arguments captured in graphs: those graphs are captured again.
+  if (h->box) box_coefficients(*h);
+  bool keep_graphs = h->problem == kCH && !h->box;
+  if (!keep_graphs) {
+    e = cudaStreamSynchronize(h->s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    for (auto& kv : h->graphs)
+      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    h->graphs.clear();
+  }
+  return BSAMG_OK;
+}
+
+int bsamg_hier_reset(bsamg_hier* h) {
+  if (!h || !h->committed) return BSAMG_ERR_ARG;
+  int r = set_device(*h);
+  if (r) return r;
+  // every field back to the zero fill of bsamg_commit
+  cudaError_t e = cudaMemsetAsync(h->pool, 0, h->pool_elems * sizeof(double), h->s);
+  if (e == cudaSuccess && h->fpool) e = cudaMemsetAsync(h->fpool, 0, h->fpool_elems * sizeof(float), h->s);
+  return e == cudaSuccess ? BSAMG_OK : cuda_fail(e, "cudaMemsetAsync(reset)");
+}
+
+int bsamg_set_tail_cells(bsamg_hier* h, long long cells) {
+  if (!h || !h->committed || cells < 0) return BSAMG_ERR_ARG;
+  int r = set_device(*h);
+  if (r) return r;
+  cudaError_t e = cudaStreamSynchronize(h->s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  // captured graphs embed the previous tail program
+  for (auto& kv : h->graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  h->graphs.clear();
+  set_tail(*h, cells);
   return BSAMG_OK;
 }
 

@@ -64,6 +64,7 @@ struct Hier {
   int mxmax[kMaxDepth + 1][3] = {};
 
   PatchDev* dP = nullptr;
+  std::vector<PatchDev> hP;  // host copy of the patch table
   double* pool = nullptr;
   size_t pool_elems = 0;
   long long q_region = 0, q_len = 0, qold_region = 0;
@@ -72,6 +73,17 @@ struct Hier {
   size_t e_len = 0;  // leading FP32 elements holding every patch's correction e
   size_t e_coarse_off = 0, e_coarse_len = 0;  // the part of it on levels < 0
   Blk* mx_norm_blk[kNLev] = {};               // padded interior lists (mixed norm)
+  Blk* mx_prep_coarse = nullptr;              // interior lists of all levels < 0
+  int mx_prep_coarse_n = 0;
+  // coarse tail of the V-cycle (levels <= tail_level run in one CTA); the
+  // recorded programs per (minlevel, nsmooth): device phases and their count
+  int tail_level = -kMaxDepth - 2;
+  long long tail_cells = 2048;  // latency-friendly; a serving loop may raise it
+  // keys: (start level, minlevel, nsmooth) for V-cycles, (start level,
+  // minlevel, -field) for FillDown
+  using TailKey = std::tuple<int, int, int>;
+  std::map<TailKey, std::pair<void*, int>> mx_tail_progs, fp_tail_progs;
+  void* rec = nullptr;  // std::vector<TailPhase> being recorded
   // periodic-box mixed path (box.cu): every level one periodic box with even
   // extents covering its parent; FP64 iterate held as float pairs
   bool box = false;
@@ -144,9 +156,20 @@ struct bsamg_ctx {
   int device = 0;
   size_t budget = 0;
   size_t used = 0;
+  // every device allocation of the context's hierarchies comes from this
+  // stream-ordered pool; it keeps freed memory (release threshold = max), so
+  // creating and destroying hierarchies neither maps nor unmaps memory
+  cudaMemPool_t mempool = nullptr;
   std::mutex mu;
   double* pinned = nullptr;     // pinned read-back words, one slot per hierarchy
   std::vector<int> free_slots;
 };
 
 struct bsamg_hier : bsamg::Hier {};
+
+namespace bsamg {
+// stream-ordered allocation from the context's pool on the hierarchy's stream
+inline cudaError_t dev_alloc(const Hier& H, void** p, size_t bytes) {
+  return cudaMallocFromPoolAsync(p, bytes, H.ctx->mempool, H.s);
+}
+}  // namespace bsamg

@@ -205,7 +205,67 @@ __global__ void __launch_bounds__(256) k_uni_scatter(const double* __restrict__ 
   U[v * uplane + u] = pool[oq + v * sq + c];
 }
 
+// splitmix64 of the seeded inputs: U(-1,1) from splitmix64(seed ^ (g * golden))
+__device__ __forceinline__ double seeded_pm1(unsigned long long seed, unsigned long long g) {
+  const unsigned long long gold = 0x9E3779B97F4A7C15ull;
+  unsigned long long z = seed ^ (g * gold);
+  z = z + gold;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z = z ^ (z >> 31);
+  return 2.0 * ((double)(z >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+}
+
+// The seeded spinodal start of one CH patch, in the order the host generator
+// evaluates it: phi = mean + amp*U on the cell's index within the patch
+// (i fastest), mu = ((phi*phi*phi) - phi) - eps2 * lap, lap =
+// ((-2 d) phi + (phi[i-1] + phi[i+1]) + ...) / (h*h) with the neighbours
+// wrapped over the patch; ghost layers zero.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_seed_spinodal(double* __restrict__ q, long long sq, int m0, int m1, int m2,
+                                                       unsigned long long seed, double mean, double amp, double eps2,
+                                                       double hh) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int n0 = m0 + 2, n1 = m1 + 2, n2 = DIM == 3 ? m2 + 2 : 1;
+  if (t >= (long long)n0 * n1 * n2) return;
+  int i = (int)(t % n0);
+  long long r = t / n0;
+  int j = (int)(r % n1);
+  int k = DIM == 3 ? (int)(r / n1) : 1;
+  bool ghost = i == 0 || i == n0 - 1 || j == 0 || j == n1 - 1 || (DIM == 3 && (k == 0 || k == n2 - 1));
+  if (ghost) {
+    q[t] = 0.0;
+    q[sq + t] = 0.0;
+    return;
+  }
+  auto phi = [&](int a, int b, int c) {  // interior cell (a, b, c), 0-based, wrapped
+    a = (a + m0) % m0;
+    b = (b + m1) % m1;
+    c = DIM == 3 ? (c + m2) % m2 : 0;
+    unsigned long long g = ((unsigned long long)c * m1 + b) * m0 + a;
+    return mean + amp * seeded_pm1(seed, g);
+  };
+  int a = i - 1, b = j - 1, c = DIM == 3 ? k - 1 : 0;
+  double p = phi(a, b, c);
+  double lap = (-2.0 * DIM) * p;
+  lap = (lap + phi(a - 1, b, c)) + phi(a + 1, b, c);
+  lap = (lap + phi(a, b - 1, c)) + phi(a, b + 1, c);
+  if (DIM == 3) lap = (lap + phi(a, b, c - 1)) + phi(a, b, c + 1);
+  lap = lap / (hh * hh);
+  q[t] = p;
+  q[sq + t] = ((p * p * p) - p) - eps2 * lap;
+}
+
 }  // namespace
+
+int launch_seed_spinodal(cudaStream_t s, int ndims, double* q, long long sq, const int mx[3], unsigned long long seed,
+                         double mean, double amp, double eps2, double h) {
+  long long n = (long long)(mx[0] + 2) * (mx[1] + 2) * (ndims == 3 ? mx[2] + 2 : 1);
+  unsigned grid = (unsigned)((n + 255) / 256);
+  if (ndims == 2) k_seed_spinodal<2><<<grid, 256, 0, s>>>(q, sq, mx[0], mx[1], 1, seed, mean, amp, eps2, h);
+  else k_seed_spinodal<3><<<grid, 256, 0, s>>>(q, sq, mx[0], mx[1], mx[2], seed, mean, amp, eps2, h);
+  return 1;
+}
 
 int launch_stats(const LaunchCtx& c, const Blk* blk, int nblk, bool coarse, int mass, int energy, double* partial,
                  int pofs) {

@@ -30,6 +30,18 @@ enum Kind : int {
   kNKind = 6
 };
 
+// One phase of a V-cycle's coarse tail run inside one thread block (the
+// operations the separate launches of those levels would run, recorded on
+// the host).  kTRing: the coarse ring (arg 0) or CorrectFine's first step
+// (arg 1); kTRelax: arg = ipass; kTFill: FillDownLevel, arg = field.
+enum TailOp : int { kTRelax = 0, kTRestrict = 1, kTRing = 2, kTLoad = 3, kTProlong = 4, kTGhost = 5, kTFill = 6 };
+struct TailPhase {
+  int op, arg, nblk, nstages;
+  const Blk* blk;
+  const GhostOp* ops;
+  const int* stage_off;
+};
+
 // ---- plain FP64 path (fp64.cu, built with --fmad=false) ----
 int launch_relax(const LaunchCtx& c, const Blk* blk, int nblk, int ipass);
 int launch_restrict_q(const LaunchCtx& c, const Blk* blk, int nblk);
@@ -60,10 +72,15 @@ int launch_stats(const LaunchCtx& c, const Blk* blk, int nblk, bool coarse, int 
 int launch_stats_finish(cudaStream_t s, const double* partial, int n, double* out);
 // F = mass-corrected prolongation of the uniform (n+2)^d block A (one variable)
 int launch_uniform_prolong(cudaStream_t s, int ndims, const double* A, double* F, const int n[3]);
+// the seeded spinodal start of one CH patch (q: its ghosted q, two planes of sq)
+int launch_seed_spinodal(cudaStream_t s, int ndims, double* q, long long sq, const int mx[3], unsigned long long seed,
+                         double mean, double amp, double eps2, double h);
 // a patch's ghosted q (nv variables) into the uniform block U (extents un)
 int launch_uniform_scatter(cudaStream_t s, int ndims, const double* pool, long long oq, long long sq, const int qn[3],
                            const int g[3], double* U, const int un[3], int nv);
 int launch_ghost_program_1cta(const LaunchCtx& c, const GhostOp* ops,
                               const int* stage_off, int nstages);
+// the recorded coarse tail of an FP64 V-cycle, one block
+int launch_tail(const LaunchCtx& c, const TailPhase* ph, int nph);
 
 }  // namespace bsamg

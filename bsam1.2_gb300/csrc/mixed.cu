@@ -22,6 +22,7 @@
 // the plain FP64 smoother, which the FP64 pipe bounds.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "launch.h"
@@ -163,12 +164,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_prep(const PatchDev* __restrict__
 //   b1  = g1 + tmp1 * sum(e_mu neighbours)
 //   b2  = g2 - tmp2 * sum(e_phi neighbours) - e^2 (3 pb + 2 e)
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_mx_relax(const PatchDev* __restrict__ P, float* __restrict__ fpool,
-                                                     const Blk* __restrict__ blk, int ipass) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_relax(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
+                                        int tid, int ipass) {
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  if (!color_cell<DIM>(p, b.start + threadIdx.x, ipass, i, j, k)) return;
+  if (!color_cell<DIM>(p, b.start + tid, ipass, i, j, k)) return;
   float* e0 = fpool + p.eq;
   float* e1 = e0 + p.sq;
   long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
@@ -194,6 +194,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_relax(const PatchDev* __restrict_
   e0[c] = (b1 - a12 * b2) * rdet;
   e1[c] = (b2 - a21 * b1) * rdet;
 }
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_mx_relax(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                     const Blk* __restrict__ blk, int ipass) {
+  u_relax<DIM>(P, fpool, blk[blockIdx.x], threadIdx.x, ipass);
+}
 
 template <int DIM, typename F>
 __device__ __forceinline__ float restrict_at(F at, int ci, int cj, int ck) {
@@ -206,12 +211,11 @@ __device__ __forceinline__ float restrict_at(F at, int ci, int cj, int ck) {
 
 // RestrictSolution on e: ec(1:cmx) = R(e); parent e(mb) = ec
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_mx_restrict(const PatchDev* __restrict__ P, float* __restrict__ fpool,
-                                                        const Blk* __restrict__ blk, int nrvars) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_restrict(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
+                                           int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
   int ci, cj, ck;
-  if (!interior_cell<DIM>(p.cmx, b.start + threadIdx.x, ci, cj, ck)) return;
+  if (!interior_cell<DIM>(p.cmx, b.start + tid, ci, cj, ck)) return;
   const PatchDev& par = P[p.parent];
   for (int v = 0; v < nrvars; v++) {
     const float* e = fpool + p.eq + v * p.sq;
@@ -222,17 +226,21 @@ __global__ void __launch_bounds__(kBlock) k_mx_restrict(const PatchDev* __restri
           gofs<DIM>(par.qn, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 0)] = val;
   }
 }
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_mx_restrict(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                        const Blk* __restrict__ blk, int nrvars) {
+  u_restrict<DIM>(P, fpool, blk[blockIdx.x], threadIdx.x, nrvars);
+}
 
 // GetCoarseGhostPoints on e (ring of ec <- parent e) when corr == 0;
 // CorrectFine step 1 (ec = parent e - ec over the whole ghosted ec) when
 // corr == 1.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_mx_coarse_ring(const PatchDev* __restrict__ P, float* __restrict__ fpool,
-                                                           const Blk* __restrict__ blk, int nrvars, int corr) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_coarse_ring(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
+                                              int tid, int nrvars, int corr) {
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  if (!ghosted_cell<DIM>(p.cn, b.start + threadIdx.x, i, j, k)) return;
+  if (!ghosted_cell<DIM>(p.cn, b.start + tid, i, j, k)) return;
   if (!corr) {
     bool ring = i == 0 || i == p.cmx[0] + 1 || j == 0 || j == p.cmx[1] + 1 ||
                 (DIM == 3 && (k == 0 || k == p.cmx[2] + 1));
@@ -248,16 +256,20 @@ __global__ void __launch_bounds__(kBlock) k_mx_coarse_ring(const PatchDev* __res
     ec[dst] = corr ? pv - ec[dst] : pv;
   }
 }
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_mx_coarse_ring(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                           const Blk* __restrict__ blk, int nrvars, int corr) {
+  u_coarse_ring<DIM>(P, fpool, blk[blockIdx.x], threadIdx.x, nrvars, corr);
+}
 
 // CoarseLoadingFunction on the correction: fine r = g - M(e) under each
 // coarse cell; parent g(mb) = R(r) + M_c(ec) with the parent's base field.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_mx_coarse_load(const PatchDev* __restrict__ P, float* __restrict__ fpool,
-                                                           const Blk* __restrict__ blk) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_coarse_load(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
+                                              int tid) {
   const PatchDev& p = P[b.patch];
   int ci, cj, ck;
-  if (!interior_cell<DIM>(p.cmx, b.start + threadIdx.x, ci, cj, ck)) return;
+  if (!interior_cell<DIM>(p.cmx, b.start + tid, ci, cj, ck)) return;
   const PatchDev& par = P[p.parent];
   const float* e = fpool + p.eq;
   long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
@@ -289,6 +301,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_coarse_load(const PatchDev* __res
   fpool[par.eg + pf] = R0 + m0;
   fpool[par.eg + par.sf + pf] = R1 + m1;
 }
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_mx_coarse_load(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                           const Blk* __restrict__ blk) {
+  u_coarse_load<DIM>(P, fpool, blk[blockIdx.x], threadIdx.x);
+}
 
 // CorrectFine step 2 on e: e(0:mx+1) += P(ec).
 // One thread per coarse index (ci,cj,ck) in 0..cmx: it produces the fine
@@ -296,12 +313,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_coarse_load(const PatchDev* __res
 // the same per-direction (3,1)/4 weights as BiLin/TriLinProlongationP1
 // (gridutilities.f90:156-195, :510-566).
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_mx_prolong(const PatchDev* __restrict__ P, float* __restrict__ fpool,
-                                                       const Blk* __restrict__ blk, int nrvars) {
-  const Blk b = blk[blockIdx.x];
+__device__ __forceinline__ void u_prolong(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
+                                          int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
   int cpn[3] = {p.cmx[0] + 1, p.cmx[1] + 1, DIM == 3 ? p.cmx[2] + 1 : 1};
-  int t = b.start + threadIdx.x;
+  int t = b.start + tid;
   int ci = t % cpn[0], r = t / cpn[0];
   int cj = r % cpn[1], ck = r / cpn[1];
   if (ck >= cpn[2]) return;
@@ -333,6 +349,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_prolong(const PatchDev* __restric
           e[gofs<DIM>(p.qn, i, j, k)] += add;
         }
   }
+}
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_mx_prolong(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                       const Blk* __restrict__ blk, int nrvars) {
+  u_prolong<DIM>(P, fpool, blk[blockIdx.x], threadIdx.x, nrvars);
 }
 
 // step 3: qbar += e (whole ghosted array).  The
@@ -509,6 +530,44 @@ __global__ void __launch_bounds__(kBlock) k_ghost32_program(const PatchDev* __re
   }
 }
 
+// The coarse tail of a V-cycle in one CTA.  Below some level every level of
+// a hierarchy is small (a few thousand cells), and the launches of its
+// V-cycle (~20 per level) cost more than their work.  The tail program is
+// the sequence of operations mx_vcycle would launch from that level down,
+// recorded once on the host; this kernel executes it phase by phase, every
+// work-list block of a phase by the whole CTA (256 threads = one block's
+// units), with a barrier between phases.  Each unit computes exactly what
+// the stand-alone kernel computes, so results are bit-identical.
+
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_mx_tail(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                   const TailPhase* __restrict__ ph, int nph, int nrvars) {
+  for (int x = 0; x < nph; x++) {
+    const TailPhase f = ph[x];
+    if (f.op == kTGhost) {
+      for (int s = 0; s < f.nstages; s++) {
+        for (int t = f.stage_off[s] + threadIdx.x; t < f.stage_off[s + 1]; t += blockDim.x) {
+          GhostOp g = f.ops[t];
+          ghost32_apply(P, fpool, g, nrvars);
+        }
+        __syncthreads();
+      }
+      continue;
+    }
+    for (int b = 0; b < f.nblk; b++) {
+      const Blk bb = f.blk[b];
+      switch (f.op) {
+        case kTRelax: u_relax<DIM>(P, fpool, bb, threadIdx.x, f.arg); break;
+        case kTRestrict: u_restrict<DIM>(P, fpool, bb, threadIdx.x, nrvars); break;
+        case kTRing: u_coarse_ring<DIM>(P, fpool, bb, threadIdx.x, nrvars, f.arg); break;
+        case kTLoad: u_coarse_load<DIM>(P, fpool, bb, threadIdx.x); break;
+        default: u_prolong<DIM>(P, fpool, bb, threadIdx.x, nrvars); break;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------------------
 // schedule
 
@@ -525,10 +584,17 @@ __global__ void __launch_bounds__(kBlock) k_ghost32_program(const PatchDev* __re
 
 #define MX_LAUNCH_W MX_LAUNCH
 
+// the tail program being recorded (mx_vcycle records instead of launching)
+std::vector<TailPhase>* rec_of(Hier& H) { return static_cast<std::vector<TailPhase>*>(H.rec); }
+
 int mx_set_ghost(Hier& H, int level, int ipass) {
   GhostProg& g = H.L(level).gp[ipass];
   int nst = (int)g.stage_off.size() - 1;
   if (nst <= 0) return BSAMG_OK;
+  if (auto* rec = rec_of(H)) {
+    rec->push_back(TailPhase{kTGhost, 0, 0, nst, nullptr, g.d_ops, g.d_stage_off});
+    return BSAMG_OK;
+  }
   int nops = g.stage_off[nst];
   if (nops <= 2048) {
     k_ghost32_program<<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, g.d_ops, g.d_stage_off, nst, H.nrvars);
@@ -545,32 +611,80 @@ int mx_set_ghost(Hier& H, int level, int ipass) {
   return BSAMG_OK;
 }
 
-int mx_level_relax(Hier& H, int level, int nsmooth) {
+// one work-list operation of the V-cycle: launched, or recorded into the
+// tail program
+int mx_op(Hier& H, int level, int kind, int op, int arg) {
   LevelT& L = H.L(level);
+  if (auto* rec = rec_of(H)) {
+    if (L.nblk[kind] > 0) rec->push_back(TailPhase{op, arg, L.nblk[kind], 0, L.d_blk[kind], nullptr, nullptr});
+    return BSAMG_OK;
+  }
+  switch (op) {
+    case kTRelax: MX_LAUNCH_W(H, kind, k_mx_relax, H.dP, H.fpool, L.d_blk[kind], arg); break;
+    case kTRestrict: MX_LAUNCH(H, kind, k_mx_restrict, H.dP, H.fpool, L.d_blk[kind], H.nrvars); break;
+    case kTRing: MX_LAUNCH_W(H, kind, k_mx_coarse_ring, H.dP, H.fpool, L.d_blk[kind], H.nrvars, arg); break;
+    case kTLoad: MX_LAUNCH_W(H, kind, k_mx_coarse_load, H.dP, H.fpool, L.d_blk[kind]); break;
+    default: MX_LAUNCH_W(H, kind, k_mx_prolong, H.dP, H.fpool, L.d_blk[kind], H.nrvars); break;
+  }
+  return BSAMG_OK;
+}
+
+int mx_level_relax(Hier& H, int level, int nsmooth) {
   for (int pass = 1; pass <= nsmooth; pass++)
     for (int rb = 1; rb <= 2; rb++) {
-      MX_LAUNCH_W(H, kKindColor, k_mx_relax, H.dP, H.fpool, L.d_blk[kKindColor], rb);
-      int r = mx_set_ghost(H, level, rb);
+      int r = mx_op(H, level, kKindColor, kTRelax, rb);
+      if (!r) r = mx_set_ghost(H, level, rb);
       if (r) return r;
     }
   return BSAMG_OK;
 }
 
 int mx_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
+  if (!H.rec && level <= H.tail_level && level >= minlevel) {
+    auto it = H.mx_tail_progs.find(std::make_tuple(level, minlevel, nsmooth));
+    if (it != H.mx_tail_progs.end()) {  // the whole V-cycle from here down in one CTA
+      const TailPhase* ph = static_cast<const TailPhase*>(it->second.first);
+      if (H.ndims == 2) k_mx_tail<2><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, it->second.second, H.nrvars);
+      else k_mx_tail<3><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, it->second.second, H.nrvars);
+      return after_launch(H, 1);
+    }
+  }
   int r = mx_level_relax(H, level, nsmooth);
   if (r) return r;
   if (level > minlevel) {
-    LevelT& L = H.L(level);
-    MX_LAUNCH(H, kKindCoarse, k_mx_restrict, H.dP, H.fpool, L.d_blk[kKindCoarse], H.nrvars);
+    if ((r = mx_op(H, level, kKindCoarse, kTRestrict, 0))) return r;
     if ((r = mx_set_ghost(H, level - 1, 0))) return r;
-    MX_LAUNCH_W(H, kKindCGhost, k_mx_coarse_ring, H.dP, H.fpool, L.d_blk[kKindCGhost], H.nrvars, 0);
-    MX_LAUNCH_W(H, kKindCoarse, k_mx_coarse_load, H.dP, H.fpool, L.d_blk[kKindCoarse]);
+    if ((r = mx_op(H, level, kKindCGhost, kTRing, 0))) return r;
+    if ((r = mx_op(H, level, kKindCoarse, kTLoad, 0))) return r;
     if ((r = mx_vcycle(H, level - 1, minlevel, nsmooth))) return r;
-    MX_LAUNCH_W(H, kKindCGhost, k_mx_coarse_ring, H.dP, H.fpool, L.d_blk[kKindCGhost], H.nrvars, 1);
-    MX_LAUNCH_W(H, kKindProl, k_mx_prolong, H.dP, H.fpool, L.d_blk[kKindProl], H.nrvars);
+    if ((r = mx_op(H, level, kKindCGhost, kTRing, 1))) return r;
+    if ((r = mx_op(H, level, kKindProl, kTProlong, 0))) return r;
     if ((r = mx_set_ghost(H, level, 0))) return r;
     if ((r = mx_level_relax(H, level, nsmooth))) return r;
   }
+  return BSAMG_OK;
+}
+
+// Record and upload the tail program of (minlevel, nsmooth) once, outside
+// any stream capture.
+int mx_prepare_tail(Hier& H, int finest, int minlevel, int nsmooth) {
+  int start = std::min(finest, H.tail_level);
+  if (start < minlevel) return BSAMG_OK;
+  auto key = std::make_tuple(start, minlevel, nsmooth);
+  if (H.mx_tail_progs.count(key)) return BSAMG_OK;
+  std::vector<TailPhase> prog;
+  H.rec = &prog;
+  int r = mx_vcycle(H, start, minlevel, nsmooth);
+  H.rec = nullptr;
+  if (r) return r;
+  void* d = nullptr;
+  if (!prog.empty()) {
+    cudaError_t e = dev_alloc(H, &d, sizeof(TailPhase) * prog.size());
+    if (e == cudaSuccess)  // staged from pageable memory before it returns
+      e = cudaMemcpyAsync(d, prog.data(), sizeof(TailPhase) * prog.size(), cudaMemcpyHostToDevice, H.s);
+    if (e != cudaSuccess) return cuda_fail(e, "tail program upload");
+  }
+  H.mx_tail_progs[key] = std::make_pair(d, (int)prog.size());
   return BSAMG_OK;
 }
 
@@ -628,6 +742,7 @@ int mx_fill_down_q(Hier& H, int finest, int minlevel) { return enq_fill_down(H, 
 
 // one outer iteration; resync: take g on the finest level from the FP64 rf
 int mx_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype, bool resync) {
+  int r__ = 0;
   // e of levels >= 0 was cleared by the previous update pass (or by
   // mixed_iterations before the first cycle); clear the coarse ones
   if (H.e_coarse_len) {
@@ -640,6 +755,14 @@ int mx_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype, 
     // from the FP64 rf after a resync, else from the tracked update
     if (level == finest && !resync) continue;
     int mode = level < 0 ? 0 : (level == finest ? 1 : 2);
+    if (level < 0 && minlevel == H.minlevel && H.mx_prep_coarse_n > 0) {
+      // every level below the root at once (phib only)
+      int nb = H.mx_prep_coarse_n;
+      if (H.ndims == 2) k_mx_prep<2><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.fpool, H.mx_prep_coarse, 0);
+      else k_mx_prep<3><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.fpool, H.mx_prep_coarse, 0);
+      if ((r__ = after_launch(H, 1))) return r__;
+      break;
+    }
     MX_LAUNCH(H, kKindInterior, k_mx_prep, H.dP, H.pool, H.fpool, L.d_blk[kKindInterior], mode);
   }
   int r = mx_vcycle(H, finest, minlevel, nsmooth);
@@ -684,8 +807,8 @@ int mixed_alloc(Hier& H) {
   if (H.problem != kCH) return BSAMG_OK;
   if (H.box) {
     H.fpool_elems = box_layout(H);
-    cudaError_t e = cudaMallocAsync((void**)&H.fpool, H.fpool_elems * sizeof(float), H.s);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(fpool)");
+    cudaError_t e = dev_alloc(H, (void**)&H.fpool, H.fpool_elems * sizeof(float));
+    if (e != cudaSuccess) return cuda_fail(e, "device allocation (fpool)");
     e = cudaMemsetAsync(H.fpool, 0, H.fpool_elems * sizeof(float), H.s);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(fpool)");
     return BSAMG_OK;
@@ -703,8 +826,8 @@ int mixed_alloc(Hier& H) {
     P.e_ophi = off[4 * p + 3];
   }
   H.fpool_elems = n;
-  cudaError_t e = cudaMallocAsync((void**)&H.fpool, n * sizeof(float), H.s);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(fpool)");
+  cudaError_t e = dev_alloc(H, (void**)&H.fpool, n * sizeof(float));
+  if (e != cudaSuccess) return cuda_fail(e, "device allocation (fpool)");
   e = cudaMemsetAsync(H.fpool, 0, n * sizeof(float), H.s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(fpool)");
   return BSAMG_OK;
@@ -713,6 +836,11 @@ int mixed_alloc(Hier& H) {
 void mixed_free(Hier& H) {
   if (H.fpool) cudaFreeAsync(H.fpool, H.s);
   H.fpool = nullptr;
+  if (H.mx_prep_coarse) cudaFreeAsync(H.mx_prep_coarse, H.s);
+  H.mx_prep_coarse = nullptr;
+  for (auto& kv : H.mx_tail_progs)
+    if (kv.second.first) cudaFreeAsync(kv.second.first, H.s);
+  H.mx_tail_progs.clear();
   for (int l = 0; l < kNLev; l++) {
     if (H.mx_norm_blk[l]) cudaFreeAsync(H.mx_norm_blk[l], H.s);
     H.mx_norm_blk[l] = nullptr;
@@ -731,16 +859,52 @@ int mixed_tables(Hier& H) {
     }
     while (v.size() % kNormCells) v.push_back(Blk{-1, 0});
     Blk* d = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&d, sizeof(Blk) * v.size(), H.s);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(norm list)");
+    cudaError_t e = dev_alloc(H, (void**)&d, sizeof(Blk) * v.size());
+    if (e != cudaSuccess) return cuda_fail(e, "device allocation (norm list)");
+    // staged from pageable memory before the call returns: v may go
     e = cudaMemcpyAsync(d, v.data(), sizeof(Blk) * v.size(), cudaMemcpyHostToDevice, H.s);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(norm list)");
-    e = cudaStreamSynchronize(H.s);  // v is freed at the end of the iteration
-    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
     H.mx_norm_blk[l + kMaxDepth] = d;
     H.bytes += sizeof(Blk) * v.size();
   }
+  // the interior lists of all levels below the root, concatenated
+  std::vector<Blk> v;
+  for (int l = H.minlevel; l < 0; l++)
+    for (int p : H.L(l).patches) {
+      const HostPatch& P = H.patches[p];
+      long long units = (long long)P.mx[0] * P.mx[1] * P.mx[2];
+      for (long long s = 0; s < units; s += kBlock) v.push_back(Blk{p, (int)s});
+    }
+  if (!v.empty()) {
+    cudaError_t e = dev_alloc(H, (void**)&H.mx_prep_coarse, sizeof(Blk) * v.size());
+    if (e == cudaSuccess)  // staged from pageable memory before it returns
+      e = cudaMemcpyAsync(H.mx_prep_coarse, v.data(), sizeof(Blk) * v.size(), cudaMemcpyHostToDevice, H.s);
+    if (e != cudaSuccess) return cuda_fail(e, "coarse prep list");
+    H.mx_prep_coarse_n = (int)v.size();
+    H.bytes += sizeof(Blk) * v.size();
+  }
   return BSAMG_OK;
+}
+
+void set_tail(Hier& H, long long cells) {
+  // the highest level whose level and every level below it together hold at
+  // most `cells` interior cells runs the rest of the V-cycle in one CTA
+  for (auto* progs : {&H.mx_tail_progs, &H.fp_tail_progs}) {
+    for (auto& kv : *progs)
+      if (kv.second.first) cudaFreeAsync(kv.second.first, H.s);
+    progs->clear();
+  }
+  H.tail_cells = cells;
+  H.tail_level = -kMaxDepth - 2;
+  long long sum = 0;
+  for (int l = H.minlevel; l <= H.maxlevel; l++) {
+    for (int p : H.L(l).patches) {
+      const HostPatch& P = H.patches[p];
+      sum += (long long)P.mx[0] * P.mx[1] * P.mx[2];
+    }
+    if (sum > cells) break;
+    H.tail_level = l;
+  }
 }
 
 int mixed_enq_relax(Hier& H, int level, int ipass) {
@@ -762,6 +926,7 @@ int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcyc
   cudaError_t ce = cudaStreamSynchronize(H.s);
   if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize");
   double r_sync = H.h_norm[0];  // FP64 residual the current g was taken from
+  if ((r = mx_prepare_tail(H, finest, minlevel, nsmooth))) return r;
   Hier::GraphRec *ga = nullptr, *gt = nullptr, *gv = nullptr;
   auto key = [&](int m) { return std::make_tuple(m, finest, minlevel, nsmooth, errortype); };
   if ((r = capture_graph(H, key(11), [&] { return mx_iteration(H, finest, minlevel, nsmooth, errortype, true); },

@@ -16,6 +16,10 @@ int mixed_tables(Hier& H);
 // FillDown(q), sources, FillDown(f)); same contract as the FP64 loop
 int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,
                      int strict, int* ncycles, double* residuals);
+// choose the coarse tail of the mixed V-cycle: levels from minlevel up to
+// the highest one at which the cumulative interior cell count is at most
+// `cells` run inside one CTA (0 disables)
+void set_tail(Hier& H, long long cells);
 // one FP32 colour sweep of the correction smoother on `level`
 int mixed_enq_relax(Hier& H, int level, int ipass);
 

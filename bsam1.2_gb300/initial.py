@@ -47,10 +47,12 @@ def periodic_lap(a, h):
 
 
 def ch_spinodal(shape, eps, h, seed, mean=0.0, amp=0.05):
-    """phi0 = mean + amp*U(-1,1), mu0 from phi0; returns the ghosted q array
-    (Fortran order, shape (mx+2, ..., 2)) with zero ghosts."""
+    """phi0 = mean + amp*U(-1,1), mu0 from phi0 (the Laplacian wrapped over
+    the array; products in the order written, as the device generator
+    bsamg_seed_spinodal forms them); returns the ghosted q array (Fortran
+    order, shape (mx+2, ..., 2)) with zero ghosts."""
     phi = mean + amp * splitmix_pm1(seed, global_index(shape))
-    mu = phi ** 3 - phi - eps * eps * periodic_lap(phi, h)
+    mu = phi * phi * phi - phi - eps * eps * periodic_lap(phi, h)
     q = np.zeros(tuple(n + 2 for n in shape) + (2,), order="F")
     sl = tuple(slice(1, -1) for _ in shape)
     q[sl + (0,)] = phi

@@ -22,7 +22,6 @@ import time
 import numpy as np
 
 from .api import BsamgError, Hierarchy
-from . import initial
 
 BSAMG_ERR_BUDGET = -3
 
@@ -36,6 +35,7 @@ class Request:
         self.unconverged = 0  # steps that reached maxvcycles above tol
         self.result = None
         self.error = None
+        self.phases = {}  # seconds spent in each part of run_request
 
     @property
     def latency(self):
@@ -86,16 +86,30 @@ def nested_spec(ndims, n, levels):
 
 
 class Server:
-    """Worker slots over one Context; submit() requests, then drain()."""
+    """Worker slots over one Context; submit() requests, then drain().
 
-    def __init__(self, ctx, slots=4, retry_wait=0.002):
+    A finished request's hierarchy is kept, idle, for the next request of the
+    same mesh shape (ndims, root size, levels): that request only sets its
+    parameters and zeroes the fields (bsamg_set_params, bsamg_hier_reset),
+    and its time steps replay the graphs the first one captured.  Idle
+    hierarchies count against the HBM budget; admission frees the oldest
+    idle ones before it waits for memory."""
+
+    def __init__(self, ctx, slots=4, retry_wait=0.002, reuse=True, tail_cells=16384):
         self.ctx = ctx
+        # many hierarchies share the GPU: the coarse tail of every V-cycle runs
+        # in one thread block up to this many cells (bsamg_set_tail_cells)
+        self.tail_cells = tail_cells
         self.slots = slots
         self.q = queue.Queue()
         self.mem = threading.Condition()
         self.retry_wait = retry_wait
         self.done = []
         self.waits = 0  # admissions that had to wait for memory
+        self.reused = 0  # admissions served by an idle hierarchy
+        self.reuse = reuse
+        self.idle = []  # (shape key, (Hierarchy, pats, minlevel)), oldest first
+        self.idle_lock = threading.Lock()
         self.lock = threading.Lock()
         self.workers = [threading.Thread(target=self._work, daemon=True) for _ in range(slots)]
         for w in self.workers:
@@ -109,9 +123,51 @@ class Server:
             self.q.put(None)
         for w in self.workers:
             w.join()
+        with self.idle_lock:
+            idle, self.idle = self.idle, []
+        for _, (h, _, _) in idle:
+            h.close()
+
+    @staticmethod
+    def _key(req):
+        return (req.ndims, req.n, req.levels)
+
+    def _take_idle(self, key):
+        with self.idle_lock:
+            for x in range(len(self.idle) - 1, -1, -1):  # the most recently used
+                if self.idle[x][0] == key:
+                    return self.idle.pop(x)[1]
+        return None
+
+    def _evict_oldest(self):
+        with self.idle_lock:
+            if not self.idle:
+                return False
+            _, (h, _, _) = self.idle.pop(0)
+        h.close()
+        return True
+
+    def _release(self, req, entry):
+        if self.reuse:
+            with self.idle_lock:
+                self.idle.append((self._key(req), entry))
+        else:
+            entry[0].close()
+        with self.mem:
+            self.mem.notify_all()
 
     def _admit(self, req):
-        """Build and commit the request's hierarchy, waiting for memory."""
+        """An idle hierarchy of the request's shape, or a new one built and
+        committed, waiting for memory (after freeing idle ones) if needed."""
+        if self.reuse:
+            entry = self._take_idle(self._key(req))
+            if entry is not None:
+                h = entry[0]
+                h.set_params([req.dt, req.eps])
+                h.reset()
+                with self.lock:
+                    self.reused += 1
+                return entry
         pats, minlevel = nested_spec(req.ndims, req.n, req.levels)
         while True:
             h = Hierarchy(self.ctx, req.ndims, 2, "ch", [req.dt, req.eps])
@@ -121,11 +177,14 @@ class Server:
             used_before = self.ctx.usage()[0]
             try:
                 h.commit()
+                h.set_tail_cells(self.tail_cells)
                 return h, pats, minlevel
             except BsamgError as e:
                 h.close()
                 if e.status != BSAMG_ERR_BUDGET:
                     raise
+                if self._evict_oldest():
+                    continue
                 if used_before == 0:  # nothing else held memory: it can never fit
                     raise RuntimeError(f"request {req.rid} needs more than the whole HBM budget") from e
                 with self.mem:
@@ -134,13 +193,17 @@ class Server:
 
     def run_request(self, req):
         """Run one request to completion in the calling thread."""
-        h, pats, minlevel = self._admit(req)
+        t0 = time.perf_counter()
+        entry = self._admit(req)
+        h, pats, minlevel = entry
+        t1 = time.perf_counter()
+        ok = False
         try:
-            req.start = time.perf_counter()
-            for p in pats:
+            req.start = t1
+            for p in pats:  # the seeded start, generated on the device
                 if p["level"] >= 0:
-                    shape = tuple(p["mx"][: req.ndims])
-                    h.put(p["id"], "q", initial.ch_spinodal(shape, req.eps, p["dx"][0], seed=req.seed + p["id"]))
+                    h.seed_spinodal(p["id"], req.seed + p["id"])
+            t2 = time.perf_counter()
             finest = max(p["level"] for p in pats)
             for s in range(req.steps):
                 # as the reference, a step that reaches maxvcycles ends there
@@ -149,12 +212,19 @@ class Server:
                 req.vcycles += n
                 if res and res[-1] >= req.tol:
                     req.unconverged += 1
+            t3 = time.perf_counter()
             req.result = {p["id"]: h.get(p["id"], "q") for p in pats if p["level"] >= 0}
+            t4 = time.perf_counter()
+            ok = True
         finally:
-            h.close()
-            with self.mem:
-                self.mem.notify_all()
+            if ok:
+                self._release(req, entry)
+            else:  # a failed run's hierarchy is not reused
+                h.close()
+                with self.mem:
+                    self.mem.notify_all()
         req.done = time.perf_counter()
+        req.phases = dict(admit=t1 - t0, init=t2 - t1, steps=t3 - t2, result=t4 - t3, close=req.done - t4)
 
     def _work(self):
         while True:
@@ -214,6 +284,7 @@ def serve(ctx, requests, slots=4, stats=None):
     srv.close()
     if stats is not None:
         stats["admission_waits"] = srv.waits
+        stats["reused_hierarchies"] = srv.reused
     wall = max(r.done for r in requests) - t0
     return srv.done, wall
 
@@ -226,7 +297,14 @@ def summarize(done, wall):
     for r in done:
         if r.error is not None:
             errs[r.error] = errs.get(r.error, 0) + 1
+    phases = {}
+    for r in ok:
+        for k, v in r.phases.items():
+            phases[k] = phases.get(k, 0.0) + v
+    phase_ms = {k: 1e3 * v / len(ok) for k, v in phases.items()} if ok else {}
+    queue_ms = float(np.mean([(r.done - r.arrival) * 1e3 - sum(r.phases.values()) * 1e3 for r in ok])) if ok else 0.0
     return dict(requests=len(done), failed=len(done) - len(ok), errors=errs, wall_s=wall,
+                mean_phase_ms=phase_ms, mean_queue_ms=queue_ms,
                 req_per_s=len(ok) / wall if wall > 0 else 0.0, steps_per_s=steps / wall if wall > 0 else 0.0,
                 p50_ms=float(np.percentile(lat, 50)), p99_ms=float(np.percentile(lat, 99)),
                 vcycles=sum(r.vcycles for r in ok), unconverged_steps=sum(r.unconverged for r in ok))

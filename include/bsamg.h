@@ -229,6 +229,16 @@ int bsamg_read_q(bsamg_hier* root, const char* path, int first_id, double* time,
 int bsamg_format_f25_12(double x, char* out);
 int bsamg_format_stats_line(double time, const double integral[2], long long meshsize, char* out, size_t n);
 
+/* The seeded spinodal start of the benchmark configurations, generated on
+ * the device for one CH patch (no reference counterpart: it stands in for
+ * the plugin's QInit2D/3D, CH/problem.f90:45-146, with the project's seeded
+ * inputs): phi = mean + amp*U(-1,1), U = splitmix64(seed ^ (g * 0x9E3779B9
+ * 7F4A7C15)) mapped to (-1,1) with g the cell's index within the patch
+ * (i fastest); mu = phi^3 - phi - eps^2 Lap_h(phi), the Laplacian wrapped
+ * over the patch; ghost layers zero.  Enqueued on the hierarchy's stream;
+ * bit-identical to the host generator of the same definition. */
+int bsamg_seed_spinodal(bsamg_hier* h, int id, unsigned long long seed, double mean, double amp);
+
 /* Wait for all work of the hierarchy; returns the first deferred error. */
 int bsamg_sync(bsamg_hier* h);
 /* CUDA stream the hierarchy launches on (cudaStream_t as void*), for
@@ -236,6 +246,25 @@ int bsamg_sync(bsamg_hier* h);
 int bsamg_stream(bsamg_hier* h, void** stream);
 /* Kernel launches issued by this hierarchy since creation. */
 int bsamg_launch_count(const bsamg_hier* h, long long* n);
+/* Reuse of a committed hierarchy for another run on the same mesh (no
+ * reference counterpart; a serving loop keeps hierarchies of recurring
+ * shapes instead of building them again).  bsamg_set_params replaces the
+ * plugin parameters (same meaning and count rules as bsamg_hier_create) and
+ * recomputes the per-patch coefficients; bsamg_hier_reset returns every
+ * field to the zero fill of bsamg_commit.  Both are stream-ordered: work
+ * already enqueued runs with the old values.  After both, a run gives the
+ * same results as on a newly built hierarchy. */
+int bsamg_set_params(bsamg_hier* h, const double* params, int nparams);
+int bsamg_hier_reset(bsamg_hier* h);
+/* Tuning (no reference counterpart): the mixed V-cycle runs its coarse
+ * tail -- the levels from minlevel up to the highest one at which the
+ * levels together hold at most `cells` interior cells -- inside one thread
+ * block, one launch instead of ~20 per level; results are bit-identical.
+ * Default 2048, where one block is still as fast as the launches it
+ * replaces; a larger value trades a single run's latency for throughput
+ * when many hierarchies share the GPU.  0 disables.  Drops the hierarchy's
+ * captured graphs. */
+int bsamg_set_tail_cells(bsamg_hier* h, long long cells);
 
 /* Timing support (no reference counterpart: measurement hooks).
  * bsamg_mark records CUDA event `slot` (0..63) on the hierarchy's stream;

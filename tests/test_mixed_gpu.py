@@ -59,3 +59,34 @@ def test_mixed_reaches_the_fp64_solution(pkg, ctx, oracle_mod, case):
           f"{err_tight:.3e} at tol {tight:g}")
     assert err_tight <= tight_bound
     assert err <= bound
+
+
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
+@pytest.mark.parametrize("nd,n,levels", [(2, 64, 2), (3, 32, 1), (3, 16, 2)])
+def test_coarse_tail_in_one_block_is_bit_identical(pkg, ctx, nd, n, levels, mode):
+    """The single-block coarse tail of the V-cycle executes the same per-unit
+    operations as the separate launches, phase by phase: the iterates after
+    time steps are bit-identical with the tail on and off (FP64 and mixed
+    paths), and the tail cuts the launches."""
+    pats, mn = pkg.serve.nested_spec(nd, n, levels)
+    res = {}
+    for cells in (16384, 0):
+        h = pkg.Hierarchy(ctx, nd, 2, "ch", [1e-3 if nd == 2 else 5e-4, 0.02])
+        for p in pats:
+            h.add_patch(p["level"], p["id"], p["parent_id"], p["mx"], p["mglobal"], p["mbounds"], p["mthbc"],
+                        p["dx"], p["xlower"])
+        h.commit()
+        h.set_tail_cells(cells)
+        for p in pats:
+            if p["level"] >= 0:
+                h.seed_spinodal(p["id"], 5 + p["id"])
+        fin = max(p["level"] for p in pats)
+        l0 = h.launch_count()
+        hist = [h.time_step(s == 0, fin, mn, 2, 30, 1e-8, mode=mode) for s in range(3)]
+        res[cells] = (hist, {p["id"]: h.get(p["id"], "q") for p in pats if p["level"] >= 0}, h.launch_count() - l0)
+        h.close()
+    (ha, qa, la), (hb, qb, lb) = res[16384], res[0]
+    assert ha == hb
+    for pid in qa:
+        assert np.array_equal(qa[pid], qb[pid]), pid
+    assert la < lb, (la, lb)

@@ -52,3 +52,53 @@ def test_request_larger_than_the_budget_fails_cleanly(pkg):
     done, _ = serve.serve(ctx, [r], slots=1)
     ctx.close()
     assert done[0].error is not None and "budget" in done[0].error
+
+
+@pytest.mark.parametrize("nd,n,levels", [(2, 64, 2), (3, 32, 1)])
+def test_device_seeded_start_equals_the_host_generator(pkg, ctx, nd, n, levels):
+    """bsamg_seed_spinodal (the serving loop's initial data) forms the same
+    doubles as initial.ch_spinodal: splitmix64 per cell, the wrapped
+    Laplacian and mu in the same operation order."""
+    pats, _ = pkg.serve.nested_spec(nd, n, levels)
+    h = pkg.Hierarchy(ctx, nd, 2, "ch", [1e-3, 0.017])
+    for p in pats:
+        h.add_patch(p["level"], p["id"], p["parent_id"], p["mx"], p["mglobal"], p["mbounds"], p["mthbc"], p["dx"],
+                    p["xlower"])
+    h.commit()
+    for p in pats:
+        if p["level"] < 0:
+            continue
+        h.seed_spinodal(p["id"], 99 + p["id"], mean=0.1, amp=0.05)
+        want = pkg.initial.ch_spinodal(tuple(p["mx"][:nd]), 0.017, p["dx"][0], seed=99 + p["id"], mean=0.1)
+        got = h.get(p["id"], "q").reshape(want.shape, order="F")
+        assert np.array_equal(got, want), (p["id"], np.max(np.abs(got - want)))
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+@pytest.mark.parametrize("shape", [(2, 64, 2), (2, 32, 0), (3, 32, 1)])
+def test_reused_hierarchy_gives_the_fresh_result(pkg, mode, shape):
+    """A request served by an idle hierarchy left by another request of the
+    same shape (other eps, dt and seed: bsamg_set_params + bsamg_hier_reset)
+    gives bit for bit what it gives on a newly built hierarchy."""
+    serve = pkg.serve
+    nd, n, lv = shape
+
+    def pair():
+        return (serve.Request(0, nd, n, lv, 3, 0.021, 1e-3, seed=31, mode=mode),
+                serve.Request(1, nd, n, lv, 2, 0.013, 5e-4, seed=32, mode=mode))
+    ctx = pkg.Context(0)
+    fresh = serve.Server(ctx, slots=1, reuse=False)
+    _, b0 = pair()
+    fresh.run_request(b0)
+    fresh.close()
+    srv = serve.Server(ctx, slots=1, reuse=True)
+    a1, b1 = pair()
+    srv.run_request(a1)
+    srv.run_request(b1)
+    assert srv.reused == 1
+    srv.close()
+    ctx.close()
+    assert b0.error is None and b1.error is None
+    assert b0.vcycles == b1.vcycles
+    for pid in b0.result:
+        assert np.array_equal(b0.result[pid], b1.result[pid]), pid
