@@ -542,11 +542,14 @@ def serve_arm(args, dist):
     out = {}
     for mode in ("mixed", "fp64"):
         ctx = pkg.Context(dist.local, hbm_budget=int(args.serve_budget_gb * 2**30))
+        if args.serve_blocking_wait:
+            ctx.set_blocking_wait(True)
         warm = pkg.serve.poisson_stream(200.0, 0.05, seed=7, mode=mode)
-        pkg.serve.serve(ctx, warm, slots=args.serve_slots)
+        pkg.serve.serve(ctx, warm, slots=args.serve_slots, tail_cells=args.serve_tail_cells)
         reqs = pkg.serve.poisson_stream(200.0, duration, seed=2024, mode=mode)
         stats = {}
-        done, wall = pkg.serve.serve(ctx, reqs, slots=args.serve_slots, stats=stats)
+        done, wall = pkg.serve.serve(ctx, reqs, slots=args.serve_slots, stats=stats,
+                                     tail_cells=args.serve_tail_cells)
         ctx.close()
         out[mode] = dict(pkg.serve.summarize(done, wall), **stats)
     m, f = out["mixed"], out["fp64"]
@@ -557,6 +560,7 @@ def serve_arm(args, dist):
         "data": "synthetic (seeded Poisson arrivals and spinodal starts)",
         "config": {"workload": "serve", "arrival_rate_per_s": 200.0, "arrival_window_s": duration,
                    "slots": args.serve_slots, "hbm_budget_gb": args.serve_budget_gb,
+                   "tail_cells": args.serve_tail_cells, "blocking_wait": bool(args.serve_blocking_wait),
                    "mix": "2D roots {32,64,128,256}^2 or 3D roots {32,64}^3, each with 0-3 nested levels, 1-20 steps"},
         "p50_ms": m["p50_ms"], "p99_ms": m["p99_ms"], "serving_mixed": m, "serving_fp64": f,
         "speedup_mixed_vs_fp64": m["steps_per_s"] / f["steps_per_s"] if f["steps_per_s"] else None,
@@ -572,8 +576,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ch3d-256", choices=list(WORKLOADS) + list(AMR_WORKLOADS) + ["serve"])
-    ap.add_argument("--serve-slots", type=int, default=32)
+    ap.add_argument("--serve-slots", type=int, default=64)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
+    ap.add_argument("--serve-tail-cells", type=int, default=16384)
+    ap.add_argument("--serve-blocking-wait", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()

@@ -89,6 +89,7 @@ def lib():
         "bsamg_init": ([I, SZ, ctypes.POINTER(P)], I),
         "bsamg_finalize": ([P], I),
         "bsamg_ctx_usage": ([P, ctypes.POINTER(SZ), ctypes.POINTER(SZ)], I),
+        "bsamg_ctx_set_blocking_wait": ([P, I], I),
         "bsamg_hier_create": ([P, I, I, I, I, DP, I, DP, ctypes.POINTER(P)], I),
         "bsamg_hier_destroy": ([P], I),
         "bsamg_patch_add": ([P, I, I, I, IP, IP, IP, IP, DP, DP], I),
@@ -171,6 +172,10 @@ class Context:
         u, b = ctypes.c_size_t(), ctypes.c_size_t()
         _ck(lib().bsamg_ctx_usage(self.h, ctypes.byref(u), ctypes.byref(b)), "bsamg_ctx_usage")
         return u.value, b.value
+
+    def set_blocking_wait(self, on=True):
+        """Host waits sleep instead of spinning (bsamg_ctx_set_blocking_wait)."""
+        _ck(lib().bsamg_ctx_set_blocking_wait(self.h, int(bool(on))), "bsamg_ctx_set_blocking_wait")
 
     def close(self):
         if getattr(self, "h", None):

@@ -777,8 +777,7 @@ int box_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycle
             H.b_oflo);
   int r = bx_resid(H, finest, errortype);
   if (r) return r;
-  cudaError_t ce = cudaStreamSynchronize(H.s);
-  if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize");
+  if (int rw = stream_wait(H)) return rw;
   if (*H.h_nonfinite) return BSAMG_ERR_NONFINITE;
   double r_sync = H.h_norm[0];
   Hier::GraphRec *gc = nullptr, *gv = nullptr;

@@ -263,11 +263,25 @@ int capture_graph(Hier& H, const GraphKey& key, const std::function<int()>& body
   return BSAMG_OK;
 }
 
+// Wait for the hierarchy's stream.  With the context's blocking waits on,
+// the host thread sleeps on an event instead of spinning, which leaves the
+// host cores to the threads that launch work when many hierarchies share
+// the GPU.
+int stream_wait(Hier& H) {
+  if (!H.ctx->blocking_wait) {
+    CK(cudaStreamSynchronize(H.s));
+    return BSAMG_OK;
+  }
+  if (!H.done_ev) CK(cudaEventCreateWithFlags(&H.done_ev, cudaEventBlockingSync | cudaEventDisableTiming));
+  CK(cudaEventRecord(H.done_ev, H.s));
+  CK(cudaEventSynchronize(H.done_ev));
+  return BSAMG_OK;
+}
+
 int replay(Hier& H, Hier::GraphRec* g) {
   CK(cudaGraphLaunch(g->exec, H.s));
   H.launches += g->nlaunch;
-  CK(cudaStreamSynchronize(H.s));
-  return BSAMG_OK;
+  return stream_wait(H);
 }
 
 // plugin coefficients for a spacing h (see PatchDev::c)
@@ -687,6 +701,7 @@ void release(Hier& H) {
   if (H.s) cudaStreamSynchronize(H.s);
   for (int m = 0; m < 64; m++)
     if (H.marks[m]) cudaEventDestroy(H.marks[m]);
+  if (H.done_ev) cudaEventDestroy(H.done_ev);
   for (auto& kv : H.graphs)
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
   H.graphs.clear();
@@ -785,6 +800,12 @@ int bsamg_finalize(bsamg_ctx* ctx) {
   if (ctx && ctx->pinned) cudaFreeHost(ctx->pinned);
   if (ctx && ctx->mempool) cudaMemPoolDestroy(ctx->mempool);
   delete ctx;
+  return BSAMG_OK;
+}
+
+int bsamg_ctx_set_blocking_wait(bsamg_ctx* ctx, int on) {
+  if (!ctx) return BSAMG_ERR_ARG;
+  ctx->blocking_wait = on != 0;
   return BSAMG_OK;
 }
 
@@ -901,8 +922,7 @@ int bsamg_put_field(bsamg_hier* h, int id, int field, const double* a, size_t n)
   if (!d || nn != n) return BSAMG_ERR_ARG;
   RET(set_device(*h));
   CK(cudaMemcpyAsync(d, a, n * sizeof(double), cudaMemcpyHostToDevice, h->s));
-  CK(cudaStreamSynchronize(h->s));
-  return BSAMG_OK;
+  return stream_wait(*h);
 }
 
 int bsamg_get_field(bsamg_hier* h, int id, int field, double* a, size_t n) {
@@ -914,8 +934,7 @@ int bsamg_get_field(bsamg_hier* h, int id, int field, double* a, size_t n) {
   if (!d || nn != n) return BSAMG_ERR_ARG;
   RET(set_device(*h));
   CK(cudaMemcpyAsync(a, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
-  CK(cudaStreamSynchronize(h->s));
-  return BSAMG_OK;
+  return stream_wait(*h);
 }
 
 int bsamg_relax_level_color(bsamg_hier* h, int level, int ipass) {

@@ -112,6 +112,7 @@ struct Hier {
   };
   std::map<std::tuple<int, int, int, int, int>, GraphRec> graphs;
   cudaEvent_t marks[64] = {};
+  cudaEvent_t done_ev = nullptr;  // blocking-sync event of stream_wait
 
   LevelT& L(int level) { return lev[level + kMaxDepth]; }
   const LevelT& L(int level) const { return lev[level + kMaxDepth]; }
@@ -149,6 +150,8 @@ using GraphKey = std::tuple<int, int, int, int, int>;
 // capture what `body` enqueues as a CUDA graph (once per key) and replay it
 int capture_graph(Hier& H, const GraphKey& key, const std::function<int()>& body, Hier::GraphRec** out);
 int replay(Hier& H, Hier::GraphRec* g);
+// wait for the hierarchy's stream (spinning, or sleeping with blocking waits)
+int stream_wait(Hier& H);
 
 }  // namespace bsamg
 
@@ -160,6 +163,7 @@ struct bsamg_ctx {
   // stream-ordered pool; it keeps freed memory (release threshold = max), so
   // creating and destroying hierarchies neither maps nor unmaps memory
   cudaMemPool_t mempool = nullptr;
+  bool blocking_wait = false;  // host waits sleep on an event instead of spinning
   std::mutex mu;
   double* pinned = nullptr;     // pinned read-back words, one slot per hierarchy
   std::vector<int> free_slots;

@@ -923,8 +923,7 @@ int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcyc
   int r = mx_norm(H, finest, errortype);
   if (r) return r;
   if ((r = to_host(H))) return r;
-  cudaError_t ce = cudaStreamSynchronize(H.s);
-  if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize");
+  if (int rw = stream_wait(H)) return rw;
   double r_sync = H.h_norm[0];  // FP64 residual the current g was taken from
   if ((r = mx_prepare_tail(H, finest, minlevel, nsmooth))) return r;
   Hier::GraphRec *ga = nullptr, *gt = nullptr, *gv = nullptr;

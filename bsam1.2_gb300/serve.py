@@ -264,11 +264,11 @@ def poisson_stream(rate, duration, seed, mode="mixed", max_requests=None):
                            mode=mode))
 
 
-def serve(ctx, requests, slots=4, stats=None):
+def serve(ctx, requests, slots=4, stats=None, tail_cells=16384):
     """Replay `requests` in real time against a Server; returns the finished
     requests and the wall time from the first arrival to the last completion
     (`stats`, if a dict, receives the number of admissions that waited)."""
-    srv = Server(ctx, slots=slots)
+    srv = Server(ctx, slots=slots, tail_cells=tail_cells)
     t0 = time.perf_counter()
     for r in requests:
         now = time.perf_counter() - t0

@@ -88,6 +88,11 @@ int bsamg_init(int device, size_t hbm_budget_bytes, bsamg_ctx** out);
 int bsamg_finalize(bsamg_ctx* ctx);
 /* bytes currently allocated by hierarchies of this context */
 int bsamg_ctx_usage(const bsamg_ctx* ctx, size_t* used, size_t* budget);
+/* Host waits of the context's hierarchies (the per-V-cycle convergence
+ * read-back, put/get) sleep on a blocking-sync event instead of spinning
+ * (on != 0).  For many host threads sharing the GPU (serving); a single run
+ * keeps the default spin, which wakes sooner. */
+int bsamg_ctx_set_blocking_wait(bsamg_ctx* ctx, int on);
 
 /* Hierarchy.  params: [0]=dt [1]=eps, then for BIOGROWTH [2]=gamma
  * [3]=lambda [4]=czero.  qpo: nrvars quasi-periodic offsets (nodeinfodef
