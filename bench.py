@@ -56,12 +56,11 @@ AMR_WORKLOADS = {
                           "Berger-Rigoutsos, <= 64 cells per side, regrid every step), circle r=0.25 + 1% "
                           "noise, eps=0.01, dt=1e-3, V(2,2), resid<=1e-9"),
     # cfg4: the three-variable growth plugin (phi, nutrient, pressure) on a
-    # 32^3 root with two refinement levels; the mixed path's correction
-    # smoother is the CH one, so this workload runs the FP64 path only
+    # 32^3 root with two refinement levels, mixed and FP64 paths
     "growth3d-amr": dict(ndims=3, n=32, minlevel=-4, mthbc=[10] * 6, problem="growth", nrvars=3,
                          params=[0.01, 0.025, 1.5, 2.0, 0.5, 1.0], eps=0.025, dt=0.01, tol=1e-8, maxlevel=2,
                          tagging="gradient", qtol=0.25, ibuffer=1, mgp=4, fill=0.9, maxside=64, radius=0.1,
-                         noise=0.02, seed=20240503, modes=("fp64",), init="sphere",
+                         noise=0.02, seed=20240503, init="sphere",
                          desc="3D growth (phi, nutrient, pressure; no reference counterpart): 32^3 root + 2 levels "
                               "(|grad phi| h > 0.25, regrid every step), sphere r = 0.1 + 0.02 U(-1,1), "
                               "eps=0.025, dt=0.01, gamma=1.5, lambda=2, c0=0.5, cpress=1, V(2,2), resid<=1e-8"),

@@ -101,6 +101,8 @@ def lib():
         "bsamg_field_size": ([P, I, I], SZ),
         "bsamg_put_field": ([P, I, I, DP, SZ], I),
         "bsamg_get_field": ([P, I, I, DP, SZ], I),
+        "bsamg_put_field_section": ([P, I, I, DP, IP, IP], I),
+        "bsamg_get_field_section": ([P, I, I, DP, IP, IP], I),
         "bsamg_relax_level_color": ([P, I, I], I),
         "bsamg_set_ghost": ([P, I, I], I),
         "bsamg_level_relax": ([P, I, I], I),
@@ -272,6 +274,22 @@ class Hierarchy:
         """The seeded spinodal start of patch pid, generated on the device
         (bsamg_seed_spinodal; the same values as initial.ch_spinodal)."""
         _ck(lib().bsamg_seed_spinodal(self.h, pid, seed, mean, amp), "bsamg_seed_spinodal")
+
+    def put_section(self, pid, field, lo, hi, arr):
+        """Write the box section lo..hi (Fortran bounds, variable last) of a
+        field from arr (bsamg_put_field_section)."""
+        a = np.ascontiguousarray(np.asarray(arr, dtype=np.float64).ravel(order="F"))
+        _ck(lib().bsamg_put_field_section(self.h, pid, FIELD[field], a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                          _ia(lo, 4), _ia(hi, 4)), "bsamg_put_field_section")
+
+    def get_section(self, pid, field, lo, hi):
+        """The box section lo..hi of a field, Fortran-ordered with shape
+        hi - lo + 1 (bsamg_get_field_section)."""
+        shape = tuple(int(h) - int(l) + 1 for l, h in zip(lo, hi))
+        a = np.empty(int(np.prod(shape)), dtype=np.float64)
+        _ck(lib().bsamg_get_field_section(self.h, pid, FIELD[field], a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                          _ia(lo, 4), _ia(hi, 4)), "bsamg_get_field_section")
+        return a.reshape(shape, order="F")
 
     def commit(self):
         _ck(lib().bsamg_commit(self.h), "bsamg_commit")

@@ -925,6 +925,60 @@ int bsamg_put_field(bsamg_hier* h, int id, int field, const double* a, size_t n)
   return stream_wait(*h);
 }
 
+// A box section lo..hi (Fortran indices of the field, variable last) of a
+// patch field to or from a host array holding exactly that section in
+// Fortran order: one strided 3D copy per variable.
+int section_copy(Hier& H, int id, int field, double* a, const int lo[4], const int hi[4], bool to_device) {
+  if (!H.committed || !a || !lo || !hi) return BSAMG_ERR_ARG;
+  HostPatch* P = find(H, id);
+  if (!P) return BSAMG_ERR_NOT_FOUND;
+  size_t nn;
+  double* d = field_ptr(H, *P, field, &nn);
+  if (!d) return BSAMG_ERR_ARG;
+  bool ghosted = field == BSAMG_FIELD_Q || field == BSAMG_FIELD_QOLD || field == BSAMG_FIELD_QC;
+  const int* ext = field == BSAMG_FIELD_QC ? P->cn : (ghosted ? P->qn : P->mx);
+  int low[3];  // Fortran lower bound of each dimension
+  for (int k = 0; k < 3; k++) low[k] = (k < H.ndims && ghosted) ? 1 - H.mbc : 1;
+  size_t plane = (size_t)ext[0] * ext[1] * ext[2];
+  for (int k = 0; k < 3; k++)
+    if (lo[k] < low[k] || hi[k] < lo[k] || hi[k] > low[k] + ext[k] - 1) return BSAMG_ERR_ARG;
+  if (lo[3] < 1 || hi[3] < lo[3] || hi[3] > H.nrvars) return BSAMG_ERR_ARG;
+  size_t sx = (size_t)(hi[0] - lo[0] + 1), sy = (size_t)(hi[1] - lo[1] + 1), sz = (size_t)(hi[2] - lo[2] + 1);
+  RET(set_device(H));
+  for (int v = lo[3]; v <= hi[3]; v++) {
+    double* hv = a + (size_t)(v - lo[3]) * sx * sy * sz;
+    double* dv = d + (size_t)(v - 1) * plane;
+    cudaMemcpy3DParms m = {};
+    cudaPitchedPtr hp = make_cudaPitchedPtr(hv, sx * sizeof(double), sx, sy);
+    cudaPitchedPtr dp = make_cudaPitchedPtr(dv, (size_t)ext[0] * sizeof(double), ext[0], ext[1]);
+    cudaPos dpos = make_cudaPos((size_t)(lo[0] - low[0]) * sizeof(double), lo[1] - low[1], lo[2] - low[2]);
+    if (to_device) {
+      m.srcPtr = hp;
+      m.dstPtr = dp;
+      m.dstPos = dpos;
+      m.kind = cudaMemcpyHostToDevice;
+    } else {
+      m.srcPtr = dp;
+      m.srcPos = dpos;
+      m.dstPtr = hp;
+      m.kind = cudaMemcpyDeviceToHost;
+    }
+    m.extent = make_cudaExtent(sx * sizeof(double), sy, sz);
+    CK(cudaMemcpy3DAsync(&m, H.s));
+  }
+  return stream_wait(H);
+}
+
+int bsamg_put_field_section(bsamg_hier* h, int id, int field, const double* a, const int lo[4], const int hi[4]) {
+  if (!h) return BSAMG_ERR_ARG;
+  return section_copy(*h, id, field, const_cast<double*>(a), lo, hi, true);
+}
+
+int bsamg_get_field_section(bsamg_hier* h, int id, int field, double* a, const int lo[4], const int hi[4]) {
+  if (!h) return BSAMG_ERR_ARG;
+  return section_copy(*h, id, field, a, lo, hi, false);
+}
+
 int bsamg_get_field(bsamg_hier* h, int id, int field, double* a, size_t n) {
   if (!h || !h->committed || !a) return BSAMG_ERR_ARG;
   HostPatch* P = find(*h, id);

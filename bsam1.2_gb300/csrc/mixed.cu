@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_prolong(const PatchDev* __restric
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_update(const PatchDev* __restrict__ P, double* __restrict__ pool,
                                                       float* __restrict__ fpool, const Blk* __restrict__ blk,
-                                                      int nrvars) {
+                                                      int nrvars, int nbase) {
   const Blk b = blk[blockIdx.x];
   const PatchDev& p = P[b.patch];
   int i, j, k;
@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_update(const PatchDev* __restrict
     double nq = pool[p.oq + v * p.sq + c] + (double)fpool[p.eq + v * p.sq + c];
     pool[p.oq + v * p.sq + c] = nq;
     fpool[p.eq + v * p.sq + c] = 0.0f;
-    if (v == 0 && interior) fpool[p.ephi + iofs<DIM>(p.mx, i, j, k)] = (float)nq;
+    if (v < nbase && interior) fpool[p.ephi + v * p.sf + iofs<DIM>(p.mx, i, j, k)] = (float)nq;
   }
 }
 
@@ -484,6 +484,190 @@ __global__ void __launch_bounds__(kBlock) k_mx_track(const PatchDev* __restrict_
   }
 }
 
+// ---------------------------------------------------------------------------
+// The growth plugin (three variables phi, n, p; see fp64.cu) in correction
+// form.  Base planes at ephi (sf each): phib, nb (the frozen phi and n),
+// G = gamma (phi_old + 1)/2 and U = lambda (phi_old + 1)/2.  With
+// w = phib + e_phi:
+//   M0 = e_phi - c0 ULap(e_phi) + dt e_phi (3 phib w + e_phi^2) - dt G e_n
+//   M1 = -c1 ULap(e_n) + U e_n
+//   M2 = -c1 ULap(e_p) - cp (phib e_n + e_phi nb + e_phi e_n)
+// and the smoother is the FP64 one (phi from its lagged equation with the
+// current n, then n, then p from the new phi and n) rewritten for e so that
+// no term cancels: e_phi = (g0 + dt G e_n + c0 sum(e_phi) - dt phib e_phi
+// (2 phib + e_phi)) / (c2 + dt w^2), e_n = (g1 + c1 sum(e_n)) / (c3 + U),
+// e_p = (g2 + c1 sum(e_p) + cp (phib e_n + e_phi nb + e_phi e_n)) / c3.
+
+template <int DIM>
+__device__ __forceinline__ void mop_growth(const float* e, long long c, const Nbr<DIM>& n, long long ps,
+                                           const float* base, long long fc, long long sf, float c0, float c1,
+                                           float dt, float cp, float* m) {
+  const float* e0 = e;
+  const float* e1 = e + ps;
+  const float* e2 = e + 2 * ps;
+  float pb = base[fc], nb = base[sf + fc], G = base[2 * sf + fc], U = base[3 * sf + fc];
+  float x = e0[c], y = e1[c];
+  m[0] = x - c0 * ulapn<DIM>(e0, c, n) + dt * x * (3.0f * pb * (pb + x) + x * x) - dt * G * y;
+  m[1] = -c1 * ulapn<DIM>(e1, c, n) + U * y;
+  m[2] = -c1 * ulapn<DIM>(e2, c, n) - cp * (pb * y + x * nb + x * y);
+}
+
+// step 1 for growth: base planes; g as in k_mx_prep (mode 0: base only,
+// 1: from the stored rf, 2: f - N(qbar) with the FP64 growth operator)
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_mg_prep(const PatchDev* __restrict__ P, const double* __restrict__ pool,
+                                                    float* __restrict__ fpool, const Blk* __restrict__ blk, int mode,
+                                                    ProbParams pp) {
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  if (!interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) return;
+  long long c = gofs<DIM>(p.qn, i, j, k);
+  long long fc = iofs<DIM>(p.mx, i, j, k);
+  const double* q0 = pool + p.oq;
+  const double* q1 = q0 + p.sq;
+  const double* q2 = q1 + p.sq;
+  double ol = pool[p.oqold + c];
+  double G = pp.gamma * 0.5 * (ol + 1.0), U = pp.lambda * 0.5 * (ol + 1.0);
+  float* base = fpool + p.ephi;
+  base[fc] = (float)q0[c];
+  base[p.sf + fc] = (float)q1[c];
+  base[2 * p.sf + fc] = (float)G;
+  base[3 * p.sf + fc] = (float)U;
+  if (mode == 0) return;
+  double r[3];
+  if (mode == 1) {
+    for (int v = 0; v < 3; v++) r[v] = pool[p.orf + v * p.sf + fc];
+  } else {
+    long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
+    double phi = q0[c];
+    double o0 = phi - p.c[0] * ulap<DIM>(q0, c, sy, sz) + pp.dt * phi * phi * phi - pp.dt * G * (q1[c] - pp.czero);
+    double o1 = -p.c[1] * ulap<DIM>(q1, c, sy, sz) + U * q1[c];
+    double o2 = -p.c[1] * ulap<DIM>(q2, c, sy, sz) - pp.cpress * phi * q1[c];
+    r[0] = pool[p.of + fc] - o0;
+    r[1] = pool[p.of + p.sf + fc] - o1;
+    r[2] = pool[p.of + 2 * p.sf + fc] - o2;
+  }
+  for (int v = 0; v < 3; v++) fpool[p.eg + v * p.sf + fc] = (float)r[v];
+}
+
+template <int DIM>
+__device__ __forceinline__ void u_mg_relax(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
+                                           int tid, int ipass, float dt, float cp) {
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  if (!color_cell<DIM>(p, b.start + tid, ipass, i, j, k)) return;
+  float* e0 = fpool + p.eq;
+  float* e1 = e0 + p.sq;
+  float* e2 = e1 + p.sq;
+  long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
+  long long c = gofs<DIM>(p.qn, i, j, k);
+  long long fc = iofs<DIM>(p.mx, i, j, k);
+  Nbr<DIM> n(c, sy, sz);
+  const float* base = fpool + p.ephi;
+  const float* g = fpool + p.eg;
+  float pb = base[fc], nb = base[p.sf + fc], G = base[2 * p.sf + fc], U = base[3 * p.sf + fc];
+  float c0 = p.cf[0], c1 = p.cf[1], c2 = p.cf[2], c3 = p.cf[3];
+  float s0 = e0[n.xm] + e0[n.xp] + e0[n.ym] + e0[n.yp];
+  float s1 = e1[n.xm] + e1[n.xp] + e1[n.ym] + e1[n.yp];
+  float s2 = e2[n.xm] + e2[n.xp] + e2[n.ym] + e2[n.yp];
+  if (DIM == 3) {
+    s0 += e0[n.zm] + e0[n.zp];
+    s1 += e1[n.zm] + e1[n.zp];
+    s2 += e2[n.zm] + e2[n.zp];
+  }
+  float x = e0[c], y = e1[c];
+  float w = pb + x;
+  float xn = (g[fc] + dt * G * y + c0 * s0 - dt * pb * x * (2.0f * pb + x)) / (c2 + dt * w * w);
+  float yn = (g[p.sf + fc] + c1 * s1) / (c3 + U);
+  float zn = (g[2 * p.sf + fc] + c1 * s2 + cp * (pb * yn + xn * nb + xn * yn)) / c3;
+  e0[c] = xn;
+  e1[c] = yn;
+  e2[c] = zn;
+}
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_mg_relax(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                     const Blk* __restrict__ blk, int ipass, float dt, float cp) {
+  u_mg_relax<DIM>(P, fpool, blk[blockIdx.x], threadIdx.x, ipass, dt, cp);
+}
+
+// CoarseLoadingFunction on the growth correction (see u_coarse_load)
+template <int DIM>
+__device__ __forceinline__ void u_mg_coarse_load(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                 const Blk b, int tid, float dt, float cp) {
+  const PatchDev& p = P[b.patch];
+  int ci, cj, ck;
+  if (!interior_cell<DIM>(p.cmx, b.start + tid, ci, cj, ck)) return;
+  const PatchDev& par = P[p.parent];
+  const float* e = fpool + p.eq;
+  long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
+  float R[3] = {0.f, 0.f, 0.f};
+  const int nk = DIM == 3 ? 2 : 1;
+  for (int dk = 0; dk < nk; dk++)
+    for (int dj = 0; dj < 2; dj++)
+      for (int di = 0; di < 2; di++) {
+        int i = 2 * ci - di, j = 2 * cj - dj, k = DIM == 3 ? 2 * ck - dk : 1;
+        long long c = gofs<DIM>(p.qn, i, j, k);
+        long long fc = iofs<DIM>(p.mx, i, j, k);
+        Nbr<DIM> n(c, sy, sz);
+        float m[3];
+        mop_growth<DIM>(e, c, n, p.sq, fpool + p.ephi, fc, p.sf, p.cf[0], p.cf[1], dt, cp, m);
+        for (int v = 0; v < 3; v++) R[v] += fpool[p.eg + v * p.sf + fc] - m[v];
+      }
+  const float rs = DIM == 2 ? 0.25f : 0.125f;
+  const float* ec = fpool + p.ecq;
+  long long csy = p.cn[0], csz = (long long)p.cn[0] * p.cn[1];
+  long long cc = gofs<DIM>(p.cn, ci, cj, ck);
+  long long pf = iofs<DIM>(par.mx, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 1);
+  Nbr<DIM> n(cc, csy, csz);
+  float m[3];
+  mop_growth<DIM>(ec, cc, n, p.sc, fpool + par.ephi, pf, par.sf, par.cf[0], par.cf[1], dt, cp, m);
+  for (int v = 0; v < 3; v++) fpool[par.eg + v * par.sf + pf] = R[v] * rs + m[v];
+}
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_mg_coarse_load(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                           const Blk* __restrict__ blk, float dt, float cp) {
+  u_mg_coarse_load<DIM>(P, fpool, blk[blockIdx.x], threadIdx.x, dt, cp);
+}
+
+// tracked residual g <- g - M(e) of the growth correction; per-block sums of
+// squares of the three variables
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_mg_track(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                     const Blk* __restrict__ blk, double* __restrict__ partial,
+                                                     float dt, float cp) {
+  __shared__ float red[3][kBlock / 32];
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  float s[3] = {0.f, 0.f, 0.f};
+  if (interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) {
+    long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
+    long long c = gofs<DIM>(p.qn, i, j, k);
+    long long fc = iofs<DIM>(p.mx, i, j, k);
+    Nbr<DIM> n(c, sy, sz);
+    float m[3];
+    mop_growth<DIM>(fpool + p.eq, c, n, p.sq, fpool + p.ephi, fc, p.sf, p.cf[0], p.cf[1], dt, cp, m);
+    for (int v = 0; v < 3; v++) {
+      float gv = fpool[p.eg + v * p.sf + fc] - m[v];
+      fpool[p.eg + v * p.sf + fc] = gv;
+      s[v] = gv * gv;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1)
+    for (int v = 0; v < 3; v++) s[v] += __shfl_down_sync(0xffffffffu, s[v], o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0)
+    for (int v = 0; v < 3; v++) red[v][w] = s[v];
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int v = 0; v < 3; v++) {
+      float t = 0.f;
+      for (int m = 0; m < kBlock / 32; m++) t += red[v][m];
+      partial[3 * blockIdx.x + v] = (double)t;
+    }
+}
+
 // ghost programs on e: homogeneous boundary conditions
 __device__ __forceinline__ void ghost32_apply(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                               const GhostOp& g, int nrvars) {
@@ -539,9 +723,10 @@ __global__ void __launch_bounds__(kBlock) k_ghost32_program(const PatchDev* __re
 // units), with a barrier between phases.  Each unit computes exactly what
 // the stand-alone kernel computes, so results are bit-identical.
 
-template <int DIM>
+template <int DIM, int PR>
 __global__ void __launch_bounds__(kBlock) k_mx_tail(const PatchDev* __restrict__ P, float* __restrict__ fpool,
-                                                   const TailPhase* __restrict__ ph, int nph, int nrvars) {
+                                                   const TailPhase* __restrict__ ph, int nph, int nrvars, float dt,
+                                                   float cp) {
   for (int x = 0; x < nph; x++) {
     const TailPhase f = ph[x];
     if (f.op == kTGhost) {
@@ -557,10 +742,16 @@ __global__ void __launch_bounds__(kBlock) k_mx_tail(const PatchDev* __restrict__
     for (int b = 0; b < f.nblk; b++) {
       const Blk bb = f.blk[b];
       switch (f.op) {
-        case kTRelax: u_relax<DIM>(P, fpool, bb, threadIdx.x, f.arg); break;
+        case kTRelax:
+          if (PR == kGrowth) u_mg_relax<DIM>(P, fpool, bb, threadIdx.x, f.arg, dt, cp);
+          else u_relax<DIM>(P, fpool, bb, threadIdx.x, f.arg);
+          break;
         case kTRestrict: u_restrict<DIM>(P, fpool, bb, threadIdx.x, nrvars); break;
         case kTRing: u_coarse_ring<DIM>(P, fpool, bb, threadIdx.x, nrvars, f.arg); break;
-        case kTLoad: u_coarse_load<DIM>(P, fpool, bb, threadIdx.x); break;
+        case kTLoad:
+          if (PR == kGrowth) u_mg_coarse_load<DIM>(P, fpool, bb, threadIdx.x, dt, cp);
+          else u_coarse_load<DIM>(P, fpool, bb, threadIdx.x);
+          break;
         default: u_prolong<DIM>(P, fpool, bb, threadIdx.x, nrvars); break;
       }
     }
@@ -620,10 +811,20 @@ int mx_op(Hier& H, int level, int kind, int op, int arg) {
     return BSAMG_OK;
   }
   switch (op) {
-    case kTRelax: MX_LAUNCH_W(H, kind, k_mx_relax, H.dP, H.fpool, L.d_blk[kind], arg); break;
+    case kTRelax:
+      if (H.problem == kGrowth)
+        MX_LAUNCH_W(H, kind, k_mg_relax, H.dP, H.fpool, L.d_blk[kind], arg, (float)H.pp.dt, (float)H.pp.cpress);
+      else
+        MX_LAUNCH_W(H, kind, k_mx_relax, H.dP, H.fpool, L.d_blk[kind], arg);
+      break;
     case kTRestrict: MX_LAUNCH(H, kind, k_mx_restrict, H.dP, H.fpool, L.d_blk[kind], H.nrvars); break;
     case kTRing: MX_LAUNCH_W(H, kind, k_mx_coarse_ring, H.dP, H.fpool, L.d_blk[kind], H.nrvars, arg); break;
-    case kTLoad: MX_LAUNCH_W(H, kind, k_mx_coarse_load, H.dP, H.fpool, L.d_blk[kind]); break;
+    case kTLoad:
+      if (H.problem == kGrowth)
+        MX_LAUNCH_W(H, kind, k_mg_coarse_load, H.dP, H.fpool, L.d_blk[kind], (float)H.pp.dt, (float)H.pp.cpress);
+      else
+        MX_LAUNCH_W(H, kind, k_mx_coarse_load, H.dP, H.fpool, L.d_blk[kind]);
+      break;
     default: MX_LAUNCH_W(H, kind, k_mx_prolong, H.dP, H.fpool, L.d_blk[kind], H.nrvars); break;
   }
   return BSAMG_OK;
@@ -644,8 +845,15 @@ int mx_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
     auto it = H.mx_tail_progs.find(std::make_tuple(level, minlevel, nsmooth));
     if (it != H.mx_tail_progs.end()) {  // the whole V-cycle from here down in one CTA
       const TailPhase* ph = static_cast<const TailPhase*>(it->second.first);
-      if (H.ndims == 2) k_mx_tail<2><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, it->second.second, H.nrvars);
-      else k_mx_tail<3><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, it->second.second, H.nrvars);
+      float dt = (float)H.pp.dt, cp = (float)H.pp.cpress;
+      int n = it->second.second;
+      if (H.problem == kGrowth) {
+        if (H.ndims == 2) k_mx_tail<2, kGrowth><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, H.nrvars, dt, cp);
+        else k_mx_tail<3, kGrowth><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, H.nrvars, dt, cp);
+      } else {
+        if (H.ndims == 2) k_mx_tail<2, kCH><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, H.nrvars, dt, cp);
+        else k_mx_tail<3, kCH><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, H.nrvars, dt, cp);
+      }
       return after_launch(H, 1);
     }
   }
@@ -707,13 +915,21 @@ std::vector<long long> layout(const Hier& H, size_t* total, size_t* e_len, size_
   *e_len = (size_t)o;
   for (size_t p = 0; p < np; p++) { off[4 * p + 1] = o; o = al(o + H.patches[p].sc * H.nrvars); }
   for (size_t p = 0; p < np; p++) { off[4 * p + 2] = o; o = al(o + H.patches[p].sf * H.nrvars); }
-  for (size_t p = 0; p < np; p++) { off[4 * p + 3] = o; o = al(o + H.patches[p].sf); }
+  // base fields: phib (CH); phib, nb, G, U (growth)
+  long long nbase = H.problem == kGrowth ? 4 : 1;
+  for (size_t p = 0; p < np; p++) { off[4 * p + 3] = o; o = al(o + nbase * H.patches[p].sf); }
   *total = (size_t)o;
   return off;
 }
 
 int mx_norm(Hier& H, int level, int errortype) {
   LevelT& L = H.L(level);
+  if (H.problem == kGrowth) {  // the plain path's FP64 residual (three variables)
+    int r = after_launch(H, launch_norm_partial(H.lc(), L.d_blk[kKindInterior], L.nblk[kKindInterior], H.d_partial, 1));
+    if (r) return r;
+    return after_launch(H, launch_norm_finish(H.s, H.d_partial, L.nblk[kKindInterior], H.nrvars, L.count, errortype,
+                                              H.d_norm, H.d_nonfinite));
+  }
   int nb = (L.nblk[kKindInterior] + kNormCells - 1) / kNormCells;
   if (nb <= 0) return BSAMG_OK;
   // the interior list is padded with patch = -1 entries to a multiple of
@@ -755,15 +971,20 @@ int mx_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype, 
     // from the FP64 rf after a resync, else from the tracked update
     if (level == finest && !resync) continue;
     int mode = level < 0 ? 0 : (level == finest ? 1 : 2);
-    if (level < 0 && minlevel == H.minlevel && H.mx_prep_coarse_n > 0) {
-      // every level below the root at once (phib only)
-      int nb = H.mx_prep_coarse_n;
-      if (H.ndims == 2) k_mx_prep<2><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.fpool, H.mx_prep_coarse, 0);
-      else k_mx_prep<3><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.fpool, H.mx_prep_coarse, 0);
+    bool all_coarse = level < 0 && minlevel == H.minlevel && H.mx_prep_coarse_n > 0;
+    const Blk* blk = all_coarse ? H.mx_prep_coarse : L.d_blk[kKindInterior];
+    int nb = all_coarse ? H.mx_prep_coarse_n : L.nblk[kKindInterior];
+    if (nb > 0) {  // all levels below the root at once (base fields only)
+      if (H.problem == kGrowth) {
+        if (H.ndims == 2) k_mg_prep<2><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.fpool, blk, mode, H.pp);
+        else k_mg_prep<3><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.fpool, blk, mode, H.pp);
+      } else {
+        if (H.ndims == 2) k_mx_prep<2><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.fpool, blk, mode);
+        else k_mx_prep<3><<<nb, kBlock, 0, H.s>>>(H.dP, H.pool, H.fpool, blk, mode);
+      }
       if ((r__ = after_launch(H, 1))) return r__;
-      break;
     }
-    MX_LAUNCH(H, kKindInterior, k_mx_prep, H.dP, H.pool, H.fpool, L.d_blk[kKindInterior], mode);
+    if (all_coarse) break;
   }
   int r = mx_vcycle(H, finest, minlevel, nsmooth);
   if (r) return r;
@@ -771,14 +992,19 @@ int mx_iteration(Hier& H, int finest, int minlevel, int nsmooth, int errortype, 
   // before the update pass replaces phib with the new base
   {
     LevelT& L = H.L(finest);
-    MX_LAUNCH_W(H, kKindInterior, k_mx_track, H.dP, H.fpool, L.d_blk[kKindInterior], H.d_partial);
+    if (H.problem == kGrowth)
+      MX_LAUNCH_W(H, kKindInterior, k_mg_track, H.dP, H.fpool, L.d_blk[kKindInterior], H.d_partial,
+                  (float)H.pp.dt, (float)H.pp.cpress);
+    else
+      MX_LAUNCH_W(H, kKindInterior, k_mx_track, H.dP, H.fpool, L.d_blk[kKindInterior], H.d_partial);
     if ((r = after_launch(H, launch_norm_finish(H.s, H.d_partial, L.nblk[kKindInterior], H.nrvars, L.count,
                                                  errortype, H.d_norm, H.d_nonfinite))))
       return r;
   }
   for (int level = finest; level >= 0; level--) {
     LevelT& L = H.L(level);
-    MX_LAUNCH_W(H, kKindFGhost, k_mx_update, H.dP, H.pool, H.fpool, L.d_blk[kKindFGhost], H.nrvars);
+    MX_LAUNCH_W(H, kKindFGhost, k_mx_update, H.dP, H.pool, H.fpool, L.d_blk[kKindFGhost], H.nrvars,
+                H.problem == kGrowth ? 2 : 1);
   }
   if ((r = mx_fill_down_q(H, finest, minlevel))) return r;
   // refinement levels: ghosts from the updated FP64 state (coarse-fine
@@ -797,14 +1023,14 @@ int mx_verify(Hier& H, int finest, int errortype) {
 }  // namespace
 
 size_t mixed_pool_bytes(const Hier& H) {
-  if (H.problem != kCH) return 0;
+  if (H.problem != kCH && H.problem != kGrowth) return 0;
   size_t n, ne, ec;
   layout(H, &n, &ne, &ec);
   return n * sizeof(float);
 }
 
 int mixed_alloc(Hier& H) {
-  if (H.problem != kCH) return BSAMG_OK;
+  if (H.problem != kCH && H.problem != kGrowth) return BSAMG_OK;
   if (H.box) {
     H.fpool_elems = box_layout(H);
     cudaError_t e = dev_alloc(H, (void**)&H.fpool, H.fpool_elems * sizeof(float));
@@ -848,7 +1074,7 @@ void mixed_free(Hier& H) {
 }
 
 int mixed_tables(Hier& H) {
-  if (H.problem != kCH || !H.fpool || H.box) return BSAMG_OK;
+  if ((H.problem != kCH && H.problem != kGrowth) || !H.fpool || H.box) return BSAMG_OK;
   for (int l = H.minlevel; l <= H.maxlevel; l++) {
     // interior work list padded with patch = -1 to a multiple of kNormCells
     std::vector<Blk> v;
@@ -908,16 +1134,14 @@ void set_tail(Hier& H, long long cells) {
 }
 
 int mixed_enq_relax(Hier& H, int level, int ipass) {
-  if (H.problem != kCH || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
+  if ((H.problem != kCH && H.problem != kGrowth) || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
   if (H.box) return box_enq_relax(H, level, ipass);
-  LevelT& L = H.L(level);
-  MX_LAUNCH_W(H, kKindColor, k_mx_relax, H.dP, H.fpool, L.d_blk[kKindColor], ipass);
-  return BSAMG_OK;
+  return mx_op(H, level, kKindColor, kTRelax, ipass);
 }
 
 int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,
                      int strict, int* ncycles, double* residuals) {
-  if (H.problem != kCH || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
+  if ((H.problem != kCH && H.problem != kGrowth) || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
   // the first outer iteration takes its right-hand side from the FP64
   // residual of the finest level
   int r = mx_norm(H, finest, errortype);

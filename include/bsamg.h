@@ -167,6 +167,14 @@ size_t bsamg_field_size(const bsamg_hier* h, int id, int field);
 int bsamg_put_field(bsamg_hier* h, int id, int field, const double* a,
                     size_t n);
 int bsamg_get_field(bsamg_hier* h, int id, int field, double* a, size_t n);
+/* The same for a box section of a field: lo[0..3], hi[0..3] are Fortran
+ * bounds in the field's own index space (q, qold: 1-mbc..mx+mbc; qc:
+ * 1-mbc..cmx+mbc; f, rf, ftmp: 1..mx; the unused dimension of a 2D patch
+ * 1..1; the variable 1..nrvars last), and `a` holds exactly the section in
+ * Fortran order, as the reference passes array sections such as
+ * info%q(1:mx(1),1:mx(2),1,1:nrvars). */
+int bsamg_put_field_section(bsamg_hier* h, int id, int field, const double* a, const int lo[4], const int hi[4]);
+int bsamg_get_field_section(bsamg_hier* h, int id, int field, double* a, const int lo[4], const int hi[4]);
 
 /* single operations, FP64 */
 int bsamg_relax_level_color(bsamg_hier* h, int level, int ipass);

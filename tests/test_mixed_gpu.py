@@ -90,3 +90,46 @@ def test_coarse_tail_in_one_block_is_bit_identical(pkg, ctx, nd, n, levels, mode
     for pid in qa:
         assert np.array_equal(qa[pid], qb[pid]), pid
     assert la < lb, (la, lb)
+
+
+def _growth_pair(pkg, ctx, amr):
+    """Two identical growth hierarchies (16^3 root, Dirichlet/reflecting
+    faces), regridded to two levels around the seed when amr."""
+    params = [0.01, 0.025, 1.5, 2.0, 0.5, 1.0]
+    fn = pkg.initial.growth_sphere(0.025, seed=5, radius=0.25)
+    out = []
+    for _ in range(2):
+        h = pkg.Hierarchy(ctx, 3, 3, "growth", params)
+        h.build_uniform([16, 16, 16], -3, [10] * 6, [0, 0, 0], [1, 1, 1])
+        h.commit()
+        h.put(0, "q", fn(0, [16] * 3, [1 / 16] * 3, [0.0] * 3))
+        if amr:
+            h = h.regrid(pkg.regrid_params(2, tagging="gradient", initial=True, qtolerance=0.25), fn)
+        out.append(h)
+    return out
+
+
+@pytest.mark.parametrize("amr", [False, True])
+def test_mixed_growth_reaches_the_fp64_solution(pkg, ctx, amr):
+    """The growth plugin's correction V-cycle (three variables) converges to
+    the FP64 path's discrete solution: tightly converged the iterates agree
+    to 1e-8 relative; at the configuration's tolerance to 1e-5."""
+    for tol, bound in ((1e-11, 1e-8), (1e-8, 1e-5)):
+        gm, gf = _growth_pair(pkg, ctx, amr)
+        tab = gm.patch_table()
+        fin = max(p["level"] for p in tab)
+        for step in range(3):
+            nm, rm = gm.time_step(step == 0, fin, -3, tol=tol, maxvcycles=40, mode="mixed", strict=True)
+            nf, rf = gf.time_step(step == 0, fin, -3, tol=tol, maxvcycles=40, mode="fp64")
+            assert rm[-1] < tol and nm <= nf + 3, (step, nm, nf, rm, rf)
+        worst = 0.0
+        for p in tab:
+            if p["level"] < 0:
+                continue
+            a, b = gm.get(p["id"], "q"), gf.get(p["id"], "q")
+            n = a.size // 3
+            for v in range(3):
+                scale = max(np.max(np.abs(b[v * n:(v + 1) * n])), 1e-30)
+                worst = max(worst, float(np.max(np.abs(a[v * n:(v + 1) * n] - b[v * n:(v + 1) * n])) / scale))
+        print(f"growth amr={amr}: max rel difference mixed vs FP64 {worst:.3e} at tol {tol:g}")
+        assert worst <= bound, (tol, worst)

@@ -178,3 +178,32 @@ def test_ch2d_128_ten_steps(pkg, ctx, oracle_mod):
         assert ng == no
     err = compare(spec, g, o, exact=False)
     print("128^2 x 10 steps: max rel diff", err)
+
+
+def test_field_sections_read_and_write_the_fortran_box(pkg, ctx):
+    """bsamg_put/get_field_section move exactly the Fortran section lo..hi of
+    a patch field (ghost layers addressed at 1-mbc, variables last)."""
+    h = pkg.Hierarchy(ctx, 3, 2, "ch", [5e-4, 0.02])
+    h.build_uniform([8, 6, 4], -1, [2] * 6, [0, 0, 0], [1, 0.75, 0.5])
+    h.commit()
+    rng = np.random.default_rng(3)
+    full = rng.standard_normal((10, 8, 6, 2))
+    h.put(0, "q", np.asfortranarray(full))
+    # q(1:8, 0:3, 2:5, 2:2): interior in x, lower ghost + 3 cells in y, variable 2
+    lo, hi = [1, 0, 2, 2], [8, 3, 5, 2]
+    sec = h.get_section(0, "q", lo, hi)
+    assert sec.shape == (8, 4, 4, 1)
+    assert np.array_equal(sec, full[1:9, 0:4, 2:6, 1:2])
+    new = rng.standard_normal(sec.shape)
+    h.put_section(0, "q", lo, hi, new)
+    want = full.copy()
+    want[1:9, 0:4, 2:6, 1:2] = new
+    got = h.get(0, "q").reshape(want.shape, order="F")
+    assert np.array_equal(got, want)
+    # f is interior-only: f(1:8, 1:6, 1:4, 1:2)
+    fsec = h.get_section(0, "f", [1, 1, 1, 1], [8, 6, 4, 2])
+    assert fsec.shape == (8, 6, 4, 2)
+    with pytest.raises(pkg.BsamgError):
+        h.get_section(0, "f", [0, 1, 1, 1], [8, 6, 4, 2])  # f has no ghost layer
+    with pytest.raises(pkg.BsamgError):
+        h.get_section(0, "q", [1, 1, 1, 1], [8, 6, 4, 3])  # nrvars = 2
