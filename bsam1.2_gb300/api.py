@@ -116,6 +116,7 @@ def lib():
         "bsamg_stream": ([P, ctypes.POINTER(P)], I),
         "bsamg_launch_count": ([P, ctypes.POINTER(ctypes.c_longlong)], I),
         "bsamg_set_tail_cells": ([P, ctypes.c_longlong], I),
+        "bsamg_graph_stats": ([P, IP, IP], I),
         "bsamg_set_params": ([P, DP, I], I),
         "bsamg_hier_reset": ([P], I),
         "bsamg_mark": ([P, I], I),
@@ -397,6 +398,12 @@ class Hierarchy:
         """Largest cumulative coarse-level size the mixed V-cycle runs inside
         one thread block (bsamg_set_tail_cells; 0 disables)."""
         _ck(lib().bsamg_set_tail_cells(self.h, cells), "bsamg_set_tail_cells")
+
+    def graph_stats(self):
+        """(graphs instantiated, graphs inherited and updated in place)."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        _ck(lib().bsamg_graph_stats(self.h, ctypes.byref(a), ctypes.byref(b)), "bsamg_graph_stats")
+        return a.value, b.value
 
     def launch_count(self):
         n = ctypes.c_longlong()

@@ -559,15 +559,15 @@ std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std:
   // arrays over the ghosted cells of the patches the operations touch.
   std::vector<Em>& ops = E.out;
   int m = (int)ops.size();
-  std::unordered_map<int, long long> base;
+  std::vector<long long> base(H.patches.size(), -1);
   long long slots = 0;
   auto slot_base = [&](int p) {
-    auto it = base.find(p);
-    if (it != base.end()) return it->second;
-    const HostPatch& P = H.patches[p];
-    long long b = slots;
-    slots += (long long)P.qn[0] * P.qn[1] * P.qn[2];
-    base[p] = b;
+    long long& b = base[p];
+    if (b < 0) {
+      const HostPatch& P = H.patches[p];
+      b = slots;
+      slots += (long long)P.qn[0] * P.qn[1] * P.qn[2];
+    }
     return b;
   };
   std::vector<long long> dkey(m), skey(2 * (size_t)m);

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -254,9 +256,32 @@ int capture_graph(Hier& H, const GraphKey& key, const std::function<int()>& body
   }
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
   Hier::GraphRec rec;
-  e = cudaGraphInstantiate(&rec.exec, g, 0);
+  // An executable graph inherited from the hierarchy this one was regridded
+  // from takes the new parameters in place when the launch sequence has the
+  // same shape (same kernels in the same order), which costs far less than
+  // instantiating a new one.
+  auto donor = H.graph_donors.find(key);
+  if (donor != H.graph_donors.end()) {
+    cudaGraphExec_t ex = donor->second.exec;
+    H.graph_donors.erase(donor);
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(ex, g, &info) == cudaSuccess) {
+      rec.exec = ex;
+      H.graphs_updated++;
+    } else {
+      cudaGetLastError();  // a failed update is not an error: instantiate instead
+      cudaGraphExecDestroy(ex);
+    }
+  }
+  if (!rec.exec) {
+    H.graphs_instantiated++;
+    e = cudaGraphInstantiate(&rec.exec, g, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return cuda_fail(e, "cudaGraphInstantiate");
+    }
+  }
   cudaGraphDestroy(g);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
   rec.nlaunch = H.capture_launches;
   H.graphs[key] = rec;
   *out = &H.graphs[key];
@@ -670,6 +695,27 @@ int commit(Hier& H) {
       const HostPatch& P = H.patches[p];
       L.count = (double)(H.nrvars * P.mx[0] * P.mx[1] * P.mx[2]) + L.count;
     }
+  }
+  // the ghost programs, compiled on host threads (they only read the tables)
+  {
+    std::vector<std::pair<int, int>> jobs;
+    for (int l = H.minlevel; l <= H.maxlevel; l++)
+      for (int ip = 0; ip < (l <= 0 ? 1 : 3); ip++) jobs.emplace_back(l, ip);
+    std::atomic<size_t> next(0);
+    auto work = [&]() {
+      for (size_t j; (j = next++) < jobs.size();) {
+        GhostProg& g = H.L(jobs[j].first).gp[jobs[j].second];
+        g.ops = compile_set_ghost(H, jobs[j].first, jobs[j].second, g.stage_off);
+      }
+    };
+    unsigned nt = std::min<unsigned>((unsigned)jobs.size(), std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nt; t++) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+  }
+  for (int l = H.minlevel; l <= H.maxlevel; l++) {
+    LevelT& L = H.L(l);
     for (int ip = 0; ip < 3; ip++) {
       // below and at the root the program does not depend on the colour
       if (l <= 0 && ip > 0) {
@@ -679,7 +725,6 @@ int commit(Hier& H) {
         L.gp[ip].d_stage_off = L.gp[0].d_stage_off;
         continue;
       }
-      L.gp[ip].ops = compile_set_ghost(H, l, ip, L.gp[ip].stage_off);
       RET(upload_ghost(H, L.gp[ip]));
     }
   }
@@ -702,8 +747,9 @@ void release(Hier& H) {
   for (int m = 0; m < 64; m++)
     if (H.marks[m]) cudaEventDestroy(H.marks[m]);
   if (H.done_ev) cudaEventDestroy(H.done_ev);
-  for (auto& kv : H.graphs)
-    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  for (auto* gm : {&H.graphs, &H.graph_donors})
+    for (auto& kv : *gm)
+      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
   H.graphs.clear();
   for (int l = 0; l < kNLev; l++) {
     LevelT& L = H.lev[l];
@@ -1079,6 +1125,13 @@ int bsamg_stream(bsamg_hier* h, void** stream) {
 int bsamg_launch_count(const bsamg_hier* h, long long* n) {
   if (!h || !n) return BSAMG_ERR_ARG;
   *n = h->launches;
+  return BSAMG_OK;
+}
+
+int bsamg_graph_stats(const bsamg_hier* h, int* instantiated, int* updated) {
+  if (!h) return BSAMG_ERR_ARG;
+  if (instantiated) *instantiated = h->graphs_instantiated;
+  if (updated) *updated = h->graphs_updated;
   return BSAMG_OK;
 }
 

@@ -111,6 +111,10 @@ struct Hier {
     long long nlaunch = 0;
   };
   std::map<std::tuple<int, int, int, int, int>, GraphRec> graphs;
+  // executable graphs of the hierarchy this one was regridded from, updated
+  // in place by capture_graph when the launch sequence keeps its shape
+  std::map<std::tuple<int, int, int, int, int>, GraphRec> graph_donors;
+  int graphs_instantiated = 0, graphs_updated = 0;
   cudaEvent_t marks[64] = {};
   cudaEvent_t done_ev = nullptr;  // blocking-sync event of stream_wait
 

@@ -1155,9 +1155,6 @@ int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcyc
   if ((r = capture_graph(H, key(11), [&] { return mx_iteration(H, finest, minlevel, nsmooth, errortype, true); },
                          &ga)))
     return r;
-  if ((r = capture_graph(H, key(12), [&] { return mx_iteration(H, finest, minlevel, nsmooth, errortype, false); },
-                         &gt)))
-    return r;
   if ((r = capture_graph(H, key(13), [&] { return mx_verify(H, finest, errortype); }, &gv))) return r;
   // With refinement levels the coarse-fine ghosts of the finest level are
   // re-interpolated from the updated parents after every cycle, which
@@ -1171,6 +1168,12 @@ int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcyc
   int it;
   double res = 0.0;
   for (it = 1; it <= maxvcycles; it++) {
+    // the tracked-residual cycle is captured when first needed (with
+    // refinement levels every cycle starts from the FP64 residual)
+    if (!resync && !gt &&
+        (r = capture_graph(H, key(12), [&] { return mx_iteration(H, finest, minlevel, nsmooth, errortype, false); },
+                           &gt)))
+      return r;
     if ((r = replay(H, resync ? ga : gt))) return r;
     if (*H.h_nonfinite) return BSAMG_ERR_NONFINITE;
     double tracked = H.h_norm[0];

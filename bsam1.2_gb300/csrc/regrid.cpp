@@ -570,7 +570,10 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
       for (size_t n = 0; n < H.patches.size(); n++)
         if (H.patches[n].level == level + 1) transfer_overlap(nv, H.patches[n], oldq[n], M.g[c], M.q[c], nd);
   }
-  if (!level_patches(level).empty() && (r = host_set_ghost(M, level))) return r;  // AMR(finest)
+  // AMR(finest) ends with SetGhost(finest, 0); nothing on the host reads its
+  // result, so it runs on the device after the upload (the compiled program
+  // gives the sequential sequence's values)
+  int final_ghost = level_patches(level).empty() ? -kMaxDepth - 1 : level;
 
   // the new hierarchy, on the same context
   bsamg_hier* nh = nullptr;
@@ -619,8 +622,13 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
                            cudaMemcpyDeviceToDevice, N.s);
     }
   if (ce != cudaSuccess) return fail(cuda_fail(ce, "cudaMemcpyAsync(regrid upload)"));
+  if (final_ghost >= 0 && (r = enq_set_ghost(N, final_ghost, 0))) return fail(r);
   ce = cudaStreamSynchronize(N.s);  // the host arrays are freed on return
   if (ce != cudaSuccess) return fail(cuda_fail(ce, "cudaStreamSynchronize(regrid upload)"));
+  // the old hierarchy's executable graphs go to the new one, which updates
+  // them in place on its first capture; the old one captures again if used
+  N.graph_donors = std::move(H.graphs);
+  H.graphs.clear();
   *out = nh;
   return BSAMG_OK;
 }

@@ -259,6 +259,9 @@ int bsamg_sync(bsamg_hier* h);
 int bsamg_stream(bsamg_hier* h, void** stream);
 /* Kernel launches issued by this hierarchy since creation. */
 int bsamg_launch_count(const bsamg_hier* h, long long* n);
+/* CUDA graphs this hierarchy instantiated, and graphs it took over from the
+ * hierarchy it was regridded from and updated in place. */
+int bsamg_graph_stats(const bsamg_hier* h, int* instantiated, int* updated);
 /* Reuse of a committed hierarchy for another run on the same mesh (no
  * reference counterpart; a serving loop keeps hierarchies of recurring
  * shapes instead of building them again).  bsamg_set_params replaces the
