@@ -661,8 +661,8 @@ __global__ void __launch_bounds__(kBlock) k_ghost_program(const PatchDev* __rest
 // barrier between phases.  Per-cell arithmetic and the order of dependent
 // updates are those of the separate kernels, so results are bit-identical.
 template <int PROB, int DIM>
-__global__ void __launch_bounds__(kBlock) k_tail(const PatchDev* __restrict__ P, double* __restrict__ pool,
-                                                 const TailPhase* __restrict__ ph, int nph, ProbParams pp) {
+__device__ __forceinline__ void run_tail(const PatchDev* __restrict__ P, double* pool, const TailPhase* __restrict__ ph,
+                                         int nph, const ProbParams& pp) {
   for (int x = 0; x < nph; x++) {
     const TailPhase f = ph[x];
     if (f.op == kTGhost) {
@@ -690,6 +690,32 @@ __global__ void __launch_bounds__(kBlock) k_tail(const PatchDev* __restrict__ P,
       }
     }
     __syncthreads();
+  }
+}
+
+template <int PROB, int DIM>
+__global__ void __launch_bounds__(kBlock) k_tail(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                 const TailPhase* __restrict__ ph, int nph, ProbParams pp) {
+  run_tail<PROB, DIM>(P, pool, ph, nph, pp);
+}
+
+// The same with the tail levels' arrays staged in shared memory (P
+// addresses them there); modified arrays are written back at the end.
+template <int PROB, int DIM>
+__global__ void __launch_bounds__(kBlock) k_tail_smem(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                      const TailPhase* __restrict__ ph, int nph, ProbParams pp,
+                                                      const StageSeg* __restrict__ segs, int nsegs) {
+  extern __shared__ double smd[];
+  for (int x = 0; x < nsegs; x++) {
+    const StageSeg sg = segs[x];
+    for (int t = threadIdx.x; t < sg.n; t += blockDim.x) smd[sg.s + t] = pool[sg.g + t];
+  }
+  __syncthreads();
+  run_tail<PROB, DIM>(P, smd, ph, nph, pp);
+  for (int x = 0; x < nsegs; x++) {
+    const StageSeg sg = segs[x];
+    if (!sg.out) continue;
+    for (int t = threadIdx.x; t < sg.n; t += blockDim.x) pool[sg.g + t] = smd[sg.s + t];
   }
 }
 
@@ -800,6 +826,39 @@ int launch_tail(const LaunchCtx& c, const TailPhase* ph, int nph) {
   const int nblk = 1;
   DISPATCH_PD(c, k_tail, c.P, c.pool, ph, nph, c.pp);
   return 1;
+}
+
+#define DISPATCH_PD_SMEM(c, SMEM, KER, ...)                                            \
+  do {                                                                                 \
+    if ((c).pp.problem == kCH) {                                                       \
+      if ((c).ndims == 2) KER<kCH, 2><<<1, kBlock, SMEM, (c).s>>>(__VA_ARGS__);        \
+      else KER<kCH, 3><<<1, kBlock, SMEM, (c).s>>>(__VA_ARGS__);                       \
+    } else if ((c).pp.problem == kBio) {                                               \
+      if ((c).ndims == 2) KER<kBio, 2><<<1, kBlock, SMEM, (c).s>>>(__VA_ARGS__);       \
+      else KER<kBio, 3><<<1, kBlock, SMEM, (c).s>>>(__VA_ARGS__);                      \
+    } else {                                                                           \
+      if ((c).ndims == 2) KER<kGrowth, 2><<<1, kBlock, SMEM, (c).s>>>(__VA_ARGS__);    \
+      else KER<kGrowth, 3><<<1, kBlock, SMEM, (c).s>>>(__VA_ARGS__);                   \
+    }                                                                                  \
+  } while (0)
+
+int launch_tail_smem(const LaunchCtx& c, const PatchDev* shadow, const TailPhase* ph, int nph, const StageSeg* segs,
+                     int nsegs, int smem_bytes) {
+  if (nph <= 0) return 0;
+  DISPATCH_PD_SMEM(c, smem_bytes, k_tail_smem, shadow, c.pool, ph, nph, c.pp, segs, nsegs);
+  return 1;
+}
+
+int tail_smem_attributes() {
+  const int m = kTailSmemMax;
+  const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e = cudaFuncSetAttribute(k_tail_smem<kCH, 2>, a, m);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tail_smem<kCH, 3>, a, m);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tail_smem<kBio, 2>, a, m);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tail_smem<kBio, 3>, a, m);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tail_smem<kGrowth, 2>, a, m);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tail_smem<kGrowth, 3>, a, m);
+  return e == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace bsamg

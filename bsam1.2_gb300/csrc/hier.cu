@@ -65,6 +65,14 @@ long long align32(long long x) { return (x + 31) & ~31LL; }
 // ---------------------------------------------------------------------------
 // schedule pieces (plain FP64)
 
+int launch_fp_tail(Hier& H, const Hier::TailProg& T) {
+  const TailPhase* ph = static_cast<const TailPhase*>(T.phases);
+  if (T.smem_bytes)
+    return after_launch(H, launch_tail_smem(H.lc(), static_cast<const PatchDev*>(T.shadow), ph, T.nph,
+                                            static_cast<const StageSeg*>(T.segs), T.nsegs, T.smem_bytes));
+  return after_launch(H, launch_tail(H.lc(), ph, T.nph));
+}
+
 // the tail program being recorded: the V-cycle schedule records its
 // operations instead of launching them
 std::vector<TailPhase>* recording(Hier& H) { return static_cast<std::vector<TailPhase>*>(H.rec); }
@@ -122,7 +130,7 @@ int enq_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
   if (!H.rec && level <= H.tail_level && level >= minlevel) {
     auto it = H.fp_tail_progs.find(std::make_tuple(level, minlevel, nsmooth));
     if (it != H.fp_tail_progs.end())  // the rest of the V-cycle in one block
-      return after_launch(H, launch_tail(H.lc(), static_cast<const TailPhase*>(it->second.first), it->second.second));
+      return launch_fp_tail(H, it->second);
   }
   RET(enq_level_relax(H, level, nsmooth));
   if (level > minlevel) {
@@ -156,12 +164,48 @@ int fp_prepare_tail(Hier& H, int finest, int minlevel, int nsmooth) {
     int r = which > 0 ? enq_vcycle(H, start, minlevel, nsmooth) : enq_fill_down_from(H, -which, start, minlevel);
     H.rec = nullptr;
     if (r) return r;
-    void* d = nullptr;
+    Hier::TailProg T;
+    T.nph = (int)prog.size();
     if (!prog.empty()) {
-      CK(dev_alloc(H, &d, sizeof(TailPhase) * prog.size()));
-      CK(cudaMemcpyAsync(d, prog.data(), sizeof(TailPhase) * prog.size(), cudaMemcpyHostToDevice, H.s));  // staged
+      CK(dev_alloc(H, &T.phases, sizeof(TailPhase) * prog.size()));
+      CK(cudaMemcpyAsync(T.phases, prog.data(), sizeof(TailPhase) * prog.size(), cudaMemcpyHostToDevice, H.s));
     }
-    H.fp_tail_progs[key] = std::make_pair(d, (int)prog.size());
+    // shared-memory staging of the tail levels' FP64 arrays when they fit:
+    // q, qc, f, rf read and written back, qold read
+    std::vector<PatchDev> shadow = H.hP;
+    std::vector<StageSeg> segs;
+    long long so = 0;
+    auto add = [&](long long g, long long n, int out) {
+      segs.push_back(StageSeg{g, (int)so, (int)n, out, 0});
+      long long at = so;
+      so += (n + 1) & ~1LL;
+      return at;
+    };
+    for (size_t p = 0; p < H.patches.size(); p++) {
+      const HostPatch& P = H.patches[p];
+      if (P.level < minlevel || P.level > start) continue;
+      PatchDev& D = shadow[p];
+      D.oq = add(D.oq, (long long)H.nrvars * P.sq, 1);
+      D.oqold = add(D.oqold, (long long)H.nrvars * P.sq, 0);
+      D.oqc = add(D.oqc, (long long)H.nrvars * P.sc, 1);
+      D.of = add(D.of, (long long)H.nrvars * P.sf, 1);
+      D.orf = add(D.orf, (long long)H.nrvars * P.sf, 1);
+    }
+    if (so * (long long)sizeof(double) <= kTailSmemMax && !segs.empty() && !prog.empty()) {
+      static bool attr = false;
+      if (!attr) {
+        if (tail_smem_attributes()) return cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute(tail)");
+        attr = true;
+      }
+      T.smem_bytes = (int)(so * sizeof(double));
+      T.nsegs = (int)segs.size();
+      CK(dev_alloc(H, &T.shadow, sizeof(PatchDev) * shadow.size()));
+      CK(cudaMemcpyAsync(T.shadow, shadow.data(), sizeof(PatchDev) * shadow.size(), cudaMemcpyHostToDevice, H.s));
+      T.hshadow = shadow;
+      CK(dev_alloc(H, &T.segs, sizeof(StageSeg) * segs.size()));
+      CK(cudaMemcpyAsync(T.segs, segs.data(), sizeof(StageSeg) * segs.size(), cudaMemcpyHostToDevice, H.s));
+    }
+    H.fp_tail_progs[key] = T;
   }
   return BSAMG_OK;
 }
@@ -172,8 +216,7 @@ int enq_fill_down_from(Hier& H, int field, int finest, int minlevel) {
     if (!H.rec && level <= H.tail_level) {
       auto it = H.fp_tail_progs.find(std::make_tuple(level, minlevel, -field));
       if (it != H.fp_tail_progs.end())  // the remaining levels in one block
-        return after_launch(H, launch_tail(H.lc(), static_cast<const TailPhase*>(it->second.first),
-                                           it->second.second));
+        return launch_fp_tail(H, it->second);
     }
     RET(enq_op(H, level, kKindCoarse, kTFill, field));
     if (field == 2) RET(enq_set_ghost(H, level - 1, 0));
@@ -292,6 +335,12 @@ int capture_graph(Hier& H, const GraphKey& key, const std::function<int()>& body
 // the host thread sleeps on an event instead of spinning, which leaves the
 // host cores to the threads that launch work when many hierarchies share
 // the GPU.
+void free_tail(Hier& H, Hier::TailProg& T) {
+  for (void* p : {T.phases, T.shadow, T.segs})
+    if (p) cudaFreeAsync(p, H.s);
+  T = Hier::TailProg();
+}
+
 int stream_wait(Hier& H) {
   if (!H.ctx->blocking_wait) {
     CK(cudaStreamSynchronize(H.s));
@@ -764,8 +813,7 @@ void release(Hier& H) {
     }
   }
   mixed_free(H);
-  for (auto& kv : H.fp_tail_progs)
-    if (kv.second.first) cudaFreeAsync(kv.second.first, H.s);
+  for (auto& kv : H.fp_tail_progs) free_tail(H, kv.second);
   H.fp_tail_progs.clear();
   if (H.dP) cudaFreeAsync(H.dP, H.s);
   if (H.pool) cudaFreeAsync(H.pool, H.s);
@@ -1159,6 +1207,19 @@ int bsamg_set_params(bsamg_hier* h, const double* params, int nparams) {
   cudaError_t e = cudaMemcpyAsync(h->dP, h->hP.data(), sizeof(PatchDev) * h->hP.size(), cudaMemcpyHostToDevice,
                                   h->s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(patch table)");
+  // the staged tails' patch tables carry the coefficients too
+  for (auto* progs : {&h->mx_tail_progs, &h->fp_tail_progs})
+    for (auto& kv : *progs) {
+      Hier::TailProg& T = kv.second;
+      if (!T.shadow) continue;
+      for (size_t n = 0; n < T.hshadow.size(); n++) {
+        std::memcpy(T.hshadow[n].c, h->hP[n].c, sizeof(h->hP[n].c));
+        std::memcpy(T.hshadow[n].cf, h->hP[n].cf, sizeof(h->hP[n].cf));
+      }
+      e = cudaMemcpyAsync(T.shadow, T.hshadow.data(), sizeof(PatchDev) * T.hshadow.size(), cudaMemcpyHostToDevice,
+                          h->s);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(tail patch table)");
+    }
   // Kernels read the coefficients from the patch table, except those of the
   // periodic-box path and the BioGrowth/growth parameters, which are kernel
   // arguments captured in graphs: those graphs are captured again.

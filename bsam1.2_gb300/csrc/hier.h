@@ -82,7 +82,19 @@ struct Hier {
   // keys: (start level, minlevel, nsmooth) for V-cycles, (start level,
   // minlevel, -field) for FillDown
   using TailKey = std::tuple<int, int, int>;
-  std::map<TailKey, std::pair<void*, int>> mx_tail_progs, fp_tail_progs;
+  struct TailProg {
+    void* phases = nullptr;  // TailPhase[nph]
+    int nph = 0;
+    // when the tail levels' arrays fit, they are staged in the block's
+    // shared memory: a patch table whose tail patches address it, and the
+    // copy segments (StageSeg[nsegs]); smem_bytes = 0 otherwise
+    void* shadow = nullptr;
+    std::vector<PatchDev> hshadow;  // host copy (coefficients follow bsamg_set_params)
+    void* segs = nullptr;
+    int nsegs = 0;
+    int smem_bytes = 0;
+  };
+  std::map<TailKey, TailProg> mx_tail_progs, fp_tail_progs;
   void* rec = nullptr;  // std::vector<TailPhase> being recorded
   // periodic-box mixed path (box.cu): every level one periodic box with even
   // extents covering its parent; FP64 iterate held as float pairs
@@ -156,6 +168,8 @@ int capture_graph(Hier& H, const GraphKey& key, const std::function<int()>& body
 int replay(Hier& H, Hier::GraphRec* g);
 // wait for the hierarchy's stream (spinning, or sleeping with blocking waits)
 int stream_wait(Hier& H);
+// release the device arrays of a tail program (stream-ordered)
+void free_tail(Hier& H, Hier::TailProg& T);
 
 }  // namespace bsamg
 

@@ -42,6 +42,14 @@ struct TailPhase {
   const int* stage_off;
 };
 
+// A contiguous run of pool elements staged in shared memory by a tail
+// kernel: pool[g .. g+n) <-> smem[s .. s+n); written back when out != 0.
+struct StageSeg {
+  long long g;
+  int s, n, out, pad;
+};
+constexpr int kTailSmemMax = 160 * 1024;  // shared-memory budget of a staged tail
+
 // ---- plain FP64 path (fp64.cu, built with --fmad=false) ----
 int launch_relax(const LaunchCtx& c, const Blk* blk, int nblk, int ipass);
 int launch_restrict_q(const LaunchCtx& c, const Blk* blk, int nblk);
@@ -82,5 +90,11 @@ int launch_ghost_program_1cta(const LaunchCtx& c, const GhostOp* ops,
                               const int* stage_off, int nstages);
 // the recorded coarse tail of an FP64 V-cycle, one block
 int launch_tail(const LaunchCtx& c, const TailPhase* ph, int nph);
+// the same on arrays staged in shared memory (shadow: the patch table that
+// addresses them); tail_smem_attributes raises the kernels' dynamic
+// shared-memory limit to kTailSmemMax once (0 on success)
+int launch_tail_smem(const LaunchCtx& c, const PatchDev* shadow, const TailPhase* ph, int nph, const StageSeg* segs,
+                     int nsegs, int smem_bytes);
+int tail_smem_attributes();
 
 }  // namespace bsamg

@@ -724,9 +724,8 @@ __global__ void __launch_bounds__(kBlock) k_ghost32_program(const PatchDev* __re
 // the stand-alone kernel computes, so results are bit-identical.
 
 template <int DIM, int PR>
-__global__ void __launch_bounds__(kBlock) k_mx_tail(const PatchDev* __restrict__ P, float* __restrict__ fpool,
-                                                   const TailPhase* __restrict__ ph, int nph, int nrvars, float dt,
-                                                   float cp) {
+__device__ __forceinline__ void run_tail(const PatchDev* __restrict__ P, float* fpool, const TailPhase* __restrict__ ph,
+                                         int nph, int nrvars, float dt, float cp) {
   for (int x = 0; x < nph; x++) {
     const TailPhase f = ph[x];
     if (f.op == kTGhost) {
@@ -756,6 +755,36 @@ __global__ void __launch_bounds__(kBlock) k_mx_tail(const PatchDev* __restrict__
       }
     }
     __syncthreads();
+  }
+}
+
+template <int DIM, int PR>
+__global__ void __launch_bounds__(kBlock) k_mx_tail(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                   const TailPhase* __restrict__ ph, int nph, int nrvars, float dt,
+                                                   float cp) {
+  run_tail<DIM, PR>(P, fpool, ph, nph, nrvars, dt, cp);
+}
+
+// The same with the tail levels' arrays staged in shared memory: P is a
+// patch table whose tail patches address the block's shared memory, so the
+// phases run on on-chip copies; the modified arrays are written back at the
+// end.  Same arithmetic on the same values: results are bit-identical.
+template <int DIM, int PR>
+__global__ void __launch_bounds__(kBlock) k_mx_tail_smem(const PatchDev* __restrict__ P, float* __restrict__ fpool,
+                                                        const TailPhase* __restrict__ ph, int nph, int nrvars,
+                                                        float dt, float cp, const StageSeg* __restrict__ segs,
+                                                        int nsegs) {
+  extern __shared__ float sm[];
+  for (int x = 0; x < nsegs; x++) {
+    const StageSeg sg = segs[x];
+    for (int t = threadIdx.x; t < sg.n; t += blockDim.x) sm[sg.s + t] = fpool[sg.g + t];
+  }
+  __syncthreads();
+  run_tail<DIM, PR>(P, sm, ph, nph, nrvars, dt, cp);
+  for (int x = 0; x < nsegs; x++) {
+    const StageSeg sg = segs[x];
+    if (!sg.out) continue;
+    for (int t = threadIdx.x; t < sg.n; t += blockDim.x) fpool[sg.g + t] = sm[sg.s + t];
   }
 }
 
@@ -844,15 +873,27 @@ int mx_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
   if (!H.rec && level <= H.tail_level && level >= minlevel) {
     auto it = H.mx_tail_progs.find(std::make_tuple(level, minlevel, nsmooth));
     if (it != H.mx_tail_progs.end()) {  // the whole V-cycle from here down in one CTA
-      const TailPhase* ph = static_cast<const TailPhase*>(it->second.first);
+      const Hier::TailProg& T = it->second;
+      const TailPhase* ph = static_cast<const TailPhase*>(T.phases);
       float dt = (float)H.pp.dt, cp = (float)H.pp.cpress;
-      int n = it->second.second;
-      if (H.problem == kGrowth) {
-        if (H.ndims == 2) k_mx_tail<2, kGrowth><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, H.nrvars, dt, cp);
-        else k_mx_tail<3, kGrowth><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, H.nrvars, dt, cp);
+      int n = T.nph, nr = H.nrvars;
+      if (T.smem_bytes) {
+        const PatchDev* sp = static_cast<const PatchDev*>(T.shadow);
+        const StageSeg* sg = static_cast<const StageSeg*>(T.segs);
+        int sb = T.smem_bytes, ns = T.nsegs;
+        if (H.problem == kGrowth) {
+          if (H.ndims == 2) k_mx_tail_smem<2, kGrowth><<<1, kBlock, sb, H.s>>>(sp, H.fpool, ph, n, nr, dt, cp, sg, ns);
+          else k_mx_tail_smem<3, kGrowth><<<1, kBlock, sb, H.s>>>(sp, H.fpool, ph, n, nr, dt, cp, sg, ns);
+        } else {
+          if (H.ndims == 2) k_mx_tail_smem<2, kCH><<<1, kBlock, sb, H.s>>>(sp, H.fpool, ph, n, nr, dt, cp, sg, ns);
+          else k_mx_tail_smem<3, kCH><<<1, kBlock, sb, H.s>>>(sp, H.fpool, ph, n, nr, dt, cp, sg, ns);
+        }
+      } else if (H.problem == kGrowth) {
+        if (H.ndims == 2) k_mx_tail<2, kGrowth><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, nr, dt, cp);
+        else k_mx_tail<3, kGrowth><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, nr, dt, cp);
       } else {
-        if (H.ndims == 2) k_mx_tail<2, kCH><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, H.nrvars, dt, cp);
-        else k_mx_tail<3, kCH><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, H.nrvars, dt, cp);
+        if (H.ndims == 2) k_mx_tail<2, kCH><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, nr, dt, cp);
+        else k_mx_tail<3, kCH><<<1, kBlock, 0, H.s>>>(H.dP, H.fpool, ph, n, nr, dt, cp);
       }
       return after_launch(H, 1);
     }
@@ -885,14 +926,61 @@ int mx_prepare_tail(Hier& H, int finest, int minlevel, int nsmooth) {
   int r = mx_vcycle(H, start, minlevel, nsmooth);
   H.rec = nullptr;
   if (r) return r;
-  void* d = nullptr;
+  Hier::TailProg T;
+  T.nph = (int)prog.size();
   if (!prog.empty()) {
-    cudaError_t e = dev_alloc(H, &d, sizeof(TailPhase) * prog.size());
+    cudaError_t e = dev_alloc(H, &T.phases, sizeof(TailPhase) * prog.size());
     if (e == cudaSuccess)  // staged from pageable memory before it returns
-      e = cudaMemcpyAsync(d, prog.data(), sizeof(TailPhase) * prog.size(), cudaMemcpyHostToDevice, H.s);
+      e = cudaMemcpyAsync(T.phases, prog.data(), sizeof(TailPhase) * prog.size(), cudaMemcpyHostToDevice, H.s);
     if (e != cudaSuccess) return cuda_fail(e, "tail program upload");
   }
-  H.mx_tail_progs[key] = std::make_pair(d, (int)prog.size());
+  // shared-memory staging of the tail levels' FP32 arrays (e, ec, g: read
+  // and written back; base fields: read) when they fit
+  std::vector<PatchDev> shadow = H.hP;
+  std::vector<StageSeg> segs;
+  long long so = 0;
+  long long nbase = H.problem == kGrowth ? 4 : 1;
+  auto add = [&](long long g, long long n, int out) {
+    segs.push_back(StageSeg{g, (int)so, (int)n, out, 0});
+    long long at = so;
+    so += (n + 3) & ~3LL;
+    return at;
+  };
+  for (size_t p = 0; p < H.patches.size(); p++) {
+    const HostPatch& P = H.patches[p];
+    if (P.level < minlevel || P.level > start) continue;
+    PatchDev& D = shadow[p];
+    D.eq = add(D.eq, (long long)H.nrvars * P.sq, 1);
+    D.ecq = add(D.ecq, (long long)H.nrvars * P.sc, 1);
+    D.eg = add(D.eg, (long long)H.nrvars * P.sf, 1);
+    D.ephi = add(D.ephi, nbase * P.sf, 0);
+  }
+  if (so * (long long)sizeof(float) <= kTailSmemMax && !segs.empty()) {
+    T.smem_bytes = (int)(so * sizeof(float));
+    T.nsegs = (int)segs.size();
+    static bool attr[2][2] = {};  // the kernels' dynamic shared-memory limit, set once
+    int a = H.ndims - 2, b = H.problem == kGrowth;
+    if (!attr[a][b]) {
+      cudaError_t e;
+      if (H.problem == kGrowth)
+        e = H.ndims == 2 ? cudaFuncSetAttribute(k_mx_tail_smem<2, kGrowth>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax)
+                         : cudaFuncSetAttribute(k_mx_tail_smem<3, kGrowth>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax);
+      else
+        e = H.ndims == 2 ? cudaFuncSetAttribute(k_mx_tail_smem<2, kCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax)
+                         : cudaFuncSetAttribute(k_mx_tail_smem<3, kCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(tail)");
+      attr[a][b] = true;
+    }
+    cudaError_t e = dev_alloc(H, &T.shadow, sizeof(PatchDev) * shadow.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(T.shadow, shadow.data(), sizeof(PatchDev) * shadow.size(), cudaMemcpyHostToDevice, H.s);
+    T.hshadow = shadow;
+    if (e == cudaSuccess) e = dev_alloc(H, &T.segs, sizeof(StageSeg) * segs.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(T.segs, segs.data(), sizeof(StageSeg) * segs.size(), cudaMemcpyHostToDevice, H.s);
+    if (e != cudaSuccess) return cuda_fail(e, "tail staging upload");
+  }
+  H.mx_tail_progs[key] = T;
   return BSAMG_OK;
 }
 
@@ -1064,8 +1152,7 @@ void mixed_free(Hier& H) {
   H.fpool = nullptr;
   if (H.mx_prep_coarse) cudaFreeAsync(H.mx_prep_coarse, H.s);
   H.mx_prep_coarse = nullptr;
-  for (auto& kv : H.mx_tail_progs)
-    if (kv.second.first) cudaFreeAsync(kv.second.first, H.s);
+  for (auto& kv : H.mx_tail_progs) free_tail(H, kv.second);
   H.mx_tail_progs.clear();
   for (int l = 0; l < kNLev; l++) {
     if (H.mx_norm_blk[l]) cudaFreeAsync(H.mx_norm_blk[l], H.s);
@@ -1116,8 +1203,7 @@ void set_tail(Hier& H, long long cells) {
   // the highest level whose level and every level below it together hold at
   // most `cells` interior cells runs the rest of the V-cycle in one CTA
   for (auto* progs : {&H.mx_tail_progs, &H.fp_tail_progs}) {
-    for (auto& kv : *progs)
-      if (kv.second.first) cudaFreeAsync(kv.second.first, H.s);
+    for (auto& kv : *progs) free_tail(H, kv.second);
     progs->clear();
   }
   H.tail_cells = cells;

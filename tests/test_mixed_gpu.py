@@ -70,7 +70,7 @@ def test_coarse_tail_in_one_block_is_bit_identical(pkg, ctx, nd, n, levels, mode
     paths), and the tail cuts the launches."""
     pats, mn = pkg.serve.nested_spec(nd, n, levels)
     res = {}
-    for cells in (16384, 0):
+    for cells in (16384, 2048, 0):
         h = pkg.Hierarchy(ctx, nd, 2, "ch", [1e-3 if nd == 2 else 5e-4, 0.02])
         for p in pats:
             h.add_patch(p["level"], p["id"], p["parent_id"], p["mx"], p["mglobal"], p["mbounds"], p["mthbc"],
@@ -85,11 +85,13 @@ def test_coarse_tail_in_one_block_is_bit_identical(pkg, ctx, nd, n, levels, mode
         hist = [h.time_step(s == 0, fin, mn, 2, 30, 1e-8, mode=mode) for s in range(3)]
         res[cells] = (hist, {p["id"]: h.get(p["id"], "q") for p in pats if p["level"] >= 0}, h.launch_count() - l0)
         h.close()
-    (ha, qa, la), (hb, qb, lb) = res[16384], res[0]
-    assert ha == hb
-    for pid in qa:
-        assert np.array_equal(qa[pid], qb[pid]), pid
-    assert la < lb, (la, lb)
+    hb, qb, lb = res[0]
+    for cells in (16384, 2048):  # 2048: the tail's arrays staged in shared memory
+        ha, qa, la = res[cells]
+        assert ha == hb, cells
+        for pid in qa:
+            assert np.array_equal(qa[pid], qb[pid]), (cells, pid)
+        assert la < lb, (cells, la, lb)
 
 
 def _growth_pair(pkg, ctx, amr):
