@@ -116,6 +116,7 @@ def lib():
         "bsamg_stream": ([P, ctypes.POINTER(P)], I),
         "bsamg_launch_count": ([P, ctypes.POINTER(ctypes.c_longlong)], I),
         "bsamg_set_tail_cells": ([P, ctypes.c_longlong], I),
+        "bsamg_set_box_sweep": ([P, I], I),
         "bsamg_graph_stats": ([P, IP, IP], I),
         "bsamg_set_params": ([P, DP, I], I),
         "bsamg_hier_reset": ([P], I),
@@ -393,6 +394,11 @@ class Hierarchy:
     def reset(self):
         """Every field back to zero, as after commit (bsamg_hier_reset)."""
         _ck(lib().bsamg_hier_reset(self.h), "bsamg_hier_reset")
+
+    def set_box_sweep(self, kind):
+        """Colour sweep of 3D periodic-box levels: 0 two rows a thread, 1
+        four (default), 2 rows staged by bulk copies (bsamg_set_box_sweep)."""
+        _ck(lib().bsamg_set_box_sweep(self.h, int(kind)), "bsamg_set_box_sweep")
 
     def set_tail_cells(self, cells):
         """Largest cumulative coarse-level size the mixed V-cycle runs inside

@@ -252,21 +252,21 @@ __device__ __forceinline__ void relax_at(float* __restrict__ fp, const BoxLev& L
   E.v1[l.own] = (b2 - a21 * b1) * rdet;
 }
 
-// Full-grid sweep: each thread takes position h of rows 2yp and 2yp+1 (n1
-// is even), loading both cells' data before either is stored so that twice
-// the loads are in flight per thread.
-template <int DIM>
-__global__ void __launch_bounds__(256, 8) k_bx_relax(float* __restrict__ fp, BoxLev L, int c, int first) {
+// Full-grid sweep: each thread takes position h of rows R*yp .. R*yp+R-1
+// (n1 is a multiple of R), loading all its cells' data before any is stored
+// so that R times the loads are in flight per thread.
+template <int DIM, int R = 2, int MINB = 8>
+__global__ void __launch_bounds__(256, MINB) k_bx_relax(float* __restrict__ fp, BoxLev L, int c, int first) {
   int h = blockIdx.x * blockDim.x + threadIdx.x;
   int yp = blockIdx.y * blockDim.y + threadIdx.y;
   int z = blockIdx.z;
-  if (h >= L.hh || 2 * yp >= L.n[1]) return;
+  if (h >= L.hh || R * yp >= L.n[1]) return;
   V2 E = var2(fp, L.oe, L.half), G = var2(fp, L.og, L.half);
   const float* PB = fp + L.opb;
-  unsigned own[2];
-  float pb[2], xv[2], s0[2], s1[2], g0[2], g1[2];
-  for (int k = 0; k < 2; k++) {
-    int y = 2 * yp + k;
+  unsigned own[R];
+  float pb[R], xv[R], s0[R], s1[R], g0[R], g1[R];
+  for (int k = 0; k < R; k++) {
+    int y = R * yp + k;
     int x = 2 * h + ((c + y + z + (DIM == 3 ? 1 : 0)) & 1);
     Loc<DIM> l(L, x, y, z);
     own[k] = l.own;
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(256, 8) k_bx_relax(float* __restrict__ fp, Box
     g0[k] = G.v0[l.own];
     g1[k] = G.v1[l.own];
   }
-  for (int k = 0; k < 2; k++) {
+  for (int k = 0; k < R; k++) {
     float w = pb[k] + xv[k];
     float a21 = -3.0f * w * w - L.tmp3;
     float b1 = g0[k] + L.c0 * s1[k];
@@ -289,6 +289,152 @@ __global__ void __launch_bounds__(256, 8) k_bx_relax(float* __restrict__ fp, Box
     E.v0[own[k]] = (b1 - L.a12 * b2) * rdet;
     E.v1[own[k]] = (b2 - a21 * b1) * rdet;
   }
+}
+
+// ---------------------------------------------------------------------------
+// The same colour sweep (3D) with its rows staged in shared memory by bulk
+// asynchronous copies (cp.async.bulk, completion counted on an mbarrier).
+// A tile is kTileRows consecutive rows y of one plane z of the own colour; it
+// needs the own rows of pb, g0, g1 (and e0 unless first) and the other
+// colour's e0, e1 rows y-1..y+kTileRows at z and y..y+kTileRows-1 at z-1 and
+// z+1 (periodic wrap).  Persistent CTAs walk the tiles plane by plane, the
+// next tile's rows in flight while the current one is computed, so the
+// memory system always has whole rows outstanding instead of one word per
+// thread.  Every expression is relax_at's, evaluated in the same order.
+constexpr int kTileThreads = 256;
+constexpr long long kWaitLimit = 1ll << 24;  // mbarrier polls before giving up
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (long long it = 0; it < kWaitLimit; it++) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// floats of one stage: own pb, g0, g1, e0 (4 T rows), other e0/e1 at z
+// (2 (T+2) rows), at z-1 and z+1 (4 T rows)
+__host__ __device__ __forceinline__ int tile_stage_floats(int T, int hh) { return (10 * T + 4) * hh; }
+
+// T rows per tile, NS stages (NS - 1 tiles in flight ahead of the one computed)
+template <int T, int NS>
+__global__ void __launch_bounds__(kTileThreads) k_bx_relax_tiled(float* __restrict__ fp, BoxLev L, int c, int first) {
+  extern __shared__ __align__(128) float tsm[];
+  __shared__ __align__(8) unsigned long long bar[NS];
+  const int hh = L.hh, n1 = L.n[1], n2 = L.n[2];
+  const int SF = tile_stage_floats(T, hh);
+  const int tiles_per_plane = n1 / T, ntiles = tiles_per_plane * n2;
+  const unsigned rowb = (unsigned)hh * 4u;
+  const long long half = L.half;
+  // bases of the colour-split arrays (variable v, colour k): off + (2v+k)*half
+  const float* E = fp + L.oe;
+  const float* G = fp + L.og;
+  const float* PB = fp + L.opb;
+  const int o = 1 - c;  // the other colour
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < NS; b++)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[b])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // rows of a tile into stage buffer sb: consecutive rows of one array are
+  // contiguous in memory, so each array's rows go as one bulk copy (two or
+  // three where the rows wrap around the plane); thread 0 issues them
+  auto issue = [&](int tile, int sb) {
+    if (threadIdx.x != 0) return;
+    int z = tile / tiles_per_plane, y0 = (tile % tiles_per_plane) * T;
+    int nrows = first == 1 ? 3 * T : (first == 2 ? 3 * T + 2 * (T + 2) + 4 * T : 4 * T + 2 * (T + 2) + 4 * T);
+    unsigned b = smem_addr(&bar[sb]);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"((unsigned)nrows * rowb)
+                 : "memory");
+    float* base = tsm + sb * SF;
+    // rows y .. y+n-1 (wrapping in the plane) of plane zz of array a -> slots from `slot`
+    auto rows = [&](const float* a, int zz, int y, int n, int slot) {
+      while (n > 0) {
+        int yy = y < 0 ? y + n1 : (y >= n1 ? y - n1 : y);
+        int run = n1 - yy < n ? n1 - yy : n;
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_addr(base + (long long)slot * hh)),
+            "l"(a + ((long long)zz * n1 + yy) * hh), "r"((unsigned)run * rowb), "r"(b)
+            : "memory");
+        y += run;
+        n -= run;
+        slot += run;
+      }
+    };
+    rows(PB + (long long)c * half, z, y0, T, 0);
+    rows(G + (long long)c * half, z, y0, T, T);
+    rows(G + (long long)(2 + c) * half, z, y0, T, 2 * T);
+    if (first == 0) rows(E + (long long)c * half, z, y0, T, 3 * T);
+    if (first != 1) {
+      int zm = z ? z - 1 : n2 - 1, zp = z + 1 < n2 ? z + 1 : 0;
+      for (int v = 0; v < 2; v++) {
+        const float* a = E + (long long)(2 * v + o) * half;
+        rows(a, z, y0 - 1, T + 2, 4 * T + v * (T + 2));
+        rows(a, zm, y0, T, 4 * T + 2 * (T + 2) + v * T);
+        rows(a, zp, y0, T, 4 * T + 2 * (T + 2) + 2 * T + v * T);
+      }
+    }
+  };
+  int it = 0;
+  int tile = blockIdx.x;
+  for (int k = 0; k < NS - 1; k++)
+    if (tile + k * (int)gridDim.x < ntiles) issue(tile + k * gridDim.x, k);
+  bool ok = true;
+  for (; tile < ntiles; tile += gridDim.x, it++) {
+    int sb = it % NS;
+    int next = tile + (NS - 1) * gridDim.x;  // its buffer was released by the barrier ending the last iteration
+    if (next < ntiles) issue(next, (it + NS - 1) % NS);
+    ok = mbar_wait(smem_addr(&bar[sb]), (unsigned)((it / NS) & 1)) && ok;
+    const float* st = tsm + sb * SF;
+    const float* sPB = st;
+    const float* sG0 = st + T * hh;
+    const float* sG1 = st + 2 * T * hh;
+    const float* sE0 = st + 3 * T * hh;
+    const float* sO0 = st + 4 * T * hh;          // other e0 at z, rows y0-1..y0+T
+    const float* sO1 = sO0 + (T + 2) * hh;       // other e1 at z
+    const float* sZ = sO1 + (T + 2) * hh;        // z-1: e0, e1; z+1: e0, e1 (T rows each)
+    int z = tile / tiles_per_plane, y0 = (tile % tiles_per_plane) * T;
+    for (int q = threadIdx.x; q < T * hh; q += kTileThreads) {
+      int yl = q / hh, h = q - yl * hh;
+      int y = y0 + yl;
+      int bb = (c + y + z + 1) & 1;  // x = 2h + bb
+      int xm = bb ? h : (h ? h - 1 : hh - 1);
+      int xp = bb ? (h + 1 < hh ? h + 1 : 0) : h;
+      float pb = sPB[q];
+      float s0 = 0.f, s1 = 0.f, xv = 0.f;
+      if (first != 1) {
+        const float* a0 = sO0 + (yl + 1) * hh;
+        const float* a1 = sO1 + (yl + 1) * hh;
+        s0 = a0[xm] + a0[xp] + a0[h - hh] + a0[h + hh] + sZ[q] + sZ[2 * T * hh + q];
+        s1 = a1[xm] + a1[xp] + a1[h - hh] + a1[h + hh] + sZ[T * hh + q] + sZ[3 * T * hh + q];
+        if (first == 0) xv = sE0[q];
+      }
+      float w = pb + xv;
+      float a21 = -3.0f * w * w - L.tmp3;
+      float b1 = sG0[q] + L.c0 * s1;
+      float b2 = sG1[q] - L.c1 * s0 - xv * xv * (3.0f * pb + 2.0f * xv);
+      float rdet = 1.0f / (1.0f - L.a12 * a21);
+      float r0 = (b1 - L.a12 * b2) * rdet, r1 = (b2 - a21 * b1) * rdet;
+      if (!ok) r0 = r1 = __int_as_float(0x7fc00000);  // a copy that never landed: poison the sweep
+      long long row = ((long long)z * n1 + y) * hh + h;
+      float* Ew = fp + L.oe;
+      Ew[(long long)c * half + row] = r0;
+      Ew[(long long)(2 + c) * half + row] = r1;
+    }
+    __syncthreads();  // every thread is done with buffer sb before it is refilled
+  }
+  if (!ok)  // a wait gave up: give the copies still in flight a bounded time to land before the block exits
+    for (int b = 0; b < NS; b++) mbar_wait(smem_addr(&bar[b]), 0u), mbar_wait(smem_addr(&bar[b]), 1u);
 }
 
 // RestrictSolution on e and on the base field: coarse e = ec = R(e_fine),
@@ -635,8 +781,41 @@ long long ctas(const Launch& s) { return (long long)s.g.x * s.g.y * s.g.z; }
 
 BoxLev& B(Hier& H, int level) { return H.blev[level + kMaxDepth]; }
 
+// The staged sweep (box_sweep 2) applies to 3D levels whose rows are whole
+// 16-byte units and whose planes split into whole 8-row tiles, large enough
+// to fill the GPU; two stages of 8 rows measured fastest of the staged forms.
+constexpr int kTileT = 8, kTileNS = 2;
+bool staged_relax(const Hier& H, const BoxLev& L) {
+  if (H.box_sweep != 2 || H.ndims != 3) return false;
+  long long smem = (long long)kTileNS * tile_stage_floats(kTileT, L.hh) * 4;
+  return L.hh % 4 == 0 && L.hh >= 64 && smem <= 200 * 1024 && L.n[1] % kTileT == 0 &&
+         (kTileT * L.hh) % kTileThreads == 0;
+}
+
+int launch_staged(Hier& H, const BoxLev& L, int c, int first) {
+  int occ = 0;
+  int smem = kTileNS * tile_stage_floats(kTileT, L.hh) * (int)sizeof(float);
+  auto ker = k_bx_relax_tiled<kTileT, kTileNS>;
+  cudaError_t e = cudaFuncSetAttribute(ker, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_bx_relax_tiled)");
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ker, kTileThreads, smem);
+  if (e != cudaSuccess || occ < 1) return cuda_fail(e, "occupancy(k_bx_relax_tiled)");
+  int ntiles = (L.n[1] / kTileT) * L.n[2];
+  int grid = std::min(ntiles, occ * H.box_sms);
+  ker<<<grid, kTileThreads, smem, H.s>>>(H.fpool, L, c, first);
+  return after_launch(H, 1);
+}
+
 int bx_relax(Hier& H, int level, int c, int first) {
   BoxLev& L = B(H, level);
+  if (staged_relax(H, L)) return launch_staged(H, L, c, first);
+  if (H.box_sweep == 1 && H.ndims == 3 && L.n[1] % 4 == 0) {
+    // four rows per thread at five blocks per SM (40 registers): four
+    // cells' loads in flight per thread
+    Launch sh = shape(L.hh, L.n[1] / 4, L.n[2]);
+    k_bx_relax<3, 4, 5><<<sh.g, sh.b, 0, H.s>>>(H.fpool, L, c, first);
+    return after_launch(H, 1);
+  }
   Launch sh = shape(L.hh, L.n[1] / 2, L.n[2]);
   BX_LAUNCH(H, sh, k_bx_relax, H.fpool, L, c, first);
   return BSAMG_OK;
@@ -738,6 +917,9 @@ void box_coefficients(Hier& H) {
 }
 
 size_t box_layout(Hier& H) {
+  if (cudaDeviceGetAttribute(&H.box_sms, cudaDevAttrMultiProcessorCount, H.ctx->device) != cudaSuccess ||
+      H.box_sms <= 0)
+    H.box_sms = 1;
   long long o = 0;
   auto al = [](long long x) { return (x + 63) & ~63LL; };
   for (int l = H.maxlevel; l >= H.minlevel; l--) {

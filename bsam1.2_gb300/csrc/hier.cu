@@ -1245,6 +1245,21 @@ int bsamg_hier_reset(bsamg_hier* h) {
   return e == cudaSuccess ? BSAMG_OK : cuda_fail(e, "cudaMemsetAsync(reset)");
 }
 
+int bsamg_set_box_sweep(bsamg_hier* h, int kind) {
+  if (!h || kind < 0 || kind > 2) return BSAMG_ERR_ARG;
+  int r = set_device(*h);
+  if (r) return r;
+  if (h->committed) {  // captured graphs hold the other sweep kernel
+    cudaError_t e = cudaStreamSynchronize(h->s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    for (auto& kv : h->graphs)
+      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    h->graphs.clear();
+  }
+  h->box_sweep = kind;
+  return BSAMG_OK;
+}
+
 int bsamg_set_tail_cells(bsamg_hier* h, long long cells) {
   if (!h || !h->committed || cells < 0) return BSAMG_ERR_ARG;
   int r = set_device(*h);

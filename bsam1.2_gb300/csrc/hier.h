@@ -99,6 +99,8 @@ struct Hier {
   // periodic-box mixed path (box.cu): every level one periodic box with even
   // extents covering its parent; FP64 iterate held as float pairs
   bool box = false;
+  int box_sweep = 1;  // 3D box colour sweep (box.cu): 0 two rows a thread, 1 four, 2 rows staged by bulk copies
+  int box_sms = 152;      // multiprocessors of the device (persistent grids)
   BoxLev blev[kNLev] = {};
   long long b_oqlo = 0, b_ofhi = 0, b_oflo = 0;  // float offsets (qhi is blev[finest].opb)
   size_t b_partials = 0;                         // partial-sum slots the box kernels need

@@ -581,6 +581,8 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   if (r) return r;
   nh->has_root_xupper = H.has_root_xupper;
   std::memcpy(nh->root_xupper, H.root_xupper, sizeof(H.root_xupper));
+  nh->tail_cells = H.tail_cells;  // tuning carries over
+  nh->box_sweep = H.box_sweep;
   auto fail = [&](int rc) {
     bsamg_hier_destroy(nh);
     return rc;

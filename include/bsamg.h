@@ -272,6 +272,14 @@ int bsamg_graph_stats(const bsamg_hier* h, int* instantiated, int* updated);
  * same results as on a newly built hierarchy. */
 int bsamg_set_params(bsamg_hier* h, const double* params, int nparams);
 int bsamg_hier_reset(bsamg_hier* h);
+/* Tuning (no reference counterpart): the colour sweep of 3D levels on the
+ * periodic-box mixed path.  0: each thread relaxes two rows' cells;
+ * 1 (the default): four rows' cells, all loads issued before any store;
+ * 2: rows staged in shared memory by bulk asynchronous copies, for rows of
+ * 128 to 512 cells (measured slower than 1 on a GB300; kept as the staged
+ * alternative).  All three evaluate the same expressions.  Drops the
+ * hierarchy's captured graphs. */
+int bsamg_set_box_sweep(bsamg_hier* h, int kind);
 /* Tuning (no reference counterpart): the mixed V-cycle runs its coarse
  * tail -- the levels from minlevel up to the highest one at which the
  * levels together hold at most `cells` interior cells -- inside one thread
