@@ -61,17 +61,32 @@ def regrid_params(maxlevel, tagging="ch", initial=False, maxside=0, first_id=100
     return r
 
 
-def qinit_callback(fn, ndims, nrvars):
+def embed_ghosted(a, mx, nrvars, mbc):
+    """A Fortran-ordered array q(1-g:mx+g, ..., nrvars) with g = 1 or mbc as
+    the hierarchy's ghosted layout q(1-mbc:mx+mbc, ...): an array with one
+    ghost layer goes to q(0:mx+1), the second layer left zero."""
+    nd = len(mx)
+    a = np.asarray(a, dtype=np.float64).ravel(order="F")
+    full = int(np.prod([v + 2 * mbc for v in mx])) * nrvars
+    one = int(np.prod([v + 2 for v in mx])) * nrvars
+    if a.size == full:
+        return a
+    if a.size != one:
+        raise ValueError(f"qinit returned {a.size} values for a patch of {full}")
+    out = np.zeros([v + 2 * mbc for v in mx] + [nrvars], order="F")
+    g = mbc - 1
+    out[tuple(slice(g, g + v + 2) for v in mx) + (slice(None),)] = a.reshape([v + 2 for v in mx] + [nrvars], order="F")
+    return out.ravel(order="F")
+
+
+def qinit_callback(fn, ndims, nrvars, mbc=1):
     """bsamg_qinit_fn around fn(level, mx, dx, xlower) -> the new patch's
-    ghosted Fortran-layout array (only its interior is used)."""
+    ghosted Fortran-layout array (only its interior is used), with mbc or
+    one ghost layer."""
     def cb(user, level, mx, dx, xl, q):
         m = [mx[d] for d in range(ndims)]
-        a = np.asarray(fn(level, m, [dx[d] for d in range(ndims)], [xl[d] for d in range(ndims)]),
-                       dtype=np.float64).ravel(order="F")
-        n = int(np.prod([v + 2 for v in m])) * nrvars
-        if a.size != n:
-            raise ValueError(f"qinit returned {a.size} values for a patch of {n}")
-        ctypes.memmove(q, a.ctypes.data, n * 8)
+        a = embed_ghosted(fn(level, m, [dx[d] for d in range(ndims)], [xl[d] for d in range(ndims)]), m, nrvars, mbc)
+        ctypes.memmove(q, a.ctypes.data, a.size * 8)
     return QINIT(cb)
 
 
@@ -195,7 +210,7 @@ class Hierarchy:
 
     def __init__(self, ctx, ndims, nrvars, problem, params, qpo=None, mbc=1):
         self.ctx = ctx
-        self.ndims, self.nrvars = ndims, nrvars
+        self.ndims, self.nrvars, self.mbc = ndims, nrvars, mbc
         h = ctypes.c_void_p()
         p = _da(params, len(params))
         q = _da(qpo if qpo is not None else [0.0] * nrvars, nrvars)
@@ -238,11 +253,11 @@ class Hierarchy:
     def regrid(self, params, qinit=None):
         """AMR regrid (bsamg_regrid): a new Hierarchy on the same context;
         this one is unchanged."""
-        cb = qinit_callback(qinit, self.ndims, self.nrvars) if qinit is not None else QINIT()
+        cb = qinit_callback(qinit, self.ndims, self.nrvars, self.mbc) if qinit is not None else QINIT()
         h = ctypes.c_void_p()
         _ck(lib().bsamg_regrid(self.h, ctypes.byref(params), cb, None, ctypes.byref(h)), "bsamg_regrid")
         new = Hierarchy.__new__(Hierarchy)
-        new.ctx, new.ndims, new.nrvars, new.h = self.ctx, self.ndims, self.nrvars, h
+        new.ctx, new.ndims, new.nrvars, new.mbc, new.h = self.ctx, self.ndims, self.nrvars, self.mbc, h
         return new
 
     def after_step_stats(self, finest):
@@ -269,7 +284,7 @@ class Hierarchy:
         _ck(lib().bsamg_read_q(self.h, os.fsencode(path), first_id, ctypes.byref(t), ctypes.byref(h)),
             "bsamg_read_q")
         new = Hierarchy.__new__(Hierarchy)
-        new.ctx, new.ndims, new.nrvars, new.h = self.ctx, self.ndims, self.nrvars, h
+        new.ctx, new.ndims, new.nrvars, new.mbc, new.h = self.ctx, self.ndims, self.nrvars, self.mbc, h
         return new, t.value
 
     def seed_spinodal(self, pid, seed, mean=0.0, amp=0.05):

@@ -883,7 +883,8 @@ int bx_cycle(Hier& H, int finest, int minlevel, int nsmooth, int errortype) {
 }  // namespace
 
 bool box_eligible(const Hier& H, bool periodic_single) {
-  if (H.problem != kCH || !periodic_single) return false;
+  // the box path's split/merge address q with one ghost layer
+  if (H.problem != kCH || !periodic_single || H.mbc != 1) return false;
   for (int l = H.minlevel; l <= H.maxlevel; l++) {
     const HostPatch& P = H.patches[H.L(l).patches[0]];
     for (int d = 0; d < H.ndims; d++) {

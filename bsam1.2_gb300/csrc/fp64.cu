@@ -144,17 +144,20 @@ __device__ __forceinline__ bool interior_cell(const int* mx, int t, int& i, int&
 }
 
 template <int DIM>
-__device__ __forceinline__ bool ghosted_cell(const int* n, int t, int& i, int& j, int& k) {
-  i = t % n[0];
+__device__ __forceinline__ bool ghosted_cell(const int* n, int gs, int t, int& i, int& j, int& k) {
+  // cell t of a ghosted array of extents n whose indices start at -gs
+  i = t % n[0] - gs;
   int r = t / n[0];
   if (DIM == 2) {
-    j = r;
+    j = r - gs;
     k = 0;
-    return j < n[1];
+    return r < n[1];
   }
-  j = r % n[1];
+  j = r % n[1] - gs;
   k = r / n[1];
-  return k < n[2];
+  bool ok = k < n[2];
+  k -= gs;
+  return ok;
 }
 
 // ---------------------------------------------------------------------------
@@ -282,10 +285,13 @@ __device__ __forceinline__ void u_coarse_ghost(const PatchDev* __restrict__ P, d
                                                int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  if (!ghosted_cell<DIM>(p.cn, b.start + tid, i, j, k)) return;
+  if (!ghosted_cell<DIM>(p.cn, p.gs, b.start + tid, i, j, k)) return;
+  // the first ring only (0 and cmx+1; a second layer, mbc = 2, is not set)
+  bool inside = i >= 0 && i <= p.cmx[0] + 1 && j >= 0 && j <= p.cmx[1] + 1 &&
+                (DIM == 2 || (k >= 0 && k <= p.cmx[2] + 1));
   bool ring = i == 0 || i == p.cmx[0] + 1 || j == 0 || j == p.cmx[1] + 1 ||
               (DIM == 3 && (k == 0 || k == p.cmx[2] + 1));
-  if (!ring) return;
+  if (!inside || !ring) return;
   const PatchDev& par = P[p.parent];
   long long src = gofs<DIM>(par.qn, p.mb[0] - 1 + i, p.mb[1] - 1 + j, DIM == 3 ? p.mb[2] - 1 + k : 0);
   long long dst = gofs<DIM>(p.cn, i, j, k);
@@ -350,13 +356,13 @@ __global__ void __launch_bounds__(kBlock) k_coarse_load(const PatchDev* __restri
 }
 
 // CorrectFine step 1, afasroutines.f90:892-895 / :934-938:
-// qc(0:cmx+1) = parent%q(mb-1:mb+1) - qc
+// qc(1-mbc:cmx+mbc) = parent%q(mb-mbc:mb+mbc) - qc
 template <int DIM>
 __device__ __forceinline__ void u_correct_a(const PatchDev* __restrict__ P, double* __restrict__ pool, const Blk b,
                                             int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  if (!ghosted_cell<DIM>(p.cn, b.start + tid, i, j, k)) return;
+  if (!ghosted_cell<DIM>(p.cn, p.gs, b.start + tid, i, j, k)) return;
   const PatchDev& par = P[p.parent];
   long long src = gofs<DIM>(par.qn, p.mb[0] - 1 + i, p.mb[1] - 1 + j, DIM == 3 ? p.mb[2] - 1 + k : 0);
   long long dst = gofs<DIM>(p.cn, i, j, k);
@@ -371,21 +377,27 @@ __global__ void __launch_bounds__(kBlock) k_correct_a(const PatchDev* __restrict
   u_correct_a<DIM>(P, pool, blk[blockIdx.x], threadIdx.x, nrvars);
 }
 
-// CorrectFine step 2: q(0:mx+1) += BiLinProlongationP1(qc)
-// (gridutilities.f90:156-195) / TriLinProlongationP1 (:510-566).  One
-// thread per coarse index (ci,cj,ck) in 0..cmx produces fine cells
-// 2ci..2ci+1 (and likewise in y, z): it forms the reference's intermediate
-// b (and c) entries for its 2x2(x2) coarse values with the reference's
-// expressions, so every fine value is bit-identical to the array form.
+// CorrectFine step 2: q(1-mbc:mx+mbc) += BiLinProlongationP1/P2(qc)
+// (gridutilities.f90:156-239) / TriLinProlongationP1/P2 (:510-625).  One
+// thread per coarse index (ci,cj,ck) in -gs..cmx+gs produces fine cells
+// 2ci..2ci+1 (and likewise in y, z) that lie in 1-mbc..mx+mbc: it forms
+// the reference's intermediate b (and c) entries for its 2x2(x2) coarse
+// values with the reference's expressions, so every fine value is
+// bit-identical to the array form.  P2 is P1 over one more layer; it
+// writes the odd cells' sum as 3 a(c+1) + a(c), the same IEEE sum.
 template <int DIM>
 __device__ __forceinline__ void u_correct_b(const PatchDev* __restrict__ P, double* __restrict__ pool, const Blk b,
                                             int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
-  int cpn[3] = {p.cmx[0] + 1, p.cmx[1] + 1, DIM == 3 ? p.cmx[2] + 1 : 1};
+  const int gs = p.gs;
+  int cpn[3] = {p.cmx[0] + 1 + 2 * gs, p.cmx[1] + 1 + 2 * gs, DIM == 3 ? p.cmx[2] + 1 + 2 * gs : 1};
   int t = b.start + tid;
   int ci = t % cpn[0], r = t / cpn[0];
   int cj = r % cpn[1], ck = r / cpn[1];
   if (ck >= cpn[2]) return;
+  ci -= gs;
+  cj -= gs;
+  if (DIM == 3) ck -= gs;
   const int nz = DIM == 3 ? 2 : 1;
   for (int v = 0; v < nrvars; v++) {
     const double* a = pool + p.oqc + v * p.sc;
@@ -401,6 +413,9 @@ __device__ __forceinline__ void u_correct_b(const PatchDev* __restrict__ P, doub
       for (int fy = 0; fy < 2; fy++)
         for (int fx = 0; fx < 2; fx++) {
           int i = 2 * ci + fx, j = 2 * cj + fy, k = DIM == 3 ? 2 * ck + fz : 0;
+          if (gs && (i < -gs || i > p.mx[0] + 1 + gs || j < -gs || j > p.mx[1] + 1 + gs ||
+                     (DIM == 3 && (k < -gs || k > p.mx[2] + 1 + gs))))
+            continue;
           double add;
           if (DIM == 2) {
             double blo = bxv[0][0][fx], bhi = bxv[0][1][fx];

@@ -332,6 +332,25 @@ int after_step_stats(Hier& H, int finest, double* integral, long long* meshsize)
   return BSAMG_OK;
 }
 
+// q(0:mx+1) of a patch's ghosted array a (all variables, any mbc): into
+// out (gather, when b is null) or from b back into a (scatter)
+void inner_cells(const Hier& H, const HostPatch& P, const double* a, const double* b, std::vector<double>& out,
+                 double* a_out = nullptr) {
+  int nd = H.ndims, s = H.mbc - 1;
+  int e[3] = {P.mx[0] + 2, P.mx[1] + 2, nd == 3 ? P.mx[2] + 2 : 1};
+  size_t cells = (size_t)e[0] * e[1] * e[2];
+  if (!b) out.resize(cells * H.nrvars);
+  size_t t = 0;
+  for (int v = 0; v < H.nrvars; v++)
+    for (int k = 0; k < e[2]; k++)
+      for (int j = 0; j < e[1]; j++)
+        for (int i = 0; i < e[0]; i++, t++) {
+          size_t c = (size_t)v * P.sq + ((size_t)(nd == 3 ? k + s : 0) * P.qn[1] + (j + s)) * P.qn[0] + (i + s);
+          if (b) a_out[c] = b[t];
+          else out[t] = a[c];
+        }
+}
+
 int write_q(Hier& H, const char* path, double time, int finest) {
   if (!H.committed || !path || finest < 0 || finest > kMaxDepth) return BSAMG_ERR_ARG;
   int r = set_device(H);
@@ -341,13 +360,18 @@ int write_q(Hier& H, const char* path, double time, int finest) {
   FILE* f = std::fopen(path, "wb");
   if (!f) return io_fail("cannot open the frame file for writing");
   bool ok = write_head(f, time, finest);
+  std::vector<double> inner;
   for (int l = 0; l <= finest && ok; l++)
     for (int p : H.L(l).patches) {
       const HostPatch& P = H.patches[p];
       double xu[3];
       for (int d = 0; d < 3; d++) xu[d] = xupper_of(H, P, d);
-      ok = ok && write_block(f, H.ndims, H.nrvars, P.level, P.dx, P.xlower, xu, P.mx, P.mglobal,
-                             q.data() + (P.oq - H.q_region));
+      const double* src = q.data() + (P.oq - H.q_region);
+      if (H.mbc > 1) {  // the records are q(0:mx+1) (OutputQ, :114-126)
+        inner_cells(H, P, src, nullptr, inner);
+        src = inner.data();
+      }
+      ok = ok && write_block(f, H.ndims, H.nrvars, P.level, P.dx, P.xlower, xu, P.mx, P.mglobal, src);
     }
   if (std::fclose(f) != 0) ok = false;
   return ok ? BSAMG_OK : io_fail("writing the frame file failed");
@@ -376,11 +400,14 @@ int write_uniform_q(Hier& H, const char* path, double time, int finest) {
   double* buf[2] = {nullptr, nullptr};
   cudaError_t e = dev_alloc(H, (void**)&buf[0], fine_elems * sizeof(double));
   if (e == cudaSuccess) e = dev_alloc(H, (void**)&buf[1], fine_elems * sizeof(double));
-  // uniform level 0 = the root's q, ghost layers included
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(buf[0], H.pool + R.oq, ghosted(n) * nv * sizeof(double), cudaMemcpyDeviceToDevice, H.s);
+  // uniform level 0 = the root's q(0:mx+1) (bsaminputoutput.f90:476-480)
+  int launches = 0;
+  if (e == cudaSuccess) {
+    int g[3] = {1, 1, 1}, un[3] = {n[0] + 2, n[1] + 2, nd == 3 ? n[2] + 2 : 1};
+    launches += launch_uniform_scatter(H.s, nd, H.pool, R.oq + origin_of(H, R.qn), R.sq, R.qn, R.mx, g, buf[0], un, nv);
+  }
   double dx[3] = {R.dx[0], R.dx[1], R.dx[2]};
-  int cur = 0, launches = 0;
+  int cur = 0;
   for (int l = 1; l <= finest && e == cudaSuccess; l++) {
     int m[3] = {2 * n[0], 2 * n[1], nd == 3 ? 2 * n[2] : 1};
     size_t cs = ghosted(n), fs = ghosted(m);
@@ -391,7 +418,8 @@ int write_uniform_q(Hier& H, const char* path, double time, int finest) {
     for (int p : H.L(l).patches) {  // CopyPatchToUniformGrid, in visiting order
       const HostPatch& P = H.patches[p];
       int g[3] = {P.mglobal[0][0], P.mglobal[1][0], P.mglobal[2][0]};
-      launches += launch_uniform_scatter(H.s, nd, H.pool, P.oq, P.sq, P.qn, g, buf[1 - cur], un, nv);
+      launches += launch_uniform_scatter(H.s, nd, H.pool, P.oq + origin_of(H, P.qn), P.sq, P.qn, P.mx, g, buf[1 - cur],
+                                         un, nv);
     }
     cur = 1 - cur;
     std::memcpy(n, m, sizeof(n));
@@ -594,15 +622,30 @@ parsed:
       continue;
     }
     size_t d0 = blocks[block_of[p]].data;
+    // the records are q(0:mx+1) (ReadQ2D/3D, :392-440): with mbc = 1 the
+    // whole ghosted array, else its inner part; the second layer keeps the
+    // persisting patch's values (a new patch's are zero)
+    std::vector<double> inner, none;
+    if (N.mbc > 1 && D.level <= 0 && root.id2idx.count(D.id)) {
+      const HostPatch& S = root.patches[root.id2idx.at(D.id)];
+      std::memcpy(dq, rq.data() + (S.oq - root.q_region), plane * nv * sizeof(double));
+    }
+    size_t recs = (size_t)(D.mx[0] + 2) * (D.mx[1] + 2) * (N.ndims == 3 ? D.mx[2] + 2 : 1);
+    double* tgt = dq;
+    if (N.mbc > 1) {
+      inner.resize(recs * nv);
+      tgt = inner.data();
+    }
     int nt = host_threads();
     std::vector<char> okt(nt, 1);
     parallel(nt, [&](int t, int n) {
-      size_t a = plane * t / n, b = plane * (t + 1) / n;
+      size_t a = recs * t / n, b = recs * (t + 1) / n;
       for (size_t c = a; c < b; c++)
         for (int v = 0; v < nv; v++)
-          if (!get_real(T, d0 + c, 27 * v, &dq[(size_t)v * plane + c])) okt[t] = 0;
+          if (!get_real(T, d0 + c, 27 * v, &tgt[(size_t)v * recs + c])) okt[t] = 0;
     });
     for (char o : okt) bad = bad || !o;
+    if (N.mbc > 1) inner_cells(N, D, nullptr, inner.data(), none, dq);
   }
   if (bad) return fail(io_fail("frame file: bad data record"));
   cudaError_t e =
@@ -611,9 +654,12 @@ parsed:
   for (size_t p = 0; p < geo.size() && e == cudaSuccess; p++) {
     const HostPatch& D = N.patches[p];
     size_t bytes = (size_t)D.sq * nv * sizeof(double);
-    if (D.level <= 0) {
+    if (D.level <= 0) {  // the persisting levels keep qold and qc
       const HostPatch& S = root.patches[root.id2idx.at(D.id)];
       e = cudaMemcpyAsync(N.pool + D.oqold, root.pool + S.oqold, bytes, cudaMemcpyDeviceToDevice, N.s);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(N.pool + D.oqc, root.pool + S.oqc, (size_t)D.sc * nv * sizeof(double),
+                            cudaMemcpyDeviceToDevice, N.s);
     } else {
       e = cudaMemcpyAsync(N.pool + D.oqold, N.pool + D.oq, bytes, cudaMemcpyDeviceToDevice, N.s);
     }
@@ -658,7 +704,7 @@ int bsamg_seed_spinodal(bsamg_hier* h, int id, unsigned long long seed, double m
   const HostPatch& P = h->patches[it->second];
   int r = set_device(*h);
   if (r) return r;
-  int n = launch_seed_spinodal(h->s, h->ndims, h->pool + P.oq, P.sq, P.mx, seed, mean, amp, h->pp.eps2, P.dx[0]);
+  int n = launch_seed_spinodal(h->s, h->ndims, h->mbc, h->pool + P.oq, P.sq, P.mx, seed, mean, amp, h->pp.eps2, P.dx[0]);
   return after_launch(*h, n);
 }
 

@@ -36,12 +36,18 @@ struct Emitter {
   std::vector<Em> out;
   explicit Emitter(const Hier& h) : H(h) {}
 
+  // offset of Fortran cell (i,j,k) from cell (0,0,0) of a q plane (the
+  // device tables address q from that cell; negative in the second ghost
+  // layer when mbc = 2)
   int cell(int p, int i, int j, int k) const {
     const HostPatch& P = H.patches[p];
     if (H.ndims == 2) return j * P.qn[0] + i;
     return (k * P.qn[1] + j) * P.qn[0] + i;
   }
-  static int64_t key(int p, int c) { return ((int64_t)p << 32) | (uint32_t)c; }
+  // (patch, cell) key; the cell counted from the array's start (>= 0)
+  int64_t key(int p, int c) const {
+    return ((int64_t)p << 32) | (uint32_t)(c + origin_of(H, H.patches[p].qn));
+  }
 
   void copy(int type, int dp, int dc, int sp, int sc) {
     Em e{};

@@ -185,9 +185,10 @@ int fp_prepare_tail(Hier& H, int finest, int minlevel, int nsmooth) {
       const HostPatch& P = H.patches[p];
       if (P.level < minlevel || P.level > start) continue;
       PatchDev& D = shadow[p];
-      D.oq = add(D.oq, (long long)H.nrvars * P.sq, 1);
-      D.oqold = add(D.oqold, (long long)H.nrvars * P.sq, 0);
-      D.oqc = add(D.oqc, (long long)H.nrvars * P.sc, 1);
+      long long zq = origin_of(H, P.qn), zc = origin_of(H, P.cn);  // staged from the arrays' starts
+      D.oq = add(P.oq, (long long)H.nrvars * P.sq, 1) + zq;
+      D.oqold = add(P.oqold, (long long)H.nrvars * P.sq, 0) + zq;
+      D.oqc = add(P.oqc, (long long)H.nrvars * P.sc, 1) + zc;
       D.of = add(D.of, (long long)H.nrvars * P.sf, 1);
       D.orf = add(D.orf, (long long)H.nrvars * P.sf, 1);
     }
@@ -584,9 +585,11 @@ int upload_blocks(Hier& H, LevelT& L, int kind) {
       case kKindCoarse: units = P.parent >= 0 ? (long long)P.cmx[0] * P.cmx[1] * P.cmx[2] : 0; break;
       case kKindCGhost: units = P.parent >= 0 ? (long long)P.cn[0] * P.cn[1] * P.cn[2] : 0; break;
       case kKindFGhost: units = (long long)P.qn[0] * P.qn[1] * P.qn[2]; break;
-      case kKindProl:
-        units = P.parent >= 0 ? (long long)(P.cmx[0] + 1) * (P.cmx[1] + 1) * (H.ndims == 3 ? P.cmx[2] + 1 : 1) : 0;
+      case kKindProl: {  // coarse indices -gs..cmx+gs, gs = mbc - 1
+        int e = 2 * (H.mbc - 1) + 1;
+        units = P.parent >= 0 ? (long long)(P.cmx[0] + e) * (P.cmx[1] + e) * (H.ndims == 3 ? P.cmx[2] + e : 1) : 0;
         break;
+      }
     }
     for (long long s = 0; s < units; s += kBlock) v.push_back(Blk{p, (int)s});
   }
@@ -602,20 +605,25 @@ int upload_blocks(Hier& H, LevelT& L, int kind) {
 
 // every cell an operation touches must lie inside its patch's ghosted
 // plane (parent plane for the coarse cells of C/F operations)
+// every cell a ghost program touches lies in its patch's q plane (cells are
+// counted from cell (0,0,0), which sits origin_of() into the plane)
 bool ghost_ops_in_bounds(const Hier& H, const GhostProg& g) {
   int np = (int)H.patches.size();
   for (const GhostOp& o : g.ops) {
     if (o.dp < 0 || o.dp >= np || o.sp < 0 || o.sp >= np) return false;
-    long long nd = H.patches[o.dp].sq, ns = H.patches[o.sp].sq;
-    if (o.dcell < 0 || o.dcell >= nd) return false;
+    const HostPatch &D = H.patches[o.dp], &S = H.patches[o.sp];
+    long long zd = origin_of(H, D.qn), zs = origin_of(H, S.qn);
+    auto in_d = [&](long long c) { return c + zd >= 0 && c + zd < D.sq; };
+    auto in_s = [&](long long c) { return c + zs >= 0 && c + zs < S.sq; };
+    if (!in_d(o.dcell)) return false;
     if (o.type <= kGBC) {
-      if (o.s0 < 0 || o.s0 >= ns) return false;
+      if (!in_s(o.s0)) return false;
     } else {
-      if (o.s0 < 0 || o.s0 >= nd || o.s1 < 0 || o.s1 >= nd) return false;
+      if (!in_d(o.s0) || !in_d(o.s1)) return false;
       int nc = o.type == kGCfA ? 1 : (o.type == kGCfAB ? 3 : 4);
       int c[4] = {o.c0, o.c1, o.c2, o.c3};
       for (int x = 0; x < nc; x++)
-        if (c[x] < 0 || c[x] >= ns) return false;
+        if (!in_s(c[x])) return false;
     }
   }
   return true;
@@ -722,9 +730,11 @@ int commit(Hier& H) {
     }
     D.parent = P.parent;
     D.level = P.level;
-    D.oq = P.oq; D.oqold = P.oqold; D.oqc = P.oqc; D.of = P.of; D.orf = P.orf; D.oftmp = P.oftmp;
+    D.gs = H.mbc - 1;
+    long long zq = origin_of(H, P.qn), zc = origin_of(H, P.cn);
+    D.oq = P.oq + zq; D.oqold = P.oqold + zq; D.oqc = P.oqc + zc; D.of = P.of; D.orf = P.orf; D.oftmp = P.oftmp;
     D.sq = P.sq; D.sc = P.sc; D.sf = P.sf;
-    D.eq = P.e_oq; D.ecq = P.e_oqc; D.eg = P.e_of; D.ephi = P.e_ophi;
+    D.eq = P.e_oq + zq; D.ecq = P.e_oqc + zc; D.eg = P.e_of; D.ephi = P.e_ophi;
     D.h = P.dx[0];
     coefficients(H, P.dx[0], D.c);
     for (int x = 0; x < 4; x++) D.cf[x] = (float)D.c[x];
@@ -914,7 +924,7 @@ int bsamg_hier_create(bsamg_ctx* ctx, int ndims, int nrvars, int mbc, int proble
                       int nparams, const double* qpo, bsamg_hier** out) {
   if (!ctx || !out || !params) return BSAMG_ERR_ARG;
   if (ndims < 2 || ndims > 3) return BSAMG_ERR_ARG;
-  if (mbc != 1) return BSAMG_ERR_UNSUPPORTED;
+  if (mbc < 1 || mbc > 2) return BSAMG_ERR_UNSUPPORTED;  // RootInit, bsamroutines.f90:305-308
   if (problem_kind != BSAMG_PROBLEM_CH && problem_kind != BSAMG_PROBLEM_BIOGROWTH &&
       problem_kind != BSAMG_PROBLEM_GROWTH)
     return BSAMG_ERR_ARG;

@@ -162,6 +162,13 @@ void coefficients(const Hier& H, double h, double* c);
 int build_tables(Hier& H);
 // xupper of a patch as the reference's frame files carry it (frames.cpp)
 double xupper_of(const Hier& H, const HostPatch& P, int d);
+// Offset of Fortran cell (0,0,0) from the start of a ghosted q-like (n =
+// qn) or qc-like (n = cn) plane: 0 for mbc = 1, one cell of each used
+// dimension's stride for mbc = 2 (the arrays start at index 1 - mbc).
+inline long long origin_of(const Hier& H, const int* n) {
+  long long s = H.mbc - 1;
+  return H.ndims == 2 ? s * (1 + n[0]) : s * (1 + n[0] + (long long)n[0] * n[1]);
+}
 // AMR regrid of a committed hierarchy into a new one (regrid.cpp)
 int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* user, bsamg_hier** out);
 using GraphKey = std::tuple<int, int, int, int, int>;

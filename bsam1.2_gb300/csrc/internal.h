@@ -31,12 +31,17 @@ struct PatchDev {
   int mb[3];   // lower mbounds in the parent (1-based)
   int parent;  // index into the patch table, -1 if none
   int level;
-  int pad;
-  long long oq, oqold, oqc, of, orf, oftmp;  // element offsets into the pool
+  int gs;      // mbc - 1: the ghosted arrays start at Fortran index -gs
+  // element offsets into the pool; for the ghosted arrays (q, qold, qc) the
+  // offset of Fortran cell (0,0,0) of variable 1, so that a cell's offset
+  // is the same expression whatever mbc is (negative indices reach the
+  // second ghost layer when mbc = 2)
+  long long oq, oqold, oqc, of, orf, oftmp;
   long long sq, sc, sf;                      // elements per variable plane
-  // mixed path, offsets into the FP32 pool: correction e (ghosted, like q),
-  // its coarse image ec (like qc), correction right-hand side g (interior,
-  // like f) and the frozen base phase field phib (interior, one plane)
+  // mixed path, offsets into the FP32 pool: correction e (ghosted, like q;
+  // the offset of cell (0,0,0) as above), its coarse image ec (like qc),
+  // correction right-hand side g (interior, like f) and the frozen base
+  // phase field phib (interior, one plane)
   long long eq, ecq, eg, ephi;
   // Plugin coefficients for this patch's spacing, computed on the host with
   // the reference's expressions (CH/problem.f90:339-347, :411-413,

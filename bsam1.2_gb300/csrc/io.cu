@@ -184,25 +184,27 @@ __global__ void __launch_bounds__(256) k_uni_prolong(const double* __restrict__ 
   F[t] = v;
 }
 
-// CopyPatchToUniformGrid: one patch's ghosted q (all variables) into the
-// uniform block U ((un0 x un1 x un2) per variable, planes of uplane) at
-// global cell mglobal - 1
+// CopyPatchToUniformGrid (bsaminputoutput.f90:543-572): q(0:mx+1) of one
+// patch (all variables) into the uniform block U ((un0 x un1 x un2) per
+// variable, planes of uplane) at global cell mglobal - 1.  oq is the offset
+// of the patch's cell (0,0,0), qn its ghosted extents (any mbc).
 template <int DIM>
 __global__ void __launch_bounds__(256) k_uni_scatter(const double* __restrict__ pool, long long oq, long long sq,
-                                                     int qn0, int qn1, int qn2, int g0, int g1, int g2,
+                                                     int qn0, int qn1, int e0, int e1, int e2, int g0, int g1, int g2,
                                                      double* __restrict__ U, int un0, int un1, long long uplane,
                                                      int nv) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long cells = (long long)qn0 * qn1 * qn2;
+  long long cells = (long long)e0 * e1 * e2;
   if (t >= cells * nv) return;
   int v = (int)(t / cells);
   long long c = t % cells;
-  int i = (int)(c % qn0);
-  long long r = c / qn0;
-  int j = (int)(r % qn1);
-  int k = (int)(r / qn1);
+  int i = (int)(c % e0);
+  long long r = c / e0;
+  int j = (int)(r % e1);
+  int k = (int)(r / e1);
   long long u = ((long long)(DIM == 3 ? g2 - 1 + k : 0) * un1 + (g1 - 1 + j)) * un0 + (g0 - 1 + i);
-  U[v * uplane + u] = pool[oq + v * sq + c];
+  long long src = ((long long)(DIM == 3 ? k : 0) * qn1 + j) * qn0 + i;
+  U[v * uplane + u] = pool[oq + v * sq + src];
 }
 
 // splitmix64 of the seeded inputs: U(-1,1) from splitmix64(seed ^ (g * golden))
@@ -220,19 +222,20 @@ __device__ __forceinline__ double seeded_pm1(unsigned long long seed, unsigned l
 // evaluates it: phi = mean + amp*U on the cell's index within the patch
 // (i fastest), mu = ((phi*phi*phi) - phi) - eps2 * lap, lap =
 // ((-2 d) phi + (phi[i-1] + phi[i+1]) + ...) / (h*h) with the neighbours
-// wrapped over the patch; ghost layers zero.
+// wrapped over the patch; ghost layers (mbc = gs + 1 of them) zero.  q is
+// the array's start, t runs over its ghosted cells.
 template <int DIM>
 __global__ void __launch_bounds__(256) k_seed_spinodal(double* __restrict__ q, long long sq, int m0, int m1, int m2,
-                                                       unsigned long long seed, double mean, double amp, double eps2,
-                                                       double hh) {
+                                                       int gs, unsigned long long seed, double mean, double amp,
+                                                       double eps2, double hh) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int n0 = m0 + 2, n1 = m1 + 2, n2 = DIM == 3 ? m2 + 2 : 1;
+  const int n0 = m0 + 2 + 2 * gs, n1 = m1 + 2 + 2 * gs, n2 = DIM == 3 ? m2 + 2 + 2 * gs : 1;
   if (t >= (long long)n0 * n1 * n2) return;
-  int i = (int)(t % n0);
+  int i = (int)(t % n0) - gs;
   long long r = t / n0;
-  int j = (int)(r % n1);
-  int k = DIM == 3 ? (int)(r / n1) : 1;
-  bool ghost = i == 0 || i == n0 - 1 || j == 0 || j == n1 - 1 || (DIM == 3 && (k == 0 || k == n2 - 1));
+  int j = (int)(r % n1) - gs;
+  int k = DIM == 3 ? (int)(r / n1) - gs : 1;
+  bool ghost = i < 1 || i > m0 || j < 1 || j > m1 || (DIM == 3 && (k < 1 || k > m2));
   if (ghost) {
     q[t] = 0.0;
     q[sq + t] = 0.0;
@@ -258,12 +261,13 @@ __global__ void __launch_bounds__(256) k_seed_spinodal(double* __restrict__ q, l
 
 }  // namespace
 
-int launch_seed_spinodal(cudaStream_t s, int ndims, double* q, long long sq, const int mx[3], unsigned long long seed,
-                         double mean, double amp, double eps2, double h) {
-  long long n = (long long)(mx[0] + 2) * (mx[1] + 2) * (ndims == 3 ? mx[2] + 2 : 1);
+int launch_seed_spinodal(cudaStream_t s, int ndims, int mbc, double* q, long long sq, const int mx[3],
+                         unsigned long long seed, double mean, double amp, double eps2, double h) {
+  long long n = (long long)(mx[0] + 2 * mbc) * (mx[1] + 2 * mbc) * (ndims == 3 ? mx[2] + 2 * mbc : 1);
   unsigned grid = (unsigned)((n + 255) / 256);
-  if (ndims == 2) k_seed_spinodal<2><<<grid, 256, 0, s>>>(q, sq, mx[0], mx[1], 1, seed, mean, amp, eps2, h);
-  else k_seed_spinodal<3><<<grid, 256, 0, s>>>(q, sq, mx[0], mx[1], mx[2], seed, mean, amp, eps2, h);
+  int gs = mbc - 1;
+  if (ndims == 2) k_seed_spinodal<2><<<grid, 256, 0, s>>>(q, sq, mx[0], mx[1], 1, gs, seed, mean, amp, eps2, h);
+  else k_seed_spinodal<3><<<grid, 256, 0, s>>>(q, sq, mx[0], mx[1], mx[2], gs, seed, mean, amp, eps2, h);
   return 1;
 }
 
@@ -295,16 +299,17 @@ int launch_uniform_prolong(cudaStream_t s, int ndims, const double* A, double* F
 }
 
 int launch_uniform_scatter(cudaStream_t s, int ndims, const double* pool, long long oq, long long sq, const int qn[3],
-                           const int g[3], double* U, const int un[3], int nv) {
-  long long cells = (long long)qn[0] * qn[1] * qn[2] * nv;
+                           const int mx[3], const int g[3], double* U, const int un[3], int nv) {
+  int e[3] = {mx[0] + 2, mx[1] + 2, ndims == 3 ? mx[2] + 2 : 1};
+  long long cells = (long long)e[0] * e[1] * e[2] * nv;
   unsigned grid = (unsigned)((cells + 255) / 256);
   long long uplane = (long long)un[0] * un[1] * un[2];
   if (ndims == 2)
-    k_uni_scatter<2><<<grid, 256, 0, s>>>(pool, oq, sq, qn[0], qn[1], qn[2], g[0], g[1], g[2], U, un[0], un[1],
-                                          uplane, nv);
+    k_uni_scatter<2><<<grid, 256, 0, s>>>(pool, oq, sq, qn[0], qn[1], e[0], e[1], e[2], g[0], g[1], g[2], U, un[0],
+                                          un[1], uplane, nv);
   else
-    k_uni_scatter<3><<<grid, 256, 0, s>>>(pool, oq, sq, qn[0], qn[1], qn[2], g[0], g[1], g[2], U, un[0], un[1],
-                                          uplane, nv);
+    k_uni_scatter<3><<<grid, 256, 0, s>>>(pool, oq, sq, qn[0], qn[1], e[0], e[1], e[2], g[0], g[1], g[2], U, un[0],
+                                          un[1], uplane, nv);
   return 1;
 }
 

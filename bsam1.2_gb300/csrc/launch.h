@@ -26,7 +26,7 @@ enum Kind : int {
   kKindCoarse = 2,    // one coarse cell under a child: cmx1*cmx2*cmx3
   kKindCGhost = 3,    // one ghosted coarse cell: (cmx+2)^d
   kKindFGhost = 4,    // one ghosted fine cell: (mx+2)^d
-  kKindProl = 5,      // one coarse index 0..cmx per dimension under a child: (cmx+1)^d
+  kKindProl = 5,      // one coarse index -gs..cmx+gs per dimension under a child: (cmx+1+2gs)^d
   kNKind = 6
 };
 
@@ -81,11 +81,12 @@ int launch_stats_finish(cudaStream_t s, const double* partial, int n, double* ou
 // F = mass-corrected prolongation of the uniform (n+2)^d block A (one variable)
 int launch_uniform_prolong(cudaStream_t s, int ndims, const double* A, double* F, const int n[3]);
 // the seeded spinodal start of one CH patch (q: its ghosted q, two planes of sq)
-int launch_seed_spinodal(cudaStream_t s, int ndims, double* q, long long sq, const int mx[3], unsigned long long seed,
+int launch_seed_spinodal(cudaStream_t s, int ndims, int mbc, double* q, long long sq, const int mx[3], unsigned long long seed,
                          double mean, double amp, double eps2, double h);
-// a patch's ghosted q (nv variables) into the uniform block U (extents un)
+// a patch's q(0:mx+1) (nv variables; oq the offset of its cell (0,0,0))
+// into the uniform block U (extents un)
 int launch_uniform_scatter(cudaStream_t s, int ndims, const double* pool, long long oq, long long sq, const int qn[3],
-                           const int g[3], double* U, const int un[3], int nv);
+                           const int mx[3], const int g[3], double* U, const int un[3], int nv);
 int launch_ghost_program_1cta(const LaunchCtx& c, const GhostOp* ops,
                               const int* stage_off, int nstages);
 // the recorded coarse tail of an FP64 V-cycle, one block

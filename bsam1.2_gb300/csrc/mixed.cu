@@ -79,17 +79,20 @@ __device__ __forceinline__ bool interior_cell(const int* mx, int t, int& i, int&
   return k <= mx[2];
 }
 template <int DIM>
-__device__ __forceinline__ bool ghosted_cell(const int* n, int t, int& i, int& j, int& k) {
-  i = t % n[0];
+__device__ __forceinline__ bool ghosted_cell(const int* n, int gs, int t, int& i, int& j, int& k) {
+  // cell t of a ghosted array of extents n whose indices start at -gs
+  i = t % n[0] - gs;
   int r = t / n[0];
   if (DIM == 2) {
-    j = r;
+    j = r - gs;
     k = 0;
-    return j < n[1];
+    return r < n[1];
   }
-  j = r % n[1];
+  j = r % n[1] - gs;
   k = r / n[1];
-  return k < n[2];
+  bool ok = k < n[2];
+  k -= gs;
+  return ok;
 }
 
 template <int DIM, typename T>
@@ -240,7 +243,10 @@ __device__ __forceinline__ void u_coarse_ring(const PatchDev* __restrict__ P, fl
                                               int tid, int nrvars, int corr) {
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  if (!ghosted_cell<DIM>(p.cn, b.start + tid, i, j, k)) return;
+  if (!ghosted_cell<DIM>(p.cn, p.gs, b.start + tid, i, j, k)) return;
+  // the correction cycle keeps one ghost layer whatever mbc is: its
+  // operators read one layer, and its second layer of e stays zero
+  if (i < 0 || i > p.cmx[0] + 1 || j < 0 || j > p.cmx[1] + 1 || (DIM == 3 && (k < 0 || k > p.cmx[2] + 1))) return;
   if (!corr) {
     bool ring = i == 0 || i == p.cmx[0] + 1 || j == 0 || j == p.cmx[1] + 1 ||
                 (DIM == 3 && (k == 0 || k == p.cmx[2] + 1));
@@ -316,11 +322,18 @@ template <int DIM>
 __device__ __forceinline__ void u_prolong(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
                                           int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
-  int cpn[3] = {p.cmx[0] + 1, p.cmx[1] + 1, DIM == 3 ? p.cmx[2] + 1 : 1};
+  // the units cover coarse indices -gs..cmx+gs (as CorrectFine's); the
+  // correction cycle prolongs over one ghost layer (0..cmx)
+  const int gs = p.gs;
+  int cpn[3] = {p.cmx[0] + 1 + 2 * gs, p.cmx[1] + 1 + 2 * gs, DIM == 3 ? p.cmx[2] + 1 + 2 * gs : 1};
   int t = b.start + tid;
   int ci = t % cpn[0], r = t / cpn[0];
   int cj = r % cpn[1], ck = r / cpn[1];
   if (ck >= cpn[2]) return;
+  ci -= gs;
+  cj -= gs;
+  if (DIM == 3) ck -= gs;
+  if (ci < 0 || ci > p.cmx[0] || cj < 0 || cj > p.cmx[1] || (DIM == 3 && (ck < 0 || ck > p.cmx[2]))) return;
   const int nz = DIM == 3 ? 2 : 1;
   for (int v = 0; v < nrvars; v++) {
     const float* a = fpool + p.ecq + v * p.sc;
@@ -367,7 +380,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_update(const PatchDev* __restrict
   const Blk b = blk[blockIdx.x];
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  if (!ghosted_cell<DIM>(p.qn, b.start + threadIdx.x, i, j, k)) return;
+  if (!ghosted_cell<DIM>(p.qn, p.gs, b.start + threadIdx.x, i, j, k)) return;
   bool interior = i >= 1 && i <= p.mx[0] && j >= 1 && j <= p.mx[1] && (DIM == 2 || (k >= 1 && k <= p.mx[2]));
   long long c = gofs<DIM>(p.qn, i, j, k);
   for (int v = 0; v < nrvars; v++) {
@@ -950,8 +963,9 @@ int mx_prepare_tail(Hier& H, int finest, int minlevel, int nsmooth) {
     const HostPatch& P = H.patches[p];
     if (P.level < minlevel || P.level > start) continue;
     PatchDev& D = shadow[p];
-    D.eq = add(D.eq, (long long)H.nrvars * P.sq, 1);
-    D.ecq = add(D.ecq, (long long)H.nrvars * P.sc, 1);
+    long long zq = origin_of(H, P.qn), zc = origin_of(H, P.cn);  // staged from the arrays' starts
+    D.eq = add(P.e_oq, (long long)H.nrvars * P.sq, 1) + zq;
+    D.ecq = add(P.e_oqc, (long long)H.nrvars * P.sc, 1) + zc;
     D.eg = add(D.eg, (long long)H.nrvars * P.sf, 1);
     D.ephi = add(D.ephi, nbase * P.sf, 0);
   }

@@ -34,13 +34,16 @@ struct Model {
   std::vector<HostPatch> g;            // geometry, in visiting order
   std::vector<std::vector<double>> q;  // ghosted q of levels >= 0 (empty below)
   std::vector<std::vector<double>> qold;
+  std::vector<std::vector<double>> qc;  // ghosted qc of new patches (InitFields)
   std::vector<int> src_idx;            // index in src, or -1 for new patches
   explicit Model(const Hier& h) : src(h) {}
   int nd() const { return src.ndims; }
   size_t nq(const HostPatch& P) const { return (size_t)P.qn[0] * P.qn[1] * P.qn[2]; }
+  // q(i,j,k,v) with Fortran indices i, j (and k in 3D; 0 in 2D)
   double& Q(int p, int i, int j, int k, int v) {
     const HostPatch& P = g[p];
-    return q[p][(((size_t)v * P.qn[2] + k) * P.qn[1] + j) * P.qn[0] + i];
+    int s = src.mbc - 1, sk = src.ndims == 3 ? s : 0;
+    return q[p][(((size_t)v * P.qn[2] + k + sk) * P.qn[1] + j + s) * P.qn[0] + i + s];
   }
 };
 
@@ -73,9 +76,9 @@ int host_set_ghost(Model& M, int level) {
   const double c1 = 09.0 / 16.0, c2 = 03.0 / 16.0, c3 = 03.0 / 16.0, c4 = 01.0 / 16.0;
   for (const GhostOp& o : ops) {
     if (M.q[o.dp].empty() || M.q[o.sp].empty()) return BSAMG_ERR_ARG;  // below-root data is not on the host
-    for (int v = 0; v < M.src.nrvars; v++) {
-      double* dq = M.q[o.dp].data() + v * M.nq(M.g[o.dp]);
-      const double* sq = M.q[o.sp].data() + v * M.nq(M.g[o.sp]);
+    for (int v = 0; v < M.src.nrvars; v++) {  // cells are counted from cell (0,0,0)
+      double* dq = M.q[o.dp].data() + origin_of(M.src, M.g[o.dp].qn) + v * M.nq(M.g[o.dp]);
+      const double* sq = M.q[o.sp].data() + origin_of(M.src, M.g[o.sp].qn) + v * M.nq(M.g[o.sp]);
       double val;
       switch (o.type) {
         case kGCopy: val = sq[o.s0]; break;
@@ -331,27 +334,33 @@ void split_long(int nd, int maxside, std::vector<Sub>& subs) {
     }
 }
 
-// BiLin/TriLinProlongationP1MC (gridutilities.f90:242-369, :628-727): a is
-// the coarse block with one ghost layer (cmx+2 per dimension), out the fine
-// block with one ghost layer (2*cmx+2)
-void prolong_mc(int nd, const std::vector<double>& a, const int cmx[3], double* out) {
-  int cn0 = cmx[0] + 2, cn1 = cmx[1] + 2, cn2 = nd == 3 ? cmx[2] + 2 : 1;
-  int fn0 = 2 * cmx[0] + 2, fn1 = 2 * cmx[1] + 2;
-  auto A = [&](int i, int j, int k) { return a[((size_t)k * cn1 + j) * cn0 + i]; };
-  auto O = [&](int i, int j, int k) -> double& { return out[((size_t)k * fn1 + j) * fn0 + i]; };
+// BiLin/TriLinProlongationP1MC and P2MC (gridutilities.f90:242-369,
+// :628-829): a is the coarse block with mbc ghost layers (cmx+2 mbc per
+// dimension, index 1-mbc first), out the fine block with mbc ghost layers.
+// Fine cell 2c takes 3 a(c) + a(c+1) and fine cell 2c+1 takes a(c) +
+// 3 a(c+1) in each direction (x, then y, then z; the last divided by 16 or
+// 64; P2 writes the odd cells' sum as 3 a(c+1) + a(c), the same IEEE sum),
+// then each interior coarse cell's mass correction goes to its 2^d cells.
+void prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double* out) {
+  const int L = 1 - mbc, kL = nd == 3 ? L : 0;
+  const int cn0 = cmx[0] + 2 * mbc, cn1 = cmx[1] + 2 * mbc, cn2 = nd == 3 ? cmx[2] + 2 * mbc : 1;
+  const int fn0 = 2 * cmx[0] + 2 * mbc, fn1 = 2 * cmx[1] + 2 * mbc, fn2 = nd == 3 ? 2 * cmx[2] + 2 * mbc : 1;
+  auto lo = [](int f) { return (f - (f & 1)) / 2; };  // f = 2c or 2c+1 -> c
+  auto A = [&](int i, int j, int k) { return a[((size_t)(k - kL) * cn1 + (j - L)) * cn0 + (i - L)]; };
+  auto O = [&](int i, int j, int k) -> double& { return out[((size_t)(k - kL) * fn1 + (j - L)) * fn0 + (i - L)]; };
   std::vector<double> b((size_t)fn0 * cn1 * cn2);
-  auto Bx = [&](int i, int j, int k) -> double& { return b[((size_t)k * cn1 + j) * fn0 + i]; };
-  for (int k = 0; k < cn2; k++)
-    for (int j = 0; j < cn1; j++)
-      for (int I = 0; I <= cmx[0]; I++) {
-        Bx(2 * I, j, k) = 3.0 * A(I, j, k) + A(I + 1, j, k);
-        Bx(2 * I + 1, j, k) = A(I, j, k) + 3.0 * A(I + 1, j, k);
+  auto Bx = [&](int i, int j, int k) -> double& { return b[((size_t)(k - kL) * cn1 + (j - L)) * fn0 + (i - L)]; };
+  for (int k = kL; k < kL + cn2; k++)
+    for (int j = L; j < L + cn1; j++)
+      for (int i = L; i < L + fn0; i++) {
+        int c = lo(i);
+        Bx(i, j, k) = (i & 1) ? A(c, j, k) + 3.0 * A(c + 1, j, k) : 3.0 * A(c, j, k) + A(c + 1, j, k);
       }
   if (nd == 2) {
-    for (int J = 0; J <= cmx[1]; J++)
-      for (int i = 0; i < fn0; i++) {
-        O(i, 2 * J, 0) = (3.0 * Bx(i, J, 0) + Bx(i, J + 1, 0)) / 16.0;
-        O(i, 2 * J + 1, 0) = (Bx(i, J, 0) + 3.0 * Bx(i, J + 1, 0)) / 16.0;
+    for (int j = L; j < L + fn1; j++)
+      for (int i = L; i < L + fn0; i++) {
+        int c = lo(j);
+        O(i, j, 0) = (j & 1) ? (Bx(i, c, 0) + 3.0 * Bx(i, c + 1, 0)) / 16.0 : (3.0 * Bx(i, c, 0) + Bx(i, c + 1, 0)) / 16.0;
       }
     for (int J = 1; J <= cmx[1]; J++)
       for (int I = 1; I <= cmx[0]; I++) {
@@ -365,18 +374,18 @@ void prolong_mc(int nd, const std::vector<double>& a, const int cmx[3], double* 
     return;
   }
   std::vector<double> c((size_t)fn0 * fn1 * cn2);
-  auto Cy = [&](int i, int j, int k) -> double& { return c[((size_t)k * fn1 + j) * fn0 + i]; };
-  for (int k = 0; k < cn2; k++)
-    for (int J = 0; J <= cmx[1]; J++)
-      for (int i = 0; i < fn0; i++) {
-        Cy(i, 2 * J, k) = 3.0 * Bx(i, J, k) + Bx(i, J + 1, k);
-        Cy(i, 2 * J + 1, k) = Bx(i, J, k) + 3.0 * Bx(i, J + 1, k);
+  auto Cy = [&](int i, int j, int k) -> double& { return c[((size_t)(k - kL) * fn1 + (j - L)) * fn0 + (i - L)]; };
+  for (int k = kL; k < kL + cn2; k++)
+    for (int j = L; j < L + fn1; j++)
+      for (int i = L; i < L + fn0; i++) {
+        int cj = lo(j);
+        Cy(i, j, k) = (j & 1) ? Bx(i, cj, k) + 3.0 * Bx(i, cj + 1, k) : 3.0 * Bx(i, cj, k) + Bx(i, cj + 1, k);
       }
-  for (int K = 0; K <= cmx[2]; K++)
-    for (int j = 0; j < fn1; j++)
-      for (int i = 0; i < fn0; i++) {
-        O(i, j, 2 * K) = (3.0 * Cy(i, j, K) + Cy(i, j, K + 1)) / 64.0;
-        O(i, j, 2 * K + 1) = (Cy(i, j, K) + 3.0 * Cy(i, j, K + 1)) / 64.0;
+  for (int k = L; k < L + fn2; k++)
+    for (int j = L; j < L + fn1; j++)
+      for (int i = L; i < L + fn0; i++) {
+        int ck = lo(k);
+        O(i, j, k) = (k & 1) ? (Cy(i, j, ck) + 3.0 * Cy(i, j, ck + 1)) / 64.0 : (3.0 * Cy(i, j, ck) + Cy(i, j, ck + 1)) / 64.0;
       }
   for (int K = 1; K <= cmx[2]; K++)
     for (int J = 1; J <= cmx[1]; J++)
@@ -421,31 +430,35 @@ void make_new_grid(Model& M, int p, const Box& b, int id, const bsamg_regrid_par
     if (P.mthbc[2 * n] < kInternalBC && C.mbounds[n][0] == 1) C.mthbc[2 * n] = P.mthbc[2 * n];
     if (P.mthbc[2 * n + 1] < kInternalBC && C.mbounds[n][1] == P.mx[n]) C.mthbc[2 * n + 1] = P.mthbc[2 * n + 1];
   }
+  const int mbc = M.src.mbc;
   for (int d = 0; d < 3; d++) {
     C.cmx[d] = d < nd ? C.mx[d] / 2 : 1;
-    C.qn[d] = d < nd ? C.mx[d] + 2 : 1;
-    C.cn[d] = d < nd ? C.cmx[d] + 2 : 1;
+    C.qn[d] = d < nd ? C.mx[d] + 2 * mbc : 1;
+    C.cn[d] = d < nd ? C.cmx[d] + 2 * mbc : 1;
   }
-  size_t nq = (size_t)C.qn[0] * C.qn[1] * C.qn[2];
-  std::vector<double> q(nq * M.src.nrvars, 0.0);
+  size_t nq = (size_t)C.qn[0] * C.qn[1] * C.qn[2], nc = (size_t)C.cn[0] * C.cn[1] * C.cn[2];
+  std::vector<double> q(nq * M.src.nrvars, 0.0), qc(nc * M.src.nrvars, 0.0);  // AllocFields' zero fill
   if (prm.initial) {
     qinit(user, C.level, C.mx, C.dx, C.xlower, q.data());
   } else {
+    // child%qc(1-mbc:cmx+mbc) = parent%q(mb-mbc:mb+mbc) (:1815-1818,
+    // :1834-1837), then child%q(1-mbc:mx+mbc) = P1MC / P2MC(child%qc)
     int cmx[3] = {C.cmx[0], C.cmx[1], nd == 3 ? C.cmx[2] : 0};
-    int k0 = nd == 3 ? b[2][0] - 1 : 0, k1 = nd == 3 ? b[2][1] + 1 : 0;  // ghost-shifted third index
-    std::vector<double> a;
+    int k0 = nd == 3 ? b[2][0] - mbc : 0, k1 = nd == 3 ? b[2][1] + mbc : 0;
     for (int v = 0; v < M.src.nrvars; v++) {
-      a.clear();
+      size_t t = v * nc;
       for (int k = k0; k <= k1; k++)
-        for (int j = b[1][0] - 1; j <= b[1][1] + 1; j++)
-          for (int i = b[0][0] - 1; i <= b[0][1] + 1; i++) a.push_back(M.Q(p, i, j, k, v));
-      prolong_mc(nd, a, cmx, q.data() + v * nq);
+        for (int j = b[1][0] - mbc; j <= b[1][1] + mbc; j++)
+          for (int i = b[0][0] - mbc; i <= b[0][1] + mbc; i++) qc[t++] = M.Q(p, i, j, k, v);
+      prolong_mc(nd, mbc, qc.data() + v * nc, cmx, q.data() + v * nq);
     }
   }
   M.g.push_back(C);
   M.src_idx.push_back(-1);
   M.qold.push_back(q);  // child%qold = child%q (:1782)
   M.q.push_back(std::move(q));
+  M.qc.resize(M.g.size());
+  M.qc.back() = std::move(qc);
 }
 
 // TransferOverlap (:1919-1951): interior q of src onto dst
@@ -458,10 +471,11 @@ void transfer_overlap(int nrvars, const HostPatch& S, const std::vector<double>&
     if (hi[d] < lo[d]) return;
   }
   size_t ns = (size_t)S.qn[0] * S.qn[1] * S.qn[2], ndd = (size_t)D.qn[0] * D.qn[1] * D.qn[2];
-  int ko = nd == 3 ? 1 : 0;
+  // local Fortran index = global - mglobal + 1; the arrays start at 1 - mbc
+  int g = (int)((D.qn[0] - D.mx[0]) / 2), ko = nd == 3 ? g : 0;
   auto at = [&](const HostPatch& P, int i, int j, int k) {
-    return ((size_t)(k - P.mglobal[2][0] + ko) * P.qn[1] + (j - P.mglobal[1][0] + 1)) * P.qn[0] +
-           (i - P.mglobal[0][0] + 1);
+    return ((size_t)(k - P.mglobal[2][0] + ko) * P.qn[1] + (j - P.mglobal[1][0] + g)) * P.qn[0] +
+           (i - P.mglobal[0][0] + g);
   };
   for (int v = 0; v < nrvars; v++)
     for (int k = lo[2]; k <= hi[2]; k++)
@@ -479,10 +493,16 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   if (r) return r;
   int nd = H.ndims, nv = H.nrvars;
   Model M(H);
-  // one copy of the whole q region (every patch, ghosts included)
+  // one copy of the whole q region (every patch, ghosts included) and one
+  // of the qc region (the persisting patches keep their qc, whose second
+  // ring, mbc = 2, carries the last correction)
   std::vector<double> qreg((size_t)H.q_len);
+  const long long qc0 = H.patches[0].oqc, qc1 = H.patches[0].of;  // the qc region lies before f
+  std::vector<double> qcreg((size_t)(qc1 - qc0));
   cudaError_t ce = cudaMemcpyAsync(qreg.data(), H.pool + H.q_region, qreg.size() * sizeof(double),
                                    cudaMemcpyDeviceToHost, H.s);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(qcreg.data(), H.pool + qc0, qcreg.size() * sizeof(double), cudaMemcpyDeviceToHost, H.s);
   if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(regrid download)");
   ce = cudaStreamSynchronize(H.s);
   if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize(regrid)");
@@ -612,10 +632,26 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
     }
     if (M.src_idx[p] < 0) std::memcpy(oimg.data() + (D.oq - N.q_region), M.qold[p].data(), n * sizeof(double));
   }
+  // qc: the persisting patches' own, InitFields' for the new ones
+  const long long nqc0 = N.patches[0].oqc, nqc1 = N.patches[0].of;
+  std::vector<double> cimg((size_t)(nqc1 - nqc0), 0.0);
+  M.qc.resize(M.g.size());
+  for (size_t p = 0; p < M.g.size(); p++) {
+    const HostPatch& D = N.patches[p];
+    size_t n = (size_t)D.sc * nv;
+    if (M.src_idx[p] >= 0) {
+      const HostPatch& S = H.patches[M.src_idx[p]];
+      std::memcpy(cimg.data() + (D.oqc - nqc0), qcreg.data() + (S.oqc - qc0), n * sizeof(double));
+    } else if (M.qc[p].size() == n) {
+      std::memcpy(cimg.data() + (D.oqc - nqc0), M.qc[p].data(), n * sizeof(double));
+    }
+  }
   ce = cudaMemcpyAsync(N.pool + N.q_region, qimg.data(), qimg.size() * sizeof(double), cudaMemcpyHostToDevice, N.s);
   if (ce == cudaSuccess)
     ce = cudaMemcpyAsync(N.pool + N.qold_region, oimg.data(), oimg.size() * sizeof(double), cudaMemcpyHostToDevice,
                          N.s);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(N.pool + nqc0, cimg.data(), cimg.size() * sizeof(double), cudaMemcpyHostToDevice, N.s);
   for (size_t p = 0; p < M.g.size() && ce == cudaSuccess; p++)
     if (M.src_idx[p] >= 0) {
       const HostPatch& D = N.patches[p];

@@ -96,7 +96,7 @@ int bsamg_ctx_set_blocking_wait(bsamg_ctx* ctx, int on);
 
 /* Hierarchy.  params: [0]=dt [1]=eps, then for BIOGROWTH [2]=gamma
  * [3]=lambda [4]=czero.  qpo: nrvars quasi-periodic offsets (nodeinfodef
- * qpo), may be NULL.  Only mbc = 1 is supported. */
+ * qpo), may be NULL.  mbc = 1 or 2 ghost layers (RootInit's range). */
 int bsamg_hier_create(bsamg_ctx* ctx, int ndims, int nrvars, int mbc,
                       int problem_kind, const double* params, int nparams,
                       const double* qpo, bsamg_hier** out);
@@ -134,8 +134,9 @@ typedef struct {
   double qtolerance[11];
   double desiredfillratio[11];
 } bsamg_regrid_params;
-/* Fill the interior of q (ghosted Fortran layout, nrvars variables) of a
- * new patch with the initial condition (the plugin's QInit2D/3D). */
+/* Fill q (ghosted Fortran layout q(1-mbc:mx+mbc, ...), nrvars variables;
+ * zero on entry) of a new patch with the initial condition (the plugin's
+ * QInit2D/3D). */
 typedef void (*bsamg_qinit_fn)(void* user, int level, const int* mx, const double* dx, const double* xlower,
                                double* q);
 int bsamg_regrid(bsamg_hier* h, const bsamg_regrid_params* prm, bsamg_qinit_fn qinit, void* user,

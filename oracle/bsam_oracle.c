@@ -108,7 +108,7 @@ int bsamo_create(int ndims, int nrvars, int mbc, int problem,
   if (!out) return -1;
   if (ndims < 2 || ndims > 3) return -2;
   if (nrvars < 1 || nrvars > 10) return -2;
-  if (mbc != 1) return -2; /* mbc = 2 (P2 prolongation) not restated */
+  if (mbc < 1 || mbc > 2) return -2; /* RootInit, bsamroutines.f90:305-308 */
   if (problem != BSAMO_PROBLEM_CH && problem != BSAMO_PROBLEM_BIOGROWTH &&
       problem != BSAMO_PROBLEM_GROWTH)
     return -2;
@@ -1270,68 +1270,78 @@ static void coarse_loading(bsamo_hier* h, OPatch* p) {
       }
 }
 
-/* CorrectFine, afasroutines.f90:860-980 with BiLinProlongationP1
- * (gridutilities.f90:156-195) / TriLinProlongationP1 (:510-566). */
+/* CorrectFine, afasroutines.f90:860-980: qc(1-mbc:cmx+mbc) = parent%q -
+ * qc, then q(1-mbc:mx+mbc) += P(qc) with BiLinProlongationP1/P2
+ * (gridutilities.f90:156-239) or TriLinProlongationP1/P2 (:510-625).  P2 is
+ * P1's stencil over one more layer: fine cell 2c takes 3 a(c) + a(c+1) and
+ * fine cell 2c+1 takes a(c) + 3 a(c+1) in each direction, x first, then y
+ * (and z), dividing by 16 (64) in the last direction.  P2 writes the odd
+ * cells' sum as 3 a(c+1) + a(c), the same IEEE sum.  The second ring of qc
+ * is written only here and by InitFields, so it carries the previous
+ * correction into the next (as the reference's does). */
 static void correct_fine(bsamo_hier* h, OPatch* p) {
   OPatch* par = parent_of(h, p);
-  int nd = h->ndims;
+  int nd = h->ndims, mbc = h->mbc, L = 1 - mbc;
   int c0 = p->cmx[0], c1 = p->cmx[1], c2 = nd == 3 ? p->cmx[2] : 1;
   int mb0 = p->mbounds[0][0], mb1 = p->mbounds[1][0], mb2 = nd == 3 ? p->mbounds[2][0] : 1;
-  int klo = nd == 3 ? 0 : 1, khi = nd == 3 ? c2 + 1 : 1;
+  int klo = nd == 3 ? L : 1, khi = nd == 3 ? c2 + mbc : 1;
   for (int v = 0; v < h->nrvars; v++)
     for (int k = klo; k <= khi; k++)
-      for (int j = 0; j <= c1 + 1; j++)
-        for (int i = 0; i <= c0 + 1; i++)
+      for (int j = L; j <= c1 + mbc; j++)
+        for (int i = L; i <= c0 + mbc; i++)
           QC(p, i, j, k, v) =
               Q(par, mb0 - 1 + i, mb1 - 1 + j, nd == 3 ? mb2 - 1 + k : 1, v) - QC(p, i, j, k, v);
-  int m0 = p->mx[0], m1 = p->mx[1], m2 = nd == 3 ? p->mx[2] : 1;
+  int m0 = p->mx[0], m1 = p->mx[1];
+  /* fine and coarse extents of the prolongation's arrays, index L first */
+  int fn0 = m0 + 2 * mbc, fn1 = m1 + 2 * mbc, cn1 = c1 + 2 * mbc, cn2 = nd == 3 ? c2 + 2 * mbc : 1;
+  /* fine index f -> its lower coarse index c (f = 2c or 2c+1) */
+#define CLO(f) (((f) - ((f) & 1)) / 2)
   if (nd == 2) {
-    size_t nb = (size_t)(m0 + 2) * (c1 + 2);
-    double* b = (double*)malloc(sizeof(double) * nb);
-#define B(i, j) b[(size_t)(j) * (m0 + 2) + (i)]
+    double* b = (double*)malloc(sizeof(double) * (size_t)fn0 * cn1);
+#define B(i, j) b[(size_t)((j) - L) * fn0 + ((i) - L)]
     for (int v = 0; v < h->nrvars; v++) {
-      for (int cj = 0; cj <= c1 + 1; cj++)
-        for (int c = 0; c <= c0; c++) {
-          B(2 * c, cj) = 3.0 * QC(p, c, cj, 1, v) + QC(p, c + 1, cj, 1, v);
-          B(2 * c + 1, cj) = QC(p, c, cj, 1, v) + 3.0 * QC(p, c + 1, cj, 1, v);
+      for (int cj = L; cj <= c1 + mbc; cj++)
+        for (int i = L; i <= m0 + mbc; i++) {
+          int c = CLO(i);
+          B(i, cj) = (i & 1) ? QC(p, c, cj, 1, v) + 3.0 * QC(p, c + 1, cj, 1, v)
+                             : 3.0 * QC(p, c, cj, 1, v) + QC(p, c + 1, cj, 1, v);
         }
-      for (int c = 0; c <= c1; c++)
-        for (int i = 0; i <= m0 + 1; i++) {
-          double pe = (3.0 * B(i, c) + B(i, c + 1)) / 16.0;
-          double po = (B(i, c) + 3.0 * B(i, c + 1)) / 16.0;
-          Q(p, i, 2 * c, 1, v) = Q(p, i, 2 * c, 1, v) + pe;
-          Q(p, i, 2 * c + 1, 1, v) = Q(p, i, 2 * c + 1, 1, v) + po;
+      for (int j = L; j <= m1 + mbc; j++)
+        for (int i = L; i <= m0 + mbc; i++) {
+          int c = CLO(j);
+          double pv = (j & 1) ? (B(i, c) + 3.0 * B(i, c + 1)) / 16.0 : (3.0 * B(i, c) + B(i, c + 1)) / 16.0;
+          Q(p, i, j, 1, v) = Q(p, i, j, 1, v) + pv;
         }
     }
 #undef B
     free(b);
   } else {
-    size_t nb = (size_t)(m0 + 2) * (c1 + 2) * (c2 + 2);
-    size_t ncc = (size_t)(m0 + 2) * (m1 + 2) * (c2 + 2);
-    double* b = (double*)malloc(sizeof(double) * nb);
-    double* cc = (double*)malloc(sizeof(double) * ncc);
-#define B(i, j, k) b[((size_t)(k) * (c1 + 2) + (j)) * (m0 + 2) + (i)]
-#define CC(i, j, k) cc[((size_t)(k) * (m1 + 2) + (j)) * (m0 + 2) + (i)]
+    int m2 = p->mx[2];
+    double* b = (double*)malloc(sizeof(double) * (size_t)fn0 * cn1 * cn2);
+    double* cc = (double*)malloc(sizeof(double) * (size_t)fn0 * fn1 * cn2);
+#define B(i, j, k) b[((size_t)((k) - L) * cn1 + ((j) - L)) * fn0 + ((i) - L)]
+#define CC(i, j, k) cc[((size_t)((k) - L) * fn1 + ((j) - L)) * fn0 + ((i) - L)]
     for (int v = 0; v < h->nrvars; v++) {
-      for (int ck = 0; ck <= c2 + 1; ck++)
-        for (int cj = 0; cj <= c1 + 1; cj++)
-          for (int c = 0; c <= c0; c++) {
-            B(2 * c, cj, ck) = 3.0 * QC(p, c, cj, ck, v) + QC(p, c + 1, cj, ck, v);
-            B(2 * c + 1, cj, ck) = QC(p, c, cj, ck, v) + 3.0 * QC(p, c + 1, cj, ck, v);
+      for (int ck = L; ck <= c2 + mbc; ck++)
+        for (int cj = L; cj <= c1 + mbc; cj++)
+          for (int i = L; i <= m0 + mbc; i++) {
+            int c = CLO(i);
+            B(i, cj, ck) = (i & 1) ? QC(p, c, cj, ck, v) + 3.0 * QC(p, c + 1, cj, ck, v)
+                                   : 3.0 * QC(p, c, cj, ck, v) + QC(p, c + 1, cj, ck, v);
           }
-      for (int ck = 0; ck <= c2 + 1; ck++)
-        for (int c = 0; c <= c1; c++)
-          for (int i = 0; i <= m0 + 1; i++) {
-            CC(i, 2 * c, ck) = 3.0 * B(i, c, ck) + B(i, c + 1, ck);
-            CC(i, 2 * c + 1, ck) = B(i, c, ck) + 3.0 * B(i, c + 1, ck);
+      for (int ck = L; ck <= c2 + mbc; ck++)
+        for (int j = L; j <= m1 + mbc; j++)
+          for (int i = L; i <= m0 + mbc; i++) {
+            int c = CLO(j);
+            CC(i, j, ck) = (j & 1) ? B(i, c, ck) + 3.0 * B(i, c + 1, ck) : 3.0 * B(i, c, ck) + B(i, c + 1, ck);
           }
-      for (int c = 0; c <= c2; c++)
-        for (int j = 0; j <= m1 + 1; j++)
-          for (int i = 0; i <= m0 + 1; i++) {
-            double pe = (3.0 * CC(i, j, c) + CC(i, j, c + 1)) / 64.0;
-            double po = (CC(i, j, c) + 3.0 * CC(i, j, c + 1)) / 64.0;
-            Q(p, i, j, 2 * c, v) = Q(p, i, j, 2 * c, v) + pe;
-            Q(p, i, j, 2 * c + 1, v) = Q(p, i, j, 2 * c + 1, v) + po;
+      for (int k = L; k <= m2 + mbc; k++)
+        for (int j = L; j <= m1 + mbc; j++)
+          for (int i = L; i <= m0 + mbc; i++) {
+            int c = CLO(k);
+            double pv = (k & 1) ? (CC(i, j, c) + 3.0 * CC(i, j, c + 1)) / 64.0
+                                : (3.0 * CC(i, j, c) + CC(i, j, c + 1)) / 64.0;
+            Q(p, i, j, k, v) = Q(p, i, j, k, v) + pv;
           }
     }
 #undef B
@@ -1339,7 +1349,7 @@ static void correct_fine(bsamo_hier* h, OPatch* p) {
     free(b);
     free(cc);
   }
-  (void)m2;
+#undef CLO
 }
 
 /* AFASVcycle, afasroutines.f90:495-529 */
@@ -1361,6 +1371,23 @@ static void afas_vcycle(bsamo_hier* h, int level, int minlevel, int nsmooth) {
 int bsamo_vcycle(bsamo_hier* h, int level, int minlevel, int nsmooth) {
   if (!h || !h->committed) return -1;
   afas_vcycle(h, level, minlevel, nsmooth);
+  return 0;
+}
+
+/* ApplyOnLevel(level, CorrectFine) alone (afasroutines.f90:518) */
+int bsamo_correct_fine(bsamo_hier* h, int level) {
+  if (!h || !h->committed || level < -MAXDEPTH || level > MAXDEPTH) return -1;
+  for (int n = 0; n < nlev(h, level); n++)
+    if (lev_patch(h, level, n)->parent < 0) return -1;
+  for (int n = 0; n < nlev(h, level); n++) correct_fine(h, lev_patch(h, level, n));
+  return 0;
+}
+
+static void prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double* out);
+/* one variable of P1MC / P2MC (InitFields' prolongation) alone */
+int bsamo_prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double* out) {
+  if ((nd != 2 && nd != 3) || mbc < 1 || mbc > 2 || !a || !cmx || !out) return -1;
+  prolong_mc(nd, mbc, a, cmx, out);
   return 0;
 }
 
@@ -1820,27 +1847,32 @@ static int split_long(int nd, int maxside, int (*sub)[3][2], int ng, int cap) {
   return ng;
 }
 
-/* BiLinProlongationP1MC / TriLinProlongationP1MC (gridutilities.f90:242-369,
- * :628-727): a = coarse values with one ghost layer, cn = cmx+2 per
- * dimension; out = fine values with one ghost layer, fn = 2*cmx+2. */
-static void prolong_mc(int nd, const double* a, const int cmx[3], double* out) {
-  int cn0 = cmx[0] + 2, cn1 = cmx[1] + 2, cn2 = nd == 3 ? cmx[2] + 2 : 1;
-  int fn0 = 2 * cmx[0] + 2, fn1 = 2 * cmx[1] + 2, fn2 = nd == 3 ? 2 * cmx[2] + 2 : 1;
-#define A(i, j, k) a[((size_t)(k) * cn1 + (j)) * cn0 + (i)]
-#define O(i, j, k) out[((size_t)(k) * fn1 + (j)) * fn0 + (i)]
+/* BiLin/TriLinProlongationP1MC and P2MC (gridutilities.f90:242-369,
+ * :628-829): a is the coarse block with mbc ghost layers (cmx+2 mbc per
+ * dimension, index 1-mbc first), out the fine block with mbc ghost layers.
+ * The prolongation is CorrectFine's (P2: one more layer); the mass
+ * correction of each coarse interior cell goes to its 2^d fine cells. */
+static void prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double* out) {
+  int L = 1 - mbc;
+  int cn0 = cmx[0] + 2 * mbc, cn1 = cmx[1] + 2 * mbc, cn2 = nd == 3 ? cmx[2] + 2 * mbc : 1;
+  int fn0 = 2 * cmx[0] + 2 * mbc, fn1 = 2 * cmx[1] + 2 * mbc, fn2 = nd == 3 ? 2 * cmx[2] + 2 * mbc : 1;
+  int kL = nd == 3 ? L : 0;
+#define A(i, j, k) a[((size_t)((k) - kL) * cn1 + ((j) - L)) * cn0 + ((i) - L)]
+#define O(i, j, k) out[((size_t)((k) - kL) * fn1 + ((j) - L)) * fn0 + ((i) - L)]
+#define CLO(f) (((f) - ((f) & 1)) / 2)
   double* b = (double*)malloc(sizeof(double) * fn0 * cn1 * cn2);
-#define Bx(i, j, k) b[((size_t)(k) * cn1 + (j)) * fn0 + (i)]
-  for (int k = 0; k < cn2; k++)
-    for (int j = 0; j < cn1; j++)
-      for (int I = 0; I <= cmx[0]; I++) {
-        Bx(2 * I, j, k) = 3.0 * A(I, j, k) + A(I + 1, j, k);
-        Bx(2 * I + 1, j, k) = A(I, j, k) + 3.0 * A(I + 1, j, k);
+#define Bx(i, j, k) b[((size_t)((k) - kL) * cn1 + ((j) - L)) * fn0 + ((i) - L)]
+  for (int k = kL; k < kL + cn2; k++)
+    for (int j = L; j < L + cn1; j++)
+      for (int i = L; i < L + fn0; i++) {
+        int c = CLO(i);
+        Bx(i, j, k) = (i & 1) ? A(c, j, k) + 3.0 * A(c + 1, j, k) : 3.0 * A(c, j, k) + A(c + 1, j, k);
       }
   if (nd == 2) {
-    for (int J = 0; J <= cmx[1]; J++)
-      for (int i = 0; i < fn0; i++) {
-        O(i, 2 * J, 0) = (3.0 * Bx(i, J, 0) + Bx(i, J + 1, 0)) / 16.0;
-        O(i, 2 * J + 1, 0) = (Bx(i, J, 0) + 3.0 * Bx(i, J + 1, 0)) / 16.0;
+    for (int j = L; j < L + fn1; j++)
+      for (int i = L; i < L + fn0; i++) {
+        int c = CLO(j);
+        O(i, j, 0) = (j & 1) ? (Bx(i, c, 0) + 3.0 * Bx(i, c + 1, 0)) / 16.0 : (3.0 * Bx(i, c, 0) + Bx(i, c + 1, 0)) / 16.0;
       }
     for (int J = 1; J <= cmx[1]; J++)
       for (int I = 1; I <= cmx[0]; I++) {
@@ -1853,18 +1885,19 @@ static void prolong_mc(int nd, const double* a, const int cmx[3], double* out) {
       }
   } else {
     double* c = (double*)malloc(sizeof(double) * fn0 * fn1 * cn2);
-#define Cy(i, j, k) c[((size_t)(k) * fn1 + (j)) * fn0 + (i)]
-    for (int k = 0; k < cn2; k++)
-      for (int J = 0; J <= cmx[1]; J++)
-        for (int i = 0; i < fn0; i++) {
-          Cy(i, 2 * J, k) = 3.0 * Bx(i, J, k) + Bx(i, J + 1, k);
-          Cy(i, 2 * J + 1, k) = Bx(i, J, k) + 3.0 * Bx(i, J + 1, k);
+#define Cy(i, j, k) c[((size_t)((k) - kL) * fn1 + ((j) - L)) * fn0 + ((i) - L)]
+    for (int k = kL; k < kL + cn2; k++)
+      for (int j = L; j < L + fn1; j++)
+        for (int i = L; i < L + fn0; i++) {
+          int cj = CLO(j);
+          Cy(i, j, k) = (j & 1) ? Bx(i, cj, k) + 3.0 * Bx(i, cj + 1, k) : 3.0 * Bx(i, cj, k) + Bx(i, cj + 1, k);
         }
-    for (int K = 0; K <= cmx[2]; K++)
-      for (int j = 0; j < fn1; j++)
-        for (int i = 0; i < fn0; i++) {
-          O(i, j, 2 * K) = (3.0 * Cy(i, j, K) + Cy(i, j, K + 1)) / 64.0;
-          O(i, j, 2 * K + 1) = (Cy(i, j, K) + 3.0 * Cy(i, j, K + 1)) / 64.0;
+    for (int k = L; k < L + fn2; k++)
+      for (int j = L; j < L + fn1; j++)
+        for (int i = L; i < L + fn0; i++) {
+          int ck = CLO(k);
+          O(i, j, k) = (k & 1) ? (Cy(i, j, ck) + 3.0 * Cy(i, j, ck + 1)) / 64.0
+                               : (3.0 * Cy(i, j, ck) + Cy(i, j, ck + 1)) / 64.0;
         }
     for (int K = 1; K <= cmx[2]; K++)
       for (int J = 1; J <= cmx[1]; J++)
@@ -1886,6 +1919,7 @@ static void prolong_mc(int nd, const double* a, const int cmx[3], double* out) {
 #undef A
 #undef O
 #undef Bx
+#undef CLO
 }
 
 /* MakeNewGrid (:1663-1784) + InitFields (:1787-1856); returns the index */
@@ -1919,19 +1953,20 @@ static int make_new_grid(bsamo_hier* h, int pidx, int mbp[3][2], int id, const b
   if (prm->initial) {
     qinit(user, ch->level, ch->mx, ch->dx, ch->xlower, ch->q);
   } else {
+    /* child%qc(1-mbc:cmx+mbc) = parent%q(mb-mbc:mb+mbc), then
+     * child%q(1-mbc:mx+mbc) = P1MC / P2MC(child%qc) (:1815-1850) */
+    int mbc = h->mbc;
     int cmx[3] = {ch->cmx[0], ch->cmx[1], nd == 3 ? ch->cmx[2] : 0};
-    size_t na = (size_t)(cmx[0] + 2) * (cmx[1] + 2) * (nd == 3 ? cmx[2] + 2 : 1);
+    size_t nc = (size_t)ch->cn[0] * ch->cn[1] * ch->cn[2];
     size_t nfine = (size_t)ch->qn[0] * ch->qn[1] * ch->qn[2];
-    double* a = (double*)malloc(sizeof(double) * na);
     for (int v = 0; v < h->nrvars; v++) {
-      size_t t = 0;
-      int k0 = nd == 3 ? mb[2][0] - 1 : 1, k1 = nd == 3 ? mb[2][1] + 1 : 1;
+      int k0 = nd == 3 ? 1 - mbc : 1, k1 = nd == 3 ? cmx[2] + mbc : 1;
       for (int k = k0; k <= k1; k++)
-        for (int j = mb[1][0] - 1; j <= mb[1][1] + 1; j++)
-          for (int i = mb[0][0] - 1; i <= mb[0][1] + 1; i++) a[t++] = Q(par, i, j, k, v);
-      prolong_mc(nd, a, cmx, ch->q + v * nfine);
+        for (int j = 1 - mbc; j <= cmx[1] + mbc; j++)
+          for (int i = 1 - mbc; i <= cmx[0] + mbc; i++)
+            QC(ch, i, j, k, v) = Q(par, mb[0][0] - 1 + i, mb[1][0] - 1 + j, nd == 3 ? mb[2][0] - 1 + k : 1, v);
+      prolong_mc(nd, mbc, ch->qc + v * nc, cmx, ch->q + v * nfine);
     }
-    free(a);
   }
   /* child%rf = parent%rf = child%f = parent%f = 0 (:1773-1776); SetSrc is
    * empty for CH; child%qold = child%q (:1782) */
@@ -2223,7 +2258,15 @@ int bsamo_write_q(const bsamo_hier* h, const char* path, double time, int finest
         mg[d][0] = p->mglobal[d][0];
         mg[d][1] = p->mglobal[d][1];
       }
-      write_block(f, h->ndims, h->nrvars, p->level, p->dx, p->xlower, xu, p->mx, mg, p->q);
+      /* q(0:mx+1) (OutputQ, :114-126), whatever mbc is */
+      size_t cells = (size_t)(p->mx[0] + 2) * (p->mx[1] + 2) * (h->ndims == 3 ? p->mx[2] + 2 : 1), t = 0;
+      double* qb = (double*)malloc(sizeof(double) * cells * h->nrvars);
+      for (int v = 0; v < h->nrvars; v++)
+        for (int k = h->ndims == 3 ? 0 : 1; k <= (h->ndims == 3 ? p->mx[2] + 1 : 1); k++)
+          for (int j = 0; j <= p->mx[1] + 1; j++)
+            for (int i = 0; i <= p->mx[0] + 1; i++) qb[t++] = Q(p, i, j, k, v);
+      write_block(f, h->ndims, h->nrvars, p->level, p->dx, p->xlower, xu, p->mx, mg, qb);
+      free(qb);
     }
   return fclose(f) ? -8 : 0;
 }
@@ -2243,24 +2286,32 @@ int bsamo_write_uniform_q(const bsamo_hier* h, const char* path, double time, in
   double dx[3] = {r->dx[0], r->dx[1], r->dx[2]};
   size_t sz = (size_t)(n[0] + 2) * (n[1] + 2) * (nd == 3 ? n[2] + 2 : 1);
   double* u = (double*)malloc(sizeof(double) * sz * nv);
-  memcpy(u, r->q, sizeof(double) * sz * nv);
+  /* the root's q(0:mx+1): the uniform grids keep one ghost layer whatever
+   * mbc is (bsaminputoutput.f90:476-480) */
+  {
+    size_t t = 0;
+    for (int v = 0; v < nv; v++)
+      for (int k = nd == 3 ? 0 : 1; k <= (nd == 3 ? n[2] + 1 : 1); k++)
+        for (int j = 0; j <= n[1] + 1; j++)
+          for (int i = 0; i <= n[0] + 1; i++) u[t++] = Q(r, i, j, k, v);
+  }
   for (int level = 1; level <= finest; level++) {
     int nf[3] = {2 * n[0], 2 * n[1], nd == 3 ? 2 * n[2] : 1};
     size_t szf = (size_t)(nf[0] + 2) * (nf[1] + 2) * (nd == 3 ? nf[2] + 2 : 1);
     double* uf = (double*)malloc(sizeof(double) * szf * nv);
     int cmx[3] = {n[0], n[1], nd == 3 ? n[2] : 0};
-    for (int v = 0; v < nv; v++) prolong_mc(nd, u + v * sz, cmx, uf + v * szf);
+    for (int v = 0; v < nv; v++) prolong_mc(nd, 1, u + v * sz, cmx, uf + v * szf);
     for (int d = 0; d < nd; d++) dx[d] = dx[d] / 2.0;
     for (int a = 0; a < nlev(h, level); a++) { /* CopyPatchToUniformGrid */
       const OPatch* p = &h->p[h->lev_list[level + MAXDEPTH][a]];
       int k0 = nd == 3 ? p->mglobal[2][0] - 1 : 0;
-      for (int v = 0; v < nv; v++)
-        for (int k = 0; k < p->qn[2]; k++)
-          for (int j = 0; j < p->qn[1]; j++)
-            for (int i = 0; i < p->qn[0]; i++)
+      int kh = nd == 3 ? p->mx[2] + 1 : 0;
+      for (int v = 0; v < nv; v++)  /* q(0:mx+1) (:566-570) */
+        for (int k = 0; k <= kh; k++)
+          for (int j = 0; j <= p->mx[1] + 1; j++)
+            for (int i = 0; i <= p->mx[0] + 1; i++)
               uf[v * szf + ((size_t)(k0 + k) * (nf[1] + 2) + (p->mglobal[1][0] - 1 + j)) * (nf[0] + 2) +
-                 (p->mglobal[0][0] - 1 + i)] =
-                  p->q[(((size_t)v * p->qn[2] + k) * p->qn[1] + j) * p->qn[0] + i];
+                 (p->mglobal[0][0] - 1 + i)] = Q(p, i, j, nd == 3 ? k : 1, v);
     }
     free(u);
     u = uf;
@@ -2483,11 +2534,16 @@ int bsamo_read_q(const bsamo_hier* root, const char* path, int first_id, double*
         int c = add_live_patch(h, level, next_id++, par, mx, mg, mb, thbc, dx, xl);
         tgt = &h->p[c];
       }
+      /* q(0:mx+1) (ReadQ2D/3D, :392-440), whatever mbc is */
       size_t plane = (size_t)tgt->qn[0] * tgt->qn[1] * tgt->qn[2];
-      if (ln + plane > L.nlines) goto fail;
-      for (size_t c = 0; c < plane; c++, ln++)
-        for (int v = 0; v < nv; v++)
-          if (read_real(&L, ln, 27 * v, &tgt->q[v * plane + c])) goto fail;
+      size_t cells = (size_t)(tgt->mx[0] + 2) * (tgt->mx[1] + 2) * (nd == 3 ? tgt->mx[2] + 2 : 1);
+      if (ln + cells > L.nlines) goto fail;
+      int k0 = nd == 3 ? 0 : 1, k1 = nd == 3 ? tgt->mx[2] + 1 : 1;
+      for (int k = k0; k <= k1; k++)
+        for (int j = 0; j <= tgt->mx[1] + 1; j++)
+          for (int i = 0; i <= tgt->mx[0] + 1; i++, ln++)
+            for (int v = 0; v < nv; v++)
+              if (read_real(&L, ln, 27 * v, &Q(tgt, i, j, k, v))) goto fail;
       if (level > 0) memcpy(tgt->qold, tgt->q, sizeof(double) * plane * nv);
     }
   }

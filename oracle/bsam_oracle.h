@@ -77,6 +77,11 @@ int bsamo_level_relax(bsamo_hier* h, int level, int nsmooth);
 int bsamo_fill_down(bsamo_hier* h, int field, int finestlevel, int minlevel);
 int bsamo_copy_q_to_qold(bsamo_hier* h, int minlevel, int finestlevel);
 int bsamo_vcycle(bsamo_hier* h, int level, int minlevel, int nsmooth);
+/* CorrectFine on every patch of a level (parent%q - qc, q += P1/P2 of it) */
+int bsamo_correct_fine(bsamo_hier* h, int level);
+/* P1MC (mbc = 1) / P2MC (mbc = 2) of one variable: a has cmx+2 mbc cells per
+ * used dimension, out 2 cmx + 2 mbc (Fortran order, ghost layers included) */
+int bsamo_prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double* out);
 int bsamo_residual_norm(bsamo_hier* h, int level, int errortype,
                         double* out);
 

@@ -46,16 +46,23 @@ def regrid_params(maxlevel, tagging="ch", initial=False, maxside=0, first_id=100
     return r
 
 
-def make_qinit(fn, ndims, nrvars):
+def make_qinit(fn, ndims, nrvars, mbc=1):
     """C callback around fn(level, mx, dx, xlower) -> ghosted Fortran-layout
-    array of the new patch (only its interior is used)."""
+    array of the new patch (only its interior is used), with mbc ghost
+    layers or one (then placed at q(0:mx+1), the second layer zero)."""
     def cb(user, level, mx, dx, xl, q):
-        m = [mx[d] for d in range(3)]
-        a = np.asarray(fn(level, m[:ndims], [dx[d] for d in range(3)][:ndims], [xl[d] for d in range(3)][:ndims]),
+        m = [mx[d] for d in range(ndims)]
+        a = np.asarray(fn(level, m, [dx[d] for d in range(3)][:ndims], [xl[d] for d in range(3)][:ndims]),
                        dtype=np.float64).ravel(order="F")
-        n = int(np.prod([v + 2 for v in m[:ndims]])) * nrvars
-        assert a.size == n, (a.size, n)
-        ctypes.memmove(q, a.ctypes.data, n * 8)
+        full = int(np.prod([v + 2 * mbc for v in m])) * nrvars
+        if a.size != full:
+            assert a.size == int(np.prod([v + 2 for v in m])) * nrvars, (a.size, full)
+            out = np.zeros([v + 2 * mbc for v in m] + [nrvars], order="F")
+            g = mbc - 1
+            out[tuple(slice(g, g + v + 2) for v in m) + (slice(None),)] = a.reshape([v + 2 for v in m] + [nrvars],
+                                                                                   order="F")
+            a = out.ravel(order="F")
+        ctypes.memmove(q, a.ctypes.data, full * 8)
     return QINIT(cb)
 
 
@@ -84,6 +91,8 @@ def lib():
         L.bsamo_fill_down.argtypes = [P, I, I, I]
         L.bsamo_copy_q_to_qold.argtypes = [P, I, I]
         L.bsamo_vcycle.argtypes = [P, I, I, I]
+        L.bsamo_correct_fine.argtypes = [P, I]
+        L.bsamo_prolong_mc.argtypes = [I, I, DP, IP, DP]
         L.bsamo_residual_norm.argtypes = [P, I, I, DP]
         L.bsamo_multigrid_iterations.argtypes = [P, I, I, I, I, D, I, I, IP, DP]
         L.bsamo_time_step.argtypes = [P, I, I, I, I, I, D, I, I, IP, DP]
@@ -120,7 +129,7 @@ class OracleHierarchy:
 
     def __init__(self, ndims, nrvars, problem, params, qpo=None, mbc=1):
         L = lib()
-        self.ndims, self.nrvars = ndims, nrvars
+        self.ndims, self.nrvars, self.mbc = ndims, nrvars, mbc
         h = ctypes.c_void_p()
         p = _da(params, len(params))
         q = _da(qpo if qpo is not None else [0.0] * nrvars, nrvars)
@@ -194,6 +203,9 @@ class OracleHierarchy:
     def vcycle(self, level, minlevel, nsmooth):
         _check(lib().bsamo_vcycle(self.h, level, minlevel, nsmooth), "vcycle")
 
+    def correct_fine(self, level):
+        _check(lib().bsamo_correct_fine(self.h, level), "correct_fine")
+
     def residual_norm(self, level, errortype=1):
         r = ctypes.c_double()
         _check(lib().bsamo_residual_norm(self.h, level, errortype, ctypes.byref(r)), "resid")
@@ -236,7 +248,7 @@ def read_q(root, path, first_id=1000):
     h = ctypes.c_void_p()
     t = ctypes.c_double()
     _check(lib().bsamo_read_q(root.h, os.fsencode(path), first_id, ctypes.byref(t), ctypes.byref(h)), "read_q")
-    return _wrap(h, root.ndims, root.nrvars), t.value
+    return _wrap(h, root.ndims, root.nrvars, root.mbc), t.value
 
 
 def format_f25(x):
@@ -251,18 +263,32 @@ def format_stats_line(time, integral, meshsize):
     return b.value.decode()
 
 
-def _wrap(h, ndims, nrvars):
+def _wrap(h, ndims, nrvars, mbc=1):
     o = OracleHierarchy.__new__(OracleHierarchy)
-    o.h, o.ndims, o.nrvars, o.patches = h, ndims, nrvars, []
+    o.h, o.ndims, o.nrvars, o.mbc, o.patches = h, ndims, nrvars, mbc, []
     return o
 
 
 def regrid(old, params, qinit=None):
     """AMR regrid of an oracle hierarchy (bsamo_regrid); returns a new one."""
-    cb = make_qinit(qinit, old.ndims, old.nrvars) if qinit is not None else QINIT()
+    cb = make_qinit(qinit, old.ndims, old.nrvars, old.mbc) if qinit is not None else QINIT()
     h = ctypes.c_void_p()
     _check(lib().bsamo_regrid(old.h, ctypes.byref(params), cb, None, ctypes.byref(h)), "regrid")
-    return _wrap(h, old.ndims, old.nrvars)
+    return _wrap(h, old.ndims, old.nrvars, old.mbc)
+
+
+def prolong_mc(a, mbc):
+    """P1MC / P2MC of one variable (bsamo_prolong_mc): a is the coarse
+    block with mbc ghost layers (Fortran order), the result the fine block."""
+    a = np.asarray(a, dtype=np.float64)
+    nd = a.ndim
+    cmx = [n - 2 * mbc for n in a.shape] + [1] * (3 - nd)
+    out = np.zeros([2 * c + 2 * mbc for c in cmx[:nd]], order="F")
+    src = np.asfortranarray(a)
+    _check(lib().bsamo_prolong_mc(nd, mbc, src.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                  (ctypes.c_int * 3)(*cmx), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+           "prolong_mc")
+    return out
 
 
 def uniform_pm1(seed, gidx):

@@ -13,8 +13,8 @@ pytestmark = pytest.mark.gpu
 
 def test_bad_arguments_return_status_codes(pkg, ctx):
     E = pkg.BsamgError
-    with pytest.raises(E):  # mbc = 2 is not built
-        pkg.Hierarchy(ctx, 2, 2, "ch", [1e-3, 0.01], mbc=2)
+    with pytest.raises(E):  # RootInit allows mbc = 1 or 2
+        pkg.Hierarchy(ctx, 2, 2, "ch", [1e-3, 0.01], mbc=3)
     with pytest.raises(E):  # the growth plugin has three variables
         pkg.Hierarchy(ctx, 3, 2, "growth", [0.01, 0.025, 1.5, 2.0, 0.5, 1.0])
     with pytest.raises(E):  # BioGrowth needs five parameters
