@@ -631,37 +631,49 @@ __global__ void __launch_bounds__(kSmallThreads) k_bx_small_vcycle(float* __rest
 
 // After a cycle on the finest level: tracked residual g <- g - M(e) (M at
 // this cycle's base field), its per-CTA sums of squares, then qbar += e as
-// double-float.  One thread per cell; every load precedes every store.
-template <int DIM>
-__global__ void __launch_bounds__(256) k_bx_track_update(float* __restrict__ fp, BoxLev L, long long oqlo,
-                                                         double* __restrict__ partial) {
+// double-float.  One row (2D) or two rows (3D) per thread; every load
+// precedes every store.
+template <int DIM, int R = 1>
+__global__ void __launch_bounds__(256, R == 1 ? 6 : 4) k_bx_track_update(float* __restrict__ fp, BoxLev L,
+                                                                       long long oqlo, double* __restrict__ partial) {
+  // R rows per thread (y = R yp .. R yp + R - 1): every load of the R cells
+  // is issued before the first store, R times the loads in flight
   int x = blockIdx.x * blockDim.x + threadIdx.x;
-  int y = blockIdx.y * blockDim.y + threadIdx.y;
+  int yp = blockIdx.y * blockDim.y + threadIdx.y;
   int z = blockIdx.z;
   float s0 = 0.f, s1 = 0.f;
-  if (x < L.n[0] && y < L.n[1]) {
+  if (x < L.n[0] && R * yp < L.n[1]) {
     V2 E = var2(fp, L.oe, L.half), G = var2(fp, L.og, L.half);
     V2 QH = var2(fp, L.opb, L.half), QL = var2(fp, oqlo, L.half);  // the base field is qhi(phi)
-    Loc<DIM> l(L, x, y, z);
-    unsigned i = l.own;
-    float h0 = QH.v0[i], h1 = QH.v1[i], lo0 = QL.v0[i], lo1 = QL.v1[i], a0 = G.v0[i], a1 = G.v1[i];
-    float e0 = E.v0[i], e1 = E.v1[i];
-    float m0, m1;
-    mop<DIM>(E, L, l, h0, m0, m1);
-    a0 -= m0;
-    a1 -= m1;
-    DF t0 = two_sum(h0, e0);
-    t0 = fast_two_sum(t0.h, t0.l + lo0);
-    DF t1 = two_sum(h1, e1);
-    t1 = fast_two_sum(t1.h, t1.l + lo1);
-    G.v0[i] = a0;
-    G.v1[i] = a1;
-    QH.v0[i] = t0.h;
-    QL.v0[i] = t0.l;
-    QH.v1[i] = t1.h;
-    QL.v1[i] = t1.l;
-    s0 = a0 * a0;
-    s1 = a1 * a1;
+    unsigned own[R];
+    float a0[R], a1[R], th0[R], tl0[R], th1[R], tl1[R];
+    for (int k = 0; k < R; k++) {
+      Loc<DIM> l(L, x, R * yp + k, z);
+      unsigned i = l.own;
+      own[k] = i;
+      float h0 = QH.v0[i], h1 = QH.v1[i], lo0 = QL.v0[i], lo1 = QL.v1[i];
+      float e0 = E.v0[i], e1 = E.v1[i];
+      float m0, m1;
+      mop<DIM>(E, L, l, h0, m0, m1);
+      a0[k] = G.v0[i] - m0;
+      a1[k] = G.v1[i] - m1;
+      DF t0 = two_sum(h0, e0);
+      t0 = fast_two_sum(t0.h, t0.l + lo0);
+      DF t1 = two_sum(h1, e1);
+      t1 = fast_two_sum(t1.h, t1.l + lo1);
+      th0[k] = t0.h, tl0[k] = t0.l, th1[k] = t1.h, tl1[k] = t1.l;
+    }
+    for (int k = 0; k < R; k++) {
+      unsigned i = own[k];
+      G.v0[i] = a0[k];
+      G.v1[i] = a1[k];
+      QH.v0[i] = th0[k];
+      QL.v0[i] = tl0[k];
+      QH.v1[i] = th1[k];
+      QL.v1[i] = tl1[k];
+      s0 += a0[k] * a0[k];
+      s1 += a1[k] * a1[k];
+    }
   }
   cta_sum2(s0, s1, partial);
 }
@@ -875,6 +887,12 @@ int bx_cycle(Hier& H, int finest, int minlevel, int nsmooth, int errortype) {
   int r = bx_vcycle(H, finest, minlevel, nsmooth, true);
   if (r) return r;
   BoxLev& L = B(H, finest);
+  if (H.ndims == 3 && L.n[1] % 2 == 0) {  // two rows per thread
+    Launch sh = shape(L.n[0], L.n[1] / 2, L.n[2]);
+    k_bx_track_update<3, 2><<<sh.g, sh.b, 0, H.s>>>(H.fpool, L, H.b_oqlo, H.d_partial);
+    if ((r = after_launch(H, 1))) return r;
+    return bx_finish(H, finest, ctas(sh), errortype);
+  }
   Launch sh = shape(L.n[0], L.n[1], L.n[2]);
   BX_LAUNCH(H, sh, k_bx_track_update, H.fpool, L, H.b_oqlo, H.d_partial);
   return bx_finish(H, finest, ctas(sh), errortype);
