@@ -377,6 +377,21 @@ __global__ void __launch_bounds__(kBlock) k_correct_a(const PatchDev* __restrict
   u_correct_a<DIM>(P, pool, blk[blockIdx.x], threadIdx.x, nrvars);
 }
 
+// InitFields' first statement (bsamroutines.f90:1815-1818, :1834-1837):
+// child qc(1-mbc:cmx+mbc) = parent%q(mb-mbc:mb+mbc), on a new patch
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_qc_from_parent(const PatchDev* __restrict__ P, double* __restrict__ pool,
+                                                           const Blk* __restrict__ blk, int nrvars) {
+  const Blk b = blk[blockIdx.x];
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  if (!ghosted_cell<DIM>(p.cn, p.gs, b.start + threadIdx.x, i, j, k)) return;
+  const PatchDev& par = P[p.parent];
+  long long src = gofs<DIM>(par.qn, p.mb[0] - 1 + i, p.mb[1] - 1 + j, DIM == 3 ? p.mb[2] - 1 + k : 0);
+  long long dst = gofs<DIM>(p.cn, i, j, k);
+  for (int v = 0; v < nrvars; v++) pool[p.oqc + v * p.sc + dst] = pool[par.oq + v * par.sq + src];
+}
+
 // CorrectFine step 2: q(1-mbc:mx+mbc) += BiLinProlongationP1/P2(qc)
 // (gridutilities.f90:156-239) / TriLinProlongationP1/P2 (:510-625).  One
 // thread per coarse index (ci,cj,ck) in -gs..cmx+gs produces fine cells
@@ -780,6 +795,11 @@ int launch_coarse_load(const LaunchCtx& c, const Blk* blk, int nblk) {
 int launch_correct_a(const LaunchCtx& c, const Blk* blk, int nblk) {
   if (nblk <= 0) return 0;
   DISPATCH_DIM(c, k_correct_a, c.P, c.pool, blk, c.pp.nrvars);
+  return 1;
+}
+int launch_qc_from_parent(const LaunchCtx& c, const Blk* blk, int nblk) {
+  if (nblk <= 0) return 0;
+  DISPATCH_DIM(c, k_qc_from_parent, c.P, c.pool, blk, c.pp.nrvars);
   return 1;
 }
 int launch_correct_b(const LaunchCtx& c, const Blk* blk, int nblk) {

@@ -34,7 +34,10 @@ struct Em {
 struct Emitter {
   const Hier& H;
   std::vector<Em> out;
-  explicit Emitter(const Hier& h) : H(h) {}
+  std::vector<int> org;  // per patch: offset of cell (0,0,0) in its q plane
+  explicit Emitter(const Hier& h) : H(h), org(h.patches.size()) {
+    for (size_t p = 0; p < h.patches.size(); p++) org[p] = (int)origin_of(h, h.patches[p].qn);
+  }
 
   // offset of Fortran cell (i,j,k) from cell (0,0,0) of a q plane (the
   // device tables address q from that cell; negative in the second ghost
@@ -46,7 +49,7 @@ struct Emitter {
   }
   // (patch, cell) key; the cell counted from the array's start (>= 0)
   int64_t key(int p, int c) const {
-    return ((int64_t)p << 32) | (uint32_t)(c + origin_of(H, H.patches[p].qn));
+    return ((int64_t)p << 32) | (uint32_t)(c + org[p]);
   }
 
   void copy(int type, int dp, int dc, int sp, int sc) {

@@ -56,6 +56,8 @@ int launch_restrict_q(const LaunchCtx& c, const Blk* blk, int nblk);
 int launch_coarse_ghost(const LaunchCtx& c, const Blk* blk, int nblk);
 int launch_coarse_load(const LaunchCtx& c, const Blk* blk, int nblk);
 int launch_correct_a(const LaunchCtx& c, const Blk* blk, int nblk);
+// qc of every patch in blk = its parent's q under it, ghost rings included
+int launch_qc_from_parent(const LaunchCtx& c, const Blk* blk, int nblk);
 int launch_correct_b(const LaunchCtx& c, const Blk* blk, int nblk);
 int launch_fill_down(const LaunchCtx& c, const Blk* blk, int nblk, int field);
 int launch_get_source(const LaunchCtx& c, const Blk* blk, int nblk);

@@ -34,7 +34,6 @@ struct Model {
   std::vector<HostPatch> g;            // geometry, in visiting order
   std::vector<std::vector<double>> q;  // ghosted q of levels >= 0 (empty below)
   std::vector<std::vector<double>> qold;
-  std::vector<std::vector<double>> qc;  // ghosted qc of new patches (InitFields)
   std::vector<int> src_idx;            // index in src, or -1 for new patches
   explicit Model(const Hier& h) : src(h) {}
   int nd() const { return src.ndims; }
@@ -74,11 +73,18 @@ int host_set_ghost(Model& M, int level) {
   const double a1 = -01.0 / 05.0, a2 = 02.0 / 03.0, a3 = 08.0 / 15.0;   // boundary.f90:54-63
   const double b1 = 05.0 / 32.0, b2 = 15.0 / 16.0, b3 = -03.0 / 32.0;
   const double c1 = 09.0 / 16.0, c2 = 03.0 / 16.0, c3 = 03.0 / 16.0, c4 = 01.0 / 16.0;
+  // cells are counted from cell (0,0,0) of each patch's q plane
+  std::vector<double*> base(M.g.size(), nullptr);
+  std::vector<size_t> plane(M.g.size());
+  for (size_t p = 0; p < M.g.size(); p++) {
+    plane[p] = M.nq(M.g[p]);
+    if (!M.q[p].empty()) base[p] = M.q[p].data() + origin_of(M.src, M.g[p].qn);
+  }
   for (const GhostOp& o : ops) {
-    if (M.q[o.dp].empty() || M.q[o.sp].empty()) return BSAMG_ERR_ARG;  // below-root data is not on the host
-    for (int v = 0; v < M.src.nrvars; v++) {  // cells are counted from cell (0,0,0)
-      double* dq = M.q[o.dp].data() + origin_of(M.src, M.g[o.dp].qn) + v * M.nq(M.g[o.dp]);
-      const double* sq = M.q[o.sp].data() + origin_of(M.src, M.g[o.sp].qn) + v * M.nq(M.g[o.sp]);
+    if (!base[o.dp] || !base[o.sp]) return BSAMG_ERR_ARG;  // below-root data is not on the host
+    for (int v = 0; v < M.src.nrvars; v++) {
+      double* dq = base[o.dp] + v * plane[o.dp];
+      const double* sq = base[o.sp] + v * plane[o.sp];
       double val;
       switch (o.type) {
         case kGCopy: val = sq[o.s0]; break;
@@ -112,8 +118,10 @@ void tag_patch(Model& M, int p, const bsamg_regrid_params& prm, Flags& F) {
   double tol = prm.qtolerance[P.level];
   for (int d = 0; d < 3; d++) F.mx[d] = P.mx[d];
   F.f.assign((size_t)P.mx[0] * P.mx[1] * P.mx[2], 0);
-  int ko = nd == 3 ? 1 : 0;  // ghost offset of the third index
-  auto q = [&](int i, int j, int k) { return M.Q(p, i, j, k - 1 + ko, 0); };
+  // phi(i,j,k) from cell (0,0,0) of the ghosted plane (k unused in 2D)
+  const double* q0 = M.q[p].data() + origin_of(M.src, P.qn);
+  const long long sy = P.qn[0], sz = nd == 3 ? (long long)P.qn[0] * P.qn[1] : 0;
+  auto q = [&](int i, int j, int k) { return q0[i + j * sy + k * sz]; };
   for (int k = 1; k <= P.mx[2]; k++)
     for (int j = 1; j <= P.mx[1]; j++)
       for (int i = 1; i <= P.mx[0]; i++) {
@@ -342,25 +350,29 @@ void split_long(int nd, int maxside, std::vector<Sub>& subs) {
 // 64; P2 writes the odd cells' sum as 3 a(c+1) + a(c), the same IEEE sum),
 // then each interior coarse cell's mass correction goes to its 2^d cells.
 void prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double* out) {
-  const int L = 1 - mbc, kL = nd == 3 ? L : 0;
+  const int L = 1 - mbc, kL = nd == 3 ? L : 0, g = mbc - 1;
   const int cn0 = cmx[0] + 2 * mbc, cn1 = cmx[1] + 2 * mbc, cn2 = nd == 3 ? cmx[2] + 2 * mbc : 1;
   const int fn0 = 2 * cmx[0] + 2 * mbc, fn1 = 2 * cmx[1] + 2 * mbc, fn2 = nd == 3 ? 2 * cmx[2] + 2 * mbc : 1;
-  auto lo = [](int f) { return (f - (f & 1)) / 2; };  // f = 2c or 2c+1 -> c
   auto A = [&](int i, int j, int k) { return a[((size_t)(k - kL) * cn1 + (j - L)) * cn0 + (i - L)]; };
   auto O = [&](int i, int j, int k) -> double& { return out[((size_t)(k - kL) * fn1 + (j - L)) * fn0 + (i - L)]; };
   std::vector<double> b((size_t)fn0 * cn1 * cn2);
   auto Bx = [&](int i, int j, int k) -> double& { return b[((size_t)(k - kL) * cn1 + (j - L)) * fn0 + (i - L)]; };
+  // fine cells 2I and 2I+1 of coarse pair (I, I+1), I = -g..cmx+g, kept
+  // where they lie in L..2 cmx + mbc
+  const int hi0 = 2 * cmx[0] + mbc, hi1 = 2 * cmx[1] + mbc, hi2 = nd == 3 ? 2 * cmx[2] + mbc : 0;
   for (int k = kL; k < kL + cn2; k++)
     for (int j = L; j < L + cn1; j++)
-      for (int i = L; i < L + fn0; i++) {
-        int c = lo(i);
-        Bx(i, j, k) = (i & 1) ? A(c, j, k) + 3.0 * A(c + 1, j, k) : 3.0 * A(c, j, k) + A(c + 1, j, k);
+      for (int I = -g; I <= cmx[0] + g; I++) {
+        double lo = A(I, j, k), up = A(I + 1, j, k);
+        if (2 * I >= L) Bx(2 * I, j, k) = 3.0 * lo + up;
+        if (2 * I + 1 <= hi0) Bx(2 * I + 1, j, k) = lo + 3.0 * up;
       }
   if (nd == 2) {
-    for (int j = L; j < L + fn1; j++)
+    for (int J = -g; J <= cmx[1] + g; J++)
       for (int i = L; i < L + fn0; i++) {
-        int c = lo(j);
-        O(i, j, 0) = (j & 1) ? (Bx(i, c, 0) + 3.0 * Bx(i, c + 1, 0)) / 16.0 : (3.0 * Bx(i, c, 0) + Bx(i, c + 1, 0)) / 16.0;
+        double lo = Bx(i, J, 0), up = Bx(i, J + 1, 0);
+        if (2 * J >= L) O(i, 2 * J, 0) = (3.0 * lo + up) / 16.0;
+        if (2 * J + 1 <= hi1) O(i, 2 * J + 1, 0) = (lo + 3.0 * up) / 16.0;
       }
     for (int J = 1; J <= cmx[1]; J++)
       for (int I = 1; I <= cmx[0]; I++) {
@@ -376,17 +388,20 @@ void prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double* out)
   std::vector<double> c((size_t)fn0 * fn1 * cn2);
   auto Cy = [&](int i, int j, int k) -> double& { return c[((size_t)(k - kL) * fn1 + (j - L)) * fn0 + (i - L)]; };
   for (int k = kL; k < kL + cn2; k++)
+    for (int J = -g; J <= cmx[1] + g; J++)
+      for (int i = L; i < L + fn0; i++) {
+        double lo = Bx(i, J, k), up = Bx(i, J + 1, k);
+        if (2 * J >= L) Cy(i, 2 * J, k) = 3.0 * lo + up;
+        if (2 * J + 1 <= hi1) Cy(i, 2 * J + 1, k) = lo + 3.0 * up;
+      }
+  for (int K = -g; K <= cmx[2] + g; K++)
     for (int j = L; j < L + fn1; j++)
       for (int i = L; i < L + fn0; i++) {
-        int cj = lo(j);
-        Cy(i, j, k) = (j & 1) ? Bx(i, cj, k) + 3.0 * Bx(i, cj + 1, k) : 3.0 * Bx(i, cj, k) + Bx(i, cj + 1, k);
+        double lo = Cy(i, j, K), up = Cy(i, j, K + 1);
+        if (2 * K >= L) O(i, j, 2 * K) = (3.0 * lo + up) / 64.0;
+        if (2 * K + 1 <= hi2) O(i, j, 2 * K + 1) = (lo + 3.0 * up) / 64.0;
       }
-  for (int k = L; k < L + fn2; k++)
-    for (int j = L; j < L + fn1; j++)
-      for (int i = L; i < L + fn0; i++) {
-        int ck = lo(k);
-        O(i, j, k) = (k & 1) ? (Cy(i, j, ck) + 3.0 * Cy(i, j, ck + 1)) / 64.0 : (3.0 * Cy(i, j, ck) + Cy(i, j, ck + 1)) / 64.0;
-      }
+  (void)fn2;
   for (int K = 1; K <= cmx[2]; K++)
     for (int J = 1; J <= cmx[1]; J++)
       for (int I = 1; I <= cmx[0]; I++) {
@@ -457,8 +472,6 @@ void make_new_grid(Model& M, int p, const Box& b, int id, const bsamg_regrid_par
   M.src_idx.push_back(-1);
   M.qold.push_back(q);  // child%qold = child%q (:1782)
   M.q.push_back(std::move(q));
-  M.qc.resize(M.g.size());
-  M.qc.back() = std::move(qc);
 }
 
 // TransferOverlap (:1919-1951): interior q of src onto dst
@@ -493,16 +506,10 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   if (r) return r;
   int nd = H.ndims, nv = H.nrvars;
   Model M(H);
-  // one copy of the whole q region (every patch, ghosts included) and one
-  // of the qc region (the persisting patches keep their qc, whose second
-  // ring, mbc = 2, carries the last correction)
+  // one copy of the whole q region (every patch, ghosts included)
   std::vector<double> qreg((size_t)H.q_len);
-  const long long qc0 = H.patches[0].oqc, qc1 = H.patches[0].of;  // the qc region lies before f
-  std::vector<double> qcreg((size_t)(qc1 - qc0));
   cudaError_t ce = cudaMemcpyAsync(qreg.data(), H.pool + H.q_region, qreg.size() * sizeof(double),
                                    cudaMemcpyDeviceToHost, H.s);
-  if (ce == cudaSuccess)
-    ce = cudaMemcpyAsync(qcreg.data(), H.pool + qc0, qcreg.size() * sizeof(double), cudaMemcpyDeviceToHost, H.s);
   if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(regrid download)");
   ce = cudaStreamSynchronize(H.s);
   if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize(regrid)");
@@ -632,34 +639,32 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
     }
     if (M.src_idx[p] < 0) std::memcpy(oimg.data() + (D.oq - N.q_region), M.qold[p].data(), n * sizeof(double));
   }
-  // qc: the persisting patches' own, InitFields' for the new ones
-  const long long nqc0 = N.patches[0].oqc, nqc1 = N.patches[0].of;
-  std::vector<double> cimg((size_t)(nqc1 - nqc0), 0.0);
-  M.qc.resize(M.g.size());
-  for (size_t p = 0; p < M.g.size(); p++) {
-    const HostPatch& D = N.patches[p];
-    size_t n = (size_t)D.sc * nv;
-    if (M.src_idx[p] >= 0) {
-      const HostPatch& S = H.patches[M.src_idx[p]];
-      std::memcpy(cimg.data() + (D.oqc - nqc0), qcreg.data() + (S.oqc - qc0), n * sizeof(double));
-    } else if (M.qc[p].size() == n) {
-      std::memcpy(cimg.data() + (D.oqc - nqc0), M.qc[p].data(), n * sizeof(double));
-    }
-  }
   ce = cudaMemcpyAsync(N.pool + N.q_region, qimg.data(), qimg.size() * sizeof(double), cudaMemcpyHostToDevice, N.s);
   if (ce == cudaSuccess)
     ce = cudaMemcpyAsync(N.pool + N.qold_region, oimg.data(), oimg.size() * sizeof(double), cudaMemcpyHostToDevice,
                          N.s);
-  if (ce == cudaSuccess)
-    ce = cudaMemcpyAsync(N.pool + nqc0, cimg.data(), cimg.size() * sizeof(double), cudaMemcpyHostToDevice, N.s);
+
   for (size_t p = 0; p < M.g.size() && ce == cudaSuccess; p++)
     if (M.src_idx[p] >= 0) {
       const HostPatch& D = N.patches[p];
       const HostPatch& S = H.patches[M.src_idx[p]];
       ce = cudaMemcpyAsync(N.pool + D.oqold, H.pool + S.oqold, (size_t)D.sq * nv * sizeof(double),
                            cudaMemcpyDeviceToDevice, N.s);
+      // the persisting patches keep their qc (with mbc = 2 its second ring
+      // carries the last correction)
+      if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(N.pool + D.oqc, H.pool + S.oqc, (size_t)D.sc * nv * sizeof(double),
+                             cudaMemcpyDeviceToDevice, N.s);
     }
   if (ce != cudaSuccess) return fail(cuda_fail(ce, "cudaMemcpyAsync(regrid upload)"));
+  // InitFields' child qc = parent q on the new patches (their parents' q is
+  // final in the uploaded image); QInit'd patches keep the zero fill
+  if (!prm.initial)
+    for (int l = 1; l <= N.maxlevel; l++) {
+      LevelT& L = N.L(l);
+      if ((r = after_launch(N, launch_qc_from_parent(N.lc(), L.d_blk[kKindCGhost], L.nblk[kKindCGhost]))))
+        return fail(r);
+    }
   if (final_ghost >= 0 && (r = enq_set_ghost(N, final_ghost, 0))) return fail(r);
   ce = cudaStreamSynchronize(N.s);  // the host arrays are freed on return
   if (ce != cudaSuccess) return fail(cuda_fail(ce, "cudaStreamSynchronize(regrid upload)"));
