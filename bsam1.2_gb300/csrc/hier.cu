@@ -193,10 +193,10 @@ int fp_prepare_tail(Hier& H, int finest, int minlevel, int nsmooth) {
       D.orf = add(D.orf, (long long)H.nrvars * P.sf, 1);
     }
     if (so * (long long)sizeof(double) <= kTailSmemMax && !segs.empty() && !prog.empty()) {
-      static bool attr = false;
-      if (!attr) {
+      static std::atomic<unsigned long long> attr{0};  // the kernels' shared-memory limit, per device
+      if (needs_setup(attr, H.ctx->device)) {
         if (tail_smem_attributes()) return cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute(tail)");
-        attr = true;
+        mark_setup(attr, H.ctx->device);
       }
       T.smem_bytes = (int)(so * sizeof(double));
       T.nsegs = (int)segs.size();

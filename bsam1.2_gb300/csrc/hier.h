@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <functional>
 #include <map>
 #include <mutex>
@@ -165,6 +166,16 @@ double xupper_of(const Hier& H, const HostPatch& P, int d);
 // Offset of Fortran cell (0,0,0) from the start of a ghosted q-like (n =
 // qn) or qc-like (n = cn) plane: 0 for mbc = 1, one cell of each used
 // dimension's stride for mbc = 2 (the arrays start at index 1 - mbc).
+// Per-device one-time setup (a kernel attribute): true when device dev has
+// not been marked in `done` yet; the caller marks it after the setup
+// succeeded.  Repeating the setup from two threads is harmless, the flag
+// itself is atomic.
+inline bool needs_setup(const std::atomic<unsigned long long>& done, int dev) {
+  return !(done.load(std::memory_order_acquire) & (1ull << (dev & 63)));
+}
+inline void mark_setup(std::atomic<unsigned long long>& done, int dev) {
+  done.fetch_or(1ull << (dev & 63), std::memory_order_release);
+}
 inline long long origin_of(const Hier& H, const int* n) {
   long long s = H.mbc - 1;
   return H.ndims == 2 ? s * (1 + n[0]) : s * (1 + n[0] + (long long)n[0] * n[1]);

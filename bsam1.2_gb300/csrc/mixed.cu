@@ -972,9 +972,9 @@ int mx_prepare_tail(Hier& H, int finest, int minlevel, int nsmooth) {
   if (so * (long long)sizeof(float) <= kTailSmemMax && !segs.empty()) {
     T.smem_bytes = (int)(so * sizeof(float));
     T.nsegs = (int)segs.size();
-    static bool attr[2][2] = {};  // the kernels' dynamic shared-memory limit, set once
+    static std::atomic<unsigned long long> attr[2][2];  // the kernels' shared-memory limit, per device
     int a = H.ndims - 2, b = H.problem == kGrowth;
-    if (!attr[a][b]) {
+    if (needs_setup(attr[a][b], H.ctx->device)) {
       cudaError_t e;
       if (H.problem == kGrowth)
         e = H.ndims == 2 ? cudaFuncSetAttribute(k_mx_tail_smem<2, kGrowth>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax)
@@ -983,7 +983,7 @@ int mx_prepare_tail(Hier& H, int finest, int minlevel, int nsmooth) {
         e = H.ndims == 2 ? cudaFuncSetAttribute(k_mx_tail_smem<2, kCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax)
                          : cudaFuncSetAttribute(k_mx_tail_smem<3, kCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax);
       if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(tail)");
-      attr[a][b] = true;
+      mark_setup(attr[a][b], H.ctx->device);
     }
     cudaError_t e = dev_alloc(H, &T.shadow, sizeof(PatchDev) * shadow.size());
     if (e == cudaSuccess)
