@@ -746,6 +746,59 @@ __global__ void __launch_bounds__(256) k_bx_split(const double* __restrict__ poo
   }
 }
 
+// k_bx_split for a step that follows a box solve on the same q: with g the
+// true residual r_old = f_old - N(q) and f_old in fhi/flo, the residual for
+// the new f = (phi_old, -phi_old) is r_old + (f_new - f_old), so g becomes
+// g + (d, -d) with d = f_new - f_old in double-float, and the per-CTA sums
+// of g^2 go to partial (what k_bx_resid would give, without its
+// double-float operator evaluation).
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_split_warm(const double* __restrict__ pool, long long oq, long long oqold,
+                                                       long long sq, int qn0, int qn1, float* __restrict__ fp,
+                                                       BoxLev L, long long oqlo, long long ofhi, long long oflo,
+                                                       double* __restrict__ partial) {
+  int h = blockIdx.x * blockDim.x + threadIdx.x;
+  int y = blockIdx.y * blockDim.y + threadIdx.y;
+  int z = blockIdx.z;
+  float s0 = 0.f, s1 = 0.f;
+  if (h < L.hh && y < L.n[1]) {
+    long long g = (2 * h + 1) + (long long)(y + 1) * qn0 + (DIM == 3 ? (long long)(z + 1) * qn0 * qn1 : 0);
+    V2 QH = var2(fp, L.opb, L.half), QL = var2(fp, oqlo, L.half), G = var2(fp, L.og, L.half);
+    double in[2][3];
+    unsigned own[2];
+    float fo[2][2], go[2][2];  // old f (hi, lo) and g, loaded before any store
+    for (int b = 0; b < 2; b++) {
+      in[b][0] = pool[oq + g + b];
+      in[b][1] = pool[oq + sq + g + b];
+      in[b][2] = pool[oqold + g + b];
+      Loc<DIM> l(L, 2 * h + b, y, z);
+      own[b] = l.own;
+      fo[b][0] = fp[ofhi + l.own];
+      fo[b][1] = fp[oflo + l.own];
+      go[b][0] = G.v0[l.own];
+      go[b][1] = G.v1[l.own];
+    }
+    for (int b = 0; b < 2; b++) {
+      unsigned i = own[b];
+      DF s0v = split64(in[b][0]), s1v = split64(in[b][1]), f = split64(in[b][2]);
+      DF d = df_add(f, df_neg(DF{fo[b][0], fo[b][1]}));
+      DF r1 = df_add(DF{go[b][0], 0.f}, d), r2 = df_add(DF{go[b][1], 0.f}, df_neg(d));
+      float a0 = r1.h + r1.l, a1 = r2.h + r2.l;
+      QH.v0[i] = s0v.h;
+      QL.v0[i] = s0v.l;
+      QH.v1[i] = s1v.h;
+      QL.v1[i] = s1v.l;
+      fp[ofhi + i] = f.h;
+      fp[oflo + i] = f.l;
+      G.v0[i] = a0;
+      G.v1[i] = a1;
+      s0 += a0 * a0;
+      s1 += a1 * a1;
+    }
+  }
+  cta_sum2(s0, s1, partial);
+}
+
 // qhi + qlo -> FP64 q (interior of the finest level)
 template <int DIM>
 __global__ void __launch_bounds__(256) k_bx_merge(double* __restrict__ pool, long long oq, long long sq, int qn0,
@@ -974,9 +1027,18 @@ int box_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycle
   const HostPatch& P = H.patches[H.L(finest).patches[0]];
   BoxLev& L = B(H, finest);
   Launch sh = shape(L.hh, L.n[1], L.n[2]);
-  BX_LAUNCH(H, sh, k_bx_split, H.pool, P.oq, P.oqold, P.sq, P.qn[0], P.qn[1], H.fpool, L, H.b_oqlo, H.b_ofhi,
-            H.b_oflo);
-  int r = bx_resid(H, finest, errortype);
+  bool warm = H.box_g_valid;  // g is the residual at this q: update it for the new f
+  H.box_g_valid = false;
+  int r;
+  if (warm) {
+    BX_LAUNCH(H, sh, k_bx_split_warm, H.pool, P.oq, P.oqold, P.sq, P.qn[0], P.qn[1], H.fpool, L, H.b_oqlo, H.b_ofhi,
+              H.b_oflo, H.d_partial);
+    r = bx_finish(H, finest, ctas(sh), errortype);
+  } else {
+    BX_LAUNCH(H, sh, k_bx_split, H.pool, P.oq, P.oqold, P.sq, P.qn[0], P.qn[1], H.fpool, L, H.b_oqlo, H.b_ofhi,
+              H.b_oflo);
+    r = bx_resid(H, finest, errortype);
+  }
   if (r) return r;
   if (int rw = stream_wait(H)) return rw;
   if (*H.h_nonfinite) return BSAMG_ERR_NONFINITE;
@@ -1016,6 +1078,8 @@ int box_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycle
   BX_LAUNCH(H, sh, k_bx_merge, H.pool, P.oq, P.sq, P.qn[0], P.qn[1], H.fpool, L, H.b_oqlo);
   if ((r = enq_set_ghost(H, finest, 0))) return r;
   if ((r = enq_fill_down(H, 2, finest, minlevel))) return r;
+  // the loop ends on a true residual (converged, or the last cycle's check)
+  H.box_g_valid = true;
   if (!conv && strict) return BSAMG_ERR_NOT_CONVERGED;
   return BSAMG_OK;
 }

@@ -699,6 +699,7 @@ int bsamg_read_q(bsamg_hier* root, const char* path, int first_id, double* time,
 
 int bsamg_seed_spinodal(bsamg_hier* h, int id, unsigned long long seed, double mean, double amp) {
   if (!h || !h->committed || h->problem != kCH || h->nrvars != 2) return BSAMG_ERR_ARG;
+  h->box_g_valid = false;
   auto it = h->id2idx.find(id);
   if (it == h->id2idx.end()) return BSAMG_ERR_NOT_FOUND;
   const HostPatch& P = h->patches[it->second];

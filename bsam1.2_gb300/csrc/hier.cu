@@ -470,6 +470,7 @@ int multigrid_iterations(Hier& H, int finest, int minlevel, int nsmooth, int max
   if (maxvcycles < 1 || nsmooth < 1 || (errortype != 1 && errortype != 2)) return BSAMG_ERR_ARG;
   if (mode != BSAMG_MODE_FP64 && mode != BSAMG_MODE_MIXED) return BSAMG_ERR_ARG;
   RET(set_device(H));
+  if (!(mode == BSAMG_MODE_MIXED && H.box)) H.box_g_valid = false;  // the FP64 cycles change q
   // afasroutines.f90:57-76
   // the periodic-box mixed path forms f from qold itself
   if (mode == BSAMG_MODE_MIXED && H.box)
@@ -1019,6 +1020,7 @@ size_t bsamg_field_size(const bsamg_hier* h, int id, int field) {
 
 int bsamg_put_field(bsamg_hier* h, int id, int field, const double* a, size_t n) {
   if (!h || !h->committed || !a) return BSAMG_ERR_ARG;
+  h->box_g_valid = false;
   HostPatch* P = find(*h, id);
   if (!P) return BSAMG_ERR_NOT_FOUND;
   size_t nn;
@@ -1075,6 +1077,7 @@ int section_copy(Hier& H, int id, int field, double* a, const int lo[4], const i
 
 int bsamg_put_field_section(bsamg_hier* h, int id, int field, const double* a, const int lo[4], const int hi[4]) {
   if (!h) return BSAMG_ERR_ARG;
+  h->box_g_valid = false;
   return section_copy(*h, id, field, const_cast<double*>(a), lo, hi, true);
 }
 
@@ -1098,18 +1101,21 @@ int bsamg_get_field(bsamg_hier* h, int id, int field, double* a, size_t n) {
 int bsamg_relax_level_color(bsamg_hier* h, int level, int ipass) {
   if (!h || !h->committed || !level_ok(*h, level) || (ipass != 1 && ipass != 2)) return BSAMG_ERR_ARG;
   RET(set_device(*h));
+  h->box_g_valid = false;
   return enq_relax(*h, level, ipass);
 }
 
 int bsamg_set_ghost(bsamg_hier* h, int level, int ipass) {
   if (!h || !h->committed || !level_ok(*h, level) || ipass < 0 || ipass > 2) return BSAMG_ERR_ARG;
   RET(set_device(*h));
+  h->box_g_valid = false;
   return enq_set_ghost(*h, level, ipass);
 }
 
 int bsamg_level_relax(bsamg_hier* h, int level, int nsmooth) {
   if (!h || !h->committed || !level_ok(*h, level) || nsmooth < 0) return BSAMG_ERR_ARG;
   RET(set_device(*h));
+  h->box_g_valid = false;
   return enq_level_relax(*h, level, nsmooth);
 }
 
@@ -1117,6 +1123,7 @@ int bsamg_fill_down(bsamg_hier* h, int field, int finestlevel, int minlevel) {
   if (!h || !h->committed || (field != 1 && field != 2)) return BSAMG_ERR_ARG;
   if (!level_ok(*h, finestlevel) || !level_ok(*h, minlevel)) return BSAMG_ERR_ARG;
   RET(set_device(*h));
+  h->box_g_valid = false;
   return enq_fill_down(*h, field, finestlevel, minlevel);
 }
 
@@ -1130,6 +1137,7 @@ int bsamg_vcycle(bsamg_hier* h, int level, int minlevel, int nsmooth) {
   if (!h || !h->committed || !level_ok(*h, level) || !level_ok(*h, minlevel) || minlevel > level)
     return BSAMG_ERR_ARG;
   RET(set_device(*h));
+  h->box_g_valid = false;
   return enq_vcycle(*h, level, minlevel, nsmooth);
 }
 
@@ -1198,6 +1206,7 @@ int bsamg_set_params(bsamg_hier* h, const double* params, int nparams) {
   if (nparams < 2 || (h->problem == kBio && nparams < 5) || (h->problem == kGrowth && nparams < 6))
     return BSAMG_ERR_ARG;
   if ((int)h->params.size() == nparams && std::equal(params, params + nparams, h->params.begin())) return BSAMG_OK;
+  h->box_g_valid = false;
   int r = set_device(*h);
   if (r) return r;
   h->params.assign(params, params + nparams);
@@ -1247,6 +1256,7 @@ int bsamg_set_params(bsamg_hier* h, const double* params, int nparams) {
 
 int bsamg_hier_reset(bsamg_hier* h) {
   if (!h || !h->committed) return BSAMG_ERR_ARG;
+  h->box_g_valid = false;
   int r = set_device(*h);
   if (r) return r;
   // every field back to the zero fill of bsamg_commit
@@ -1257,6 +1267,7 @@ int bsamg_hier_reset(bsamg_hier* h) {
 
 int bsamg_set_box_sweep(bsamg_hier* h, int kind) {
   if (!h || kind < 0 || kind > 2) return BSAMG_ERR_ARG;
+  h->box_g_valid = false;
   int r = set_device(*h);
   if (r) return r;
   if (h->committed) {  // captured graphs hold the other sweep kernel
@@ -1306,6 +1317,7 @@ int bsamg_time_smoother(bsamg_hier* h, int level, int mode, int reps, double* ms
   if (!h || !h->committed || !level_ok(*h, level) || reps < 1 || !ms_per_launch) return BSAMG_ERR_ARG;
   if (mode != BSAMG_MODE_FP64 && mode != BSAMG_MODE_MIXED) return BSAMG_ERR_ARG;
   RET(set_device(*h));
+  h->box_g_valid = false;  // the sweeps overwrite the box path's e
   RET(bsamg_mark(h, 62));
   for (int r = 0; r < reps; r++)
     RET(mode == BSAMG_MODE_FP64 ? enq_relax(*h, level, 1 + (r & 1)) : mixed_enq_relax(*h, level, 1 + (r & 1)));

@@ -101,6 +101,10 @@ struct Hier {
   // extents covering its parent; FP64 iterate held as float pairs
   bool box = false;
   int box_sweep = 1;  // 3D box colour sweep (box.cu): 0 two rows a thread, 1 four, 2 rows staged by bulk copies
+  // the box path's g holds the true residual of the finest level at the
+  // current q for the f in fhi/flo (set when box_iterations returns; any
+  // entry point that changes fields or coefficients clears it)
+  bool box_g_valid = false;
   int box_sms = 152;      // multiprocessors of the device (persistent grids)
   BoxLev blev[kNLev] = {};
   long long b_oqlo = 0, b_ofhi = 0, b_oflo = 0;  // float offsets (qhi is blev[finest].opb)

@@ -167,3 +167,36 @@ def test_box_sweep_forms_agree(pkg, ctx):
             h.set_box_sweep(3)
         finally:
             h.close()
+
+
+def test_box_step_reuses_the_last_residual(pkg, ctx):
+    """A box solve that follows one on the same q starts from the residual
+    the last one ended with, updated for the new f (r + (f_new - f_old)),
+    instead of evaluating the double-float operator again.  Against runs
+    forced to recompute it (any mutating call clears the reuse): the same
+    V-cycle counts, residual histories to 1e-6 relative or 1e-12 absolute
+    (the FP32 g rounds the two starting residuals differently) and iterates
+    to 1e-10; a put between steps is honoured."""
+    n = 64
+    runs = []
+    for cold in (False, True):
+        h = pkg.Hierarchy(ctx, 3, 2, "ch", [5e-4, 0.02])
+        h.build_uniform([n] * 3, -5, [2] * 6, [0, 0, 0], [1, 1, 1])
+        h.commit()
+        h.seed_spinodal(0, 17, mean=0.1, amp=0.05)
+        hist = []
+        for s in range(5):
+            if cold:
+                h.set_box_sweep(1)  # clears the reuse (and keeps the default sweep)
+            if s == 3:
+                q = h.get(0, "q")
+                h.put(0, "q", q * 0.999)
+            hist.append(h.time_step(s == 0, 0, -5, tol=1e-9, maxvcycles=30, mode="mixed", strict=True))
+        runs.append((hist, h.get(0, "q")))
+        h.close()
+    (ha, qa), (hb, qb) = runs
+    for (na, ra), (nb, rb) in zip(ha, hb):
+        assert na == nb, (ha, hb)
+        np.testing.assert_allclose(ra, rb, rtol=1e-6, atol=1e-12)
+    k = qa.size // 2
+    assert np.max(np.abs(qa[:k] - qb[:k])) <= 1e-10 * np.max(np.abs(qb[:k]))
