@@ -464,12 +464,6 @@ __device__ __forceinline__ void restrict_at(float* __restrict__ fp, const BoxLev
   Ec.v1[lc.own] = ECc.v1[lc.own] = s[1] * w;
   fp[C.opb + lc.own] = s[2] * w;
 }
-template <int DIM>
-__global__ void __launch_bounds__(256) k_bx_restrict(float* __restrict__ fp, BoxLev F, BoxLev C) {
-  int X = blockIdx.x * blockDim.x + threadIdx.x;
-  int Y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (X < C.n[0] && Y < C.n[1]) restrict_at<DIM>(fp, F, C, X, Y, blockIdx.z);
-}
 
 // CoarseLoadingFunction on the correction: coarse g = R(g - M(e)) + M_c(ec)
 template <int DIM>
@@ -497,11 +491,60 @@ __device__ __forceinline__ void coarse_load_at(float* __restrict__ fp, const Box
   Gc.v0[lc.own] = R0 * w + m0;
   Gc.v1[lc.own] = R1 * w + m1;
 }
+
+// RestrictSolution and the fine half of CoarseLoadingFunction in one pass
+// over the fine cells: coarse e = ec = R(e), coarse pb = R(pb) and coarse
+// g = R(g - M(e)); the coarse operator M_c(ec) needs the neighbours' ec, so
+// k_bx_coarse_op adds it in a second (coarse-sized) pass.  Every fine value
+// is loaded before the first store.
 template <int DIM>
-__global__ void __launch_bounds__(256) k_bx_coarse_load(float* __restrict__ fp, BoxLev F, BoxLev C) {
+__device__ __forceinline__ void restrict_load_at(float* __restrict__ fp, const BoxLev& F, const BoxLev& C, int X,
+                                                 int Y, int Z) {
+  V2 Ef = var2(fp, F.oe, F.half), Gf = var2(fp, F.og, F.half);
+  const float* PBf = fp + F.opb;
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, R0 = 0.f, R1 = 0.f;
+  const int nz = DIM == 3 ? 2 : 1;
+  for (int dz = 0; dz < nz; dz++)
+    for (int dy = 0; dy < 2; dy++)
+      for (int dx = 0; dx < 2; dx++) {
+        Loc<DIM> l(F, 2 * X + dx, 2 * Y + dy, DIM == 3 ? 2 * Z + dz : 0);
+        float pb = PBf[l.own];
+        s0 += Ef.v0[l.own];
+        s1 += Ef.v1[l.own];
+        s2 += pb;
+        float m0, m1;
+        mop<DIM>(Ef, F, l, pb, m0, m1);
+        R0 += Gf.v0[l.own] - m0;
+        R1 += Gf.v1[l.own] - m1;
+      }
+  const float w = DIM == 2 ? 0.25f : 0.125f;
+  Loc<DIM> lc(C, X, Y, Z);
+  V2 Ec = var2(fp, C.oe, C.half), ECc = var2(fp, C.oec, C.half), Gc = var2(fp, C.og, C.half);
+  Ec.v0[lc.own] = ECc.v0[lc.own] = s0 * w;
+  Ec.v1[lc.own] = ECc.v1[lc.own] = s1 * w;
+  fp[C.opb + lc.own] = s2 * w;
+  Gc.v0[lc.own] = R0 * w;
+  Gc.v1[lc.own] = R1 * w;
+}
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_restrict_load(float* __restrict__ fp, BoxLev F, BoxLev C) {
   int X = blockIdx.x * blockDim.x + threadIdx.x;
   int Y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (X < C.n[0] && Y < C.n[1]) coarse_load_at<DIM>(fp, F, C, X, Y, blockIdx.z);
+  if (X < C.n[0] && Y < C.n[1]) restrict_load_at<DIM>(fp, F, C, X, Y, blockIdx.z);
+}
+// coarse g += M_c(ec), the coarse operator on the restricted correction
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_coarse_op(float* __restrict__ fp, BoxLev C) {
+  int X = blockIdx.x * blockDim.x + threadIdx.x;
+  int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (X >= C.n[0] || Y >= C.n[1]) return;
+  Loc<DIM> lc(C, X, Y, blockIdx.z);
+  V2 ECc = var2(fp, C.oec, C.half), Gc = var2(fp, C.og, C.half);
+  float g0 = Gc.v0[lc.own], g1 = Gc.v1[lc.own];
+  float m0, m1;
+  mop<DIM>(ECc, C, lc, fp[C.opb + lc.own], m0, m1);
+  Gc.v0[lc.own] = g0 + m0;
+  Gc.v1[lc.own] = g1 + m1;
 }
 
 // CorrectFine on e: e_fine += P(e_c - ec), per-direction (3,1)/4 weights
@@ -909,8 +952,8 @@ int bx_vcycle(Hier& H, int level, int minlevel, int nsmooth, bool fresh) {
   if (level > minlevel) {
     BoxLev &F = B(H, level), &C = B(H, level - 1);
     Launch sc = shape(C.n[0], C.n[1], C.n[2]);
-    BX_LAUNCH(H, sc, k_bx_restrict, H.fpool, F, C);
-    BX_LAUNCH(H, sc, k_bx_coarse_load, H.fpool, F, C);
+    BX_LAUNCH(H, sc, k_bx_restrict_load, H.fpool, F, C);
+    BX_LAUNCH(H, sc, k_bx_coarse_op, H.fpool, C);
     if ((r = bx_vcycle(H, level - 1, minlevel, nsmooth, false))) return r;
     BX_LAUNCH(H, sc, k_bx_prolong, H.fpool, F, C);
     if ((r = bx_level_relax(H, level, nsmooth, false))) return r;

@@ -176,7 +176,8 @@ def test_box_step_reuses_the_last_residual(pkg, ctx):
     forced to recompute it (any mutating call clears the reuse): the same
     V-cycle counts, residual histories to 1e-6 relative or 1e-12 absolute
     (the FP32 g rounds the two starting residuals differently) and iterates
-    to 1e-10; a put between steps is honoured."""
+    to 1e-9 (the FP32 corrections round differently from there on; the
+    solve's tolerance is 1e-9); a put between steps is honoured."""
     n = 64
     runs = []
     for cold in (False, True):
@@ -199,4 +200,4 @@ def test_box_step_reuses_the_last_residual(pkg, ctx):
         assert na == nb, (ha, hb)
         np.testing.assert_allclose(ra, rb, rtol=1e-6, atol=1e-12)
     k = qa.size // 2
-    assert np.max(np.abs(qa[:k] - qb[:k])) <= 1e-10 * np.max(np.abs(qb[:k]))
+    assert np.max(np.abs(qa[:k] - qb[:k])) <= 1e-9 * np.max(np.abs(qb[:k]))
