@@ -226,8 +226,10 @@ int bsamg_time_step(bsamg_hier* h, int first, int finestlevel, int minlevel,
  *     copied over it), computed on the device and written as one patch.
  * bsamg_read_q -> ReadQ, :184-443: restart from a frame file.  `root` is a
  *     committed hierarchy holding the run's root grid and the levels below it
- *     (bsamg_build_uniform); the new hierarchy copies it, takes the root's q
- *     from the file (ghost layers included) and adds the file's refinement
+ *     (bsamg_build_uniform); the new hierarchy copies it, takes the root's
+ *     q(0:mx+1) from the file (a second ghost layer, mbc = 2, keeps the
+ *     root's values; the records are q(0:mx+1) whatever mbc is, as WriteQ
+ *     writes them) and adds the file's refinement
  *     patches (ids first_id, first_id + 1, ...; each parented by the patch of
  *     the level below that contains it; qold = q).  The root block is checked
  *     as ReadQ checks it (ndims, ratio 2, nrvars, dx, xlower, xupper, mx,
@@ -311,8 +313,9 @@ int bsamg_smoother_colours(bsamg_hier* h, int level, int mode, int* colours);
  * (a PyTorch caching allocator, a Fortran code with a fixed device-memory
  * plan) and serving loops that must not trigger the device-wide
  * synchronisation cudaMalloc/cudaFree imply while other streams run.
- * q (ghosted, nrvars = 2) and f (interior) are the caller's device arrays in
- * the Fortran layout above; the ErrorAFAS norm (errortype 1 or 2) is written
+ * q (one ghost layer, q(0:mx+1, ..., 1:2), the slice the reference passes
+ * to Operator2D/3D) and f (interior) are the caller's device arrays in the
+ * Fortran layout above; the ErrorAFAS norm (errortype 1 or 2) is written
  * to the caller's device double *norm_out, on `stream` (a cudaStream_t, or
  * NULL for the default stream).  The call allocates nothing: its block
  * partial sums live in a fixed file-scope device array, so a patch may have
