@@ -1,0 +1,195 @@
+"""The oracle against a literal numpy transcription of the reference's array
+statements (no GPU).
+
+The reference has no tests, so beyond the known-answer properties of
+test_oracle_kat.py the oracle's arithmetic is pinned here by a second,
+independent restatement of the Fortran source written as numpy array
+expressions in the source's own evaluation order (IEEE double, no fused
+multiply-add, like the oracle's -ffp-contract=off build):
+
+* CH RelaxGrid2D / RelaxGrid3D (PROBLEM/CH/problem.f90:318-369, :554-614):
+  one colour of the red-black update, compared bit for bit;
+* CH Operator2D / Operator3D with ULap2D / ULap3D (CH:393-422, :638-669;
+  LIBRARY/gridutilities.f90:50-72, :372-399) through Residual
+  (afasroutines.f90:817-857): rf bit for bit;
+* ErrorAFAS errortype 1 and 2 (afasroutines.f90:113-233) with SquareSum's
+  sequential SUM: the norm bit for bit;
+* BioGrowth RelaxGrid2D and Operator2D with Growth / Uptake
+  (PROBLEM/BioGrowth/problem.f90:255-353, :743-766): bit for bit.
+"""
+import numpy as np
+import pytest
+
+CH = dict(dt=1e-3, eps=0.02)
+BIO = dict(dt=0.1, eps=0.05, gamma=1.5, lam=2.0, czero=0.5)
+
+
+def hierarchy(oracle_mod, nd, problem, params, mx, seed):
+    o = oracle_mod.OracleHierarchy(nd, 2, problem, params)
+    o.build_uniform(list(mx) + [1] * (3 - nd), 0, [10] * 6, [0, 0, 0],
+                    [mx[d] / mx[0] if d < nd else 1.0 for d in range(3)])
+    o.commit()
+    rng = np.random.default_rng(seed)
+    fields = {}
+    for fld in ("q", "qold", "f"):
+        a = rng.uniform(-1, 1, size=o.field_size(0, fld))
+        o.put(0, fld, a)
+        fields[fld] = a
+    gh = [m + 2 for m in mx] + [2]
+    return o, {k: v.reshape(gh if k != "f" else list(mx) + [2], order="F") for k, v in fields.items()}
+
+
+def spacing(o):
+    return o.patch_table()[0]["dx"][0]
+
+
+def interior(nd, mx, di=(0, 0, 0)):
+    """slice of the ghosted array for interior cells shifted by di"""
+    return tuple(slice(1 + di[d], 1 + di[d] + mx[d]) for d in range(nd))
+
+
+def ulap(a, nd, mx):
+    """ULap2D / ULap3D: neighbours in the source's order minus (4|6) centre"""
+    e = np.eye(3, dtype=int)
+    r = a[interior(nd, mx, e[0])] + a[interior(nd, mx, -e[0])]
+    r = r + a[interior(nd, mx, e[1])]
+    r = r + a[interior(nd, mx, -e[1])]
+    if nd == 3:
+        r = r + a[interior(nd, mx, e[2])]
+        r = r + a[interior(nd, mx, -e[2])]
+    return r - (4.0 if nd == 2 else 6.0) * a[interior(nd, mx)]
+
+
+def colour_mask(nd, mx, ipass):
+    """cells i = 1 + MODULO(j (+k) + ipass, 2), ..., mx(1), 2"""
+    idx = np.indices(mx) + 1
+    return (idx.sum(axis=0) + ipass) % 2 == 1
+
+
+def ch_relax(q, f, nd, mx, h, ipass, dt, eps):
+    eps2 = eps * eps
+    h2 = h * h
+    tmp1, tmp2 = dt / h2, eps2 / h2
+    tmp3 = (4.0 if nd == 2 else 6.0) * eps2 / h2
+    a12 = (4.0 if nd == 2 else 6.0) * tmp1
+    e = np.eye(3, dtype=int)
+    q = q.copy()
+    c = interior(nd, mx)
+    phi, mu = q[c + (0,)], q[c + (1,)]
+
+    def nb(v, order):
+        s = None
+        for d, sgn in order:
+            t = q[interior(nd, mx, sgn * e[d]) + (v,)]
+            s = t if s is None else s + t
+        return s
+    if nd == 2:
+        s_mu = nb(1, [(0, -1), (0, 1), (1, -1), (1, 1)])   # q(i-1,j,2)+q(i+1,j,2)+q(i,j-1,2)+q(i,j+1,2)
+        s_phi = nb(0, [(0, 1), (0, -1), (1, 1), (1, -1)])  # q(i+1,j,1)+q(i-1,j,1)+q(i,j+1,1)+q(i,j-1,1)
+    else:
+        s_mu = nb(1, [(0, -1), (0, 1), (1, -1), (1, 1), (2, -1), (2, 1)])
+        s_phi = nb(0, [(0, 1), (0, -1), (1, 1), (1, -1), (2, 1), (2, -1)])
+    a21 = -3.0 * (phi * phi) - tmp3
+    b1 = f[..., 0] + tmp1 * s_mu
+    b2 = f[..., 1] - tmp2 * s_phi - 2.0 * ((phi * phi) * phi)
+    det = 1.0 - a12 * a21
+    new_phi = (b1 - a12 * b2) / det
+    new_mu = (b2 - a21 * b1) / det
+    m = colour_mask(nd, mx, ipass)
+    phi[m] = new_phi[m]
+    mu[m] = new_mu[m]
+    return q
+
+
+def ch_residual(q, f, nd, mx, h, dt, eps):
+    eps2 = eps * eps
+    h2 = h * h
+    tmp1, tmp2 = dt / h2, eps2 / h2
+    c = interior(nd, mx)
+    phi, mu = q[c + (0,)], q[c + (1,)]
+    op1 = phi - tmp1 * ulap(q[..., 1], nd, mx)
+    op2 = mu - ((phi * phi) * phi) + tmp2 * ulap(q[..., 0], nd, mx)
+    return np.stack([f[..., 0] - op1, f[..., 1] - op2], axis=-1)
+
+
+def error_afas(rf, errortype, nv=2):
+    """SQRT(SUM(rf*rf) / (nrvars * cells)) with SUM in element order
+    (errortype 1); the largest per-component value (errortype 2)"""
+    seq = lambda a: np.cumsum(np.ravel(a * a, order="F"))[-1]
+    cells = float(np.prod(rf.shape[:-1]))
+    if errortype == 1:
+        return float(np.sqrt(seq(rf) / (nv * cells)))
+    return float(max(np.sqrt(seq(rf[..., v]) / cells) for v in range(nv)))
+
+
+@pytest.mark.parametrize("nd,mx", [(2, (16, 12)), (3, (8, 6, 4))])
+def test_ch_relax_is_the_reference_statements(oracle_mod, nd, mx):
+    o, F = hierarchy(oracle_mod, nd, "ch", [CH["dt"], CH["eps"]], mx, 80 + nd)
+    h = spacing(o)
+    q = F["q"]
+    for ipass in (1, 2):
+        o.relax_level_color(0, ipass)
+        q = ch_relax(q, F["f"], nd, list(mx), h, ipass, CH["dt"], CH["eps"])
+        got = o.get(0, "q").reshape(q.shape, order="F")
+        assert np.array_equal(got, q), (ipass, np.max(np.abs(got - q)))
+
+
+@pytest.mark.parametrize("nd,mx", [(2, (16, 12)), (3, (8, 6, 4))])
+@pytest.mark.parametrize("errortype", [1, 2])
+def test_ch_residual_and_error_afas_are_the_reference_statements(oracle_mod, nd, mx, errortype):
+    o, F = hierarchy(oracle_mod, nd, "ch", [CH["dt"], CH["eps"]], mx, 90 + nd)
+    rf = ch_residual(F["q"], F["f"], nd, list(mx), spacing(o), CH["dt"], CH["eps"])
+    norm = o.residual_norm(0, errortype)
+    got = o.get(0, "rf").reshape(rf.shape, order="F")
+    assert np.array_equal(got, rf)
+    assert norm == error_afas(rf, errortype)
+
+
+def bio_relax(q, qold, f, mx, h, ipass, p):
+    dt, eps2 = p["dt"], p["eps"] * p["eps"]
+    h2 = h * h
+    tmp1, tmp3 = dt * eps2 / h2, 1.0 / h2
+    growth = lambda x: p["gamma"] * 0.5 * (x + 1.0)
+    uptake = lambda x: p["lam"] * 0.5 * (x + 1.0)
+    q = q.copy()
+    c = interior(2, mx)
+    e = np.eye(3, dtype=int)
+    sh = lambda v, d, s: q[interior(2, mx, s * e[d]) + (v,)]
+    phi, n, po = q[c + (0,)], q[c + (1,)], qold[c + (0,)]
+    tmp2 = 4.0 * tmp1 + 1.0 + dt * (phi * phi)
+    new_phi = (f[..., 0] + dt * growth(po) * (n - p["czero"])
+               + tmp1 * (sh(0, 0, -1) + sh(0, 0, 1) + sh(0, 1, -1) + sh(0, 1, 1))) / tmp2
+    m = colour_mask(2, mx, ipass)
+    phi[m] = new_phi[m]
+    tmp4 = 4.0 * tmp3 + uptake(po)
+    new_n = (f[..., 1] + tmp3 * (sh(1, 0, 1) + sh(1, 0, -1) + sh(1, 1, 1) + sh(1, 1, -1))) / tmp4
+    n[m] = new_n[m]
+    return q
+
+
+def bio_residual(q, qold, f, mx, h, p):
+    dt, eps2 = p["dt"], p["eps"] * p["eps"]
+    h2 = h * h
+    tmp1, tmp3 = dt * eps2 / h2, 1.0 / h2
+    growth = lambda x: p["gamma"] * 0.5 * (x + 1.0)
+    uptake = lambda x: p["lam"] * 0.5 * (x + 1.0)
+    c = interior(2, mx)
+    phi, n, po = q[c + (0,)], q[c + (1,)], qold[c + (0,)]
+    op1 = phi - tmp1 * ulap(q[..., 0], 2, mx) + dt * ((phi * phi) * phi) - dt * growth(po) * (n - p["czero"])
+    op2 = -tmp3 * ulap(q[..., 1], 2, mx) + uptake(po) * n
+    return np.stack([f[..., 0] - op1, f[..., 1] - op2], axis=-1)
+
+
+def test_biogrowth_relax_and_residual_are_the_reference_statements(oracle_mod):
+    mx = [16, 12]
+    params = [BIO["dt"], BIO["eps"], BIO["gamma"], BIO["lam"], BIO["czero"]]
+    o, F = hierarchy(oracle_mod, 2, "biogrowth", params, mx, 77)
+    h = spacing(o)
+    rf = bio_residual(F["q"], F["qold"], F["f"], mx, h, BIO)
+    assert o.residual_norm(0, 1) == error_afas(rf, 1)
+    assert np.array_equal(o.get(0, "rf").reshape(rf.shape, order="F"), rf)
+    q = F["q"]
+    for ipass in (1, 2):
+        o.relax_level_color(0, ipass)
+        q = bio_relax(q, F["qold"], F["f"], mx, h, ipass, BIO)
+        assert np.array_equal(o.get(0, "q").reshape(q.shape, order="F"), q), ipass
