@@ -15,7 +15,9 @@ multiply-add, like the oracle's -ffp-contract=off build):
 * ErrorAFAS errortype 1 and 2 (afasroutines.f90:113-233) with SquareSum's
   sequential SUM: the norm bit for bit;
 * BioGrowth RelaxGrid2D and Operator2D with Growth / Uptake
-  (PROBLEM/BioGrowth/problem.f90:255-353, :743-766): bit for bit.
+  (PROBLEM/BioGrowth/problem.f90:255-353, :743-766): bit for bit;
+* Interpolate2D, the coarse-fine ghost statements (LIBRARY/boundary.f90:
+  143-333) for ipass 0, 1 and 2: bit for bit.
 """
 import numpy as np
 import pytest
@@ -193,3 +195,87 @@ def test_biogrowth_relax_and_residual_are_the_reference_statements(oracle_mod):
         o.relax_level_color(0, ipass)
         q = bio_relax(q, F["qold"], F["f"], mx, h, ipass, BIO)
         assert np.array_equal(o.get(0, "q").reshape(q.shape, order="F"), q), ipass
+
+
+# --- Interpolate2D (LIBRARY/boundary.f90:143-333), constants :54-63 -------
+A1, A2, A3 = -1.0 / 5.0, 2.0 / 3.0, 8.0 / 15.0
+B1, B2, B3 = 5.0 / 32.0, 15.0 / 16.0, -3.0 / 32.0
+
+
+def interpolate2d(qf, qc, mx, mb, mthbc, ipass):
+    """The C/F ghost statements on qf(0:mx+1,0:my+1,:) from the parent's
+    qc(0:,0:,:); Fortran index = python index, a:b:2 inclusive."""
+    qf = qf.copy()
+    m0, m1 = mx
+    (l0, h0), (l1, h1) = mb
+    red, black = ipass in (1, 0), ipass in (2, 0)
+    s = lambda a, b: slice(a, b + 1, 2)
+    r = lambda a, b: slice(a, b + 1)
+    if red:
+        qf[m0 + 1, m1 + 1] = A1 * qf[m0 - 1, m1 - 1] + A2 * qf[m0, m1] + A3 * qc[h0 + 1, h1 + 1]
+        qf[0, 0] = A1 * qf[2, 2] + A2 * qf[1, 1] + A3 * qc[l0 - 1, l1 - 1]
+    if black:
+        qf[m0 + 1, 0] = A1 * qf[m0 - 1, 2] + A2 * qf[m0, 1] + A3 * qc[h0 + 1, l1 - 1]
+        qf[0, m1 + 1] = A1 * qf[2, m1 - 1] + A2 * qf[1, m1] + A3 * qc[l0 - 1, h1 + 1]
+    bsum = lambda u, v, w: A3 * (B1 * u + B2 * v + B3 * w)
+    if mthbc[0] in (2, 999):
+        if red:
+            qf[0, s(2, m1 - 2)] = A1 * qf[2, s(4, m1)] + A2 * qf[1, s(3, m1 - 1)] + A3 * qc[l0 - 1, r(l1, h1 - 1)]
+            qf[0, m1] = A1 * qf[2, m1] + A2 * qf[1, m1] + bsum(qc[l0 - 1, h1 + 1], qc[l0 - 1, h1], qc[l0 - 1, h1 - 1])
+        if black:
+            qf[0, s(3, m1 - 1)] = A1 * qf[2, s(1, m1 - 3)] + A2 * qf[1, s(2, m1 - 2)] + A3 * qc[l0 - 1, r(l1 + 1, h1)]
+            qf[0, 1] = A1 * qf[2, 1] + A2 * qf[1, 1] + bsum(qc[l0 - 1, l1 - 1], qc[l0 - 1, l1], qc[l0 - 1, l1 + 1])
+    if mthbc[1] in (2, 999):
+        if red:
+            qf[m0 + 1, s(3, m1 - 1)] = (A1 * qf[m0 - 1, s(1, m1 - 3)] + A2 * qf[m0, s(2, m1 - 2)]
+                                        + A3 * qc[h0 + 1, r(l1 + 1, h1)])
+            qf[m0 + 1, 1] = A1 * qf[m0 - 1, 1] + A2 * qf[m0, 1] + bsum(qc[h0 + 1, l1 - 1], qc[h0 + 1, l1],
+                                                                       qc[h0 + 1, l1 + 1])
+        if black:
+            qf[m0 + 1, s(2, m1 - 2)] = (A1 * qf[m0 - 1, s(4, m1)] + A2 * qf[m0, s(3, m1 - 1)]
+                                        + A3 * qc[h0 + 1, r(l1, h1 - 1)])
+            qf[m0 + 1, m1] = A1 * qf[m0 - 1, m1] + A2 * qf[m0, m1] + bsum(qc[h0 + 1, h1 + 1], qc[h0 + 1, h1],
+                                                                          qc[h0 + 1, h1 - 1])
+    if mthbc[2] in (2, 999):
+        if red:
+            qf[s(2, m0 - 2), 0] = A1 * qf[s(4, m0), 2] + A2 * qf[s(3, m0 - 1), 1] + A3 * qc[r(l0, h0 - 1), l1 - 1]
+            qf[m0, 0] = A1 * qf[m0, 2] + A2 * qf[m0, 1] + bsum(qc[h0 + 1, l1 - 1], qc[h0, l1 - 1], qc[h0 - 1, l1 - 1])
+        if black:
+            qf[s(3, m0 - 1), 0] = A1 * qf[s(1, m0 - 3), 2] + A2 * qf[s(2, m0 - 2), 1] + A3 * qc[r(l0 + 1, h0), l1 - 1]
+            qf[1, 0] = A1 * qf[1, 2] + A2 * qf[1, 1] + bsum(qc[l0 - 1, l1 - 1], qc[l0, l1 - 1], qc[l0 + 1, l1 - 1])
+    if mthbc[3] in (2, 999):
+        if red:
+            qf[s(3, m0 - 1), m1 + 1] = (A1 * qf[s(1, m0 - 3), m1 - 1] + A2 * qf[s(2, m0 - 2), m1]
+                                        + A3 * qc[r(l0 + 1, h0), h1 + 1])
+            qf[1, m1 + 1] = A1 * qf[1, m1 - 1] + A2 * qf[1, m1] + bsum(qc[l0 - 1, h1 + 1], qc[l0, h1 + 1],
+                                                                       qc[l0 + 1, h1 + 1])
+        if black:
+            qf[s(2, m0 - 2), m1 + 1] = (A1 * qf[s(4, m0), m1 - 1] + A2 * qf[s(3, m0 - 1), m1]
+                                        + A3 * qc[r(l0, h0 - 1), h1 + 1])
+            qf[m0, m1 + 1] = A1 * qf[m0, m1 - 1] + A2 * qf[m0, m1] + bsum(qc[h0 + 1, h1 + 1], qc[h0, h1 + 1],
+                                                                          qc[h0 - 1, h1 + 1])
+    return qf
+
+
+@pytest.mark.parametrize("ipass", [0, 1, 2])
+def test_cf_interpolation_2d_is_the_reference_statements(oracle_mod, ipass):
+    """SetGhost on a child with internal faces only (no siblings, no
+    physical or periodic faces) is Interpolate2D alone."""
+    from tests import hierarchies as H
+    s = H.Spec(2)
+    s.root_and_below(16, 0, [10] * 6)
+    s.child(0, 101, [5, 4], [10, 11])  # 12 x 16 fine cells, faces internal
+    o = oracle_mod.OracleHierarchy(2, 2, "ch", [CH["dt"], CH["eps"]])
+    s.apply(o)
+    rng = np.random.default_rng(50 + ipass)
+    q = {}
+    for p in s.patches:
+        a = rng.uniform(-1, 1, size=o.field_size(p["id"], "q"))
+        o.put(p["id"], "q", a)
+        q[p["id"]] = a.reshape([m + 2 for m in p["mx"][:2]] + [2], order="F")
+    child = s.patches[-1]
+    o.set_ghost(1, ipass)
+    mb = [(child["mbounds"][0], child["mbounds"][1]), (child["mbounds"][2], child["mbounds"][3])]
+    want = interpolate2d(q[101], q[0], child["mx"][:2], mb, child["mthbc"][:4], ipass)
+    got = o.get(101, "q").reshape(want.shape, order="F")
+    assert np.array_equal(got, want)
