@@ -1383,6 +1383,22 @@ int bsamo_correct_fine(bsamo_hier* h, int level) {
   return 0;
 }
 
+/* one operation of the V-cycle's coarse branch on every patch of a level
+ * (ApplyOnLevel, afasroutines.f90:505-512): 1 RestrictSolution, 2
+ * GetCoarseGhostPoints, 3 CoarseLoadingFunction */
+int bsamo_level_op(bsamo_hier* h, int level, int which) {
+  if (!h || !h->committed || level < -MAXDEPTH || level > MAXDEPTH || which < 1 || which > 3) return -1;
+  for (int n = 0; n < nlev(h, level); n++)
+    if (lev_patch(h, level, n)->parent < 0) return -1;
+  for (int n = 0; n < nlev(h, level); n++) {
+    OPatch* p = lev_patch(h, level, n);
+    if (which == 1) restrict_solution(h, p);
+    else if (which == 2) get_coarse_ghost_points(h, p);
+    else coarse_loading(h, p);
+  }
+  return 0;
+}
+
 static void prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double* out);
 /* one variable of P1MC / P2MC (InitFields' prolongation) alone */
 int bsamo_prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double* out) {

@@ -92,6 +92,7 @@ def lib():
         L.bsamo_copy_q_to_qold.argtypes = [P, I, I]
         L.bsamo_vcycle.argtypes = [P, I, I, I]
         L.bsamo_correct_fine.argtypes = [P, I]
+        L.bsamo_level_op.argtypes = [P, I, I]
         L.bsamo_prolong_mc.argtypes = [I, I, DP, IP, DP]
         L.bsamo_residual_norm.argtypes = [P, I, I, DP]
         L.bsamo_multigrid_iterations.argtypes = [P, I, I, I, I, D, I, I, IP, DP]
@@ -205,6 +206,12 @@ class OracleHierarchy:
 
     def correct_fine(self, level):
         _check(lib().bsamo_correct_fine(self.h, level), "correct_fine")
+
+    def level_op(self, level, which):
+        """RestrictSolution, GetCoarseGhostPoints or CoarseLoadingFunction
+        on every patch of a level ("restrict", "coarse_ghost", "coarse_load")"""
+        code = {"restrict": 1, "coarse_ghost": 2, "coarse_load": 3}[which]
+        _check(lib().bsamo_level_op(self.h, level, code), "level_op")
 
     def residual_norm(self, level, errortype=1):
         r = ctypes.c_double()

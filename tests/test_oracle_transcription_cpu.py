@@ -17,7 +17,11 @@ multiply-add, like the oracle's -ffp-contract=off build):
 * BioGrowth RelaxGrid2D and Operator2D with Growth / Uptake
   (PROBLEM/BioGrowth/problem.f90:255-353, :743-766): bit for bit;
 * Interpolate2D, the coarse-fine ghost statements (LIBRARY/boundary.f90:
-  143-333) for ipass 0, 1 and 2: bit for bit.
+  143-333) for ipass 0, 1 and 2: bit for bit;
+* the V-cycle's coarse branch in 2D and 3D: RestrictSolution with
+  Restriction2D/3D, GetCoarseGhostPoints and CoarseLoadingFunction (the
+  child's Residual, then Restriction(rf) + Operator(qc) at the parent's
+  spacing): bit for bit.
 """
 import numpy as np
 import pytest
@@ -279,3 +283,85 @@ def test_cf_interpolation_2d_is_the_reference_statements(oracle_mod, ipass):
     want = interpolate2d(q[101], q[0], child["mx"][:2], mb, child["mthbc"][:4], ipass)
     got = o.get(101, "q").reshape(want.shape, order="F")
     assert np.array_equal(got, want)
+
+
+# --- RestrictSolution, GetCoarseGhostPoints, CoarseLoadingFunction --------
+# (afasroutines.f90:610-652, :673-736; boundary.f90:957-1015; Restriction2D/
+# 3D gridutilities.f90:103-127, :437-468)
+
+def restriction(a, nd):
+    """a: interior values (Fortran 1..mx -> python 0..mx-1), variables last;
+    2:mx:2 is python 1::2 and 1:mx-1:2 python 0::2"""
+    e, o = slice(1, None, 2), slice(0, None, 2)
+    if nd == 2:
+        return 0.25 * (a[e, e] + a[o, e] + a[e, o] + a[o, o])
+    t = [(e, e, e), (o, e, e), (e, o, e), (o, o, e), (e, e, o), (o, e, o), (e, o, o), (o, o, o)]
+    s = a[t[0]]
+    for x in t[1:]:
+        s = s + a[x]
+    return 0.125 * s
+
+
+def ch_operator(q, nd, mx, h, dt, eps):
+    eps2 = eps * eps
+    h2 = h * h
+    tmp1, tmp2 = dt / h2, eps2 / h2
+    c = interior(nd, mx)
+    phi, mu = q[c + (0,)], q[c + (1,)]
+    return np.stack([phi - tmp1 * ulap(q[..., 1], nd, mx),
+                     mu - ((phi * phi) * phi) + tmp2 * ulap(q[..., 0], nd, mx)], axis=-1)
+
+
+@pytest.mark.parametrize("nd", [2, 3])
+def test_coarse_branch_is_the_reference_statements(oracle_mod, nd):
+    from tests import hierarchies as H
+    s = H.Spec(nd)
+    if nd == 2:
+        s.root_and_below(16, 0, [10] * 6)
+        s.child(0, 101, [3, 5], [8, 12])
+    else:
+        s.root_and_below(8, 0, [10] * 6)
+        s.child(0, 101, [2, 3, 2], [5, 6, 7])
+    o = oracle_mod.OracleHierarchy(nd, 2, "ch", [CH["dt"], CH["eps"]])
+    s.apply(o)
+    root, child = s.patches[0], s.patches[-1]
+    rng = np.random.default_rng(60 + nd)
+    arr = {}
+    for p in (root, child):
+        for fld in ("q", "qold", "qc", "f"):
+            a = rng.uniform(-1, 1, size=o.field_size(p["id"], fld))
+            o.put(p["id"], fld, a)
+            arr[p["id"], fld] = a
+    mx, cmx, pmx = child["mx"][:nd], [m // 2 for m in child["mx"][:nd]], root["mx"][:nd]
+    shp = lambda m, g: [x + 2 * g for x in m] + [2]
+    q = arr[101, "q"].reshape(shp(mx, 1), order="F")
+    qc = arr[101, "qc"].reshape(shp(cmx, 1), order="F")
+    pq = arr[0, "q"].reshape(shp(pmx, 1), order="F")
+    f = arr[101, "f"].reshape(shp(mx, 0), order="F")
+    lo = [child["mbounds"][2 * d] for d in range(nd)]
+    under = tuple(slice(lo[d], lo[d] + cmx[d]) for d in range(nd))  # parent cells mb(1):mb(2)
+    # RestrictSolution
+    o.level_op(1, "restrict")
+    r = restriction(q[interior(nd, mx)], nd)
+    qc[interior(nd, cmx)] = r
+    pq[under] = r
+    assert np.array_equal(o.get(101, "qc").reshape(qc.shape, order="F"), qc)
+    assert np.array_equal(o.get(0, "q").reshape(pq.shape, order="F"), pq)
+    # GetCoarseGhostPoints: every ring cell of qc(0:cmx+1) from parent%q(mb-1+i, ...)
+    o.level_op(1, "coarse_ghost")
+    idx = np.indices([c + 2 for c in cmx])
+    ring = np.zeros(idx.shape[1:], dtype=bool)
+    for d in range(nd):
+        ring |= (idx[d] == 0) | (idx[d] == cmx[d] + 1)
+    for cell in zip(*np.nonzero(ring)):
+        qc[cell] = pq[tuple(lo[d] - 1 + cell[d] for d in range(nd))]
+    assert np.array_equal(o.get(101, "qc").reshape(qc.shape, order="F"), qc)
+    # CoarseLoadingFunction: Residual on the child, then parent%f(mb) =
+    # Restriction(rf) + Operator(qc(0:cmx+1)) at the parent's spacing
+    o.level_op(1, "coarse_load")
+    rf = f - ch_operator(q, nd, mx, child["dx"][0], CH["dt"], CH["eps"])
+    pf = arr[0, "f"].reshape(shp(pmx, 0), order="F").copy()
+    pf[tuple(slice(lo[d] - 1, lo[d] - 1 + cmx[d]) for d in range(nd))] = (
+        restriction(rf, nd) + ch_operator(qc, nd, cmx, root["dx"][0], CH["dt"], CH["eps"]))
+    assert np.array_equal(o.get(101, "rf").reshape(rf.shape, order="F"), rf)
+    assert np.array_equal(o.get(0, "f").reshape(pf.shape, order="F"), pf)
