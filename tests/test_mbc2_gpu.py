@@ -223,3 +223,23 @@ def test_mixed_path_with_two_ghost_layers(pkg, ctx, oracle_mod):
         b = inner(o.get(p["id"], "q"), p["mx"][:2], 2, 2)[..., 0]
         worst = max(worst, float(np.max(np.abs(a - b)) / np.max(np.abs(b))))
     assert worst <= 1e-9, worst
+
+
+@pytest.mark.parametrize("nd,mthbc", [(2, [10, 10, 10, 10]), (2, [2, 2, 10, 10]), (2, [2, 2, 2, 2]),
+                                      (3, [10] * 6), (3, [2, 2, 10, 10, 2, 2]), (3, [2] * 6)])
+@pytest.mark.parametrize("mbc", [1, 2])
+def test_root_ghosts_with_offsets_match_oracle(pkg, ctx, oracle_mod, nd, mthbc, mbc):
+    """SelfPeriodicBC with a quasi-periodic offset (qpo) and SetPhysicalBC on
+    a root patch, one and two ghost layers: the whole array bit for bit."""
+    mx = [12, 8, 6][:nd]
+    qpo = [0.25, -0.5]
+    hs = [pkg.Hierarchy(ctx, nd, 2, "ch", [1e-3, 0.02], qpo=qpo, mbc=mbc),
+          oracle_mod.OracleHierarchy(nd, 2, "ch", [1e-3, 0.02], qpo=qpo, mbc=mbc)]
+    a = np.random.default_rng(sum(mthbc) + 7 * mbc + nd).uniform(-1, 1, size=int(np.prod([m + 2 * mbc for m in mx])) * 2)
+    for h in hs:
+        h.build_uniform(mx + [1] * (3 - nd), 0, mthbc + [10] * (6 - 2 * nd), [0, 0, 0],
+                        [mx[d] / mx[0] if d < nd else 1.0 for d in range(3)])
+        h.commit()
+        h.put(0, "q", a)
+        h.set_ghost(0, 0)
+    assert np.array_equal(hs[0].get(0, "q"), hs[1].get(0, "q"))

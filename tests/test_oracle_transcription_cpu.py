@@ -21,7 +21,10 @@ multiply-add, like the oracle's -ffp-contract=off build):
 * the V-cycle's coarse branch in 2D and 3D: RestrictSolution with
   Restriction2D/3D, GetCoarseGhostPoints and CoarseLoadingFunction (the
   child's Residual, then Restriction(rf) + Operator(qc) at the parent's
-  spacing): bit for bit.
+  spacing): bit for bit;
+* SelfPeriodicBC with the quasi-periodic offset qpo and SetPhysicalBC with
+  CH UserBC2D / UserBC3D (boundary.f90:478-575, :640-800; CH:770-881) on a
+  root patch, one and two ghost layers: bit for bit.
 """
 import numpy as np
 import pytest
@@ -365,3 +368,58 @@ def test_coarse_branch_is_the_reference_statements(oracle_mod, nd):
         restriction(rf, nd) + ch_operator(qc, nd, cmx, root["dx"][0], CH["dt"], CH["eps"]))
     assert np.array_equal(o.get(101, "rf").reshape(rf.shape, order="F"), rf)
     assert np.array_equal(o.get(0, "f").reshape(pf.shape, order="F"), pf)
+
+
+# --- SelfPeriodicBC and SetPhysicalBC2D/3D with CH UserBC2D/3D -----------
+# (boundary.f90:478-575, :640-800; CH/problem.f90:770-881).  A root patch:
+# SetGhost(rootlevel) is SelfPeriodicBC then SetPhysicalBC.
+
+def root_ghosts(q, nd, mx, mbc, mthbc, qpo):
+    """q indexed from 1-mbc (python = Fortran + mbc - 1), variables last"""
+    q = q.copy()
+    o = mbc - 1
+    F = lambda i: i + o  # Fortran index -> python index
+    nv = q.shape[-1]
+    ax = lambda d, i: tuple(F(i) if e == d else slice(None) for e in range(nd))
+    # SelfPeriodicBC: x with the quasi-periodic offset, then y (then z)
+    if mthbc[0] == 2 and mthbc[1] == 2:
+        for ibc in range(1, mbc + 1):
+            for n in range(nv):
+                q[ax(0, mx[0] + ibc) + (n,)] = q[ax(0, ibc) + (n,)] + qpo[n]
+                q[ax(0, 1 - ibc) + (n,)] = q[ax(0, mx[0] + 1 - ibc) + (n,)] - qpo[n]
+    for d in range(1, nd):
+        if mthbc[2 * d] == 2 and mthbc[2 * d + 1] == 2:
+            for ibc in range(1, mbc + 1):
+                q[ax(d, mx[d] + ibc)] = q[ax(d, ibc)]
+                q[ax(d, 1 - ibc)] = q[ax(d, mx[d] + 1 - ibc)]
+    # SetPhysicalBC: faces in order, UserBC2D reflects, UserBC3D is 2 - q
+    refl = (lambda v: v) if nd == 2 else (lambda v: 2.0 - v)
+    for face in range(2 * nd):
+        if mthbc[face] != 10:
+            continue
+        d, hi = face // 2, face % 2
+        for ibc in range(1, mbc + 1):
+            if hi:
+                q[ax(d, mx[d] + ibc)] = refl(q[ax(d, mx[d] - ibc + 1)])
+            else:
+                q[ax(d, 1 - ibc)] = refl(q[ax(d, ibc)])
+    return q
+
+
+@pytest.mark.parametrize("nd,mthbc", [(2, [10, 10, 10, 10]), (2, [2, 2, 10, 10]), (2, [2, 2, 2, 2]),
+                                      (3, [10] * 6), (3, [2, 2, 10, 10, 2, 2]), (3, [2] * 6)])
+@pytest.mark.parametrize("mbc", [1, 2])
+def test_root_ghosts_are_the_reference_statements(oracle_mod, nd, mthbc, mbc):
+    mx = [12, 8, 6][:nd]
+    qpo = [0.25, -0.5]
+    o = oracle_mod.OracleHierarchy(nd, 2, "ch", [CH["dt"], CH["eps"]], qpo=qpo, mbc=mbc)
+    o.build_uniform(mx + [1] * (3 - nd), 0, mthbc + [10] * (6 - 2 * nd), [0, 0, 0],
+                    [mx[d] / mx[0] if d < nd else 1.0 for d in range(3)])
+    o.commit()
+    rng = np.random.default_rng(sum(mthbc) + 7 * mbc + nd)
+    a = rng.uniform(-1, 1, size=o.field_size(0, "q"))
+    o.put(0, "q", a)
+    q = a.reshape([m + 2 * mbc for m in mx] + [2], order="F")
+    o.set_ghost(0, 0)
+    want = root_ghosts(q, nd, mx, mbc, mthbc, qpo)
+    assert np.array_equal(o.get(0, "q").reshape(want.shape, order="F"), want)
