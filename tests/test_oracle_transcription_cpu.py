@@ -24,7 +24,9 @@ multiply-add, like the oracle's -ffp-contract=off build):
   spacing): bit for bit;
 * SelfPeriodicBC with the quasi-periodic offset qpo and SetPhysicalBC with
   CH UserBC2D / UserBC3D (boundary.f90:478-575, :640-800; CH:770-881) on a
-  root patch, one and two ghost layers: bit for bit.
+  root patch, one and two ghost layers: bit for bit;
+* TransferBC / GhostOverlap between touching siblings after their
+  Interpolate2D (boundary.f90:336-480): bit for bit.
 """
 import numpy as np
 import pytest
@@ -423,3 +425,46 @@ def test_root_ghosts_are_the_reference_statements(oracle_mod, nd, mthbc, mbc):
     o.set_ghost(0, 0)
     want = root_ghosts(q, nd, mx, mbc, mthbc, qpo)
     assert np.array_equal(o.get(0, "q").reshape(want.shape, order="F"), want)
+
+
+# --- TransferBC / GhostOverlap (boundary.f90:336-480) after Interpolate2D --
+
+def ghost_overlap(q1, q2, mg1, mg2, mbc, nd):
+    """grid1's ghost cells from grid2's interior and back; q indexed from 0
+    (mbc = 1: python = Fortran), mg = [(lo, hi)] per dimension"""
+    ovg = [(max(mg1[n][0] - mbc, mg2[n][0] - mbc), min(mg1[n][1] + mbc, mg2[n][1] + mbc)) for n in range(nd)]
+    if any(h < l for l, h in ovg):
+        return
+    ov1 = [(max(ovg[n][0], mg2[n][0]), min(ovg[n][1], mg2[n][1])) for n in range(nd)]
+    ov2 = [(max(ovg[n][0], mg1[n][0]), min(ovg[n][1], mg1[n][1])) for n in range(nd)]
+    loc = lambda ov, mg: tuple(slice(ov[n][0] - mg[n][0] + 1, ov[n][1] - mg[n][0] + 2) for n in range(nd))
+    q1[loc(ov1, mg1)] = q2[loc(ov1, mg2)]
+    q2[loc(ov2, mg2)] = q1[loc(ov2, mg1)]
+
+
+def test_sibling_transfer_after_interpolation_is_the_reference_statements(oracle_mod):
+    """Two touching siblings with internal faces: SetGhost(level, 0) is
+    Interpolate2D on each, then GhostOverlap of the pair."""
+    from tests import hierarchies as H
+    s = H.Spec(2)
+    s.root_and_below(16, 0, [10] * 6)
+    s.child(0, 101, [3, 3], [6, 8])
+    s.child(0, 102, [7, 5], [10, 10])
+    o = oracle_mod.OracleHierarchy(2, 2, "ch", [CH["dt"], CH["eps"]])
+    s.apply(o)
+    rng = np.random.default_rng(99)
+    q = {}
+    for p in s.patches:
+        a = rng.uniform(-1, 1, size=o.field_size(p["id"], "q"))
+        o.put(p["id"], "q", a)
+        q[p["id"]] = a.reshape([m + 2 for m in p["mx"][:2]] + [2], order="F")
+    o.set_ghost(1, 0)
+    want = {}
+    for p in s.patches[1:]:
+        mb = [(p["mbounds"][0], p["mbounds"][1]), (p["mbounds"][2], p["mbounds"][3])]
+        want[p["id"]] = interpolate2d(q[p["id"]], q[0], p["mx"][:2], mb, p["mthbc"][:4], 0)
+    a, b = s.patches[1], s.patches[2]
+    mg = lambda p: [(p["mglobal"][0], p["mglobal"][1]), (p["mglobal"][2], p["mglobal"][3])]
+    ghost_overlap(want[101], want[102], mg(a), mg(b), 1, 2)
+    for pid in (101, 102):
+        assert np.array_equal(o.get(pid, "q").reshape(want[pid].shape, order="F"), want[pid]), pid
