@@ -26,7 +26,10 @@ multiply-add, like the oracle's -ffp-contract=off build):
   CH UserBC2D / UserBC3D (boundary.f90:478-575, :640-800; CH:770-881) on a
   root patch, one and two ghost layers: bit for bit;
 * TransferBC / GhostOverlap between touching siblings after their
-  Interpolate2D (boundary.f90:336-480): bit for bit.
+  Interpolate2D (boundary.f90:336-480): bit for bit;
+* AFASVcycle / LevelRelax (afasroutines.f90:495-557) as the reference's
+  sequence of those operations on 2D and 3D AMR hierarchies: the oracle's
+  V-cycle equals it bit for bit.
 """
 import numpy as np
 import pytest
@@ -468,3 +471,51 @@ def test_sibling_transfer_after_interpolation_is_the_reference_statements(oracle
     ghost_overlap(want[101], want[102], mg(a), mg(b), 1, 2)
     for pid in (101, 102):
         assert np.array_equal(o.get(pid, "q").reshape(want[pid].shape, order="F"), want[pid]), pid
+
+
+# --- AFASVcycle / LevelRelax composition (afasroutines.f90:495-557) -------
+
+def afas_vcycle(o, level, minlevel, nsmooth):
+    """The reference's recursive V-cycle written with the oracle's single
+    operations (each pinned above): LevelRelax, then RestrictSolution,
+    SetGhost(level-1, 0), GetCoarseGhostPoints, GetCoarseLevelLoading, the
+    coarser cycle, CorrectFine, SetGhost(level, 0), LevelRelax"""
+    def level_relax(l):
+        for _ in range(nsmooth):
+            for rb in (1, 2):
+                o.relax_level_color(l, rb)
+                o.set_ghost(l, rb)
+    level_relax(level)
+    if level > minlevel:
+        o.level_op(level, "restrict")
+        o.set_ghost(level - 1, 0)
+        o.level_op(level, "coarse_ghost")
+        o.level_op(level, "coarse_load")
+        afas_vcycle(o, level - 1, minlevel, nsmooth)
+        o.correct_fine(level)
+        o.set_ghost(level, 0)
+        level_relax(level)
+
+
+@pytest.mark.parametrize("nd", [2, 3])
+def test_vcycle_is_the_reference_composition(oracle_mod, nd):
+    """The oracle's V-cycle equals the reference's sequence of operations on
+    an AMR hierarchy with levels below the root, bit for bit."""
+    from tests import hierarchies as H
+    s = H.amr2d(periodic=True) if nd == 2 else H.amr3d(periodic=False)
+    params = [1e-3, 0.01] if nd == 2 else [5e-4, 0.02]
+    a, b = (oracle_mod.OracleHierarchy(nd, 2, "ch", params) for _ in range(2))
+    s.apply(a)
+    s.apply(b)
+    rng = np.random.default_rng(5 + nd)
+    for p in s.patches:
+        for fld in ("q", "qold", "f"):
+            v = rng.uniform(-1, 1, size=a.field_size(p["id"], fld))
+            a.put(p["id"], fld, v)
+            b.put(p["id"], fld, v)
+    fin, mn = s.finest(), s.minlevel()
+    a.vcycle(fin, mn, 2)
+    afas_vcycle(b, fin, mn, 2)
+    for p in s.patches:
+        for fld in ("q", "qc", "f", "rf"):
+            assert np.array_equal(a.get(p["id"], fld), b.get(p["id"], fld)), (p["id"], fld)
