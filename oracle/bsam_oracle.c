@@ -1383,18 +1383,28 @@ int bsamo_correct_fine(bsamo_hier* h, int level) {
   return 0;
 }
 
-/* one operation of the V-cycle's coarse branch on every patch of a level
- * (ApplyOnLevel, afasroutines.f90:505-512): 1 RestrictSolution, 2
- * GetCoarseGhostPoints, 3 CoarseLoadingFunction */
+static void get_source(bsamo_hier* h, OPatch* p);
+static void update_source(bsamo_hier* h, OPatch* p);
+static void fill_down_level(bsamo_hier* h, OPatch* p, int field);
+/* one per-patch operation on every patch of a level (ApplyOnLevel,
+ * treeops.f90:515-552): 1 RestrictSolution, 2 GetCoarseGhostPoints,
+ * 3 CoarseLoadingFunction, 4 GetSourceFunction, 5 UpdateSourceFunction,
+ * 6 FillDownLevel(source), 7 FillDownLevel(solution) */
 int bsamo_level_op(bsamo_hier* h, int level, int which) {
-  if (!h || !h->committed || level < -MAXDEPTH || level > MAXDEPTH || which < 1 || which > 3) return -1;
-  for (int n = 0; n < nlev(h, level); n++)
-    if (lev_patch(h, level, n)->parent < 0) return -1;
+  if (!h || !h->committed || level < -MAXDEPTH || level > MAXDEPTH || which < 1 || which > 7) return -1;
+  if (which != 4 && which != 5)
+    for (int n = 0; n < nlev(h, level); n++)
+      if (lev_patch(h, level, n)->parent < 0) return -1;
   for (int n = 0; n < nlev(h, level); n++) {
     OPatch* p = lev_patch(h, level, n);
-    if (which == 1) restrict_solution(h, p);
-    else if (which == 2) get_coarse_ghost_points(h, p);
-    else coarse_loading(h, p);
+    switch (which) {
+      case 1: restrict_solution(h, p); break;
+      case 2: get_coarse_ghost_points(h, p); break;
+      case 3: coarse_loading(h, p); break;
+      case 4: get_source(h, p); break;
+      case 5: update_source(h, p); break;
+      default: fill_down_level(h, p, which == 6 ? 1 : 2); break;
+    }
   }
   return 0;
 }
@@ -1408,22 +1418,25 @@ int bsamo_prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double*
 }
 
 /* FillDown / FillDownLevel, afasroutines.f90:236-327 (1 = source, 2 = q) */
+/* FillDownLevel, afasroutines.f90:262-327: parent f (field 1) or q (2)
+ * under the patch = Restriction of the patch's */
+static void fill_down_level(bsamo_hier* h, OPatch* p, int field) {
+  OPatch* par = parent_of(h, p);
+  int kc = h->ndims == 3 ? p->cmx[2] : 1;
+  for (int v = 0; v < h->nrvars; v++)
+    for (int k = 1; k <= kc; k++)
+      for (int j = 1; j <= p->cmx[1]; j++)
+        for (int i = 1; i <= p->cmx[0]; i++) {
+          int pi = p->mbounds[0][0] + i - 1, pj = p->mbounds[1][0] + j - 1;
+          int pk = h->ndims == 3 ? p->mbounds[2][0] + k - 1 : 1;
+          if (field == 1) FF(par, pi, pj, pk, v) = restrict_at(h, p, get_f, i, j, k, v);
+          else Q(par, pi, pj, pk, v) = restrict_at(h, p, get_q, i, j, k, v);
+        }
+}
+
 static void fill_down(bsamo_hier* h, int field, int finest, int minlevel) {
   for (int level = finest; level >= minlevel + 1; level--) {
-    for (int a = 0; a < nlev(h, level); a++) {
-      OPatch* p = lev_patch(h, level, a);
-      OPatch* par = parent_of(h, p);
-      int kc = h->ndims == 3 ? p->cmx[2] : 1;
-      for (int v = 0; v < h->nrvars; v++)
-        for (int k = 1; k <= kc; k++)
-          for (int j = 1; j <= p->cmx[1]; j++)
-            for (int i = 1; i <= p->cmx[0]; i++) {
-              int pi = p->mbounds[0][0] + i - 1, pj = p->mbounds[1][0] + j - 1;
-              int pk = h->ndims == 3 ? p->mbounds[2][0] + k - 1 : 1;
-              if (field == 1) FF(par, pi, pj, pk, v) = restrict_at(h, p, get_f, i, j, k, v);
-              else Q(par, pi, pj, pk, v) = restrict_at(h, p, get_q, i, j, k, v);
-            }
-    }
+    for (int a = 0; a < nlev(h, level); a++) fill_down_level(h, lev_patch(h, level, a), field);
     if (field == 2) set_ghost(h, level - 1, 0);
   }
 }

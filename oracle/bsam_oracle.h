@@ -79,8 +79,10 @@ int bsamo_copy_q_to_qold(bsamo_hier* h, int minlevel, int finestlevel);
 int bsamo_vcycle(bsamo_hier* h, int level, int minlevel, int nsmooth);
 /* CorrectFine on every patch of a level (parent%q - qc, q += P1/P2 of it) */
 int bsamo_correct_fine(bsamo_hier* h, int level);
-/* RestrictSolution (which = 1), GetCoarseGhostPoints (2) or
- * CoarseLoadingFunction (3) on every patch of a level */
+/* a per-patch operation on every patch of a level: RestrictSolution (which
+ * = 1), GetCoarseGhostPoints (2), CoarseLoadingFunction (3),
+ * GetSourceFunction (4), UpdateSourceFunction (5), FillDownLevel of f (6)
+ * or of q (7) */
 int bsamo_level_op(bsamo_hier* h, int level, int which);
 /* P1MC (mbc = 1) / P2MC (mbc = 2) of one variable: a has cmx+2 mbc cells per
  * used dimension, out 2 cmx + 2 mbc (Fortran order, ghost layers included) */

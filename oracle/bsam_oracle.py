@@ -208,9 +208,11 @@ class OracleHierarchy:
         _check(lib().bsamo_correct_fine(self.h, level), "correct_fine")
 
     def level_op(self, level, which):
-        """RestrictSolution, GetCoarseGhostPoints or CoarseLoadingFunction
-        on every patch of a level ("restrict", "coarse_ghost", "coarse_load")"""
-        code = {"restrict": 1, "coarse_ghost": 2, "coarse_load": 3}[which]
+        """a per-patch operation on every patch of a level: "restrict",
+        "coarse_ghost", "coarse_load", "get_source", "update_source",
+        "fill_f", "fill_q" (FillDownLevel of f or q)"""
+        code = {"restrict": 1, "coarse_ghost": 2, "coarse_load": 3, "get_source": 4, "update_source": 5,
+                "fill_f": 6, "fill_q": 7}[which]
         _check(lib().bsamo_level_op(self.h, level, code), "level_op")
 
     def residual_norm(self, level, errortype=1):

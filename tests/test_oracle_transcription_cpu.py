@@ -29,7 +29,10 @@ multiply-add, like the oracle's -ffp-contract=off build):
   Interpolate2D (boundary.f90:336-480): bit for bit;
 * AFASVcycle / LevelRelax (afasroutines.f90:495-557) as the reference's
   sequence of those operations on 2D and 3D AMR hierarchies: the oracle's
-  V-cycle equals it bit for bit.
+  V-cycle equals it bit for bit;
+* MultigridIterations (afasroutines.f90:48-110) as its sequence of FillDown,
+  GetSourceFunction / UpdateSourceFunction, V-cycles and ErrorAFAS: the same
+  V-cycle count, residuals and fields bit for bit.
 """
 import numpy as np
 import pytest
@@ -519,3 +522,66 @@ def test_vcycle_is_the_reference_composition(oracle_mod, nd):
     for p in s.patches:
         for fld in ("q", "qc", "f", "rf"):
             assert np.array_equal(a.get(p["id"], fld), b.get(p["id"], fld)), (p["id"], fld)
+
+
+# --- FillDown and MultigridIterations composition (afasroutines.f90:48-110,
+# :236-327, :330-492) ------------------------------------------------------
+
+def fill_down(o, field, finest, minlevel):
+    """FillDown: FillDownLevel from the finest level down, SetGhost(level-1,
+    0) after each level when the field is the solution"""
+    for level in range(finest, minlevel, -1):
+        o.level_op(level, "fill_q" if field == "q" else "fill_f")
+        if field == "q":
+            o.set_ghost(level - 1, 0)
+
+
+def multigrid_iterations(o, finest, minlevel, nsmooth, maxvcycles, tol):
+    fill_down(o, "q", finest, minlevel)
+    for level in range(finest, -1, -1):  # finestlevel .. rootlevel
+        o.level_op(level, "get_source")
+    for level in range(finest, -1, -1):
+        o.level_op(level, "update_source")
+    fill_down(o, "f", finest, minlevel)
+    res = []
+    for _ in range(maxvcycles):
+        afas_vcycle(o, finest, minlevel, nsmooth)
+        fill_down(o, "q", finest, minlevel)
+        for level in range(finest, -1, -1):
+            o.level_op(level, "update_source")
+        fill_down(o, "f", finest, minlevel)
+        res.append(o.residual_norm(finest, 1))
+        if res[-1] < tol:
+            break
+    return len(res), res
+
+
+def test_multigrid_iterations_are_the_reference_composition(oracle_mod, pkg):
+    """The oracle's MultigridIterations equals the reference's sequence
+    (FillDown, source functions, V-cycles, ErrorAFAS) of pinned operations:
+    the same V-cycle count, residuals and fields bit for bit; CH's
+    Source2D is (qold_phi, -qold_phi) in ftmp, SourceUpdate2D zero."""
+    from tests import hierarchies as H
+    s = H.amr2d(periodic=False)
+    a, b = (oracle_mod.OracleHierarchy(2, 2, "ch", [1e-3, 0.01]) for _ in range(2))
+    s.apply(a)
+    s.apply(b)
+    for p in s.patches:
+        q = pkg.initial.ch_spinodal(tuple(p["mx"][:2]), 0.01, p["dx"][0], seed=40 + p["id"])
+        for h in (a, b):
+            h.put(p["id"], "q", q)
+            h.copy_q_to_qold(s.minlevel(), s.finest())
+    fin, mn = s.finest(), s.minlevel()
+    na, ra = a.multigrid_iterations(fin, mn, 2, 20, 1e-9)
+    nb, rb = multigrid_iterations(b, fin, mn, 2, 20, 1e-9)
+    assert na == nb and list(ra[:na]) == rb, (na, nb, ra, rb)
+    for p in s.patches:
+        for fld in ("q", "qc", "f", "ftmp"):
+            assert np.array_equal(a.get(p["id"], fld), b.get(p["id"], fld)), (p["id"], fld)
+    # the source statements themselves on the finest level
+    for p in s.patches:
+        if p["level"] == fin:
+            qold = b.get(p["id"], "qold").reshape([m + 2 for m in p["mx"][:2]] + [2], order="F")
+            ftmp = b.get(p["id"], "ftmp").reshape(p["mx"][:2] + [2], order="F")
+            assert np.array_equal(ftmp[..., 0], qold[1:-1, 1:-1, 0])
+            assert np.array_equal(ftmp[..., 1], -qold[1:-1, 1:-1, 0])
