@@ -18,6 +18,10 @@ multiply-add, like the oracle's -ffp-contract=off build):
   (PROBLEM/BioGrowth/problem.f90:255-353, :743-766): bit for bit;
 * Interpolate2D, the coarse-fine ghost statements (LIBRARY/boundary.f90:
   143-333) for ipass 0, 1 and 2: bit for bit;
+* Interpolate3D (boundary.f90:1018-1550): corners, the 12 edges (with the
+  z-face test of edges 1-4 that reads /= 99), the four colour classes of
+  each face and the grey face corners, for ipass 0, 1, 2, inside the
+  parent and at a physical face: bit for bit;
 * the V-cycle's coarse branch in 2D and 3D: RestrictSolution with
   Restriction2D/3D, GetCoarseGhostPoints and CoarseLoadingFunction (the
   child's Residual, then Restriction(rf) + Operator(qc) at the parent's
@@ -585,3 +589,168 @@ def test_multigrid_iterations_are_the_reference_composition(oracle_mod, pkg):
             ftmp = b.get(p["id"], "ftmp").reshape(p["mx"][:2] + [2], order="F")
             assert np.array_equal(ftmp[..., 0], qold[1:-1, 1:-1, 0])
             assert np.array_equal(ftmp[..., 1], -qold[1:-1, 1:-1, 0])
+
+
+# --- Interpolate3D (LIBRARY/boundary.f90:1018-1550) ------------------------
+C1, C2, C3, C4 = 9.0 / 16.0, 3.0 / 16.0, 3.0 / 16.0, 1.0 / 16.0
+
+
+def face_index(mx, mb, d, parity):
+    """GetFaceIndex (:1018-1045): ghost, second and first interior cells
+    along d, the coarse cell beyond the patch and the one at its edge"""
+    if parity == 1:
+        return (0, 2, 1, mb[d][0] - 1, mb[d][0])
+    return (mx[d] + 1, mx[d] - 1, mx[d], mb[d][1] + 1, mb[d][1])
+
+
+def interpolate3d(qf, qc, mx, mb, mthbc, ipass):
+    """qf(0:mx+1, ...) and qc(0:, ...) indexed as in Fortran; mb[d] =
+    (lo, hi); every statement assigns cells no other statement reads, so
+    each is applied to the incoming array"""
+    qf = qf.copy()
+    src = qf.copy()
+    s = lambda a, b: slice(a, b + 1, 2)
+    r = lambda a, b: slice(a, b + 1)
+    ok = lambda face: not (mthbc[face] not in (2, 999) and ipass == 1)
+
+    def at(pos):  # {dim: index or slice} -> index tuple
+        return tuple(pos[d] for d in range(3))
+
+    # (1) the 8 corners
+    for p1 in (1, 2):
+        if not ok(p1 - 1):
+            continue
+        f1 = face_index(mx, mb, 0, p1)
+        for p2 in (1, 2):
+            if not ok(p2 + 1):
+                continue
+            f2 = face_index(mx, mb, 1, p2)
+            for p3 in (1, 2):
+                if not ok(p3 + 3):
+                    continue
+                f3 = face_index(mx, mb, 2, p3)
+                qf[f1[0], f2[0], f3[0]] = (A1 * src[f1[1], f2[1], f3[1]] + A2 * src[f1[2], f2[2], f3[2]]
+                                           + A3 * qc[f1[3], f2[3], f3[3]])
+
+    # (2) the 12 edges: fixed dims (da, db), running along w
+    def edge(da, fa, db, fb, w):
+        m, (lo, hi) = mx[w], mb[w]
+
+        def P(k, wv):
+            pos = {da: fa[k], db: fb[k], w: wv}
+            return at(pos)
+
+        def Q(wv):
+            return qc[at({da: fa[3], db: fb[3], w: wv})]
+        qf[P(0, s(3, m - 1))] = A1 * src[P(1, s(1, m - 3))] + A2 * src[P(2, s(2, m - 2))] + A3 * Q(r(lo + 1, hi))
+        qf[P(0, 1)] = A1 * src[P(1, 1)] + A2 * src[P(2, 1)] + A3 * (B1 * Q(lo - 1) + B2 * Q(lo) + B3 * Q(lo + 1))
+        qf[P(0, s(2, m - 2))] = A1 * src[P(1, s(4, m))] + A2 * src[P(2, s(3, m - 1))] + A3 * Q(r(lo, hi - 1))
+        qf[P(0, m)] = A1 * src[P(1, m)] + A2 * src[P(2, m)] + A3 * (B1 * Q(hi + 1) + B2 * Q(hi) + B3 * Q(hi - 1))
+
+    for p1 in (1, 2):  # edges 1-4 (coordinates 1 and 3 fixed); the z test reads /= 99 (:1106)
+        if not ok(p1 - 1):
+            continue
+        for p3 in (1, 2):
+            if mthbc[p3 + 3] != 2 and mthbc[p3 + 3] != 99 and ipass == 1:
+                continue
+            edge(0, face_index(mx, mb, 0, p1), 2, face_index(mx, mb, 2, p3), 1)
+    for p1 in (1, 2):  # edges 5-8 (coordinates 1 and 2 fixed)
+        if not ok(p1 - 1):
+            continue
+        for p2 in (1, 2):
+            if not ok(p2 + 1):
+                continue
+            edge(0, face_index(mx, mb, 0, p1), 1, face_index(mx, mb, 1, p2), 2)
+    for p2 in (1, 2):  # edges 9-12 (coordinates 2 and 3 fixed)
+        if not ok(p2 + 1):
+            continue
+        for p3 in (1, 2):
+            if not ok(p3 + 3):
+                continue
+            edge(1, face_index(mx, mb, 1, p2), 2, face_index(mx, mb, 2, p3), 0)
+
+    # (3) the 6 faces, periodic or internal only: normal n, in-face (u, v)
+    for n, (ud, vd) in ((0, (1, 2)), (1, (0, 2)), (2, (0, 1))):
+        for p in (1, 2):
+            if mthbc[2 * n + p - 1] not in (2, 999):
+                continue
+            fn = face_index(mx, mb, n, p)
+            mu, mv = mx[ud], mx[vd]
+            (ul, uh), (vl, vh) = mb[ud], mb[vd]
+
+            def F(k, u, v):
+                return at({n: fn[k], ud: u, vd: v})
+
+            def Q(u, v):
+                return qc[at({n: fn[3], ud: u, vd: v})]
+
+            def put(u, v, du2, dv2, du1, dv1, coarse):
+                qf[F(0, u, v)] = A1 * src[F(1, du2, dv2)] + A2 * src[F(2, du1, dv1)] + A3 * coarse
+
+            if ipass == 0 or (p + ipass) % 2 == 0:
+                # yellow
+                put(s(2, mu - 2), s(2, mv - 2), s(4, mu), s(4, mv), s(3, mu - 1), s(3, mv - 1), Q(r(ul, uh - 1), r(vl, vh - 1)))
+                put(mu, s(2, mv - 2), mu, s(4, mv), mu, s(3, mv - 1),
+                    B1 * Q(uh + 1, r(vl, vh - 1)) + B2 * Q(uh, r(vl, vh - 1)) + B3 * Q(uh - 1, r(vl, vh - 1)))
+                put(s(2, mu - 2), mv, s(4, mu), mv, s(3, mu - 1), mv,
+                    B1 * Q(r(ul, uh - 1), vh + 1) + B2 * Q(r(ul, uh - 1), vh) + B3 * Q(r(ul, uh - 1), vh - 1))
+                # blue
+                put(s(3, mu - 1), s(3, mv - 1), s(1, mu - 3), s(1, mv - 3), s(2, mu - 2), s(2, mv - 2), Q(r(ul + 1, uh), r(vl + 1, vh)))
+                put(s(3, mu - 1), 1, s(1, mu - 3), 1, s(2, mu - 2), 1,
+                    B1 * Q(r(ul + 1, uh), vl - 1) + B2 * Q(r(ul + 1, uh), vl) + B3 * Q(r(ul + 1, uh), vl + 1))
+                put(1, s(3, mv - 1), 1, s(1, mv - 3), 1, s(2, mv - 2),
+                    B1 * Q(ul - 1, r(vl + 1, vh)) + B2 * Q(ul, r(vl + 1, vh)) + B3 * Q(ul + 1, r(vl + 1, vh)))
+            if ipass == 0 or (p + ipass) % 2 == 1:
+                # green
+                put(s(3, mu - 1), s(2, mv - 2), s(1, mu - 3), s(4, mv), s(2, mu - 2), s(3, mv - 1), Q(r(ul + 1, uh), r(vl, vh - 1)))
+                put(1, s(2, mv - 2), 1, s(4, mv), 1, s(3, mv - 1),
+                    B1 * Q(ul - 1, r(vl, vh - 1)) + B2 * Q(ul, r(vl, vh - 1)) + B3 * Q(ul + 1, r(vl, vh - 1)))
+                put(s(3, mu - 1), mv, s(1, mu - 3), mv, s(2, mu - 2), mv,
+                    B1 * Q(r(ul + 1, uh), vh + 1) + B2 * Q(r(ul + 1, uh), vh) + B3 * Q(r(ul + 1, uh), vh - 1))
+                # red
+                put(s(2, mu - 2), s(3, mv - 1), s(4, mu), s(1, mv - 3), s(3, mu - 1), s(2, mv - 2), Q(r(ul, uh - 1), r(vl + 1, vh)))
+                put(s(2, mu - 2), 1, s(4, mu), 1, s(3, mu - 1), 1,
+                    B1 * Q(r(ul, uh - 1), vl - 1) + B2 * Q(r(ul, uh - 1), vl) + B3 * Q(r(ul, uh - 1), vl + 1))
+                put(mu, s(3, mv - 1), mu, s(1, mv - 3), mu, s(2, mv - 2),
+                    B1 * Q(uh + 1, r(vl + 1, vh)) + B2 * Q(uh, r(vl + 1, vh)) + B3 * Q(uh - 1, r(vl + 1, vh)))
+            # grey corner cells of the face, every ipass
+            for pu in (1, 2):
+                fu = face_index(mx, mb, ud, pu)
+                for pv in (1, 2):
+                    fv = face_index(mx, mb, vd, pv)
+                    put(fu[2], fv[2], fu[2], fv[2], fu[2], fv[2],
+                        C1 * Q(fu[4], fv[4]) + C2 * Q(fu[3], fv[4]) + C3 * Q(fu[4], fv[3]) + C4 * Q(fu[3], fv[3]))
+    return qf
+
+
+@pytest.mark.parametrize("ipass", [0, 1, 2])
+@pytest.mark.parametrize("where", ["inside", "at-low-x"])
+def test_cf_interpolation_3d_is_the_reference_statements(oracle_mod, ipass, where):
+    """SetGhost on one 3D child: Interpolate3D (corners, the 12 edges with
+    the z-face test of edges 1-4 reading /= 99, the yellow/blue/green/red
+    face classes and the grey face corners), then the physical boundary of
+    a face the child shares with the root (UserBC3D, 2 - q)."""
+    from tests import hierarchies as H
+    s = H.Spec(3)
+    s.root_and_below(8, 0, [10] * 6)
+    if where == "inside":
+        s.child(0, 101, [2, 3, 2], [5, 6, 7])
+    else:
+        s.child(0, 101, [1, 3, 2], [4, 6, 7])
+    o = oracle_mod.OracleHierarchy(3, 2, "ch", [CH["dt"], CH["eps"]])
+    s.apply(o)
+    rng = np.random.default_rng(70 + ipass + (where == "inside"))
+    q = {}
+    for p in s.patches:
+        a = rng.uniform(-1, 1, size=o.field_size(p["id"], "q"))
+        o.put(p["id"], "q", a)
+        q[p["id"]] = a.reshape([m + 2 for m in p["mx"][:3]] + [2], order="F")
+    child = s.patches[-1]
+    o.set_ghost(1, ipass)
+    mx = child["mx"][:3]
+    mb = [(child["mbounds"][2 * d], child["mbounds"][2 * d + 1]) for d in range(3)]
+    want = interpolate3d(q[101], q[0], mx, mb, child["mthbc"], ipass)
+    want = root_ghosts(want, 3, mx, 1, child["mthbc"], [0.0, 0.0])
+    got = o.get(101, "q").reshape(want.shape, order="F")
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, (len(bad), bad[:6])
