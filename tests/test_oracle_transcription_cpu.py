@@ -36,7 +36,10 @@ multiply-add, like the oracle's -ffp-contract=off build):
   V-cycle equals it bit for bit;
 * MultigridIterations (afasroutines.f90:48-110) as its sequence of FillDown,
   GetSourceFunction / UpdateSourceFunction, V-cycles and ErrorAFAS: the same
-  V-cycle count, residuals and fields bit for bit.
+  V-cycle count, residuals and fields bit for bit;
+* AfterStepStatistics with CH AfterStep2D, Energy2D and Ff
+  (bsamroutines.f90:763-775, :918-963; CH/problem.f90:149-183, :512-547,
+  :901-915) on a 2D AMR hierarchy: both integrals bit for bit.
 """
 import numpy as np
 import pytest
@@ -754,3 +757,60 @@ def test_cf_interpolation_3d_is_the_reference_statements(oracle_mod, ipass, wher
     got = o.get(101, "q").reshape(want.shape, order="F")
     bad = np.argwhere(got != want)
     assert bad.size == 0, (len(bad), bad[:6])
+
+
+# --- AfterStepStatistics with CH AfterStep2D / Energy2D / Ff ---------------
+# (bsamroutines.f90:763-775, :918-963; CH/problem.f90:149-183, :512-547,
+# :901-915)
+
+def seq_sum(a):
+    """Fortran SUM in element order"""
+    return np.cumsum(np.ravel(a, order="F"))[-1]
+
+
+def energy2d(c, h, eps):
+    mx, my = c.shape[0] - 2, c.shape[1] - 2
+    h2 = h * h
+    f1 = c[1:mx + 2, 1:my + 1] - c[0:mx + 1, 1:my + 1]   # f1(0:mx, 1:my)
+    f1 = f1 * f1
+    f2 = c[1:mx + 1, 1:my + 2] - c[1:mx + 1, 0:my + 1]   # f2(1:mx, 0:my)
+    f2 = f2 * f2
+    tmp = eps * eps / h2 / 4.0
+    ci = c[1:mx + 1, 1:my + 1]
+    c2 = ci * ci
+    ff = c2 * (c2 - 2.0) / 4.0
+    return h2 * (seq_sum(ff) + tmp * seq_sum(f1[1:mx + 1, :] + f1[0:mx, :] + f2[:, 1:my + 1] + f2[:, 0:my]))
+
+
+def test_after_step_statistics_are_the_reference_statements(oracle_mod, pkg):
+    from tests import hierarchies as H
+    s = H.amr2d(periodic=True)
+    eps = 0.01
+    o = oracle_mod.OracleHierarchy(2, 2, "ch", [1e-3, eps])
+    s.apply(o)
+    q = {}
+    for p in s.patches:
+        v = pkg.initial.ch_spinodal(tuple(p["mx"][:2]), eps, p["dx"][0], seed=11 + p["id"])
+        o.put(p["id"], "q", v)
+        q[p["id"]] = o.get(p["id"], "q").reshape([m + 2 for m in p["mx"][:2]] + [2], order="F")[..., 0]
+    byid = {p["id"]: p for p in s.patches}
+    fin = s.finest()
+    i1 = i2 = 0.0
+    for level in range(fin, -1, -1):
+        for p in [x for x in s.patches if x["level"] == level]:
+            h = p["dx"][0]
+            h2, ch = h * h, h * 2.0
+            ch2 = ch * ch
+            c = q[p["id"]]
+            if level == 0:
+                i1 = i1 + h2 * seq_sum(c[1:-1, 1:-1])
+                i2 = i2 + energy2d(c, h, eps)
+            else:
+                par = byid[p["parent_id"]]
+                lo = [p["mbounds"][0], p["mbounds"][2]]
+                hi = [p["mbounds"][1], p["mbounds"][3]]
+                pc = q[par["id"]][lo[0] - 1:hi[0] + 2, lo[1] - 1:hi[1] + 2]  # parent%q(mb-1:mb+1)
+                i1 = i1 + h2 * seq_sum(c[1:-1, 1:-1]) - ch2 * seq_sum(pc[1:-1, 1:-1])
+                i2 = i2 + energy2d(c, h, eps) - energy2d(pc, ch, eps)
+    got = o.after_step_stats(fin)
+    assert (got[0], got[1]) == (i1, i2), (got, i1, i2)
