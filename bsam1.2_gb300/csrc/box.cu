@@ -496,7 +496,8 @@ __device__ __forceinline__ void coarse_load_at(float* __restrict__ fp, const Box
 // over the fine cells: coarse e = ec = R(e), coarse pb = R(pb) and coarse
 // g = R(g - M(e)); the coarse operator M_c(ec) needs the neighbours' ec, so
 // k_bx_coarse_op adds it in a second (coarse-sized) pass.  Every fine value
-// is loaded before the first store.
+// is loaded before the first store; six blocks per SM (40 registers, no
+// spills) against five uncapped: 30 vs 37 us averaged over the levels.
 template <int DIM>
 __device__ __forceinline__ void restrict_load_at(float* __restrict__ fp, const BoxLev& F, const BoxLev& C, int X,
                                                  int Y, int Z) {
@@ -527,7 +528,7 @@ __device__ __forceinline__ void restrict_load_at(float* __restrict__ fp, const B
   Gc.v1[lc.own] = R1 * w;
 }
 template <int DIM>
-__global__ void __launch_bounds__(256) k_bx_restrict_load(float* __restrict__ fp, BoxLev F, BoxLev C) {
+__global__ void __launch_bounds__(256, 6) k_bx_restrict_load(float* __restrict__ fp, BoxLev F, BoxLev C) {
   int X = blockIdx.x * blockDim.x + threadIdx.x;
   int Y = blockIdx.y * blockDim.y + threadIdx.y;
   if (X < C.n[0] && Y < C.n[1]) restrict_load_at<DIM>(fp, F, C, X, Y, blockIdx.z);
