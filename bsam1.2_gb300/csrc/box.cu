@@ -676,9 +676,11 @@ __global__ void __launch_bounds__(kSmallThreads) k_bx_small_vcycle(float* __rest
 // After a cycle on the finest level: tracked residual g <- g - M(e) (M at
 // this cycle's base field), its per-CTA sums of squares, then qbar += e as
 // double-float.  One row (2D) or two rows (3D) per thread; every load
-// precedes every store.
+// precedes every store.  Two rows fit 48 registers without spills, five
+// blocks per SM (61 registers at four blocks took 185 us at 256^3, 174 us
+// capped).
 template <int DIM, int R = 1>
-__global__ void __launch_bounds__(256, R == 1 ? 6 : 4) k_bx_track_update(float* __restrict__ fp, BoxLev L,
+__global__ void __launch_bounds__(256, R == 1 ? 6 : 5) k_bx_track_update(float* __restrict__ fp, BoxLev L,
                                                                        long long oqlo, double* __restrict__ partial) {
   // R rows per thread (y = R yp .. R yp + R - 1): every load of the R cells
   // is issued before the first store, R times the loads in flight
