@@ -30,7 +30,9 @@ multiply-add, like the oracle's -ffp-contract=off build):
   CH UserBC2D / UserBC3D (boundary.f90:478-575, :640-800; CH:770-881) on a
   root patch, one and two ghost layers: bit for bit;
 * TransferBC / GhostOverlap between touching siblings after their
-  Interpolate2D (boundary.f90:336-480): bit for bit;
+  Interpolate2D (boundary.f90:336-480), and TransferPeriodicBC's
+  GhostOverlap through every periodic offset (:582-605, :824-954): bit for
+  bit;
 * AFASVcycle / LevelRelax (afasroutines.f90:495-557) as the reference's
   sequence of those operations on 2D and 3D AMR hierarchies: the oracle's
   V-cycle equals it bit for bit;
@@ -814,3 +816,39 @@ def test_after_step_statistics_are_the_reference_statements(oracle_mod, pkg):
                 i2 = i2 + energy2d(c, h, eps) - energy2d(pc, ch, eps)
     got = o.after_step_stats(fin)
     assert (got[0], got[1]) == (i1, i2), (got, i1, i2)
+
+
+def test_periodic_transfer_between_patches_is_the_reference_statements(oracle_mod):
+    """Two children at opposite faces of a periodic root: Interpolate2D on
+    both (their periodic faces included, CASE(2, 999)), then
+    TransferPeriodicBC's GhostOverlap of the pair through every periodic
+    offset of GetPeriodicOffsets (boundary.f90:582-605, :824-954) with
+    both polarities; no quasi-periodic offset in these transfers."""
+    from tests import hierarchies as H
+    s = H.Spec(2)
+    s.root_and_below(16, 0, [2, 2, 2, 2, 10, 10])
+    s.child(0, 101, [1, 5], [4, 12])
+    s.child(0, 102, [13, 9], [16, 16])
+    o = oracle_mod.OracleHierarchy(2, 2, "ch", [CH["dt"], CH["eps"]])
+    s.apply(o)
+    rng = np.random.default_rng(123)
+    q = {}
+    for p in s.patches:
+        a = rng.uniform(-1, 1, size=o.field_size(p["id"], "q"))
+        o.put(p["id"], "q", a)
+        q[p["id"]] = a.reshape([m + 2 for m in p["mx"][:2]] + [2], order="F")
+    o.set_ghost(1, 0)
+    want = {}
+    for p in s.patches[1:]:
+        mb = [(p["mbounds"][0], p["mbounds"][1]), (p["mbounds"][2], p["mbounds"][3])]
+        want[p["id"]] = interpolate2d(q[p["id"]], q[0], p["mx"][:2], mb, p["mthbc"][:4], 0)
+    mxmax = [32, 32]  # level 1 of a 16^2 root
+    offsets = [(mxmax[0], 0), (0, mxmax[1]), (mxmax[0], mxmax[1]), (-mxmax[0], mxmax[1])]  # indices 1, 2, 4, 5
+    a, b = s.patches[1], s.patches[2]
+    mg = lambda p, o=(0, 0): [(p["mglobal"][0] + o[0], p["mglobal"][1] + o[0]),
+                              (p["mglobal"][2] + o[1], p["mglobal"][3] + o[1])]
+    for pol in (-1, 1):
+        for off in offsets:
+            ghost_overlap(want[101], want[102], mg(a), mg(b, (pol * off[0], pol * off[1])), 1, 2)
+    for pid in (101, 102):
+        assert np.array_equal(o.get(pid, "q").reshape(want[pid].shape, order="F"), want[pid]), pid
