@@ -1848,6 +1848,36 @@ static int new_sub_grids(const bsamo_hier* h, const OPatch* p, const int* fl, co
 /* Patches longer than maxside child cells (maxside/2 parent cells) are cut
  * into nearly equal even pieces along that dimension (not a reference
  * feature: it bounds the patch size for the batched kernels). */
+/* NewSubGrids alone on a flag field of one patch (level 0, mbounds the
+ * whole patch): the boxes (lo, hi per dimension) in the order it makes
+ * them, at most cap; returns their number or a negative status */
+int bsamo_new_sub_grids(int nd, const int mx[3], const int* flags, double desfill, int mgp, int* out, int cap) {
+  if ((nd != 2 && nd != 3) || !mx || !flags || !out || cap < 0) return -1;
+  bsamo_hier hh;
+  memset(&hh, 0, sizeof(hh));
+  hh.ndims = nd;
+  OPatch p;
+  memset(&p, 0, sizeof(p));
+  for (int d = 0; d < 3; d++) {
+    p.mx[d] = d < nd ? mx[d] : 1;
+    p.mglobal[d][0] = 1;
+    p.mglobal[d][1] = p.mx[d];
+  }
+  bsamo_regrid_params prm;
+  memset(&prm, 0, sizeof(prm));
+  prm.desiredfillratio[0] = desfill;
+  prm.minimumgridpoints[0] = mgp;
+  int (*sub)[3][2] = malloc(sizeof(*sub) * MAXSUBGRIDS);
+  int ng = new_sub_grids(&hh, &p, flags, &prm, sub);
+  for (int g = 0; g < ng && g < cap; g++)
+    for (int d = 0; d < 3; d++) {
+      out[6 * g + 2 * d] = sub[g][d][0];
+      out[6 * g + 2 * d + 1] = sub[g][d][1];
+    }
+  free(sub);
+  return ng;
+}
+
 static int split_long(int nd, int maxside, int (*sub)[3][2], int ng, int cap) {
   if (maxside <= 0) return ng;
   int P = maxside / 2;

@@ -84,6 +84,9 @@ int bsamo_correct_fine(bsamo_hier* h, int level);
  * GetSourceFunction (4), UpdateSourceFunction (5), FillDownLevel of f (6)
  * or of q (7) */
 int bsamo_level_op(bsamo_hier* h, int level, int which);
+/* NewSubGrids alone on one patch's flags (x fastest): boxes as (lo, hi) per
+ * dimension, at most cap of them into out; returns their number */
+int bsamo_new_sub_grids(int nd, const int mx[3], const int* flags, double desfill, int mgp, int* out, int cap);
 /* P1MC (mbc = 1) / P2MC (mbc = 2) of one variable: a has cmx+2 mbc cells per
  * used dimension, out 2 cmx + 2 mbc (Fortran order, ghost layers included) */
 int bsamo_prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double* out);

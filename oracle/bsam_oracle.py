@@ -93,6 +93,7 @@ def lib():
         L.bsamo_vcycle.argtypes = [P, I, I, I]
         L.bsamo_correct_fine.argtypes = [P, I]
         L.bsamo_level_op.argtypes = [P, I, I]
+        L.bsamo_new_sub_grids.argtypes = [I, IP, IP, D, I, IP, I]
         L.bsamo_prolong_mc.argtypes = [I, I, DP, IP, DP]
         L.bsamo_residual_norm.argtypes = [P, I, I, DP]
         L.bsamo_multigrid_iterations.argtypes = [P, I, I, I, I, D, I, I, IP, DP]
@@ -284,6 +285,20 @@ def regrid(old, params, qinit=None):
     h = ctypes.c_void_p()
     _check(lib().bsamo_regrid(old.h, ctypes.byref(params), cb, None, ctypes.byref(h)), "regrid")
     return _wrap(h, old.ndims, old.nrvars, old.mbc)
+
+
+def new_sub_grids(flags, desfill, mgp):
+    """NewSubGrids on one patch's flags (a 2D or 3D int array): the boxes
+    [(lo, hi) per dimension] in the order the oracle makes them"""
+    f = np.asfortranarray(np.asarray(flags, dtype=np.int32))
+    nd = f.ndim
+    mx = list(f.shape) + [1] * (3 - nd)
+    cap = 4096
+    out = (ctypes.c_int * (6 * cap))()
+    n = lib().bsamo_new_sub_grids(nd, (ctypes.c_int * 3)(*mx), f.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                  desfill, mgp, out, cap)
+    _check(0 if n >= 0 else n, "new_sub_grids")
+    return [[(out[6 * g + 2 * d], out[6 * g + 2 * d + 1]) for d in range(nd)] for g in range(n)]
 
 
 def prolong_mc(a, mbc):

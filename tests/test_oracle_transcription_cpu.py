@@ -41,7 +41,10 @@ multiply-add, like the oracle's -ffp-contract=off build):
   V-cycle count, residuals and fields bit for bit;
 * AfterStepStatistics with CH AfterStep2D, Energy2D and Ff
   (bsamroutines.f90:763-775, :918-963; CH/problem.f90:149-183, :512-547,
-  :901-915) on a 2D AMR hierarchy: both integrals bit for bit.
+  :901-915) on a 2D AMR hierarchy: both integrals bit for bit;
+* the regrid's clustering, NewSubGrids with GetSignatures and
+  GridFlagRatio (bsamroutines.f90:1408-1662), on 160 random 2D and 3D flag
+  fields, fill ratios and minimum sizes: the same boxes in the same order.
 """
 import numpy as np
 import pytest
@@ -852,3 +855,130 @@ def test_periodic_transfer_between_patches_is_the_reference_statements(oracle_mo
             ghost_overlap(want[101], want[102], mg(a), mg(b, (pol * off[0], pol * off[1])), 1, 2)
     for pid in (101, 102):
         assert np.array_equal(o.get(pid, "q").reshape(want[pid].shape, order="F"), want[pid]), pid
+
+
+# --- NewSubGrids, GetSignatures, GridFlagRatio (bsamroutines.f90:1408-1662)
+
+def new_sub_grids_ref(flags, desfill, mgp, maxsubgrids=1024, maxsplitpasses=15):
+    """The Berger-Rigoutsos variant of NewSubGrids, statement by statement;
+    flags[i-1, j-1(, k-1)] is errorflags(i, j(, k)); boxes 1-based"""
+    nd = flags.ndim
+    mx = flags.shape
+
+    def box_sum(b):
+        return int(flags[tuple(slice(b[d][0] - 1, b[d][1]) for d in range(nd))].sum())
+
+    def ratio(b):
+        total = 1.0
+        for d in range(nd):
+            total = total * float(b[d][1] - b[d][0] + 1)
+        return float(box_sum(b)) / total
+
+    maxm = max(mx)
+    sig = np.zeros((maxm + 2, nd), dtype=np.int64)
+    dds = np.zeros((maxm + 2, nd), dtype=np.int64)
+
+    def signatures(b):
+        for n in range(nd):
+            for i in range(b[n][0], b[n][1] + 1):
+                bb = [list(x) for x in b]
+                bb[n] = [i, i]
+                sig[i, n] = box_sum(bb)
+
+    whole = [[1, mx[d]] for d in range(nd)]
+    if ratio(whole) < 1.0e-10:
+        return []
+    ngrid = 1
+    cansplit = [True] * (maxsubgrids + 2)
+    msub = [None, [list(x) for x in whole]]
+    igrid = 1
+    while ngrid < maxsubgrids and igrid <= ngrid:
+        npass = 0
+        while cansplit[igrid] and npass < maxsplitpasses:
+            npass += 1
+            signatures(msub[igrid])
+            for n in range(nd):  # trim unflagged edges, then whole coarse cells
+                i1, i2 = msub[igrid][n]
+                while sig[i1, n] == 0 and i1 < msub[igrid][n][1] and i2 - i1 + 1 > mgp:
+                    i1 += 1
+                while sig[i2, n] == 0 and i2 > msub[igrid][n][0] and i2 - i1 + 1 > mgp:
+                    i2 -= 1
+                msub[igrid][n] = [i1 - (i1 + 1) % 2, i2 + i2 % 2]
+            if ratio(msub[igrid]) < desfill:
+                signatures(msub[igrid])
+                isplit, havesplit = [0, 0, 0], False
+                for n in range(nd):  # a hole
+                    i1, i2 = msub[igrid][n]
+                    for i in range(i1 + mgp - 1, i2 - mgp + 1, 2):
+                        if sig[i, n] == 0 and min(i - i1 + 1, i2 - i) >= mgp:
+                            isplit[n], havesplit = i, True
+                            break
+                    if havesplit:
+                        break
+                if not havesplit:  # the strongest inflection
+                    for n in range(nd):
+                        i1, i2 = msub[igrid][n]
+                        for i in range(i1 + 1, i2):
+                            dds[i, n] = sig[i - 1, n] - 2 * sig[i, n] + sig[i + 1, n]
+                    inflect = dist0 = 0
+                    for n in range(nd):
+                        i1, i2 = msub[igrid][n]
+                        for i in range(i1 + mgp, i2 - mgp + 2, 2):
+                            dl = abs(int(dds[i, n]) - int(dds[i - 1, n]))
+                            if dl > inflect:
+                                inflect, isplit, havesplit = dl, [0, 0, 0], True
+                                isplit[n] = i - 1
+                                dist0 = min(i - i1, i2 - i + 1)
+                            elif dl == inflect and inflect > 0:
+                                dist1 = min(i - i1, i2 - i + 1)
+                                if dist1 > dist0:
+                                    isplit, havesplit = [0, 0, 0], True
+                                    isplit[n] = i - 1
+                                    dist0 = dist1
+                if havesplit:
+                    for n in range(nd):
+                        lo, hi = msub[igrid][n]
+                        if isplit[n] > 0 and min(hi - isplit[n], isplit[n] - lo + 1) >= mgp:
+                            ngrid += 1
+                            cansplit[ngrid] = True
+                            new = [list(x) for x in msub[igrid]]
+                            new[n] = [isplit[n] + 1, hi]
+                            msub.append(new)
+                            msub[igrid][n] = [lo, isplit[n]]
+                            break
+                else:
+                    cansplit[igrid] = False
+            else:
+                cansplit[igrid] = False
+        igrid += 1
+    return [[tuple(x) for x in msub[g]] for g in range(1, ngrid + 1)]
+
+
+def random_flags(rng, shape):
+    f = np.zeros(shape, dtype=np.int32)
+    for _ in range(rng.integers(1, 5)):  # a few blobs and scattered points
+        c = [rng.integers(0, n) for n in shape]
+        r = [rng.integers(1, max(2, n // 3)) for n in shape]
+        idx = np.indices(shape)
+        inside = np.ones(shape, dtype=bool)
+        for d in range(len(shape)):
+            inside &= np.abs(idx[d] - c[d]) <= r[d]
+        f[inside] = 1
+    f[rng.random(shape) < rng.choice([0.0, 0.01, 0.05])] = 1
+    return f
+
+
+@pytest.mark.parametrize("nd", [2, 3])
+def test_new_sub_grids_is_the_reference_algorithm(oracle_mod, nd):
+    rng = np.random.default_rng(2000 + nd)
+    cases = 120 if nd == 2 else 40
+    for c in range(cases):
+        shape = tuple(int(2 * rng.integers(4, 25 if nd == 2 else 9)) for _ in range(nd))
+        flags = random_flags(rng, shape)
+        desfill = float(rng.choice([0.5, 0.7, 0.8, 0.9]))
+        mgp = int(rng.choice([4, 6, 8]))
+        if min(shape) < mgp:
+            continue
+        want = new_sub_grids_ref(flags, desfill, mgp)
+        got = oracle_mod.new_sub_grids(flags, desfill, mgp)
+        assert got == want, (c, shape, desfill, mgp, got, want)
