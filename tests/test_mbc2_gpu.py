@@ -243,3 +243,29 @@ def test_root_ghosts_with_offsets_match_oracle(pkg, ctx, oracle_mod, nd, mthbc, 
         h.put(0, "q", a)
         h.set_ghost(0, 0)
     assert np.array_equal(hs[0].get(0, "q"), hs[1].get(0, "q"))
+
+
+def test_regrid_3d_with_two_ghost_layers(pkg, ctx, oracle_mod):
+    """3D regrid (InitFields with TriLinProlongationP2MC, qc of the new
+    patches from their parents) and a time step, as the oracle's."""
+    from tests.test_regrid_gpu import sphere3d
+    om = oracle_mod
+    params = [5e-4, 0.05]
+    g = pkg.Hierarchy(ctx, 3, 2, "ch", params, mbc=2)
+    o = om.OracleHierarchy(3, 2, "ch", params, mbc=2)
+    q0 = embed(sphere3d()(0, [16] * 3, [1 / 16] * 3, [0.0] * 3), [16] * 3, 2, 2)
+    for h in (g, o):
+        h.build_uniform([16, 16, 16], -3, [2] * 6, [0, 0, 0], [1, 1, 1])
+        h.commit()
+        h.put(0, "q", q0)
+    for step in range(2):
+        kw = dict(tagging="ch", initial=step == 0, qtolerance=0.05, first_id=500 * (step + 1))
+        g = g.regrid(pkg.regrid_params(2, **kw), sphere3d() if step == 0 else None)
+        o = om.regrid(o, om.regrid_params(2, **kw), sphere3d() if step == 0 else None)
+        tab = _same(g, o)
+        fin = max(p["level"] for p in tab)
+        assert fin >= 1
+        ng, rg = g.time_step(step == 0, fin, -3, tol=1e-8, maxvcycles=30)
+        no, ro = o.time_step(step == 0, fin, -3, tol=1e-8, maxvcycles=30)
+        assert ng == no, (step, rg, ro)
+        np.testing.assert_allclose(rg, ro, rtol=1e-10, atol=0)
