@@ -229,18 +229,29 @@ def run_arm(h, q0, w, mode, steps, warmup, dist, clocks=None):
 def run_e2e(pkg, h, q0, w, mode, steps, warmup, dist):
     """Public-API end to end: per step, H2D of q from pinned host memory,
     the time step, D2H of q into pinned host memory (two pinned buffers
-    alternate as input and output, as a host that keeps its state would)."""
+    alternate as input and output, as a host that keeps its state would).
+    Returns the total time, the bytes of q and the device time of the
+    uploads and of the downloads over the timed steps (events around each
+    copy on the hierarchy's stream)."""
     bufs = [pkg.pin(np.array(q0, copy=True)), pkg.pin(np.empty_like(q0))]
     reset(h, q0, w)
     first = True
     cur = 0
+    up_ms = down_ms = 0.0
     for s in range(warmup + steps):
         if s == warmup:
             dist.barrier()
             h.mark(10)
+        h.mark(12)
         h.put_flat(0, "q", bufs[cur])
+        h.mark(13)
         h.time_step(first, 0, w["minlevel"], NSMOOTH, MAXV, w["tol"], mode=mode, strict=True)
+        h.mark(14)
         h.get(0, "q", out=bufs[1 - cur])
+        h.mark(15)
+        if s >= warmup:
+            up_ms += h.elapsed_ms(12, 13)
+            down_ms += h.elapsed_ms(14, 15)
         cur = 1 - cur
         first = False
     h.mark(11)
@@ -248,7 +259,7 @@ def run_e2e(pkg, h, q0, w, mode, steps, warmup, dist):
     dist.barrier()
     for b in bufs:
         pkg.unpin(b)
-    return ms, bufs[0].nbytes
+    return ms, bufs[0].nbytes, up_ms, down_ms
 
 
 def pct(x, p):
@@ -621,8 +632,10 @@ def main():
     fp64 = run_arm(h, q0, w, "fp64", args.steps, args.warmup, dist)
     q_fp64 = h.get(0, "q")
     ms_fp64 = h.time_smoother(0, "fp64", reps=10)
-    e2e_ms, qbytes = (None, 0) if args.no_e2e else run_e2e(pkg, h, q0, w, "mixed", args.steps,
-                                                           min(args.warmup, 1), dist)
+    # the same time steps as the resident run (same warm-up), so both legs
+    # see the same V-cycle counts
+    e2e_ms, qbytes, up_ms, down_ms = (None, 0, 0, 0) if args.no_e2e else run_e2e(
+        pkg, h, q0, w, "mixed", args.steps, args.warmup, dist)
 
     t_mixed = dist.max(mixed["total_ms"])
     t_fp64 = dist.max(fp64["total_ms"])
@@ -677,7 +690,11 @@ def main():
     line["dof_sweeps_per_s"] = 2 * N * (2 * NSMOOTH) * vps_m * value
     if e2e_ms is not None:
         line["e2e"] = {"value": dist.ws * args.steps / (e2e_ms * 1e-3), "unit": "steps/s",
-                       "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes}
+                       "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes,
+                       # the host link's share: device time of the copies alone
+                       "h2d_ms_per_step": up_ms / args.steps, "d2h_ms_per_step": down_ms / args.steps,
+                       "h2d_gbs": qbytes * args.steps / (up_ms * 1e6),
+                       "d2h_gbs": qbytes * args.steps / (down_ms * 1e6)}
     if not args.no_cpu_baseline:
         per_v, cb = cpu_baseline(pkg, w, vps_f)
         line["cpu_baseline"] = cb

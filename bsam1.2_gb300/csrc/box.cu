@@ -642,8 +642,7 @@ __device__ __forceinline__ void small_relax(float* fp, const BoxLev& L, int nsmo
 }
 
 template <int DIM>
-__global__ void __launch_bounds__(kSmallThreads) k_bx_small_vcycle(float* __restrict__ fp, SmallLevels S, int nsmooth,
-                                                                   int fresh) {
+__device__ __forceinline__ void small_cycle(float* fp, const SmallLevels& S, int nsmooth, int fresh) {
   for (int i = 0; i < S.n; i++) {
     const BoxLev& F = S.L[i];
     small_relax<DIM>(fp, F, nsmooth, fresh && i == 0);
@@ -671,6 +670,56 @@ __global__ void __launch_bounds__(kSmallThreads) k_bx_small_vcycle(float* __rest
     __syncthreads();
     small_relax<DIM>(fp, F, nsmooth, false);
   }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kSmallThreads) k_bx_small_vcycle(float* __restrict__ fp, SmallLevels S, int nsmooth,
+                                                                   int fresh) {
+  small_cycle<DIM>(fp, S, nsmooth, fresh);
+}
+
+// The same cycle on a copy in shared memory: the small levels' arrays are
+// one contiguous range of the pool, fp[lo, lo + nf) (levels are laid out
+// finest first, every array start a multiple of 64 floats), so the CTA
+// copies the range in, cycles on it with S's offsets taken relative to lo,
+// and copies it back.  Every phase then waits on shared memory instead of
+// L2.
+constexpr int kSmallSmemMax = 200 * 1024;
+template <int DIM>
+__global__ void __launch_bounds__(kSmallThreads) k_bx_small_vcycle_smem(float* __restrict__ fp, SmallLevels S,
+                                                                        long long lo, int nf, int nsmooth, int fresh) {
+  extern __shared__ float4 sm4[];
+  float4* g4 = reinterpret_cast<float4*>(fp + lo);
+  for (int i = threadIdx.x; i < nf / 4; i += blockDim.x) sm4[i] = g4[i];
+  __syncthreads();
+  small_cycle<DIM>(reinterpret_cast<float*>(sm4), S, nsmooth, fresh);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nf / 4; i += blockDim.x) g4[i] = sm4[i];
+}
+
+// The pool range [lo, hi) of the small levels' arrays, S rebased to lo.
+// False when it does not fit kSmallSmemMax.
+bool small_in_smem(SmallLevels& S, long long& lo, int& nf) {
+  lo = S.L[0].oe;
+  long long hi = 0;
+  for (int i = 0; i < S.n; i++) {
+    const BoxLev& L = S.L[i];
+    long long ends[4] = {L.oe + 4 * L.half, L.og + 4 * L.half,
+                         L.opb + (L.oec < 0 ? 4 : 2) * L.half, L.oec < 0 ? 0 : L.oec + 4 * L.half};
+    for (long long e : ends) hi = std::max(hi, e);
+    lo = std::min({lo, L.oe, L.og, L.opb, L.oec < 0 ? lo : L.oec});
+  }
+  hi = (hi + 63) & ~63LL;
+  if (lo % 4 || (hi - lo) * (long long)sizeof(float) > kSmallSmemMax) return false;
+  nf = (int)(hi - lo);
+  for (int i = 0; i < S.n; i++) {
+    BoxLev& L = S.L[i];
+    L.oe -= lo;
+    L.og -= lo;
+    L.opb -= lo;
+    if (L.oec >= 0) L.oec -= lo;
+  }
+  return true;
 }
 
 // After a cycle on the finest level: tracked residual g <- g - M(e) (M at
@@ -946,6 +995,25 @@ int bx_vcycle(Hier& H, int level, int minlevel, int nsmooth, bool fresh) {
   if (2 * B(H, level).half <= kSmallCells) {
     SmallLevels S{};
     for (int l = level; l >= minlevel; l--) S.L[S.n++] = B(H, l);
+    long long lo;
+    int nf;
+    if (small_in_smem(S, lo, nf)) {
+      static std::atomic<unsigned long long> attr[2];  // the kernels' shared-memory limit, per device
+      if (needs_setup(attr[H.ndims - 2], H.ctx->device)) {
+        cudaError_t e = H.ndims == 2 ? cudaFuncSetAttribute(k_bx_small_vcycle_smem<2>,
+                                                            cudaFuncAttributeMaxDynamicSharedMemorySize, kSmallSmemMax)
+                                     : cudaFuncSetAttribute(k_bx_small_vcycle_smem<3>,
+                                                            cudaFuncAttributeMaxDynamicSharedMemorySize, kSmallSmemMax);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_bx_small_vcycle_smem)");
+        mark_setup(attr[H.ndims - 2], H.ctx->device);
+      }
+      size_t smem = (size_t)nf * sizeof(float);
+      if (H.ndims == 2)
+        k_bx_small_vcycle_smem<2><<<1, kSmallThreads, smem, H.s>>>(H.fpool, S, lo, nf, nsmooth, fresh ? 1 : 0);
+      else
+        k_bx_small_vcycle_smem<3><<<1, kSmallThreads, smem, H.s>>>(H.fpool, S, lo, nf, nsmooth, fresh ? 1 : 0);
+      return after_launch(H, 1);
+    }
     if (H.ndims == 2) k_bx_small_vcycle<2><<<1, kSmallThreads, 0, H.s>>>(H.fpool, S, nsmooth, fresh ? 1 : 0);
     else k_bx_small_vcycle<3><<<1, kSmallThreads, 0, H.s>>>(H.fpool, S, nsmooth, fresh ? 1 : 0);
     return after_launch(H, 1);
