@@ -627,6 +627,25 @@ struct SmallLevels {
   int n;
 };
 
+// q = i / n, r = i % n for i >= 0: a shift and a mask when n is a power of
+// two (every extent of a periodic box level here; the branch is uniform
+// across the CTA), the division otherwise
+__device__ __forceinline__ void divmod(int i, int n, int& q, int& r) {
+  if ((n & (n - 1)) == 0) {
+    q = i >> (__ffs(n) - 1);
+    r = i & (n - 1);
+  } else {
+    q = i / n;
+    r = i - q * n;
+  }
+}
+// linear index j of an n0 x n1 x n2 grid -> (x, y, z)
+__device__ __forceinline__ void unflatten(int j, int n0, int n1, int& x, int& y, int& z) {
+  int r;
+  divmod(j, n0, r, x);
+  divmod(r, n1, z, y);
+}
+
 template <int DIM>
 __device__ __forceinline__ void small_relax(float* fp, const BoxLev& L, int nsmooth, bool fresh) {
   int cnt = L.hh * L.n[1] * L.n[2];
@@ -634,8 +653,9 @@ __device__ __forceinline__ void small_relax(float* fp, const BoxLev& L, int nsmo
     for (int c = 0; c < 2; c++) {
       int first = (fresh && pass == 1) ? c + 1 : 0;
       for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-        int h = i % L.hh, r = i / L.hh;
-        relax_at<DIM>(fp, L, c, first, h, r % L.n[1], r / L.n[1]);
+        int h, y, z;
+        unflatten(i, L.hh, L.n[1], h, y, z);
+        relax_at<DIM>(fp, L, c, first, h, y, z);
       }
       __syncthreads();
     }
@@ -650,13 +670,15 @@ __device__ __forceinline__ void small_cycle(float* fp, const SmallLevels& S, int
     const BoxLev& C = S.L[i + 1];
     int cnt = C.n[0] * C.n[1] * C.n[2];
     for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
-      int X = j % C.n[0], r = j / C.n[0];
-      restrict_at<DIM>(fp, F, C, X, r % C.n[1], r / C.n[1]);
+      int X, Y, Z;
+      unflatten(j, C.n[0], C.n[1], X, Y, Z);
+      restrict_at<DIM>(fp, F, C, X, Y, Z);
     }
     __syncthreads();
     for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
-      int X = j % C.n[0], r = j / C.n[0];
-      coarse_load_at<DIM>(fp, F, C, X, r % C.n[1], r / C.n[1]);
+      int X, Y, Z;
+      unflatten(j, C.n[0], C.n[1], X, Y, Z);
+      coarse_load_at<DIM>(fp, F, C, X, Y, Z);
     }
     __syncthreads();
   }
@@ -664,8 +686,9 @@ __device__ __forceinline__ void small_cycle(float* fp, const SmallLevels& S, int
     const BoxLev &F = S.L[i], &C = S.L[i + 1];
     int cnt = C.n[0] * C.n[1] * C.n[2];
     for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
-      int X = j % C.n[0], r = j / C.n[0];
-      prolong_at<DIM>(fp, F, C, X, r % C.n[1], r / C.n[1]);
+      int X, Y, Z;
+      unflatten(j, C.n[0], C.n[1], X, Y, Z);
+      prolong_at<DIM>(fp, F, C, X, Y, Z);
     }
     __syncthreads();
     small_relax<DIM>(fp, F, nsmooth, false);
