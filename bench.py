@@ -124,25 +124,79 @@ def ncu_traffic(workload, kernel):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """SM clock and clock-event reasons during the timed region: NVML (the
+    driver's libnvidia-ml, through ctypes) read every 2 ms on a thread, or
+    nvidia-smi every 25 ms when NVML cannot be loaded.  Read-only queries."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits of nvml.h
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
+    NVML_CLOCK_SM = 1
 
     def __init__(self, gpu):
-        self.gpu = gpu
+        # the NVML / nvidia-smi name of CUDA device `gpu`: its entry in
+        # CUDA_VISIBLE_DEVICES (an index or a UUID) when that is set
+        vis = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+        self.gpu = vis[gpu] if gpu < len(vis) else str(gpu)
         self.proc = None
+        self.thread = None
+
+    def _nvml(self):
+        import ctypes
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return None
+            h = ctypes.c_void_p()
+            if self.gpu.isdigit():
+                rc = lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(int(self.gpu)), ctypes.byref(h))
+            else:
+                rc = lib.nvmlDeviceGetHandleByUUID(self.gpu.encode(), ctypes.byref(h))
+            if rc != 0:
+                return None
+            rs = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+            return lib, h, rs or lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        except (OSError, AttributeError):
+            return None
+
+    def _loop(self, lib, h, rs):
+        import ctypes
+        clk, mx, r = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        if lib.nvmlDeviceGetMaxClockInfo(h, self.NVML_CLOCK_SM, ctypes.byref(mx)) == 0:
+            self.max = float(mx.value)
+        while not self.done.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, self.NVML_CLOCK_SM, ctypes.byref(clk)) == 0:
+                self.sm.append(float(clk.value))
+            if rs(h, ctypes.byref(r)) == 0:
+                self.reasons.update(nm for nm, bit in self.BITS.items() if r.value & bit)
+            time.sleep(0.002)
 
     def start(self):
+        nv = self._nvml()
+        if nv:
+            import threading
+            self.sm, self.max, self.reasons = [], None, set()
+            self.done = threading.Event()
+            self.thread = threading.Thread(target=self._loop, args=nv, daemon=True)
+            self.thread.start()
+            return
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self.gpu, f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "25"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
 
     def stop(self):
+        if self.thread:
+            self.done.set()
+            self.thread.join(timeout=5)
+            if not self.sm:
+                return None
+            return {"sm_mhz": statistics.median(self.sm), "sm_max_mhz": self.max, "samples": len(self.sm),
+                    "reasons": sorted(self.reasons), "source": "nvml, every 2 ms"}
         if not self.proc:
             return None
         self.proc.terminate()
@@ -166,7 +220,7 @@ class Clocks:
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "samples": len(sm),
-                "reasons": sorted(reasons)}
+                "reasons": sorted(reasons), "source": "nvidia-smi, every 25 ms"}
 
 
 def root_mx(w):
