@@ -16,6 +16,15 @@ from tests.test_parity_gpu import CH2, CH3, uniform_spec, make_pair, PERIODIC2, 
 
 pytestmark = pytest.mark.gpu
 
+
+def levels_spec(nd, n, minlevel, mthbc):
+    """uniform root of n cells per side and the levels below it down to
+    minlevel (extents that are not powers of two, all even)"""
+    s = H.Spec(nd)
+    s.root_and_below(n, minlevel, mthbc, 1.0)
+    return s
+
+
 # case: (config, hierarchy, config tolerance, its error bound, tight tolerance, tight bound)
 MIXED_CASES = {
     "ch2d-periodic-64": (CH2, lambda: uniform_spec(2, 64, PERIODIC2), 1e-9, 2e-6, 1e-12, 1e-9),
@@ -23,6 +32,10 @@ MIXED_CASES = {
     "ch3d-periodic-32": (CH3, lambda: uniform_spec(3, 32, PERIODIC3), 1e-8, 1e-5, 1e-11, 1e-8),
     "ch3d-periodic-64": (CH3, lambda: uniform_spec(3, 64, PERIODIC3), 1e-8, 1e-5, 1e-11, 1e-8),
     "ch3d-dirichlet-16": (CH3, lambda: uniform_spec(3, 16, DIRICHLET3), 1e-8, 1e-5, 1e-11, 1e-8),
+    # periodic boxes whose extents are not powers of two (48..6, 24..6): the
+    # box path's coarse-end cycle takes cell coordinates by division
+    "ch2d-periodic-48": (CH2, lambda: levels_spec(2, 48, -3, PERIODIC2), 1e-9, 2e-6, 1e-12, 1e-9),
+    "ch3d-periodic-24": (CH3, lambda: levels_spec(3, 24, -2, PERIODIC3), 1e-8, 1e-5, 1e-11, 1e-8),
     "ch2d-amr-periodic": (CH2, lambda: H.amr2d(periodic=True), 1e-9, 2e-6, 1e-12, 1e-9),
     "ch3d-amr-periodic": (CH3, lambda: H.amr3d(periodic=True), 1e-8, 1e-5, 1e-11, 1e-8),
 }
