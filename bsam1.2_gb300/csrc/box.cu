@@ -621,7 +621,7 @@ __global__ void __launch_bounds__(256) k_bx_prolong(float* __restrict__ fp, BoxL
 // __syncthreads() instead of kernel boundaries, so a cycle spends one launch
 // instead of eleven per level on grids too small to fill the GPU.
 constexpr int kSmallCells = 8192;
-constexpr int kSmallThreads = 1024;
+constexpr int kSmallThreads = 512;
 struct SmallLevels {
   BoxLev L[kNLev];  // L[0] the top (finest) small level, then coarser
   int n;
