@@ -34,15 +34,17 @@ METRIC = "CH steps/s at resid≤1e-8: batched+mixed vs plain FP64, 1 GB300; p50/
 
 WORKLOADS = {
     "ch3d-256": dict(ndims=3, n=256, minlevel=-7, mthbc=[2, 2, 2, 2, 2, 2], eps=0.02, dt=5e-4, tol=1e-8,
-                     mean=0.1, amp=0.05, seed=20240503,
+                     mean=0.1, amp=0.05, seed=20240503, l2="inputs larger than L2 (q+qold 550 MB FP64)",
                      desc="3D Cahn-Hilliard 256^3 periodic, eps=0.02, dt=5e-4, V(2,2), resid<=1e-8"),
     # a smaller 3D box with the same kernels and a working set still above
     # L2 (relax ~150 MB per sweep): the case the detailed ncu profiles use
     "ch3d-256x256x128": dict(ndims=3, n=256, mx=[256, 256, 128], minlevel=-6, mthbc=[2, 2, 2, 2, 2, 2], eps=0.02,
                              dt=5e-4, tol=1e-8, mean=0.1, amp=0.05, seed=20240503,
+                             l2="inputs larger than L2 (q+qold 275 MB FP64)",
                              desc="3D Cahn-Hilliard 256x256x128 periodic, eps=0.02, dt=5e-4, V(2,2), resid<=1e-8"),
     "ch2d-128": dict(ndims=2, n=128, minlevel=-6, mthbc=[2, 2, 2, 2, 10, 10], eps=0.01, dt=1e-3, tol=1e-9,
                      mean=0.0, amp=0.05, seed=20240503,
+                     l2="L2-resident (q+qold 0.5 MB FP64), no flush between steps: launch-bound",
                      desc="2D Cahn-Hilliard 128^2 periodic, eps=0.01, dt=1e-3, V(2,2), resid<=1e-9"),
 }
 # cfg2: adaptive mesh rebuilt before every step by the regrid (TakeTimeSteps'
@@ -345,12 +347,21 @@ def cpu_baseline(pkg, w, vcycles_per_step, nvc=2):
                               f"V-cycles per step of the FP64 run)")
 
 
+def arm_config(args, w, dist):
+    """the config block of a uniform workload's JSON line (both arms)"""
+    return {"workload": args.workload, "desc": w["desc"], "n": w["n"], "ndims": w["ndims"],
+            "minlevel": w["minlevel"], "nsmooth": NSMOOTH, "tol": w["tol"],
+            "parallelism": f"replicas x{dist.ws}",
+            "l2": w["l2"]}
+
+
 def reference_arm(args, w, dist):
     """--impl reference: the reference algorithm on the host cores (the CPU
-    oracle; the reference itself is Fortran and no Fortran compiler exists
-    on these machines).  Each step is a bounded sample: one V-cycle of the
-    workload's first time step; a full first time step during warm-up gives
-    the V-cycles per step used to convert to steps/s."""
+    oracle, one thread like the reference: the reference itself is Fortran
+    and no Fortran compiler exists on these machines).  The same time steps
+    as the GPU arms: --warmup full steps untimed, then --steps full steps
+    timed, each a CopyQToQold + MultigridIterations to the tolerance
+    (TakeTimeSteps, bsamroutines.f90:608-816, on a fixed mesh)."""
     if dist.rank != 0:
         return
     import __graft_entry__ as ge
@@ -365,29 +376,31 @@ def reference_arm(args, w, dist):
     o.put(0, "q", q)
     o.set_ghost(0, 0)
     o.copy_q_to_qold(w["minlevel"], 0)
-    t = time.perf_counter()
-    nv, _ = o.time_step(True, 0, w["minlevel"], NSMOOTH, MAXV, w["tol"])
-    t_step = time.perf_counter() - t
-    for _ in range(max(0, args.warmup - 1)):
-        o.multigrid_iterations(0, w["minlevel"], NSMOOTH, 1, 0.0)
-    ts = []
-    for _ in range(args.steps):
+    vc, ts = [], []
+    t_warm = time.perf_counter()
+    for s in range(args.warmup):
+        nv, _ = o.time_step(s == 0, 0, w["minlevel"], NSMOOTH, MAXV, w["tol"])
+    t_warm = time.perf_counter() - t_warm
+    for s in range(args.steps):
         t = time.perf_counter()
-        o.multigrid_iterations(0, w["minlevel"], NSMOOTH, 1, 0.0)
+        nv, _ = o.time_step(args.warmup == 0 and s == 0, 0, w["minlevel"], NSMOOTH, MAXV, w["tol"])
         ts.append(time.perf_counter() - t)
-    per_v = statistics.mean(ts)
-    value = 1.0 / (per_v * nv)
+        vc.append(nv)
+    total = sum(ts)
+    value = args.steps / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_v * nv * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded splitmix64 spinodal start)",
-        "config": {"workload": args.workload, "desc": w["desc"]},
+        "data": "synthetic (seeded splitmix64 spinodal start, mu0 from phi0)",
+        "config": arm_config(args, w, dist),
+        "p50_ms": 1e3 * pct(ts, 50), "p99_ms": 1e3 * pct(ts, 99),
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": 1, "kind": "port",
-                         "sample": f"each step = one V-cycle of the first time step; a full first step "
-                                   f"({nv} V-cycles, {t_step:.1f} s) measured during warm-up"},
+                         "sample": f"oracle (C restatement of the reference, 1 thread, -O2 -ffp-contract=off): "
+                                   f"{args.warmup} full time steps untimed ({t_warm:.1f} s), then {args.steps} "
+                                   f"full time steps timed ({total:.1f} s), the same steps as the GPU arms"},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "vcycles_per_step": nv, "first_step_s": t_step,
+        "vcycles_per_step": statistics.mean(vc),
     }
     print(json.dumps(line), flush=True)
 
@@ -717,10 +730,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": t_mixed / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded splitmix64 spinodal start, mu0 from phi0)",
-        "config": {"workload": args.workload, "desc": w["desc"], "n": w["n"], "ndims": w["ndims"],
-                   "minlevel": w["minlevel"], "nsmooth": NSMOOTH, "tol": w["tol"],
-                   "parallelism": f"replicas x{dist.ws}",
-                   "l2": "inputs larger than L2 (q+qold 550 MB FP64 at 256^3)"},
+        "config": arm_config(args, w, dist),
         "p50_ms": pct(mixed["per_ms"], 50), "p99_ms": pct(mixed["per_ms"], 99),
         "vcycles_per_step": vps_m,
         "plain_fp64": {"value": v_fp64, "unit": "steps/s", "ms_per_step": t_fp64 / args.steps,

@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(kFinishThreads) k_norm_finish(const double* __
     }
     out[0] = r;
     out[1] = sum;
-    nonfinite[0] = isfinite(r) ? 0 : 1;
+    if (nonfinite) nonfinite[0] = isfinite(r) ? 0 : 1;
   }
 }
 

@@ -66,7 +66,8 @@ int launch_update_source(const LaunchCtx& c, const Blk* blk, int nblk);
 int launch_norm_partial(const LaunchCtx& c, const Blk* blk, int nblk,
                         double* partial, int store_rf);
 // deterministic final sum; writes out[0] = norm, out[1] = raw sum,
-// and ok[0] = 0 when the norm is finite, 1 otherwise.  out must hold
+// and nonfinite[0] = 0 when the norm is finite, 1 otherwise (nothing when
+// nonfinite is null).  out must hold
 // kNormOutLen doubles (out[8 ..] is scratch of the two-stage sum); the
 // partials hold nrvars values per block.
 int launch_norm_finish(cudaStream_t s, const double* partial, int nblk,

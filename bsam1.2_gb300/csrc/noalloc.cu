@@ -8,20 +8,25 @@
 // other streams are busy.  This entry point computes ErrorAFAS
 // (afasroutines.f90:113-233) of one CH patch from q and f the caller already
 // has on the device and writes the norm to a device double the caller owns.
-// Its only scratch -- one partial sum per block -- lives in a file-scope
-// __device__ array of fixed size, so a patch may have at most
-// BSAMG_NOALLOC_MAX_CELLS interior cells (256^3).
+// Its only scratch -- one partial sum per block plus the final reduction's
+// stage sums -- lives in a file-scope __device__ array of fixed size, so a
+// patch may have at most BSAMG_NOALLOC_MAX_CELLS interior cells (256^3).
 //
 // The array exists once per device for the life of the process and every
 // call on that device shares it: two calls whose kernels overlap on the GPU
 // (different streams, no ordering between them) race on it.  Each call
 // writes every partial it later reads, so nothing needs clearing between
 // calls.  The first call on a device looks the array's device address up
-// (cudaGetSymbolAddress, with that device current); make that first call
-// before any stream capture that includes this entry point.
+// (cudaGetSymbolAddress, with that device current) and keeps it for the
+// rest of the process; make that first call before any stream capture that
+// includes this entry point.  The kept address does not survive
+// cudaDeviceReset (the module is loaded again, possibly elsewhere): a host
+// that resets a device must not call this entry point on it afterwards.
 //
-// Same arithmetic and block decomposition as the hierarchy's norm kernel
-// (this file is also built with --fmad=false), so the two agree bit for bit.
+// Same arithmetic, block decomposition and final reduction as the
+// hierarchy's norm (the partial kernel below is k_norm_partial's for one CH
+// patch, built with --fmad=false like it, and the final sum is
+// launch_norm_finish itself), so the two agree bit for bit.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -29,6 +34,7 @@
 #include "../../include/bsamg.h"
 #include "hier.h"
 #include "internal.h"
+#include "launch.h"
 
 namespace {
 
@@ -37,8 +43,9 @@ using namespace bsamg;
 constexpr int kMaxBlocks = BSAMG_NOALLOC_MAX_CELLS / kBlock;
 
 // [0, 2*kMaxBlocks): per-block partial sums of rf^2 (two variables);
-// [2*kMaxBlocks]: non-finite flag of the last call
-__device__ __align__(256) double g_norm_scratch[2 * kMaxBlocks + 32];
+// [2*kMaxBlocks, 2*kMaxBlocks + kNormOutLen): the final reduction's output
+// and stage sums (launch_norm_finish's `out`)
+__device__ __align__(256) double g_norm_scratch[2 * kMaxBlocks + kNormOutLen];
 
 std::mutex g_mu;
 constexpr int kMaxDevices = 256;
@@ -123,40 +130,6 @@ __global__ void __launch_bounds__(kBlock) k_norm_single(const double* __restrict
   }
 }
 
-// final reduction in block order (as k_norm_finish), norm to the caller's
-// double, non-finite flag to the scratch tail
-__global__ void k_norm_single_finish(const double* __restrict__ partial, int nblk, double count, int errortype,
-                                     double* norm_out, double* flag) {
-  __shared__ double red[2][kBlock];
-  double t0 = 0.0, t1 = 0.0;
-  for (int n = threadIdx.x; n < nblk; n += blockDim.x) {
-    t0 = t0 + partial[2 * n];
-    t1 = t1 + partial[2 * n + 1];
-  }
-  red[0][threadIdx.x] = t0;
-  red[1][threadIdx.x] = t1;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      red[0][threadIdx.x] = red[0][threadIdx.x] + red[0][threadIdx.x + s];
-      red[1][threadIdx.x] = red[1][threadIdx.x] + red[1][threadIdx.x + s];
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    double a = red[0][0], c = red[1][0], r;
-    if (errortype == 1) {
-      r = sqrt((a + c) / count);
-    } else {
-      double cells = count / 2.0;
-      double e0 = sqrt(a / cells), e1 = sqrt(c / cells);
-      r = e1 > e0 ? e1 : e0;
-    }
-    norm_out[0] = r;
-    flag[0] = isfinite(r) ? 0.0 : 1.0;
-  }
-}
-
 }  // namespace
 
 extern "C" int bsamg_ch_residual_norm_noalloc(const double* q, const double* f, int ndims, const int mx[3],
@@ -187,9 +160,13 @@ extern "C" int bsamg_ch_residual_norm_noalloc(const double* q, const double* f, 
     k_norm_single<2><<<nblk, kBlock, 0, s>>>(q, f, mx[0], mx[1], 1, c0, c1, scratch);
   else
     k_norm_single<3><<<nblk, kBlock, 0, s>>>(q, f, mx[0], mx[1], mx[2], c0, c1, scratch);
-  k_norm_single_finish<<<1, kBlock, 0, s>>>(scratch, nblk, 2.0 * (double)cells, errortype, norm_out,
-                                            scratch + 2 * kMaxBlocks);
+  // the hierarchy's own final reduction (two stages above 2048 blocks);
+  // no non-finite flag: a NaN or Inf input shows as a NaN or Inf norm
+  double* out = scratch + 2 * kMaxBlocks;
+  launch_norm_finish(s, scratch, nblk, 2, 2.0 * (double)cells, errortype, out, nullptr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "bsamg_ch_residual_norm_noalloc launch");
+  e = cudaMemcpyAsync(norm_out, out, sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "bsamg_ch_residual_norm_noalloc copy");
   return BSAMG_OK;
 }

@@ -322,8 +322,12 @@ int bsamg_smoother_colours(bsamg_hier* h, int level, int mode, int* colours);
  * at most BSAMG_NOALLOC_MAX_CELLS interior cells (larger patches return
  * BSAMG_ERR_ARG).  Every call on a device shares that array, so calls whose
  * kernels overlap on the GPU race; order them on one stream.  The first call
- * on a device looks up the array's address: make it before any stream
- * capture.  Agrees bit for bit with bsamg_residual_norm on the same data. */
+ * on a device looks up the array's address and keeps it for the process:
+ * make it before any stream capture, and do not call this entry point on a
+ * device after cudaDeviceReset.  Same per-block partials and final
+ * reduction as bsamg_residual_norm, so it agrees with it bit for bit on the
+ * same data.  A NaN or Inf in the data gives a NaN or Inf norm (there is no
+ * separate non-finite flag). */
 #define BSAMG_NOALLOC_MAX_CELLS 16777216
 int bsamg_ch_residual_norm_noalloc(const double* q, const double* f,
                                    int ndims, const int mx[3], double h,

@@ -25,19 +25,24 @@ def levels_spec(nd, n, minlevel, mthbc):
     return s
 
 
-# case: (config, hierarchy, config tolerance, its error bound, tight tolerance, tight bound)
+# case: (config, hierarchy, config tolerance, its error bound, tight tolerance, tight bound).
+# The bounds are what the path delivers with a margin of about three: the
+# largest errors measured on a GB300 were 3.4e-8 (3D) and 7.8e-9 (2D) at the
+# configuration tolerances, 5.4e-11 (3D at 1e-11) and 5.7e-12 (2D at 1e-12)
+# tightly converged.
+B2, B2T, B3, B3T = 3e-8, 3e-11, 1e-7, 2e-10
 MIXED_CASES = {
-    "ch2d-periodic-64": (CH2, lambda: uniform_spec(2, 64, PERIODIC2), 1e-9, 2e-6, 1e-12, 1e-9),
-    "ch2d-neumann-64": (CH2, lambda: uniform_spec(2, 64, NEUMANN2), 1e-9, 2e-6, 1e-12, 1e-9),
-    "ch3d-periodic-32": (CH3, lambda: uniform_spec(3, 32, PERIODIC3), 1e-8, 1e-5, 1e-11, 1e-8),
-    "ch3d-periodic-64": (CH3, lambda: uniform_spec(3, 64, PERIODIC3), 1e-8, 1e-5, 1e-11, 1e-8),
-    "ch3d-dirichlet-16": (CH3, lambda: uniform_spec(3, 16, DIRICHLET3), 1e-8, 1e-5, 1e-11, 1e-8),
+    "ch2d-periodic-64": (CH2, lambda: uniform_spec(2, 64, PERIODIC2), 1e-9, B2, 1e-12, B2T),
+    "ch2d-neumann-64": (CH2, lambda: uniform_spec(2, 64, NEUMANN2), 1e-9, B2, 1e-12, B2T),
+    "ch3d-periodic-32": (CH3, lambda: uniform_spec(3, 32, PERIODIC3), 1e-8, B3, 1e-11, B3T),
+    "ch3d-periodic-64": (CH3, lambda: uniform_spec(3, 64, PERIODIC3), 1e-8, B3, 1e-11, B3T),
+    "ch3d-dirichlet-16": (CH3, lambda: uniform_spec(3, 16, DIRICHLET3), 1e-8, B3, 1e-11, B3T),
     # periodic boxes whose extents are not powers of two (48..6, 24..6): the
     # box path's coarse-end cycle takes cell coordinates by division
-    "ch2d-periodic-48": (CH2, lambda: levels_spec(2, 48, -3, PERIODIC2), 1e-9, 2e-6, 1e-12, 1e-9),
-    "ch3d-periodic-24": (CH3, lambda: levels_spec(3, 24, -2, PERIODIC3), 1e-8, 1e-5, 1e-11, 1e-8),
-    "ch2d-amr-periodic": (CH2, lambda: H.amr2d(periodic=True), 1e-9, 2e-6, 1e-12, 1e-9),
-    "ch3d-amr-periodic": (CH3, lambda: H.amr3d(periodic=True), 1e-8, 1e-5, 1e-11, 1e-8),
+    "ch2d-periodic-48": (CH2, lambda: levels_spec(2, 48, -3, PERIODIC2), 1e-9, B2, 1e-12, B2T),
+    "ch3d-periodic-24": (CH3, lambda: levels_spec(3, 24, -2, PERIODIC3), 1e-8, B3, 1e-11, B3T),
+    "ch2d-amr-periodic": (CH2, lambda: H.amr2d(periodic=True), 1e-9, B2, 1e-12, B2T),
+    "ch3d-amr-periodic": (CH3, lambda: H.amr3d(periodic=True), 1e-8, B3, 1e-11, B3T),
 }
 
 
@@ -70,8 +75,8 @@ def test_mixed_reaches_the_fp64_solution(pkg, ctx, oracle_mod, case):
     err = _run(pkg, ctx, oracle_mod, cfg, mk(), tol)
     print(f"{case}: max rel error of phi vs FP64 oracle: {err:.3e} at tol {tol:g}, "
           f"{err_tight:.3e} at tol {tight:g}")
-    assert err_tight <= tight_bound
-    assert err <= bound
+    assert err_tight <= tight_bound, err_tight
+    assert err <= bound, err
 
 
 @pytest.mark.parametrize("mode", ["mixed", "fp64"])
