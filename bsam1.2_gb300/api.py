@@ -12,10 +12,11 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libbsamg.so")
+# BSAMG_LIBRARY names another build of the library (one linked with extra
+# problem plugins, bsam1.2_gb300/build.py build(extra_plugins=...))
+LIB_PATH = os.environ.get("BSAMG_LIBRARY") or os.path.join(HERE, "libbsamg.so")
 
 FIELD = {"q": 0, "qold": 1, "qc": 2, "f": 3, "rf": 4, "ftmp": 5}
-PROBLEM = {"ch": 1, "biogrowth": 2, "growth": 3}
 MODE = {"fp64": 0, "mixed": 1}
 
 _lib = None
@@ -149,6 +150,8 @@ def lib():
         "bsamg_format_f25_12": ([D, ctypes.c_char_p], I),
         "bsamg_seed_spinodal": ([P, I, ctypes.c_ulonglong, D, D], I),
         "bsamg_format_stats_line": ([D, DP, ctypes.c_longlong, ctypes.c_char_p, SZ], I),
+        "bsamg_problem_kind": ([ctypes.c_char_p, IP], I),
+        "bsamg_problem_info": ([I, IP, IP, IP], I),
         "bsamg_strerror": ([I], ctypes.c_char_p),
         "bsamg_last_error_detail": ([], ctypes.c_char_p),
     }
@@ -158,6 +161,24 @@ def lib():
         fn.restype = res
     _lib = L
     return L
+
+
+def problem_kind(problem):
+    """The kind of a registered problem plugin, by name ("ch", "biogrowth",
+    "growth", or any plugin linked into the library) or kind."""
+    if isinstance(problem, int):
+        return problem
+    k = ctypes.c_int()
+    _ck(lib().bsamg_problem_kind(problem.encode(), ctypes.byref(k)), f"bsamg_problem_kind({problem!r})")
+    return k.value
+
+
+def problem_info(problem):
+    """(nrvars, minimum parameter count, has a mixed-precision form) of a plugin."""
+    nv, npar, mixed = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _ck(lib().bsamg_problem_info(problem_kind(problem), ctypes.byref(nv), ctypes.byref(npar), ctypes.byref(mixed)),
+        "bsamg_problem_info")
+    return nv.value, npar.value, bool(mixed.value)
 
 
 def exported_symbols():
@@ -214,7 +235,7 @@ class Hierarchy:
         h = ctypes.c_void_p()
         p = _da(params, len(params))
         q = _da(qpo if qpo is not None else [0.0] * nrvars, nrvars)
-        _ck(lib().bsamg_hier_create(ctx.h, ndims, nrvars, mbc, PROBLEM[problem], p, len(params), q,
+        _ck(lib().bsamg_hier_create(ctx.h, ndims, nrvars, mbc, problem_kind(problem), p, len(params), q,
                                     ctypes.byref(h)), "bsamg_hier_create")
         self.h = h
 

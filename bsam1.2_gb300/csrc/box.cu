@@ -1092,7 +1092,10 @@ int bx_cycle(Hier& H, int finest, int minlevel, int nsmooth, int errortype) {
 
 bool box_eligible(const Hier& H, bool periodic_single) {
   // the box path's split/merge address q with one ghost layer
-  if (H.problem != kCH || !periodic_single || H.mbc != 1) return false;
+  // the box kernels carry CH's equations: only a plugin that declares the
+  // box path (CH) takes it
+  const Plugin* pl = find_plugin(H.problem);
+  if (!pl || !pl->box || !periodic_single || H.mbc != 1) return false;
   for (int l = H.minlevel; l <= H.maxlevel; l++) {
     const HostPatch& P = H.patches[H.L(l).patches[0]];
     for (int d = 0; d < H.ndims; d++) {

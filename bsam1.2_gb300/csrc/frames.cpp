@@ -287,8 +287,11 @@ int after_step_stats(Hier& H, int finest, double* integral, long long* meshsize)
   int r = set_device(H);
   if (r) return r;
   int nd = H.ndims;
-  int mass = !(H.problem == kBio && nd == 3);
-  int energy = H.problem == kCH && nd == 2;
+  // which of AfterStep2D/3D's sums the plugin has (bit 0: the integral of
+  // phi, bit 1: CH's energy)
+  int which = find_plugin(H.problem)->stats(nd);
+  int mass = which & 1;
+  int energy = (which >> 1) & 1;
   long long ms = 0;
   int total = 0;
   for (int l = 0; l <= finest; l++) {
@@ -698,7 +701,7 @@ int bsamg_read_q(bsamg_hier* root, const char* path, int first_id, double* time,
 }
 
 int bsamg_seed_spinodal(bsamg_hier* h, int id, unsigned long long seed, double mean, double amp) {
-  if (!h || !h->committed || h->problem != kCH || h->nrvars != 2) return BSAMG_ERR_ARG;
+  if (!h || !h->committed || h->problem != BSAMG_PROBLEM_CH || h->nrvars != 2) return BSAMG_ERR_ARG;
   h->box_g_valid = false;
   auto it = h->id2idx.find(id);
   if (it == h->id2idx.end()) return BSAMG_ERR_NOT_FOUND;

@@ -439,16 +439,11 @@ struct Emitter {
       }
   }
 
-  // Dirichlet masks of the plugin's UserBC (CH/problem.f90:770-881,
-  // BioGrowth/problem.f90:623-736): 2D CH reflects both variables, 2D
-  // BioGrowth reflects phi and sets n = 2 - n, both 3D plugins set 2 - q;
-  // the growth plugin reflects phi, sets n = 2 - n (value 1) and p = -p
-  // (value 0).  Bits 0-7: 2 - q; bits 8-15: -q.
-  int bc_mask() const {
-    if (H.problem == kGrowth) return 2 | (4 << 8);
-    if (H.ndims == 3) return (1 << H.nrvars) - 1;
-    return H.problem == kCH ? 0 : 2;
-  }
+  // Dirichlet masks of the plugin's UserBC2D/3D (CH/problem.f90:770-881,
+  // BioGrowth/problem.f90:623-736; the plugin files state theirs): bits 0-7
+  // the variables set to 2 - q, bits 8-15 those set to -q, the others
+  // reflected.
+  int bc_mask() const { return find_plugin(H.problem)->bc_mask(H.ndims); }
 
   // SetPhysicalBC2D/3D (boundary.f90:614-802) -> UserBC on each face with
   // mthbc = 10, faces in order 1..2*ndims.

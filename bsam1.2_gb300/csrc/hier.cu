@@ -193,10 +193,12 @@ int fp_prepare_tail(Hier& H, int finest, int minlevel, int nsmooth) {
       D.orf = add(D.orf, (long long)H.nrvars * P.sf, 1);
     }
     if (so * (long long)sizeof(double) <= kTailSmemMax && !segs.empty() && !prog.empty()) {
-      static std::atomic<unsigned long long> attr{0};  // the kernels' shared-memory limit, per device
-      if (needs_setup(attr, H.ctx->device)) {
-        if (tail_smem_attributes()) return cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute(tail)");
-        mark_setup(attr, H.ctx->device);
+      // the kernels' shared-memory limit, per plugin and device
+      static std::atomic<unsigned long long> attr[kMaxPlugins];
+      std::atomic<unsigned long long>& a = attr[H.problem & (kMaxPlugins - 1)];
+      if (needs_setup(a, H.ctx->device)) {
+        if (tail_smem_attributes(H.problem)) return cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute(tail)");
+        mark_setup(a, H.ctx->device);
       }
       T.smem_bytes = (int)(so * sizeof(double));
       T.nsegs = (int)segs.size();
@@ -361,21 +363,19 @@ int replay(Hier& H, Hier::GraphRec* g) {
 
 // plugin coefficients for a spacing h (see PatchDev::c)
 void coefficients(const Hier& H, double h, double* c) {
-  double h2 = h * h;
-  if (H.problem == kCH) {
-    double k = H.ndims == 2 ? 4.0 : 6.0;
-    c[0] = H.pp.dt / h2;       // tmp1, CH/problem.f90:341
-    c[1] = H.pp.eps2 / h2;     // tmp2, :342
-    c[2] = k * H.pp.eps2 / h2; // tmp3, :343 (:579)
-    c[3] = k * c[0];           // a(1,2), :346 (:582)
-  } else {
-    // BioGrowth's 2D expressions; the growth plugin uses 2*ndims neighbours
-    double k = H.problem == kGrowth ? 2.0 * H.ndims : 4.0;
-    c[0] = H.pp.dt * H.pp.eps2 / h2;  // tmp1, BioGrowth/problem.f90:277
-    c[1] = 1.0 / h2;                  // tmp3, :278
-    c[2] = k * c[0] + 1.0;            // first two terms of tmp2, :282
-    c[3] = k * c[1];                  // first term of tmp4, :288
-  }
+  find_plugin(H.problem)->coefficients(H.pp, H.ndims, h, c);
+}
+
+// SetProb: the plugin's parameters from the caller's list (validated
+// against the plugin's minimum count by the caller)
+void set_problem_params(Hier& H, const double* params, int nparams) {
+  double qpo[kMaxVars];
+  std::memcpy(qpo, H.pp.qpo, sizeof(qpo));
+  H.pp = ProbParams{};
+  std::memcpy(H.pp.qpo, qpo, sizeof(qpo));
+  H.pp.nrvars = H.nrvars;
+  H.pp.problem = H.problem;
+  find_plugin(H.problem)->set_params(H.pp, params, nparams);
 }
 
 // PeriodicSetup, boundary.f90:805-872
@@ -926,13 +926,10 @@ int bsamg_hier_create(bsamg_ctx* ctx, int ndims, int nrvars, int mbc, int proble
   if (!ctx || !out || !params) return BSAMG_ERR_ARG;
   if (ndims < 2 || ndims > 3) return BSAMG_ERR_ARG;
   if (mbc < 1 || mbc > 2) return BSAMG_ERR_UNSUPPORTED;  // RootInit, bsamroutines.f90:305-308
-  if (problem_kind != BSAMG_PROBLEM_CH && problem_kind != BSAMG_PROBLEM_BIOGROWTH &&
-      problem_kind != BSAMG_PROBLEM_GROWTH)
-    return BSAMG_ERR_ARG;
-  if (nrvars != nvars_of(problem_kind)) return BSAMG_ERR_UNSUPPORTED;  // CH, BioGrowth: 2; growth: 3
-  if (nparams < 2 || (problem_kind == BSAMG_PROBLEM_BIOGROWTH && nparams < 5) ||
-      (problem_kind == BSAMG_PROBLEM_GROWTH && nparams < 6))
-    return BSAMG_ERR_ARG;
+  const Plugin* pl = find_plugin(problem_kind);  // a registered problem plugin
+  if (!pl) return BSAMG_ERR_ARG;
+  if (nrvars != pl->nvars) return BSAMG_ERR_UNSUPPORTED;  // CH, BioGrowth: 2; growth: 3
+  if (nparams < 2 || nparams < pl->nparams) return BSAMG_ERR_ARG;
   bsamg_hier* h = new (std::nothrow) bsamg_hier();
   if (!h) return BSAMG_ERR_ARG;
   h->ctx = ctx;
@@ -941,15 +938,8 @@ int bsamg_hier_create(bsamg_ctx* ctx, int ndims, int nrvars, int mbc, int proble
   h->mbc = mbc;
   h->problem = problem_kind;
   h->params.assign(params, params + nparams);
-  h->pp.dt = params[0];
-  h->pp.eps2 = params[1] * params[1];  // SetProb, CH/problem.f90:32
-  h->pp.gamma = nparams > 2 ? params[2] : 0.0;
-  h->pp.lambda = nparams > 3 ? params[3] : 0.0;
-  h->pp.czero = nparams > 4 ? params[4] : 0.0;
-  h->pp.cpress = nparams > 5 ? params[5] : 0.0;
   for (int v = 0; v < kMaxVars; v++) h->pp.qpo[v] = (qpo && v < nrvars) ? qpo[v] : 0.0;
-  h->pp.nrvars = nrvars;
-  h->pp.problem = problem_kind;
+  set_problem_params(*h, params, nparams);
   *out = h;
   return BSAMG_OK;
 }
@@ -1203,19 +1193,14 @@ int bsamg_graph_stats(const bsamg_hier* h, int* instantiated, int* updated) {
 
 int bsamg_set_params(bsamg_hier* h, const double* params, int nparams) {
   if (!h || !h->committed || !params) return BSAMG_ERR_ARG;
-  if (nparams < 2 || (h->problem == kBio && nparams < 5) || (h->problem == kGrowth && nparams < 6))
-    return BSAMG_ERR_ARG;
+  const Plugin* pl = find_plugin(h->problem);
+  if (nparams < 2 || nparams < pl->nparams) return BSAMG_ERR_ARG;
   if ((int)h->params.size() == nparams && std::equal(params, params + nparams, h->params.begin())) return BSAMG_OK;
   h->box_g_valid = false;
   int r = set_device(*h);
   if (r) return r;
   h->params.assign(params, params + nparams);
-  h->pp.dt = params[0];
-  h->pp.eps2 = params[1] * params[1];  // SetProb, CH/problem.f90:32
-  h->pp.gamma = nparams > 2 ? params[2] : 0.0;
-  h->pp.lambda = nparams > 3 ? params[3] : 0.0;
-  h->pp.czero = nparams > 4 ? params[4] : 0.0;
-  h->pp.cpress = nparams > 5 ? params[5] : 0.0;
+  set_problem_params(*h, params, nparams);
   for (size_t n = 0; n < h->patches.size(); n++) {
     PatchDev& D = h->hP[n];
     coefficients(*h, h->patches[n].dx[0], D.c);
@@ -1240,10 +1225,10 @@ int bsamg_set_params(bsamg_hier* h, const double* params, int nparams) {
       if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(tail patch table)");
     }
   // Kernels read the coefficients from the patch table, except those of the
-  // periodic-box path and the BioGrowth/growth parameters, which are kernel
-  // arguments captured in graphs: those graphs are captured again.
+  // periodic-box path and the parameters of plugins whose kernels take them
+  // as arguments (captured in graphs): those graphs are captured again.
   if (h->box) box_coefficients(*h);
-  bool keep_graphs = h->problem == kCH && !h->box;
+  bool keep_graphs = pl->coeffs_only && !h->box;
   if (!keep_graphs) {
     e = cudaStreamSynchronize(h->s);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");

@@ -13,6 +13,7 @@
 #include "../../include/bsamg.h"
 #include "internal.h"
 #include "launch.h"
+#include "plugin.h"
 
 namespace bsamg {
 

@@ -19,10 +19,6 @@ constexpr int kInternalBC = 999;         // nodeinfodef.f90:59
 constexpr int kMaxVars = 10;             // nodeinfodef.f90:64
 constexpr int kBlock = 256;              // threads per block of the cell kernels
 
-enum Problem : int { kCH = 1, kBio = 2, kGrowth = 3 };
-// variables of a plugin
-constexpr int nvars_of(int problem) { return problem == kGrowth ? 3 : 2; }
-
 struct PatchDev {
   int mx[3];   // interior extents (1 for the unused dimension in 2D)
   int qn[3];   // ghosted extents of q/qold (1 for the unused dimension)
@@ -43,11 +39,12 @@ struct PatchDev {
   // correction right-hand side g (interior, like f) and the frozen base
   // phase field phib (interior, one plane)
   long long eq, ecq, eg, ephi;
-  // Plugin coefficients for this patch's spacing, computed on the host with
-  // the reference's expressions (CH/problem.f90:339-347, :411-413,
-  // BioGrowth/problem.f90:276-278, :333-336):
+  // Plugin coefficients for this patch's spacing, computed on the host by
+  // the plugin's coefficients() with the reference's expressions, e.g.
   //   CH : c0 = dt/h^2, c1 = eps^2/h^2, c2 = (4|6)*eps^2/h^2, c3 = (4|6)*c0
+  //        (CH/problem.f90:339-346, :575-582)
   //   Bio: c0 = dt*eps^2/h^2, c1 = 1/h^2, c2 = 4*c0 + 1, c3 = 4*c1
+  //        (BioGrowth/problem.f90:276-288)
   double c[4];
   float cf[4];  // the same coefficients rounded to FP32 on the host (mixed path)
   double h;
@@ -76,7 +73,7 @@ struct Blk {
   int start;
 };
 
-// Ghost program operations (see ghost.cu).
+// Ghost program operations (compiled by ghostc.cpp).
 enum GhostType : int {
   kGCopy = 0,     // dst = src
   kGCopyAdd = 1,  // dst = src + qpo[v]
@@ -97,9 +94,15 @@ struct GhostOp {
   int mask;   // BC: bits 0-7 variables with value 1 on the face (2 - q), bits 8-15 value 0 (-q)
 };
 
+// The problem's parameters as the plugin's kernels see them (a kernel
+// argument): dt and the reference plugins' problemdata (eps^2, gamma,
+// lambda, c0), the growth plugin's pressure coefficient, and eight slots a
+// new plugin may fill in its set_params; the quasi-periodic offsets qpo of
+// SelfPeriodicBC; nrvars; the plugin's kind.
 struct ProbParams {
   double dt, eps2, gamma, lambda, czero;
-  double cpress;  // growth plugin: pressure source coefficient
+  double cpress;
+  double user[8];
   double qpo[kMaxVars];
   int nrvars;
   int problem;

@@ -95,10 +95,10 @@ int launch_ghost_program_1cta(const LaunchCtx& c, const GhostOp* ops,
 // the recorded coarse tail of an FP64 V-cycle, one block
 int launch_tail(const LaunchCtx& c, const TailPhase* ph, int nph);
 // the same on arrays staged in shared memory (shadow: the patch table that
-// addresses them); tail_smem_attributes raises the kernels' dynamic
-// shared-memory limit to kTailSmemMax once (0 on success)
+// addresses them); tail_smem_attributes raises the dynamic shared-memory
+// limit of a plugin's kernels to kTailSmemMax (0 on success)
 int launch_tail_smem(const LaunchCtx& c, const PatchDev* shadow, const TailPhase* ph, int nph, const StageSeg* segs,
                      int nsegs, int smem_bytes);
-int tail_smem_attributes();
+int tail_smem_attributes(int problem);
 
 }  // namespace bsamg

@@ -70,6 +70,17 @@ typedef struct bsamg_hier bsamg_hier;
  * cpress.  Physical faces: phi reflected, n = 1, p = 0. */
 #define BSAMG_PROBLEM_GROWTH 3
 
+/* Problem plugins linked into this library.  Replaces the compile-time
+ * binding `USE Problem, ONLY: RelaxGrid2D, ...` (afasroutines.f90:333, :387,
+ * :441, :563, :677; boundary.f90:644, :717): every PROBLEM/<name> plugin
+ * has a device plugin file (bsam1.2_gb300/plugins/<name>.cu) that registers
+ * a kind and a name when the library loads.  bsamg_problem_kind returns the
+ * kind of the plugin called `name` (BSAMG_ERR_NOT_FOUND if none);
+ * bsamg_problem_info its nrvars, its minimum parameter count and whether it
+ * has a mixed-precision correction form (BSAMG_MODE_MIXED). */
+int bsamg_problem_kind(const char* name, int* kind);
+int bsamg_problem_info(int kind, int* nrvars, int* nparams, int* has_mixed);
+
 /* fields of a patch (nodeinfodef.f90:184-214) */
 #define BSAMG_FIELD_Q 0
 #define BSAMG_FIELD_QOLD 1

@@ -132,9 +132,11 @@ def _growth_pair(pkg, ctx, amr):
 @pytest.mark.parametrize("amr", [False, True])
 def test_mixed_growth_reaches_the_fp64_solution(pkg, ctx, amr):
     """The growth plugin's correction V-cycle (three variables) converges to
-    the FP64 path's discrete solution: tightly converged the iterates agree
-    to 1e-8 relative; at the configuration's tolerance to 1e-5."""
-    for tol, bound in ((1e-11, 1e-8), (1e-8, 1e-5)):
+    the FP64 path's discrete solution: tightly converged (1e-11) the iterates
+    agree to 1e-12 relative, at the configuration's tolerance (1e-8) to 5e-9
+    (measured on a GB300: 2.3e-13 and 1.1e-9 uniform, 1.6e-13 and 1.1e-10
+    with refinement)."""
+    for tol, bound in ((1e-11, 1e-12), (1e-8, 5e-9)):
         gm, gf = _growth_pair(pkg, ctx, amr)
         tab = gm.patch_table()
         fin = max(p["level"] for p in tab)
