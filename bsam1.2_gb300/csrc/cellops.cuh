@@ -26,6 +26,42 @@ __device__ __forceinline__ T ulap(const T* a, long long c, long long sy, long lo
   return a[c + 1] + a[c - 1] + a[c + sy] + a[c - sy] + a[c + sz] + a[c - sz] - T(6) * a[c];
 }
 
+// The quotients a0/b and a1/b, each bit-identical to the IEEE
+// round-to-nearest division, from one correctly rounded reciprocal
+// y = RN(1/b) (the __drcp_rn intrinsic): q = RN(a*y) is within one ulp of
+// a/b, the remainder r = a - b*q is exact in one fused multiply-add, and
+// RN(q + r*y) is the correctly rounded quotient (P. Markstein, "Computation
+// of elementary functions on the IBM RISC System/6000 processor", IBM J.
+// Res. Dev. 34(1), 1990).  The argument needs every intermediate in the
+// normal range: the fast form is taken for 1 <= b < 2^400 and
+// 2^-400 <= |a| < 2^400 (exponent tests on the integer pipe), and `/` for
+// everything else (zeros, tiny or huge values, NaN and Inf).  A zero
+// remainder returns q, which is then exact.  One reciprocal and three
+// operations per quotient replace two full divisions; bit-identity with `/`
+// is checked on the GPU over random and edge-case operands.
+__device__ __forceinline__ bool mk_fast_num(double a) {
+  unsigned e = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu;
+  return e - (1023u - 400u) <= 800u;
+}
+__device__ __forceinline__ bool mk_fast_den(double b) {
+  return ((unsigned)__double2hiint(b) >> 20) - 1023u < 400u;  // sign bit set: huge, slow form
+}
+__device__ __forceinline__ double mk_quot(double a, double b, double y) {
+  double q = __dmul_rn(a, y);
+  double r = __fma_rn(-b, q, a);
+  return (__double_as_longlong(r) << 1) ? __fma_rn(r, y, q) : q;
+}
+__device__ __forceinline__ void div2_rn(double a0, double a1, double b, double& q0, double& q1) {
+  if (mk_fast_den(b) && mk_fast_num(a0) && mk_fast_num(a1)) {
+    double y = __drcp_rn(b);
+    q0 = mk_quot(a0, b, y);
+    q1 = mk_quot(a1, b, y);
+  } else {
+    q0 = a0 / b;
+    q1 = a1 / b;
+  }
+}
+
 __device__ __forceinline__ double cube(double c) { return c * c * c; }  // CH/problem.f90:918
 __device__ __forceinline__ double sqr(double c) { return c * c; }       // CH/problem.f90:931
 

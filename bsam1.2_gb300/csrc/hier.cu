@@ -250,7 +250,8 @@ int enq_update_source(Hier& H, int finest) {
 int enq_norm(Hier& H, int level, int errortype) {
   LevelT& L = H.L(level);
   RET(after_launch(H, launch_norm_partial(H.lc(), L.d_blk[kKindInterior], L.nblk[kKindInterior], H.d_partial, 1)));
-  return after_launch(H, launch_norm_finish(H.s, H.d_partial, L.nblk[kKindInterior], H.nrvars, L.count, errortype,
+  return after_launch(H, launch_norm_finish(H.s, H.d_partial, norm_partials(L.nblk[kKindInterior]), H.nrvars, L.count,
+                                            errortype,
                                             H.d_norm, H.d_nonfinite));
 }
 

@@ -323,19 +323,24 @@ __global__ void __launch_bounds__(kBlock) k_update_source(const PatchDev* __rest
 }
 
 // ErrorAFAS partial sums (afasroutines.f90:113-233): rf = f - Op(q) on the
-// level's patches, per-block sums of rf^2 per variable.
+// level's patches, sums of rf^2 per variable over kNormGroup consecutive
+// blocks of the work list per CTA (each thread adds its cells in block
+// order, then one fixed reduction tree).
 template <class PL, int DIM>
 __global__ void __launch_bounds__(kBlock) k_norm_partial(const PatchDev* __restrict__ P, double* __restrict__ pool,
-                                                         const Blk* __restrict__ blk, ProbParams pp,
+                                                         const Blk* __restrict__ blk, int nblk, ProbParams pp,
                                                          double* __restrict__ partial, int store_rf) {
   constexpr int NV = PL::kNV;
   __shared__ double red[NV][kBlock / 32];
-  const Blk b = blk[blockIdx.x];
-  const PatchDev& p = P[b.patch];
-  int i, j, k;
   double s[NV];
   for (int v = 0; v < NV; v++) s[v] = 0.0;
-  if (interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) {
+  for (int sub = 0; sub < kNormGroup; sub++) {
+    int bi = blockIdx.x * kNormGroup + sub;
+    if (bi >= nblk) break;
+    const Blk b = blk[bi];
+    const PatchDev& p = P[b.patch];
+    int i, j, k;
+    if (!interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) continue;
     const double* q = pool + p.oq;
     long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
     long long c = gofs<DIM>(p.qn, i, j, k);
@@ -345,7 +350,7 @@ __global__ void __launch_bounds__(kBlock) k_norm_partial(const PatchDev* __restr
     for (int v = 0; v < NV; v++) {
       double e = pool[p.of + v * p.sf + fc] - r[v];
       if (store_rf) pool[p.orf + v * p.sf + fc] = e;
-      s[v] = e * e;
+      s[v] = s[v] + e * e;
     }
   }
   for (int o = 16; o > 0; o >>= 1)
@@ -449,8 +454,9 @@ struct Fp64Launchers {
   }
   static int norm_partial(const LaunchCtx& c, const Blk* blk, int nblk, double* partial, int store_rf) {
     if (nblk <= 0) return 0;
-    if (c.ndims == 2) k_norm_partial<PL, 2><<<nblk, kBlock, 0, c.s>>>(c.P, c.pool, blk, c.pp, partial, store_rf);
-    else k_norm_partial<PL, 3><<<nblk, kBlock, 0, c.s>>>(c.P, c.pool, blk, c.pp, partial, store_rf);
+    int g = norm_partials(nblk);
+    if (c.ndims == 2) k_norm_partial<PL, 2><<<g, kBlock, 0, c.s>>>(c.P, c.pool, blk, nblk, c.pp, partial, store_rf);
+    else k_norm_partial<PL, 3><<<g, kBlock, 0, c.s>>>(c.P, c.pool, blk, nblk, c.pp, partial, store_rf);
     return 1;
   }
   static int get_source(const LaunchCtx& c, const Blk* blk, int nblk) {

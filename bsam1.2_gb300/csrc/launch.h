@@ -62,7 +62,11 @@ int launch_correct_b(const LaunchCtx& c, const Blk* blk, int nblk);
 int launch_fill_down(const LaunchCtx& c, const Blk* blk, int nblk, int field);
 int launch_get_source(const LaunchCtx& c, const Blk* blk, int nblk);
 int launch_update_source(const LaunchCtx& c, const Blk* blk, int nblk);
-// per-block partial sums of rf^2 (nrvars per block) -> partial[nblk*nrvars]
+// partial sums of rf^2 (nrvars per CTA) -> partial[norm_partials(nblk)*nrvars]:
+// one CTA per kNormGroup consecutive blocks of the work list, so the FP64
+// shuffle reduction is paid once per kNormGroup * 256 cells
+constexpr int kNormGroup = 4;
+inline int norm_partials(int nblk) { return (nblk + kNormGroup - 1) / kNormGroup; }
 int launch_norm_partial(const LaunchCtx& c, const Blk* blk, int nblk,
                         double* partial, int store_rf);
 // deterministic final sum; writes out[0] = norm, out[1] = raw sum,

@@ -40,9 +40,9 @@ namespace {
 
 using namespace bsamg;
 
-constexpr int kMaxBlocks = BSAMG_NOALLOC_MAX_CELLS / kBlock;
+constexpr int kMaxBlocks = BSAMG_NOALLOC_MAX_CELLS / (kBlock * kNormGroup);
 
-// [0, 2*kMaxBlocks): per-block partial sums of rf^2 (two variables);
+// [0, 2*kMaxBlocks): per-CTA partial sums of rf^2 (two variables);
 // [2*kMaxBlocks, 2*kMaxBlocks + kNormOutLen): the final reduction's output
 // and stage sums (launch_norm_finish's `out`)
 __device__ __align__(256) double g_norm_scratch[2 * kMaxBlocks + kNormOutLen];
@@ -74,26 +74,28 @@ __device__ __forceinline__ double ulap(const double* a, long long c, long long s
 }
 
 // rf = f - Operator(q) (CH/problem.f90:393-422, :638-669) per interior cell,
-// per-block sums of rf^2 in the same order as the hierarchy's k_norm_partial
+// sums of rf^2 over kNormGroup consecutive runs of kBlock cells per CTA, in
+// the order of the hierarchy's k_norm_partial on a one-patch level (whose
+// work-list blocks are the same runs of cells)
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_norm_single(const double* __restrict__ q, const double* __restrict__ f,
                                                         int mx0, int mx1, int mx2, double c0, double c1,
                                                         double* __restrict__ partial) {
   __shared__ double red[2][kBlock / 32];
-  int t = blockIdx.x * kBlock + threadIdx.x;
-  int i = t % mx0 + 1, r = t / mx0, j, k;
-  bool in;
-  if (DIM == 2) {
-    j = r + 1;
-    k = 1;
-    in = j <= mx1;
-  } else {
-    j = r % mx1 + 1;
-    k = r / mx1 + 1;
-    in = k <= mx2;
-  }
   double s0 = 0.0, s1 = 0.0;
-  if (in) {
+  for (int sub = 0; sub < kNormGroup; sub++) {
+    long long t = ((long long)blockIdx.x * kNormGroup + sub) * kBlock + threadIdx.x;
+    int i = (int)(t % mx0) + 1, j, k;
+    long long r = t / mx0;
+    if (DIM == 2) {
+      j = (int)r + 1;
+      k = 1;
+      if (j > mx1) break;
+    } else {
+      j = (int)(r % mx1) + 1;
+      k = (int)(r / mx1) + 1;
+      if (k > mx2) break;
+    }
     long long n0 = mx0 + 2, n1 = mx1 + 2;
     long long sy = n0, sz = n0 * n1;
     long long sq = DIM == 2 ? n0 * n1 : n0 * n1 * (mx2 + 2);
@@ -106,8 +108,8 @@ __global__ void __launch_bounds__(kBlock) k_norm_single(const double* __restrict
     double r1 = a1[c] - a0[c] * a0[c] * a0[c] + c1 * ulap<DIM>(a0, c, sy, sz);
     double e0 = f[fc] - r0;
     double e1 = f[sf + fc] - r1;
-    s0 = e0 * e0;
-    s1 = e1 * e1;
+    s0 = s0 + e0 * e0;
+    s1 = s1 + e1 * e1;
   }
   for (int o = 16; o > 0; o >>= 1) {
     s0 = s0 + __shfl_down_sync(0xffffffffu, s0, o);
@@ -154,7 +156,7 @@ extern "C" int bsamg_ch_residual_norm_noalloc(const double* q, const double* f, 
   double h2 = h * h;
   double eps2 = eps * eps;
   double c0 = dt / h2, c1 = eps2 / h2;
-  int nblk = (int)((cells + kBlock - 1) / kBlock);
+  int nblk = norm_partials((int)((cells + kBlock - 1) / kBlock));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (ndims == 2)
     k_norm_single<2><<<nblk, kBlock, 0, s>>>(q, f, mx[0], mx[1], 1, c0, c1, scratch);

@@ -60,9 +60,13 @@ struct CH {
       b2 = f1[fc] - cf[1] * (q0[c + 1] + q0[c - 1] + q0[c + sy] + q0[c - sy] + q0[c + sz] + q0[c - sz]) -
            2.0 * cube(phi);
     }
-    double det = 1.0 - cf[3] * a21;
-    q0[c] = (b1 - cf[3] * b2) / det;
-    q1[c] = (b2 - a21 * b1) / det;
+    double det = 1.0 - cf[3] * a21;  // >= 1: a21 <= -tmp3 < 0
+    // the reference's two divisions by det, :365-366 (:609-610), each
+    // correctly rounded as `/` is, from one reciprocal
+    double n0, n1;
+    div2_rn(b1 - cf[3] * b2, b2 - a21 * b1, det, n0, n1);
+    q0[c] = n0;
+    q1[c] = n1;
   }
 
   // Operator2D/3D, CH/problem.f90:393-422, :638-669
