@@ -450,8 +450,11 @@ int build_tables(Hier& H) {
       for (int d = 0; d < H.ndims; d++)
         if (P.mx[d] < 4) return BSAMG_ERR_UNSUPPORTED;  // Interpolate2D/3D read cells 1..2 from each side
   }
-  // level lists in insertion (visiting) order
-  for (size_t n = 0; n < H.patches.size(); n++) H.L(H.patches[n].level).patches.push_back((int)n);
+  // level lists in the reference's visiting order: ApplyOnLevel walks a
+  // level from its youngest node to its eldest (treeops.f90:536-550), and
+  // each node added is the youngest of its level, so a level is visited in
+  // the reverse of the order the patches were added
+  for (size_t n = H.patches.size(); n-- > 0;) H.L(H.patches[n].level).patches.push_back((int)n);
   const HostPatch& R = H.patches[root];
   for (int l = 0; l <= kMaxDepth; l++)
     for (int d = 0; d < 3; d++) H.mxmax[l][d] = d < H.ndims ? (R.mx[d] << l) : 1;

@@ -535,9 +535,12 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   int next_id = prm.first_id;
   int level;
   std::vector<Sub> subs;
+  // a level's patches in visiting order (youngest first: the reverse of
+  // creation order, as ApplyOnLevel walks them), so that RefineGrid runs
+  // over the parents, and creates their children, in the reference's order
   auto level_patches = [&](int l) {
     std::vector<int> v;
-    for (size_t p = 0; p < M.g.size(); p++)
+    for (size_t p = M.g.size(); p-- > 0;)
       if (M.g[p].level == l) v.push_back((int)p);
     return v;
   };

@@ -94,8 +94,16 @@ static int nlev(const bsamo_hier* h, int level) {
   if (level < -MAXDEPTH || level > MAXDEPTH) return 0;
   return h->lev_n[level + MAXDEPTH];
 }
+/* The n-th patch of a level in the reference's visiting order:
+ * ApplyOnLevel walks a level from its youngest node to its eldest
+ * (treeops.f90:536-550; CreateChild makes each new node the youngest of
+ * its level, :349-395), i.e. the reverse of the order of creation that
+ * lev_list keeps. */
+static int lev_index(const bsamo_hier* h, int level, int n) {
+  return h->lev_list[level + MAXDEPTH][h->lev_n[level + MAXDEPTH] - 1 - n];
+}
 static OPatch* lev_patch(bsamo_hier* h, int level, int n) {
-  return &h->p[h->lev_list[level + MAXDEPTH][n]];
+  return &h->p[lev_index(h, level, n)];
 }
 static inline int imod(int a, int b) { int r = a % b; return r < 0 ? r + b : r; }
 
@@ -2121,7 +2129,7 @@ int bsamo_regrid(const bsamo_hier* old, const bsamo_regrid_params* prm, bsamo_qi
     free(tl.c);
     int first_new = h->np;
     for (int a = 0; a < np && rc == 0; a++) { /* GridAdapt -> RefineGrid, :1366-1405 */
-      int pidx = h->lev_list[level + MAXDEPTH][a];
+      int pidx = lev_index(h, level, a);
       int ng = new_sub_grids(h, &h->p[pidx], fl[a], prm, sub);
       if (ng < 0) { rc = -5; break; }
       ng = split_long(h->ndims, prm->maxside, sub, ng, 4 * MAXSUBGRIDS);
@@ -2236,7 +2244,7 @@ int bsamo_after_step_stats(const bsamo_hier* h, int finest, double integral[2], 
   long long ms = 0;
   for (int level = finest; level >= 0; level--)
     for (int a = 0; a < nlev(h, level); a++) {
-      const OPatch* p = &h->p[h->lev_list[level + MAXDEPTH][a]];
+      const OPatch* p = &h->p[lev_index(h, level, a)];
       double hh = p->dx[0], ch = hh * 2.0;
       double hd = nd == 2 ? hh * hh : hh * hh * hh;
       double chd = nd == 2 ? ch * ch : ch * ch * ch;
@@ -2309,7 +2317,7 @@ int bsamo_write_q(const bsamo_hier* h, const char* path, double time, int finest
   fprintf(f, "\n%3d\n", finest);
   for (int level = 0; level <= finest; level++)
     for (int a = 0; a < nlev(h, level); a++) {
-      const OPatch* p = &h->p[h->lev_list[level + MAXDEPTH][a]];
+      const OPatch* p = &h->p[lev_index(h, level, a)];
       double xu[3];
       int mg[3][2];
       for (int d = 0; d < 3; d++) {
@@ -2362,7 +2370,7 @@ int bsamo_write_uniform_q(const bsamo_hier* h, const char* path, double time, in
     for (int v = 0; v < nv; v++) prolong_mc(nd, 1, u + v * sz, cmx, uf + v * szf);
     for (int d = 0; d < nd; d++) dx[d] = dx[d] / 2.0;
     for (int a = 0; a < nlev(h, level); a++) { /* CopyPatchToUniformGrid */
-      const OPatch* p = &h->p[h->lev_list[level + MAXDEPTH][a]];
+      const OPatch* p = &h->p[lev_index(h, level, a)];
       int k0 = nd == 3 ? p->mglobal[2][0] - 1 : 0;
       int kh = nd == 3 ? p->mx[2] + 1 : 0;
       for (int v = 0; v < nv; v++)  /* q(0:mx+1) (:566-570) */
@@ -2573,7 +2581,7 @@ int bsamo_read_q(const bsamo_hier* root, const char* path, int first_id, double*
         for (int d = 0; d < nd; d++)
           if (mx[d] < 2 || mg[d][0] % 2 != 1 || mg[d][1] % 2 != 0 || mg[d][1] - mg[d][0] + 1 != mx[d]) goto fail;
         for (int a = 0; a < nlev(h, level - 1) && par < 0; a++) {
-          int c = h->lev_list[level - 1 + MAXDEPTH][a], in = 1;
+          int c = lev_index(h, level - 1, a), in = 1;
           const OPatch* q = &h->p[c];
           for (int d = 0; d < nd; d++)
             if ((mg[d][0] + 1) / 2 < q->mglobal[d][0] || mg[d][1] / 2 > q->mglobal[d][1]) in = 0;

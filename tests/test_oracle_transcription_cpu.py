@@ -802,7 +802,8 @@ def test_after_step_statistics_are_the_reference_statements(oracle_mod, pkg):
     fin = s.finest()
     i1 = i2 = 0.0
     for level in range(fin, -1, -1):
-        for p in [x for x in s.patches if x["level"] == level]:
+        # ApplyOnLevel: youngest node first (the reverse of creation order)
+        for p in reversed([x for x in s.patches if x["level"] == level]):
             h = p["dx"][0]
             h2, ch = h * h, h * 2.0
             ch2 = ch * ch
