@@ -32,6 +32,8 @@
 // N(q) = (phi - dt/h^2 ULap(mu), mu - phi^3 + eps^2/h^2 ULap(phi))
 // (Operator2D/3D, :393-422, :638-669).
 #include <algorithm>
+#include <cstddef>
+#include <functional>
 
 #include "box.h"
 #include "launch.h"
@@ -1055,10 +1057,10 @@ int bx_vcycle(Hier& H, int level, int minlevel, int nsmooth, bool fresh) {
   return BSAMG_OK;
 }
 
-int bx_finish(Hier& H, int finest, long long nparts, int errortype) {
+int bx_finish(Hier& H, int finest, long long nparts, int errortype, bool to_host = true) {
   int r = after_launch(H, launch_norm_finish(H.s, H.d_partial, (int)nparts, H.nrvars, H.L(finest).count, errortype,
                                              H.d_norm, H.d_nonfinite));
-  if (r) return r;
+  if (r || !to_host) return r;
   cudaError_t ce = cudaMemcpyAsync(H.h_norm, H.d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, H.s);
   if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(norm)");
   ce = cudaMemcpyAsync(H.h_nonfinite, H.d_nonfinite, sizeof(int), cudaMemcpyDeviceToHost, H.s);
@@ -1066,14 +1068,14 @@ int bx_finish(Hier& H, int finest, long long nparts, int errortype) {
   return BSAMG_OK;
 }
 
-int bx_resid(Hier& H, int finest, int errortype) {
+int bx_resid(Hier& H, int finest, int errortype, bool to_host = true) {
   BoxLev& L = B(H, finest);
   Launch sh = shape(L.n[0], L.n[1], L.n[2]);
   BX_LAUNCH(H, sh, k_bx_resid, H.fpool, L, H.b_oqlo, H.b_ofhi, H.b_oflo, H.d_partial);
-  return bx_finish(H, finest, ctas(sh), errortype);
+  return bx_finish(H, finest, ctas(sh), errortype, to_host);
 }
 
-int bx_cycle(Hier& H, int finest, int minlevel, int nsmooth, int errortype) {
+int bx_cycle(Hier& H, int finest, int minlevel, int nsmooth, int errortype, bool to_host = true) {
   int r = bx_vcycle(H, finest, minlevel, nsmooth, true);
   if (r) return r;
   BoxLev& L = B(H, finest);
@@ -1081,11 +1083,153 @@ int bx_cycle(Hier& H, int finest, int minlevel, int nsmooth, int errortype) {
     Launch sh = shape(L.n[0], L.n[1] / 2, L.n[2]);
     k_bx_track_update<3, 2><<<sh.g, sh.b, 0, H.s>>>(H.fpool, L, H.b_oqlo, H.d_partial);
     if ((r = after_launch(H, 1))) return r;
-    return bx_finish(H, finest, ctas(sh), errortype);
+    return bx_finish(H, finest, ctas(sh), errortype, to_host);
   }
   Launch sh = shape(L.n[0], L.n[1], L.n[2]);
   BX_LAUNCH(H, sh, k_bx_track_update, H.fpool, L, H.b_oqlo, H.d_partial);
-  return bx_finish(H, finest, ctas(sh), errortype);
+  return bx_finish(H, finest, ctas(sh), errortype, to_host);
+}
+
+// ---------------------------------------------------------------------------
+// The solve as one graph launch.  MultigridIterations' loop (afasroutines.f90:
+// 81-107) with this path's exit test runs on the device: a WHILE node whose
+// body is one cycle (V-cycle, tracked-residual update, norm) and a decision
+// kernel, followed by an IF node that evaluates the true residual when the
+// decision asks for it.  The host enqueues the loop and reads the control
+// block once, instead of waiting for every cycle's norm.
+
+constexpr int kLoopMaxCycles = 64;
+struct BoxCtl {
+  double tol, r_sync;
+  int maxv, it, conv, status, nconfirm, pad;
+  double res[kLoopMaxCycles];
+};
+constexpr int kCtlSlotOffset = 16;  // doubles into the hierarchy's pinned slot
+static_assert(sizeof(BoxCtl) <= (128 - kCtlSlotOffset) * sizeof(double), "pinned slot too small");
+
+// after a cycle: the tracked norm decides whether to confirm on the true
+// residual (the host loop's test: below the tolerance, 1e5 below the last
+// true residual, or the last cycle)
+__global__ void k_bx_decide_cycle(BoxCtl* c, const double* __restrict__ norm, const int* __restrict__ nonfinite,
+                                  cudaGraphConditionalHandle hw, cudaGraphConditionalHandle hi) {
+  int it = ++c->it;
+  if (c->status || nonfinite[0]) {
+    c->status = 1;
+    cudaGraphSetConditional(hi, 0);
+    cudaGraphSetConditional(hw, 0);
+    return;
+  }
+  double tracked = norm[0];
+  bool confirm = tracked < c->tol || tracked < 1e-5 * c->r_sync || it >= c->maxv;
+  cudaGraphSetConditional(hi, confirm ? 1u : 0u);
+  if (!confirm) c->res[it - 1] = tracked;
+}
+
+// after a true residual: converged or the last cycle ends the loop
+__global__ void k_bx_decide_true(BoxCtl* c, const double* __restrict__ norm, const int* __restrict__ nonfinite,
+                                 cudaGraphConditionalHandle hw) {
+  int it = c->it;
+  c->nconfirm++;
+  if (nonfinite[0]) {
+    c->status = 1;
+    cudaGraphSetConditional(hw, 0);
+    return;
+  }
+  double res = norm[0];
+  c->r_sync = res;
+  c->res[it - 1] = res;
+  if (res < c->tol) {
+    c->conv = 1;
+    cudaGraphSetConditional(hw, 0);
+  } else if (it >= c->maxv) {
+    cudaGraphSetConditional(hw, 0);
+  }
+}
+
+// capture what body() enqueues into graph g (a conditional node's body)
+int capture_into(Hier& H, cudaGraph_t g, const std::function<int()>& body, long long* nlaunch) {
+  cudaError_t e = cudaStreamBeginCaptureToGraph(H.s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCaptureToGraph");
+  H.capturing = true;
+  H.capture_launches = 0;
+  int r = body();
+  H.capturing = false;
+  *nlaunch = H.capture_launches;
+  cudaGraph_t out = nullptr;
+  e = cudaStreamEndCapture(H.s, &out);
+  if (r) return r;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  return BSAMG_OK;
+}
+
+int box_loop_graph(Hier& H, int finest, int minlevel, int nsmooth, int errortype) {
+  auto key = std::make_tuple(finest, minlevel, nsmooth, errortype);
+  if (H.box_loop && H.box_loop_key == key) return BSAMG_OK;
+  if (H.box_loop) cudaGraphExecDestroy(H.box_loop);
+  H.box_loop = nullptr;
+  if (!H.box_ctl) {
+    cudaError_t e = dev_alloc(H, &H.box_ctl, sizeof(BoxCtl));
+    if (e != cudaSuccess) return cuda_fail(e, "device allocation (loop control)");
+  }
+  BoxCtl* ctl = static_cast<BoxCtl*>(H.box_ctl);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphCreate");
+  int r = BSAMG_OK;
+  cudaGraphConditionalHandle hw, hi;
+  cudaGraphNodeParams wp = {}, ip = {};
+  cudaGraphNode_t wn = nullptr;
+  do {
+    if ((e = cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) break;
+    if ((e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault)) != cudaSuccess) break;
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = hw;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    if ((e = cudaGraphAddNode(&wn, g, nullptr, nullptr, 0, &wp)) != cudaSuccess) break;
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    // the cycle, its decision, then the IF node on what was captured
+    r = capture_into(H, body, [&]() -> int {
+      int rr = bx_cycle(H, finest, minlevel, nsmooth, errortype, false);
+      if (rr) return rr;
+      k_bx_decide_cycle<<<1, 1, 0, H.s>>>(ctl, H.d_norm, H.d_nonfinite, hw, hi);
+      if ((rr = after_launch(H, 1))) return rr;
+      cudaStreamCaptureStatus st;
+      cudaGraph_t cg = nullptr;
+      const cudaGraphNode_t* deps = nullptr;
+      size_t nd = 0;
+      cudaError_t ce = cudaStreamGetCaptureInfo(H.s, &st, nullptr, &cg, &deps, nullptr, &nd);
+      if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamGetCaptureInfo");
+      ip.type = cudaGraphNodeTypeConditional;
+      ip.conditional.handle = hi;
+      ip.conditional.type = cudaGraphCondTypeIf;
+      ip.conditional.size = 1;
+      cudaGraphNode_t in = nullptr;
+      ce = cudaGraphAddNode(&in, cg, deps, nullptr, nd, &ip);
+      if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphAddNode(if)");
+      ce = cudaStreamUpdateCaptureDependencies(H.s, &in, nullptr, 1, cudaStreamSetCaptureDependencies);
+      if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamUpdateCaptureDependencies");
+      return BSAMG_OK;
+    }, &H.box_loop_n1);
+    if (r) break;
+    r = capture_into(H, ip.conditional.phGraph_out[0], [&]() -> int {
+      int rr = bx_resid(H, finest, errortype, false);
+      if (rr) return rr;
+      k_bx_decide_true<<<1, 1, 0, H.s>>>(ctl, H.d_norm, H.d_nonfinite, hw);
+      return after_launch(H, 1);
+    }, &H.box_loop_n2);
+    if (r) break;
+    e = cudaGraphInstantiate(&H.box_loop, g, 0);
+  } while (0);
+  cudaGraphDestroy(g);
+  if (r) return r;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    H.box_loop = nullptr;
+    return cuda_fail(e, "conditional solve graph");
+  }
+  H.box_loop_key = key;
+  return BSAMG_OK;
 }
 
 }  // namespace
@@ -1169,17 +1313,62 @@ int box_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycle
   Launch sh = shape(L.hh, L.n[1], L.n[2]);
   bool warm = H.box_g_valid;  // g is the residual at this q: update it for the new f
   H.box_g_valid = false;
+  // the whole solve as one graph launch when the loop fits its control block
+  bool loop = maxvcycles >= 1 && maxvcycles <= kLoopMaxCycles && !H.box_loop_off;
+  if (loop) {
+    int rl = box_loop_graph(H, finest, minlevel, nsmooth, errortype);
+    if (rl == BSAMG_ERR_CUDA && !H.box_loop) {
+      H.box_loop_off = true;  // conditional graphs unavailable: the host loop below
+      loop = false;
+    } else if (rl) {
+      return rl;
+    }
+  }
   int r;
   if (warm) {
     BX_LAUNCH(H, sh, k_bx_split_warm, H.pool, P.oq, P.oqold, P.sq, P.qn[0], P.qn[1], H.fpool, L, H.b_oqlo, H.b_ofhi,
               H.b_oflo, H.d_partial);
-    r = bx_finish(H, finest, ctas(sh), errortype);
+    r = bx_finish(H, finest, ctas(sh), errortype, !loop);
   } else {
     BX_LAUNCH(H, sh, k_bx_split, H.pool, P.oq, P.oqold, P.sq, P.qn[0], P.qn[1], H.fpool, L, H.b_oqlo, H.b_ofhi,
               H.b_oflo);
-    r = bx_resid(H, finest, errortype);
+    r = bx_resid(H, finest, errortype, !loop);
   }
   if (r) return r;
+  bool conv = false;
+  int it = 0;
+  if (loop) {
+    // control block: the tolerance and cycle limit from the host, the
+    // starting residual and its finiteness from the device
+    BoxCtl* hc = reinterpret_cast<BoxCtl*>(H.h_norm + kCtlSlotOffset);
+    BoxCtl* dc = static_cast<BoxCtl*>(H.box_ctl);
+    hc->tol = tol;
+    hc->maxv = maxvcycles;
+    hc->it = hc->conv = hc->status = hc->nconfirm = 0;
+    cudaError_t ce = cudaMemcpyAsync(dc, hc, offsetof(BoxCtl, res), cudaMemcpyHostToDevice, H.s);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&dc->r_sync, H.d_norm, sizeof(double), cudaMemcpyDeviceToDevice, H.s);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&dc->status, H.d_nonfinite, sizeof(int), cudaMemcpyDeviceToDevice, H.s);
+    if (ce == cudaSuccess) ce = cudaGraphLaunch(H.box_loop, H.s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "solve graph");
+    // leave the state as the FP64 path leaves it (see below), then read
+    // the control block once
+    BX_LAUNCH(H, sh, k_bx_merge, H.pool, P.oq, P.sq, P.qn[0], P.qn[1], H.fpool, L, H.b_oqlo);
+    if ((r = enq_set_ghost(H, finest, 0))) return r;
+    if ((r = enq_fill_down(H, 2, finest, minlevel))) return r;
+    ce = cudaMemcpyAsync(hc, dc, sizeof(BoxCtl), cudaMemcpyDeviceToHost, H.s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(loop control)");
+    if (int rw = stream_wait(H)) return rw;
+    H.launches += hc->it * H.box_loop_n1 + hc->nconfirm * H.box_loop_n2;
+    if (hc->status) return BSAMG_ERR_NONFINITE;
+    it = hc->it;
+    conv = hc->conv != 0;
+    if (residuals)
+      for (int n = 0; n < it; n++) residuals[n] = hc->res[n];
+    if (ncycles) *ncycles = conv ? it : maxvcycles;
+    H.box_g_valid = true;
+    if (!conv && strict) return BSAMG_ERR_NOT_CONVERGED;
+    return BSAMG_OK;
+  }
   if (int rw = stream_wait(H)) return rw;
   if (*H.h_nonfinite) return BSAMG_ERR_NONFINITE;
   double r_sync = H.h_norm[0];
@@ -1188,8 +1377,6 @@ int box_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycle
   if ((r = capture_graph(H, key(21), [&] { return bx_cycle(H, finest, minlevel, nsmooth, errortype); }, &gc)))
     return r;
   if ((r = capture_graph(H, key(22), [&] { return bx_resid(H, finest, errortype); }, &gv))) return r;
-  bool conv = false;
-  int it;
   for (it = 1; it <= maxvcycles; it++) {
     if ((r = replay(H, gc))) return r;
     if (*H.h_nonfinite) return BSAMG_ERR_NONFINITE;

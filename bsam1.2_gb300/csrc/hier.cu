@@ -356,6 +356,17 @@ int stream_wait(Hier& H) {
   return BSAMG_OK;
 }
 
+// every captured graph of the hierarchy, the box path's solve graph
+// included (after a change of what the kernels take as arguments); the
+// stream is idle
+void drop_graphs(Hier& H) {
+  for (auto& kv : H.graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  H.graphs.clear();
+  if (H.box_loop) cudaGraphExecDestroy(H.box_loop);
+  H.box_loop = nullptr;
+}
+
 int replay(Hier& H, Hier::GraphRec* g) {
   CK(cudaGraphLaunch(g->exec, H.s));
   H.launches += g->nlaunch;
@@ -649,7 +660,7 @@ int upload_ghost(Hier& H, GhostProg& g) {
 // Pinned host words for the norm read-back come from a per-context pool, so
 // hierarchies never call cudaMallocHost/cudaFreeHost (the latter
 // synchronises the device) while other hierarchies run.
-constexpr int kPinnedSlots = 1024, kSlotDoubles = 16;
+constexpr int kPinnedSlots = 1024, kSlotDoubles = 128;  // [0, 16): norms; [16, 128): the box loop's control block
 
 int pinned_slot_take(Hier& H) {
   bsamg_ctx* c = H.ctx;
@@ -1236,9 +1247,7 @@ int bsamg_set_params(bsamg_hier* h, const double* params, int nparams) {
   if (!keep_graphs) {
     e = cudaStreamSynchronize(h->s);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
-    for (auto& kv : h->graphs)
-      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
-    h->graphs.clear();
+    drop_graphs(*h);
   }
   return BSAMG_OK;
 }
@@ -1262,9 +1271,7 @@ int bsamg_set_box_sweep(bsamg_hier* h, int kind) {
   if (h->committed) {  // captured graphs hold the other sweep kernel
     cudaError_t e = cudaStreamSynchronize(h->s);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
-    for (auto& kv : h->graphs)
-      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
-    h->graphs.clear();
+    drop_graphs(*h);
   }
   h->box_sweep = kind;
   return BSAMG_OK;
@@ -1277,9 +1284,7 @@ int bsamg_set_tail_cells(bsamg_hier* h, long long cells) {
   cudaError_t e = cudaStreamSynchronize(h->s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
   // captured graphs embed the previous tail program
-  for (auto& kv : h->graphs)
-    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
-  h->graphs.clear();
+  drop_graphs(*h);
   set_tail(*h, cells);
   return BSAMG_OK;
 }

@@ -110,6 +110,13 @@ struct Hier {
   BoxLev blev[kNLev] = {};
   long long b_oqlo = 0, b_ofhi = 0, b_oflo = 0;  // float offsets (qhi is blev[finest].opb)
   size_t b_partials = 0;                         // partial-sum slots the box kernels need
+  // the box path's solve as one graph launch: a device-side loop of
+  // V-cycles with the exit test on the device (box.cu box_loop_graph)
+  cudaGraphExec_t box_loop = nullptr;
+  std::tuple<int, int, int, int> box_loop_key{};
+  long long box_loop_n1 = 0, box_loop_n2 = 0;  // launches per cycle, per confirming residual
+  bool box_loop_off = false;                   // the loop graph could not be built: host loop
+  void* box_ctl = nullptr;                     // device control block of the loop
   size_t bytes = 0;
   size_t reserved = 0;  // bytes counted against the context budget
 
@@ -191,6 +198,7 @@ using GraphKey = std::tuple<int, int, int, int, int>;
 // capture what `body` enqueues as a CUDA graph (once per key) and replay it
 int capture_graph(Hier& H, const GraphKey& key, const std::function<int()>& body, Hier::GraphRec** out);
 int replay(Hier& H, Hier::GraphRec* g);
+void drop_graphs(Hier& H);
 // wait for the hierarchy's stream (spinning, or sleeping with blocking waits)
 int stream_wait(Hier& H);
 // release the device arrays of a tail program (stream-ordered)

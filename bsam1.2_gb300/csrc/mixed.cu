@@ -410,6 +410,10 @@ int mixed_alloc(Hier& H) {
 void mixed_free(Hier& H) {
   if (H.fpool) cudaFreeAsync(H.fpool, H.s);
   H.fpool = nullptr;
+  if (H.box_loop) cudaGraphExecDestroy(H.box_loop);
+  H.box_loop = nullptr;
+  if (H.box_ctl) cudaFreeAsync(H.box_ctl, H.s);
+  H.box_ctl = nullptr;
   if (H.mx_prep_coarse) cudaFreeAsync(H.mx_prep_coarse, H.s);
   H.mx_prep_coarse = nullptr;
   for (auto& kv : H.mx_tail_progs) free_tail(H, kv.second);

@@ -1,6 +1,7 @@
 /*
  * CPU oracle: plain-C restatement of the BSAM 1.2 FAS V-cycle.
- * TEST INFRASTRUCTURE ONLY -- see bsam_oracle.h for scope and parity status.
+ * TEST INFRASTRUCTURE ONLY -- see bsam_oracle.h for scope and parity status
+ * (pinned to the reference's own outputs, run by oracle/fortran_exec.py).
  *
  * Every routine cites the reference routine it restates (file:line, paths
  * within the reference project).  Evaluation order of each floating-point

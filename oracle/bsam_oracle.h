@@ -8,10 +8,20 @@
  * problem.f90).  Only the tests, the smoke check and the CPU-baseline leg of
  * the benchmark may load it; the product library never links it.
  *
- * Parity status: UNPINNED by the reference itself.  The reference ships no
+ * Parity status: pinned to the reference itself.  The reference ships no
  * tests, golden vectors or fixtures, and no Fortran compiler exists on the
- * build or GPU machines, so the reference cannot be run.  The oracle is pinned
- * instead by math-derived known-answer tests (tests/test_oracle_kat.py).
+ * build or GPU machines; its unmodified source is run instead by a
+ * Fortran-subset interpreter (oracle/fortran_exec.py), whose outputs on 2D
+ * and 3D CH (periodic, Neumann, Dirichlet, two ghost layers), 2D BioGrowth
+ * and 2D/3D CH on meshes regridded before every step are committed as
+ * fixtures (tests/golden/ref_*.npz, tests/golden/make_reference_golden.py).
+ * The oracle reproduces them bit for bit: every node's q after every time
+ * step, the residual of every V-cycle, the mesh and the order in which
+ * ApplyOnLevel visits it (tests/test_reference_golden_cpu.py).  Math-derived
+ * known-answer tests (tests/test_oracle_kat.py) and a numpy transcription of
+ * the reference's statements (tests/test_oracle_transcription_cpu.py) check
+ * it as well.  The three-variable growth plugin has no reference counterpart
+ * and is pinned by exact solutions only.
  *
  * Arithmetic follows the reference's evaluation order term by term and is
  * compiled with -ffp-contract=off (no FMA contraction), so the CUDA plain-FP64

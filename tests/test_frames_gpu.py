@@ -119,8 +119,16 @@ def test_restart_matches_oracle(pkg, ctx, oracle_mod, tmp_path):
     o2, to = om.read_q(oroot, path, first_id=700)
     assert tg == to == 3e-3
     same(g2, o2)
+    # a frame written after ReadQ lists each level in the reverse order (ReadQ
+    # creates the nodes in file order, WriteQ visits youngest first), as
+    # the oracle's does; written once more after reading that, it is the
+    # original again
     g2.write_q(tmp_path / "again.dat", tg, fin)
-    assert (tmp_path / "again.dat").read_bytes() == path.read_bytes()
+    o2.write_q(tmp_path / "again_oracle.dat", tg, fin)
+    assert (tmp_path / "again.dat").read_bytes() == (tmp_path / "again_oracle.dat").read_bytes()
+    g4, _ = groot.read_q(tmp_path / "again.dat", first_id=800)
+    g4.write_q(tmp_path / "third.dat", tg, fin)
+    assert (tmp_path / "third.dat").read_bytes() == path.read_bytes()
     kw = dict(tagging="gradient", initial=False, maxside=64, qtolerance=0.25, first_id=4000)
     g3, o3 = g2.regrid(pkg.regrid_params(3, **kw)), om.regrid(o2, om.regrid_params(3, **kw))
     tab = same(g3, o3)

@@ -198,8 +198,16 @@ def test_regrid_frames_and_restart_with_two_ghost_layers(pkg, ctx, oracle_mod, t
     o2, to = om.read_q(oroot, path, first_id=700)
     assert tg == to == 0.5
     _same(g2, o2)
+    # a frame written after ReadQ lists each level in the reverse order (ReadQ
+    # creates the nodes in file order, WriteQ visits youngest first), as
+    # the oracle's does; written once more after reading that, it is the
+    # original again
     g2.write_q(tmp_path / "again.dat", tg, fin)
-    assert (tmp_path / "again.dat").read_bytes() == path.read_bytes()
+    o2.write_q(tmp_path / "again_oracle.dat", tg, fin)
+    assert (tmp_path / "again.dat").read_bytes() == (tmp_path / "again_oracle.dat").read_bytes()
+    g4, _ = groot.read_q(tmp_path / "again.dat", first_id=800)
+    g4.write_q(tmp_path / "third.dat", tg, fin)
+    assert (tmp_path / "third.dat").read_bytes() == path.read_bytes()
 
 
 def test_mixed_path_with_two_ghost_layers(pkg, ctx, oracle_mod):
