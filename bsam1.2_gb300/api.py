@@ -133,6 +133,11 @@ def lib():
         "bsamg_launch_count": ([P, ctypes.POINTER(ctypes.c_longlong)], I),
         "bsamg_set_tail_cells": ([P, ctypes.c_longlong], I),
         "bsamg_set_box_sweep": ([P, I], I),
+        "bsamg_set_solve": ([P, I, I, I, ctypes.c_longlong], I),
+        "bsamg_get_solve": ([P, IP, IP, IP, ctypes.POINTER(ctypes.c_longlong)], I),
+        "bsamg_solve_trace": ([P, I], I),
+        "bsamg_solve_info": ([P, ctypes.POINTER(ctypes.c_longlong), I], I),
+        "bsamg_solve_trace_read": ([P, I, IP, IP, ctypes.POINTER(ctypes.c_longlong), IP], I),
         "bsamg_graph_stats": ([P, IP, IP], I),
         "bsamg_set_params": ([P, DP, I], I),
         "bsamg_hier_reset": ([P], I),
@@ -440,6 +445,41 @@ class Hierarchy:
         """Largest cumulative coarse-level size the mixed V-cycle runs inside
         one thread block (bsamg_set_tail_cells; 0 disables)."""
         _ck(lib().bsamg_set_tail_cells(self.h, cells), "bsamg_set_tail_cells")
+
+    def set_solve(self, mode=1, ctas=16, threads=512, solo_cells=2048):
+        """How a mixed-mode solve of an adaptive hierarchy runs
+        (bsamg_set_solve): mode 1 as one launch of a cluster of `ctas` CTAs
+        of `threads` threads, the levels holding at most `solo_cells` cells
+        together run by one CTA; mode 0 as separate launches from captured
+        graphs.  Both give the same iterates."""
+        _ck(lib().bsamg_set_solve(self.h, int(mode), int(ctas), int(threads), int(solo_cells)), "bsamg_set_solve")
+
+    def get_solve(self):
+        """(mode, ctas, threads, solo_cells) of bsamg_set_solve."""
+        m, c, t, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        _ck(lib().bsamg_get_solve(self.h, ctypes.byref(m), ctypes.byref(c), ctypes.byref(t), ctypes.byref(s)),
+            "bsamg_get_solve")
+        return m.value, c.value, t.value, s.value
+
+    def solve_info(self):
+        """dict of the last one-launch solve program (bsamg_solve_info)."""
+        v = (ctypes.c_longlong * 8)()
+        _ck(lib().bsamg_solve_info(self.h, v, 8), "bsamg_solve_info")
+        keys = ("phases", "body", "dsm_levels", "data_bytes", "image_bytes", "ctas", "threads", "too_large")
+        return dict(zip(keys, list(v)))
+
+    def solve_trace(self, enable=True):
+        """Record per-phase clocks of the next one-launch solves (bsamg_solve_trace)."""
+        _ck(lib().bsamg_solve_trace(self.h, int(bool(enable))), "bsamg_solve_trace")
+
+    def solve_trace_read(self):
+        """[(op, n, cycles)] per phase of the last traced solve (bsamg_solve_trace_read)."""
+        cnt = ctypes.c_int()
+        _ck(lib().bsamg_solve_trace_read(self.h, 0, None, None, None, ctypes.byref(cnt)), "bsamg_solve_trace_read")
+        k = cnt.value
+        op, n, cy = (ctypes.c_int * max(k, 1))(), (ctypes.c_int * max(k, 1))(), (ctypes.c_longlong * max(k, 1))()
+        _ck(lib().bsamg_solve_trace_read(self.h, k, op, n, cy, ctypes.byref(cnt)), "bsamg_solve_trace_read")
+        return [(op[x], n[x], cy[x]) for x in range(k)]
 
     def graph_stats(self):
         """(graphs instantiated, graphs inherited and updated in place)."""

@@ -616,6 +616,7 @@ int upload_blocks(Hier& H, LevelT& L, int kind) {
   // a copy from pageable memory returns once the source has been staged, so
   // v may be freed on return
   CK(cudaMemcpyAsync(L.d_blk[kind], v.data(), sizeof(Blk) * v.size(), cudaMemcpyHostToDevice, H.s));
+  L.h_blk[kind] = std::move(v);
   return BSAMG_OK;
 }
 
@@ -1239,6 +1240,8 @@ int bsamg_set_params(bsamg_hier* h, const double* params, int nparams) {
                           h->s);
       if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(tail patch table)");
     }
+  // the one-launch solve's program image holds a copy of the patch table
+  solve_invalidate(*h);
   // Kernels read the coefficients from the patch table, except those of the
   // periodic-box path and the parameters of plugins whose kernels take them
   // as arguments (captured in graphs): those graphs are captured again.
@@ -1286,6 +1289,61 @@ int bsamg_set_tail_cells(bsamg_hier* h, long long cells) {
   // captured graphs embed the previous tail program
   drop_graphs(*h);
   set_tail(*h, cells);
+  return BSAMG_OK;
+}
+
+int bsamg_set_solve(bsamg_hier* h, int mode, int ctas, int threads, long long solo_cells) {
+  if (!h || (mode != 0 && mode != 1) || ctas < 1 || ctas > 16 || solo_cells < 0) return BSAMG_ERR_ARG;
+  if (threads != 256 && threads != 512 && threads != 1024) return BSAMG_ERR_ARG;
+  int r = set_device(*h);
+  if (r) return r;
+  if (mode == 1 && h->committed && h->fpool && !solve_shape_runs(*h, SolveShape{ctas, threads}))
+    return BSAMG_ERR_UNSUPPORTED;
+  h->solve_mode = mode;
+  h->solve_shape = SolveShape{ctas, threads};
+  h->solve_solo_cells = solo_cells;
+  h->solve_tuned = true;
+  return BSAMG_OK;
+}
+
+int bsamg_get_solve(const bsamg_hier* h, int* mode, int* ctas, int* threads, long long* solo_cells) {
+  if (!h) return BSAMG_ERR_ARG;
+  if (mode) *mode = h->solve_mode;
+  if (ctas) *ctas = h->solve_shape.ctas;
+  if (threads) *threads = h->solve_shape.threads;
+  if (solo_cells) *solo_cells = h->solve_solo_cells;
+  return BSAMG_OK;
+}
+
+int bsamg_solve_info(const bsamg_hier* h, long long* info, int n) {
+  if (!h || !info || n < 0) return BSAMG_ERR_ARG;
+  long long v[8] = {h->solve_nph, h->solve_body, h->solve_dsm_levels, h->solve_im.data, h->solve_im.bytes,
+                    h->solve_shape.ctas, h->solve_shape.threads, h->solve_nofit ? 1 : 0};
+  for (int x = 0; x < n && x < 8; x++) info[x] = v[x];
+  return BSAMG_OK;
+}
+
+int bsamg_solve_trace(bsamg_hier* h, int enable) {
+  if (!h) return BSAMG_ERR_ARG;
+  h->solve_trace_on = enable != 0;
+  return BSAMG_OK;
+}
+
+int bsamg_solve_trace_read(const bsamg_hier* h, int cap, int* op, int* n, long long* cycles, int* count) {
+  if (!h || !count || cap < 0) return BSAMG_ERR_ARG;
+  int np = (int)h->solve_trace_ops.size();
+  *count = np;
+  if (h->solve_trace_h.size() != (size_t)np + 1) return BSAMG_OK;
+  long long prev = h->solve_trace_h[np];
+  for (int x = 0; x < np && x < cap; x++) {
+    if (op) op[x] = h->solve_trace_ops[x];
+    if (n) n[x] = h->solve_trace_n[x];
+    // a solo block's clock is taken after its last phase: the block's time
+    // goes to that phase, the others read 0
+    long long t = h->solve_trace_h[x];
+    if (cycles) cycles[x] = t ? t - prev : 0;
+    if (t) prev = t;
+  }
   return BSAMG_OK;
 }
 

@@ -40,6 +40,7 @@ struct LevelT {
   std::vector<int> patches;  // visiting order
   Blk* d_blk[kNKind] = {};
   int nblk[kNKind] = {};
+  std::vector<Blk> h_blk[kNKind];  // host copies (program images of the one-launch solve)
   GhostProg gp[3];           // ipass 0, 1, 2
   double count = 0.0;        // nrvars * cells (ErrorAFAS denominator)
 };
@@ -77,6 +78,7 @@ struct Hier {
   Blk* mx_norm_blk[kNLev] = {};               // padded interior lists (mixed norm)
   Blk* mx_prep_coarse = nullptr;              // interior lists of all levels < 0
   int mx_prep_coarse_n = 0;
+  std::vector<Blk> h_mx_norm_blk[kNLev], h_mx_prep_coarse;  // host copies of the two
   // coarse tail of the V-cycle (levels <= tail_level run in one CTA); the
   // recorded programs per (minlevel, nsmooth): device phases and their count
   int tail_level = -kMaxDepth - 2;
@@ -98,6 +100,32 @@ struct Hier {
   };
   std::map<TailKey, TailProg> mx_tail_progs, fp_tail_progs;
   void* rec = nullptr;  // std::vector<TailPhase> being recorded
+  // while a solve program is recorded: the V-cycle level from which CTA 0
+  // runs the coarse end alone (a kTSolo marker precedes those phases)
+  int rec_solo = -kMaxDepth - 2;
+  // the mixed solve of a hierarchy with refinement levels as one cluster
+  // launch (kern_solve.cuh): mode 1 uses it where it applies, 0 keeps the
+  // per-launch graphs; its launch shape and the cells of the coarse end run
+  // by one CTA; the recorded program of (finest, minlevel, nsmooth, solo
+  // level) and the device control block (SolveCtl + residuals)
+  int solve_mode = 1;
+  SolveShape solve_shape{16, 512};
+  long long solve_solo_cells = 2048;
+  bool solve_tuned = false;  // the shape came from the autotuner (or the caller)
+  void* solve_img = nullptr;  // program image (SolveImage layout)
+  SolveImage solve_im{};
+  bool solve_nofit = false;   // the program of solve_key is too large to stage
+  int solve_nph = 0, solve_body = 0, solve_nb = 0;
+  std::tuple<int, int, int, int, int> solve_key{kMaxDepth + 1, 0, 0, 0, 0};
+  GhostOp* solve_ops = nullptr;  // the program's FP32 ghost operations, each stage in owner order
+  int solve_dsm_levels = 0;      // levels whose FP32 arrays the program keeps in distributed shared memory
+  void* solve_ctl = nullptr;
+  int solve_ctl_cap = 0;  // residual slots of solve_ctl
+  bool solve_trace_on = false;
+  long long* solve_trace = nullptr;  // device, solve_trace_cap + 1 clocks
+  int solve_trace_cap = 0;
+  std::vector<long long> solve_trace_h;  // the last traced solve's clocks
+  std::vector<int> solve_trace_ops, solve_trace_n;  // op and n of each phase
   // periodic-box mixed path (box.cu): every level one periodic box with even
   // extents covering its parent; FP64 iterate held as float pairs
   bool box = false;

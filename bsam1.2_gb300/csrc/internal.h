@@ -28,6 +28,11 @@ struct PatchDev {
   int parent;  // index into the patch table, -1 if none
   int level;
   int gs;      // mbc - 1: the ghosted arrays start at Fortran index -gs
+  // Read only by the one-launch solve, in the copy of the table in its
+  // program image: the CTA of the cluster that works on this patch's FP32
+  // arrays, and whether those arrays live in that CTA's shared memory (then
+  // eq, ecq, eg and ephi count from the start of its shared-memory data).
+  int owner, dsm;
   // element offsets into the pool; for the ghosted arrays (q, qold, qc) the
   // offset of Fortran cell (0,0,0) of variable 1, so that a cell's offset
   // is the same expression whatever mbc is (negative indices reach the

@@ -14,6 +14,27 @@
 namespace bsamg {
 namespace mx {
 
+// The dynamic shared memory of a one-launch solve (kern_solve.cuh): its
+// FP32 data area first, then the staged program image.
+extern __shared__ __align__(16) unsigned char solve_smem[];
+
+// The base of patch p's FP32 arrays: the FP32 pool, or -- inside a
+// one-launch solve (CL), for a patch whose arrays live in distributed
+// shared memory -- the data area of the CTA of the cluster that owns it.
+template <bool CL>
+__device__ __forceinline__ float* fbase(float* fpool, const PatchDev& p) {
+  if constexpr (CL) {
+    if (p.dsm) {
+      unsigned me;
+      asm("mov.u32 %0, %%cluster_ctarank;" : "=r"(me));
+      // this CTA's own data through the local window, another's through the cluster's
+      if ((unsigned)p.owner == me) return reinterpret_cast<float*>(solve_smem);
+      return static_cast<float*>(__cluster_map_shared_rank(static_cast<void*>(solve_smem), p.owner));
+    }
+  }
+  return fpool;
+}
+
 constexpr float fA1 = -01.0f / 05.0f, fA2 = 02.0f / 03.0f, fA3 = 08.0f / 15.0f;
 constexpr float fB1 = 05.0f / 32.0f, fB2 = 15.0f / 16.0f, fB3 = -03.0f / 32.0f;
 constexpr float fC1 = 09.0f / 16.0f, fC2 = 03.0f / 16.0f, fC3 = 03.0f / 16.0f, fC4 = 01.0f / 16.0f;
@@ -28,20 +49,22 @@ __device__ __forceinline__ float restrict_at32(F at, int ci, int cj, int ck) {
 }
 
 // RestrictSolution on e: ec(1:cmx) = R(e); parent e(mb) = ec
-template <int DIM>
+template <int DIM, bool CL = false>
 __device__ __forceinline__ void u_restrict(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
                                            int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
   int ci, cj, ck;
   if (!interior_cell<DIM>(p.cmx, b.start + tid, ci, cj, ck)) return;
   const PatchDev& par = P[p.parent];
+  float* fp = fbase<CL>(fpool, p);
+  float* fq = fbase<CL>(fpool, par);
   for (int v = 0; v < nrvars; v++) {
-    const float* e = fpool + p.eq + v * p.sq;
+    const float* e = fp + p.eq + v * p.sq;
     auto at = [&](int i, int j, int k) { return e[gofs<DIM>(p.qn, i, j, k)]; };
     float val = restrict_at32<DIM>(at, ci, cj, ck);
-    fpool[p.ecq + v * p.sc + gofs<DIM>(p.cn, ci, cj, ck)] = val;
-    fpool[par.eq + v * par.sq +
-          gofs<DIM>(par.qn, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 0)] = val;
+    fp[p.ecq + v * p.sc + gofs<DIM>(p.cn, ci, cj, ck)] = val;
+    fq[par.eq + v * par.sq + gofs<DIM>(par.qn, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 0)] =
+        val;
   }
 }
 
@@ -49,7 +72,7 @@ __device__ __forceinline__ void u_restrict(const PatchDev* __restrict__ P, float
 // GetCoarseGhostPoints on e (ring of ec <- parent e) when corr == 0;
 // CorrectFine step 1 (ec = parent e - ec over the whole ghosted ec) when
 // corr == 1.
-template <int DIM>
+template <int DIM, bool CL = false>
 __device__ __forceinline__ void u_coarse_ring(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
                                               int tid, int nrvars, int corr) {
   const PatchDev& p = P[b.patch];
@@ -67,9 +90,11 @@ __device__ __forceinline__ void u_coarse_ring(const PatchDev* __restrict__ P, fl
   int pi = p.mb[0] - 1 + i, pj = p.mb[1] - 1 + j, pk = DIM == 3 ? p.mb[2] - 1 + k : 0;
   long long src = gofs<DIM>(par.qn, pi, pj, pk);
   long long dst = gofs<DIM>(p.cn, i, j, k);
+  float* fp = fbase<CL>(fpool, p);
+  const float* fq = fbase<CL>(fpool, par);
   for (int v = 0; v < nrvars; v++) {
-    float* ec = fpool + p.ecq + v * p.sc;
-    float pv = fpool[par.eq + v * par.sq + src];
+    float* ec = fp + p.ecq + v * p.sc;
+    float pv = fq[par.eq + v * par.sq + src];
     ec[dst] = corr ? pv - ec[dst] : pv;
   }
 }
@@ -80,7 +105,7 @@ __device__ __forceinline__ void u_coarse_ring(const PatchDev* __restrict__ P, fl
 // cells 2ci..2ci+1 (x) etc. from the 2x2(x2) coarse values they share, with
 // the same per-direction (3,1)/4 weights as BiLin/TriLinProlongationP1
 // (gridutilities.f90:156-195, :510-566).
-template <int DIM>
+template <int DIM, bool CL = false>
 __device__ __forceinline__ void u_prolong(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
                                           int tid, int nrvars) {
   const PatchDev& p = P[b.patch];
@@ -97,9 +122,10 @@ __device__ __forceinline__ void u_prolong(const PatchDev* __restrict__ P, float*
   if (DIM == 3) ck -= gs;
   if (ci < 0 || ci > p.cmx[0] || cj < 0 || cj > p.cmx[1] || (DIM == 3 && (ck < 0 || ck > p.cmx[2]))) return;
   const int nz = DIM == 3 ? 2 : 1;
+  float* fp = fbase<CL>(fpool, p);
   for (int v = 0; v < nrvars; v++) {
-    const float* a = fpool + p.ecq + v * p.sc;
-    float* e = fpool + p.eq + v * p.sq;
+    const float* a = fp + p.ecq + v * p.sc;
+    float* e = fp + p.eq + v * p.sq;
     // x-direction values b[dz][dy][fx] for coarse rows (cj+dy, ck+dz)
     float bxv[2][2][2];
     for (int dz = 0; dz < nz; dz++)
@@ -127,13 +153,16 @@ __device__ __forceinline__ void u_prolong(const PatchDev* __restrict__ P, float*
 }
 
 // ghost programs on e: homogeneous boundary conditions
+template <bool CL = false>
 __device__ __forceinline__ void ghost32_apply(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                               const GhostOp& g, int nrvars) {
   const PatchDev& d = P[g.dp];
   const PatchDev& s = P[g.sp];
+  float* fd = fbase<CL>(fpool, d);
+  const float* fs = fbase<CL>(fpool, s);
   for (int v = 0; v < nrvars; v++) {
-    float* dq = fpool + d.eq + v * d.sq;
-    const float* sq = fpool + s.eq + v * s.sq;
+    float* dq = fd + d.eq + v * d.sq;
+    const float* sq = fs + s.eq + v * s.sq;
     float val;
     switch (g.type) {
       case kGCopy:
@@ -159,16 +188,14 @@ __device__ __forceinline__ void ghost32_apply(const PatchDev* __restrict__ P, fl
 // step 1 of an outer iteration: the frozen base planes and g, the FP32
 // image of the FP64 residual (mode 0: base planes only, 1: g from the
 // stored rf, 2: g = f - N(qbar) recomputed)
-template <class PL, int DIM>
-__global__ void __launch_bounds__(kBlock) k_mx_prep(const PatchDev* __restrict__ P, const double* __restrict__ pool,
-                                                    float* __restrict__ fpool, const Blk* __restrict__ blk, int mode,
-                                                    ProbParams pp) {
-  const Blk b = blk[blockIdx.x];
+template <class PL, int DIM, bool CL = false>
+__device__ __forceinline__ void u_prep(const PatchDev* __restrict__ P, double* pool, float* fpool, const Blk b,
+                                       int tid, int mode, const ProbParams& pp) {
   const PatchDev& p = P[b.patch];
   int i, j, k;
-  if (!interior_cell<DIM>(p.mx, b.start + threadIdx.x, i, j, k)) return;
+  if (!interior_cell<DIM>(p.mx, b.start + tid, i, j, k)) return;
   Cell64 x;
-  x.q = const_cast<double*>(pool) + p.oq;
+  x.q = pool + p.oq;
   x.f = pool + p.of;
   x.qold = pool + p.oqold;
   x.c = gofs<DIM>(p.qn, i, j, k);
@@ -177,15 +204,43 @@ __global__ void __launch_bounds__(kBlock) k_mx_prep(const PatchDev* __restrict__
   x.sz = (long long)p.qn[0] * p.qn[1];
   x.sq = p.sq;
   x.sf = p.sf;
-  PL::template mx_prep<DIM>(x, pool + p.orf, fpool + p.ephi, fpool + p.eg, mode, p.c, pp);
+  float* fp = fbase<CL>(fpool, p);
+  PL::template mx_prep<DIM>(x, pool + p.orf, fp + p.ephi, fp + p.eg, mode, p.c, pp);
+}
+template <class PL, int DIM>
+__global__ void __launch_bounds__(kBlock) k_mx_prep(const PatchDev* __restrict__ P, double* pool, float* fpool,
+                                                    const Blk* __restrict__ blk, int mode, ProbParams pp) {
+  u_prep<PL, DIM>(P, pool, fpool, blk[blockIdx.x], threadIdx.x, mode, pp);
 }
 
-template <class PL, int DIM>
+// step 3 of an outer iteration: qbar += e over the whole ghosted array; the
+// same pass refreshes the first nbase base planes for the next cycle and
+// clears e, so the next cycle needs neither a prep pass over those planes
+// nor a memset on this level
+template <int DIM, bool CL = false>
+__device__ __forceinline__ void u_update(const PatchDev* __restrict__ P, double* pool, float* fpool, const Blk b,
+                                         int tid, int nrvars, int nbase) {
+  const PatchDev& p = P[b.patch];
+  int i, j, k;
+  if (!ghosted_cell<DIM>(p.qn, p.gs, b.start + tid, i, j, k)) return;
+  bool interior = i >= 1 && i <= p.mx[0] && j >= 1 && j <= p.mx[1] && (DIM == 2 || (k >= 1 && k <= p.mx[2]));
+  long long c = gofs<DIM>(p.qn, i, j, k);
+  float* fp = fbase<CL>(fpool, p);
+  for (int v = 0; v < nrvars; v++) {
+    double nq = pool[p.oq + v * p.sq + c] + (double)fp[p.eq + v * p.sq + c];
+    pool[p.oq + v * p.sq + c] = nq;
+    fp[p.eq + v * p.sq + c] = 0.0f;
+    if (v < nbase && interior) fp[p.ephi + v * p.sf + iofs<DIM>(p.mx, i, j, k)] = (float)nq;
+  }
+}
+
+template <class PL, int DIM, bool CL = false>
 __device__ __forceinline__ Cell32 cell32(const PatchDev& p, float* fpool, int i, int j, int k) {
   Cell32 x;
-  x.e = fpool + p.eq;
-  x.g = fpool + p.eg;
-  x.base = fpool + p.ephi;
+  float* fp = fbase<CL>(fpool, p);
+  x.e = fp + p.eq;
+  x.g = fp + p.eg;
+  x.base = fp + p.ephi;
   x.c = gofs<DIM>(p.qn, i, j, k);
   x.fc = iofs<DIM>(p.mx, i, j, k);
   x.sy = p.qn[0];
@@ -196,13 +251,13 @@ __device__ __forceinline__ Cell32 cell32(const PatchDev& p, float* fpool, int i,
 }
 
 // red-black pointwise relaxation of the correction
-template <class PL, int DIM>
+template <class PL, int DIM, bool CL = false>
 __device__ __forceinline__ void u_relax(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
                                         int tid, int ipass, const MxParams& mp) {
   const PatchDev& p = P[b.patch];
   int i, j, k;
   if (!color_cell<DIM>(p, b.start + tid, ipass, i, j, k)) return;
-  PL::template mx_relax<DIM>(cell32<PL, DIM>(p, fpool, i, j, k), p.cf, mp);
+  PL::template mx_relax<DIM>(cell32<PL, DIM, CL>(p, fpool, i, j, k), p.cf, mp);
 }
 template <class PL, int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_relax(const PatchDev* __restrict__ P, float* __restrict__ fpool,
@@ -212,7 +267,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_relax(const PatchDev* __restrict_
 
 // CoarseLoadingFunction on the correction: fine r = g - M(e) under each
 // coarse cell; parent g(mb) = R(r) + M_c(ec) with the parent's base planes.
-template <class PL, int DIM>
+template <class PL, int DIM, bool CL = false>
 __device__ __forceinline__ void u_coarse_load(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
                                               int tid, const MxParams& mp) {
   constexpr int NV = PL::kNV;
@@ -220,7 +275,9 @@ __device__ __forceinline__ void u_coarse_load(const PatchDev* __restrict__ P, fl
   int ci, cj, ck;
   if (!interior_cell<DIM>(p.cmx, b.start + tid, ci, cj, ck)) return;
   const PatchDev& par = P[p.parent];
-  const float* e = fpool + p.eq;
+  float* fp = fbase<CL>(fpool, p);
+  float* fq = fbase<CL>(fpool, par);
+  const float* e = fp + p.eq;
   long long sy = p.qn[0], sz = (long long)p.qn[0] * p.qn[1];
   float R[NV];
   for (int v = 0; v < NV; v++) R[v] = 0.f;
@@ -232,18 +289,18 @@ __device__ __forceinline__ void u_coarse_load(const PatchDev* __restrict__ P, fl
         long long c = gofs<DIM>(p.qn, i, j, k);
         long long fc = iofs<DIM>(p.mx, i, j, k);
         float m[NV];
-        PL::template mx_op<DIM>(e, c, sy, sz, p.sq, fpool + p.ephi, fc, p.sf, p.cf, mp, m);
-        for (int v = 0; v < NV; v++) R[v] += fpool[p.eg + v * p.sf + fc] - m[v];
+        PL::template mx_op<DIM>(e, c, sy, sz, p.sq, fp + p.ephi, fc, p.sf, p.cf, mp, m);
+        for (int v = 0; v < NV; v++) R[v] += fp[p.eg + v * p.sf + fc] - m[v];
       }
   for (int v = 0; v < NV; v++) R[v] *= DIM == 2 ? 0.25f : 0.125f;
-  const float* ec = fpool + p.ecq;
+  const float* ec = fp + p.ecq;
   long long csy = p.cn[0], csz = (long long)p.cn[0] * p.cn[1];
   long long cc = gofs<DIM>(p.cn, ci, cj, ck);
   long long pf = iofs<DIM>(par.mx, p.mb[0] + ci - 1, p.mb[1] + cj - 1, DIM == 3 ? p.mb[2] + ck - 1 : 1);
   // the coarse operator reads the ec ring, which coarse_ring has filled
   float m[NV];
-  PL::template mx_op<DIM>(ec, cc, csy, csz, p.sc, fpool + par.ephi, pf, par.sf, par.cf, mp, m);
-  for (int v = 0; v < NV; v++) fpool[par.eg + v * par.sf + pf] = R[v] + m[v];
+  PL::template mx_op<DIM>(ec, cc, csy, csz, p.sc, fq + par.ephi, pf, par.sf, par.cf, mp, m);
+  for (int v = 0; v < NV; v++) fq[par.eg + v * par.sf + pf] = R[v] + m[v];
 }
 template <class PL, int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_coarse_load(const PatchDev* __restrict__ P, float* __restrict__ fpool,
@@ -405,6 +462,14 @@ __global__ void __launch_bounds__(kBlock) k_mx_tail_smem(const PatchDev* __restr
   }
 }
 
+}  // namespace mx
+}  // namespace bsamg
+
+#include "kern_solve.cuh"
+
+namespace bsamg {
+namespace mx {
+
 // The launchers of one plugin's correction-form kernels (the table the
 // plugin registers)
 template <class PL>
@@ -458,6 +523,77 @@ struct Launchers {
     }
     return 1;
   }
+  // the whole solve in one cluster launch (kern_solve.cuh); 1 on success,
+  // -1 when the launch shape is not one of the compiled ones or the launch
+  // failed (cudaGetLastError then says why)
+  template <int DIM, int T>
+  static cudaError_t solve_launch(const MxLaunch& L, const void* img, SolveImage im, SolveCtl* ctl, double* res,
+                                  double* partial, int ctas) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(T);
+    cfg.dynamicSmemBytes = im.data + im.ops + im.bytes;  // FP32 data, ghost operations, image
+    cfg.stream = L.s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = ctas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_mx_solve<PL, DIM, T>, static_cast<const unsigned char*>(img), im, L.pool,
+                              L.fpool, ctl, res, partial, L.pp, PL::mx_params(L.pp));
+  }
+  static int solve(const MxLaunch& L, const void* ph, SolveImage im, SolveCtl* ctl, double* res, double* partial,
+                   SolveShape sh) {
+    cudaError_t e = cudaErrorInvalidValue;
+    if (L.ndims == 2) {
+      if (sh.threads == 256) e = solve_launch<2, 256>(L, ph, im, ctl, res, partial, sh.ctas);
+      else if (sh.threads == 512) e = solve_launch<2, 512>(L, ph, im, ctl, res, partial, sh.ctas);
+      else if (sh.threads == 1024) e = solve_launch<2, 1024>(L, ph, im, ctl, res, partial, sh.ctas);
+    } else {
+      if (sh.threads == 256) e = solve_launch<3, 256>(L, ph, im, ctl, res, partial, sh.ctas);
+      else if (sh.threads == 512) e = solve_launch<3, 512>(L, ph, im, ctl, res, partial, sh.ctas);
+      else if (sh.threads == 1024) e = solve_launch<3, 1024>(L, ph, im, ctl, res, partial, sh.ctas);
+    }
+    return e == cudaSuccess ? 1 : -1;
+  }
+  // allow clusters above the portable 8 CTAs and report how many clusters of
+  // this shape fit on the device at once (0: the shape cannot run)
+  template <int DIM, int T>
+  static int solve_fit(int ctas) {
+    auto k = k_mx_solve<PL, DIM, T>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return 0;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSolveSmemMax) != cudaSuccess) return 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(T);
+    cfg.dynamicSmemBytes = kSolveSmemMax;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = ctas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) != cudaSuccess) return 0;
+    return n;
+  }
+  static int solve_setup(int ndims, SolveShape sh) {
+    int n = 0;
+    if (ndims == 2) {
+      if (sh.threads == 256) n = solve_fit<2, 256>(sh.ctas);
+      else if (sh.threads == 512) n = solve_fit<2, 512>(sh.ctas);
+      else if (sh.threads == 1024) n = solve_fit<2, 1024>(sh.ctas);
+    } else {
+      if (sh.threads == 256) n = solve_fit<3, 256>(sh.ctas);
+      else if (sh.threads == 512) n = solve_fit<3, 512>(sh.ctas);
+      else if (sh.threads == 1024) n = solve_fit<3, 1024>(sh.ctas);
+    }
+    cudaGetLastError();  // a shape that does not fit is an answer, not an error
+    return n;
+  }
   static int tail_smem_attributes(int ndims) {
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e = ndims == 2 ? cudaFuncSetAttribute(k_mx_tail_smem<PL, 2>, a, kTailSmemMax)
@@ -470,7 +606,8 @@ template <class PL>
 const PluginMixed* mixed_ops() {
   static const PluginMixed ops = {PL::kMxBase,           PL::kMxUpdate,          &Launchers<PL>::prep,
                                   &Launchers<PL>::relax, &Launchers<PL>::coarse_load, &Launchers<PL>::track,
-                                  &Launchers<PL>::norm,  &Launchers<PL>::tail,   &Launchers<PL>::tail_smem_attributes};
+                                  &Launchers<PL>::norm,  &Launchers<PL>::tail,   &Launchers<PL>::tail_smem_attributes,
+                                  &Launchers<PL>::solve, &Launchers<PL>::solve_setup};
   return &ops;
 }
 

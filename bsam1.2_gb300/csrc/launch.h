@@ -42,6 +42,76 @@ struct TailPhase {
   const int* stage_off;
 };
 
+// Marks, while a solve program is recorded, the start of the coarse end of
+// a V-cycle that one CTA runs alone (nblk = number of phases that follow).
+constexpr int kTSolo = 7;
+
+// The whole mixed-precision solve of a hierarchy with refinement levels as
+// one program executed by a single thread-block cluster (kern_solve.cuh):
+// the FP32 correction V-cycle's operations (ops 0-5, as TailOp), the FP64
+// operations of the defect-correction loop around it, and the exit test.
+enum SolveOp : int {
+  kSClear = 8,     // fpool[a .. a+len) = 0
+  kSPrep = 9,      // base planes and g of a level (arg = mode of mx_prep)
+  kSUpdate = 10,   // qbar += e over the ghosted cells, e = 0, base refresh (arg = variables refreshed)
+  kSFill64 = 11,   // FillDown of q in FP64 (FillDownLevel, field 2)
+  kSGhost64 = 12,  // an FP64 ghost program
+  kSNorm = 13,     // FP64 residual of the finest level: rf and n partial sums (padded interior list)
+  kSFinish = 14,   // one CTA: the deterministic final sum, the residual record and the exit decision
+  kSSolo = 15      // the next n phases run in CTA 0 alone (barriers of that CTA between them)
+};
+// FP32 operations (0-5, kSClear, kSPrep, kSUpdate) take their work by
+// owner: each CTA the blocks (ghost operations) of the patches it owns,
+// part[rank] .. part[rank+1] of the phase's list (of each stage), CTA 0
+// all of them inside a solo block.  FP64 operations spread their list over
+// all threads of the cluster.
+struct SolvePhase {
+  int op, arg, n, nstages;
+  int bar;    // a cluster barrier follows the phase
+  int blk;    // the phase's work list: first entry in the program image's block pool
+  int stage;  // ghost programs: first entry of their stage offsets in the image's stage pool
+              // (FP64: nstages+1 offsets; FP32: for stage s and CTA r, the pair at 2*(s*ctas + r))
+  int part;   // owner partition: first of ctas+1 entries in the image's part pool (-1: none)
+  const GhostOp* ops;  // a ghost program's operations (global memory)
+  long long a, len;    // kSClear: the range of the FP32 pool
+};
+// The program image every CTA of a solve copies into its shared memory at
+// the start, after a data area of `data` bytes that holds the FP32 arrays
+// of the patches it owns in distributed shared memory: the phases at
+// offset 0, then the patch table, the block, stage and part pools (byte
+// offsets from the image's start, 16-byte aligned).  Read-only data read
+// from shared memory is not lost at a cluster barrier, whose acquire
+// discards what the L1 cache holds.
+struct SolveImage {
+  int bytes, data, off_patches, off_blk, off_stage, off_part;
+  // the FP32 ghost operations are ordered by CTA: CTA r's are [seg[r],
+  // seg[r+1]) of the program's operation array (seg: ctas+1 entries of the
+  // part pool at off_seg); when ops_smem, each CTA stages its own after its
+  // data area (ops bytes reserved per CTA)
+  int seg, ops_smem, ops;
+};
+constexpr int kSolveSmemMax = 192 * 1024;  // largest image a solve stages
+// Control block of a solve launch (device memory); the residual of V-cycle
+// it (1-based) follows it at res[it-1].
+struct SolveCtl {
+  int body, nph;      // first phase of the loop body, phases in the program
+  int maxv, errortype;
+  double tol, count;  // exit tolerance, ErrorAFAS denominator of the finest level
+  int nb, nrvars;     // partial sums of the norm, variables
+  // results
+  int ncycles, converged, nonfinite, stop;
+  double norm[2];     // the last norm and its raw sum
+  const GhostOp* ops;  // the program's FP32 ghost operations, CTA after CTA
+  // when set: CTA 0's clock at the end of every phase of the prologue and
+  // the first outer iteration (trace[x], cycles of the SM it runs on), and
+  // at the start (trace[nph])
+  long long* trace;
+};
+// launch shape of the solve kernel: CTAs in the cluster, threads per CTA
+struct SolveShape {
+  int ctas, threads;
+};
+
 // A contiguous run of pool elements staged in shared memory by a tail
 // kernel: pool[g .. g+n) <-> smem[s .. s+n); written back when out != 0.
 struct StageSeg {

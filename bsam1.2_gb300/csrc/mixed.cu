@@ -23,6 +23,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "kern_mixed.cuh"
@@ -53,26 +57,12 @@ __global__ void __launch_bounds__(kBlock) k_mx_prolong(const PatchDev* __restric
   u_prolong<DIM>(P, fpool, blk[blockIdx.x], threadIdx.x, nrvars);
 }
 
-// step 3: qbar += e (whole ghosted array).  The
-// same pass refreshes the base field phib of the next cycle and clears e,
-// so the next cycle needs neither a separate prep pass over q nor a memset
-// on this level.
+// step 3: qbar += e (whole ghosted array), base refresh, e = 0 (u_update)
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_mx_update(const PatchDev* __restrict__ P, double* __restrict__ pool,
                                                       float* __restrict__ fpool, const Blk* __restrict__ blk,
                                                       int nrvars, int nbase) {
-  const Blk b = blk[blockIdx.x];
-  const PatchDev& p = P[b.patch];
-  int i, j, k;
-  if (!ghosted_cell<DIM>(p.qn, p.gs, b.start + threadIdx.x, i, j, k)) return;
-  bool interior = i >= 1 && i <= p.mx[0] && j >= 1 && j <= p.mx[1] && (DIM == 2 || (k >= 1 && k <= p.mx[2]));
-  long long c = gofs<DIM>(p.qn, i, j, k);
-  for (int v = 0; v < nrvars; v++) {
-    double nq = pool[p.oq + v * p.sq + c] + (double)fpool[p.eq + v * p.sq + c];
-    pool[p.oq + v * p.sq + c] = nq;
-    fpool[p.eq + v * p.sq + c] = 0.0f;
-    if (v < nbase && interior) fpool[p.ephi + v * p.sf + iofs<DIM>(p.mx, i, j, k)] = (float)nq;
-  }
+  u_update<DIM>(P, pool, fpool, blk[blockIdx.x], threadIdx.x, nrvars, nbase);
 }
 
 __global__ void __launch_bounds__(kBlock) k_ghost32_stage(const PatchDev* __restrict__ P, float* __restrict__ fpool,
@@ -184,6 +174,18 @@ int mx_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
       return after_launch(H, mxp(H).tail(mxl(H), table, ph, T.nph, static_cast<const StageSeg*>(T.segs), T.nsegs,
                                          T.smem_bytes));
     }
+  }
+  // while a solve program is recorded, CTA 0 alone runs the coarse end from
+  // level rec_solo down: a marker counts the phases that follow it
+  std::vector<TailPhase>* rec = rec_of(H);
+  if (rec && level == H.rec_solo) {
+    size_t at = rec->size();
+    rec->push_back(TailPhase{kTSolo, 0, 0, 0, nullptr, nullptr, nullptr});
+    H.rec_solo = -kMaxDepth - 2;
+    int r = mx_vcycle(H, level, minlevel, nsmooth);
+    H.rec_solo = level;
+    (*rec)[at].nblk = (int)(rec->size() - at - 1);
+    return r;
   }
   int r = mx_level_relax(H, level, nsmooth);
   if (r) return r;
@@ -368,6 +370,515 @@ int mx_verify(Hier& H, int finest, int errortype) {
   return to_host(H);
 }
 
+// ---------------------------------------------------------------------------
+// The whole solve of a hierarchy with refinement levels in one launch of one
+// thread-block cluster (kern_solve.cuh).  The program below is the sequence
+// mixed_iterations runs on such a hierarchy -- the FP64 residual of the
+// finest level, e = 0, then per outer iteration: coarse e = 0, the base
+// planes and g of every level, the FP32 V-cycle, qbar += e, FillDown(q),
+// the refinement levels' ghosts and the FP64 residual -- recorded from the
+// same schedule functions, so the launch computes the same iterates.
+
+// the highest level whose level and every level below it together hold at
+// most `cells` interior cells: the coarse end that CTA 0 runs alone
+int solo_level(const Hier& H, long long cells) {
+  int lvl = -kMaxDepth - 2;
+  if (cells <= 0) return lvl;
+  long long sum = 0;
+  for (int l = H.minlevel; l <= H.maxlevel; l++) {
+    for (int p : H.L(l).patches) {
+      const HostPatch& P = H.patches[p];
+      sum += (long long)P.mx[0] * P.mx[1] * P.mx[2];
+    }
+    if (sum > cells) break;
+    lvl = l;
+  }
+  return lvl;
+}
+
+int solve_norm_groups(const Hier& H, int finest) {
+  return (H.L(finest).nblk[kKindInterior] + kNormCells - 1) / kNormCells;
+}
+
+// clusters of this shape that fit on the device at once (0: it cannot run);
+// asked once per device, plugin, dimension and shape
+int solve_fit(const Hier& H, SolveShape sh) {
+  if (sh.ctas < 1 || sh.ctas > 16 || (sh.threads != 256 && sh.threads != 512 && sh.threads != 1024)) return 0;
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int, int>, int> fit;
+  auto key = std::make_tuple(H.ctx->device, H.problem, H.ndims, sh.ctas, sh.threads);
+  {
+    std::lock_guard<std::mutex> g(mu);
+    auto it = fit.find(key);
+    if (it != fit.end()) return it->second;
+  }
+  int n = mxp(H).solve_setup(H.ndims, sh);
+  std::lock_guard<std::mutex> g(mu);
+  fit[key] = n;
+  return n;
+}
+
+bool solve_applies(const Hier& H, int finest) {
+  return H.solve_mode == 1 && !H.box && H.fpool && finest >= 1 && solve_norm_groups(H, finest) <= 2048 &&
+         solve_norm_groups(H, finest) <= H.partial_cap && solve_fit(H, H.solve_shape) > 0;
+}
+
+// The program, its pools and the FP32 ghost operations, as the builder
+// lays them out for one choice of which patches keep their FP32 arrays in
+// distributed shared memory.
+struct SolveBuild {
+  std::vector<SolvePhase> prog;
+  std::vector<Blk> bpool;
+  std::vector<int> spool, ppool;
+  std::vector<std::vector<GhostOp>> ops;  // per CTA
+  std::vector<size_t> clears;             // phases whose shared-memory ranges follow the layout
+  int body = 0, bad = 0;
+};
+
+int solve_record(Hier& H, int finest, int minlevel, int nsmooth, int solo, int C, const std::vector<int>& owner,
+                 const std::vector<char>& dsm, SolveBuild& B) {
+  B = SolveBuild();
+  B.ops.assign(C, {});
+  // the host copies behind the device lists and ghost programs the schedule
+  // functions record
+  std::map<const Blk*, const std::vector<Blk>*> lists;
+  std::map<const int*, const std::vector<int>*> stages;
+  std::map<const GhostOp*, const GhostProg*> progs;
+  for (int l = H.minlevel; l <= H.maxlevel; l++) {
+    LevelT& L = H.L(l);
+    for (int k = 0; k < kNKind; k++)
+      if (L.d_blk[k]) lists[L.d_blk[k]] = &L.h_blk[k];
+    for (int ip = 0; ip < 3; ip++) {
+      if (L.gp[ip].d_stage_off) stages[L.gp[ip].d_stage_off] = &L.gp[ip].stage_off;
+      if (L.gp[ip].d_ops) progs[L.gp[ip].d_ops] = &L.gp[ip];
+    }
+    if (H.mx_norm_blk[l + kMaxDepth]) lists[H.mx_norm_blk[l + kMaxDepth]] = &H.h_mx_norm_blk[l + kMaxDepth];
+  }
+  if (H.mx_prep_coarse) lists[H.mx_prep_coarse] = &H.h_mx_prep_coarse;
+  // the CTA that works on a block or ghost operation of patch p (the i-th of
+  // its list or stage): CTA 0 for the levels it runs alone, the owner for
+  // arrays in shared memory, else the CTAs in turn
+  auto sched = [&](int p, int i) {
+    if (H.patches[p].level <= solo) return 0;
+    return dsm[p] ? owner[p] : i % C;
+  };
+  std::map<const Blk*, int> boff;
+  std::map<const Blk*, std::pair<int, int>> poff;
+  std::map<const int*, int> soff;
+  std::map<const GhostOp*, int> goff;
+  auto host_list = [&](const Blk* d) -> const std::vector<Blk>* {
+    auto h = lists.find(d);
+    if (h == lists.end()) {
+      B.bad = 1;
+      return nullptr;
+    }
+    return h->second;
+  };
+  auto blk_at = [&](const Blk* d) {  // a list as it is (FP64 phases)
+    if (!d) return 0;
+    auto it = boff.find(d);
+    if (it != boff.end()) return it->second;
+    const std::vector<Blk>* v = host_list(d);
+    if (!v) return 0;
+    int at = (int)B.bpool.size();
+    B.bpool.insert(B.bpool.end(), v->begin(), v->end());
+    return boff[d] = at;
+  };
+  auto part_at = [&](const Blk* d) {  // a list in CTA order, with its ctas+1 offsets
+    if (!d) return std::make_pair(0, -1);
+    auto it = poff.find(d);
+    if (it != poff.end()) return it->second;
+    const std::vector<Blk>* v = host_list(d);
+    if (!v) return std::make_pair(0, -1);
+    std::vector<std::vector<Blk>> by(C);
+    for (size_t i = 0; i < v->size(); i++) by[sched((*v)[i].patch, (int)i)].push_back((*v)[i]);
+    int at = (int)B.bpool.size(), pt = (int)B.ppool.size();
+    for (int r = 0; r < C; r++) {
+      B.ppool.push_back((int)(B.bpool.size() - at));
+      B.bpool.insert(B.bpool.end(), by[r].begin(), by[r].end());
+    }
+    B.ppool.push_back((int)(B.bpool.size() - at));
+    return poff[d] = std::make_pair(at, pt);
+  };
+  auto stage_at = [&](const int* d) {  // plain stage offsets (FP64 ghost programs)
+    if (!d) return 0;
+    auto it = soff.find(d);
+    if (it != soff.end()) return it->second;
+    auto h = stages.find(d);
+    if (h == stages.end()) {
+      B.bad = 1;
+      return 0;
+    }
+    int at = (int)B.spool.size();
+    B.spool.insert(B.spool.end(), h->second->begin(), h->second->end());
+    return soff[d] = at;
+  };
+  auto ghost_at = [&](const GhostOp* d) {  // an FP32 ghost program split by CTA within each stage
+    auto it = goff.find(d);
+    if (it != goff.end()) return it->second;
+    auto h = progs.find(d);
+    if (h == progs.end()) {
+      B.bad = 1;
+      return 0;
+    }
+    const GhostProg& G = *h->second;
+    int at = (int)B.spool.size();
+    int ns = (int)G.stage_off.size() - 1;
+    for (int st = 0; st < ns; st++) {
+      std::vector<std::vector<GhostOp>> by(C);
+      for (int i = G.stage_off[st]; i < G.stage_off[st + 1]; i++)
+        by[sched(G.ops[i].dp, i - G.stage_off[st])].push_back(G.ops[i]);
+      for (int r = 0; r < C; r++) {  // (first, end) in CTA r's own operation list
+        B.spool.push_back((int)B.ops[r].size());
+        B.ops[r].insert(B.ops[r].end(), by[r].begin(), by[r].end());
+        B.spool.push_back((int)B.ops[r].size());
+      }
+    }
+    return goff[d] = at;
+  };
+  auto phase = [&](int op, int arg, int bar) {
+    SolvePhase f{};
+    f.op = op;
+    f.arg = arg;
+    f.bar = bar;
+    f.part = -1;
+    return f;
+  };
+  auto push_fp64 = [&](int op, int arg, int n, const Blk* blk, int bar) {
+    SolvePhase f = phase(op, arg, bar);
+    f.n = n;
+    f.blk = blk_at(blk);
+    B.prog.push_back(f);
+  };
+  auto push_owned = [&](int op, int arg, int n, const Blk* blk, int bar) {
+    SolvePhase f = phase(op, arg, bar);
+    f.n = n;
+    auto pr = part_at(blk);
+    f.blk = pr.first;
+    f.part = pr.second;
+    B.prog.push_back(f);
+  };
+  auto clear = [&](long long a, long long len, int bar) {
+    SolvePhase f = phase(kSClear, 0, bar);
+    f.a = a;
+    f.len = len;
+    f.part = (int)B.ppool.size();
+    B.ppool.insert(B.ppool.end(), 2 * C, 0);
+    B.clears.push_back(B.prog.size());
+    B.prog.push_back(f);
+  };
+  // what the schedule functions record, as solve phases (FP64 ghost
+  // programs when fp64)
+  auto record = [&](const std::function<int()>& body, bool fp64) {
+    std::vector<TailPhase> rec;
+    H.rec = &rec;
+    int r = body();
+    H.rec = nullptr;
+    for (const TailPhase& t : rec) {
+      SolvePhase f = phase(t.op, t.arg, 1);
+      f.n = t.nblk;
+      f.nstages = t.nstages;
+      if (t.op == kTSolo) {
+        f.op = kSSolo;
+        f.bar = 0;
+      } else if (t.op == kTGhost && fp64) {
+        f.op = kSGhost64;
+        f.ops = t.ops;
+        f.stage = stage_at(t.stage_off);
+      } else if (t.op == kTGhost) {
+        f.stage = ghost_at(t.ops);  // f.ops: the operations by CTA, set after their upload
+      } else {
+        auto pr = part_at(t.blk);
+        f.blk = pr.first;
+        f.part = pr.second;
+      }
+      B.prog.push_back(f);
+    }
+    return r;
+  };
+  const int nb = solve_norm_groups(H, finest);
+  const Blk* nlist = H.mx_norm_blk[finest + kMaxDepth];
+  // prologue (mixed_iterations before its loop)
+  push_fp64(kSNorm, 0, nb, nlist, 1);
+  clear(0, (long long)H.e_len, 1);
+  B.body = (int)B.prog.size();
+  // mx_iteration, every cycle from the FP64 residual
+  if (H.e_coarse_len) clear((long long)H.e_coarse_off, (long long)H.e_coarse_len, 0);
+  for (int level = finest; level >= minlevel; level--) {
+    LevelT& L = H.L(level);
+    int mode = level < 0 ? 0 : (level == finest ? 1 : 2);
+    bool all_coarse = level < 0 && minlevel == H.minlevel && H.mx_prep_coarse_n > 0;
+    const Blk* blk = all_coarse ? H.mx_prep_coarse : L.d_blk[kKindInterior];
+    int n = all_coarse ? H.mx_prep_coarse_n : L.nblk[kKindInterior];
+    if (n > 0) push_owned(kSPrep, mode, n, blk, 0);
+    if (all_coarse) break;
+  }
+  B.prog.back().bar = 1;
+  H.rec_solo = solo;
+  int r = record([&] { return mx_vcycle(H, finest, minlevel, nsmooth); }, false);
+  H.rec_solo = -kMaxDepth - 2;
+  if (r) return r;
+  for (int level = finest; level >= 0; level--) {
+    LevelT& L = H.L(level);
+    if (L.nblk[kKindFGhost] > 0) push_owned(kSUpdate, mxp(H).nupdate, L.nblk[kKindFGhost], L.d_blk[kKindFGhost], 0);
+  }
+  B.prog.back().bar = 1;
+  // FillDown(q) (enq_fill_down's order); from the level above the solo
+  // level down in CTA 0 alone
+  size_t solo_at = (size_t)-1;
+  for (int level = finest; level >= minlevel + 1; level--) {
+    if (level - 1 <= solo && solo_at == (size_t)-1) {
+      solo_at = B.prog.size();
+      B.prog.push_back(phase(kSSolo, 0, 0));
+    }
+    LevelT& L = H.L(level);
+    if (L.nblk[kKindCoarse] > 0) push_fp64(kSFill64, 2, L.nblk[kKindCoarse], L.d_blk[kKindCoarse], 1);
+    if ((r = record([&] { return enq_set_ghost(H, level - 1, 0); }, true))) return r;
+  }
+  if (solo_at != (size_t)-1) B.prog[solo_at].n = (int)(B.prog.size() - solo_at - 1);
+  for (int level = 1; level <= finest; level++)
+    if ((r = record([&] { return enq_set_ghost(H, level, 0); }, true))) return r;
+  push_fp64(kSNorm, 0, nb, nlist, 1);
+  push_fp64(kSFinish, 0, nb, nullptr, 1);
+  return B.bad ? BSAMG_ERR_ARG : BSAMG_OK;  // a recorded list without a host copy is not expected
+}
+
+int solve_build(Hier& H, int finest, int minlevel, int nsmooth) {
+  const int C = H.solve_shape.ctas;
+  const int solo = solo_level(H, H.solve_solo_cells);
+  auto key = std::make_tuple(finest, minlevel, nsmooth, solo, C);
+  if (H.solve_key == key && (H.solve_img || H.solve_nofit)) return H.solve_img ? BSAMG_OK : BSAMG_ERR_UNSUPPORTED;
+  const int np = (int)H.patches.size();
+  auto cells = [&](int p) {
+    const HostPatch& P = H.patches[p];
+    return (long long)P.mx[0] * P.mx[1] * P.mx[2];
+  };
+  const long long nbase = mxp(H).nbase;
+  auto al4 = [](long long x) { return (x + 3) & ~3LL; };
+  auto floats = [&](int p) {  // a patch's FP32 arrays: e, ec, g, base planes
+    const HostPatch& P = H.patches[p];
+    return al4(H.nrvars * P.sq) + al4(H.nrvars * P.sc) + al4(H.nrvars * P.sf) + al4(nbase * P.sf);
+  };
+  // owners: the levels CTA 0 runs alone belong to it; every other level's
+  // patches, finest level first, are dealt by size, largest first, each to
+  // the CTA with the fewest cells of that level (then the least memory)
+  std::vector<int> owner(np, 0);
+  std::vector<long long> mem_all(C, 0);
+  for (int l = H.maxlevel; l >= H.minlevel; l--) {
+    std::vector<int> ps = H.L(l).patches;
+    if (l <= solo) {
+      for (int p : ps) mem_all[0] += floats(p);
+      continue;
+    }
+    std::stable_sort(ps.begin(), ps.end(), [&](int x, int y) { return cells(x) > cells(y); });
+    std::vector<long long> load(C, 0);
+    for (int p : ps) {
+      int r = 0;
+      for (int q = 1; q < C; q++)
+        if (load[q] < load[r] || (load[q] == load[r] && mem_all[q] < mem_all[r])) r = q;
+      owner[p] = r;
+      load[r] += cells(p);
+      mem_all[r] += floats(p);
+    }
+  }
+  // the image's size does not depend on where the arrays live: record once
+  // to size it, choose the levels kept in distributed shared memory
+  // (coarsest first, each level where every CTA's share fits beside the
+  // image), then record the final program
+  std::vector<char> dsm(np, 0);
+  SolveBuild B;
+  int r = solve_record(H, finest, minlevel, nsmooth, solo, C, owner, dsm, B);
+  if (r) return r;
+  auto al16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  SolveImage im{};
+  size_t o = al16(sizeof(SolvePhase) * B.prog.size());
+  im.off_patches = (int)o;
+  o = al16(o + sizeof(PatchDev) * H.hP.size());
+  im.off_blk = (int)o;
+  o = al16(o + sizeof(Blk) * B.bpool.size());
+  im.off_stage = (int)o;
+  o = al16(o + sizeof(int) * B.spool.size());
+  im.off_part = (int)o;
+  o = al16(o + sizeof(int) * (B.ppool.size() + C + 1));  // + the CTAs' operation segments
+  im.bytes = (int)o;
+  if (o > (size_t)kSolveSmemMax) {  // too large to stage: the per-launch path runs this hierarchy
+    solve_invalidate(H);
+    H.solve_key = key;
+    H.solve_nofit = true;
+    return BSAMG_ERR_UNSUPPORTED;
+  }
+  const long long budget = ((long long)kSolveSmemMax - (long long)o) / 4;
+  std::vector<long long> mem(C, 0);
+  int dsm_levels = 0;
+  for (int l = minlevel; l <= finest; l++) {
+    std::vector<long long> add(C, 0);
+    for (int p : H.L(l).patches) add[owner[p]] += floats(p);
+    bool fits = true;
+    for (int q = 0; q < C; q++) fits = fits && mem[q] + add[q] <= budget;
+    if (!fits) continue;
+    for (int q = 0; q < C; q++) mem[q] += add[q];
+    for (int p : H.L(l).patches) dsm[p] = 1;
+    dsm_levels++;
+  }
+  if ((r = solve_record(H, finest, minlevel, nsmooth, solo, C, owner, dsm, B))) return r;
+  // each CTA's data area: e of its levels >= 0, e of its levels < 0, then
+  // ec, g and the base planes
+  std::vector<PatchDev> table = H.hP;
+  std::vector<long long> elen(C, 0), ecoarse(C, 0), top(C, 0);
+  for (int pass = 0; pass < 2; pass++) {
+    for (int q = 0; q < C && pass == 1; q++) ecoarse[q] = top[q];
+    for (int p = 0; p < np; p++)
+      if (dsm[p] && (H.patches[p].level < 0) == (pass == 1)) {
+        const HostPatch& P = H.patches[p];
+        table[p].eq = top[owner[p]] + origin_of(H, P.qn);
+        top[owner[p]] += al4(H.nrvars * P.sq);
+      }
+  }
+  for (int q = 0; q < C; q++) elen[q] = top[q];
+  for (int p = 0; p < np; p++) {
+    table[p].owner = owner[p];
+    table[p].dsm = dsm[p];
+    if (!dsm[p]) continue;
+    const HostPatch& P = H.patches[p];
+    long long& t = top[owner[p]];
+    table[p].ecq = t + origin_of(H, P.cn);
+    t += al4(H.nrvars * P.sc);
+    table[p].eg = t;
+    t += al4(H.nrvars * P.sf);
+    table[p].ephi = t;
+    t += al4(nbase * P.sf);
+  }
+  long long dmax = 0;
+  for (int q = 0; q < C; q++) dmax = std::max(dmax, top[q]);
+  im.data = (int)al16((size_t)dmax * 4);
+  for (size_t k = 0; k < B.clears.size(); k++) {
+    int* pr = B.ppool.data() + B.prog[B.clears[k]].part;
+    for (int q = 0; q < C; q++) {
+      long long from = k == 0 ? 0 : ecoarse[q];  // the prologue clears all e, the loop the coarse levels' e
+      pr[2 * q] = (int)from;
+      pr[2 * q + 1] = (int)(elen[q] - from);
+    }
+  }
+  // the FP32 ghost operations, CTA after CTA; each CTA stages its own in
+  // shared memory when every CTA's fit in what the data area leaves
+  im.seg = (int)B.ppool.size();
+  std::vector<GhostOp> sops;
+  size_t opmax = 0;
+  for (int q = 0; q < C; q++) {
+    B.ppool.push_back((int)sops.size());
+    sops.insert(sops.end(), B.ops[q].begin(), B.ops[q].end());
+    opmax = std::max(opmax, B.ops[q].size());
+  }
+  B.ppool.push_back((int)sops.size());
+  im.ops = (int)al16(sizeof(GhostOp) * opmax);
+  im.ops_smem = (size_t)im.data + im.ops + o <= (size_t)kSolveSmemMax ? 1 : 0;
+  if (!im.ops_smem) im.ops = 0;
+  if (H.solve_ops) cudaFreeAsync(H.solve_ops, H.s);
+  H.solve_ops = nullptr;
+  if (!sops.empty()) {
+    cudaError_t e = dev_alloc(H, (void**)&H.solve_ops, sizeof(GhostOp) * sops.size());
+    if (e == cudaSuccess)  // staged from pageable memory before it returns
+      e = cudaMemcpyAsync(H.solve_ops, sops.data(), sizeof(GhostOp) * sops.size(), cudaMemcpyHostToDevice, H.s);
+    if (e != cudaSuccess) return cuda_fail(e, "solve ghost operations upload");
+  }
+  for (SolvePhase& f : B.prog)
+    if (f.op == kTGhost) f.ops = H.solve_ops;
+  std::vector<unsigned char> img(o, 0);
+  std::memcpy(img.data(), B.prog.data(), sizeof(SolvePhase) * B.prog.size());
+  std::memcpy(img.data() + im.off_patches, table.data(), sizeof(PatchDev) * table.size());
+  if (!B.bpool.empty()) std::memcpy(img.data() + im.off_blk, B.bpool.data(), sizeof(Blk) * B.bpool.size());
+  if (!B.spool.empty()) std::memcpy(img.data() + im.off_stage, B.spool.data(), sizeof(int) * B.spool.size());
+  std::memcpy(img.data() + im.off_part, B.ppool.data(), sizeof(int) * B.ppool.size());
+  if (H.solve_img) cudaFreeAsync(H.solve_img, H.s);
+  H.solve_img = nullptr;
+  cudaError_t e = dev_alloc(H, &H.solve_img, img.size());
+  if (e == cudaSuccess)  // staged from pageable memory before it returns
+    e = cudaMemcpyAsync(H.solve_img, img.data(), img.size(), cudaMemcpyHostToDevice, H.s);
+  if (e != cudaSuccess) return cuda_fail(e, "solve program upload");
+  H.solve_im = im;
+  H.solve_nofit = false;
+  H.solve_nph = (int)B.prog.size();
+  H.solve_body = B.body;
+  H.solve_nb = solve_norm_groups(H, finest);
+  H.solve_key = key;
+  H.solve_dsm_levels = dsm_levels;
+  return BSAMG_OK;
+}
+
+int solve_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,
+                     int strict, int* ncycles, double* residuals) {
+  int r = solve_build(H, finest, minlevel, nsmooth);
+  if (r) return r;
+  if (H.solve_ctl_cap < maxvcycles) {
+    if (H.solve_ctl) cudaFreeAsync(H.solve_ctl, H.s);
+    H.solve_ctl = nullptr;
+    H.solve_ctl_cap = 0;
+    cudaError_t e = dev_alloc(H, &H.solve_ctl, sizeof(SolveCtl) + sizeof(double) * (size_t)maxvcycles);
+    if (e != cudaSuccess) return cuda_fail(e, "device allocation (solve control)");
+    H.solve_ctl_cap = maxvcycles;
+  }
+  SolveCtl c{};
+  c.body = H.solve_body;
+  c.nph = H.solve_nph;
+  c.maxv = maxvcycles;
+  c.errortype = errortype;
+  c.tol = tol;
+  c.count = H.L(finest).count;
+  c.nb = H.solve_nb;
+  c.nrvars = H.nrvars;
+  if (H.solve_trace_on && H.solve_trace_cap < H.solve_nph) {
+    if (H.solve_trace) cudaFreeAsync(H.solve_trace, H.s);
+    H.solve_trace = nullptr;
+    H.solve_trace_cap = 0;
+    cudaError_t e = dev_alloc(H, (void**)&H.solve_trace, sizeof(long long) * (H.solve_nph + 1));
+    if (e != cudaSuccess) return cuda_fail(e, "device allocation (solve trace)");
+    H.solve_trace_cap = H.solve_nph;
+  }
+  c.trace = H.solve_trace_on ? H.solve_trace : nullptr;
+  c.ops = H.solve_ops;
+  if (c.trace) {
+    cudaError_t e = cudaMemsetAsync(c.trace, 0, sizeof(long long) * (H.solve_nph + 1), H.s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(solve trace)");
+  }
+  SolveCtl* ctl = static_cast<SolveCtl*>(H.solve_ctl);
+  double* res = reinterpret_cast<double*>(ctl + 1);
+  cudaError_t e = cudaMemcpyAsync(ctl, &c, sizeof(c), cudaMemcpyHostToDevice, H.s);  // staged before it returns
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(solve control)");
+  if (mxp(H).solve(mxl(H), H.solve_img, H.solve_im, ctl, res, H.d_partial, H.solve_shape) < 0)
+    return cuda_fail(cudaGetLastError(), "solve launch");
+  if ((r = after_launch(H, 1))) return r;
+  if ((r = stream_wait(H))) return r;
+  std::vector<unsigned char> out(sizeof(SolveCtl) + sizeof(double) * (size_t)maxvcycles);
+  e = cudaMemcpy(out.data(), ctl, out.size(), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(solve control)");
+  SolveCtl o;
+  std::memcpy(&o, out.data(), sizeof(o));
+  if (c.trace) {
+    H.solve_trace_h.assign(H.solve_nph + 1, 0);
+    e = cudaMemcpy(H.solve_trace_h.data(), c.trace, sizeof(long long) * (H.solve_nph + 1), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(solve trace)");
+    std::vector<SolvePhase> ph(H.solve_nph);
+    e = cudaMemcpy(ph.data(), H.solve_img, sizeof(SolvePhase) * H.solve_nph, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(solve program)");
+    H.solve_trace_ops.resize(H.solve_nph);
+    H.solve_trace_n.resize(H.solve_nph);
+    for (int x = 0; x < H.solve_nph; x++) {
+      H.solve_trace_ops[x] = ph[x].op;
+      H.solve_trace_n[x] = ph[x].op == kTGhost || ph[x].op == kSGhost64 ? ph[x].nstages : ph[x].n;
+    }
+  }
+  const double* rv = reinterpret_cast<const double*>(out.data() + sizeof(SolveCtl));
+  int done = o.nonfinite ? o.ncycles - 1 : o.ncycles;
+  if (residuals)
+    for (int i = 0; i < done && i < maxvcycles; i++) residuals[i] = rv[i];
+  H.h_norm[0] = o.norm[0];
+  H.h_norm[1] = o.norm[1];
+  if (o.nonfinite) return BSAMG_ERR_NONFINITE;
+  if (ncycles) *ncycles = o.converged ? o.ncycles : maxvcycles;
+  if (!o.converged && strict) return BSAMG_ERR_NOT_CONVERGED;
+  return BSAMG_OK;
+}
+
 }  // namespace
 
 size_t mixed_pool_bytes(const Hier& H) {
@@ -418,6 +929,11 @@ void mixed_free(Hier& H) {
   H.mx_prep_coarse = nullptr;
   for (auto& kv : H.mx_tail_progs) free_tail(H, kv.second);
   H.mx_tail_progs.clear();
+  for (void** p : {&H.solve_img, &H.solve_ctl, (void**)&H.solve_trace, (void**)&H.solve_ops}) {
+    if (*p) cudaFreeAsync(*p, H.s);
+    *p = nullptr;
+  }
+  H.solve_ctl_cap = 0;
   for (int l = 0; l < kNLev; l++) {
     if (H.mx_norm_blk[l]) cudaFreeAsync(H.mx_norm_blk[l], H.s);
     H.mx_norm_blk[l] = nullptr;
@@ -443,6 +959,7 @@ int mixed_tables(Hier& H) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(norm list)");
     H.mx_norm_blk[l + kMaxDepth] = d;
     H.bytes += sizeof(Blk) * v.size();
+    H.h_mx_norm_blk[l + kMaxDepth] = v;
   }
   // the interior lists of all levels below the root, concatenated
   std::vector<Blk> v;
@@ -459,6 +976,7 @@ int mixed_tables(Hier& H) {
     if (e != cudaSuccess) return cuda_fail(e, "coarse prep list");
     H.mx_prep_coarse_n = (int)v.size();
     H.bytes += sizeof(Blk) * v.size();
+    H.h_mx_prep_coarse = v;
   }
   return BSAMG_OK;
 }
@@ -483,6 +1001,15 @@ void set_tail(Hier& H, long long cells) {
   }
 }
 
+void solve_invalidate(Hier& H) {
+  if (H.solve_img) cudaFreeAsync(H.solve_img, H.s);
+  H.solve_img = nullptr;
+  H.solve_nofit = false;
+  H.solve_key = std::make_tuple(kMaxDepth + 1, 0, 0, 0, 0);  // no program has this key
+}
+
+bool solve_shape_runs(const Hier& H, SolveShape sh) { return has_mixed(H) && solve_fit(H, sh) > 0; }
+
 int mixed_enq_relax(Hier& H, int level, int ipass) {
   if (!has_mixed(H) || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
   if (H.box) return box_enq_relax(H, level, ipass);
@@ -492,6 +1019,10 @@ int mixed_enq_relax(Hier& H, int level, int ipass) {
 int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,
                      int strict, int* ncycles, double* residuals) {
   if (!has_mixed(H) || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
+  if (solve_applies(H, finest)) {
+    int rs = solve_iterations(H, finest, minlevel, nsmooth, maxvcycles, tol, errortype, strict, ncycles, residuals);
+    if (rs != BSAMG_ERR_UNSUPPORTED) return rs;  // else its program is too large to stage: per-launch path
+  }
   // the first outer iteration takes its right-hand side from the FP64
   // residual of the finest level
   int r = mx_norm(H, finest, errortype);

@@ -20,6 +20,10 @@ int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcyc
 // the highest one at which the cumulative interior cell count is at most
 // `cells` run inside one CTA (0 disables)
 void set_tail(Hier& H, long long cells);
+// drop the one-launch solve's program image (rebuilt on its next use)
+void solve_invalidate(Hier& H);
+// whether the device runs the one-launch solve's cluster in this shape
+bool solve_shape_runs(const Hier& H, SolveShape sh);
 // one FP32 colour sweep of the correction smoother on `level`
 int mixed_enq_relax(Hier& H, int level, int ipass);
 

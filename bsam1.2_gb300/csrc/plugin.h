@@ -130,6 +130,11 @@ struct PluginMixed {
   int (*tail)(const MxLaunch&, const PatchDev* table, const TailPhase*, int nph, const StageSeg*, int nsegs,
               int smem_bytes);
   int (*tail_smem_attributes)(int ndims);
+  // the whole solve of a hierarchy with refinement levels in one cluster
+  // launch; solve_setup returns how many clusters of that shape fit at once
+  // (0: the shape cannot run)
+  int (*solve)(const MxLaunch&, const void* image, SolveImage, SolveCtl*, double* res, double* partial, SolveShape);
+  int (*solve_setup)(int ndims, SolveShape);
 };
 
 struct Plugin {
@@ -146,7 +151,10 @@ struct Plugin {
 };
 
 constexpr int kMaxPlugins = 64;
-constexpr int kNormCells = 8;  // interior blocks per CTA of the mixed path's FP64 norm
+// interior blocks per partial sum of the mixed path's FP64 norm: one, so that
+// a one-launch solve spreads the finest level's residual over the whole
+// cluster (every group of 256 threads a few blocks)
+constexpr int kNormCells = 1;
 
 // registry (plugin.cu); a plugin file registers its FP64 part and, when it
 // has one, its mixed part from static initialisers

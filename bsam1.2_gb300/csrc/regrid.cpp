@@ -613,6 +613,10 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   std::memcpy(nh->root_xupper, H.root_xupper, sizeof(H.root_xupper));
   nh->tail_cells = H.tail_cells;  // tuning carries over
   nh->box_sweep = H.box_sweep;
+  nh->solve_mode = H.solve_mode;
+  nh->solve_shape = H.solve_shape;
+  nh->solve_solo_cells = H.solve_solo_cells;
+  nh->solve_tuned = H.solve_tuned;
   auto fail = [&](int rc) {
     bsamg_hier_destroy(nh);
     return rc;

@@ -348,6 +348,43 @@ INTERFACE
     INTEGER(C_LONG_LONG), VALUE:: cells
     INTEGER(C_INT):: status
   END FUNCTION
+  FUNCTION bsamg_set_solve(h, mode, ctas, threads, solo_cells) BIND(C, NAME='bsamg_set_solve') RESULT(status)
+    IMPORT
+    TYPE(C_PTR), VALUE:: h
+    INTEGER(C_INT), VALUE:: mode, ctas, threads
+    INTEGER(C_LONG_LONG), VALUE:: solo_cells
+    INTEGER(C_INT):: status
+  END FUNCTION
+  FUNCTION bsamg_get_solve(h, mode, ctas, threads, solo_cells) BIND(C, NAME='bsamg_get_solve') RESULT(status)
+    IMPORT
+    TYPE(C_PTR), VALUE:: h
+    INTEGER(C_INT):: mode, ctas, threads
+    INTEGER(C_LONG_LONG):: solo_cells
+    INTEGER(C_INT):: status
+  END FUNCTION
+  FUNCTION bsamg_solve_info(h, info, n) BIND(C, NAME='bsamg_solve_info') RESULT(status)
+    IMPORT
+    TYPE(C_PTR), VALUE:: h
+    INTEGER(C_LONG_LONG):: info(*)
+    INTEGER(C_INT), VALUE:: n
+    INTEGER(C_INT):: status
+  END FUNCTION
+  FUNCTION bsamg_solve_trace(h, enable) BIND(C, NAME='bsamg_solve_trace') RESULT(status)
+    IMPORT
+    TYPE(C_PTR), VALUE:: h
+    INTEGER(C_INT), VALUE:: enable
+    INTEGER(C_INT):: status
+  END FUNCTION
+  FUNCTION bsamg_solve_trace_read(h, cap, op, n, cycles, count) BIND(C, NAME='bsamg_solve_trace_read') &
+      RESULT(status)
+    IMPORT
+    TYPE(C_PTR), VALUE:: h
+    INTEGER(C_INT), VALUE:: cap
+    INTEGER(C_INT):: op(*), n(*)
+    INTEGER(C_LONG_LONG):: cycles(*)
+    INTEGER(C_INT):: count
+    INTEGER(C_INT):: status
+  END FUNCTION
   FUNCTION bsamg_mark(h, slot) BIND(C, NAME='bsamg_mark') RESULT(status)
     IMPORT
     TYPE(C_PTR), VALUE:: h

@@ -303,6 +303,40 @@ int bsamg_set_box_sweep(bsamg_hier* h, int kind);
  * when many hierarchies share the GPU.  0 disables.  Drops the hierarchy's
  * captured graphs. */
 int bsamg_set_tail_cells(bsamg_hier* h, long long cells);
+/* Tuning (no reference counterpart; replaces the loop of
+ * MultigridIterations, afasroutines.f90:78-104, and the ApplyOnLevel loops
+ * of AFASVcycle, :495-529, on the mixed path of adaptive hierarchies).
+ * mode 1 (the default): a mixed-mode solve whose finest level is above 0
+ * runs as ONE launch of one thread-block cluster -- every operation of
+ * every V-cycle, the FP64 residual and the exit test on the device -- with
+ * `ctas` CTAs of `threads` threads (ctas 1..16, threads 256, 512 or 1024;
+ * default 16 x 512); the levels from minlevel up to the highest one at
+ * which they hold at most `solo_cells` interior cells together run in one
+ * CTA of the cluster (default 2048; 0: none).  Same iterates, V-cycle
+ * counts and residuals, bit for bit, as mode 0, which launches every
+ * operation on its own from captured graphs.  BSAMG_ERR_UNSUPPORTED when the
+ * device cannot run a cluster of that shape.  The settings carry over to
+ * the hierarchies bsamg_regrid makes from this one. */
+int bsamg_set_solve(bsamg_hier* h, int mode, int ctas, int threads, long long solo_cells);
+int bsamg_get_solve(const bsamg_hier* h, int* mode, int* ctas, int* threads, long long* solo_cells);
+/* Profiling of the one-launch solve (no reference counterpart).  With the
+ * trace enabled, the next solves record CTA 0's clock (cycles of its SM)
+ * at the end of every phase of the program's prologue and first outer
+ * iteration; bsamg_solve_trace_read returns, for each of the `count` phases
+ * of the last traced solve (up to cap), its operation code (0-5 the FP32
+ * V-cycle's relax, restrict, ring, load, prolong, ghost; 8-15 clear, prep,
+ * update, FP64 FillDown, FP64 ghost, norm, finish, solo block), its work
+ * size (blocks, or ghost stages) and the cycles since the previous phase
+ * ended (a solo block's time is given on its last phase, 0 on the others). */
+int bsamg_solve_trace(bsamg_hier* h, int enable);
+/* The last one-launch solve program of the hierarchy: info[0] phases,
+ * [1] first phase of the loop body, [2] levels whose FP32 arrays it keeps in
+ * the cluster's distributed shared memory, [3] bytes of that data area per
+ * CTA, [4] bytes of the program image each CTA stages, [5] CTAs, [6]
+ * threads per CTA, [7] 1 when the last program was too large to stage (the
+ * per-launch path ran).  Up to n of the 8 values. */
+int bsamg_solve_info(const bsamg_hier* h, long long* info, int n);
+int bsamg_solve_trace_read(const bsamg_hier* h, int cap, int* op, int* n, long long* cycles, int* count);
 
 /* Timing support (no reference counterpart: measurement hooks).
  * bsamg_mark records CUDA event `slot` (0..63) on the hierarchy's stream;
