@@ -133,9 +133,13 @@ def lib():
         "bsamg_launch_count": ([P, ctypes.POINTER(ctypes.c_longlong)], I),
         "bsamg_set_tail_cells": ([P, ctypes.c_longlong], I),
         "bsamg_set_box_sweep": ([P, I], I),
-        "bsamg_set_solve": ([P, I, I, I, ctypes.c_longlong], I),
-        "bsamg_get_solve": ([P, IP, IP, IP, ctypes.POINTER(ctypes.c_longlong)], I),
+        "bsamg_set_solve": ([P, I, I, I, I, ctypes.c_longlong], I),
+        "bsamg_get_solve": ([P, IP, IP, IP, IP, ctypes.POINTER(ctypes.c_longlong)], I),
         "bsamg_solve_trace": ([P, I], I),
+        "bsamg_ctx_set_autotune": ([P, I], I),
+        "bsamg_tune_save": ([P, ctypes.c_char_p], I),
+        "bsamg_tune_load": ([P, ctypes.c_char_p], I),
+        "bsamg_tune_count": ([P, IP], I),
         "bsamg_solve_info": ([P, ctypes.POINTER(ctypes.c_longlong), I], I),
         "bsamg_solve_trace_read": ([P, I, IP, IP, ctypes.POINTER(ctypes.c_longlong), IP], I),
         "bsamg_graph_stats": ([P, IP, IP], I),
@@ -221,6 +225,24 @@ class Context:
     def set_blocking_wait(self, on=True):
         """Host waits sleep instead of spinning (bsamg_ctx_set_blocking_wait)."""
         _ck(lib().bsamg_ctx_set_blocking_wait(self.h, int(bool(on))), "bsamg_ctx_set_blocking_wait")
+
+    def set_autotune(self, on=True):
+        """The one-launch solve's autotuner on or off (bsamg_ctx_set_autotune)."""
+        _ck(lib().bsamg_ctx_set_autotune(self.h, int(bool(on))), "bsamg_ctx_set_autotune")
+
+    def tune_save(self, path):
+        """Write the autotuner's choices as JSON (bsamg_tune_save)."""
+        _ck(lib().bsamg_tune_save(self.h, str(path).encode()), "bsamg_tune_save")
+
+    def tune_load(self, path):
+        """Add the choices of a file written by tune_save (bsamg_tune_load)."""
+        _ck(lib().bsamg_tune_load(self.h, str(path).encode()), "bsamg_tune_load")
+
+    def tune_count(self):
+        """Size classes the autotuner has a choice for (bsamg_tune_count)."""
+        n = ctypes.c_int()
+        _ck(lib().bsamg_tune_count(self.h, ctypes.byref(n)), "bsamg_tune_count")
+        return n.value
 
     def close(self):
         if getattr(self, "h", None):
@@ -446,20 +468,21 @@ class Hierarchy:
         one thread block (bsamg_set_tail_cells; 0 disables)."""
         _ck(lib().bsamg_set_tail_cells(self.h, cells), "bsamg_set_tail_cells")
 
-    def set_solve(self, mode=1, ctas=16, threads=512, solo_cells=2048):
+    def set_solve(self, mode=1, ctas=16, threads=512, tile=64, solo_cells=8192):
         """How a mixed-mode solve of an adaptive hierarchy runs
         (bsamg_set_solve): mode 1 as one launch of a cluster of `ctas` CTAs
-        of `threads` threads, the levels holding at most `solo_cells` cells
-        together run by one CTA; mode 0 as separate launches from captured
-        graphs.  Both give the same iterates."""
-        _ck(lib().bsamg_set_solve(self.h, int(mode), int(ctas), int(threads), int(solo_cells)), "bsamg_set_solve")
+        of `threads` threads, work lists in tiles of `tile` units, the levels
+        holding at most `solo_cells` cells together run by one CTA; mode 0 as
+        separate launches from captured graphs.  Both give the same iterates."""
+        _ck(lib().bsamg_set_solve(self.h, int(mode), int(ctas), int(threads), int(tile), int(solo_cells)),
+            "bsamg_set_solve")
 
     def get_solve(self):
-        """(mode, ctas, threads, solo_cells) of bsamg_set_solve."""
-        m, c, t, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
-        _ck(lib().bsamg_get_solve(self.h, ctypes.byref(m), ctypes.byref(c), ctypes.byref(t), ctypes.byref(s)),
-            "bsamg_get_solve")
-        return m.value, c.value, t.value, s.value
+        """(mode, ctas, threads, tile, solo_cells) of bsamg_set_solve."""
+        m, c, t, g, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        _ck(lib().bsamg_get_solve(self.h, ctypes.byref(m), ctypes.byref(c), ctypes.byref(t), ctypes.byref(g),
+                                  ctypes.byref(s)), "bsamg_get_solve")
+        return m.value, c.value, t.value, g.value, s.value
 
     def solve_info(self):
         """dict of the last one-launch solve program (bsamg_solve_info)."""

@@ -31,6 +31,7 @@ UNITS = {
     "noalloc.cu": ["--fmad=false"],
     "mixed.cu": [],
     "box.cu": [],
+    "tune.cu": [],
     "hier.cu": [],
     "ghostc.cpp": [],
     "regrid.cpp": [],

@@ -590,23 +590,31 @@ int build_uniform(Hier& H, const int mx[3], int minlevel, const int mthbc[6], co
 
 
 
+}  // namespace
+
+namespace bsamg {
+long long kind_units(const Hier& H, const HostPatch& P, int kind) {
+  switch (kind) {
+    case kKindColor: return (long long)((P.mx[0] + 1) / 2) * P.mx[1] * P.mx[2];
+    case kKindInterior: return (long long)P.mx[0] * P.mx[1] * P.mx[2];
+    case kKindCoarse: return P.parent >= 0 ? (long long)P.cmx[0] * P.cmx[1] * P.cmx[2] : 0;
+    case kKindCGhost: return P.parent >= 0 ? (long long)P.cn[0] * P.cn[1] * P.cn[2] : 0;
+    case kKindFGhost: return (long long)P.qn[0] * P.qn[1] * P.qn[2];
+    case kKindProl: {  // coarse indices -gs..cmx+gs, gs = mbc - 1
+      int e = 2 * (H.mbc - 1) + 1;
+      return P.parent >= 0 ? (long long)(P.cmx[0] + e) * (P.cmx[1] + e) * (H.ndims == 3 ? P.cmx[2] + e : 1) : 0;
+    }
+  }
+  return 0;
+}
+}  // namespace bsamg
+
+namespace {
+
 int upload_blocks(Hier& H, LevelT& L, int kind) {
   std::vector<Blk> v;
   for (int p : L.patches) {
-    HostPatch& P = H.patches[p];
-    long long units = 0;
-    switch (kind) {
-      case kKindColor: units = (long long)((P.mx[0] + 1) / 2) * P.mx[1] * P.mx[2]; break;
-      case kKindInterior: units = (long long)P.mx[0] * P.mx[1] * P.mx[2]; break;
-      case kKindCoarse: units = P.parent >= 0 ? (long long)P.cmx[0] * P.cmx[1] * P.cmx[2] : 0; break;
-      case kKindCGhost: units = P.parent >= 0 ? (long long)P.cn[0] * P.cn[1] * P.cn[2] : 0; break;
-      case kKindFGhost: units = (long long)P.qn[0] * P.qn[1] * P.qn[2]; break;
-      case kKindProl: {  // coarse indices -gs..cmx+gs, gs = mbc - 1
-        int e = 2 * (H.mbc - 1) + 1;
-        units = P.parent >= 0 ? (long long)(P.cmx[0] + e) * (P.cmx[1] + e) * (H.ndims == 3 ? P.cmx[2] + e : 1) : 0;
-        break;
-      }
-    }
+    long long units = kind_units(H, H.patches[p], kind);
     for (long long s = 0; s < units; s += kBlock) v.push_back(Blk{p, (int)s});
   }
   L.nblk[kind] = (int)v.size();
@@ -1292,25 +1300,27 @@ int bsamg_set_tail_cells(bsamg_hier* h, long long cells) {
   return BSAMG_OK;
 }
 
-int bsamg_set_solve(bsamg_hier* h, int mode, int ctas, int threads, long long solo_cells) {
+int bsamg_set_solve(bsamg_hier* h, int mode, int ctas, int threads, int tile, long long solo_cells) {
   if (!h || (mode != 0 && mode != 1) || ctas < 1 || ctas > 16 || solo_cells < 0) return BSAMG_ERR_ARG;
   if (threads != 256 && threads != 512 && threads != 1024) return BSAMG_ERR_ARG;
+  if (tile != 32 && tile != 64 && tile != 128 && tile != 256) return BSAMG_ERR_ARG;
   int r = set_device(*h);
   if (r) return r;
-  if (mode == 1 && h->committed && h->fpool && !solve_shape_runs(*h, SolveShape{ctas, threads}))
+  if (mode == 1 && h->committed && h->fpool && !solve_shape_runs(*h, SolveShape{ctas, threads, tile}))
     return BSAMG_ERR_UNSUPPORTED;
   h->solve_mode = mode;
-  h->solve_shape = SolveShape{ctas, threads};
+  h->solve_shape = SolveShape{ctas, threads, tile};
   h->solve_solo_cells = solo_cells;
   h->solve_tuned = true;
   return BSAMG_OK;
 }
 
-int bsamg_get_solve(const bsamg_hier* h, int* mode, int* ctas, int* threads, long long* solo_cells) {
+int bsamg_get_solve(const bsamg_hier* h, int* mode, int* ctas, int* threads, int* tile, long long* solo_cells) {
   if (!h) return BSAMG_ERR_ARG;
   if (mode) *mode = h->solve_mode;
   if (ctas) *ctas = h->solve_shape.ctas;
   if (threads) *threads = h->solve_shape.threads;
+  if (tile) *tile = h->solve_shape.tile;
   if (solo_cells) *solo_cells = h->solve_solo_cells;
   return BSAMG_OK;
 }

@@ -109,9 +109,10 @@ struct Hier {
   // by one CTA; the recorded program of (finest, minlevel, nsmooth, solo
   // level) and the device control block (SolveCtl + residuals)
   int solve_mode = 1;
-  SolveShape solve_shape{16, 512};
-  long long solve_solo_cells = 2048;
-  bool solve_tuned = false;  // the shape came from the autotuner (or the caller)
+  SolveShape solve_shape{16, 512, 64};
+  long long solve_solo_cells = 8192;
+  bool solve_tuned = false;     // the caller set the shape (bsamg_set_solve): not tuned
+  bool solve_launches = false;  // the autotuner chose the per-launch path for this hierarchy
   void* solve_img = nullptr;  // program image (SolveImage layout)
   SolveImage solve_im{};
   bool solve_nofit = false;   // the program of solve_key is too large to stage
@@ -220,6 +221,8 @@ inline long long origin_of(const Hier& H, const int* n) {
   long long s = H.mbc - 1;
   return H.ndims == 2 ? s * (1 + n[0]) : s * (1 + n[0] + (long long)n[0] * n[1]);
 }
+// units of a level work list of this kind for patch P (blocks of kBlock units)
+long long kind_units(const Hier& H, const HostPatch& P, int kind);
 // AMR regrid of a committed hierarchy into a new one (regrid.cpp)
 int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* user, bsamg_hier** out);
 using GraphKey = std::tuple<int, int, int, int, int>;
@@ -246,6 +249,16 @@ struct bsamg_ctx {
   std::mutex mu;
   double* pinned = nullptr;     // pinned read-back words, one slot per hierarchy
   std::vector<int> free_slots;
+  // the one-launch solve's autotuner (tune.cu): on, and the launch shape it
+  // chose per size class of adaptive hierarchy (kept until the context
+  // ends; bsamg_tune_save / bsamg_tune_load persist it as JSON)
+  bool autotune = true;
+  struct Tuned {
+    int ctas, threads, tile;
+    long long solo_cells;
+    double us_per_cycle;
+  };
+  std::map<std::vector<int>, Tuned> tuned;
 };
 
 struct bsamg_hier : bsamg::Hier {};

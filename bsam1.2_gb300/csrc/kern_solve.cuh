@@ -57,12 +57,16 @@ constexpr double dB1 = 05.0 / 32.0, dB2 = 15.0 / 16.0, dB3 = -03.0 / 32.0;
 constexpr double dC1 = 09.0 / 16.0, dC2 = 03.0 / 16.0, dC3 = 03.0 / 16.0, dC4 = 01.0 / 16.0;
 
 // An FP64 ghost operation (the FP64 path's ghost_apply), each product and
-// sum rounded on its own in the same order.
+// sum rounded on its own in the same order.  The variable loop has the
+// plugin's constant bound: a runtime index into pp.qpo would place the
+// parameters in local memory, which every cluster barrier evicts from L1.
+template <int NV>
 __device__ __forceinline__ void s_ghost64(const PatchDev* __restrict__ P, double* pool, const GhostOp& g,
                                           const ProbParams& pp) {
   const PatchDev& d = P[g.dp];
   const PatchDev& s = P[g.sp];
-  for (int v = 0; v < pp.nrvars; v++) {
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
     double* dq = pool + d.oq + v * d.sq;
     const double* sq = pool + s.oq + v * s.sq;
     double val;
@@ -228,6 +232,7 @@ struct SolveRun {
   const int* spool;   // the image's stage pool
   const int* ppool;   // the image's part pool
   float* sdata;       // this CTA's FP32 data area (shared memory)
+  int lg;             // log2 of the units per tile of the FP32 work lists
   const GhostOp* sops;  // this CTA's FP32 ghost operations in shared memory, or null
   const GhostOp* gops;  // the same in global memory, from this CTA's segment on
   int rank, ctas;
@@ -243,15 +248,15 @@ struct SolveRun {
     const Blk* blk = bpool + f.blk;
     const int* pt = ppool + f.part;
     const int lo = cluster ? pt[rank] : pt[0], hi = cluster ? pt[rank + 1] : pt[ctas];
-    const int u = threadIdx.x & 255;
-    for (int b = lo + (int)(threadIdx.x >> 8); b < hi; b += T / 256) unit(blk[b], u);
+    const int u = threadIdx.x & ((1 << lg) - 1);
+    for (int b = lo + (int)(threadIdx.x >> lg); b < hi; b += T >> lg) unit(blk[b], u);
   }
 
   // one phase by the threads t0 = 0 .. nt-1 of the scope (the cluster, or
   // this CTA alone)
   __device__ __forceinline__ void exec(const SolvePhase& f, int t0, int nt, bool cluster,
                                        double (*red)[PL::kNV][kBlock / 32]) const {
-    const int nr = pp.nrvars;
+    constexpr int nr = PL::kNV;
     switch (f.op) {
       case kTRelax:
         owned(f, cluster, [&](const Blk& b, int u) { u_relax<PL, DIM, true>(P, fpool, b, u, f.arg, mp); });
@@ -293,7 +298,7 @@ struct SolveRun {
         for (int s = 0; s < f.nstages; s++) {
           for (int t = st[s] + t0; t < st[s + 1]; t += nt) {
             const GhostOp g = f.ops[t];
-            s_ghost64(P, pool, g, pp);
+            s_ghost64<PL::kNV>(P, pool, g, pp);
           }
           if (s + 1 < f.nstages) sync(cluster);
         }
@@ -363,12 +368,15 @@ __global__ void __launch_bounds__(T, 1)
                                reinterpret_cast<const int*>(simg + im.off_stage),
                                reinterpret_cast<const int*>(simg + im.off_part),
                                reinterpret_cast<float*>(solve_smem),
+                               im.tile_log2,
                                sops,
                                gops,
                                rank,
                                ctas};
   const int nt = ctas * T, t0 = rank * T + (int)threadIdx.x;
-  const int body = ctl->body, nph = ctl->nph, maxv = ctl->maxv;
+  const int body = ctl->body, nph = ctl->nph, maxv = ctl->maxv, errortype = ctl->errortype;
+  const double tol = ctl->tol, count = ctl->count;
+  __shared__ int stop;  // set by thread 0 after each finish
   long long* trace = (rank == 0 && threadIdx.x == 0) ? ctl->trace : nullptr;
   if (trace) trace[nph] = clock64();
   for (int it = 0; it <= maxv; it++) {
@@ -388,40 +396,43 @@ __global__ void __launch_bounds__(T, 1)
         continue;
       }
       if (f.op == kSFinish) {
-        if (rank == 0) {
-          double sum, comp[NV];
-          s_finish<NV, T>(partial, f.n, tv, r2, &sum, comp);
-          if (threadIdx.x == 0) {
-            double r;
-            const double count = ctl->count;
-            if (ctl->errortype == 1) {
-              r = sqrt(sum / count);  // ErrorAFAS, afasroutines.f90:135
-            } else {
-              double cells = count / NV;
-              r = sqrt(comp[0] / cells);
-              for (int v = 1; v < NV; v++) {  // MAXVAL of the component errors, :146-153
-                double e = sqrt(comp[v] / cells);
-                r = e > r ? e : r;
-              }
+        // every CTA sums the partials in the same order and takes the same
+        // decision; CTA 0 records it
+        double sum, comp[NV];
+        s_finish<NV, T>(partial, f.n, tv, r2, &sum, comp);
+        if (threadIdx.x == 0) {
+          double r;
+          if (errortype == 1) {
+            r = sqrt(sum / count);  // ErrorAFAS, afasroutines.f90:135
+          } else {
+            double cells = count / NV;
+            r = sqrt(comp[0] / cells);
+            for (int v = 1; v < NV; v++) {  // MAXVAL of the component errors, :146-153
+              double e = sqrt(comp[v] / cells);
+              r = e > r ? e : r;
             }
-            const bool nonfinite = !isfinite(r);
-            const bool conv = !nonfinite && r < ctl->tol;
+          }
+          const bool nonfinite = !isfinite(r);
+          const bool conv = !nonfinite && r < tol;
+          stop = conv || nonfinite || it == maxv;
+          if (rank == 0) {
             if (!nonfinite) res[it - 1] = r;
             ctl->norm[0] = r;
             ctl->norm[1] = sum;
             ctl->ncycles = it;
             ctl->converged = conv;
             ctl->nonfinite = nonfinite;
-            ctl->stop = conv || nonfinite || it == maxv;
+            ctl->stop = stop;
           }
         }
+        __syncthreads();
       } else {
         R.exec(f, t0, nt, true, red);
       }
       if (f.bar) cluster_barrier();
       if (trace && it <= 1) trace[x] = clock64();
     }
-    if (it > 0 && *(volatile int*)&ctl->stop) break;
+    if (it > 0 && stop) break;
   }
 }
 

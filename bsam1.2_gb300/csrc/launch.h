@@ -89,6 +89,7 @@ struct SolveImage {
   // part pool at off_seg); when ops_smem, each CTA stages its own after its
   // data area (ops bytes reserved per CTA)
   int seg, ops_smem, ops;
+  int tile_log2;  // FP32 work lists are split into tiles of 2^tile_log2 units (at most 256)
 };
 constexpr int kSolveSmemMax = 192 * 1024;  // largest image a solve stages
 // Control block of a solve launch (device memory); the residual of V-cycle
@@ -110,6 +111,7 @@ struct SolveCtl {
 // launch shape of the solve kernel: CTAs in the cluster, threads per CTA
 struct SolveShape {
   int ctas, threads;
+  int tile;  // units per tile of the FP32 work lists (32, 64, 128 or 256)
 };
 
 // A contiguous run of pool elements staged in shared memory by a tail

@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -84,6 +85,17 @@ __global__ void __launch_bounds__(kBlock) k_ghost32_program(const PatchDev* __re
     }
     __syncthreads();
   }
+}
+
+// the one-launch solve's FP32 ghost operations in CTA order: out[i] =
+// operation (ref & 0xfffff) of program (ref >> 20)
+__global__ void __launch_bounds__(kBlock) k_gather_ops(const GhostOp* const* __restrict__ base,
+                                                       const unsigned* __restrict__ ref, int n,
+                                                       GhostOp* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned r = ref[i];
+  out[i] = base[r >> 20][r & 0xfffffu];
 }
 
 // ---------------------------------------------------------------------------
@@ -404,6 +416,7 @@ int solve_norm_groups(const Hier& H, int finest) {
 // asked once per device, plugin, dimension and shape
 int solve_fit(const Hier& H, SolveShape sh) {
   if (sh.ctas < 1 || sh.ctas > 16 || (sh.threads != 256 && sh.threads != 512 && sh.threads != 1024)) return 0;
+  if (sh.tile != 32 && sh.tile != 64 && sh.tile != 128 && sh.tile != 256) return 0;
   static std::mutex mu;
   static std::map<std::tuple<int, int, int, int, int>, int> fit;
   auto key = std::make_tuple(H.ctx->device, H.problem, H.ndims, sh.ctas, sh.threads);
@@ -418,7 +431,7 @@ int solve_fit(const Hier& H, SolveShape sh) {
   return n;
 }
 
-bool solve_applies(const Hier& H, int finest) {
+bool solve_applies_(const Hier& H, int finest) {
   return H.solve_mode == 1 && !H.box && H.fpool && finest >= 1 && solve_norm_groups(H, finest) <= 2048 &&
          solve_norm_groups(H, finest) <= H.partial_cap && solve_fit(H, H.solve_shape) > 0;
 }
@@ -430,31 +443,42 @@ struct SolveBuild {
   std::vector<SolvePhase> prog;
   std::vector<Blk> bpool;
   std::vector<int> spool, ppool;
-  std::vector<std::vector<GhostOp>> ops;  // per CTA
+  std::vector<std::vector<unsigned>> ops;  // per CTA: program << 20 | operation of the FP32 ghost programs
+  std::vector<const GhostOp*> progs;       // the programs' device operation arrays
   std::vector<size_t> clears;             // phases whose shared-memory ranges follow the layout
   int body = 0, bad = 0;
 };
 
+// size_only: the pools get their final sizes but the ghost operations are
+// not distributed (the image's size depends on neither)
 int solve_record(Hier& H, int finest, int minlevel, int nsmooth, int solo, int C, const std::vector<int>& owner,
-                 const std::vector<char>& dsm, SolveBuild& B) {
+                 const std::vector<char>& dsm, bool size_only, SolveBuild& B) {
   B = SolveBuild();
   B.ops.assign(C, {});
   // the host copies behind the device lists and ghost programs the schedule
   // functions record
   std::map<const Blk*, const std::vector<Blk>*> lists;
+  std::map<const Blk*, int> kinds;
   std::map<const int*, const std::vector<int>*> stages;
   std::map<const GhostOp*, const GhostProg*> progs;
   for (int l = H.minlevel; l <= H.maxlevel; l++) {
     LevelT& L = H.L(l);
     for (int k = 0; k < kNKind; k++)
-      if (L.d_blk[k]) lists[L.d_blk[k]] = &L.h_blk[k];
+      if (L.d_blk[k]) {
+        lists[L.d_blk[k]] = &L.h_blk[k];
+        kinds[L.d_blk[k]] = k;
+      }
     for (int ip = 0; ip < 3; ip++) {
       if (L.gp[ip].d_stage_off) stages[L.gp[ip].d_stage_off] = &L.gp[ip].stage_off;
       if (L.gp[ip].d_ops) progs[L.gp[ip].d_ops] = &L.gp[ip];
     }
     if (H.mx_norm_blk[l + kMaxDepth]) lists[H.mx_norm_blk[l + kMaxDepth]] = &H.h_mx_norm_blk[l + kMaxDepth];
   }
-  if (H.mx_prep_coarse) lists[H.mx_prep_coarse] = &H.h_mx_prep_coarse;
+  if (H.mx_prep_coarse) {
+    lists[H.mx_prep_coarse] = &H.h_mx_prep_coarse;
+    kinds[H.mx_prep_coarse] = kKindInterior;
+  }
+  const int tile = H.solve_shape.tile;
   // the CTA that works on a block or ghost operation of patch p (the i-th of
   // its list or stage): CTA 0 for the levels it runs alone, the owner for
   // arrays in shared memory, else the CTAs in turn
@@ -490,8 +514,21 @@ int solve_record(Hier& H, int finest, int minlevel, int nsmooth, int solo, int C
     if (it != poff.end()) return it->second;
     const std::vector<Blk>* v = host_list(d);
     if (!v) return std::make_pair(0, -1);
+    // each block of kBlock units as tiles of `tile` units (up to the list's
+    // end for its patch), so that the small patches of an adaptive level do
+    // not leave most of a block's threads idle
+    auto kd = kinds.find(d);
+    if (kd == kinds.end()) {
+      B.bad = 1;
+      return std::make_pair(0, -1);
+    }
     std::vector<std::vector<Blk>> by(C);
-    for (size_t i = 0; i < v->size(); i++) by[sched((*v)[i].patch, (int)i)].push_back((*v)[i]);
+    for (size_t i = 0; i < v->size(); i++) {
+      const Blk bb = (*v)[i];
+      long long end = std::min<long long>(bb.start + kBlock, kind_units(H, H.patches[bb.patch], kd->second));
+      int q = sched(bb.patch, (int)i);
+      for (long long t = bb.start; t < end; t += tile) by[q].push_back(Blk{bb.patch, (int)t});
+    }
     int at = (int)B.bpool.size(), pt = (int)B.ppool.size();
     for (int r = 0; r < C; r++) {
       B.ppool.push_back((int)(B.bpool.size() - at));
@@ -524,10 +561,21 @@ int solve_record(Hier& H, int finest, int minlevel, int nsmooth, int solo, int C
     const GhostProg& G = *h->second;
     int at = (int)B.spool.size();
     int ns = (int)G.stage_off.size() - 1;
+    if (size_only) {
+      B.spool.insert(B.spool.end(), 2 * C * ns, 0);
+      return goff[d] = at;
+    }
+    const unsigned pid = (unsigned)B.progs.size();
+    if (pid >= 4096 || G.ops.size() >= (1u << 20)) {  // beyond the references' fields
+      B.bad = 2;
+      return 0;
+    }
+    B.progs.push_back(d);
+    std::vector<std::vector<unsigned>> by(C);
     for (int st = 0; st < ns; st++) {
-      std::vector<std::vector<GhostOp>> by(C);
+      for (auto& v : by) v.clear();
       for (int i = G.stage_off[st]; i < G.stage_off[st + 1]; i++)
-        by[sched(G.ops[i].dp, i - G.stage_off[st])].push_back(G.ops[i]);
+        by[sched(G.ops[i].dp, i - G.stage_off[st])].push_back(pid << 20 | (unsigned)i);
       for (int r = 0; r < C; r++) {  // (first, end) in CTA r's own operation list
         B.spool.push_back((int)B.ops[r].size());
         B.ops[r].insert(B.ops[r].end(), by[r].begin(), by[r].end());
@@ -639,14 +687,16 @@ int solve_record(Hier& H, int finest, int minlevel, int nsmooth, int solo, int C
   for (int level = 1; level <= finest; level++)
     if ((r = record([&] { return enq_set_ghost(H, level, 0); }, true))) return r;
   push_fp64(kSNorm, 0, nb, nlist, 1);
-  push_fp64(kSFinish, 0, nb, nullptr, 1);
-  return B.bad ? BSAMG_ERR_ARG : BSAMG_OK;  // a recorded list without a host copy is not expected
+  push_fp64(kSFinish, 0, nb, nullptr, 0);  // every CTA decides alone
+  // 2: too many ghost programs or operations for the one-launch solve;
+  // 1: a recorded list without a host copy (not expected)
+  return B.bad == 2 ? BSAMG_ERR_UNSUPPORTED : B.bad ? BSAMG_ERR_ARG : BSAMG_OK;
 }
 
 int solve_build(Hier& H, int finest, int minlevel, int nsmooth) {
   const int C = H.solve_shape.ctas;
   const int solo = solo_level(H, H.solve_solo_cells);
-  auto key = std::make_tuple(finest, minlevel, nsmooth, solo, C);
+  auto key = std::make_tuple(finest, minlevel, nsmooth, solo, C * 4096 + H.solve_shape.tile);
   if (H.solve_key == key && (H.solve_img || H.solve_nofit)) return H.solve_img ? BSAMG_OK : BSAMG_ERR_UNSUPPORTED;
   const int np = (int)H.patches.size();
   auto cells = [&](int p) {
@@ -687,7 +737,14 @@ int solve_build(Hier& H, int finest, int minlevel, int nsmooth) {
   // image), then record the final program
   std::vector<char> dsm(np, 0);
   SolveBuild B;
-  int r = solve_record(H, finest, minlevel, nsmooth, solo, C, owner, dsm, B);
+  int r = solve_record(H, finest, minlevel, nsmooth, solo, C, owner, dsm, true, B);
+  auto no_fit = [&] {  // the per-launch path runs this hierarchy
+    solve_invalidate(H);
+    H.solve_key = key;
+    H.solve_nofit = true;
+    return BSAMG_ERR_UNSUPPORTED;
+  };
+  if (r == BSAMG_ERR_UNSUPPORTED) return no_fit();
   if (r) return r;
   auto al16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
   SolveImage im{};
@@ -701,12 +758,7 @@ int solve_build(Hier& H, int finest, int minlevel, int nsmooth) {
   im.off_part = (int)o;
   o = al16(o + sizeof(int) * (B.ppool.size() + C + 1));  // + the CTAs' operation segments
   im.bytes = (int)o;
-  if (o > (size_t)kSolveSmemMax) {  // too large to stage: the per-launch path runs this hierarchy
-    solve_invalidate(H);
-    H.solve_key = key;
-    H.solve_nofit = true;
-    return BSAMG_ERR_UNSUPPORTED;
-  }
+  if (o > (size_t)kSolveSmemMax) return no_fit();  // too large to stage
   const long long budget = ((long long)kSolveSmemMax - (long long)o) / 4;
   std::vector<long long> mem(C, 0);
   int dsm_levels = 0;
@@ -720,7 +772,8 @@ int solve_build(Hier& H, int finest, int minlevel, int nsmooth) {
     for (int p : H.L(l).patches) dsm[p] = 1;
     dsm_levels++;
   }
-  if ((r = solve_record(H, finest, minlevel, nsmooth, solo, C, owner, dsm, B))) return r;
+  if ((r = solve_record(H, finest, minlevel, nsmooth, solo, C, owner, dsm, false, B)))
+    return r == BSAMG_ERR_UNSUPPORTED ? no_fit() : r;
   // each CTA's data area: e of its levels >= 0, e of its levels < 0, then
   // ec, g and the base planes
   std::vector<PatchDev> table = H.hP;
@@ -762,24 +815,40 @@ int solve_build(Hier& H, int finest, int minlevel, int nsmooth) {
   // the FP32 ghost operations, CTA after CTA; each CTA stages its own in
   // shared memory when every CTA's fit in what the data area leaves
   im.seg = (int)B.ppool.size();
-  std::vector<GhostOp> sops;
+  std::vector<unsigned> perm;  // the operations CTA after CTA, as references into their programs
   size_t opmax = 0;
   for (int q = 0; q < C; q++) {
-    B.ppool.push_back((int)sops.size());
-    sops.insert(sops.end(), B.ops[q].begin(), B.ops[q].end());
+    B.ppool.push_back((int)perm.size());
+    perm.insert(perm.end(), B.ops[q].begin(), B.ops[q].end());
     opmax = std::max(opmax, B.ops[q].size());
   }
-  B.ppool.push_back((int)sops.size());
+  B.ppool.push_back((int)perm.size());
   im.ops = (int)al16(sizeof(GhostOp) * opmax);
+  im.tile_log2 = 0;
+  while ((1 << im.tile_log2) < H.solve_shape.tile) im.tile_log2++;
   im.ops_smem = (size_t)im.data + im.ops + o <= (size_t)kSolveSmemMax ? 1 : 0;
   if (!im.ops_smem) im.ops = 0;
   if (H.solve_ops) cudaFreeAsync(H.solve_ops, H.s);
   H.solve_ops = nullptr;
-  if (!sops.empty()) {
-    cudaError_t e = dev_alloc(H, (void**)&H.solve_ops, sizeof(GhostOp) * sops.size());
+  if (!perm.empty()) {  // gathered on the device from the programs' own arrays
+    size_t nperm = perm.size(), np8 = B.progs.size();
+    void* tmp = nullptr;
+    cudaError_t e = dev_alloc(H, (void**)&H.solve_ops, sizeof(GhostOp) * nperm);
+    // the programs' base pointers first (8-byte aligned), then the references
+    if (e == cudaSuccess) e = dev_alloc(H, &tmp, sizeof(void*) * np8 + sizeof(unsigned) * nperm);
+    const GhostOp** dbase = static_cast<const GhostOp**>(tmp);
+    unsigned* dperm = reinterpret_cast<unsigned*>(dbase + np8);
     if (e == cudaSuccess)  // staged from pageable memory before it returns
-      e = cudaMemcpyAsync(H.solve_ops, sops.data(), sizeof(GhostOp) * sops.size(), cudaMemcpyHostToDevice, H.s);
-    if (e != cudaSuccess) return cuda_fail(e, "solve ghost operations upload");
+      e = cudaMemcpyAsync(dperm, perm.data(), sizeof(unsigned) * nperm, cudaMemcpyHostToDevice, H.s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dbase, B.progs.data(), sizeof(void*) * np8, cudaMemcpyHostToDevice, H.s);
+    if (e == cudaSuccess) {
+      k_gather_ops<<<(unsigned)((nperm + kBlock - 1) / kBlock), kBlock, 0, H.s>>>(dbase, dperm, (int)nperm,
+                                                                                 H.solve_ops);
+      e = cudaGetLastError();
+    }
+    if (tmp) cudaFreeAsync(tmp, H.s);
+    if (e != cudaSuccess) return cuda_fail(e, "solve ghost operations");
   }
   for (SolvePhase& f : B.prog)
     if (f.op == kTGhost) f.ops = H.solve_ops;
@@ -805,10 +874,8 @@ int solve_build(Hier& H, int finest, int minlevel, int nsmooth) {
   return BSAMG_OK;
 }
 
-int solve_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,
-                     int strict, int* ncycles, double* residuals) {
-  int r = solve_build(H, finest, minlevel, nsmooth);
-  if (r) return r;
+// upload the control block and launch the program built for this hierarchy
+int solve_launch(Hier& H, int finest, int maxvcycles, double tol, int errortype) {
   if (H.solve_ctl_cap < maxvcycles) {
     if (H.solve_ctl) cudaFreeAsync(H.solve_ctl, H.s);
     H.solve_ctl = nullptr;
@@ -846,16 +913,26 @@ int solve_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcyc
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(solve control)");
   if (mxp(H).solve(mxl(H), H.solve_img, H.solve_im, ctl, res, H.d_partial, H.solve_shape) < 0)
     return cuda_fail(cudaGetLastError(), "solve launch");
-  if ((r = after_launch(H, 1))) return r;
+  return after_launch(H, 1);
+}
+
+int solve_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,
+                     int strict, int* ncycles, double* residuals) {
+  int r;
+  if ((r = solve_build(H, finest, minlevel, nsmooth))) return r;
+  if ((r = solve_launch(H, finest, maxvcycles, tol, errortype))) return r;
   if ((r = stream_wait(H))) return r;
+  SolveCtl* ctl = static_cast<SolveCtl*>(H.solve_ctl);
+  cudaError_t e;
   std::vector<unsigned char> out(sizeof(SolveCtl) + sizeof(double) * (size_t)maxvcycles);
   e = cudaMemcpy(out.data(), ctl, out.size(), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(solve control)");
   SolveCtl o;
   std::memcpy(&o, out.data(), sizeof(o));
-  if (c.trace) {
+  if (H.solve_trace_on && H.solve_trace) {
     H.solve_trace_h.assign(H.solve_nph + 1, 0);
-    e = cudaMemcpy(H.solve_trace_h.data(), c.trace, sizeof(long long) * (H.solve_nph + 1), cudaMemcpyDeviceToHost);
+    e = cudaMemcpy(H.solve_trace_h.data(), H.solve_trace, sizeof(long long) * (H.solve_nph + 1),
+                   cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(solve trace)");
     std::vector<SolvePhase> ph(H.solve_nph);
     e = cudaMemcpy(ph.data(), H.solve_img, sizeof(SolvePhase) * H.solve_nph, cudaMemcpyDeviceToHost);
@@ -1010,6 +1087,19 @@ void solve_invalidate(Hier& H) {
 
 bool solve_shape_runs(const Hier& H, SolveShape sh) { return has_mixed(H) && solve_fit(H, sh) > 0; }
 
+bool solve_applies(const Hier& H, int finest) { return solve_applies_(H, finest); }
+
+int solve_time_one_cycle(Hier& H, int finest, int minlevel, int nsmooth, int errortype, double* ms) {
+  int r = solve_build(H, finest, minlevel, nsmooth);
+  if (r) return r;
+  if ((r = stream_wait(H))) return r;
+  auto t0 = std::chrono::steady_clock::now();
+  if ((r = solve_launch(H, finest, 1, 0.0, errortype))) return r;
+  if ((r = stream_wait(H))) return r;
+  *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return BSAMG_OK;
+}
+
 int mixed_enq_relax(Hier& H, int level, int ipass) {
   if (!has_mixed(H) || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
   if (H.box) return box_enq_relax(H, level, ipass);
@@ -1020,8 +1110,13 @@ int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcyc
                      int strict, int* ncycles, double* residuals) {
   if (!has_mixed(H) || !H.fpool) return BSAMG_ERR_UNSUPPORTED;
   if (solve_applies(H, finest)) {
-    int rs = solve_iterations(H, finest, minlevel, nsmooth, maxvcycles, tol, errortype, strict, ncycles, residuals);
-    if (rs != BSAMG_ERR_UNSUPPORTED) return rs;  // else its program is too large to stage: per-launch path
+    // the autotuner may choose the shape, or the per-launch path
+    int rs = !H.solve_tuned && H.ctx->autotune ? solve_autotune(H, finest, minlevel, nsmooth, errortype) : 0;
+    if (rs) return rs;
+    if (!H.solve_launches) {
+      rs = solve_iterations(H, finest, minlevel, nsmooth, maxvcycles, tol, errortype, strict, ncycles, residuals);
+      if (rs != BSAMG_ERR_UNSUPPORTED) return rs;  // else its program is too large to stage: per-launch path
+    }
   }
   // the first outer iteration takes its right-hand side from the FP64
   // residual of the finest level

@@ -20,6 +20,13 @@ int mixed_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcyc
 // the highest one at which the cumulative interior cell count is at most
 // `cells` run inside one CTA (0 disables)
 void set_tail(Hier& H, long long cells);
+// one outer iteration of the one-launch solve in the current shape, timed
+// with CUDA events on the hierarchy's stream (ms); changes q
+int solve_time_one_cycle(Hier& H, int finest, int minlevel, int nsmooth, int errortype, double* ms);
+bool solve_applies(const Hier& H, int finest);
+// the autotuner (tune.cu): the shape of the one-launch solve for this
+// hierarchy's size class, from the context's cache or measured now
+int solve_autotune(Hier& H, int finest, int minlevel, int nsmooth, int errortype);
 // drop the one-launch solve's program image (rebuilt on its next use)
 void solve_invalidate(Hier& H);
 // whether the device runs the one-launch solve's cluster in this shape

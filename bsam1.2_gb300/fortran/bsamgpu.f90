@@ -348,17 +348,19 @@ INTERFACE
     INTEGER(C_LONG_LONG), VALUE:: cells
     INTEGER(C_INT):: status
   END FUNCTION
-  FUNCTION bsamg_set_solve(h, mode, ctas, threads, solo_cells) BIND(C, NAME='bsamg_set_solve') RESULT(status)
+  FUNCTION bsamg_set_solve(h, mode, ctas, threads, tile, solo_cells) BIND(C, NAME='bsamg_set_solve') &
+      RESULT(status)
     IMPORT
     TYPE(C_PTR), VALUE:: h
-    INTEGER(C_INT), VALUE:: mode, ctas, threads
+    INTEGER(C_INT), VALUE:: mode, ctas, threads, tile
     INTEGER(C_LONG_LONG), VALUE:: solo_cells
     INTEGER(C_INT):: status
   END FUNCTION
-  FUNCTION bsamg_get_solve(h, mode, ctas, threads, solo_cells) BIND(C, NAME='bsamg_get_solve') RESULT(status)
+  FUNCTION bsamg_get_solve(h, mode, ctas, threads, tile, solo_cells) BIND(C, NAME='bsamg_get_solve') &
+      RESULT(status)
     IMPORT
     TYPE(C_PTR), VALUE:: h
-    INTEGER(C_INT):: mode, ctas, threads
+    INTEGER(C_INT):: mode, ctas, threads, tile
     INTEGER(C_LONG_LONG):: solo_cells
     INTEGER(C_INT):: status
   END FUNCTION
@@ -367,6 +369,30 @@ INTERFACE
     TYPE(C_PTR), VALUE:: h
     INTEGER(C_LONG_LONG):: info(*)
     INTEGER(C_INT), VALUE:: n
+    INTEGER(C_INT):: status
+  END FUNCTION
+  FUNCTION bsamg_ctx_set_autotune(ctx, on) BIND(C, NAME='bsamg_ctx_set_autotune') RESULT(status)
+    IMPORT
+    TYPE(C_PTR), VALUE:: ctx
+    INTEGER(C_INT), VALUE:: on
+    INTEGER(C_INT):: status
+  END FUNCTION
+  FUNCTION bsamg_tune_save(ctx, path) BIND(C, NAME='bsamg_tune_save') RESULT(status)
+    IMPORT
+    TYPE(C_PTR), VALUE:: ctx
+    CHARACTER(KIND=C_CHAR):: path(*)
+    INTEGER(C_INT):: status
+  END FUNCTION
+  FUNCTION bsamg_tune_load(ctx, path) BIND(C, NAME='bsamg_tune_load') RESULT(status)
+    IMPORT
+    TYPE(C_PTR), VALUE:: ctx
+    CHARACTER(KIND=C_CHAR):: path(*)
+    INTEGER(C_INT):: status
+  END FUNCTION
+  FUNCTION bsamg_tune_count(ctx, n) BIND(C, NAME='bsamg_tune_count') RESULT(status)
+    IMPORT
+    TYPE(C_PTR), VALUE:: ctx
+    INTEGER(C_INT):: n
     INTEGER(C_INT):: status
   END FUNCTION
   FUNCTION bsamg_solve_trace(h, enable) BIND(C, NAME='bsamg_solve_trace') RESULT(status)

@@ -178,6 +178,9 @@ class Server:
             try:
                 h.commit()
                 h.set_tail_cells(self.tail_cells)
+                # one-launch solves in clusters of 8 CTAs (several requests
+                # share the GPU at once), not tuned per request
+                h.set_solve(1, 8, 512, 64, 8192)
                 return h, pats, minlevel
             except BsamgError as e:
                 h.close()

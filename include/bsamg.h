@@ -309,16 +309,19 @@ int bsamg_set_tail_cells(bsamg_hier* h, long long cells);
  * mode 1 (the default): a mixed-mode solve whose finest level is above 0
  * runs as ONE launch of one thread-block cluster -- every operation of
  * every V-cycle, the FP64 residual and the exit test on the device -- with
- * `ctas` CTAs of `threads` threads (ctas 1..16, threads 256, 512 or 1024;
- * default 16 x 512); the levels from minlevel up to the highest one at
+ * `ctas` CTAs of `threads` threads (ctas 1..16, threads 256, 512 or 1024),
+ * the FP32 work lists cut into tiles of `tile` units (32, 64, 128 or 256:
+ * a tile is the work of one group of `tile` threads, so small patches keep
+ * few threads idle); the levels from minlevel up to the highest one at
  * which they hold at most `solo_cells` interior cells together run in one
- * CTA of the cluster (default 2048; 0: none).  Same iterates, V-cycle
- * counts and residuals, bit for bit, as mode 0, which launches every
- * operation on its own from captured graphs.  BSAMG_ERR_UNSUPPORTED when the
- * device cannot run a cluster of that shape.  The settings carry over to
- * the hierarchies bsamg_regrid makes from this one. */
-int bsamg_set_solve(bsamg_hier* h, int mode, int ctas, int threads, long long solo_cells);
-int bsamg_get_solve(const bsamg_hier* h, int* mode, int* ctas, int* threads, long long* solo_cells);
+ * CTA of the cluster (0: none).  Defaults 16 x 512, tiles of 64, 8192
+ * cells.  Same iterates, V-cycle counts and residuals, bit for bit, as
+ * mode 0, which launches every operation on its own from captured graphs.
+ * BSAMG_ERR_UNSUPPORTED when the device cannot run a cluster of that
+ * shape.  The settings carry over to the hierarchies bsamg_regrid makes
+ * from this one. */
+int bsamg_set_solve(bsamg_hier* h, int mode, int ctas, int threads, int tile, long long solo_cells);
+int bsamg_get_solve(const bsamg_hier* h, int* mode, int* ctas, int* threads, int* tile, long long* solo_cells);
 /* Profiling of the one-launch solve (no reference counterpart).  With the
  * trace enabled, the next solves record CTA 0's clock (cycles of its SM)
  * at the end of every phase of the program's prologue and first outer
@@ -336,6 +339,24 @@ int bsamg_solve_trace(bsamg_hier* h, int enable);
  * threads per CTA, [7] 1 when the last program was too large to stage (the
  * per-launch path ran).  Up to n of the 8 values. */
 int bsamg_solve_info(const bsamg_hier* h, long long* info, int n);
+/* Autotuner of the mixed solve of adaptive hierarchies (no reference
+ * counterpart).  While on (the default), the first mixed solve of an
+ * adaptive hierarchy whose size class (plugin, dimension, variables, levels
+ * in the V-cycle, binary order of magnitude of the cells on levels >= 0)
+ * the context has not seen times one V-cycle of each candidate -- the
+ * per-launch path, and the one-launch solve with 16 CTAs of 256, 512 or
+ * 1024 threads, tiles of 32, 64 or 128 units and 2048 or 8192 cells run by
+ * one CTA -- each from the same q, which it restores: the solve's result is
+ * unchanged.  The fastest is used and kept in the context for that class; a
+ * hierarchy whose shape was set by bsamg_set_solve is not tuned.
+ * bsamg_tune_save writes the context's choices as JSON (ctas 0: the
+ * per-launch path), bsamg_tune_load adds those of a file written by it
+ * (BSAMG_ERR_IO for anything else), bsamg_tune_count returns how many
+ * classes the context holds. */
+int bsamg_ctx_set_autotune(bsamg_ctx* ctx, int on);
+int bsamg_tune_save(bsamg_ctx* ctx, const char* path);
+int bsamg_tune_load(bsamg_ctx* ctx, const char* path);
+int bsamg_tune_count(const bsamg_ctx* ctx, int* n);
 int bsamg_solve_trace_read(const bsamg_hier* h, int cap, int* op, int* n, long long* cycles, int* count);
 
 /* Timing support (no reference counterpart: measurement hooks).

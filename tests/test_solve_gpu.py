@@ -18,11 +18,11 @@ from tests.test_parity_gpu import CH2, CH3
 pytestmark = pytest.mark.gpu
 
 SHAPES = [
-    (16, 512, 2048),   # the default
-    (16, 1024, 0),     # every level cluster-wide
-    (8, 256, 1 << 30),  # the whole V-cycle in CTA 0
-    (1, 512, 2048),    # a cluster of one CTA
-    (4, 1024, 512),
+    (16, 512, 64, 8192),    # the default
+    (16, 1024, 256, 0),     # every level cluster-wide, whole blocks
+    (8, 256, 32, 1 << 30),  # the whole V-cycle in CTA 0
+    (1, 512, 128, 2048),    # a cluster of one CTA
+    (4, 1024, 64, 512),
 ]
 
 
@@ -60,7 +60,7 @@ CASES = {
 
 
 @pytest.mark.parametrize("case", list(CASES))
-@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: f"{s[0]}x{s[1]}-solo{s[2]}")
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: f"{s[0]}x{s[1]}-tile{s[2]}-solo{s[3]}")
 def test_cluster_solve_is_bit_identical(pkg, ctx, case, shape):
     cfg, mk, tol = CASES[case]
     spec = mk()
@@ -149,9 +149,57 @@ def test_cluster_solve_limits(pkg, ctx):
         with pytest.raises(pkg.BsamgError):
             h.time_step(False, fin, mn, 2, 2, 1e-14, mode="mixed", strict=True)
     with pytest.raises(pkg.BsamgError):
-        b.set_solve(1, 17, 512, 0)
+        b.set_solve(1, 17, 512, 64, 0)
     with pytest.raises(pkg.BsamgError):
-        b.set_solve(1, 8, 384, 0)
+        b.set_solve(1, 8, 384, 64, 0)
+    with pytest.raises(pkg.BsamgError):
+        b.set_solve(1, 8, 512, 48, 0)
     _same_state(a, b, spec.patches)
     a.close()
     b.close()
+
+
+def test_autotuned_solve(pkg, tmp_path):
+    """The autotuner (a fresh context, tuning on): the first solve of a size
+    class times the candidate shapes from the same q and restores it, so the
+    iterates equal the per-launch path's bit for bit; the choice is kept for
+    the class, reused by a regridded hierarchy of the same class, and
+    survives a JSON round trip."""
+    import json
+
+    ctx = pkg.Context(0)
+    try:
+        spec = H.amr2d(periodic=True)
+        a, b = _ch_pair(pkg, ctx, CH2, spec)
+        a.set_solve(0)
+        fin, mn = spec.finest(), spec.minlevel()
+        assert ctx.tune_count() == 0
+        ha = _steps(a, fin, mn, "mixed", 1e-9)
+        hb = _steps(b, fin, mn, "mixed", 1e-9)
+        assert ha == hb
+        _same_state(a, b, spec.patches)
+        assert ctx.tune_count() == 1
+        mode, ctas, threads, tile, solo = b.get_solve()
+        path = tmp_path / "tune.json"
+        ctx.tune_save(path)
+        doc = json.loads(path.read_text())
+        assert len(doc["entries"]) == 1
+        e = doc["entries"][0]
+        assert e["ctas"] in (0, 16) and e["us_per_cycle"] > 0  # 0: the per-launch path won
+        if e["ctas"]:
+            assert mode == 1 and (e["ctas"], e["threads"], e["tile"], e["solo_cells"]) == (ctas, threads, tile, solo)
+            assert threads in (256, 512, 1024) and tile in (32, 64, 128)
+        ctx2 = pkg.Context(0)
+        try:
+            ctx2.tune_load(path)
+            assert ctx2.tune_count() == 1
+            bad = tmp_path / "bad.json"
+            bad.write_text('{"something": 2}')
+            with pytest.raises(pkg.BsamgError):
+                ctx2.tune_load(bad)
+        finally:
+            ctx2.close()
+        a.close()
+        b.close()
+    finally:
+        ctx.close()
