@@ -416,7 +416,7 @@ def amr_run(api, make_root, w, mode, steps, warmup, use_events=True):
     counts and the final mesh."""
     qinit = api_qinit(w)
     h = make_root()
-    wall, solve, vc = [], [], []
+    wall, solve, vc, rgt = [], [], [], []
     t_start = None
     for s in range(warmup + steps):
         if s == warmup:
@@ -438,9 +438,11 @@ def amr_run(api, make_root, w, mode, steps, warmup, use_events=True):
         if s >= warmup:
             wall.append(t2 - t0)
             solve.append(t2 - t1)
+            if hasattr(h, "regrid_timing"):
+                rgt.append(h.regrid_timing())
         vc.append(n)
     total = time.perf_counter() - t_start
-    return dict(total_s=total, wall=wall, solve=solve, vcycles=vc[warmup:], h=h)
+    return dict(total_s=total, wall=wall, solve=solve, vcycles=vc[warmup:], h=h, regrid_parts=rgt)
 
 
 def api_qinit(w):
@@ -530,6 +532,21 @@ def amr_arm(args, w, dist):
         "mesh": mesh_stats(f["tab"], nd),
         "timing": "host clock around regrid + time step, device synchronised after each step",
     }
+    if modes[0] == "mixed":
+        hm = m["h"]
+        form, ctas, threads, tile, solo = hm.get_solve()
+        info = hm.solve_info()
+        one_launch = form == 1 and info["phases"] > 0
+        line["mixed_solve"] = {
+            "form": "one cluster launch per solve" if one_launch else "per-launch graphs (chosen by the autotuner)",
+            "ctas": ctas if one_launch else None, "threads": threads if one_launch else None,
+            "tile_units": tile if one_launch else None, "one_cta_coarse_cells": solo if one_launch else None,
+            "phases_per_program": info["phases"], "levels_in_dsmem": info["dsm_levels"],
+            "dsmem_bytes_per_cta": info["data_bytes"], "image_bytes_per_cta": info["image_bytes"],
+            "tuned_size_classes": ctx.tune_count()}
+    if m["regrid_parts"]:
+        keys = m["regrid_parts"][0].keys()
+        line["regrid_breakdown_ms"] = {k: statistics.mean(r[k] for r in m["regrid_parts"]) for k in keys}
     if not args.no_cpu_baseline:
         from oracle import bsam_oracle as om
 

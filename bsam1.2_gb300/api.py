@@ -136,6 +136,7 @@ def lib():
         "bsamg_set_solve": ([P, I, I, I, I, ctypes.c_longlong], I),
         "bsamg_get_solve": ([P, IP, IP, IP, IP, ctypes.POINTER(ctypes.c_longlong)], I),
         "bsamg_solve_trace": ([P, I], I),
+        "bsamg_regrid_timing": ([P, DP, I], I),
         "bsamg_ctx_set_autotune": ([P, I], I),
         "bsamg_tune_save": ([P, ctypes.c_char_p], I),
         "bsamg_tune_load": ([P, ctypes.c_char_p], I),
@@ -490,6 +491,13 @@ class Hierarchy:
         _ck(lib().bsamg_solve_info(self.h, v, 8), "bsamg_solve_info")
         keys = ("phases", "body", "dsm_levels", "data_bytes", "image_bytes", "ctas", "threads", "too_large")
         return dict(zip(keys, list(v)))
+
+    def regrid_timing(self):
+        """Host ms of the regrid that made this hierarchy (bsamg_regrid_timing):
+        download, host model, create + commit, upload, ghost compilation, rest of commit."""
+        v = (ctypes.c_double * 6)()
+        _ck(lib().bsamg_regrid_timing(self.h, v, 6), "bsamg_regrid_timing")
+        return dict(zip(("download", "model", "commit", "upload", "ghost_compile", "commit_rest"), list(v)))
 
     def solve_trace(self, enable=True):
         """Record per-phase clocks of the next one-launch solves (bsamg_solve_trace)."""

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <atomic>
 #include <thread>
 #include <cmath>
@@ -696,6 +697,7 @@ void pinned_slot_give(Hier& H) {
 }
 
 int commit(Hier& H) {
+  auto tc0 = std::chrono::steady_clock::now();
   if (H.committed) return BSAMG_ERR_ARG;
   RET(set_device(H));
   RET(build_tables(H));
@@ -781,6 +783,7 @@ int commit(Hier& H) {
     }
   }
   // the ghost programs, compiled on host threads (they only read the tables)
+  auto tg0 = std::chrono::steady_clock::now();
   {
     std::vector<std::pair<int, int>> jobs;
     for (int l = H.minlevel; l <= H.maxlevel; l++)
@@ -798,6 +801,7 @@ int commit(Hier& H) {
     work();
     for (auto& t : th) t.join();
   }
+  H.regrid_ms[4] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tg0).count();
   for (int l = H.minlevel; l <= H.maxlevel; l++) {
     LevelT& L = H.L(l);
     for (int ip = 0; ip < 3; ip++) {
@@ -822,6 +826,8 @@ int commit(Hier& H) {
   RET(pinned_slot_take(H));
   CK(cudaStreamSynchronize(H.s));
   H.committed = true;
+  H.regrid_ms[5] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tc0).count() -
+                   H.regrid_ms[4];
   return BSAMG_OK;
 }
 
@@ -1330,6 +1336,12 @@ int bsamg_solve_info(const bsamg_hier* h, long long* info, int n) {
   long long v[8] = {h->solve_nph, h->solve_body, h->solve_dsm_levels, h->solve_im.data, h->solve_im.bytes,
                     h->solve_shape.ctas, h->solve_shape.threads, h->solve_nofit ? 1 : 0};
   for (int x = 0; x < n && x < 8; x++) info[x] = v[x];
+  return BSAMG_OK;
+}
+
+int bsamg_regrid_timing(const bsamg_hier* h, double* ms, int n) {
+  if (!h || !ms || n < 0) return BSAMG_ERR_ARG;
+  for (int x = 0; x < n && x < 6; x++) ms[x] = h->regrid_ms[x];
   return BSAMG_OK;
 }
 

@@ -122,6 +122,11 @@ struct Hier {
   int solve_dsm_levels = 0;      // levels whose FP32 arrays the program keeps in distributed shared memory
   void* solve_ctl = nullptr;
   int solve_ctl_cap = 0;  // residual slots of solve_ctl
+  // host clock of the regrid that made this hierarchy (ms): download of q,
+  // the host model (tagging, clustering, new patches' values), creating and
+  // committing the new hierarchy, the upload; and of commit: the ghost
+  // programs' compilation, everything else
+  double regrid_ms[6] = {};
   bool solve_trace_on = false;
   long long* solve_trace = nullptr;  // device, solve_trace_cap + 1 clocks
   int solve_trace_cap = 0;

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -506,6 +507,9 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   if (r) return r;
   int nd = H.ndims, nv = H.nrvars;
   Model M(H);
+  using clk = std::chrono::steady_clock;
+  auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+  const clk::time_point t0 = clk::now();
   // one copy of the whole q region (every patch, ghosts included)
   std::vector<double> qreg((size_t)H.q_len);
   cudaError_t ce = cudaMemcpyAsync(qreg.data(), H.pool + H.q_region, qreg.size() * sizeof(double),
@@ -513,6 +517,7 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(regrid download)");
   ce = cudaStreamSynchronize(H.s);
   if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize(regrid)");
+  const clk::time_point t1 = clk::now();
   auto slice = [&](int n) {
     const HostPatch& P = H.patches[n];
     const double* b = qreg.data() + (P.oq - H.q_region);
@@ -605,6 +610,7 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   // gives the sequential sequence's values)
   int final_ghost = level_patches(level).empty() ? -kMaxDepth - 1 : level;
 
+  const clk::time_point t2 = clk::now();
   // the new hierarchy, on the same context
   bsamg_hier* nh = nullptr;
   r = bsamg_hier_create(H.ctx, nd, nv, H.mbc, H.problem, H.params.data(), (int)H.params.size(), H.pp.qpo, &nh);
@@ -630,6 +636,7 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
     if ((r = bsamg_patch_add(nh, P.level, P.id, P.parent_id, P.mx, mg, mb, P.mthbc, P.dx, P.xlower))) return fail(r);
   }
   if ((r = bsamg_commit(nh))) return fail(r);
+  const clk::time_point t3 = clk::now();
   Hier& N = *nh;
   // q: one image of the new q region; qold: one image (new patches) and a
   // device-to-device copy for the persisting levels <= 0
@@ -679,6 +686,11 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   // them in place on its first capture; the old one captures again if used
   N.graph_donors = std::move(H.graphs);
   H.graphs.clear();
+  const clk::time_point t4 = clk::now();
+  N.regrid_ms[0] = ms(t0, t1);
+  N.regrid_ms[1] = ms(t1, t2);
+  N.regrid_ms[2] = ms(t2, t3);
+  N.regrid_ms[3] = ms(t3, t4);
   *out = nh;
   return BSAMG_OK;
 }

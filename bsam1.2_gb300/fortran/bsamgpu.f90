@@ -395,6 +395,13 @@ INTERFACE
     INTEGER(C_INT):: n
     INTEGER(C_INT):: status
   END FUNCTION
+  FUNCTION bsamg_regrid_timing(h, ms, n) BIND(C, NAME='bsamg_regrid_timing') RESULT(status)
+    IMPORT
+    TYPE(C_PTR), VALUE:: h
+    REAL(C_DOUBLE):: ms(*)
+    INTEGER(C_INT), VALUE:: n
+    INTEGER(C_INT):: status
+  END FUNCTION
   FUNCTION bsamg_solve_trace(h, enable) BIND(C, NAME='bsamg_solve_trace') RESULT(status)
     IMPORT
     TYPE(C_PTR), VALUE:: h

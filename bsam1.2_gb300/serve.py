@@ -178,9 +178,11 @@ class Server:
             try:
                 h.commit()
                 h.set_tail_cells(self.tail_cells)
-                # one-launch solves in clusters of 8 CTAs (several requests
-                # share the GPU at once), not tuned per request
-                h.set_solve(1, 8, 512, 64, 8192)
+                # the per-launch path: many requests share the GPU, and their
+                # launches interleave; a one-launch solve would hold its
+                # cluster's SMs for a whole step (measured: 129 against 195
+                # requests/s at 200 offered)
+                h.set_solve(0)
                 return h, pats, minlevel
             except BsamgError as e:
                 h.close()

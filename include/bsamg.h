@@ -339,6 +339,12 @@ int bsamg_solve_trace(bsamg_hier* h, int enable);
  * threads per CTA, [7] 1 when the last program was too large to stage (the
  * per-launch path ran).  Up to n of the 8 values. */
 int bsamg_solve_info(const bsamg_hier* h, long long* info, int n);
+/* Host clock (ms) of the regrid that made hierarchy h (no reference
+ * counterpart: measurement): [0] download of q, [1] the host model
+ * (tagging, clustering, the new patches' values), [2] creating and
+ * committing the new hierarchy, [3] the upload; [4] and [5] the part of [2]
+ * spent compiling ghost programs and the rest of the commit. */
+int bsamg_regrid_timing(const bsamg_hier* h, double* ms, int n);
 /* Autotuner of the mixed solve of adaptive hierarchies (no reference
  * counterpart).  While on (the default), the first mixed solve of an
  * adaptive hierarchy whose size class (plugin, dimension, variables, levels
