@@ -34,6 +34,7 @@ UNITS = {
     "tune.cu": [],
     "hier.cu": [],
     "ghostc.cpp": [],
+    "pool.cpp": [],
     "regrid.cpp": [],
     "io.cu": ["--fmad=false"],
     "frames.cpp": [],

@@ -16,6 +16,8 @@
 // order on the device gives exactly the state the sequential sequence gives.
 #include <algorithm>
 #include <cstdint>
+#include <iterator>
+#include <memory>
 #include <unordered_map>
 
 #include "hier.h"
@@ -34,10 +36,8 @@ struct Em {
 struct Emitter {
   const Hier& H;
   std::vector<Em> out;
-  std::vector<int> org;  // per patch: offset of cell (0,0,0) in its q plane
-  explicit Emitter(const Hier& h) : H(h), org(h.patches.size()) {
-    for (size_t p = 0; p < h.patches.size(); p++) org[p] = (int)origin_of(h, h.patches[p].qn);
-  }
+  const std::vector<int>& org;  // per patch: offset of cell (0,0,0) in its q plane
+  Emitter(const Hier& h, const std::vector<int>& o) : H(h), org(o) {}
 
   // offset of Fortran cell (i,j,k) from cell (0,0,0) of a q plane (the
   // device tables address q from that cell; negative in the second ghost
@@ -505,63 +505,140 @@ struct Emitter {
 
 namespace {
 
-// the writer sequence of SetGhost(level, ipass), in the reference's order
-void emit_set_ghost(const Hier& H, int level, int ipass, Emitter& E) {
-  const LevelT& L = H.L(level);
-  const std::vector<int>& ps = L.patches;
-  int n = (int)ps.size();
-  if (level > 0) {
-    for (int a = 0; a < n; a++) {
-      if (H.ndims == 2) E.interpolate2d(ps[a], ipass);
-      else E.interpolate3d(ps[a], ipass);
-    }
-    for (int a = 0; a < n; a++)
-      for (int b = a + 1; b < n; b++) E.ghost_overlap(ps[a], ps[b], nullptr);
-  }
-  if (H.periodic) {
-    for (int a = 0; a < n; a++) E.self_periodic(ps[a]);
-    if (level > 0) {
-      int poff[13][3];
+// The writer sequence of SetGhost(level, ipass), in the reference's order,
+// as five segments of per-patch items: coarse-fine interpolation of patch a
+// (levels > 0), its sibling overlaps with the patches after it (levels >
+// 0), its self-periodic copies, its periodic-image overlaps with the patches
+// after it (periodic levels > 0), its physical boundary condition.  Item
+// (segment, a) appends exactly what the reference's loops append at that
+// point, so concatenating the items in (segment, a) order is the sequence;
+// the items are independent, so they are emitted in parallel.
+struct LevelEmit {
+  const Hier& H;
+  int level, ipass, n;
+  const std::vector<int>& ps;
+  std::vector<int> org;
+  int poff[13][3] = {};
+  std::vector<char> edge;
+  LevelEmit(const Hier& h, int l, int ip) : H(h), level(l), ipass(ip), ps(h.L(l).patches), org(h.patches.size()) {
+    n = (int)ps.size();
+    for (size_t p = 0; p < h.patches.size(); p++) org[p] = (int)origin_of(h, h.patches[p].qn);
+    if (H.periodic && level > 0) {
+      Emitter E(H, org);
       E.periodic_offsets(level, poff);
       // Only patches within 2*mbc of the domain edge can meet another
       // patch's periodic image (for offset +N in dimension d the ghost boxes
       // meet only if (N - hi_a) + (lo_b - 1) <= 2*mbc); other pairs emit
       // nothing, so skipping them leaves the operation sequence unchanged.
-      std::vector<char> edge(n, 0);
+      edge.assign(n, 0);
       for (int a = 0; a < n; a++) {
         const HostPatch& P = H.patches[ps[a]];
         for (int d = 0; d < H.ndims; d++)
           if (P.mglobal[d][0] - 1 <= 2 * H.mbc || H.mxmax[level][d] - P.mglobal[d][1] <= 2 * H.mbc) edge[a] = 1;
       }
-      for (int a = 0; a < n; a++)
-        for (int b = a + 1; b < n; b++)
-          if (edge[a] && edge[b])
-          for (int pol = -1; pol <= 1; pol += 2)
-            for (int o = 0; o < H.nperoff; o++) {
-              int off[3] = {pol * poff[o][0], pol * poff[o][1], pol * poff[o][2]};
-              E.ghost_overlap(ps[a], ps[b], off);
-            }
     }
   }
-  for (int a = 0; a < n; a++) E.physical_bc(ps[a]);
+  int items() const { return 5 * n; }
+  void item(int x, std::vector<Em>& out) const {
+    Emitter E(H, org);
+    E.out.swap(out);
+    const int seg = x / n, a = x % n;
+    switch (seg) {
+      case 0:
+        if (level > 0) {
+          if (H.ndims == 2) E.interpolate2d(ps[a], ipass);
+          else E.interpolate3d(ps[a], ipass);
+        }
+        break;
+      case 1:
+        if (level > 0)
+          for (int b = a + 1; b < n; b++) E.ghost_overlap(ps[a], ps[b], nullptr);
+        break;
+      case 2:
+        if (H.periodic) E.self_periodic(ps[a]);
+        break;
+      case 3:
+        if (H.periodic && level > 0 && edge[a])
+          for (int b = a + 1; b < n; b++)
+            if (edge[b])
+              for (int pol = -1; pol <= 1; pol += 2)
+                for (int o = 0; o < H.nperoff; o++) {
+                  int off[3] = {pol * poff[o][0], pol * poff[o][1], pol * poff[o][2]};
+                  E.ghost_overlap(ps[a], ps[b], off);
+                }
+        break;
+      default:
+        E.physical_bc(ps[a]);
+        break;
+    }
+    E.out.swap(out);
+  }
+};
+
+std::vector<Em> concat(std::vector<std::vector<Em>>& parts) {
+  size_t m = 0;
+  for (auto& v : parts) m += v.size();
+  std::vector<Em> all;
+  all.reserve(m);
+  for (auto& v : parts) {
+    all.insert(all.end(), v.begin(), v.end());
+    std::vector<Em>().swap(v);
+  }
+  return all;
 }
+
+// the sequence of one (level, ipass), its items emitted in parallel
+std::vector<Em> emit_set_ghost(const Hier& H, int level, int ipass) {
+  LevelEmit L(H, level, ipass);
+  std::vector<std::vector<Em>> parts(L.items());
+  parallel_for(L.items(), [&](int x) { L.item(x, parts[x]); });
+  return concat(parts);
+}
+
+// Dead writes and stages of one emitted sequence (see the file comment).
+std::vector<GhostOp> stage_ops(const Hier& H, std::vector<Em>& ops, std::vector<int>& stage_off);
 
 }  // namespace
 
 std::vector<GhostOp> set_ghost_sequence(const Hier& H, int level, int ipass) {
-  Emitter E(H);
-  emit_set_ghost(H, level, ipass, E);
-  std::vector<GhostOp> res(E.out.size());
-  for (size_t x = 0; x < E.out.size(); x++) res[x] = E.out[x].op;
+  std::vector<Em> em = emit_set_ghost(H, level, ipass);
+  std::vector<GhostOp> res(em.size());
+  for (size_t x = 0; x < em.size(); x++) res[x] = em[x].op;
   return res;
 }
 
 std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std::vector<int>& stage_off) {
-  Emitter E(H);
-  emit_set_ghost(H, level, ipass, E);
+  std::vector<Em> em = emit_set_ghost(H, level, ipass);
+  return stage_ops(H, em, stage_off);
+}
+
+void compile_set_ghost_all(const Hier& H, const std::vector<std::pair<int, int>>& jobs,
+                           std::vector<std::vector<GhostOp>*> out, std::vector<std::vector<int>*> stage_off) {
+  // every item of every job in one parallel pass, then the jobs' staging
+  std::vector<std::unique_ptr<LevelEmit>> le;
+  std::vector<int> first(jobs.size() + 1, 0);
+  for (size_t j = 0; j < jobs.size(); j++) {
+    le.emplace_back(new LevelEmit(H, jobs[j].first, jobs[j].second));
+    first[j + 1] = first[j] + le.back()->items();
+  }
+  std::vector<std::vector<Em>> parts(first.back());
+  parallel_for(first.back(), [&](int x) {
+    size_t j = std::upper_bound(first.begin(), first.end(), x) - first.begin() - 1;
+    le[j]->item(x - first[j], parts[x]);
+  });
+  parallel_for((int)jobs.size(), [&](int j) {
+    std::vector<std::vector<Em>> mine(std::make_move_iterator(parts.begin() + first[j]),
+                                      std::make_move_iterator(parts.begin() + first[j + 1]));
+    std::vector<Em> em = concat(mine);
+    *out[j] = stage_ops(H, em, *stage_off[j]);
+  });
+}
+
+namespace {
+
+std::vector<GhostOp> stage_ops(const Hier& H, std::vector<Em>& ops, std::vector<int>& stage_off) {
   // Cells are keyed by patch and cell offset; the passes below use flat
   // arrays over the ghosted cells of the patches the operations touch.
-  std::vector<Em>& ops = E.out;
   int m = (int)ops.size();
   std::vector<long long> base(H.patches.size(), -1);
   long long slots = 0;
@@ -626,5 +703,7 @@ std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std:
     if (!dead[x]) res[fill[stage[x]]++] = ops[x].op;
   return res;
 }
+
+}  // namespace
 
 }  // namespace bsamg

@@ -786,20 +786,15 @@ int commit(Hier& H) {
   auto tg0 = std::chrono::steady_clock::now();
   {
     std::vector<std::pair<int, int>> jobs;
+    std::vector<std::vector<GhostOp>*> out;
+    std::vector<std::vector<int>*> so;
     for (int l = H.minlevel; l <= H.maxlevel; l++)
-      for (int ip = 0; ip < (l <= 0 ? 1 : 3); ip++) jobs.emplace_back(l, ip);
-    std::atomic<size_t> next(0);
-    auto work = [&]() {
-      for (size_t j; (j = next++) < jobs.size();) {
-        GhostProg& g = H.L(jobs[j].first).gp[jobs[j].second];
-        g.ops = compile_set_ghost(H, jobs[j].first, jobs[j].second, g.stage_off);
+      for (int ip = 0; ip < (l <= 0 ? 1 : 3); ip++) {
+        jobs.emplace_back(l, ip);
+        out.push_back(&H.L(l).gp[ip].ops);
+        so.push_back(&H.L(l).gp[ip].stage_off);
       }
-    };
-    unsigned nt = std::min<unsigned>((unsigned)jobs.size(), std::max(1u, std::thread::hardware_concurrency()));
-    std::vector<std::thread> th;
-    for (unsigned t = 1; t < nt; t++) th.emplace_back(work);
-    work();
-    for (auto& t : th) t.join();
+    compile_set_ghost_all(H, jobs, out, so);
   }
   H.regrid_ms[4] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tg0).count();
   for (int l = H.minlevel; l <= H.maxlevel; l++) {

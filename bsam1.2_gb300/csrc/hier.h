@@ -46,8 +46,15 @@ struct LevelT {
 };
 
 struct Hier;
+// f(0) .. f(n-1) on the library's host thread pool and the calling thread
+// (pool.cpp); returns when all are done
+void parallel_for(int n, const std::function<void(int)>& f);
 // Inputs of the ghost compiler.
 std::vector<GhostOp> compile_set_ghost(const Hier& H, int level, int ipass, std::vector<int>& stage_off);
+// the programs of several (level, ipass) jobs at once, every emission item
+// of every job on the thread pool
+void compile_set_ghost_all(const Hier& H, const std::vector<std::pair<int, int>>& jobs,
+                           std::vector<std::vector<GhostOp>*> out, std::vector<std::vector<int>*> stage_off);
 // the same writes unprocessed, in the reference's order (for sequential
 // execution on the host)
 std::vector<GhostOp> set_ghost_sequence(const Hier& H, int level, int ipass);

@@ -417,7 +417,31 @@ void prolong_mc(int nd, int mbc, const double* a, const int cmx[3], double* out)
       }
 }
 
-// MakeNewGrid (:1663-1784) and InitFields (:1787-1856) for box b of patch p
+// InitFields' prolongation for child c of patch p over box b (:1815-1818,
+// :1834-1837): child%qc(1-mbc:cmx+mbc) = parent%q(mb-mbc:mb+mbc), then
+// child%q(1-mbc:mx+mbc) = P1MC / P2MC(child%qc); child%qold = child%q (:1782)
+void init_from_parent(Model& M, int c, int p, const Box& b) {
+  const HostPatch& C = M.g[c];
+  int nd = M.nd();
+  const int mbc = M.src.mbc;
+  size_t nq = (size_t)C.qn[0] * C.qn[1] * C.qn[2], nc = (size_t)C.cn[0] * C.cn[1] * C.cn[2];
+  std::vector<double> qc(nc * M.src.nrvars, 0.0);
+  std::vector<double>& q = M.q[c];
+  int cmx[3] = {C.cmx[0], C.cmx[1], nd == 3 ? C.cmx[2] : 0};
+  int k0 = nd == 3 ? b[2][0] - mbc : 0, k1 = nd == 3 ? b[2][1] + mbc : 0;
+  for (int v = 0; v < M.src.nrvars; v++) {
+    size_t t = v * nc;
+    for (int k = k0; k <= k1; k++)
+      for (int j = b[1][0] - mbc; j <= b[1][1] + mbc; j++)
+        for (int i = b[0][0] - mbc; i <= b[0][1] + mbc; i++) qc[t++] = M.Q(p, i, j, k, v);
+    prolong_mc(nd, mbc, qc.data() + v * nc, cmx, q.data() + v * nq);
+  }
+  M.qold[c] = q;
+}
+
+// MakeNewGrid (:1663-1784) and InitFields (:1787-1856) for box b of patch p;
+// without QInit the values come later from init_from_parent (the caller
+// runs it for every new child of the level, in parallel)
 void make_new_grid(Model& M, int p, const Box& b, int id, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit,
                    void* user) {
   int nd = M.nd();
@@ -452,26 +476,12 @@ void make_new_grid(Model& M, int p, const Box& b, int id, const bsamg_regrid_par
     C.qn[d] = d < nd ? C.mx[d] + 2 * mbc : 1;
     C.cn[d] = d < nd ? C.cmx[d] + 2 * mbc : 1;
   }
-  size_t nq = (size_t)C.qn[0] * C.qn[1] * C.qn[2], nc = (size_t)C.cn[0] * C.cn[1] * C.cn[2];
-  std::vector<double> q(nq * M.src.nrvars, 0.0), qc(nc * M.src.nrvars, 0.0);  // AllocFields' zero fill
-  if (prm.initial) {
-    qinit(user, C.level, C.mx, C.dx, C.xlower, q.data());
-  } else {
-    // child%qc(1-mbc:cmx+mbc) = parent%q(mb-mbc:mb+mbc) (:1815-1818,
-    // :1834-1837), then child%q(1-mbc:mx+mbc) = P1MC / P2MC(child%qc)
-    int cmx[3] = {C.cmx[0], C.cmx[1], nd == 3 ? C.cmx[2] : 0};
-    int k0 = nd == 3 ? b[2][0] - mbc : 0, k1 = nd == 3 ? b[2][1] + mbc : 0;
-    for (int v = 0; v < M.src.nrvars; v++) {
-      size_t t = v * nc;
-      for (int k = k0; k <= k1; k++)
-        for (int j = b[1][0] - mbc; j <= b[1][1] + mbc; j++)
-          for (int i = b[0][0] - mbc; i <= b[0][1] + mbc; i++) qc[t++] = M.Q(p, i, j, k, v);
-      prolong_mc(nd, mbc, qc.data() + v * nc, cmx, q.data() + v * nq);
-    }
-  }
+  size_t nq = (size_t)C.qn[0] * C.qn[1] * C.qn[2];
+  std::vector<double> q(nq * M.src.nrvars, 0.0);  // AllocFields' zero fill
+  if (prm.initial) qinit(user, C.level, C.mx, C.dx, C.xlower, q.data());
   M.g.push_back(C);
   M.src_idx.push_back(-1);
-  M.qold.push_back(q);  // child%qold = child%q (:1782)
+  M.qold.push_back(prm.initial ? q : std::vector<double>());  // child%qold = child%q (:1782)
   M.q.push_back(std::move(q));
 }
 
@@ -539,7 +549,6 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
 
   int next_id = prm.first_id;
   int level;
-  std::vector<Sub> subs;
   // a level's patches in visiting order (youngest first: the reverse of
   // creation order, as ApplyOnLevel walks them), so that RefineGrid runs
   // over the parents, and creates their children, in the reference's order
@@ -556,9 +565,13 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
     std::vector<Flags> fl(lp.size());
     std::vector<Tag> list;
     int ib = prm.ibuffer[level];
-    for (size_t a = 0; a < lp.size(); a++) {  // ErrFlag
-      tag_patch(M, lp[a], prm, fl[a]);
-      if (ib > 0) buffer_and_list(M, M.g[lp[a]], ib, fl[a], list);
+    {  // ErrFlag, per patch on the thread pool; the edge lists joined in patch order
+      std::vector<std::vector<Tag>> lists(lp.size());
+      parallel_for((int)lp.size(), [&](int a) {
+        tag_patch(M, lp[a], prm, fl[a]);
+        if (ib > 0) buffer_and_list(M, M.g[lp[a]], ib, fl[a], lists[a]);
+      });
+      for (auto& v : lists) list.insert(list.end(), v.begin(), v.end());
     }
     if (!list.empty()) {  // InflateEdgeTags
       Hier T;
@@ -584,26 +597,51 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
         }
         poff[o][0] = a, poff[o][1] = b, poff[o][2] = c;
       }
-      for (int t = (int)list.size() - 1; t >= 0; t--) {
-        for (size_t a = 0; a < lp.size(); a++) buffer_tagged(nd, M.g[lp[a]], list[t].c, ib, fl[a]);
-        if (T.periodic)
-          for (int pol = -1; pol <= 1; pol += 2)
-            for (int o = 0; o < T.nperoff; o++) {
-              int c[3];
-              for (int d = 0; d < 3; d++) c[d] = list[t].c[d] + pol * poff[o][d];
-              for (size_t a = 0; a < lp.size(); a++) buffer_tagged(nd, M.g[lp[a]], c, ib, fl[a]);
-            }
-      }
+      // every patch's flags see the tags in the reference's order; the
+      // patches are independent, so each is done on the thread pool
+      parallel_for((int)lp.size(), [&](int a) {
+        for (int t = (int)list.size() - 1; t >= 0; t--) {
+          buffer_tagged(nd, M.g[lp[a]], list[t].c, ib, fl[a]);
+          if (T.periodic)
+            for (int pol = -1; pol <= 1; pol += 2)
+              for (int o = 0; o < T.nperoff; o++) {
+                int c[3];
+                for (int d = 0; d < 3; d++) c[d] = list[t].c[d] + pol * poff[o][d];
+                buffer_tagged(nd, M.g[lp[a]], c, ib, fl[a]);
+              }
+        }
+      });
     }
     size_t first_new = M.g.size();
-    for (size_t a = 0; a < lp.size(); a++) {  // GridAdapt -> RefineGrid
-      if (!new_sub_grids(nd, M.g[lp[a]], fl[a], prm, subs)) return BSAMG_ERR_ARG;
-      split_long(nd, prm.maxside, subs);
-      for (const Sub& s : subs) make_new_grid(M, lp[a], s.b, next_id++, prm, qinit, user);
+    {  // GridAdapt -> RefineGrid: each parent's clustering on the thread pool,
+       // the children made in the parents' order (their ids and visiting
+       // order), then their values, in parallel again
+      std::vector<std::vector<Sub>> subs_of(lp.size());
+      std::vector<char> ok(lp.size(), 1);
+      parallel_for((int)lp.size(), [&](int a) {
+        ok[a] = new_sub_grids(nd, M.g[lp[a]], fl[a], prm, subs_of[a]) ? 1 : 0;
+        if (ok[a]) split_long(nd, prm.maxside, subs_of[a]);
+      });
+      std::vector<std::pair<int, const Sub*>> made;  // (parent, box) of each new child
+      for (size_t a = 0; a < lp.size(); a++) {
+        if (!ok[a]) return BSAMG_ERR_ARG;
+        for (const Sub& sb : subs_of[a]) {
+          make_new_grid(M, lp[a], sb.b, next_id++, prm, qinit, user);
+          made.emplace_back(lp[a], &sb);
+        }
+      }
+      if (!prm.initial)
+        parallel_for((int)made.size(), [&](int x) {
+          init_from_parent(M, (int)(first_new + x), made[x].first, made[x].second->b);
+        });
     }
-    for (size_t c = first_new; c < M.g.size(); c++)  // TransferValues
-      for (size_t n = 0; n < H.patches.size(); n++)
-        if (H.patches[n].level == level + 1) transfer_overlap(nv, H.patches[n], oldq[n], M.g[c], M.q[c], nd);
+    std::vector<int> olds;  // TransferValues from the previous level-(l+1) patches
+    for (size_t n = 0; n < H.patches.size(); n++)
+      if (H.patches[n].level == level + 1) olds.push_back((int)n);
+    parallel_for((int)(M.g.size() - first_new), [&](int x) {
+      size_t c = first_new + x;
+      for (int n : olds) transfer_overlap(nv, H.patches[n], oldq[n], M.g[c], M.q[c], nd);
+    });
   }
   // AMR(finest) ends with SetGhost(finest, 0); nothing on the host reads its
   // result, so it runs on the device after the upload (the compiled program
