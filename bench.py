@@ -429,7 +429,7 @@ def amr_run(api, make_root, w, mode, steps, warmup, use_events=True):
         if use_events:
             old.close()
         t1 = time.perf_counter()
-        fin = max(p["level"] for p in h.patch_table())
+        fin = h.level_range()[1]
         kw = dict(mode=mode, strict=True) if use_events else {}
         n, res = h.time_step(s == 0, fin, w["minlevel"], NSMOOTH, MAXV, w["tol"], **kw)
         if use_events:
@@ -570,6 +570,9 @@ def amr_arm(args, w, dist):
 
                 def patch_table(self):
                     return self.o.patch_table()
+
+                def level_range(self):
+                    return self.o.level_range()
 
                 def time_step(self, *a, **k):
                     return self.o.time_step(*a, **k)

@@ -112,6 +112,7 @@ def lib():
         "bsamg_build_uniform": ([P, IP, I, IP, DP, DP], I),
         "bsamg_commit": ([P], I),
         "bsamg_num_patches": ([P, IP], I),
+        "bsamg_level_range": ([P, IP, IP], I),
         "bsamg_patch_info": ([P, I, IP, DP], I),
         "bsamg_regrid": ([P, ctypes.POINTER(RegridParams), QINIT, P, ctypes.POINTER(P)], I),
         "bsamg_field_size": ([P, I, I], SZ),
@@ -283,6 +284,12 @@ class Hierarchy:
     def build_uniform(self, mx, minlevel, mthbc, xlower, xupper):
         _ck(lib().bsamg_build_uniform(self.h, _ia(mx, 3), minlevel, _ia(mthbc, 6), _da(xlower, 3),
                                       _da(xupper, 3)), "bsamg_build_uniform")
+
+    def level_range(self):
+        """(minlevel, finest level) of the committed hierarchy (bsamg_level_range)."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        _ck(lib().bsamg_level_range(self.h, ctypes.byref(a), ctypes.byref(b)), "bsamg_level_range")
+        return a.value, b.value
 
     def patch_table(self):
         """Geometry of every patch in visiting order (bsamg_patch_info)."""
@@ -487,9 +494,10 @@ class Hierarchy:
 
     def solve_info(self):
         """dict of the last one-launch solve program (bsamg_solve_info)."""
-        v = (ctypes.c_longlong * 8)()
-        _ck(lib().bsamg_solve_info(self.h, v, 8), "bsamg_solve_info")
-        keys = ("phases", "body", "dsm_levels", "data_bytes", "image_bytes", "ctas", "threads", "too_large")
+        v = (ctypes.c_longlong * 11)()
+        _ck(lib().bsamg_solve_info(self.h, v, 11), "bsamg_solve_info")
+        keys = ("phases", "body", "dsm_levels", "data_bytes", "image_bytes", "ctas", "threads", "too_large",
+                "build_us", "run_us", "readback_us")
         return dict(zip(keys, list(v)))
 
     def regrid_timing(self):

@@ -1004,6 +1004,13 @@ int bsamg_num_patches(const bsamg_hier* h, int* n) {
   return BSAMG_OK;
 }
 
+int bsamg_level_range(const bsamg_hier* h, int* minlevel, int* maxlevel) {
+  if (!h || !h->committed) return BSAMG_ERR_ARG;
+  if (minlevel) *minlevel = h->minlevel;
+  if (maxlevel) *maxlevel = h->maxlevel;
+  return BSAMG_OK;
+}
+
 int bsamg_patch_info(const bsamg_hier* h, int index, int* out, double* dxl) {
   if (!h || !out || !dxl || index < 0 || index >= (int)h->patches.size()) return BSAMG_ERR_ARG;
   const HostPatch& P = h->patches[index];
@@ -1328,9 +1335,18 @@ int bsamg_get_solve(const bsamg_hier* h, int* mode, int* ctas, int* threads, int
 
 int bsamg_solve_info(const bsamg_hier* h, long long* info, int n) {
   if (!h || !info || n < 0) return BSAMG_ERR_ARG;
-  long long v[8] = {h->solve_nph, h->solve_body, h->solve_dsm_levels, h->solve_im.data, h->solve_im.bytes,
-                    h->solve_shape.ctas, h->solve_shape.threads, h->solve_nofit ? 1 : 0};
-  for (int x = 0; x < n && x < 8; x++) info[x] = v[x];
+  long long v[11] = {h->solve_nph,
+                     h->solve_body,
+                     h->solve_dsm_levels,
+                     h->solve_im.data,
+                     h->solve_im.bytes,
+                     h->solve_shape.ctas,
+                     h->solve_shape.threads,
+                     h->solve_nofit ? 1 : 0,
+                     (long long)(1e3 * h->solve_ms[0]),
+                     (long long)(1e3 * h->solve_ms[1]),
+                     (long long)(1e3 * h->solve_ms[2])};
+  for (int x = 0; x < n && x < 11; x++) info[x] = v[x];
   return BSAMG_OK;
 }
 

@@ -123,6 +123,7 @@ struct Hier {
   void* solve_img = nullptr;  // program image (SolveImage layout)
   SolveImage solve_im{};
   bool solve_nofit = false;   // the program of solve_key is too large to stage
+  double solve_ms[3] = {};    // last solve, host clock: program build, launch to finish, read-back
   int solve_nph = 0, solve_body = 0, solve_nb = 0;
   std::tuple<int, int, int, int, int> solve_key{kMaxDepth + 1, 0, 0, 0, 0};
   GhostOp* solve_ops = nullptr;  // the program's FP32 ghost operations, each stage in owner order

@@ -919,9 +919,14 @@ int solve_launch(Hier& H, int finest, int maxvcycles, double tol, int errortype)
 int solve_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,
                      int strict, int* ncycles, double* residuals) {
   int r;
+  using clk = std::chrono::steady_clock;
+  auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+  const clk::time_point t0 = clk::now();
   if ((r = solve_build(H, finest, minlevel, nsmooth))) return r;
+  const clk::time_point t1 = clk::now();
   if ((r = solve_launch(H, finest, maxvcycles, tol, errortype))) return r;
   if ((r = stream_wait(H))) return r;
+  const clk::time_point t2 = clk::now();
   SolveCtl* ctl = static_cast<SolveCtl*>(H.solve_ctl);
   cudaError_t e;
   std::vector<unsigned char> out(sizeof(SolveCtl) + sizeof(double) * (size_t)maxvcycles);
@@ -950,6 +955,9 @@ int solve_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcyc
     for (int i = 0; i < done && i < maxvcycles; i++) residuals[i] = rv[i];
   H.h_norm[0] = o.norm[0];
   H.h_norm[1] = o.norm[1];
+  H.solve_ms[0] = ms(t0, t1);
+  H.solve_ms[1] = ms(t1, t2);
+  H.solve_ms[2] = ms(t2, clk::now());
   if (o.nonfinite) return BSAMG_ERR_NONFINITE;
   if (ncycles) *ncycles = o.converged ? o.ncycles : maxvcycles;
   if (!o.converged && strict) return BSAMG_ERR_NOT_CONVERGED;

@@ -127,6 +127,12 @@ INTERFACE
     INTEGER(C_INT):: n
     INTEGER(C_INT):: status
   END FUNCTION
+  FUNCTION bsamg_level_range(h, minlevel, maxlevel) BIND(C, NAME='bsamg_level_range') RESULT(status)
+    IMPORT
+    TYPE(C_PTR), VALUE:: h
+    INTEGER(C_INT):: minlevel, maxlevel
+    INTEGER(C_INT):: status
+  END FUNCTION
   FUNCTION bsamg_patch_info(h, index, info, dxl) BIND(C, NAME='bsamg_patch_info') RESULT(status)
     IMPORT
     TYPE(C_PTR), VALUE:: h

@@ -169,6 +169,10 @@ int bsamg_build_uniform(bsamg_hier* h, const int mx[3], int minlevel,
  * schedule.  No patch may be added afterwards. */
 int bsamg_commit(bsamg_hier* h);
 int bsamg_num_patches(const bsamg_hier* h, int* n);
+/* The coarsest and finest levels of a committed hierarchy (the host's
+ * minlevel and finestlevel, bsamdriver's tree bookkeeping: after a regrid
+ * the finest level is the deepest one the clustering produced). */
+int bsamg_level_range(const bsamg_hier* h, int* minlevel, int* maxlevel);
 /* Geometry of the patch at `index` in visiting order: out[0..23] = level,
  * id, parent_id, mx[3], mglobal[6], mbounds[6], mthbc[6]; dxl[0..5] =
  * dx[3], xlower[3] -- the nodeinfo fields a host walks after a regrid
@@ -337,7 +341,9 @@ int bsamg_solve_trace(bsamg_hier* h, int enable);
  * the cluster's distributed shared memory, [3] bytes of that data area per
  * CTA, [4] bytes of the program image each CTA stages, [5] CTAs, [6]
  * threads per CTA, [7] 1 when the last program was too large to stage (the
- * per-launch path ran).  Up to n of the 8 values. */
+ * per-launch path ran); the last solve's host clock in microseconds: [8]
+ * building its program (0 when it was cached), [9] launch to finish, [10]
+ * reading the results back.  Up to n of the 11 values. */
 int bsamg_solve_info(const bsamg_hier* h, long long* info, int n);
 /* Host clock (ms) of the regrid that made hierarchy h (no reference
  * counterpart: measurement): [0] download of q, [1] the host model

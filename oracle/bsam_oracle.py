@@ -170,6 +170,11 @@ class OracleHierarchy:
                             xlower=list(d)[3:6]))
         return out
 
+    def level_range(self):
+        """(minlevel, finest level), as the library's bsamg_level_range."""
+        levels = [p["level"] for p in self.patch_table()]
+        return min(levels), max(levels)
+
     def field_size(self, pid, field):
         return lib().bsamo_field_size(self.h, pid, FIELD[field])
 
