@@ -105,6 +105,30 @@ __device__ __forceinline__ void mop(V2 E, const BoxLev& L, const Loc<DIM>& l, fl
   m1 = y - x * (3.0f * pb * (pb + x) + x * x) + L.c1 * (nsum<DIM>(E.v0, l) - k * x);
 }
 
+// the undivided Laplacian as a sum of neighbour differences: for a smooth
+// correction each difference of two close values is exact (Sterbenz), so the
+// rounding error is relative to the Laplacian, not to the values (the sum of
+// neighbours minus k times the centre cancels and keeps ~1e-7 of |e|)
+template <int DIM>
+__device__ __forceinline__ float ndiff(const float* a, const Loc<DIM>& l, float c) {
+  float s = ((a[l.xm] - c) + (a[l.xp] - c)) + ((a[l.ym] - c) + (a[l.yp] - c));
+  if (DIM == 3) s += (a[l.zm] - c) + (a[l.zp] - c);
+  return s;
+}
+
+// M(e) for the tracked residual g <- g - M(e): its rounding accumulates into
+// the right-hand side of every later cycle (the smoother's and the coarse
+// correction's only slow convergence down), so the Laplacians are evaluated
+// in the difference form.  With c0 = dt/h^2 ~ 33 at 256^3 the summed form
+// left a floor near 1e-5 |e| in g: from the 12th step on the last cycle of a
+// step gained 5x instead of 12x, and later steps needed a sixth cycle.
+template <int DIM>
+__device__ __forceinline__ void mop_track(V2 E, const BoxLev& L, const Loc<DIM>& l, float pb, float& m0, float& m1) {
+  float x = E.v0[l.own], y = E.v1[l.own];
+  m0 = x - L.c0 * ndiff<DIM>(E.v1, l, y);
+  m1 = y - x * (3.0f * pb * (pb + x) + x * x) + L.c1 * ndiff<DIM>(E.v0, l, x);
+}
+
 // ---------------------------------------------------------------------------
 // double-float arithmetic (value = h + l, |l| <= ulp(h)/2 after
 // normalisation): Dekker/Knuth error-free transformations
@@ -774,7 +798,7 @@ __global__ void __launch_bounds__(256, R == 1 ? 6 : 5) k_bx_track_update(float* 
       float h0 = QH.v0[i], h1 = QH.v1[i], lo0 = QL.v0[i], lo1 = QL.v1[i];
       float e0 = E.v0[i], e1 = E.v1[i];
       float m0, m1;
-      mop<DIM>(E, L, l, h0, m0, m1);
+      mop_track<DIM>(E, L, l, h0, m0, m1);
       a0[k] = G.v0[i] - m0;
       a1[k] = G.v1[i] - m1;
       DF t0 = two_sum(h0, e0);
