@@ -80,10 +80,10 @@ struct Loc {
   }
 };
 
-template <int DIM>
-__device__ __forceinline__ float nsum(const float* a, const Loc<DIM>& l) {
-  float s = a[l.xm] + a[l.xp] + a[l.ym] + a[l.yp];
-  if (DIM == 3) s += a[l.zm] + a[l.zp];
+template <int DIM, typename T = float>
+__device__ __forceinline__ T nsum(const float* a, const Loc<DIM>& l) {
+  T s = T(a[l.xm]) + T(a[l.xp]) + T(a[l.ym]) + T(a[l.yp]);
+  if (DIM == 3) s += T(a[l.zm]) + T(a[l.zp]);
   return s;
 }
 
@@ -254,28 +254,41 @@ __device__ __forceinline__ void cta_sum2(float s0, float s1, double* partial) {
 // One cell of a colour half-sweep of the correction smoother (RelaxGrid2D/3D
 // in correction form, see mixed.cu k_mx_relax).  first = 1: e of both
 // colours counts as zero (first half-sweep of a cycle); first = 2: the own
-// colour's e counts as zero (second half-sweep).
-template <int DIM>
+// colour's e counts as zero (second half-sweep).  Arithmetic T: float, or
+// double with the FP64 coefficients on the coarsest level (FP32 storage).
+template <int DIM, typename T = float>
 __device__ __forceinline__ void relax_at(float* __restrict__ fp, const BoxLev& L, int c, int first, int h, int y,
                                          int z) {
+  constexpr bool D = sizeof(T) == sizeof(double);
+  const T c0 = D ? T(L.cd[0]) : T(L.c0), c1 = D ? T(L.cd[1]) : T(L.c1);
+  const T tmp3 = D ? T(L.cd[2]) : T(L.tmp3), a12 = D ? T(L.cd[3]) : T(L.a12);
   V2 E = var2(fp, L.oe, L.half), G = var2(fp, L.og, L.half);
   const float* PB = fp + L.opb;
   int x = 2 * h + ((c + y + z + (DIM == 3 ? 1 : 0)) & 1);
   Loc<DIM> l(L, x, y, z);
-  float pb = PB[l.own];
-  float s0 = 0.f, s1 = 0.f, xv = 0.f;
+  T pb = PB[l.own];
+  T s0 = T(0), s1 = T(0), xv = T(0);
   if (first != 1) {
-    s0 = nsum<DIM>(E.v0, l);
-    s1 = nsum<DIM>(E.v1, l);
+    s0 = nsum<DIM, T>(E.v0, l);
+    s1 = nsum<DIM, T>(E.v1, l);
     if (first == 0) xv = E.v0[l.own];
   }
-  float w = pb + xv;
-  float a21 = -3.0f * w * w - L.tmp3;
-  float b1 = G.v0[l.own] + L.c0 * s1;
-  float b2 = G.v1[l.own] - L.c1 * s0 - xv * xv * (3.0f * pb + 2.0f * xv);
-  float rdet = 1.0f / (1.0f - L.a12 * a21);
-  E.v0[l.own] = (b1 - L.a12 * b2) * rdet;
-  E.v1[l.own] = (b2 - a21 * b1) * rdet;
+  T w = pb + xv;
+  T a21 = T(-3) * w * w - tmp3;
+  T b1 = T(G.v0[l.own]) + c0 * s1;
+  T b2 = T(G.v1[l.own]) - c1 * s0 - xv * xv * (T(3) * pb + T(2) * xv);
+  T rdet = T(1) / (T(1) - a12 * a21);
+  E.v0[l.own] = (float)((b1 - a12 * b2) * rdet);
+  E.v1[l.own] = (float)((b2 - a21 * b1) * rdet);
+}
+
+// the FP64 smoother over a whole level (the coarsest level of a V-cycle
+// that no small-level cycle covers): one cell of the colour per thread
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bx_relax64(float* __restrict__ fp, BoxLev L, int c, int first) {
+  int h = blockIdx.x * blockDim.x + threadIdx.x;
+  int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (h < L.hh && y < L.n[1]) relax_at<DIM, double>(fp, L, c, first, h, y, blockIdx.z);
 }
 
 // Full-grid sweep: each thread takes position h of rows R*yp .. R*yp+R-1
@@ -672,7 +685,7 @@ __device__ __forceinline__ void unflatten(int j, int n0, int n1, int& x, int& y,
   divmod(r, n1, z, y);
 }
 
-template <int DIM>
+template <int DIM, typename T = float>
 __device__ __forceinline__ void small_relax(float* fp, const BoxLev& L, int nsmooth, bool fresh) {
   int cnt = L.hh * L.n[1] * L.n[2];
   for (int pass = 1; pass <= nsmooth; pass++)
@@ -681,7 +694,7 @@ __device__ __forceinline__ void small_relax(float* fp, const BoxLev& L, int nsmo
       for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
         int h, y, z;
         unflatten(i, L.hh, L.n[1], h, y, z);
-        relax_at<DIM>(fp, L, c, first, h, y, z);
+        relax_at<DIM, T>(fp, L, c, first, h, y, z);
       }
       __syncthreads();
     }
@@ -691,8 +704,11 @@ template <int DIM>
 __device__ __forceinline__ void small_cycle(float* fp, const SmallLevels& S, int nsmooth, int fresh) {
   for (int i = 0; i < S.n; i++) {
     const BoxLev& F = S.L[i];
+    if (i == S.n - 1) {  // the coarsest level: FP64 arithmetic
+      small_relax<DIM, double>(fp, F, nsmooth, fresh && i == 0);
+      break;
+    }
     small_relax<DIM>(fp, F, nsmooth, fresh && i == 0);
-    if (i == S.n - 1) break;
     const BoxLev& C = S.L[i + 1];
     int cnt = C.n[0] * C.n[1] * C.n[2];
     for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
@@ -1030,10 +1046,18 @@ int bx_relax(Hier& H, int level, int c, int first) {
   return BSAMG_OK;
 }
 
-int bx_level_relax(Hier& H, int level, int nsmooth, bool fresh) {
+// coarse: the V-cycle's coarsest level, smoothed in FP64 arithmetic
+int bx_level_relax(Hier& H, int level, int nsmooth, bool fresh, bool coarse = false) {
   for (int pass = 1; pass <= nsmooth; pass++)
     for (int c = 0; c < 2; c++) {
-      int r = bx_relax(H, level, c, (fresh && pass == 1) ? c + 1 : 0);
+      const int first = (fresh && pass == 1) ? c + 1 : 0;
+      if (coarse) {
+        BoxLev& L = B(H, level);
+        Launch sh = shape(L.hh, L.n[1], L.n[2]);
+        BX_LAUNCH(H, sh, k_bx_relax64, H.fpool, L, c, first);
+        continue;
+      }
+      int r = bx_relax(H, level, c, first);
       if (r) return r;
     }
   return BSAMG_OK;
@@ -1067,7 +1091,7 @@ int bx_vcycle(Hier& H, int level, int minlevel, int nsmooth, bool fresh) {
     else k_bx_small_vcycle<3><<<1, kSmallThreads, 0, H.s>>>(H.fpool, S, nsmooth, fresh ? 1 : 0);
     return after_launch(H, 1);
   }
-  int r = bx_level_relax(H, level, nsmooth, fresh);
+  int r = bx_level_relax(H, level, nsmooth, fresh, level == minlevel);
   if (r) return r;
   if (level > minlevel) {
     BoxLev &F = B(H, level), &C = B(H, level - 1);
@@ -1293,6 +1317,7 @@ void box_coefficients(Hier& H) {
     L.c0l = (float)(c[0] - (double)L.c0h);
     L.c1h = (float)c[1];
     L.c1l = (float)(c[1] - (double)L.c1h);
+    for (int x = 0; x < 4; x++) L.cd[x] = c[x];
   }
 }
 

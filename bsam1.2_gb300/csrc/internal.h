@@ -69,6 +69,7 @@ struct BoxLev {
   long long oe, og, opb, oec;   // float offsets: e, g, pb, ec (ec: levels below the finest)
   float c0, c1, tmp3, a12;      // dt/h^2, eps^2/h^2, (4|6) eps^2/h^2, (4|6) dt/h^2
   float c0h, c0l, c1h, c1l;     // dt/h^2 and eps^2/h^2 as float pairs (hi + lo)
+  double cd[4];                 // c0, c1, tmp3, a12 in FP64 (the coarsest level's FP64 smoother)
 };
 
 // One block of a level's work list: block covers units [start, start+kBlock)

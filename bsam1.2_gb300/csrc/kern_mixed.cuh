@@ -250,19 +250,30 @@ __device__ __forceinline__ Cell32 cell32(const PatchDev& p, float* fpool, int i,
   return x;
 }
 
-// red-black pointwise relaxation of the correction
-template <class PL, int DIM, bool CL = false>
+// red-black pointwise relaxation of the correction, in arithmetic T (FP64
+// with the patch's FP64 coefficients on the coarsest level)
+template <class PL, int DIM, bool CL = false, typename T = float>
 __device__ __forceinline__ void u_relax(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
                                         int tid, int ipass, const MxParams& mp) {
   const PatchDev& p = P[b.patch];
   int i, j, k;
   if (!color_cell<DIM>(p, b.start + tid, ipass, i, j, k)) return;
-  PL::template mx_relax<DIM>(cell32<PL, DIM, CL>(p, fpool, i, j, k), p.cf, mp);
+  if constexpr (sizeof(T) == sizeof(double))
+    PL::template mx_relax<DIM, double>(cell32<PL, DIM, CL>(p, fpool, i, j, k), p.c, mp);
+  else
+    PL::template mx_relax<DIM, float>(cell32<PL, DIM, CL>(p, fpool, i, j, k), p.cf, mp);
 }
-template <class PL, int DIM>
+// ipass with kRelax64: the FP64 smoother
+template <class PL, int DIM, bool CL = false>
+__device__ __forceinline__ void u_relax_any(const PatchDev* __restrict__ P, float* __restrict__ fpool, const Blk b,
+                                            int tid, int ipass, const MxParams& mp) {
+  if (ipass & kRelax64) u_relax<PL, DIM, CL, double>(P, fpool, b, tid, ipass & 3, mp);
+  else u_relax<PL, DIM, CL>(P, fpool, b, tid, ipass, mp);
+}
+template <class PL, int DIM, typename T>
 __global__ void __launch_bounds__(kBlock) k_mx_relax(const PatchDev* __restrict__ P, float* __restrict__ fpool,
                                                      const Blk* __restrict__ blk, int ipass, MxParams mp) {
-  u_relax<PL, DIM>(P, fpool, blk[blockIdx.x], threadIdx.x, ipass, mp);
+  u_relax<PL, DIM, false, T>(P, fpool, blk[blockIdx.x], threadIdx.x, ipass, mp);
 }
 
 // CoarseLoadingFunction on the correction: fine r = g - M(e) under each
@@ -423,7 +434,7 @@ __device__ __forceinline__ void run_tail(const PatchDev* __restrict__ P, float* 
     for (int b = 0; b < f.nblk; b++) {
       const Blk bb = f.blk[b];
       switch (f.op) {
-        case kTRelax: u_relax<PL, DIM>(P, fpool, bb, threadIdx.x, f.arg, mp); break;
+        case kTRelax: u_relax_any<PL, DIM>(P, fpool, bb, threadIdx.x, f.arg, mp); break;
         case kTRestrict: u_restrict<DIM>(P, fpool, bb, threadIdx.x, nrvars); break;
         case kTRing: u_coarse_ring<DIM>(P, fpool, bb, threadIdx.x, nrvars, f.arg); break;
         case kTLoad: u_coarse_load<PL, DIM>(P, fpool, bb, threadIdx.x, mp); break;
@@ -483,8 +494,14 @@ struct Launchers {
   static int relax(const MxLaunch& L, const Blk* blk, int nblk, int ipass) {
     if (nblk <= 0) return 0;
     MxParams mp = PL::mx_params(L.pp);
-    if (L.ndims == 2) k_mx_relax<PL, 2><<<nblk, kBlock, 0, L.s>>>(L.P, L.fpool, blk, ipass, mp);
-    else k_mx_relax<PL, 3><<<nblk, kBlock, 0, L.s>>>(L.P, L.fpool, blk, ipass, mp);
+    const int ip = ipass & 3;
+    if (ipass & kRelax64) {
+      if (L.ndims == 2) k_mx_relax<PL, 2, double><<<nblk, kBlock, 0, L.s>>>(L.P, L.fpool, blk, ip, mp);
+      else k_mx_relax<PL, 3, double><<<nblk, kBlock, 0, L.s>>>(L.P, L.fpool, blk, ip, mp);
+    } else {
+      if (L.ndims == 2) k_mx_relax<PL, 2, float><<<nblk, kBlock, 0, L.s>>>(L.P, L.fpool, blk, ip, mp);
+      else k_mx_relax<PL, 3, float><<<nblk, kBlock, 0, L.s>>>(L.P, L.fpool, blk, ip, mp);
+    }
     return 1;
   }
   static int coarse_load(const MxLaunch& L, const Blk* blk, int nblk) {

@@ -259,7 +259,7 @@ struct SolveRun {
     constexpr int nr = PL::kNV;
     switch (f.op) {
       case kTRelax:
-        owned(f, cluster, [&](const Blk& b, int u) { u_relax<PL, DIM, true>(P, fpool, b, u, f.arg, mp); });
+        owned(f, cluster, [&](const Blk& b, int u) { u_relax_any<PL, DIM, true>(P, fpool, b, u, f.arg, mp); });
         break;
       case kTRestrict:
         owned(f, cluster, [&](const Blk& b, int u) { u_restrict<DIM, true>(P, fpool, b, u, nr); });

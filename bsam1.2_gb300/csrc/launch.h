@@ -35,6 +35,10 @@ enum Kind : int {
 // the host).  kTRing: the coarse ring (arg 0) or CorrectFine's first step
 // (arg 1); kTRelax: arg = ipass; kTFill: FillDownLevel, arg = field.
 enum TailOp : int { kTRelax = 0, kTRestrict = 1, kTRing = 2, kTLoad = 3, kTProlong = 4, kTGhost = 5, kTFill = 6 };
+// Flag of a relaxation's ipass on the correction's coarsest level: the
+// smoother computes in FP64 (FP32 storage), the coarse solve of the
+// V-cycle at the reference's precision.
+constexpr int kRelax64 = 4;
 struct TailPhase {
   int op, arg, nblk, nstages;
   const Blk* blk;

@@ -166,10 +166,12 @@ int mx_op(Hier& H, int level, int kind, int op, int arg) {
   return BSAMG_OK;
 }
 
-int mx_level_relax(Hier& H, int level, int nsmooth) {
+// the smoothing of one level; on the V-cycle's coarsest level (coarse) in
+// FP64 arithmetic
+int mx_level_relax(Hier& H, int level, int nsmooth, bool coarse) {
   for (int pass = 1; pass <= nsmooth; pass++)
     for (int rb = 1; rb <= 2; rb++) {
-      int r = mx_op(H, level, kKindColor, kTRelax, rb);
+      int r = mx_op(H, level, kKindColor, kTRelax, coarse ? rb | kRelax64 : rb);
       if (!r) r = mx_set_ghost(H, level, rb);
       if (r) return r;
     }
@@ -199,7 +201,7 @@ int mx_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
     (*rec)[at].nblk = (int)(rec->size() - at - 1);
     return r;
   }
-  int r = mx_level_relax(H, level, nsmooth);
+  int r = mx_level_relax(H, level, nsmooth, level == minlevel);
   if (r) return r;
   if (level > minlevel) {
     if ((r = mx_op(H, level, kKindCoarse, kTRestrict, 0))) return r;
@@ -210,7 +212,7 @@ int mx_vcycle(Hier& H, int level, int minlevel, int nsmooth) {
     if ((r = mx_op(H, level, kKindCGhost, kTRing, 1))) return r;
     if ((r = mx_op(H, level, kKindProl, kTProlong, 0))) return r;
     if ((r = mx_set_ghost(H, level, 0))) return r;
-    if ((r = mx_level_relax(H, level, nsmooth))) return r;
+    if ((r = mx_level_relax(H, level, nsmooth, false))) return r;
   }
   return BSAMG_OK;
 }

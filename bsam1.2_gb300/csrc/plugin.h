@@ -48,7 +48,10 @@
 //   static MxParams mx_params(const ProbParams&);
 //   template <int DIM> __device__ static void mx_prep(const Cell64&, const double* rf, float* base, float* g,
 //                                                     int mode, const double* c, const ProbParams&);
-//   template <int DIM> __device__ static void mx_relax(const Cell32&, const float* cf, const MxParams&);
+//   // the correction smoother in arithmetic T: float on every level, double
+//   // on the coarsest (cf: the patch's coefficients in T; e, g and the
+//   // base planes are FP32 either way)
+//   template <int DIM, typename T> __device__ static void mx_relax(const Cell32&, const T* cf, const MxParams&);
 //   template <int DIM> __device__ static void mx_op(const float* e, long long c, long long sy, long long sz,
 //                                                  long long ps, const float* base, long long fc, long long sf,
 //                                                  const float* cf, const MxParams&, float* m);

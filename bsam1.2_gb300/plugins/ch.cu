@@ -123,33 +123,34 @@ struct CH {
   }
 
   // red-black pointwise Newton on the correction (RelaxGrid2D/3D in
-  // correction form):
+  // correction form), in arithmetic T (float on every level, double on the
+  // coarsest; e, g and the base plane stay FP32, cf is in T):
   //   a21 = -3 (pb + e)^2 - tmp3
   //   b1  = g1 + tmp1 * sum(e_mu neighbours)
   //   b2  = g2 - tmp2 * sum(e_phi neighbours) - e^2 (3 pb + 2 e)
-  template <int DIM>
-  __device__ __forceinline__ static void mx_relax(const Cell32& x, const float* cf, const MxParams&) {
+  template <int DIM, typename T>
+  __device__ __forceinline__ static void mx_relax(const Cell32& x, const T* cf, const MxParams&) {
     float* e0 = x.e;
     float* e1 = e0 + x.sq;
     const long long c = x.c, fc = x.fc, sy = x.sy, sz = x.sz;
-    float tmp1 = cf[0], tmp2 = cf[1], tmp3 = cf[2], a12 = cf[3];
-    float pb = x.base[fc];
-    float xx = e0[c];
-    float w = pb + xx;
-    float a21 = -3.0f * w * w - tmp3;
-    float s1, s0;
+    T tmp1 = cf[0], tmp2 = cf[1], tmp3 = cf[2], a12 = cf[3];
+    T pb = x.base[fc];
+    T xx = e0[c];
+    T w = pb + xx;
+    T a21 = T(-3) * w * w - tmp3;
+    T s1, s0;
     if (DIM == 2) {
-      s1 = e1[c - 1] + e1[c + 1] + e1[c - sy] + e1[c + sy];
-      s0 = e0[c + 1] + e0[c - 1] + e0[c + sy] + e0[c - sy];
+      s1 = T(e1[c - 1]) + T(e1[c + 1]) + T(e1[c - sy]) + T(e1[c + sy]);
+      s0 = T(e0[c + 1]) + T(e0[c - 1]) + T(e0[c + sy]) + T(e0[c - sy]);
     } else {
-      s1 = e1[c - 1] + e1[c + 1] + e1[c - sy] + e1[c + sy] + e1[c - sz] + e1[c + sz];
-      s0 = e0[c + 1] + e0[c - 1] + e0[c + sy] + e0[c - sy] + e0[c + sz] + e0[c - sz];
+      s1 = T(e1[c - 1]) + T(e1[c + 1]) + T(e1[c - sy]) + T(e1[c + sy]) + T(e1[c - sz]) + T(e1[c + sz]);
+      s0 = T(e0[c + 1]) + T(e0[c - 1]) + T(e0[c + sy]) + T(e0[c - sy]) + T(e0[c + sz]) + T(e0[c - sz]);
     }
-    float b1 = x.g[fc] + tmp1 * s1;
-    float b2 = x.g[x.sf + fc] - tmp2 * s0 - xx * xx * (3.0f * pb + 2.0f * xx);
-    float rdet = 1.0f / (1.0f - a12 * a21);
-    e0[c] = (b1 - a12 * b2) * rdet;
-    e1[c] = (b2 - a21 * b1) * rdet;
+    T b1 = T(x.g[fc]) + tmp1 * s1;
+    T b2 = T(x.g[x.sf + fc]) - tmp2 * s0 - xx * xx * (T(3) * pb + T(2) * xx);
+    T rdet = T(1) / (T(1) - a12 * a21);
+    e0[c] = (float)((b1 - a12 * b2) * rdet);
+    e1[c] = (float)((b2 - a21 * b1) * rdet);
   }
 
   // M(e) = N(pb + e) - N(pb), written so that no term cancels

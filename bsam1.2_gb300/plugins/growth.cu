@@ -142,33 +142,35 @@ struct Growth {
     for (int v = 0; v < 3; v++) g[v * sf + fc] = (float)r[v];
   }
 
-  template <int DIM>
-  __device__ __forceinline__ static void mx_relax(const Cell32& x, const float* cf, const MxParams& mp) {
+  // the correction smoother in arithmetic T (float on every level, double
+  // on the coarsest; e, g and the base planes stay FP32, cf is in T)
+  template <int DIM, typename T>
+  __device__ __forceinline__ static void mx_relax(const Cell32& x, const T* cf, const MxParams& mp) {
     float* e0 = x.e;
     float* e1 = e0 + x.sq;
     float* e2 = e1 + x.sq;
     const long long c = x.c, fc = x.fc, sy = x.sy, sz = x.sz, sf = x.sf;
     const float* base = x.base;
     const float* g = x.g;
-    float dt = mp.p[0], cp = mp.p[1];
-    float pb = base[fc], nb = base[sf + fc], G = base[2 * sf + fc], U = base[3 * sf + fc];
-    float c0 = cf[0], c1 = cf[1], c2 = cf[2], c3 = cf[3];
-    float s0 = e0[c - 1] + e0[c + 1] + e0[c - sy] + e0[c + sy];
-    float s1 = e1[c - 1] + e1[c + 1] + e1[c - sy] + e1[c + sy];
-    float s2 = e2[c - 1] + e2[c + 1] + e2[c - sy] + e2[c + sy];
+    T dt = mp.p[0], cp = mp.p[1];
+    T pb = base[fc], nb = base[sf + fc], G = base[2 * sf + fc], U = base[3 * sf + fc];
+    T c0 = cf[0], c1 = cf[1], c2 = cf[2], c3 = cf[3];
+    T s0 = T(e0[c - 1]) + T(e0[c + 1]) + T(e0[c - sy]) + T(e0[c + sy]);
+    T s1 = T(e1[c - 1]) + T(e1[c + 1]) + T(e1[c - sy]) + T(e1[c + sy]);
+    T s2 = T(e2[c - 1]) + T(e2[c + 1]) + T(e2[c - sy]) + T(e2[c + sy]);
     if (DIM == 3) {
-      s0 += e0[c - sz] + e0[c + sz];
-      s1 += e1[c - sz] + e1[c + sz];
-      s2 += e2[c - sz] + e2[c + sz];
+      s0 += T(e0[c - sz]) + T(e0[c + sz]);
+      s1 += T(e1[c - sz]) + T(e1[c + sz]);
+      s2 += T(e2[c - sz]) + T(e2[c + sz]);
     }
-    float xx = e0[c], y = e1[c];
-    float w = pb + xx;
-    float xn = (g[fc] + dt * G * y + c0 * s0 - dt * pb * xx * (2.0f * pb + xx)) / (c2 + dt * w * w);
-    float yn = (g[sf + fc] + c1 * s1) / (c3 + U);
-    float zn = (g[2 * sf + fc] + c1 * s2 + cp * (pb * yn + xn * nb + xn * yn)) / c3;
-    e0[c] = xn;
-    e1[c] = yn;
-    e2[c] = zn;
+    T xx = e0[c], y = e1[c];
+    T w = pb + xx;
+    T xn = (T(g[fc]) + dt * G * y + c0 * s0 - dt * pb * xx * (T(2) * pb + xx)) / (c2 + dt * w * w);
+    T yn = (T(g[sf + fc]) + c1 * s1) / (c3 + U);
+    T zn = (T(g[2 * sf + fc]) + c1 * s2 + cp * (pb * yn + xn * nb + xn * yn)) / c3;
+    e0[c] = (float)xn;
+    e1[c] = (float)yn;
+    e2[c] = (float)zn;
   }
 
   template <int DIM>

@@ -94,12 +94,12 @@ struct Heat {
     if (DIM == 3) s = s + a[c - sz] + a[c + sz];
     return s;
   }
-  template <int DIM>
-  __device__ __forceinline__ static void mx_relax(const Cell32& x, const float* cf, const MxParams&) {
+  template <int DIM, typename T>
+  __device__ __forceinline__ static void mx_relax(const Cell32& x, const T* cf, const MxParams&) {
     float* u = x.e;
     float* v = u + x.sq;
-    u[x.c] = (x.g[x.fc] + cf[0] * nsum32<DIM>(u, x.c, x.sy, x.sz)) / cf[2];
-    v[x.c] = (x.g[x.sf + x.fc] + cf[1] * nsum32<DIM>(v, x.c, x.sy, x.sz)) / cf[3];
+    u[x.c] = (float)((T(x.g[x.fc]) + cf[0] * T(nsum32<DIM>(u, x.c, x.sy, x.sz))) / cf[2]);
+    v[x.c] = (float)((T(x.g[x.sf + x.fc]) + cf[1] * T(nsum32<DIM>(v, x.c, x.sy, x.sz))) / cf[3]);
   }
   template <int DIM>
   __device__ __forceinline__ static void mx_op(const float* e, long long c, long long sy, long long sz, long long ps,
