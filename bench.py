@@ -679,6 +679,8 @@ def main():
     ap.add_argument("--serve-blocking-wait", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--box-sweep", type=int, default=None,
+                    help="smoothing form of periodic-box levels (bsamg_set_box_sweep); default: the library's")
     args = ap.parse_args()
     dist = Dist()
     if args.workload == "serve":
@@ -708,6 +710,8 @@ def main():
     pkg = ge.load_package()
     ctx = pkg.Context(dist.local)
     h = make_hierarchy(pkg, ctx, w)
+    if args.box_sweep is not None:
+        h.set_box_sweep(args.box_sweep)
     q0 = pkg.pin(initial_q(pkg, w))
     N = int(np.prod(root_mx(w)[0]))
 
@@ -734,8 +738,13 @@ def main():
     # uniform periodic workloads with even extents run the periodic-box mixed
     # path (colour-split arrays), the others the general one
     kmix = "k_bx_relax" if all(m == 2 for m in w["mthbc"][:2 * w["ndims"]]) else "k_mx_relax"
-    # per colour: e read (N*2*4) + g, phib and e write of that colour (N/2*(2*4+4+2*4)) = 18 N;
-    # a fused launch does both colours: 36 N (the per-sweep figure 4*N*V*s + N*s)
+    kdesc = "FP32 colour sweep of the correction, finest level"
+    if kmix == "k_bx_relax" and col_mixed == 4:
+        kmix = "k_bx_smooth"
+        kdesc = "one-pass V(2,2) smoothing of the correction (four colour half-sweeps), finest level"
+    # per colour half-sweep: e read (N*2*4) + g, phib and e write of that colour (N/2*(2*4+4+2*4)) = 18 N
+    # (the per-sweep figure 4*N*V*s + N*s for the two colours); the one-pass smoothing performs four
+    # half-sweeps per launch (72 N) while moving 28 N (e, g, phib read once, e written once)
     b_mixed = 18.0 * N * col_mixed
     b_fp64 = 32.0 * N   # q read (N*2*8) + f read and q write of one colour (N/2*(2*8+2*8))
     ach = b_mixed / (ms_mixed * 1e-3) / 1e9
@@ -759,9 +768,11 @@ def main():
         "speedup_mixed_vs_fp64": value / v_fp64,
         "error_vs_fp64": {"max_rel_phi": err, "after_steps": args.warmup + args.steps},
         "dof_sweeps_per_s": None,
-        "roofline": {"bound": "hbm", "kernel": f"{kmix} (FP32 colour sweep of the correction, finest level)",
+        "roofline": {"bound": "hbm", "kernel": f"{kmix} ({kdesc})",
                      "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                      "peak_kind": peak_kind, "bytes_per_launch": b_mixed, "ms_per_launch": ms_mixed,
+                     "half_sweeps_per_launch": col_mixed,
+                     "dram_bytes_needed": (28.0 if col_mixed == 4 else 18.0) * N,
                      "traffic": ncu_traffic(args.workload, kmix)},
         "roofline_fp64": {"bound": "fp64 pipe", "kernel": "k_relax (FP64 colour sweep, finest level)",
                           "achieved_hbm": ach64, "peak_hbm": peak, "frac_hbm": ach64 / peak,

@@ -468,7 +468,8 @@ class Hierarchy:
 
     def set_box_sweep(self, kind):
         """Colour sweep of 3D periodic-box levels: 0 two rows a thread, 1
-        four (default), 2 rows staged by bulk copies (bsamg_set_box_sweep)."""
+        four, 2 rows staged by bulk copies, 3 (default) one-pass V(2,2)
+        smoothing where it applies (bsamg_set_box_sweep)."""
         _ck(lib().bsamg_set_box_sweep(self.h, int(kind)), "bsamg_set_box_sweep")
 
     def set_tail_cells(self, cells):

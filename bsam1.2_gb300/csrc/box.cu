@@ -251,6 +251,24 @@ __device__ __forceinline__ void cta_sum2(float s0, float s1, double* partial) {
 // kernels.  Grid (x, y, z) = (position in a colour row or coarse x,
 // y, z); blockDim.z = 1.
 
+// The pointwise Newton update of one cell in FP32 (the 2x2 solve of
+// RelaxGrid2D/3D in correction form), every rounding explicit so that each
+// kernel that smooths computes the same bits whatever the compiler would
+// contract:  a21 = -3 (pb + xv)^2 - tmp3,  b1 = g0 + c0 s1,
+// b2 = g1 - c1 s0 - xv^2 (3 pb + 2 xv),  det = 1 - a12 a21,
+// e0 = (b1 - a12 b2) / det,  e1 = (b2 - a21 b1) / det.
+__device__ __forceinline__ void newton_cell(const BoxLev& L, float pb, float xv, float s0, float s1, float g0,
+                                            float g1, float& r0, float& r1) {
+  const float w = __fadd_rn(pb, xv);
+  const float a21 = __fmaf_rn(__fmul_rn(-3.0f, w), w, -L.tmp3);
+  const float b1 = __fmaf_rn(L.c0, s1, g0);
+  const float t = __fmaf_rn(3.0f, pb, __fmul_rn(2.0f, xv));
+  const float b2 = __fmaf_rn(-__fmul_rn(xv, xv), t, __fmaf_rn(-L.c1, s0, g1));
+  const float rdet = __frcp_rn(__fmaf_rn(-L.a12, a21, 1.0f));
+  r0 = __fmul_rn(__fmaf_rn(-L.a12, b2, b1), rdet);
+  r1 = __fmul_rn(__fmaf_rn(-a21, b1, b2), rdet);
+}
+
 // One cell of a colour half-sweep of the correction smoother (RelaxGrid2D/3D
 // in correction form, see mixed.cu k_mx_relax).  first = 1: e of both
 // colours counts as zero (first half-sweep of a cycle); first = 2: the own
@@ -273,13 +291,20 @@ __device__ __forceinline__ void relax_at(float* __restrict__ fp, const BoxLev& L
     s1 = nsum<DIM, T>(E.v1, l);
     if (first == 0) xv = E.v0[l.own];
   }
-  T w = pb + xv;
-  T a21 = T(-3) * w * w - tmp3;
-  T b1 = T(G.v0[l.own]) + c0 * s1;
-  T b2 = T(G.v1[l.own]) - c1 * s0 - xv * xv * (T(3) * pb + T(2) * xv);
-  T rdet = T(1) / (T(1) - a12 * a21);
-  E.v0[l.own] = (float)((b1 - a12 * b2) * rdet);
-  E.v1[l.own] = (float)((b2 - a21 * b1) * rdet);
+  if constexpr (!D) {
+    float r0, r1;
+    newton_cell(L, pb, xv, s0, s1, G.v0[l.own], G.v1[l.own], r0, r1);
+    E.v0[l.own] = r0;
+    E.v1[l.own] = r1;
+  } else {
+    T w = pb + xv;
+    T a21 = T(-3) * w * w - tmp3;
+    T b1 = T(G.v0[l.own]) + c0 * s1;
+    T b2 = T(G.v1[l.own]) - c1 * s0 - xv * xv * (T(3) * pb + T(2) * xv);
+    T rdet = T(1) / (T(1) - a12 * a21);
+    E.v0[l.own] = (float)((b1 - a12 * b2) * rdet);
+    E.v1[l.own] = (float)((b2 - a21 * b1) * rdet);
+  }
 }
 
 // the FP64 smoother over a whole level (the coarsest level of a V-cycle
@@ -320,13 +345,10 @@ __global__ void __launch_bounds__(256, MINB) k_bx_relax(float* __restrict__ fp, 
     g1[k] = G.v1[l.own];
   }
   for (int k = 0; k < R; k++) {
-    float w = pb[k] + xv[k];
-    float a21 = -3.0f * w * w - L.tmp3;
-    float b1 = g0[k] + L.c0 * s1[k];
-    float b2 = g1[k] - L.c1 * s0[k] - xv[k] * xv[k] * (3.0f * pb[k] + 2.0f * xv[k]);
-    float rdet = 1.0f / (1.0f - L.a12 * a21);
-    E.v0[own[k]] = (b1 - L.a12 * b2) * rdet;
-    E.v1[own[k]] = (b2 - a21 * b1) * rdet;
+    float r0, r1;
+    newton_cell(L, pb[k], xv[k], s0[k], s1[k], g0[k], g1[k], r0, r1);
+    E.v0[own[k]] = r0;
+    E.v1[own[k]] = r1;
   }
 }
 
@@ -458,12 +480,8 @@ __global__ void __launch_bounds__(kTileThreads) k_bx_relax_tiled(float* __restri
         s1 = a1[xm] + a1[xp] + a1[h - hh] + a1[h + hh] + sZ[T * hh + q] + sZ[3 * T * hh + q];
         if (first == 0) xv = sE0[q];
       }
-      float w = pb + xv;
-      float a21 = -3.0f * w * w - L.tmp3;
-      float b1 = sG0[q] + L.c0 * s1;
-      float b2 = sG1[q] - L.c1 * s0 - xv * xv * (3.0f * pb + 2.0f * xv);
-      float rdet = 1.0f / (1.0f - L.a12 * a21);
-      float r0 = (b1 - L.a12 * b2) * rdet, r1 = (b2 - a21 * b1) * rdet;
+      float r0, r1;
+      newton_cell(L, pb, xv, s0, s1, sG0[q], sG1[q], r0, r1);
       if (!ok) r0 = r1 = __int_as_float(0x7fc00000);  // a copy that never landed: poison the sweep
       long long row = ((long long)z * n1 + y) * hh + h;
       float* Ew = fp + L.oe;
@@ -474,6 +492,229 @@ __global__ void __launch_bounds__(kTileThreads) k_bx_relax_tiled(float* __restri
   }
   if (!ok)  // a wait gave up: give the copies still in flight a bounded time to land before the block exits
     for (int b = 0; b < NS; b++) mbar_wait(smem_addr(&bar[b]), 0u), mbar_wait(smem_addr(&bar[b]), 1u);
+}
+
+// ---------------------------------------------------------------------------
+// One smoothing of a 3D level's V-cycle visit (nsmooth = 2: colour
+// half-sweeps 0, 1, 0, 1) in one pass over memory.  A CTA owns TY rows y0 ..
+// y0+TY-1 of the planes z0 .. z1-1 and streams the planes z0-NS .. z1+NS-1
+// through a ring of NS+3 shared-memory slots, each holding the four
+// colour-split e arrays of rows y0-NS .. y0+TY+NS-1 of one plane (one bulk
+// copy per array, two where the rows wrap).  Once plane i has landed, stage
+// s (half-sweep s) updates plane i-s: it needs the other colour of planes
+// i-s-1 .. i-s+1 at stage s-1, which stage s-1 produced in this pass or the
+// last.  Each stage's rows shrink by one at both ends (its neighbours must
+// be at the previous stage), so stage NS leaves rows y0 .. y0+TY-1 final,
+// and the planes outside z0 .. z1-1 are computed only as halo.  Colour
+// updates read only the other colour and their own cell, so the result is
+// the NS separate half-sweeps' bit for bit.  g and pb come from global
+// memory into registers one plane ahead of the stage that uses them.  The
+// output goes to a second e array (oe_out): the input rows of a tile's halo
+// belong to other CTAs' outputs.  DRAM bytes per cell for NS = 4: 8 (e,
+// none when fresh) + 8 (g) + 4 (pb) read, 8 written, against 4 x 18 for four
+// separate half-sweeps.
+constexpr int kSmStages = 4;      // half-sweeps per pass
+constexpr int kSmThreads = 512;
+constexpr int kSmMinPlanes = 16;  // smallest z range of a CTA (the halo costs 2 NS planes)
+
+__host__ __device__ constexpr int smooth_slots(int ns) { return ns + 3; }  // planes i-ns-1 .. i, i+1 in flight
+__host__ __device__ constexpr long long smooth_slot_floats(int ty, int hh, int ns = kSmStages) {
+  return 4LL * (ty + 2 * ns) * hh;
+}
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
+
+template <int TY, int HH, bool FRESH, int NS = kSmStages>
+__global__ void __launch_bounds__(kSmThreads, 1) k_bx_smooth(float* __restrict__ fp, BoxLev L, long long oe_out,
+                                                            int nz) {
+  extern __shared__ __align__(128) float ssm[];
+  constexpr int NSL = smooth_slots(NS);
+  constexpr int R = TY + 2 * NS, AR = R * HH, SL = 4 * AR, LG = ilog2(HH);
+  constexpr int W = HH / 4;                 // threads of a colour row: four consecutive cells each
+  constexpr int RK = kSmThreads / W;        // rows between a thread's row segments
+  constexpr int KQ = (R + RK - 1) / RK;     // row segments of a thread (the same rows in every stage)
+  static_assert((1 << LG) == HH && W <= 32 && (W & (W - 1)) == 0 && RK % 2 == 0, "rows of 4 x 2^k cells");
+  __shared__ __align__(8) unsigned long long bar[NSL];
+  const int n1 = L.n[1], n2 = L.n[2];
+  const unsigned half = (unsigned)L.half;  // a level's cells are fewer than 2^31
+  const int ytiles = n1 / TY;
+  const int y0 = (blockIdx.x % ytiles) * TY, zc = blockIdx.x / ytiles;
+  const int z0 = (int)((long long)zc * n2 / nz), z1 = (int)((long long)(zc + 1) * n2 / nz);
+  const int P = z1 - z0 + 2 * NS;  // local plane j is z0 - NS + j
+  const float* E = fp + L.oe;
+  const float* G = fp + L.og;
+  const float* PB = fp + L.opb;
+  float* EO = fp + oe_out;
+  auto wrap = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
+  // this thread's cells h4 .. h4+3 of rows rb + k RK: the same in every stage,
+  // so that a stage's z+1 values are the ones the thread computed in the
+  // stage before it, and no other thread writes what a stage reads in the
+  // same pass but the rows y+-1, which were written in the pass before
+  const int li = threadIdx.x & (W - 1), rb = threadIdx.x / W, h4 = 4 * li;
+  unsigned goff[KQ];  // the cells' offset within a plane of a colour-split array
+#pragma unroll
+  for (int k = 0; k < KQ; k++) goff[k] = (unsigned)(wrap(y0 - NS + rb + k * RK, n1) * HH + h4);
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < NSL; b++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[b])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // rows y0-NS .. y0+TY+NS-1 of plane zw as one or two contiguous runs:
+  // f(offset of the run's first row, rows, its row in the slot)
+  auto runs = [&](int zw, auto&& f) {
+    int y = y0 - NS, n = R, at = 0;
+    while (n > 0) {
+      const int yy = wrap(y, n1);
+      const int run = n1 - yy < n ? n1 - yy : n;
+      f((zw * n1 + yy) * HH, run, at);
+      y += run;
+      n -= run;
+      at += run;
+    }
+  };
+  // lane 0 of warps 0-3: the rows of array a = warp of local plane j into
+  // slot k, warp 0 arming the barrier with the plane's bytes (nothing when
+  // fresh: the first half-sweeps count the old e as zero)
+  auto issue = [&](int j, int k) {
+    const int a = threadIdx.x >> 5;
+    if (FRESH || (threadIdx.x & 31) || a >= 4 || j >= P) return;
+    const unsigned b = smem_addr(&bar[k]);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (a == 0)
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"((unsigned)SL * 4u)
+                   : "memory");
+    runs(wrap(z0 - NS + j, n2), [&](int off, int run, int at) {
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              smem_addr(ssm + k * SL + a * AR + at * HH)),
+          "l"(E + (unsigned)a * half + off), "r"((unsigned)(run * HH * 4)), "r"(b)
+          : "memory");
+    });
+  };
+  // pb, g0, g1 of this thread's cells of stage s for the pass over local
+  // plane j, in registers before that pass
+  float4 v[NS][KQ][3];
+  auto load = [&](int s, int j) {
+    if (j < s || j > P - 1 - s) return;  // uniform over the CTA
+    const unsigned c = (s - 1) & 1;
+    const unsigned zoff = (unsigned)(wrap(z0 - NS + j, n2) * n1 * HH);
+#pragma unroll
+    for (int k = 0; k < KQ; k++) {
+      const int r = rb + k * RK;
+      if (r >= s && r <= R - 1 - s) {
+        const unsigned gi = zoff + goff[k];
+        v[s - 1][k][0] = *reinterpret_cast<const float4*>(PB + (c * half + gi));
+        v[s - 1][k][1] = *reinterpret_cast<const float4*>(G + (c * half + gi));
+        v[s - 1][k][2] = *reinterpret_cast<const float4*>(G + ((2 + c) * half + gi));
+      }
+    }
+  };
+  // the x-neighbour sums of four cells of colour parity bb from the other
+  // colour's values a (cells h4 .. h4+3) and the row's periodic wrap:
+  // a[xm] + a[xp] with xm, xp = h, h+1 (bb = 1) or h-1, h (bb = 0)
+  auto xsum = [&](const float4 a, int bb, unsigned m, float4& t) {
+    const float left = __shfl_sync(m, a.w, li - 1 + W, W), right = __shfl_sync(m, a.x, li + 1, W);
+    if (bb) {
+      t.x = a.x + a.y, t.y = a.y + a.z, t.z = a.z + a.w, t.w = a.w + right;
+    } else {
+      t.x = left + a.x, t.y = a.x + a.y, t.z = a.y + a.z, t.w = a.z + a.w;
+    }
+  };
+  // per stage, the other colour of the thread's cells in the plane after the
+  // one last passed
+  float4 cz[NS][KQ][2];
+  issue(0, 0);
+  issue(1, 1);
+  bool ok = true;
+  int si = 0;               // the slot of plane i: i mod NSL
+  unsigned phase = 0;       // its barrier's phase parity: (i / NSL) & 1
+  auto slot = [&](int d) {  // the slot of plane i - d (0 <= d < NSL)
+    const int t = si - d;
+    return t < 0 ? t + NSL : t;
+  };
+  for (int i = 0; i < P; i++) {
+    if (!FRESH) ok = mbar_wait(smem_addr(&bar[si]), phase) && ok;
+    float4 fw[KQ][2];  // the last stage's new values: the z+1 values of the next stage
+#pragma unroll
+    for (int s = 1; s <= NS; s++) {
+      const int j = i - s;
+      if (j >= s && j <= P - 1 - s) {  // uniform over the CTA
+        const int c = (s - 1) & 1, o = 1 - c;
+        const int first = FRESH ? (s <= 2 ? s : 0) : 0;
+        // x = 2h + bb: the parity is the same for all of the thread's rows (RK is even)
+        const int bb = (c + y0 - NS + rb + z0 - NS + j + 1) & 1;
+        float* S = ssm + slot(s) * SL + (rb << LG) + h4;
+        const float* Sm = ssm + slot(s + 1) * SL + (rb << LG) + h4;
+        const float* Sp = ssm + slot(s - 1) * SL + (rb << LG) + h4;
+#pragma unroll
+        for (int k = 0; k < KQ; k++) {
+          const int r = rb + k * RK;
+          const bool act = r >= s && r <= R - 1 - s;
+          const unsigned m = __ballot_sync(0xffffffffu, act);  // whole rows are active or not
+          if (act) {
+            const int ro = k * RK * HH;
+            float4 s0 = make_float4(0.f, 0.f, 0.f, 0.f), s1 = s0, xv = s0;
+            if (first != 1) {
+              auto f4 = [](const float* p) { return *reinterpret_cast<const float4*>(p); };
+              // the other colour of this plane was the z+1 value of the pass
+              // over plane j-1, unchanged since
+              float4 a0, a1, zp0, zp1;
+              if (j > s) {
+                a0 = cz[s - 1][k][0], a1 = cz[s - 1][k][1];
+              } else {
+                a0 = f4(S + o * AR + ro), a1 = f4(S + (2 + o) * AR + ro);
+              }
+              if (s == 1) {
+                zp0 = f4(Sp + o * AR + ro), zp1 = f4(Sp + (2 + o) * AR + ro);
+              } else {
+                zp0 = fw[k][0], zp1 = fw[k][1];
+              }
+              const float4 zm0 = f4(Sm + o * AR + ro), zm1 = f4(Sm + (2 + o) * AR + ro);
+              cz[s - 1][k][0] = zp0, cz[s - 1][k][1] = zp1;
+              float4 t0, t1;
+              xsum(a0, bb, m, t0);
+              xsum(a1, bb, m, t1);
+              const float4 ym0 = f4(S + o * AR + ro - HH), yp0 = f4(S + o * AR + ro + HH);
+              const float4 ym1 = f4(S + (2 + o) * AR + ro - HH), yp1 = f4(S + (2 + o) * AR + ro + HH);
+              s0.x = t0.x + ym0.x + yp0.x, s0.y = t0.y + ym0.y + yp0.y;
+              s0.z = t0.z + ym0.z + yp0.z, s0.w = t0.w + ym0.w + yp0.w;
+              s0.x += zm0.x + zp0.x, s0.y += zm0.y + zp0.y, s0.z += zm0.z + zp0.z, s0.w += zm0.w + zp0.w;
+              s1.x = t1.x + ym1.x + yp1.x, s1.y = t1.y + ym1.y + yp1.y;
+              s1.z = t1.z + ym1.z + yp1.z, s1.w = t1.w + ym1.w + yp1.w;
+              s1.x += zm1.x + zp1.x, s1.y += zm1.y + zp1.y, s1.z += zm1.z + zp1.z, s1.w += zm1.w + zp1.w;
+              if (first == 0) xv = f4(S + c * AR + ro);
+            }
+            const float4 pb = v[s - 1][k][0], g0 = v[s - 1][k][1], g1 = v[s - 1][k][2];
+            float4 r0, r1;
+            newton_cell(L, pb.x, xv.x, s0.x, s1.x, g0.x, g1.x, r0.x, r1.x);
+            newton_cell(L, pb.y, xv.y, s0.y, s1.y, g0.y, g1.y, r0.y, r1.y);
+            newton_cell(L, pb.z, xv.z, s0.z, s1.z, g0.z, g1.z, r0.z, r1.z);
+            newton_cell(L, pb.w, xv.w, s0.w, s1.w, g0.w, g1.w, r0.w, r1.w);
+            if (!ok) r0 = r1 = make_float4(nanf(""), nanf(""), nanf(""), nanf(""));  // a copy never landed
+            *reinterpret_cast<float4*>(S + c * AR + ro) = r0;
+            *reinterpret_cast<float4*>(S + (2 + c) * AR + ro) = r1;
+            fw[k][0] = r0, fw[k][1] = r1;
+          }
+        }
+      }
+      load(s, i + 1 - s);  // the next pass's cells of this stage, in flight while the others compute
+    }
+    __syncthreads();  // rows y+-1 of this pass are read by the next; the slot below is free
+    issue(i + 2, slot(NSL - 2));  // plane i + 2 into the slot of plane i - NS - 1, which stage NS read last
+    const int j = i - NS;
+    if (j >= NS && j <= P - 1 - NS) {  // plane j is final: rows NS .. NS+TY-1 of the slot
+      const float* S = ssm + slot(NS) * SL + NS * HH;
+      float* D = EO + (unsigned)(((z0 - NS + j) * n1 + y0) * HH);
+      constexpr int n4 = (TY * HH) >> 2;
+#pragma unroll
+      for (int q = threadIdx.x; q < 4 * n4; q += kSmThreads) {
+        const int a = q / n4, t = q - a * n4;
+        reinterpret_cast<float4*>(D + (unsigned)a * half)[t] = reinterpret_cast<const float4*>(S + a * AR)[t];
+      }
+    }
+    if (++si == NSL) si = 0, phase ^= 1u;
+  }
+  if (!ok)  // a wait gave up: give the copies still in flight a bounded time to land before the block exits
+    for (int b = 0; b < NSL; b++) mbar_wait(smem_addr(&bar[b]), 0u), mbar_wait(smem_addr(&bar[b]), 1u);
 }
 
 // RestrictSolution on e and on the base field: coarse e = ec = R(e_fine),
@@ -1031,10 +1272,45 @@ int launch_staged(Hier& H, const BoxLev& L, int c, int first) {
   return after_launch(H, 1);
 }
 
+// The one-pass smoothing (box_sweep 3): 3D levels whose colour rows hold 128
+// cells (tiles of 8 rows; the ring fills 224 KB of shared memory), at least
+// one tile and its halo per plane.  Levels of 64-cell rows (tiles of 16 rows)
+// compile but measured slower than four sweeps on a GB300 (128^3: 62 against
+// 36 us: 64 CTAs), so they keep the sweeps.
+int smooth_rows(const BoxLev& L) {
+  const int ty = L.hh == 128 ? 8 : 0;
+  return ty && L.n[1] % ty == 0 && L.n[1] >= ty + 2 * kSmStages ? ty : 0;
+}
+bool smooth_fits(const Hier& H, const BoxLev& L) {
+  return H.ndims == 3 && L.n[2] >= kSmStages && smooth_rows(L) > 0;
+}
+
+// out_oe = e after two red-black passes from e at in.oe (fresh: from zero)
+int bx_smooth(Hier& H, const BoxLev& in, long long out_oe, bool fresh) {
+  const int ty = smooth_rows(in);
+  const int ytiles = in.n[1] / ty;
+  int nz = std::max(1, std::min(H.box_sms / ytiles, in.n[2] / kSmMinPlanes));
+  size_t smem = (size_t)smooth_slots(kSmStages) * smooth_slot_floats(ty, in.hh) * sizeof(float);
+  static std::atomic<unsigned long long> attr;  // the kernels' shared-memory limit, per device
+  if (needs_setup(attr, H.ctx->device)) {
+    for (auto kf : {k_bx_smooth<8, 128, true>, k_bx_smooth<8, 128, false>}) {
+      cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_bx_smooth)");
+    }
+    mark_setup(attr, H.ctx->device);
+  }
+  auto ker = fresh ? k_bx_smooth<8, 128, true> : k_bx_smooth<8, 128, false>;
+  ker<<<ytiles * nz, kSmThreads, smem, H.s>>>(H.fpool, in, out_oe, nz);
+  return after_launch(H, 1);
+}
+bool smooth_applies(const Hier& H, const BoxLev& L, int nsmooth) {
+  return H.box_sweep == 3 && nsmooth == 2 && L.oe2 >= 0;
+}
+
 int bx_relax(Hier& H, int level, int c, int first) {
   BoxLev& L = B(H, level);
   if (staged_relax(H, L)) return launch_staged(H, L, c, first);
-  if (H.box_sweep == 1 && H.ndims == 3 && L.n[1] % 4 == 0) {
+  if ((H.box_sweep == 1 || H.box_sweep == 3) && H.ndims == 3 && L.n[1] % 4 == 0) {
     // four rows per thread at five blocks per SM (40 registers): four
     // cells' loads in flight per thread
     Launch sh = shape(L.hh, L.n[1] / 4, L.n[2]);
@@ -1090,6 +1366,21 @@ int bx_vcycle(Hier& H, int level, int minlevel, int nsmooth, bool fresh) {
     if (H.ndims == 2) k_bx_small_vcycle<2><<<1, kSmallThreads, 0, H.s>>>(H.fpool, S, nsmooth, fresh ? 1 : 0);
     else k_bx_small_vcycle<3><<<1, kSmallThreads, 0, H.s>>>(H.fpool, S, nsmooth, fresh ? 1 : 0);
     return after_launch(H, 1);
+  }
+  if (level > minlevel && smooth_applies(H, B(H, level), nsmooth)) {
+    // one-pass smoothings: e to the level's second array before the
+    // coarse correction and back after it
+    BoxLev F = B(H, level), Fb = F;
+    Fb.oe = F.oe2;
+    const BoxLev& C = B(H, level - 1);
+    Launch sc = shape(C.n[0], C.n[1], C.n[2]);
+    int r = bx_smooth(H, F, F.oe2, fresh);
+    if (r) return r;
+    BX_LAUNCH(H, sc, k_bx_restrict_load, H.fpool, Fb, C);
+    BX_LAUNCH(H, sc, k_bx_coarse_op, H.fpool, C);
+    if ((r = bx_vcycle(H, level - 1, minlevel, nsmooth, false))) return r;
+    BX_LAUNCH(H, sc, k_bx_prolong, H.fpool, Fb, C);
+    return bx_smooth(H, Fb, F.oe, false);
   }
   int r = bx_level_relax(H, level, nsmooth, fresh, level == minlevel);
   if (r) return r;
@@ -1345,6 +1636,11 @@ size_t box_layout(Hier& H) {
       L.opb = o; o = al(o + 2 * L.half);
       L.oec = o; o = al(o + 4 * L.half);
     }
+    L.oe2 = -1;
+    if (l > H.minlevel && smooth_fits(H, L)) {  // the one-pass smoothing's output
+      L.oe2 = o;
+      o = al(o + 4 * L.half);
+    }
   }
   box_coefficients(H);
   const BoxLev& F = H.blev[H.maxlevel + kMaxDepth];
@@ -1353,6 +1649,15 @@ size_t box_layout(Hier& H) {
 }
 
 int box_enq_relax(Hier& H, int level, int ipass) { return bx_relax(H, level, ipass - 1, 0); }
+
+int box_smoother_colours(const Hier& H, int level) {
+  return level > H.minlevel && smooth_applies(H, H.blev[level + kMaxDepth], 2) ? 4 : 1;
+}
+
+int box_enq_smoother(Hier& H, int level, int ipass) {
+  if (box_smoother_colours(H, level) == 4) return bx_smooth(H, B(H, level), B(H, level).oe2, false);
+  return bx_relax(H, level, ipass - 1, 0);
+}
 
 int box_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycles, double tol, int errortype,
                    int strict, int* ncycles, double* residuals) {

@@ -19,5 +19,10 @@ int box_iterations(Hier& H, int finest, int minlevel, int nsmooth, int maxvcycle
                    int strict, int* ncycles, double* residuals);
 // one colour sweep of the FP32 correction smoother on `level`
 int box_enq_relax(Hier& H, int level, int ipass);
+// colour half-sweeps of one launch of the smoother the V-cycle runs on
+// `level` (4 where it smooths in one pass, else 1), and one such launch
+// (the one-pass smoothing writes the level's second e array)
+int box_smoother_colours(const Hier& H, int level);
+int box_enq_smoother(Hier& H, int level, int ipass);
 
 }  // namespace bsamg

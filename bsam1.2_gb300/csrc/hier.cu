@@ -1283,7 +1283,7 @@ int bsamg_hier_reset(bsamg_hier* h) {
 }
 
 int bsamg_set_box_sweep(bsamg_hier* h, int kind) {
-  if (!h || kind < 0 || kind > 2) return BSAMG_ERR_ARG;
+  if (!h || kind < 0 || kind > 3) return BSAMG_ERR_ARG;
   h->box_g_valid = false;
   int r = set_device(*h);
   if (r) return r;
@@ -1405,7 +1405,9 @@ int bsamg_time_smoother(bsamg_hier* h, int level, int mode, int reps, double* ms
   h->box_g_valid = false;  // the sweeps overwrite the box path's e
   RET(bsamg_mark(h, 62));
   for (int r = 0; r < reps; r++)
-    RET(mode == BSAMG_MODE_FP64 ? enq_relax(*h, level, 1 + (r & 1)) : mixed_enq_relax(*h, level, 1 + (r & 1)));
+    RET(mode == BSAMG_MODE_FP64 ? enq_relax(*h, level, 1 + (r & 1))
+                                : (h->box && h->fpool ? box_enq_smoother(*h, level, 1 + (r & 1))
+                                          : mixed_enq_relax(*h, level, 1 + (r & 1))));
   RET(bsamg_mark(h, 63));
   double ms;
   RET(bsamg_elapsed_ms(h, 62, 63, &ms));
@@ -1427,8 +1429,7 @@ int bsamg_host_unregister(void* ptr) {
 
 int bsamg_smoother_colours(bsamg_hier* h, int level, int mode, int* colours) {
   if (!h || !h->committed || !level_ok(*h, level) || !colours) return BSAMG_ERR_ARG;
-  (void)mode;
-  *colours = 1;  // every smoother launch updates one colour
+  *colours = mode == BSAMG_MODE_MIXED && h->box && h->fpool ? box_smoother_colours(*h, level) : 1;
   return BSAMG_OK;
 }
 

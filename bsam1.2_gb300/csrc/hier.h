@@ -143,7 +143,10 @@ struct Hier {
   // periodic-box mixed path (box.cu): every level one periodic box with even
   // extents covering its parent; FP64 iterate held as float pairs
   bool box = false;
-  int box_sweep = 1;  // 3D box colour sweep (box.cu): 0 two rows a thread, 1 four, 2 rows staged by bulk copies
+  // 3D box smoothing (box.cu): colour sweeps of two (0) or four (1) rows a
+  // thread or rows staged by bulk copies (2); 3: a level's V(2,2) smoothing in
+  // one pass where it applies, four-row sweeps elsewhere
+  int box_sweep = 3;
   // the box path's g holds the true residual of the finest level at the
   // current q for the f in fhi/flo (set when box_iterations returns; any
   // entry point that changes fields or coefficients clears it)

@@ -67,6 +67,7 @@ struct BoxLev {
   int pad;
   long long half;  // cells of one colour
   long long oe, og, opb, oec;   // float offsets: e, g, pb, ec (ec: levels below the finest)
+  long long oe2;                // a second e (the one-pass smoothing's output), -1: none
   float c0, c1, tmp3, a12;      // dt/h^2, eps^2/h^2, (4|6) eps^2/h^2, (4|6) dt/h^2
   float c0h, c0l, c1h, c1l;     // dt/h^2 and eps^2/h^2 as float pairs (hi + lo)
   double cd[4];                 // c0, c1, tmp3, a12 in FP64 (the coarsest level's FP64 smoother)

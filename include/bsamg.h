@@ -290,13 +290,16 @@ int bsamg_graph_stats(const bsamg_hier* h, int* instantiated, int* updated);
  * same results as on a newly built hierarchy. */
 int bsamg_set_params(bsamg_hier* h, const double* params, int nparams);
 int bsamg_hier_reset(bsamg_hier* h);
-/* Tuning (no reference counterpart): the colour sweep of 3D levels on the
- * periodic-box mixed path.  0: each thread relaxes two rows' cells;
- * 1 (the default): four rows' cells, all loads issued before any store;
+/* Tuning (no reference counterpart): the smoothing of 3D levels on the
+ * periodic-box mixed path.  0: colour sweeps, each thread relaxing two
+ * rows' cells; 1: four rows' cells, all loads issued before any store;
  * 2: rows staged in shared memory by bulk asynchronous copies, for rows of
  * 128 to 512 cells (measured slower than 1 on a GB300; kept as the staged
- * alternative).  All three evaluate the same expressions.  Drops the
- * hierarchy's captured graphs. */
+ * alternative; it sums the neighbours in another order); 3 (the default):
+ * a level visit's V(2,2) smoothing (four colour half-sweeps) as one pass
+ * over z-planes staged in shared memory, on levels with rows of 256 cells,
+ * and the four-row sweeps elsewhere.  0, 1 and 3 give the same bits.
+ * Drops the hierarchy's captured graphs. */
 int bsamg_set_box_sweep(bsamg_hier* h, int kind);
 /* Tuning (no reference counterpart): the mixed V-cycle runs its coarse
  * tail -- the levels from minlevel up to the highest one at which the
@@ -376,13 +379,15 @@ int bsamg_solve_trace_read(const bsamg_hier* h, int cap, int* op, int* n, long l
  * bsamg_elapsed_ms waits for event b and returns the time from a to b. */
 int bsamg_mark(bsamg_hier* h, int slot);
 int bsamg_elapsed_ms(bsamg_hier* h, int a, int b, double* ms);
-/* Launches the colour smoother of `level` reps times (alternating red and
- * black) in the given mode on the current state and returns the mean device
- * time of one launch; the state is modified. */
+/* Launches the smoother of `level` reps times in the given mode on the
+ * current state and returns the mean device time of one launch; the state
+ * is modified.  A launch is one colour half-sweep (alternating red and
+ * black), or, where the periodic-box mixed path smooths the level in one
+ * pass (bsamg_set_box_sweep 3), one V(2,2) smoothing. */
 int bsamg_time_smoother(bsamg_hier* h, int level, int mode, int reps,
                         double* ms_per_launch);
-/* Colours one launch of that smoother updates (1: each launch is one
- * colour half-sweep). */
+/* Colour half-sweeps one launch of that smoother performs (1, or 4 for the
+ * one-pass smoothing). */
 int bsamg_smoother_colours(bsamg_hier* h, int level, int mode, int* colours);
 
 /* Allocation-free convergence norm of one CH patch.  No counterpart in the

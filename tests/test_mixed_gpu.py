@@ -159,15 +159,17 @@ def test_mixed_growth_reaches_the_fp64_solution(pkg, ctx, amr):
 
 
 def test_box_sweep_forms_agree(pkg, ctx):
-    """The three forms of the 3D periodic-box colour sweep (two or four rows
-    per thread, or rows staged in shared memory by bulk copies) evaluate the
-    same expressions on the same values.  The two direct forms are
-    bit-identical after mixed time steps on a 128^3 box; the staged one
-    agrees to FP32 rounding of the converged iterates and takes the same
-    number of V-cycles (within one)."""
+    """The forms of the 3D periodic-box smoothing (two or four rows per
+    thread, rows staged in shared memory by bulk copies, or a whole V(2,2)
+    smoothing in one pass over z-planes staged in shared memory) evaluate
+    the same expressions on the same values.  The two direct forms and the
+    one-pass form are bit-identical after mixed time steps on a 128^3 box;
+    the staged one sums the neighbours in another order, so it agrees to
+    FP32 rounding of the converged iterates and takes the same number of
+    V-cycles (within one)."""
     n = 128
     out = {}
-    for kind in (0, 1, 2):
+    for kind in (0, 1, 2, 3):
         h = pkg.Hierarchy(ctx, 3, 2, "ch", [5e-4, 0.02])
         h.build_uniform([n] * 3, -6, [2] * 6, [0, 0, 0], [1, 1, 1])
         h.commit()
@@ -176,18 +178,41 @@ def test_box_sweep_forms_agree(pkg, ctx):
         hist = [h.time_step(s == 0, 0, -6, tol=1e-9, maxvcycles=30, mode="mixed", strict=True) for s in range(3)]
         out[kind] = (hist, h.get(0, "q"))
         h.close()
-    (h0, q0), (h1, q1), (h2, q2) = out[0], out[1], out[2]
-    assert h0 == h1
+    (h0, q0), (h1, q1), (h2, q2), (h3, q3) = out[0], out[1], out[2], out[3]
+    assert h0 == h1 == h3
     assert np.array_equal(q0, q1)
+    assert np.array_equal(q0, q3)
     assert all(abs(a[0] - b[0]) <= 1 for a, b in zip(h2, h0)), (h2, h0)
     k = q0.size // 2
     assert np.max(np.abs(q2[:k] - q0[:k])) <= 1e-6 * np.max(np.abs(q0[:k]))
     with pytest.raises(pkg.BsamgError):
         h = pkg.Hierarchy(ctx, 3, 2, "ch", [5e-4, 0.02])
         try:
-            h.set_box_sweep(3)
+            h.set_box_sweep(4)
         finally:
             h.close()
+
+
+@pytest.mark.parametrize("mx,minlevel", [((256, 64, 32), -4), ((256, 16, 8), -2), ((256, 256, 16), -3)])
+def test_box_one_pass_smoothing_bit_identical(pkg, ctx, mx, minlevel):
+    """The one-pass V(2,2) smoothing on boxes whose halo rows and planes wrap
+    around the box, with one or several tiles per plane and z ranges shorter
+    than the halo: the mixed time steps equal the four-row sweeps' bit for
+    bit, residual histories included (8 V-cycles a step, converged or not)."""
+    out = {}
+    for kind in (1, 3):
+        h = pkg.Hierarchy(ctx, 3, 2, "ch", [5e-4, 0.02])
+        h.build_uniform(list(mx), minlevel, [2] * 6, [0, 0, 0], [1, mx[1] / mx[0], mx[2] / mx[0]])
+        h.commit()
+        h.set_box_sweep(kind)
+        h.seed_spinodal(0, 23, mean=0.1, amp=0.05)
+        hist = [h.time_step(s == 0, 0, minlevel, tol=1e-12, maxvcycles=8, mode="mixed", strict=False)
+                for s in range(3)]
+        out[kind] = (hist, h.get(0, "q"))
+        h.close()
+    (ha, qa), (hb, qb) = out[1], out[3]
+    assert ha == hb
+    assert np.array_equal(qa, qb)
 
 
 def test_box_step_reuses_the_last_residual(pkg, ctx):
