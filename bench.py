@@ -679,9 +679,13 @@ def main():
     ap.add_argument("--serve-blocking-wait", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--maxv", type=int, default=MAXV,
+                    help="V-cycles allowed per step; above 64 the periodic-box solve runs its host loop "
+                         "instead of one graph launch (the same cycles, launched one by one)")
     ap.add_argument("--box-sweep", type=int, default=None,
                     help="smoothing form of periodic-box levels (bsamg_set_box_sweep); default: the library's")
     args = ap.parse_args()
+    globals()["MAXV"] = args.maxv
     dist = Dist()
     if args.workload == "serve":
         if args.impl == "reference":
