@@ -503,10 +503,12 @@ class Hierarchy:
 
     def regrid_timing(self):
         """Host ms of the regrid that made this hierarchy (bsamg_regrid_timing):
-        download, host model, create + commit, upload, ghost compilation, rest of commit."""
-        v = (ctypes.c_double * 6)()
-        _ck(lib().bsamg_regrid_timing(self.h, v, 6), "bsamg_regrid_timing")
-        return dict(zip(("download", "model", "commit", "upload", "ghost_compile", "commit_rest"), list(v)))
+        download, host model, create + commit, upload, ghost compilation, rest of commit, and the
+        model's parts (ghost fill, tagging, edge-tag inflation, clustering, new patches, transfer)."""
+        v = (ctypes.c_double * 12)()
+        _ck(lib().bsamg_regrid_timing(self.h, v, 12), "bsamg_regrid_timing")
+        return dict(zip(("download", "model", "commit", "upload", "ghost_compile", "commit_rest", "m_ghost",
+                         "m_tag", "m_inflate", "m_cluster", "m_new", "m_transfer"), list(v)))
 
     def solve_trace(self, enable=True):
         """Record per-phase clocks of the next one-launch solves (bsamg_solve_trace)."""

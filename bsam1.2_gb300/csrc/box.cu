@@ -361,7 +361,9 @@ __global__ void __launch_bounds__(256, MINB) k_bx_relax(float* __restrict__ fp, 
 // z+1 (periodic wrap).  Persistent CTAs walk the tiles plane by plane, the
 // next tile's rows in flight while the current one is computed, so the
 // memory system always has whole rows outstanding instead of one word per
-// thread.  Every expression is relax_at's, evaluated in the same order.
+// thread.  The cell update is relax_at's (newton_cell); the six neighbours
+// are summed left to right, where relax_at adds the two z-neighbours as a
+// pair, so the values agree to rounding, not bit for bit.
 constexpr int kTileThreads = 256;
 constexpr long long kWaitLimit = 1ll << 24;  // mbarrier polls before giving up
 

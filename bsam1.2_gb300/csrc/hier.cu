@@ -1352,7 +1352,7 @@ int bsamg_solve_info(const bsamg_hier* h, long long* info, int n) {
 
 int bsamg_regrid_timing(const bsamg_hier* h, double* ms, int n) {
   if (!h || !ms || n < 0) return BSAMG_ERR_ARG;
-  for (int x = 0; x < n && x < 6; x++) ms[x] = h->regrid_ms[x];
+  for (int x = 0; x < n && x < 12; x++) ms[x] = h->regrid_ms[x];
   return BSAMG_OK;
 }
 

@@ -134,7 +134,7 @@ struct Hier {
   // the host model (tagging, clustering, new patches' values), creating and
   // committing the new hierarchy, the upload; and of commit: the ghost
   // programs' compilation, everything else
-  double regrid_ms[6] = {};
+  double regrid_ms[12] = {};
   bool solve_trace_on = false;
   long long* solve_trace = nullptr;  // device, solve_trace_cap + 1 clocks
   int solve_trace_cap = 0;

@@ -549,6 +549,13 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
 
   int next_id = prm.first_id;
   int level;
+  double part[6] = {};  // host ms of the model's parts, summed over levels
+  clk::time_point tp = clk::now();
+  auto lap = [&](int x) {
+    const clk::time_point t = clk::now();
+    part[x] += ms(tp, t);
+    tp = t;
+  };
   // a level's patches in visiting order (youngest first: the reverse of
   // creation order, as ApplyOnLevel walks them), so that RefineGrid runs
   // over the parents, and creates their children, in the reference's order
@@ -561,7 +568,9 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   for (level = 0; level < prm.maxlevel; level++) {  // AMR(level), :966-991
     std::vector<int> lp = level_patches(level);
     if (lp.empty()) break;
+    tp = clk::now();
     if ((r = host_set_ghost(M, level))) return r;
+    lap(0);
     std::vector<Flags> fl(lp.size());
     std::vector<Tag> list;
     int ib = prm.ibuffer[level];
@@ -573,6 +582,7 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
       });
       for (auto& v : lists) list.insert(list.end(), v.begin(), v.end());
     }
+    lap(1);
     if (!list.empty()) {  // InflateEdgeTags
       Hier T;
       if ((r = host_tables(M, T))) return r;
@@ -612,6 +622,7 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
         }
       });
     }
+    lap(2);
     size_t first_new = M.g.size();
     {  // GridAdapt -> RefineGrid: each parent's clustering on the thread pool,
        // the children made in the parents' order (their ids and visiting
@@ -622,6 +633,7 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
         ok[a] = new_sub_grids(nd, M.g[lp[a]], fl[a], prm, subs_of[a]) ? 1 : 0;
         if (ok[a]) split_long(nd, prm.maxside, subs_of[a]);
       });
+      lap(3);
       std::vector<std::pair<int, const Sub*>> made;  // (parent, box) of each new child
       for (size_t a = 0; a < lp.size(); a++) {
         if (!ok[a]) return BSAMG_ERR_ARG;
@@ -635,6 +647,7 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
           init_from_parent(M, (int)(first_new + x), made[x].first, made[x].second->b);
         });
     }
+    lap(4);
     std::vector<int> olds;  // TransferValues from the previous level-(l+1) patches
     for (size_t n = 0; n < H.patches.size(); n++)
       if (H.patches[n].level == level + 1) olds.push_back((int)n);
@@ -642,6 +655,7 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
       size_t c = first_new + x;
       for (int n : olds) transfer_overlap(nv, H.patches[n], oldq[n], M.g[c], M.q[c], nd);
     });
+    lap(5);
   }
   // AMR(finest) ends with SetGhost(finest, 0); nothing on the host reads its
   // result, so it runs on the device after the upload (the compiled program
@@ -729,6 +743,7 @@ int regrid(Hier& H, const bsamg_regrid_params& prm, bsamg_qinit_fn qinit, void* 
   N.regrid_ms[1] = ms(t1, t2);
   N.regrid_ms[2] = ms(t2, t3);
   N.regrid_ms[3] = ms(t3, t4);
+  for (int x = 0; x < 6; x++) N.regrid_ms[6 + x] = part[x];
   *out = nh;
   return BSAMG_OK;
 }

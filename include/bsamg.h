@@ -352,7 +352,10 @@ int bsamg_solve_info(const bsamg_hier* h, long long* info, int n);
  * counterpart: measurement): [0] download of q, [1] the host model
  * (tagging, clustering, the new patches' values), [2] creating and
  * committing the new hierarchy, [3] the upload; [4] and [5] the part of [2]
- * spent compiling ghost programs and the rest of the commit. */
+ * spent compiling ghost programs and the rest of the commit; [6] .. [11]
+ * the parts of [1], summed over levels: ghost fill, tagging and buffer
+ * lists, edge-tag inflation, clustering, the new patches and their values,
+ * TransferValues.  n entries are written (at most 12). */
 int bsamg_regrid_timing(const bsamg_hier* h, double* ms, int n);
 /* Autotuner of the mixed solve of adaptive hierarchies (no reference
  * counterpart).  While on (the default), the first mixed solve of an
