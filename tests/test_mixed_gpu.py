@@ -247,3 +247,25 @@ def test_box_step_reuses_the_last_residual(pkg, ctx):
         np.testing.assert_allclose(ra, rb, rtol=1e-6, atol=1e-12)
     k = qa.size // 2
     assert np.max(np.abs(qa[:k] - qb[:k])) <= 1e-9 * np.max(np.abs(qb[:k]))
+
+
+def test_box_smoother_timing_reports_the_one_pass_form(pkg, ctx):
+    """bsamg_time_smoother times the smoother the V-cycle runs on a level:
+    on a 256-wide periodic box level one launch is a whole V(2,2) smoothing
+    (four colour half-sweeps), elsewhere one colour sweep; the FP64 path
+    always sweeps one colour.  After the timing launches a time step still
+    converges (the one-pass launches write only the level's second e array,
+    the sweeps only e, which every cycle starts from zero)."""
+    for mx, minlevel, kind, want in (((256, 16, 8), -2, 3, 4), ((256, 16, 8), -2, 1, 1), ((128, 128, 8), -2, 3, 1)):
+        h = pkg.Hierarchy(ctx, 3, 2, "ch", [5e-4, 0.02])
+        h.build_uniform(list(mx), minlevel, [2] * 6, [0, 0, 0], [1, mx[1] / mx[0], mx[2] / mx[0]])
+        h.commit()
+        h.set_box_sweep(kind)
+        h.seed_spinodal(0, 5, mean=0.1, amp=0.05)
+        assert h.smoother_colours(0, "mixed") == want, (mx, kind)
+        assert h.smoother_colours(0, "fp64") == 1
+        assert h.smoother_colours(minlevel, "mixed") == 1
+        assert h.time_smoother(0, "mixed", reps=3) > 0.0
+        n, res = h.time_step(True, 0, minlevel, tol=1e-6, maxvcycles=30, mode="mixed", strict=False)
+        assert np.isfinite(res[-1])
+        h.close()
