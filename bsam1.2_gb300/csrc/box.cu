@@ -525,16 +525,34 @@ __host__ __device__ constexpr long long smooth_slot_floats(int ty, int hh, int n
 }
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
 
-template <int TY, int HH, bool FRESH, int NS = kSmStages>
-__global__ void __launch_bounds__(kSmThreads, 1) k_bx_smooth(float* __restrict__ fp, BoxLev L, long long oe_out,
-                                                            int nz) {
+// CPT consecutive cells of a colour row per thread (4: float4 rows, 2:
+// float2), NT threads per CTA
+template <int CPT>
+__device__ __forceinline__ void ldv(const float* p, float* v) {
+  if constexpr (CPT == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+  } else {
+    const float2 t = *reinterpret_cast<const float2*>(p);
+    v[0] = t.x, v[1] = t.y;
+  }
+}
+template <int CPT>
+__device__ __forceinline__ void stv(float* p, const float* v) {
+  if constexpr (CPT == 4) *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  else *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+}
+
+template <int TY, int HH, bool FRESH, int NS = kSmStages, int CPT = 4, int NT = kSmThreads>
+__global__ void __launch_bounds__(NT, 1) k_bx_smooth(float* __restrict__ fp, BoxLev L, long long oe_out, int nz) {
   extern __shared__ __align__(128) float ssm[];
   constexpr int NSL = smooth_slots(NS);
   constexpr int R = TY + 2 * NS, AR = R * HH, SL = 4 * AR, LG = ilog2(HH);
-  constexpr int W = HH / 4;                 // threads of a colour row: four consecutive cells each
-  constexpr int RK = kSmThreads / W;        // rows between a thread's row segments
+  constexpr int W = HH / CPT;               // threads of a colour row: CPT consecutive cells each
+  constexpr int RK = NT / W;                // rows between a thread's row segments
   constexpr int KQ = (R + RK - 1) / RK;     // row segments of a thread (the same rows in every stage)
-  static_assert((1 << LG) == HH && W <= 32 && (W & (W - 1)) == 0 && RK % 2 == 0, "rows of 4 x 2^k cells");
+  constexpr bool CARRY = CPT == 4;          // registers for the carried in-plane values
+  static_assert((1 << LG) == HH && HH % 4 == 0 && RK % 2 == 0 && (CPT == 2 || CPT == 4), "rows of 2^k cells");
   __shared__ __align__(8) unsigned long long bar[NSL];
   const int n1 = L.n[1], n2 = L.n[2];
   const unsigned half = (unsigned)L.half;  // a level's cells are fewer than 2^31
@@ -547,14 +565,16 @@ __global__ void __launch_bounds__(kSmThreads, 1) k_bx_smooth(float* __restrict__
   const float* PB = fp + L.opb;
   float* EO = fp + oe_out;
   auto wrap = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
-  // this thread's cells h4 .. h4+3 of rows rb + k RK: the same in every stage,
-  // so that a stage's z+1 values are the ones the thread computed in the
-  // stage before it, and no other thread writes what a stage reads in the
-  // same pass but the rows y+-1, which were written in the pass before
-  const int li = threadIdx.x & (W - 1), rb = threadIdx.x / W, h4 = 4 * li;
+  // this thread's cells hc .. hc+CPT-1 of rows rb + k RK: the same in every
+  // stage, so that a stage's z+1 values are the ones the thread computed in
+  // the stage before it, and no other thread writes what a stage reads in
+  // the same pass but the rows y+-1 and the row neighbours beyond the
+  // thread's cells, which were written in the pass before
+  const int li = threadIdx.x % W, rb = threadIdx.x / W, hc = CPT * li;
+  const int hm = (hc - 1) & (HH - 1), hp = (hc + CPT) & (HH - 1);  // the row's periodic wrap
   unsigned goff[KQ];  // the cells' offset within a plane of a colour-split array
 #pragma unroll
-  for (int k = 0; k < KQ; k++) goff[k] = (unsigned)(wrap(y0 - NS + rb + k * RK, n1) * HH + h4);
+  for (int k = 0; k < KQ; k++) goff[k] = (unsigned)(wrap(y0 - NS + rb + k * RK, n1) * HH + hc);
   if (threadIdx.x == 0) {
     for (int b = 0; b < NSL; b++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[b])));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -594,7 +614,7 @@ __global__ void __launch_bounds__(kSmThreads, 1) k_bx_smooth(float* __restrict__
   };
   // pb, g0, g1 of this thread's cells of stage s for the pass over local
   // plane j, in registers before that pass
-  float4 v[NS][KQ][3];
+  float v[NS][KQ][3][CPT];
   auto load = [&](int s, int j) {
     if (j < s || j > P - 1 - s) return;  // uniform over the CTA
     const unsigned c = (s - 1) & 1;
@@ -604,26 +624,15 @@ __global__ void __launch_bounds__(kSmThreads, 1) k_bx_smooth(float* __restrict__
       const int r = rb + k * RK;
       if (r >= s && r <= R - 1 - s) {
         const unsigned gi = zoff + goff[k];
-        v[s - 1][k][0] = *reinterpret_cast<const float4*>(PB + (c * half + gi));
-        v[s - 1][k][1] = *reinterpret_cast<const float4*>(G + (c * half + gi));
-        v[s - 1][k][2] = *reinterpret_cast<const float4*>(G + ((2 + c) * half + gi));
+        ldv<CPT>(PB + (c * half + gi), v[s - 1][k][0]);
+        ldv<CPT>(G + (c * half + gi), v[s - 1][k][1]);
+        ldv<CPT>(G + ((2 + c) * half + gi), v[s - 1][k][2]);
       }
-    }
-  };
-  // the x-neighbour sums of four cells of colour parity bb from the other
-  // colour's values a (cells h4 .. h4+3) and the row's periodic wrap:
-  // a[xm] + a[xp] with xm, xp = h, h+1 (bb = 1) or h-1, h (bb = 0)
-  auto xsum = [&](const float4 a, int bb, unsigned m, float4& t) {
-    const float left = __shfl_sync(m, a.w, li - 1 + W, W), right = __shfl_sync(m, a.x, li + 1, W);
-    if (bb) {
-      t.x = a.x + a.y, t.y = a.y + a.z, t.z = a.z + a.w, t.w = a.w + right;
-    } else {
-      t.x = left + a.x, t.y = a.x + a.y, t.z = a.y + a.z, t.w = a.z + a.w;
     }
   };
   // per stage, the other colour of the thread's cells in the plane after the
   // one last passed
-  float4 cz[NS][KQ][2];
+  float cz[NS][CARRY ? KQ : 1][2][CPT];
   issue(0, 0);
   issue(1, 1);
   bool ok = true;
@@ -635,7 +644,7 @@ __global__ void __launch_bounds__(kSmThreads, 1) k_bx_smooth(float* __restrict__
   };
   for (int i = 0; i < P; i++) {
     if (!FRESH) ok = mbar_wait(smem_addr(&bar[si]), phase) && ok;
-    float4 fw[KQ][2];  // the last stage's new values: the z+1 values of the next stage
+    float fw[KQ][2][CPT];  // the last stage's new values: the z+1 values of the next stage
 #pragma unroll
     for (int s = 1; s <= NS; s++) {
       const int j = i - s;
@@ -644,57 +653,67 @@ __global__ void __launch_bounds__(kSmThreads, 1) k_bx_smooth(float* __restrict__
         const int first = FRESH ? (s <= 2 ? s : 0) : 0;
         // x = 2h + bb: the parity is the same for all of the thread's rows (RK is even)
         const int bb = (c + y0 - NS + rb + z0 - NS + j + 1) & 1;
-        float* S = ssm + slot(s) * SL + (rb << LG) + h4;
-        const float* Sm = ssm + slot(s + 1) * SL + (rb << LG) + h4;
-        const float* Sp = ssm + slot(s - 1) * SL + (rb << LG) + h4;
+        float* S = ssm + slot(s) * SL + (rb << LG);
+        const float* Sm = ssm + slot(s + 1) * SL + (rb << LG);
+        const float* Sp = ssm + slot(s - 1) * SL + (rb << LG);
 #pragma unroll
         for (int k = 0; k < KQ; k++) {
           const int r = rb + k * RK;
-          const bool act = r >= s && r <= R - 1 - s;
-          const unsigned m = __ballot_sync(0xffffffffu, act);  // whole rows are active or not
-          if (act) {
+          if (r >= s && r <= R - 1 - s) {
             const int ro = k * RK * HH;
-            float4 s0 = make_float4(0.f, 0.f, 0.f, 0.f), s1 = s0, xv = s0;
+            float s0[CPT], s1[CPT], xv[CPT];
+#pragma unroll
+            for (int q = 0; q < CPT; q++) s0[q] = s1[q] = xv[q] = 0.f;
             if (first != 1) {
-              auto f4 = [](const float* p) { return *reinterpret_cast<const float4*>(p); };
-              // the other colour of this plane was the z+1 value of the pass
-              // over plane j-1, unchanged since
-              float4 a0, a1, zp0, zp1;
-              if (j > s) {
-                a0 = cz[s - 1][k][0], a1 = cz[s - 1][k][1];
-              } else {
-                a0 = f4(S + o * AR + ro), a1 = f4(S + (2 + o) * AR + ro);
+#pragma unroll
+              for (int var = 0; var < 2; var++) {
+                const int ao = (2 * var + o) * AR + ro;
+                float a[CPT], zp[CPT], zm[CPT], ym[CPT], yp[CPT];
+                // the other colour of this plane was the z+1 value of the
+                // pass over plane j-1, unchanged since
+                if (CARRY && j > s) {
+#pragma unroll
+                  for (int q = 0; q < CPT; q++) a[q] = cz[s - 1][CARRY ? k : 0][var][q];
+                } else {
+                  ldv<CPT>(S + ao + hc, a);
+                }
+                if (s == 1) {
+                  ldv<CPT>(Sp + ao + hc, zp);
+                } else {
+#pragma unroll
+                  for (int q = 0; q < CPT; q++) zp[q] = fw[k][var][q];
+                }
+                if (CARRY) {
+#pragma unroll
+                  for (int q = 0; q < CPT; q++) cz[s - 1][CARRY ? k : 0][var][q] = zp[q];
+                }
+                ldv<CPT>(Sm + ao + hc, zm);
+                ldv<CPT>(S + ao - HH + hc, ym);
+                ldv<CPT>(S + ao + HH + hc, yp);
+                // a[xm] + a[xp] with xm, xp = h, h+1 (bb = 1) or h-1, h (bb = 0)
+                const float edge = S[ao + (bb ? hp : hm)];
+                float* acc = var ? s1 : s0;
+#pragma unroll
+                for (int q = 0; q < CPT; q++) {
+                  const float lft = bb ? a[q] : (q ? a[q - 1] : edge);
+                  const float rgt = bb ? (q + 1 < CPT ? a[q + 1] : edge) : a[q];
+                  float t = lft + rgt + ym[q] + yp[q];
+                  t += zm[q] + zp[q];
+                  acc[q] = t;
+                }
               }
-              if (s == 1) {
-                zp0 = f4(Sp + o * AR + ro), zp1 = f4(Sp + (2 + o) * AR + ro);
-              } else {
-                zp0 = fw[k][0], zp1 = fw[k][1];
-              }
-              const float4 zm0 = f4(Sm + o * AR + ro), zm1 = f4(Sm + (2 + o) * AR + ro);
-              cz[s - 1][k][0] = zp0, cz[s - 1][k][1] = zp1;
-              float4 t0, t1;
-              xsum(a0, bb, m, t0);
-              xsum(a1, bb, m, t1);
-              const float4 ym0 = f4(S + o * AR + ro - HH), yp0 = f4(S + o * AR + ro + HH);
-              const float4 ym1 = f4(S + (2 + o) * AR + ro - HH), yp1 = f4(S + (2 + o) * AR + ro + HH);
-              s0.x = t0.x + ym0.x + yp0.x, s0.y = t0.y + ym0.y + yp0.y;
-              s0.z = t0.z + ym0.z + yp0.z, s0.w = t0.w + ym0.w + yp0.w;
-              s0.x += zm0.x + zp0.x, s0.y += zm0.y + zp0.y, s0.z += zm0.z + zp0.z, s0.w += zm0.w + zp0.w;
-              s1.x = t1.x + ym1.x + yp1.x, s1.y = t1.y + ym1.y + yp1.y;
-              s1.z = t1.z + ym1.z + yp1.z, s1.w = t1.w + ym1.w + yp1.w;
-              s1.x += zm1.x + zp1.x, s1.y += zm1.y + zp1.y, s1.z += zm1.z + zp1.z, s1.w += zm1.w + zp1.w;
-              if (first == 0) xv = f4(S + c * AR + ro);
+              if (first == 0) ldv<CPT>(S + c * AR + ro + hc, xv);
             }
-            const float4 pb = v[s - 1][k][0], g0 = v[s - 1][k][1], g1 = v[s - 1][k][2];
-            float4 r0, r1;
-            newton_cell(L, pb.x, xv.x, s0.x, s1.x, g0.x, g1.x, r0.x, r1.x);
-            newton_cell(L, pb.y, xv.y, s0.y, s1.y, g0.y, g1.y, r0.y, r1.y);
-            newton_cell(L, pb.z, xv.z, s0.z, s1.z, g0.z, g1.z, r0.z, r1.z);
-            newton_cell(L, pb.w, xv.w, s0.w, s1.w, g0.w, g1.w, r0.w, r1.w);
-            if (!ok) r0 = r1 = make_float4(nanf(""), nanf(""), nanf(""), nanf(""));  // a copy never landed
-            *reinterpret_cast<float4*>(S + c * AR + ro) = r0;
-            *reinterpret_cast<float4*>(S + (2 + c) * AR + ro) = r1;
-            fw[k][0] = r0, fw[k][1] = r1;
+            float r0[CPT], r1[CPT];
+#pragma unroll
+            for (int q = 0; q < CPT; q++) {
+              newton_cell(L, v[s - 1][k][0][q], xv[q], s0[q], s1[q], v[s - 1][k][1][q], v[s - 1][k][2][q], r0[q],
+                          r1[q]);
+              if (!ok) r0[q] = r1[q] = nanf("");  // a copy that never landed: poison the pass
+              fw[k][0][q] = r0[q], fw[k][1][q] = r1[q];
+            }
+            stv<CPT>(S + c * AR + ro + hc, r0);
+            stv<CPT>(S + (2 + c) * AR + ro + hc, r1);
           }
         }
       }
@@ -708,7 +727,7 @@ __global__ void __launch_bounds__(kSmThreads, 1) k_bx_smooth(float* __restrict__
       float* D = EO + (unsigned)(((z0 - NS + j) * n1 + y0) * HH);
       constexpr int n4 = (TY * HH) >> 2;
 #pragma unroll
-      for (int q = threadIdx.x; q < 4 * n4; q += kSmThreads) {
+      for (int q = threadIdx.x; q < 4 * n4; q += NT) {
         const int a = q / n4, t = q - a * n4;
         reinterpret_cast<float4*>(D + (unsigned)a * half)[t] = reinterpret_cast<const float4*>(S + a * AR)[t];
       }
