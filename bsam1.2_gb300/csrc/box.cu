@@ -525,8 +525,8 @@ __host__ __device__ constexpr long long smooth_slot_floats(int ty, int hh, int n
 }
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
 
-// CPT consecutive cells of a colour row per thread (4: float4 rows, 2:
-// float2), NT threads per CTA
+// CPT consecutive cells of a colour row as one vector access (4: float4,
+// 2: float2)
 template <int CPT>
 __device__ __forceinline__ void ldv(const float* p, float* v) {
   if constexpr (CPT == 4) {
@@ -543,6 +543,11 @@ __device__ __forceinline__ void stv(float* p, const float* v) {
   else *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
 }
 
+// TY rows a tile, HH cells a colour row, FRESH: the old e counts as zero (the
+// finest level's pre-smoothing), NS stages, CPT consecutive cells of a row a
+// thread, NT threads a CTA.  The library runs CPT = 4 at 512 threads (two
+// cells a thread at 1024 threads measured no faster: the kernel is bound by
+// its instructions, not by the warps it has to hide latency).
 template <int TY, int HH, bool FRESH, int NS = kSmStages, int CPT = 4, int NT = kSmThreads>
 __global__ void __launch_bounds__(NT, 1) k_bx_smooth(float* __restrict__ fp, BoxLev L, long long oe_out, int nz) {
   extern __shared__ __align__(128) float ssm[];
