@@ -116,3 +116,22 @@ def test_box_double_float_residual_equals_fp64_norm(pkg, ctx, n):
     assert abs(r2[-1] - f2) <= 1e-12, (r2, f2)
     assert f2 < 1e-8
     h.close()
+
+
+def test_ch3d_256_one_pass_smoothing_equals_the_sweeps(pkg, ctx):
+    """At the headline size the one-pass V(2,2) smoothing of the 256^3 level
+    (the default) and the four-row colour sweeps give the same mixed time
+    steps bit for bit: iterates and residual histories."""
+    out = {}
+    for kind in (1, 3):
+        h = pkg.Hierarchy(ctx, 3, 2, "ch", [DT, EPS])
+        h.build_uniform([256] * 3, -7, PERIODIC3, [0, 0, 0], [1, 1, 1])
+        h.commit()
+        h.set_box_sweep(kind)
+        assert h.smoother_colours(0, "mixed") == (4 if kind == 3 else 1)
+        h.seed_spinodal(0, SEED, mean=0.1, amp=0.05)
+        hist = [h.time_step(s == 0, 0, -7, 2, 30, 1e-8, mode="mixed", strict=True) for s in range(2)]
+        out[kind] = (hist, h.get(0, "q"))
+        h.close()
+    assert out[1][0] == out[3][0]
+    assert np.array_equal(out[1][1], out[3][1])
