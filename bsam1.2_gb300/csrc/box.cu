@@ -31,6 +31,9 @@
 // (Source2D/3D, :425-450, :672-695) and whose operator is
 // N(q) = (phi - dt/h^2 ULap(mu), mu - phi^3 + eps^2/h^2 ULap(phi))
 // (Operator2D/3D, :393-422, :638-669).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cstddef>
 #include <functional>
@@ -501,8 +504,9 @@ __global__ void __launch_bounds__(kTileThreads) k_bx_relax_tiled(float* __restri
 // half-sweeps 0, 1, 0, 1) in one pass over memory.  A CTA owns TY rows y0 ..
 // y0+TY-1 of the planes z0 .. z1-1 and streams the planes z0-NS .. z1+NS-1
 // through a ring of NS+3 shared-memory slots, each holding the four
-// colour-split e arrays of rows y0-NS .. y0+TY+NS-1 of one plane (one bulk
-// copy per array, two where the rows wrap).  Once plane i has landed, stage
+// colour-split e arrays of rows y0-NS .. y0+TY+NS-1 of one plane (TMA tensor
+// copies of four rows of one array, at row chunks wrapped around the plane).
+// Once plane i has landed, stage
 // s (half-sweep s) updates plane i-s: it needs the other colour of planes
 // i-s-1 .. i-s+1 at stage s-1, which stage s-1 produced in this pass or the
 // last.  Each stage's rows shrink by one at both ends (its neighbours must
@@ -549,7 +553,8 @@ __device__ __forceinline__ void stv(float* p, const float* v) {
 // cells a thread at 1024 threads measured no faster: the kernel is bound by
 // its instructions, not by the warps it has to hide latency).
 template <int TY, int HH, bool FRESH, int NS = kSmStages, int CPT = 4, int NT = kSmThreads>
-__global__ void __launch_bounds__(NT, 1) k_bx_smooth(float* __restrict__ fp, BoxLev L, long long oe_out, int nz) {
+__global__ void __launch_bounds__(NT, 1) k_bx_smooth(float* __restrict__ fp, BoxLev L, long long oe_out, int nz,
+                                                   const __grid_constant__ CUtensorMap emap) {
   extern __shared__ __align__(128) float ssm[];
   constexpr int NSL = smooth_slots(NS);
   constexpr int R = TY + 2 * NS, AR = R * HH, SL = 4 * AR, LG = ilog2(HH);
@@ -558,6 +563,7 @@ __global__ void __launch_bounds__(NT, 1) k_bx_smooth(float* __restrict__ fp, Box
   constexpr int KQ = (R + RK - 1) / RK;     // row segments of a thread (the same rows in every stage)
   constexpr bool CARRY = CPT == 4;          // registers for the carried in-plane values
   static_assert((1 << LG) == HH && HH % 4 == 0 && RK % 2 == 0 && (CPT == 2 || CPT == 4), "rows of 2^k cells");
+  static_assert(R % 4 == 0 && TY % 4 == 0, "slots fill in chunks of four rows");
   __shared__ __align__(8) unsigned long long bar[NSL];
   const int n1 = L.n[1], n2 = L.n[2];
   const unsigned half = (unsigned)L.half;  // a level's cells are fewer than 2^31
@@ -565,7 +571,6 @@ __global__ void __launch_bounds__(NT, 1) k_bx_smooth(float* __restrict__ fp, Box
   const int y0 = (blockIdx.x % ytiles) * TY, zc = blockIdx.x / ytiles;
   const int z0 = (int)((long long)zc * n2 / nz), z1 = (int)((long long)(zc + 1) * n2 / nz);
   const int P = z1 - z0 + 2 * NS;  // local plane j is z0 - NS + j
-  const float* E = fp + L.oe;
   const float* G = fp + L.og;
   const float* PB = fp + L.opb;
   float* EO = fp + oe_out;
@@ -585,37 +590,31 @@ __global__ void __launch_bounds__(NT, 1) k_bx_smooth(float* __restrict__ fp, Box
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  // rows y0-NS .. y0+TY+NS-1 of plane zw as one or two contiguous runs:
-  // f(offset of the run's first row, rows, its row in the slot)
-  auto runs = [&](int zw, auto&& f) {
-    int y = y0 - NS, n = R, at = 0;
-    while (n > 0) {
-      const int yy = wrap(y, n1);
-      const int run = n1 - yy < n ? n1 - yy : n;
-      f((zw * n1 + yy) * HH, run, at);
-      y += run;
-      n -= run;
-      at += run;
-    }
-  };
-  // lane 0 of warps 0-3: the rows of array a = warp of local plane j into
-  // slot k, warp 0 arming the barrier with the plane's bytes (nothing when
-  // fresh: the first half-sweeps count the old e as zero)
+  // lane 0 of warps 0-3: the rows y0-NS .. y0+TY+NS-1 of the four e arrays
+  // of local plane j into slot k, by tensor copies of four rows of one array
+  // (emap: the input e as [array][z][y][h], a box of 4 x HH cells); warp w
+  // copies the row chunks w, w+4, ..., whose start rows, wrapped around the
+  // plane, are whole chunks (n1 is a multiple of 4); warp 0 arms the barrier
+  // with the plane's bytes.  Nothing when fresh: the first half-sweeps count
+  // the old e as zero.
   auto issue = [&](int j, int k) {
-    const int a = threadIdx.x >> 5;
-    if (FRESH || (threadIdx.x & 31) || a >= 4 || j >= P) return;
+    const int w = threadIdx.x >> 5;
+    if (FRESH || (threadIdx.x & 31) || w >= 4 || j >= P) return;
     const unsigned b = smem_addr(&bar[k]);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    if (a == 0)
+    if (w == 0)
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"((unsigned)SL * 4u)
                    : "memory");
-    runs(wrap(z0 - NS + j, n2), [&](int off, int run, int at) {
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-              smem_addr(ssm + k * SL + a * AR + at * HH)),
-          "l"(E + (unsigned)a * half + off), "r"((unsigned)(run * HH * 4)), "r"(b)
-          : "memory");
-    });
+    const int zw = wrap(z0 - NS + j, n2);
+    for (int ck = w; ck < R / 4; ck += 4) {
+      const int yc = wrap(y0 - NS + 4 * ck, n1);
+      for (int a = 0; a < 4; a++)
+        asm volatile(
+            "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+            "[%6];" ::"r"(smem_addr(ssm + k * SL + a * AR + ck * 4 * HH)),
+            "l"(reinterpret_cast<unsigned long long>(&emap)), "r"(0), "r"(yc), "r"(zw), "r"(a), "r"(b)
+            : "memory");
+    }
   };
   // pb, g0, g1 of this thread's cells of stage s for the pass over local
   // plane j, in registers before that pass
@@ -1311,6 +1310,36 @@ bool smooth_fits(const Hier& H, const BoxLev& L) {
   return H.ndims == 3 && L.n[2] >= kSmStages && smooth_rows(L) > 0;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); null when the driver does not provide it
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// the tensor map of a level's e arrays at offset oe: [array][z][y][h] with
+// h innermost, a box of four rows of one array
+int e_tensor_map(Hier& H, const BoxLev& L, long long oe, CUtensorMap* m) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return cuda_fail(cudaErrorNotSupported, "cuTensorMapEncodeTiled entry point");
+  const cuuint64_t dims[4] = {(cuuint64_t)L.hh, (cuuint64_t)L.n[1], (cuuint64_t)L.n[2], 4};
+  const cuuint64_t strides[3] = {(cuuint64_t)L.hh * 4, (cuuint64_t)L.hh * L.n[1] * 4, (cuuint64_t)L.half * 4};
+  const cuuint32_t box[4] = {(cuuint32_t)L.hh, 4, 1, 1};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, H.fpool + oe, dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return cuda_fail(cudaErrorInvalidValue, "cuTensorMapEncodeTiled");
+  return BSAMG_OK;
+}
+
 // out_oe = e after two red-black passes from e at in.oe (fresh: from zero)
 int bx_smooth(Hier& H, const BoxLev& in, long long out_oe, bool fresh) {
   const int ty = smooth_rows(in);
@@ -1325,8 +1354,11 @@ int bx_smooth(Hier& H, const BoxLev& in, long long out_oe, bool fresh) {
     }
     mark_setup(attr, H.ctx->device);
   }
+  CUtensorMap emap;
+  int r = e_tensor_map(H, in, in.oe, &emap);
+  if (r) return r;
   auto ker = fresh ? k_bx_smooth<8, 128, true> : k_bx_smooth<8, 128, false>;
-  ker<<<ytiles * nz, kSmThreads, smem, H.s>>>(H.fpool, in, out_oe, nz);
+  ker<<<ytiles * nz, kSmThreads, smem, H.s>>>(H.fpool, in, out_oe, nz, emap);
   return after_launch(H, 1);
 }
 bool smooth_applies(const Hier& H, const BoxLev& L, int nsmooth) {
