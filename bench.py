@@ -282,14 +282,25 @@ def run_arm(h, q0, w, mode, steps, warmup, dist, clocks=None):
                 final_resid=res[-1])
 
 
-def run_e2e(pkg, h, q0, w, mode, steps, warmup, dist):
+def run_e2e(pkg, h, q0, w, mode, steps, warmup, dist, buffers="allocated"):
     """Public-API end to end: per step, H2D of q from pinned host memory,
     the time step, D2H of q into pinned host memory (two pinned buffers
     alternate as input and output, as a host that keeps its state would).
+    The buffers come from the CUDA pinned allocator (through torch), or are
+    numpy arrays page-locked in place (buffers="registered"); on one GB300 the
+    allocator's buffers moved 173-208 GB/s host to device against 184-185 for
+    registered ones (two runs each): the link's own variation dominates.
     Returns the total time, the bytes of q and the device time of the
     uploads and of the downloads over the timed steps (events around each
     copy on the hierarchy's stream)."""
-    bufs = [pkg.pin(np.array(q0, copy=True)), pkg.pin(np.empty_like(q0))]
+    keep = None
+    if buffers == "registered":
+        bufs = [pkg.pin(np.array(q0, copy=True)), pkg.pin(np.empty_like(q0))]
+    else:
+        import torch
+        keep = [torch.empty(q0.size, dtype=torch.float64, pin_memory=True) for _ in range(2)]
+        bufs = [t.numpy() for t in keep]
+        bufs[0][:] = q0
     reset(h, q0, w)
     first = True
     cur = 0
@@ -313,9 +324,12 @@ def run_e2e(pkg, h, q0, w, mode, steps, warmup, dist):
     h.mark(11)
     ms = h.elapsed_ms(10, 11)
     dist.barrier()
-    for b in bufs:
-        pkg.unpin(b)
-    return ms, bufs[0].nbytes, up_ms, down_ms
+    nbytes = bufs[0].nbytes
+    if keep is None:
+        for b in bufs:
+            pkg.unpin(b)
+    del keep
+    return ms, nbytes, up_ms, down_ms
 
 
 def pct(x, p):
@@ -679,6 +693,8 @@ def main():
     ap.add_argument("--serve-blocking-wait", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-buffers", default="allocated", choices=["allocated", "registered"],
+                    help="the e2e leg's pinned host buffers: from the CUDA pinned allocator or registered numpy")
     ap.add_argument("--maxv", type=int, default=MAXV,
                     help="V-cycles allowed per step; above 64 the periodic-box solve runs its host loop "
                          "instead of one graph launch (the same cycles, launched one by one)")
@@ -730,7 +746,7 @@ def main():
     # the same time steps as the resident run (same warm-up), so both legs
     # see the same V-cycle counts
     e2e_ms, qbytes, up_ms, down_ms = (None, 0, 0, 0) if args.no_e2e else run_e2e(
-        pkg, h, q0, w, "mixed", args.steps, args.warmup, dist)
+        pkg, h, q0, w, "mixed", args.steps, args.warmup, dist, args.e2e_buffers)
 
     t_mixed = dist.max(mixed["total_ms"])
     t_fp64 = dist.max(fp64["total_ms"])
@@ -793,7 +809,9 @@ def main():
                        # the host link's share: device time of the copies alone
                        "h2d_ms_per_step": up_ms / args.steps, "d2h_ms_per_step": down_ms / args.steps,
                        "h2d_gbs": qbytes * args.steps / (up_ms * 1e6),
-                       "d2h_gbs": qbytes * args.steps / (down_ms * 1e6)}
+                       "d2h_gbs": qbytes * args.steps / (down_ms * 1e6),
+                       "host_buffers": "CUDA pinned allocator" if args.e2e_buffers == "allocated"
+                       else "numpy arrays page-locked in place"}
     if not args.no_cpu_baseline:
         per_v, cb = cpu_baseline(pkg, w, vps_f)
         line["cpu_baseline"] = cb
